@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Throughput of the rigid-water MD path on GB300: ns/day of TIP4P water.
+
+Workload (N=1): 4,096 rigid TIP4P waters at 1.0 g/cm^3 (L = 49.655 A), seeded
+lattice with random quaternions, pre-equilibrated 2,000 steps, cutoff 9.0 A
+with a 2 A switch, Nose-Hoover NVT at 300 K, dt = 2 fs.  One step = one full
+MD step (Gear predict, placement, neighbour-list upkeep, force, collect,
+correct, reductions, thermostat).  ``value`` is the mixed-precision ns/day;
+the plain FP64 mode and the 32,768-molecule system are reported beside it.
+
+Timing: per-step CUDA events on the library's stream, an L2 flush (256 MiB
+write) between timed steps, W untimed warm-up steps, barrier + synchronize on
+both sides, max over ranks.  ``e2e`` runs the host-buffer entry point
+g6_md_step_host (state uploaded from pinned host memory and read back every
+step).  ``--impl reference`` times the CPU restatement of the reference on all
+host cores.  With --gpus N each rank runs an independent replica (the
+single-system path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ns/day TIP4P 4k/32k mixed vs FP64, 1 GB300; MC ESS/GPU-s learned vs plain"
+DT = 0.002          # ps
+RC, SWITCH = 9.0, 2.0
+TEMP = 300.0
+TAU_NOSE = 0.5      # ps; q = T0 tau^2 / dt in the reference's internal form
+N_MAIN = 4096
+N_BIG = 32768
+EQUIL_STEPS = 2000
+FLOPS_PER_PAIR = {"TIP4P": 287, "TIP5P": 441, "ST2": 456}   # algorithmic flops per pair within rc
+
+
+def ns_per_day(ms_per_step, dt=DT):
+    return dt * 1e-3 * 86400.0 / (ms_per_step * 1e-3)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-32k", action="store_true")
+    p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config_block(args, world):
+    return {"workload": "TIP4P-4096 rigid water, NVT Nose-Hoover 300 K, dt 2 fs, rc 9.0 A (2 A switch)",
+            "molecules": N_MAIN, "box_A": round((N_MAIN / 0.033456) ** (1 / 3), 3), "cutoff_A": RC,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "flushed between timed steps (256 MiB write)", "precision": "mixed (fp32 site math, fp64 sums)"}
+
+
+# ---------------------------------------------------------------------------
+# CPU side (reference arm and cpu_baseline): oracle restatement, all host cores
+# ---------------------------------------------------------------------------
+def cpu_md_rate(nsteps_max=None, budget_s=15.0, rec=None):
+    import oracle
+    from genesis6_gb300 import config
+    oracle.build()
+    b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
+    rec = b["rec"] if rec is None else rec
+    threads = os.cpu_count() or 1
+    q = TEMP * TAU_NOSE ** 2 / DT
+    th = np.array([1, q, 0.0, TEMP, 0, 0, 0, 0, 0, 0], float)
+    t0 = time.perf_counter()
+    r, th, _ = oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, 2, th, threads)
+    probe = (time.perf_counter() - t0) / 2
+    n = max(2, int(budget_s / max(probe, 1e-6)))
+    if nsteps_max:
+        n = min(n, nsteps_max)
+    t0 = time.perf_counter()
+    oracle.md_run_threaded("TIP4P", r, b["L"], [RC] * 3, RC - SWITCH, RC, DT, n, th, threads)
+    dt_s = time.perf_counter() - t0
+    ms = 1e3 * dt_s / n
+    return {"value": ns_per_day(ms), "unit": "ns/day", "cores": threads, "kind": "port",
+            "sample": "%d MD steps of TIP4P-4096 (oracle restatement, OpenMP force and pair search, %d threads, "
+                      "g++ -O2)" % (n, threads), "ms_per_step": ms}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import oracle
+    from genesis6_gb300 import config
+    oracle.build()
+    b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
+    threads = os.cpu_count() or 1
+    q = TEMP * TAU_NOSE ** 2 / DT
+    th = np.array([1, q, 0.0, TEMP, 0, 0, 0, 0, 0, 0], float)
+    rec = b["rec"]
+    if args.warmup:
+        rec, th, _ = oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, args.warmup, th,
+                                            threads)
+    steps = max(1, min(args.steps, 400))
+    t0 = time.perf_counter()
+    oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, steps, th, threads)
+    wall = time.perf_counter() - t0
+    ms = 1e3 * wall / steps
+    v = ns_per_day(ms)
+    line = {"metric": METRIC, "value": v, "unit": "ns/day", "impl": "reference", "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_block(args, world),
+            "cpu_baseline": {"value": v, "unit": "ns/day", "cores": threads, "kind": "port",
+                             "sample": "%d MD steps of TIP4P-4096 on %d host threads (Fortran reference not "
+                                       "compilable: no Fortran compiler; CPU restatement used)" % (steps, threads)},
+            "e2e": {"value": v, "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0])); mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp32_peak_tflops(torch):
+    """FP32 CUDA-core throughput of cuBLAS SGEMM with TF32 off (the roofline denominator)."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(); torch.mm(a, b); e1.record(); e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def make_system(model, n, prec, L, rec):
+    import genesis6_gb300 as g6
+    s = g6.RigidWater(model, n, L, path="custom", precision=prec, rc=RC, switch=SWITCH)
+    s.upload_state(rec)
+    return s
+
+
+def thermo_for(s, n=1):
+    q = TEMP * TAU_NOSE ** 2 / DT
+    return s.thermostats(n, "nose", temp=TEMP, q=q, dump=0.0)
+
+
+def timed_md(torch, s, steps, warmup, flush):
+    """Per-step CUDA-event timing of `steps` MD steps, L2 flushed between them."""
+    L = s.L
+    th = thermo_for(s)
+    if warmup:
+        s.md_run(DT, warmup, th, log=False)
+    sp = ctypes.c_void_p()
+    s._check(L.g6_stream(s.ctx, ctypes.byref(sp)))
+    stream = torch.cuda.ExternalStream(sp.value)
+    s._check(L.g6_set_timing(s.ctx, steps))
+    log = np.zeros((steps, 1, 10))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    s._check(L.g6_md_begin(s.ctx, DT, steps, th, 1))
+    with torch.cuda.stream(stream):
+        flush.add_(1.0)
+        for k in range(steps):
+            ev[k][0].record(stream)
+            s._check(L.g6_md_advance(s.ctx, 1))
+            ev[k][1].record(stream)
+            flush.add_(1.0)
+    s._check(L.g6_md_end(s.ctx, th, log.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    torch.cuda.synchronize()
+    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
+    kms = np.zeros(steps)
+    cnt = ctypes.c_int()
+    s._check(L.g6_get_timing(s.ctx, kms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), steps, ctypes.byref(cnt)))
+    s._check(L.g6_set_timing(s.ctx, 0))
+    return step_ms, kms, log
+
+
+def e2e_md(torch, s, rec, steps):
+    """g6_md_step_host with pinned host state: H2D + step + D2H every step, wall clock."""
+    n = rec.shape[0]
+    host = torch.empty((n, 53), dtype=torch.float64, pin_memory=True)
+    host.copy_(torch.from_numpy(rec))
+    hv = host.numpy()
+    th = thermo_for(s)
+    lg = np.zeros(10)
+    s.md_step_host(DT, hv, th, lg)     # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.md_step_host(DT, hv, th, lg)
+    wall = time.perf_counter() - t0
+    rec_b = n * 53 * 8
+    h2d = rec_b + 88 + 32                       # records, thermostat, control words
+    d2h = rec_b + 32 + 4 + 88 + 24 * 8 + 80     # records, control, overflow flag, thermostat, sums, log
+    return 1e3 * wall / steps, h2d, d2h
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import config
+    g6.lib()
+    b = config.water_box("TIP4P", N_MAIN, 20261203 + rank, temp=TEMP, dt=DT)
+    L = b["L"]
+    # pre-equilibration (untimed): 2,000 steps from the lattice start
+    s = make_system("TIP4P", N_MAIN, "mixed", L, b["rec"])
+    if args.equil:
+        s.md_run(DT, args.equil, thermo_for(s), log=False)
+    rec_eq = s.download_state()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    s.upload_state(rec_eq)
+    barrier()
+    with Clocks(local) as clk:
+        step_ms, kms, log = timed_md(torch, s, args.steps, args.warmup, flush)
+        barrier()
+    total_ms = float(step_ms.sum())
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / args.steps
+    value = world * ns_per_day(ms)
+
+    # plain FP64 mode, same state
+    s64 = make_system("TIP4P", N_MAIN, "fp64", L, rec_eq)
+    k64 = max(5, min(args.steps, 60))
+    step64, kms64, log64 = timed_md(torch, s64, k64, min(args.warmup, 5), flush)
+    ms64 = float(step64.mean())
+
+    # e2e through the host-buffer entry point
+    s.upload_state(rec_eq)
+    e2e_steps = max(10, min(args.steps, 200))
+    e2e_ms, h2d, d2h = e2e_md(torch, s, rec_eq, e2e_steps)
+
+    big = None
+    if not args.no_32k:
+        bb = config.water_box("TIP4P", N_BIG, 7 + rank, temp=TEMP, dt=DT)
+        sb = make_system("TIP4P", N_BIG, "mixed", bb["L"], bb["rec"])
+        sb.md_run(DT, 200, thermo_for(sb), log=False)
+        rb = sb.download_state()
+        kb = max(5, min(args.steps, 100))
+        stb, kmb, logb = timed_md(torch, sb, kb, min(args.warmup, 5), flush)
+        s64b = make_system("TIP4P", N_BIG, "fp64", bb["L"], rb)
+        stb64, _, _ = timed_md(torch, s64b, 5, 2, flush)
+        pb = float(logb[:, 0, 6].mean())
+        big = {"mixed_ns_per_day": ns_per_day(float(stb.mean())), "fp64_ns_per_day": ns_per_day(float(stb64.mean())),
+               "mixed_ms_per_step": float(stb.mean()), "fp64_ms_per_step": float(stb64.mean()),
+               "mixed_over_fp64": float(stb64.mean() / stb.mean()), "force_kernel_ms": float(kmb.mean()),
+               "pairs_within_rc": pb,
+               "force_tflops": FLOPS_PER_PAIR["TIP4P"] * pb / (float(kmb.mean()) * 1e-3) / 1e12,
+               "note": "lattice start + 200 untimed steps (no 2,000-step melt)"}
+        sb.close(); s64b.close()
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    fp32_peak = fp32_peak_tflops(torch)
+    pairs = float(log[:, 0, 6].mean())
+    kmean = float(kms.mean())
+    achieved = FLOPS_PER_PAIR["TIP4P"] * pairs / (kmean * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "force_tip4p4096_mixed.txt")
+    if os.path.exists(tpath):
+        for l in open(tpath):
+            if l.startswith("traffic_bytes_per_launch:"):
+                traffic = float(l.split(":")[1])
+    cpu = None if args.no_cpu else cpu_md_rate(budget_s=12.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 site math / f64 accumulation", "data": "synthetic (seeded lattice, random quaternions, "
+        "Maxwell-Boltzmann 300 K, 2,000-step pre-equilibration)", "config": config_block(args, world),
+        "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
+        "tip4p_32k": big,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": traffic,
+                     "kernel": "k_force<TIP4P, mixed>", "flops_per_pair": FLOPS_PER_PAIR["TIP4P"],
+                     "pairs_per_launch": pairs, "kernel_ms": kmean,
+                     "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run (FP32 CUDA-core "
+                                    "pipe; the kernel uses no tensor cores and moves a few MB per launch)",
+                     "hbm_peak_gbs": peaks.get("hbm_gbs")},
+        "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": world * ns_per_day(e2e_ms), "unit": "ns/day", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "entry": "g6_md_step_host"},
+        "gpu_launches": 8 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1118 @@
+// g6_capi.cu -- context, model tables and the extern "C" entry points of g6gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "g6_internal.cuh"
+
+namespace g6 {
+
+// ---------------------------------------------------------------------------
+// Model tables (host).  Values and formulas follow the reference:
+// TIP4P TIP4PModule.F90:43-97 + TIP4PConst.F90; TIP5P TIP5PModule.F90:38-83 +
+// RigidModule.F90:429-477; ST2 ST2Module.F90:10-100 (float literals promoted).
+// ---------------------------------------------------------------------------
+static void five_site(ModelHost& m, double theta, double phi, double l1, double l2) {
+  const double hmass = 1.0, omass = 16.0;
+  double x[6] = {0}, y[6] = {0}, z[6] = {0};
+  y[1] = l1 * std::sin(0.5 * theta); z[1] = l1 * std::cos(0.5 * theta);
+  y[2] = -l1 * std::sin(0.5 * theta); z[2] = l1 * std::cos(0.5 * theta);
+  x[3] = l2 * std::sin(0.5 * phi); z[3] = -l2 * std::cos(0.5 * phi);
+  x[4] = -l2 * std::sin(0.5 * phi); z[4] = -l2 * std::cos(0.5 * phi);
+  const double zshift = z[1] * 2.0 * hmass / (2.0 * hmass + omass);
+  for (int i = 0; i < 5; ++i) z[i] = z[i] - zshift;
+  for (int s = 0; s < 6; ++s) { m.body[s][0] = x[s]; m.body[s][1] = y[s]; m.body[s][2] = z[s]; }
+  m.I[0] = omass * (y[0] * y[0] + z[0] * z[0]) + hmass * (y[1] * y[1] + z[1] * z[1]) * 2.0;
+  m.I[1] = omass * (z[0] * z[0] + x[0] * x[0]) + hmass * (z[1] * z[1] + x[1] * x[1]) * 2.0;
+  m.I[2] = omass * (x[0] * x[0] + y[0] * y[0]) + hmass * (x[1] * x[1] + y[1] * y[1]) * 2.0;
+  m.mass = 2.0 * hmass + omass;
+  m.nsite = 6;
+  m.nq = 4;
+}
+
+static const double ST2_QM = (double)(-0.2357f), ST2_QH = (double)(+0.2357f);
+static const double ST2_EPS = (double)(0.52605e-21f) * NA * 1e-3, ST2_SIG = 3.100;
+
+bool make_model(int model, ModelHost& m) {
+  m = ModelHost();
+  m.model = model;
+  if (model == G6_TIP4P) {
+    m.nsite = 5; m.nq = 3;
+    const double y[5] = {0.0, 0.0, 7.56950327263661182e-01, -7.56950327263661182e-01, 0.0};
+    const double z[5] = {-6.50980307353661025e-02, 8.49019692646338919e-02, 5.20784245882928820e-01,
+                         5.20784245882928820e-01, 0.0};
+    for (int s = 0; s < 5; ++s) { m.body[s][0] = 0; m.body[s][1] = y[s]; m.body[s][2] = z[s]; }
+    m.I[0] = 1.75618411509879202e+00; m.I[1] = 6.10236519209664374e-01; m.I[2] = 1.14594759588912742e+00;
+    m.mass = 18.0;
+    m.param[1][0] = -1.04; m.param[2][0] = 0.52; m.param[3][0] = 0.52;
+    m.param[0][1] = 0.15504166666666666666666 * CA; m.param[0][2] = 3.15357794197649532464;
+    return true;
+  }
+  if (model == G6_TIP5P) {
+    five_site(m, 104.52 * PI / 180.0, 109.47 * PI / 180.0, 0.9572, 0.70);
+    m.param[1][0] = 0.2410; m.param[2][0] = 0.2410; m.param[3][0] = -0.2410; m.param[4][0] = -0.2410;
+    m.param[0][1] = 0.6694; m.param[0][2] = 3.12;
+    return true;
+  }
+  if (model == G6_ST2) {
+    const double th = 109.47 * PI / 180.0;
+    five_site(m, th, th, 1.0, 0.8);
+    m.param[1][0] = ST2_QH; m.param[2][0] = ST2_QH; m.param[3][0] = ST2_QM; m.param[4][0] = ST2_QM;
+    m.param[0][1] = ST2_EPS; m.param[0][2] = ST2_SIG;
+    return true;
+  }
+  return false;
+}
+
+static inline double p6(double x) { double x2 = x * x; return x2 * x2 * x2; }
+
+// Pair constants for the chosen path.  PATH_STD: StdInteraction.F90:201-222
+// (q_i q_j COEFF KX2X J2I; LB-mixed aa, bb).  PATH_CUSTOM: the hand kernels'
+// precomputed products (TIP4PConst.F90:4-11, ST2Module.F90:123-127).
+void make_pair_const(const ModelHost& m, int path, PairConst& pc) {
+  std::memset(&pc, 0, sizeof pc);
+  const int nq = m.nq;
+  const bool custom = path == G6_PATH_CUSTOM;
+  if (custom && m.model == G6_TIP4P) {
+    const double WM = -1.04, WH = 0.52;
+    const double WWMM = WM * WM * COEFF * 100.0, WWMH = WM * WH * COEFF * 100.0, WWHH = WH * WH * COEFF * 100.0;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) pc.qq[a][b] = (a == 0 && b == 0) ? WWMM : ((a == 0 || b == 0) ? WWMH : WWHH);
+    pc.aa = 600000.0 * CA * 100.0;
+    pc.bb = -610.0 * CA * 100.0;
+  } else if (custom && m.model == G6_ST2) {
+    const double QMM = ST2_QM * ST2_QM * COEFF * 100.0, QHM = ST2_QH * ST2_QM * COEFF * 100.0,
+                 QHH = ST2_QH * ST2_QH * COEFF * 100.0;
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b) {
+        const bool ah = a < 2, bh = b < 2;
+        pc.qq[a][b] = (ah && bh) ? QHH : ((!ah && !bh) ? QMM : QHM);
+      }
+    const double s6 = p6(ST2_SIG);
+    pc.aa = 4.0 * ST2_EPS * (s6 * s6) * 100.0;
+    pc.bb = -4.0 * ST2_EPS * s6 * 100.0;
+    pc.taper = 1;
+    pc.rl = 2.0160; pc.ru = 3.1287;
+    pc.w3 = (pc.ru - pc.rl) * (pc.ru - pc.rl) * (pc.ru - pc.rl);
+  } else {
+    for (int a = 0; a < nq; ++a)
+      for (int b = 0; b < nq; ++b) pc.qq[a][b] = m.param[a + 1][0] * m.param[b + 1][0] * COEFF * KX2X * J2I * 1.0;
+    const double ljeps = std::sqrt(m.param[0][1] * m.param[0][1]);
+    const double ljsig = p6((m.param[0][2] + m.param[0][2]) * 0.5);
+    pc.aa = 4.0 * ljeps * ljsig * ljsig * KX2X * J2I * 1.0;
+    pc.bb = -4.0 * ljeps * ljsig * KX2X * J2I * 1.0;
+  }
+  for (int a = 0; a < MAXQ; ++a)
+    for (int b = 0; b < MAXQ; ++b) pc.fqq[a][b] = (float)pc.qq[a][b];
+  pc.faa = (float)pc.aa; pc.fbb = (float)pc.bb;
+  pc.frl = (float)pc.rl; pc.fru = (float)pc.ru; pc.fw3 = (float)pc.w3;
+}
+
+// cutoff_initialize CutoffModule.F90:25-36 (x**5 by binary powering).
+void make_cut_const(double rin, double rout, CutConst& cc) {
+  const double x = rin - rout, x2 = x * x;
+  cc.rin = rin; cc.rout = rout;
+  cc.c1 = 1.0 / (x * (x2 * x2));
+  cc.c2 = cc.c1 * 30.0;
+  cc.rin2 = rin * rin; cc.rout2 = rout * rout;
+  cc.frin = (float)rin; cc.frout = (float)rout; cc.frin2 = (float)cc.rin2; cc.frout2 = (float)cc.rout2;
+  cc.fc1 = (float)cc.c1; cc.fc2 = (float)cc.c2;
+}
+
+// NeighborCell_ListHomo GridModule.F90:279-374 (maxradius == 0): half-shell
+// offsets (kind 0) and self-mirror offsets (kind 1) as (x,y,z,kind).
+static void homo_stencil(const int nd[3], std::vector<int>& out) {
+  int nmax[3], nmin[3];
+  for (int d = 0; d < 3; ++d) {
+    nmax[d] = std::min(1, (nd[d] - 1) / 2);
+    nmin[d] = std::max(-1, -(nd[d] / 2));
+  }
+  std::vector<int> mark((size_t)nd[0] * nd[1] * nd[2], 0);
+  auto at = [&](int x, int y, int z) -> int& { return mark[((size_t)z * nd[1] + y) * nd[0] + x]; };
+  for (int jz = nmin[2]; jz <= nmax[2]; ++jz) {
+    const int pz = jz < 0 ? jz + nd[2] : jz, mz = pz == 0 ? 0 : nd[2] - pz;
+    for (int jy = nmin[1]; jy <= nmax[1]; ++jy) {
+      const int py = jy < 0 ? jy + nd[1] : jy, my = py == 0 ? 0 : nd[1] - py;
+      for (int jx = nmin[0]; jx <= nmax[0]; ++jx) {
+        const int px = jx < 0 ? jx + nd[0] : jx, mx = px == 0 ? 0 : nd[0] - px;
+        if (at(px, py, pz) == 0) {
+          at(mx, my, mz) += 1;
+          at(px, py, pz) += 1;
+          out.push_back(px); out.push_back(py); out.push_back(pz);
+          out.push_back(at(px, py, pz) != 1 ? 1 : 0);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace g6
+
+using namespace g6;
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+struct HostGrid {
+  std::vector<int> nd, cell_off;
+  std::vector<double> cell, icell;
+  int ncell = 0;
+  int* d_nd = nullptr; double* d_edge = nullptr; double* d_icell = nullptr; int* d_cell_off = nullptr;
+  int* d_cell = nullptr; int* d_slot = nullptr; int* d_count = nullptr; int* d_start = nullptr; int* d_cellmol = nullptr;
+  bool valid = false;
+};
+
+struct g6_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<void*> allocs;      // freed on redefinition / destroy
+  // system
+  bool have_system = false, have_cut = false, have_state = false;
+  int model = 0, path = 0, prec = 0, nrep = 0, n = 0, nq = 0, w64 = 0, npk = 0;
+  ModelHost mh;
+  PairConst pc;
+  CutConst cc;
+  double req = 0.0, skin = 1.0;
+  std::vector<int> off;
+  std::vector<double> L;
+  int lpi = 0;                    // lanes per molecule in the force kernel (0 = tune)
+  // device arrays
+  int* d_off = nullptr; int* d_mol_rep = nullptr; double* d_L = nullptr; double* d_invL = nullptr;
+  float* d_fscale = nullptr;
+  double* d_st = nullptr; double* d_tmat = nullptr; double* d_pk64 = nullptr; float4* d_pk32 = nullptr;
+  uint32_t* d_fix = nullptr;
+  double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
+  int* d_npin = nullptr;
+  double* d_stage = nullptr;      // AoS staging (53 n)
+  // grids
+  HostGrid gref, glist;
+  std::vector<int> sten, sten_off;
+  int* d_sten = nullptr; int* d_sten_off = nullptr;
+  // neighbour list
+  int cap = 0;
+  int* d_nbr = nullptr; int* d_nnb = nullptr; double* d_com_build = nullptr; int* d_overflow = nullptr;
+  // reductions and control
+  int nblk = 0;
+  double* d_part = nullptr; double* d_partmax = nullptr; double* d_red = nullptr;
+  unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
+  ThermoDev* d_th = nullptr; double* d_scale = nullptr; double* d_beta = nullptr; int* d_acc = nullptr;
+  double* d_epot_rep = nullptr;
+  // pair set
+  long long* d_pcnt = nullptr;
+  long long npairs = -1;
+  size_t pair_capacity = 0;
+  int* d_pi = nullptr; int* d_pj = nullptr;
+  double *d_ox = nullptr, *d_oy = nullptr, *d_oz = nullptr, *d_hh = nullptr, *d_dh = nullptr;
+  // scratch for the pair-list entry points (grow only)
+  void* d_scratch = nullptr; size_t scratch_bytes = 0;
+  // log buffer
+  double* d_log = nullptr; size_t log_cap = 0;
+  // pinned host staging for g6_md_step_host
+  double* h_pinned = nullptr; size_t pinned_bytes = 0;
+  // graph of a block of MD steps
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  double graph_dt = 0.0;
+  int graph_log = -1;
+  std::vector<double> last_epot;  // per replica, from the last MD step
+  unsigned long long steps_done = 0;
+  unsigned long long seed = 0;
+  // open g6_md_begin .. g6_md_end run
+  bool in_run = false, run_log = false;
+  double run_dt = 0.0;
+  int run_max = 0, run_done = 0;
+  // optional per-step CUDA events around the force kernel
+  std::vector<cudaEvent_t> tev;
+  int tcap = 0, tnext = 0;
+};
+
+static int fail(g6_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+static int cuda_fail(g6_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, G6_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                                   \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);       \
+  } while (0)
+
+template <class T>
+static cudaError_t dalloc(g6_ctx* c, T** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  c->allocs.push_back(q);
+  *p = (T*)q;
+  return cudaMemset(q, 0, std::max<size_t>(count, 1) * sizeof(T));
+}
+
+static void free_timing(g6_ctx* c) {
+  for (cudaEvent_t e : c->tev) cudaEventDestroy(e);
+  c->tev.clear();
+  c->tcap = 0; c->tnext = 0;
+}
+
+static void free_all(g6_ctx* c) {
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  free_timing(c);
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  if (c->d_scratch) { cudaFree(c->d_scratch); c->d_scratch = nullptr; c->scratch_bytes = 0; }
+  if (c->d_log) { cudaFree(c->d_log); c->d_log = nullptr; c->log_cap = 0; }
+  if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
+  c->gref = HostGrid(); c->glist = HostGrid();
+  c->pair_capacity = 0; c->npairs = -1; c->cap = 0;
+}
+
+static RepDev rep_dev(const g6_ctx* c) {
+  RepDev r;
+  r.nrep = c->nrep; r.off = c->d_off; r.mol_rep = c->d_mol_rep; r.L = c->d_L; r.invL = c->d_invL; r.fscale = c->d_fscale;
+  return r;
+}
+static GridDev grid_dev(const HostGrid& g) {
+  GridDev d;
+  d.ncell_total = g.ncell; d.nd = g.d_nd; d.cell = g.d_edge; d.icell = g.d_icell; d.cell_off = g.d_cell_off;
+  return d;
+}
+
+// Grid_Update (adaptive), GridModule.F90:95-125 and 473-501, per replica.
+static int build_grid(g6_ctx* ctx, HostGrid& g, double edge, bool with_stencil) {
+  const int R = ctx->nrep;
+  g.nd.assign(3 * R, 1); g.cell.assign(3 * R, 0.0); g.icell.assign(3 * R, 0.0); g.cell_off.assign(R + 1, 0);
+  if (with_stencil) { ctx->sten.clear(); ctx->sten_off.assign(R + 1, 0); }
+  for (int r = 0; r < R; ++r) {
+    for (int d = 0; d < 3; ++d) {
+      int nd = (int)(ctx->L[3 * r + d] / edge);
+      nd = std::max(1, nd);
+      g.nd[3 * r + d] = nd;
+      g.cell[3 * r + d] = ctx->L[3 * r + d] / nd;
+      g.icell[3 * r + d] = 1.0 / g.cell[3 * r + d];
+    }
+    g.cell_off[r + 1] = g.cell_off[r] + g.nd[3 * r] * g.nd[3 * r + 1] * g.nd[3 * r + 2];
+    if (with_stencil) {
+      homo_stencil(&g.nd[3 * r], ctx->sten);
+      ctx->sten_off[r + 1] = (int)ctx->sten.size() / 4;
+    }
+  }
+  g.ncell = g.cell_off[R];
+  const int n = ctx->n;
+  if (!g.d_nd) {
+    CK(dalloc(ctx, &g.d_nd, 3 * R)); CK(dalloc(ctx, &g.d_edge, 3 * R)); CK(dalloc(ctx, &g.d_icell, 3 * R));
+    CK(dalloc(ctx, &g.d_cell_off, R + 1)); CK(dalloc(ctx, &g.d_cell, n)); CK(dalloc(ctx, &g.d_slot, n));
+    CK(dalloc(ctx, &g.d_cellmol, n));
+  }
+  // cell-count arrays are sized per grid (re-allocated if the grid grows)
+  CK(dalloc(ctx, &g.d_count, g.ncell + 1));
+  CK(dalloc(ctx, &g.d_start, g.ncell + 1));
+  CK(cudaMemcpy(g.d_nd, g.nd.data(), 3 * R * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g.d_edge, g.cell.data(), 3 * R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g.d_icell, g.icell.data(), 3 * R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g.d_cell_off, g.cell_off.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  if (with_stencil) {
+    CK(dalloc(ctx, &ctx->d_sten, std::max<size_t>(ctx->sten.size(), 4)));
+    CK(dalloc(ctx, &ctx->d_sten_off, R + 1));
+    CK(cudaMemcpy(ctx->d_sten, ctx->sten.data(), ctx->sten.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_sten_off, ctx->sten_off.data(), (R + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  g.valid = true;
+  return G6_OK;
+}
+
+static double grid_edge_ref(const g6_ctx* c) { return c->req > 0.0 ? c->req : c->cc.rout; }
+
+// Effective Verlet margin: rc + skin must not exceed half the smallest box edge.
+static double effective_skin(const g6_ctx* c) {
+  double s = c->skin;
+  for (int r = 0; r < c->nrep; ++r)
+    for (int d = 0; d < 3; ++d) s = std::min(s, 0.5 * c->L[3 * r + d] - c->cc.rout);
+  return std::max(0.0, s);
+}
+
+static int check_ready(g6_ctx* ctx, bool need_state) {
+  if (!ctx) return G6_ERR_ARG;
+  if (!ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system defined (g6_system)");
+  if (!ctx->have_cut) return fail(ctx, G6_ERR_STATE, "no cutoff defined (g6_set_cutoff)");
+  if (need_state && !ctx->have_state) return fail(ctx, G6_ERR_STATE, "no state uploaded");
+  for (int r = 0; r < ctx->nrep; ++r)
+    for (int d = 0; d < 3; ++d)
+      if (!(ctx->cc.rout <= 0.5 * ctx->L[3 * r + d]))
+        return fail(ctx, G6_ERR_ARG, "cutoff exceeds half the box edge (minimum image)");
+  CK(cudaSetDevice(ctx->device));
+  return G6_OK;
+}
+
+// Neighbour-list grid, capacity and buffers for the current box/cutoff/skin.
+static int prepare_list(g6_ctx* ctx) {
+  if (ctx->glist.valid && ctx->cap > 0) return G6_OK;
+  const double skin = effective_skin(ctx);
+  const double rlist = ctx->cc.rout + skin;
+  int rc = build_grid(ctx, ctx->glist, rlist, false);
+  if (rc) return rc;
+  double rho = 0.0;
+  for (int r = 0; r < ctx->nrep; ++r) {
+    const double V = ctx->L[3 * r] * ctx->L[3 * r + 1] * ctx->L[3 * r + 2];
+    rho = std::max(rho, (ctx->off[r + 1] - ctx->off[r]) / V);
+  }
+  const double expect = 4.18879020478639 * rlist * rlist * rlist * rho;
+  int cap = (int)(2.0 * expect + 64.0);
+  int nmax = 0;
+  for (int r = 0; r < ctx->nrep; ++r) nmax = std::max(nmax, ctx->off[r + 1] - ctx->off[r]);
+  cap = std::min(cap, std::max(nmax - 1, 1));
+  cap = (cap + 31) / 32 * 32;
+  if (cap != ctx->cap) {
+    CK(dalloc(ctx, &ctx->d_nbr, (size_t)cap * ctx->n));
+    ctx->cap = cap;
+  }
+  return G6_OK;
+}
+
+static int prepare_ref_grid(g6_ctx* ctx) {
+  if (ctx->gref.valid) return G6_OK;
+  return build_grid(ctx, ctx->gref, grid_edge_ref(ctx), true);
+}
+
+static PlaceArgs place_args(g6_ctx* c) {
+  PlaceArgs p;
+  p.n = c->n; p.nq = c->nq; p.npk = c->npk; p.w64 = c->w64;
+  p.rep = rep_dev(c);
+  for (int s = 0; s < MAXSITE; ++s)
+    for (int k = 0; k < 3; ++k) p.body[s][k] = c->mh.body[s][k];
+  p.st = c->d_st; p.tmat = c->d_tmat; p.pk64 = c->d_pk64; p.pk32 = c->d_pk32; p.fix = c->d_fix;
+  return p;
+}
+
+static CellArgs cell_args(g6_ctx* c, HostGrid& g, const int* ctrl) {
+  CellArgs a;
+  a.n = c->n; a.rep = rep_dev(c); a.g = grid_dev(g); a.com = c->d_st;
+  a.cell = g.d_cell; a.slot = g.d_slot; a.count = g.d_count; a.ctrl = ctrl;
+  return a;
+}
+
+static ListArgs list_args(g6_ctx* c, const int* ctrl) {
+  ListArgs a;
+  a.n = c->n; a.cap = c->cap; a.rep = rep_dev(c); a.g = grid_dev(c->glist); a.cell = c->glist.d_cell;
+  a.start = c->glist.d_start; a.cellmol = c->glist.d_cellmol; a.fix = c->d_fix; a.com = c->d_st;
+  a.com_build = c->d_com_build;
+  const double rl = c->cc.rout + effective_skin(c);
+  a.rlist2 = (float)(rl * rl) + 1e-3f;   // superset margin over the fixed-point rounding
+  a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.overflow = c->d_overflow; a.ctrl = ctrl;
+  return a;
+}
+
+static ForceArgs force_args(g6_ctx* c) {
+  ForceArgs a;
+  a.n = c->n; a.cap = c->cap; a.stride_pk32 = c->npk; a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.rep = rep_dev(c);
+  a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
+  a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin;
+  return a;
+}
+
+static int default_lpi(const g6_ctx* c) {
+  // enough lanes per molecule to put ~16 warps on each of the 152 SMs
+  const long long want = 152LL * 16 * 32;
+  int l = 4;
+  while (l < 32 && (long long)c->n * l < want) l *= 2;
+  return l;
+}
+
+// Enqueue the neighbour-list rebuild (conditional on ctrl[0] when ctrl != NULL).
+static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl) {
+  CellArgs ca = cell_args(ctx, ctx->glist, ctrl);
+  CK(launch_cells(ca, ctx->glist.d_start, ctx->glist.d_cellmol, ctx->stream));
+  CK(launch_list(list_args(ctx, ctrl), ctx->stream));
+  return G6_OK;
+}
+
+static int force_once(g6_ctx* ctx) {
+  int rc = prepare_list(ctx);
+  if (rc) return rc;
+  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
+  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  CK(launch_predict_place(place_args(ctx), 0, ctx->d_th, 0, ctx->stream));
+  rc = enqueue_rebuild(ctx, nullptr);
+  if (rc) return rc;
+  CK(launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
+  int ovf = 0;
+  CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow");
+  return G6_OK;
+}
+
+extern "C" {
+
+int g6_version(void) { return 10000; }
+
+const char* g6_last_error(const g6_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+const char* g6_status_string(int s) {
+  switch (s) {
+    case G6_OK: return "ok";
+    case G6_ERR_ARG: return "bad argument";
+    case G6_ERR_CUDA: return "CUDA error";
+    case G6_ERR_CAPACITY: return "capacity exceeded";
+    case G6_ERR_NONFINITE: return "non-finite value";
+    case G6_ERR_TIMEOUT: return "device wait timed out";
+    case G6_ERR_STATE: return "call order";
+    default: return "unknown status";
+  }
+}
+
+int g6_model_info(int model, int* nsite, double* body, double* param, double* mass_inertia) {
+  ModelHost m;
+  if (!make_model(model, m)) return G6_ERR_ARG;
+  if (nsite) *nsite = m.nsite;
+  for (int s = 0; s < m.nsite; ++s)
+    for (int k = 0; k < 3; ++k) {
+      if (body) body[3 * s + k] = m.body[s][k];
+      if (param) param[3 * s + k] = m.param[s][k];
+    }
+  if (mass_inertia) { mass_inertia[0] = m.mass; mass_inertia[1] = m.I[0]; mass_inertia[2] = m.I[1]; mass_inertia[3] = m.I[2]; }
+  return G6_OK;
+}
+
+int g6_ctx_create(int device, g6_ctx** out) {
+  if (!out) return G6_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return G6_ERR_CUDA;
+  if (device < 0 || device >= ndev) return G6_ERR_ARG;
+  g6_ctx* c = new g6_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return G6_ERR_CUDA;
+  }
+  *out = c;
+  return G6_OK;
+}
+
+int g6_ctx_destroy(g6_ctx* ctx) {
+  if (!ctx) return G6_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  free_all(ctx);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return G6_OK;
+}
+
+int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const int* nmol, const double* box) {
+  if (!ctx) return G6_ERR_ARG;
+  if (nrep < 1 || !nmol || !box) return fail(ctx, G6_ERR_ARG, "nrep, nmol and box are required");
+  if (path != G6_PATH_STD && path != G6_PATH_CUSTOM) return fail(ctx, G6_ERR_ARG, "unknown path");
+  if (precision != G6_FP64 && precision != G6_MIXED) return fail(ctx, G6_ERR_ARG, "unknown precision");
+  ModelHost mh;
+  if (!make_model(model, mh)) return fail(ctx, G6_ERR_ARG, "unknown model");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  free_all(ctx);
+  ctx->have_system = false; ctx->have_state = false;
+  ctx->model = model; ctx->path = path; ctx->prec = precision; ctx->nrep = nrep; ctx->mh = mh; ctx->nq = mh.nq;
+  make_pair_const(mh, path, ctx->pc);
+  ctx->w64 = pk64_width(model); ctx->npk = pk32_width(model);
+  ctx->off.assign(nrep + 1, 0); ctx->L.assign(3 * (size_t)nrep, 0.0);
+  for (int r = 0; r < nrep; ++r) {
+    if (nmol[r] < 2) return fail(ctx, G6_ERR_ARG, "every replica needs at least 2 molecules");
+    ctx->off[r + 1] = ctx->off[r] + nmol[r];
+    for (int d = 0; d < 3; ++d) {
+      if (!(box[3 * r + d] > 0.0)) return fail(ctx, G6_ERR_ARG, "box edges must be positive");
+      ctx->L[3 * r + d] = box[3 * r + d];
+    }
+  }
+  const int n = ctx->n = ctx->off[nrep];
+  // every update block may touch at most MAXREP_PER_BLOCK replicas
+  for (int b = 0; b * RED_BLOCK < n; ++b) {
+    const int i0 = b * RED_BLOCK, i1 = std::min(n, i0 + RED_BLOCK) - 1;
+    int r0 = (int)(std::upper_bound(ctx->off.begin(), ctx->off.end(), i0) - ctx->off.begin()) - 1;
+    int r1 = (int)(std::upper_bound(ctx->off.begin(), ctx->off.end(), i1) - ctx->off.begin()) - 1;
+    if (r1 - r0 + 1 > MAXREP_PER_BLOCK) return fail(ctx, G6_ERR_ARG, "replicas too small for the update blocks");
+  }
+  std::vector<int> mol_rep(n);
+  for (int r = 0; r < nrep; ++r)
+    for (int i = ctx->off[r]; i < ctx->off[r + 1]; ++i) mol_rep[i] = r;
+  std::vector<double> invL(3 * nrep);
+  std::vector<float> fs(3 * nrep);
+  for (int k = 0; k < 3 * nrep; ++k) { invL[k] = 1.0 / ctx->L[k]; fs[k] = (float)(ctx->L[k] / 4294967296.0); }
+  CK(dalloc(ctx, &ctx->d_off, nrep + 1)); CK(dalloc(ctx, &ctx->d_mol_rep, n)); CK(dalloc(ctx, &ctx->d_L, 3 * nrep));
+  CK(dalloc(ctx, &ctx->d_invL, 3 * nrep)); CK(dalloc(ctx, &ctx->d_fscale, 3 * nrep));
+  CK(cudaMemcpy(ctx->d_off, ctx->off.data(), (nrep + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_mol_rep, mol_rep.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_L, ctx->L.data(), 3 * nrep * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_invL, invL.data(), 3 * nrep * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_fscale, fs.data(), 3 * nrep * sizeof(float), cudaMemcpyHostToDevice));
+  CK(dalloc(ctx, &ctx->d_st, (size_t)REC * n)); CK(dalloc(ctx, &ctx->d_tmat, 9 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_pk64, (size_t)ctx->w64 * n)); CK(dalloc(ctx, &ctx->d_pk32, (size_t)ctx->npk * n));
+  CK(dalloc(ctx, &ctx->d_fix, 3 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
+  CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
+  CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_overflow, 1));
+  ctx->nblk = (n + RED_BLOCK - 1) / RED_BLOCK;
+  CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
+  CK(dalloc(ctx, &ctx->d_partmax, ctx->nblk)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
+  CK(dalloc(ctx, &ctx->d_done, 1)); CK(dalloc(ctx, &ctx->d_ctrl, 8));
+  CK(dalloc(ctx, &ctx->d_th, nrep)); CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
+  CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
+  CK(dalloc(ctx, &ctx->d_pcnt, 2 * (size_t)n + 2));
+  ctx->last_epot.assign(nrep, 0.0);
+  ctx->have_system = true;
+  return G6_OK;
+}
+
+int g6_set_cutoff(g6_ctx* ctx, double r_in, double r_out) {
+  if (!ctx) return G6_ERR_ARG;
+  if (!(r_out > 0.0) || !(r_in < r_out)) return fail(ctx, G6_ERR_ARG, "need r_in < r_out, r_out > 0");
+  make_cut_const(r_in, r_out, ctx->cc);
+  ctx->have_cut = true;
+  ctx->gref.valid = false; ctx->glist.valid = false; ctx->cap = 0;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return G6_OK;
+}
+
+int g6_set_grid(g6_ctx* ctx, double edge) {
+  if (!ctx) return G6_ERR_ARG;
+  if (edge < 0.0) return fail(ctx, G6_ERR_ARG, "cell edge must be >= 0");
+  ctx->req = edge;
+  ctx->gref.valid = false;
+  return G6_OK;
+}
+
+int g6_set_skin(g6_ctx* ctx, double skin) {
+  if (!ctx) return G6_ERR_ARG;
+  if (!(skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
+  ctx->skin = skin;
+  ctx->glist.valid = false; ctx->cap = 0;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return G6_OK;
+}
+
+int g6_set_box(g6_ctx* ctx, int replica, const double* L3) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (replica < 0 || replica >= ctx->nrep || !L3) return fail(ctx, G6_ERR_ARG, "bad replica or box");
+  for (int d = 0; d < 3; ++d) {
+    if (!(L3[d] > 0.0)) return fail(ctx, G6_ERR_ARG, "box edges must be positive");
+    ctx->L[3 * replica + d] = L3[d];
+  }
+  CK(cudaSetDevice(ctx->device));
+  std::vector<double> invL(3 * ctx->nrep);
+  std::vector<float> fs(3 * ctx->nrep);
+  for (int k = 0; k < 3 * ctx->nrep; ++k) { invL[k] = 1.0 / ctx->L[k]; fs[k] = (float)(ctx->L[k] / 4294967296.0); }
+  CK(cudaMemcpy(ctx->d_L, ctx->L.data(), 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_invL, invL.data(), 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_fscale, fs.data(), 3 * ctx->nrep * sizeof(float), cudaMemcpyHostToDevice));
+  ctx->gref.valid = false; ctx->glist.valid = false; ctx->cap = 0;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return G6_OK;
+}
+
+int g6_upload_state(g6_ctx* ctx, const double* rec) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->n;
+  CK(cudaMemcpyAsync(ctx->d_stage, rec, (size_t)REC * n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_state = true;
+  return G6_OK;
+}
+
+int g6_download_state(g6_ctx* ctx, double* rec) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->n;
+  CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
+  CK(cudaMemcpyAsync(rec, ctx->d_stage, (size_t)REC * n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return G6_OK;
+}
+
+int g6_upload_poses(g6_ctx* ctx, const double* com, const double* quat) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (!com || !quat) return fail(ctx, G6_ERR_ARG, "com and quat are required");
+  CK(cudaSetDevice(ctx->device));
+  const int n = ctx->n;
+  std::vector<double> soa(7 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < 3; ++k) soa[(size_t)k * n + i] = com[3 * i + k];
+    for (int k = 0; k < 4; ++k) soa[(size_t)(3 + k) * n + i] = quat[4 * i + k];
+  }
+  CK(cudaMemcpy(ctx->d_st, soa.data(), 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_st + 33 * (size_t)n, soa.data() + 3 * (size_t)n, 4 * (size_t)n * sizeof(double),
+                cudaMemcpyHostToDevice));
+  ctx->have_state = true;
+  return G6_OK;
+}
+
+int g6_cells(g6_ctx* ctx, int* cell) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!cell) return fail(ctx, G6_ERR_ARG, "cell is NULL");
+  rc = prepare_ref_grid(ctx);
+  if (rc) return rc;
+  CellArgs ca = cell_args(ctx, ctx->gref, nullptr);
+  CK(launch_cells(ca, ctx->gref.d_start, ctx->gref.d_cellmol, ctx->stream));
+  CK(cudaMemcpyAsync(cell, ctx->gref.d_cell, ctx->n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return G6_OK;
+}
+
+int g6_pairsearch(g6_ctx* ctx, int64_t* npair) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  rc = prepare_ref_grid(ctx);
+  if (rc) return rc;
+  CellArgs ca = cell_args(ctx, ctx->gref, nullptr);
+  CK(launch_cells(ca, ctx->gref.d_start, ctx->gref.d_cellmol, ctx->stream));
+  PairSetArgs pa;
+  std::memset(&pa, 0, sizeof pa);
+  pa.n = ctx->n; pa.rep = rep_dev(ctx); pa.g = grid_dev(ctx->gref); pa.cell = ctx->gref.d_cell;
+  pa.start = ctx->gref.d_start; pa.cellmol = ctx->gref.d_cellmol; pa.sten = ctx->d_sten; pa.sten_off = ctx->d_sten_off;
+  pa.com = ctx->d_st; pa.rout2 = ctx->cc.rout2; pa.rin2 = ctx->cc.rin2; pa.rin = ctx->cc.rin; pa.rout = ctx->cc.rout;
+  pa.c1 = ctx->cc.c1; pa.c2 = ctx->cc.c2; pa.cnt = ctx->d_pcnt; pa.off = ctx->d_pcnt + ctx->n + 1;
+  CK(launch_pairset_count(pa, ctx->stream));
+  long long total = 0;
+  CK(cudaMemcpyAsync(&total, ctx->d_pcnt + 2 * (size_t)ctx->n + 1, sizeof(long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if ((size_t)total > ctx->pair_capacity) {
+    const size_t cap = (size_t)(total * 1.25) + 1024;
+    CK(dalloc(ctx, &ctx->d_pi, cap)); CK(dalloc(ctx, &ctx->d_pj, cap));
+    CK(dalloc(ctx, &ctx->d_ox, cap)); CK(dalloc(ctx, &ctx->d_oy, cap)); CK(dalloc(ctx, &ctx->d_oz, cap));
+    CK(dalloc(ctx, &ctx->d_hh, cap)); CK(dalloc(ctx, &ctx->d_dh, cap));
+    ctx->pair_capacity = cap;
+  }
+  pa.pi = ctx->d_pi; pa.pj = ctx->d_pj; pa.ox = ctx->d_ox; pa.oy = ctx->d_oy; pa.oz = ctx->d_oz;
+  pa.hh = ctx->d_hh; pa.dh = ctx->d_dh;
+  CK(launch_pairset_write(pa, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->npairs = total;
+  if (npair) *npair = total;
+  return G6_OK;
+}
+
+int g6_get_pairs(g6_ctx* ctx, int64_t cap, int* pi, int* pj, double* ox, double* oy, double* oz, double* hh,
+                 double* dh) {
+  if (!ctx) return G6_ERR_ARG;
+  if (ctx->npairs < 0) return fail(ctx, G6_ERR_STATE, "no pair set (g6_pairsearch)");
+  CK(cudaSetDevice(ctx->device));
+  const size_t m = (size_t)std::min<long long>(cap, ctx->npairs);
+  if (m == 0) return G6_OK;
+  if (pi) CK(cudaMemcpy(pi, ctx->d_pi, m * sizeof(int), cudaMemcpyDeviceToHost));
+  if (pj) CK(cudaMemcpy(pj, ctx->d_pj, m * sizeof(int), cudaMemcpyDeviceToHost));
+  if (ox) CK(cudaMemcpy(ox, ctx->d_ox, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (oy) CK(cudaMemcpy(oy, ctx->d_oy, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (oz) CK(cudaMemcpy(oz, ctx->d_oz, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (hh) CK(cudaMemcpy(hh, ctx->d_hh, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (dh) CK(cudaMemcpy(dh, ctx->d_dh, m * sizeof(double), cudaMemcpyDeviceToHost));
+  return G6_OK;
+}
+
+int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  rc = force_once(ctx);
+  if (rc) return rc;
+  const int n = ctx->n;
+  std::vector<double> hF(3 * (size_t)n), hT(3 * (size_t)n), hM(9 * (size_t)n), hE(n), hW(9 * (size_t)n);
+  CK(cudaMemcpy(hF.data(), ctx->d_F, hF.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hT.data(), ctx->d_tl, hT.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hM.data(), ctx->d_tmat, hM.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hE.data(), ctx->d_emol, hE.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hW.data(), ctx->d_wmol, hW.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) {
+    if (F)
+      for (int k = 0; k < 3; ++k) F[3 * i + k] = hF[(size_t)k * n + i];
+    if (tau) {
+      double t[9], l[3] = {hT[i], hT[(size_t)n + i], hT[2 * (size_t)n + i]};
+      for (int k = 0; k < 9; ++k) t[k] = hM[(size_t)k * n + i];
+      // rigid_collectforce RigidModule.F90:305-310: tau_body = T^T tau_lab
+      tau[3 * i] = t[0] * l[0] + t[3] * l[1] + t[6] * l[2];
+      tau[3 * i + 1] = t[1] * l[0] + t[4] * l[1] + t[7] * l[2];
+      tau[3 * i + 2] = t[2] * l[0] + t[5] * l[1] + t[8] * l[2];
+    }
+  }
+  for (int r = 0; r < ctx->nrep; ++r) {
+    double e = 0.0, w[9] = {0};
+    for (int i = ctx->off[r]; i < ctx->off[r + 1]; ++i) {
+      e += hE[i];
+      for (int k = 0; k < 9; ++k) w[k] += hW[(size_t)k * n + i];
+    }
+    if (epot) epot[r] = e;
+    if (vir)
+      for (int k = 0; k < 9; ++k) vir[9 * r + k] = w[k];
+  }
+  return G6_OK;
+}
+
+int g6_molecule_energies(g6_ctx* ctx, double* e) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!e) return fail(ctx, G6_ERR_ARG, "e is NULL");
+  rc = force_once(ctx);
+  if (rc) return rc;
+  CK(cudaMemcpy(e, ctx->d_emol, ctx->n * sizeof(double), cudaMemcpyDeviceToHost));
+  return G6_OK;
+}
+
+static int ensure_scratch(g6_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->scratch_bytes) return G6_OK;
+  if (ctx->d_scratch) { cudaFree(ctx->d_scratch); ctx->d_scratch = nullptr; ctx->scratch_bytes = 0; }
+  CK(cudaMalloc(&ctx->d_scratch, bytes));
+  ctx->scratch_bytes = bytes;
+  return G6_OK;
+}
+
+static int pairlist_call(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, double* fx,
+                         double* fy, double* fz, int64_t npair, const int* pi, const int* pj, const double* ox,
+                         const double* oy, const double* oz, const double* er, const double* fr, double* ep,
+                         double* vrmat, bool with_force) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (nsites < 0 || npair < 0) return fail(ctx, G6_ERR_ARG, "negative size");
+  if (nsites % ctx->mh.nsite != 0) return fail(ctx, G6_ERR_ARG, "nsites is not a multiple of the model's sites");
+  if (!x || !y || !z || (npair > 0 && (!pi || !pj || !ox || !oy || !oz || !er || !ep)))
+    return fail(ctx, G6_ERR_ARG, "NULL array");
+  if (with_force && (!fx || !fy || !fz || !vrmat || (npair > 0 && !fr))) return fail(ctx, G6_ERR_ARG, "NULL array");
+  const int nmol = nsites / ctx->mh.nsite;
+  for (int64_t k = 0; k < npair; ++k)
+    if (pi[k] < 0 || pi[k] >= nmol || pj[k] < 0 || pj[k] >= nmol)
+      return fail(ctx, G6_ERR_ARG, "pair index out of range");
+  CK(cudaSetDevice(ctx->device));
+  const size_t S = (size_t)nsites, P = (size_t)npair;
+  const size_t bytes = (with_force ? 6 : 3) * S * 8 + P * (2 * 4 + (with_force ? 6 : 5) * 8 + 8) + 9 * 8 + 64 * 16;
+  int rc = ensure_scratch(ctx, bytes);
+  if (rc) return rc;
+  char* p = (char*)ctx->d_scratch;
+  auto take = [&](size_t b) { char* q = p; p += (b + 255) / 256 * 256; return (void*)q; };
+  double* dx = (double*)take(S * 8); double* dy = (double*)take(S * 8); double* dz = (double*)take(S * 8);
+  double *dfx = nullptr, *dfy = nullptr, *dfz = nullptr;
+  if (with_force) { dfx = (double*)take(S * 8); dfy = (double*)take(S * 8); dfz = (double*)take(S * 8); }
+  int* dpi = (int*)take(P * 4); int* dpj = (int*)take(P * 4);
+  double* dox = (double*)take(P * 8); double* doy = (double*)take(P * 8); double* doz = (double*)take(P * 8);
+  double* dhh = (double*)take(P * 8); double* ddh = with_force ? (double*)take(P * 8) : nullptr;
+  double* dep = (double*)take(P * 8); double* dvir = (double*)take(9 * 8);
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemcpyAsync(dx, x, S * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dy, y, S * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dz, z, S * 8, cudaMemcpyHostToDevice, s));
+  if (with_force) {
+    CK(cudaMemcpyAsync(dfx, fx, S * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dfy, fy, S * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dfz, fz, S * 8, cudaMemcpyHostToDevice, s));
+  }
+  if (P) {
+    CK(cudaMemcpyAsync(dpi, pi, P * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dpj, pj, P * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dox, ox, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(doy, oy, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(doz, oz, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dhh, er, P * 8, cudaMemcpyHostToDevice, s));
+    if (with_force) CK(cudaMemcpyAsync(ddh, fr, P * 8, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemsetAsync(dvir, 0, 9 * 8, s));
+  SitesArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.nsite = ctx->mh.nsite; a.nq = ctx->nq; a.npair = npair; a.x = dx; a.y = dy; a.z = dz;
+  a.fx = dfx; a.fy = dfy; a.fz = dfz; a.pi = dpi; a.pj = dpj; a.ox = dox; a.oy = doy; a.oz = doz; a.hh = dhh;
+  a.dh = ddh; a.ep = dep; a.vir = dvir; a.pc = ctx->pc; a.with_force = with_force ? 1 : 0;
+  CK(launch_force_sites(a, ctx->model, s));
+  if (P) CK(cudaMemcpyAsync(ep, dep, P * 8, cudaMemcpyDeviceToHost, s));
+  if (with_force) {
+    CK(cudaMemcpyAsync(fx, dfx, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(fy, dfy, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(fz, dfz, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(vrmat, dvir, 9 * 8, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return G6_OK;
+}
+
+int g6_force_sites(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, double* fx, double* fy,
+                   double* fz, int64_t npair, const int* pair_i, const int* pair_j, const double* ox, const double* oy,
+                   const double* oz, const double* eratio, const double* fratio, double* ep, double* vrmat) {
+  return pairlist_call(ctx, nsites, x, y, z, fx, fy, fz, npair, pair_i, pair_j, ox, oy, oz, eratio, fratio, ep, vrmat,
+                       true);
+}
+
+int g6_pair_potential(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, int64_t npair,
+                      const int* pair_i, const int* pair_j, const double* ox, const double* oy, const double* oz,
+                      const double* eratio, double* ep) {
+  return pairlist_call(ctx, nsites, x, y, z, nullptr, nullptr, nullptr, npair, pair_i, pair_j, ox, oy, oz, eratio,
+                       nullptr, ep, nullptr, false);
+}
+
+// ---------------------------------------------------------------------------
+// Molecular dynamics
+// ---------------------------------------------------------------------------
+static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
+  StepArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.p = place_args(ctx);
+  a.mass = ctx->mh.mass; a.I[0] = ctx->mh.I[0]; a.I[1] = ctx->mh.I[1]; a.I[2] = ctx->mh.I[2]; a.dt = dt;
+  a.F = ctx->d_F; a.tl = ctx->d_tl; a.emol = ctx->d_emol; a.wmol = ctx->d_wmol; a.npin = ctx->d_npin;
+  a.com_build = ctx->d_com_build;
+  const double hs = 0.5 * effective_skin(ctx);
+  a.half_skin2 = hs * hs;
+  a.th = ctx->d_th; a.part = ctx->d_part; a.partmax = ctx->d_partmax; a.red = ctx->d_red; a.done = ctx->d_done;
+  a.ctrl = ctx->d_ctrl; a.log = log; a.seed = ctx->seed;
+  return a;
+}
+
+static int enqueue_step(g6_ctx* ctx, const StepArgs& sa) {
+  int rc = enqueue_rebuild(ctx, ctx->d_ctrl);
+  if (rc) return rc;
+  const bool timed = ctx->tcap > 0 && ctx->tnext < ctx->tcap;
+  if (timed) CK(cudaEventRecord(ctx->tev[2 * ctx->tnext], ctx->stream));
+  CK(launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
+  if (timed) { CK(cudaEventRecord(ctx->tev[2 * ctx->tnext + 1], ctx->stream)); ++ctx->tnext; }
+  CK(launch_correct_step(sa, ctx->stream));
+  return G6_OK;
+}
+
+static const int GRAPH_STEPS = 16;
+
+static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log, uint64_t seed) {
+  int rc = prepare_list(ctx);
+  if (rc) return rc;
+  if (ctx->lpi == 0) {
+    const char* env = std::getenv("G6_LPI");
+    ctx->lpi = env ? std::atoi(env) : default_lpi(ctx);
+    if (ctx->lpi != 4 && ctx->lpi != 8 && ctx->lpi != 16 && ctx->lpi != 32) ctx->lpi = default_lpi(ctx);
+  }
+  std::vector<ThermoDev> th(ctx->nrep);
+  for (int r = 0; r < ctx->nrep; ++r) {
+    ThermoDev& t = th[r];
+    std::memset(&t, 0, sizeof t);
+    if (thermo) {
+      t.kind = thermo[r].kind; t.temp = thermo[r].temp; t.q = thermo[r].q; t.dump = thermo[r].dump;
+      for (int k = 0; k < 5; ++k) t.z[k] = thermo[r].zeta[k];
+      t.zsum = thermo[r].zetasum; t.rate = thermo[r].collision_rate;
+      if (t.kind == G6_NOSE && !(t.q > 0.0)) return fail(ctx, G6_ERR_ARG, "Nose q must be > 0");
+      if (t.kind < G6_NVE || t.kind > G6_ANDERSEN) return fail(ctx, G6_ERR_ARG, "unknown thermostat");
+    }
+  }
+  CK(cudaMemcpyAsync(ctx->d_th, th.data(), th.size() * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
+  const size_t need_log = want_log ? (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH : 0;
+  if (need_log > ctx->log_cap) {
+    if (ctx->d_log) { cudaFree(ctx->d_log); ctx->d_log = nullptr; ctx->log_cap = 0; }
+    CK(cudaMalloc(&ctx->d_log, need_log * sizeof(double)));
+    ctx->log_cap = need_log;
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  }
+  int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
+  CK(cudaMemcpyAsync(ctx->d_ctrl, ctrl, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  (void)dt;
+  if (thermo && thermo[0].seed != ctx->seed) {
+    ctx->seed = thermo[0].seed;
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  }
+  (void)seed;
+  return G6_OK;
+}
+
+static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log) {
+  int ctrl[8], ovf = 0;
+  std::vector<ThermoDev> th(ctx->nrep);
+  std::vector<double> red((size_t)ctx->nrep * NRED);
+  CK(cudaMemcpyAsync(ctrl, ctx->d_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(th.data(), ctx->d_th, th.size() * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(red.data(), ctx->d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (log && nsteps > 0)
+    CK(cudaMemcpyAsync(log, ctx->d_log, (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int r = 0; r < ctx->nrep; ++r) {
+    ctx->last_epot[r] = red[(size_t)r * NRED];
+    if (thermo) {
+      thermo[r].temp = th[r].temp;
+      for (int k = 0; k < 5; ++k) thermo[r].zeta[k] = th[r].z[k];
+      thermo[r].zetasum = th[r].zsum;
+    }
+  }
+  if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow (raise the skin or density)");
+  if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");
+  if (ctrl[1] != nsteps) return fail(ctx, G6_ERR_STATE, "step counter mismatch");
+  ctx->steps_done += (unsigned long long)nsteps;
+  return G6_OK;
+}
+
+static int md_enqueue_steps(g6_ctx* ctx, int nsteps) {
+  StepArgs sa = step_args(ctx, ctx->run_dt, ctx->run_log ? ctx->d_log : nullptr);
+  // with per-step kernel timing the steps are launched directly (events per step)
+  const int full = ctx->tcap > 0 ? 0 : nsteps / GRAPH_STEPS;
+  const int rest = nsteps - full * GRAPH_STEPS;
+  int rc;
+  if (full > 0) {
+    const int want_log = ctx->run_log ? 1 : 0;
+    if (!ctx->graph || ctx->graph_dt != ctx->run_dt || ctx->graph_log != want_log) {
+      if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < GRAPH_STEPS; ++k) {
+        rc = enqueue_step(ctx, sa);
+        if (rc) { cudaStreamEndCapture(ctx->stream, &g); return rc; }
+      }
+      CK(cudaStreamEndCapture(ctx->stream, &g));
+      CK(cudaGraphInstantiate(&ctx->graph, g, 0));
+      cudaGraphDestroy(g);
+      ctx->graph_dt = ctx->run_dt; ctx->graph_log = want_log;
+    }
+    for (int k = 0; k < full; ++k) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+  }
+  for (int k = 0; k < rest; ++k) {
+    rc = enqueue_step(ctx, sa);
+    if (rc) return rc;
+  }
+  return G6_OK;
+}
+
+int g6_md_begin(g6_ctx* ctx, double dt, int max_steps, const g6_thermostat* thermo, int want_log) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!(dt > 0.0) || max_steps < 1) return fail(ctx, G6_ERR_ARG, "need dt > 0 and max_steps >= 1");
+  rc = md_prepare(ctx, dt, max_steps, const_cast<g6_thermostat*>(thermo), want_log != 0, 0);
+  if (rc) return rc;
+  ctx->run_dt = dt; ctx->run_log = want_log != 0; ctx->run_max = max_steps; ctx->run_done = 0; ctx->in_run = true;
+  CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
+  return G6_OK;
+}
+
+int g6_md_advance(g6_ctx* ctx, int nsteps) {
+  if (!ctx || !ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_md_advance outside g6_md_begin/g6_md_end");
+  if (nsteps < 0 || ctx->run_done + nsteps > ctx->run_max) return fail(ctx, G6_ERR_ARG, "more steps than max_steps");
+  CK(cudaSetDevice(ctx->device));
+  int rc = md_enqueue_steps(ctx, nsteps);
+  if (rc) return rc;
+  ctx->run_done += nsteps;
+  return G6_OK;
+}
+
+int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log) {
+  if (!ctx || !ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_md_end without g6_md_begin");
+  ctx->in_run = false;
+  CK(cudaSetDevice(ctx->device));
+  int rc = md_finish(ctx, ctx->run_done, thermo, ctx->run_log ? log : nullptr);
+  if (rc) return rc;
+  // every step but the last predicts the next one; the state is a corrected
+  // (reference-consistent) state only after exactly max_steps steps
+  if (ctx->run_done != ctx->run_max)
+    return fail(ctx, G6_ERR_STATE, "g6_md_end after fewer than max_steps steps: state holds a predicted step");
+  return G6_OK;
+}
+
+int g6_set_timing(g6_ctx* ctx, int max_steps) {
+  if (!ctx || max_steps < 0) return G6_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  free_timing(ctx);
+  for (int k = 0; k < 2 * max_steps; ++k) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    ctx->tev.push_back(e);
+  }
+  ctx->tcap = max_steps;
+  ctx->tnext = 0;
+  return G6_OK;
+}
+
+int g6_get_timing(g6_ctx* ctx, double* ms, int cap, int* count) {
+  if (!ctx || (cap > 0 && !ms)) return G6_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int m = std::min(cap, ctx->tnext);
+  for (int k = 0; k < m; ++k) {
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, ctx->tev[2 * k], ctx->tev[2 * k + 1]));
+    ms[k] = t;
+  }
+  if (count) *count = ctx->tnext;
+  return G6_OK;
+}
+
+int g6_stream(g6_ctx* ctx, void** stream) {
+  if (!ctx || !stream) return G6_ERR_ARG;
+  *stream = (void*)ctx->stream;
+  return G6_OK;
+}
+
+int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double* log) {
+  if (nsteps == 0 && ctx) return G6_OK;
+  int rc = g6_md_begin(ctx, dt, nsteps, thermo, log != nullptr);
+  if (rc) return rc;
+  rc = g6_md_advance(ctx, nsteps);
+  if (rc) { ctx->in_run = false; cudaStreamSynchronize(ctx->stream); return rc; }
+  return g6_md_end(ctx, thermo, log);
+}
+
+int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log) {
+  int rc = check_ready(ctx, false);
+  if (rc) return rc;
+  if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
+  const int n = ctx->n;
+  const size_t bytes = (size_t)REC * n * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));
+  ctx->have_state = true;
+  rc = md_prepare(ctx, dt, 1, thermo, log != nullptr, 0);
+  if (rc) return rc;
+  StepArgs sa = step_args(ctx, dt, log ? ctx->d_log : nullptr);
+  CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
+  rc = enqueue_step(ctx, sa);
+  if (rc) return rc;
+  CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
+  CK(cudaMemcpyAsync(rec, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return md_finish(ctx, 1, thermo, log);
+}
+
+int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta, g6_thermostat* thermo,
+                        int* accepted) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!beta || !thermo) return fail(ctx, G6_ERR_ARG, "beta and thermo are required");
+  if (parity != 0 && parity != 1) return fail(ctx, G6_ERR_ARG, "parity must be 0 or 1");
+  const int R = ctx->nrep;
+  std::vector<ThermoDev> th(R);
+  for (int r = 0; r < R; ++r) {
+    std::memset(&th[r], 0, sizeof(ThermoDev));
+    th[r].kind = thermo[r].kind; th[r].temp = thermo[r].temp; th[r].q = thermo[r].q; th[r].dump = thermo[r].dump;
+    for (int k = 0; k < 5; ++k) th[r].z[k] = thermo[r].zeta[k];
+    th[r].zsum = thermo[r].zetasum; th[r].rate = thermo[r].collision_rate;
+  }
+  CK(cudaMemcpyAsync(ctx->d_th, th.data(), R * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_beta, beta, R * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_epot_rep, ctx->last_epot.data(), R * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_acc, 0, R * sizeof(int), ctx->stream));
+  ExchArgs ea;
+  ea.nrep = R; ea.parity = parity; ea.seed = seed; ea.counter = counter; ea.epot = ctx->d_epot_rep; ea.beta = ctx->d_beta;
+  ea.th = ctx->d_th; ea.accepted = ctx->d_acc; ea.scale = ctx->d_scale;
+  CK(launch_exchange(ea, ctx->d_st, ctx->n, ctx->d_mol_rep, ctx->stream));
+  std::vector<int> acc(R);
+  CK(cudaMemcpyAsync(beta, ctx->d_beta, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(th.data(), ctx->d_th, R * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(acc.data(), ctx->d_acc, R * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int r = 0; r < R; ++r) {
+    thermo[r].temp = th[r].temp;
+    for (int k = 0; k < 5; ++k) thermo[r].zeta[k] = th[r].z[k];
+    if (accepted) accepted[r] = acc[r];
+  }
+  return G6_OK;
+}
+
+}  // extern "C"

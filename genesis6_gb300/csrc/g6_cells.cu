@@ -1,0 +1,274 @@
+// g6_cells.cu -- cell grid, exact pair set, and device neighbour list.
+//
+// K1 cell build (Address_Assign, GridModule.F90:503-552): every molecule gets
+// the reference's cell index, computed with the reference's FP64 steps
+// (box_renormalize, then dnint(delta * (1/cell)) wrapped into [0, ndiv)), a
+// warp-aggregated atomic count per cell, an exclusive scan, a scatter, and a
+// per-cell sort so that residents are listed in molecule order like the
+// reference's resident table.
+//
+// K3 exact pair set (Grid_NeighborList GridModule.F90:557-752 +
+// Interaction_Compress2 InteractionModule.F90:398-605 + CutOff_Dimmer2
+// CutoffModule.F90:220-278): for every i, the half-shell stencil cells and the
+// self-mirror cells with j > i, the strict FP64 test dd < rc^2, image offsets
+// and the switch values.  Two passes (count, scan, write) give a
+// deterministic order.
+//
+// Neighbour list: full list (both directions) over the 27 (distinct)
+// surrounding cells of a grid whose edge is >= rc + skin, screened with the
+// 32-bit fixed-point COM; compacted per warp with ballots.
+#include <cuda_runtime.h>
+
+#include "g6_internal.cuh"
+
+namespace g6 {
+
+
+__device__ __forceinline__ bool skip_ctrl(const int* ctrl) { return ctrl != nullptr && ctrl[0] == 0; }
+
+__global__ void k_cell_clear(int* count, int ncell, const int* ctrl) {
+  if (skip_ctrl(ctrl)) return;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c <= ncell; c += gridDim.x * blockDim.x) count[c] = 0;
+}
+
+// Reference cell index of one molecule (0-based, global over replicas).
+__device__ __forceinline__ int ref_cell(const RepDev& rep, const GridDev& g, int r, double x, double y, double z) {
+  double c[3] = {x, y, z};
+  int j[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double L = rep.L[3 * r + d], iL = rep.invL[3 * r + d];
+    double delta = c[d];
+    double cellv = xmul(xdnint(xmul(delta, iL)), L);
+    delta = xsub(delta, cellv);
+    int nd = g.nd[3 * r + d];
+    int jj = (int)xdnint(xmul(delta, g.icell[3 * r + d]));
+    if (jj < 0) jj += nd;
+    if (jj >= nd) jj -= nd;
+    // non-finite or absurd coordinates cannot index outside the grid; the
+    // integrator reports them separately (G6_ERR_NONFINITE)
+    if (!(jj >= 0 && jj < nd)) jj = 0;
+    j[d] = jj;
+  }
+  const int nx = g.nd[3 * r], ny = g.nd[3 * r + 1];
+  return g.cell_off[r] + (j[2] * ny + j[1]) * nx + j[0];
+}
+
+__global__ void k_cell_assign(CellArgs a) {
+  if (skip_ctrl(a.ctrl)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < a.n;
+  int c = -1;
+  if (valid) {
+    const int r = a.rep.mol_rep[i];
+    c = ref_cell(a.rep, a.g, r, a.com[i], a.com[a.n + i], a.com[2 * a.n + i]);
+    a.cell[i] = c;
+  }
+  // warp-aggregated atomic increment of the cell population
+  const unsigned act = __ballot_sync(0xffffffffu, valid);
+  if (!valid) return;
+  const unsigned peers = __match_any_sync(act, c);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&a.count[c], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  a.slot[i] = base + rank;
+}
+
+// Exclusive scan of count[0..m) into start[0..m] with one block of 1024 threads.
+template <class T>
+__global__ void __launch_bounds__(1024) k_scan(const T* count, T* start, int m, const int* ctrl) {
+  if (skip_ctrl(ctrl)) return;
+  __shared__ T part[1024];
+  const int t = threadIdx.x;
+  const int per = (m + 1023) / 1024;
+  const int b = t * per, e = min(m, b + per);
+  T s = 0;
+  for (int k = b; k < e; ++k) s += count[k];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    T v = (t >= off) ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  T run = (t == 0) ? 0 : part[t - 1];
+  for (int k = b; k < e; ++k) { start[k] = run; run += count[k]; }
+  if (t == 1023) start[m] = part[1023];
+}
+
+__global__ void k_cell_fill(CellArgs a, const int* start, int* cellmol) {
+  if (skip_ctrl(a.ctrl)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) cellmol[start[a.cell[i]] + a.slot[i]] = i;
+}
+
+// Residents of each cell in molecule order (insertion sort; cells are small).
+__global__ void k_cell_sort(const int* start, int* cellmol, int ncell, const int* ctrl) {
+  if (skip_ctrl(ctrl)) return;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const int b = start[c], e = start[c + 1];
+  for (int k = b + 1; k < e; ++k) {
+    int v = cellmol[k];
+    int m = k - 1;
+    while (m >= b && cellmol[m] > v) { cellmol[m + 1] = cellmol[m]; --m; }
+    cellmol[m + 1] = v;
+  }
+}
+
+cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream_t s) {
+  const int nc = a.g.ncell_total;
+  k_cell_clear<<<(nc + 256) / 256, 256, 0, s>>>(a.count, nc, a.ctrl);
+  if (a.n > 0) k_cell_assign<<<(a.n + 255) / 256, 256, 0, s>>>(a);
+  k_scan<int><<<1, 1024, 0, s>>>(a.count, start, nc, a.ctrl);
+  if (a.n > 0) k_cell_fill<<<(a.n + 255) / 256, 256, 0, s>>>(a, start, cellmol);
+  k_cell_sort<<<(nc + 127) / 128, 128, 0, s>>>(start, cellmol, nc, a.ctrl);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour list.  One warp per molecule.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
+  if (skip_ctrl(a.ctrl)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= a.n) return;   // whole warp leaves together
+  const int i = warp, n = a.n;
+  const int r = a.rep.mol_rep[i];
+  const int nx = a.g.nd[3 * r], ny = a.g.nd[3 * r + 1], nz = a.g.nd[3 * r + 2];
+  const int loc = a.cell[i] - a.g.cell_off[r];
+  const int cx = loc % nx, cy = (loc / nx) % ny, cz = loc / (nx * ny);
+  const uint32_t xi = a.fix[i], yi = a.fix[n + i], zi = a.fix[2 * n + i];
+  const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
+  // distinct neighbour offsets per dimension: {-1,0,1} (nd>=3), {0,1} (nd==2), {0} (nd==1)
+  const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
+  const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
+  const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
+  int* row = a.nbr + (size_t)i * a.cap;
+  int cnt = 0;
+  for (int oz = loz; oz <= hiz; ++oz) {
+    const int zz = (cz + oz + nz) % nz;
+    for (int oy = loy; oy <= hiy; ++oy) {
+      const int yy = (cy + oy + ny) % ny;
+      for (int ox = lox; ox <= hix; ++ox) {
+        const int xx = (cx + ox + nx) % nx;
+        const int c = a.g.cell_off[r] + (zz * ny + yy) * nx + xx;
+        const int b = a.start[c], e = a.start[c + 1];
+        for (int k0 = b; k0 < e; k0 += 32) {
+          const int k = k0 + lane;
+          bool in = false;
+          int j = -1;
+          if (k < e) {
+            j = a.cellmol[k];
+            if (j != i) {
+              float dx = (float)(int)(xi - a.fix[j]) * sx;
+              float dy = (float)(int)(yi - a.fix[n + j]) * sy;
+              float dz = (float)(int)(zi - a.fix[2 * n + j]) * sz;
+              in = dx * dx + dy * dy + dz * dz < a.rlist2;
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, in);
+          if (in) {
+            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+            if (pos < a.cap) row[pos] = j;
+          }
+          cnt += __popc(m);
+        }
+      }
+    }
+  }
+  if (lane == 0) {
+    if (cnt > a.cap) { atomicExch(a.overflow, 1); cnt = a.cap; }
+    a.nnb[i] = cnt;
+    a.com_build[i] = a.com[i];
+    a.com_build[n + i] = a.com[n + i];
+    a.com_build[2 * n + i] = a.com[2 * n + i];
+  }
+}
+
+cudaError_t launch_list(const ListArgs& a, cudaStream_t s) {
+  if (a.n == 0) return cudaSuccess;
+  const long long threads = (long long)a.n * 32;
+  k_list_build<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K3: exact pair set under the reference grid and stencil.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void exact_switch(double dd, double rin2, double rout2, double rin, double rout, double c1,
+                                             double c2, double& hh, double& dh) {
+  hh = 0.0; dh = 0.0;
+  if (dd < rout2) {
+    if (dd > rin2) {
+      double dr = __dsqrt_rn(dd);
+      double u = xsub(dr, rout), l = xsub(dr, rin), uu = xmul(u, u), ll = xmul(l, l);
+      double poly = xadd(xsub(xmul(10.0, ll), xmul(xmul(5.0, u), l)), uu);
+      hh = xmul(xmul(xmul(c1, uu), u), poly);
+      dh = -__ddiv_rn(xmul(xmul(c2, uu), ll), dr);
+    } else {
+      hh = 1.0; dh = 0.0;
+    }
+  }
+}
+
+__global__ void k_pairset(PairSetArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int n = a.n;
+  const int r = a.rep.mol_rep[i];
+  const int nx = a.g.nd[3 * r], ny = a.g.nd[3 * r + 1], nz = a.g.nd[3 * r + 2];
+  const int loc = a.cell[i] - a.g.cell_off[r];
+  const int cx = loc % nx, cy = (loc / nx) % ny, cz = loc / (nx * ny);
+  double L[3], iL[3], ci[3] = {a.com[i], a.com[n + i], a.com[2 * n + i]};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) { L[d] = a.rep.L[3 * r + d]; iL[d] = a.rep.invL[3 * r + d]; }
+  long long cnt = 0;
+  long long w = a.pass ? a.off[i] : 0;
+  for (int kind = 0; kind < 2; ++kind) {
+    for (int e = a.sten_off[r]; e < a.sten_off[r + 1]; ++e) {
+      if (a.sten[4 * e + 3] != kind) continue;
+      const int xx = (cx + a.sten[4 * e]) % nx, yy = (cy + a.sten[4 * e + 1]) % ny, zz = (cz + a.sten[4 * e + 2]) % nz;
+      const int c = a.g.cell_off[r] + (zz * ny + yy) * nx + xx;
+      for (int k = a.start[c]; k < a.start[c + 1]; ++k) {
+        const int j = a.cellmol[k];
+        if (kind == 1 && !(j > i)) continue;
+        double cj[3] = {a.com[j], a.com[n + j], a.com[2 * n + j]}, o[3], d[3];
+        double dd = exact_dd(ci, cj, L, iL, o, d);
+        if (!(dd < a.rout2)) continue;
+        if (a.pass) {
+          double h, dh;
+          exact_switch(dd, a.rin2, a.rout2, a.rin, a.rout, a.c1, a.c2, h, dh);
+          a.pi[w] = i; a.pj[w] = j;
+          a.ox[w] = o[0]; a.oy[w] = o[1]; a.oz[w] = o[2];
+          a.hh[w] = h; a.dh[w] = dh;
+          ++w;
+        }
+        ++cnt;
+      }
+    }
+  }
+  if (!a.pass) a.cnt[i] = cnt;
+}
+
+cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s) {
+  a.pass = 0;
+  if (a.n > 0) k_pairset<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+  k_scan<long long><<<1, 1024, 0, s>>>(a.cnt, a.cnt + a.n + 1, a.n, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s) {
+  a.pass = 1;
+  if (a.n > 0) k_pairset<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace g6

@@ -1,0 +1,454 @@
+// g6_force.cu -- site-site Lennard-Jones + Coulomb under the COM switch.
+//
+// k_force<Model, Real, LPI>: the hot kernel.  LPI lanes cooperate on one
+// i-molecule and walk its neighbour-list row (full list, both directions, so
+// no scatter to j and no atomics); each lane keeps FP32 (mixed) or FP64
+// (plain) partial sums of the i-site forces, the COM-site switch force, the
+// pair energy and the 3x3 molecular virial, and the lanes are combined in FP64
+// with warp shuffles.  The epilogue is rigid_collectforce: F = sum of site
+// forces, lab torque = sum r_s x f_s.
+//
+// Physics per molecule pair (i,j), restating StdForce StdInteraction.F90:201-604,
+// interaction_force_tip4p TIP4PModule.F90:187-758 and force_st2
+// ST2Module.F90:187-750:
+//   d   = com_i - com_j - image                     (Interaction_Compress2)
+//   hh, dh = cutoff_func(|d|^2)                      (CutoffModule.F90:38-59)
+//   e_lj = aa/r^12 + bb/r^6 on the LJ site pair, e_c = sum qq/r on charged pairs
+//   f_site = hh * (site-site force) [ST2 custom path: charged pairs x hh*s12]
+//   f_COM  = dh*e*d  [ST2: dh*e_lj*d + (dh*s12 + hh*ds12)*e_c*d]
+//   e_pair = hh*e    [ST2: e_c*hh*s12 + e_lj*hh]
+//   W     += d (x) (sum of i-site forces incl. f_COM)
+#include <cuda_runtime.h>
+
+#include "g6_internal.cuh"
+
+namespace g6 {
+
+template <int NQ_, bool TAPER_>
+struct MT {
+  static constexpr int NQ = NQ_;
+  static constexpr bool TAPER = TAPER_;
+  static constexpr int W64 = ((6 + 3 * NQ_) + 1) / 2 * 2;   // doubles per molecule in pk64
+  static constexpr int NPK = ((6 + 3 * NQ_) + 3) / 4;        // float4 per molecule in pk32
+};
+
+
+// ---------------------------------------------------------------------------
+// Switch and taper in either precision.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void switch_fn(R dd, R rin2, R rin, R rout, R c1, R c2, R& hh, R& dh) {
+  if (dd > rin2) {
+    R r = sqrt(dd);
+    R u = r - rout, l = r - rin, uu = u * u, ll = l * l;
+    hh = c1 * uu * u * (R(10) * ll - R(5) * u * l + uu);
+    dh = -c2 * uu * ll / r;
+  } else {
+    hh = R(1);
+    dh = R(0);
+  }
+}
+template <class R>
+__device__ __forceinline__ void taper_fn(R d12, R rl, R ru, R w3, R& s12, R& ds12) {
+  if (d12 < ru * ru) {
+    if (d12 < rl * rl) {
+      s12 = R(0); ds12 = R(0);
+    } else {
+      R r12 = sqrt(d12);
+      s12 = (r12 - rl) * (r12 - rl) * (R(3) * ru - rl - R(2) * r12) / w3;
+      ds12 = -(R(6) * (r12 - rl) * (ru - r12) / w3) / r12;
+    }
+  } else {
+    s12 = R(1); ds12 = R(0);
+  }
+}
+
+__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
+
+template <class R> struct Prm;
+template <> struct Prm<double> {
+  __device__ static double qq(const PairConst& p, int a, int b) { return p.qq[a][b]; }
+  __device__ static double aa(const PairConst& p) { return p.aa; }
+  __device__ static double bb(const PairConst& p) { return p.bb; }
+};
+template <> struct Prm<float> {
+  __device__ static float qq(const PairConst& p, int a, int b) { return p.fqq[a][b]; }
+  __device__ static float aa(const PairConst& p) { return p.faa; }
+  __device__ static float bb(const PairConst& p) { return p.fbb; }
+};
+
+// Site-site loop of one molecule pair.  ri/rj: site offsets from their COM
+// (index 0 = LJ site, 1..NQ = charged sites).  Adds i-side results to acc.
+template <class M, class R>
+struct Acc {
+  R fs[M::NQ + 1][3];
+  R fc[3];
+  R e;
+  R w[9];
+  __device__ void zero() {
+#pragma unroll
+    for (int s = 0; s <= M::NQ; ++s) fs[s][0] = fs[s][1] = fs[s][2] = R(0);
+    fc[0] = fc[1] = fc[2] = R(0);
+    e = R(0);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[k] = R(0);
+  }
+};
+
+template <class M, class R>
+__device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::NQ + 1][3],
+                                          const R (&rj)[M::NQ + 1][3], const PairConst& pc, R rin2, R rin, R rout,
+                                          R c1, R c2, R trl, R tru, R tw3, Acc<M, R>& acc) {
+  R hh, dh;
+  switch_fn<R>(dd, rin2, rin, rout, c1, c2, hh, dh);
+  // LJ site pair (site 0 - site 0)
+  R v[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) v[k] = d[k] + ri[0][k] - rj[0][k];
+  R inv = R(1) / (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  R d6 = inv * inv * inv, d12 = d6 * d6;
+  const R aa = Prm<R>::aa(pc), bb = Prm<R>::bb(pc);
+  R elj = aa * d12 + bb * d6;
+  R flj = inv * (aa * R(12) * d12 + bb * R(6) * d6);
+  R fsite[M::NQ + 1][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) fsite[0][k] = v[k] * flj;
+  // charged site pairs
+  R ec = R(0);
+#pragma unroll
+  for (int a = 1; a <= M::NQ; ++a) {
+    R fa0 = R(0), fa1 = R(0), fa2 = R(0);
+#pragma unroll
+    for (int b = 1; b <= M::NQ; ++b) {
+      R x = d[0] + ri[a][0] - rj[b][0];
+      R y = d[1] + ri[a][1] - rj[b][1];
+      R z = d[2] + ri[a][2] - rj[b][2];
+      R rr = rsqrt_r(x * x + y * y + z * z);
+      R e0 = Prm<R>::qq(pc, a - 1, b - 1) * rr;
+      R f0 = e0 * rr * rr;
+      ec += e0;
+      fa0 += x * f0; fa1 += y * f0; fa2 += z * f0;
+    }
+    fsite[a][0] = fa0; fsite[a][1] = fa1; fsite[a][2] = fa2;
+  }
+  R scc = hh, dcc = dh;
+  if (M::TAPER) {
+    R s12, ds12;
+    taper_fn<R>(dd, trl, tru, tw3, s12, ds12);
+    scc = hh * s12;
+    dcc = dh * s12 + hh * ds12;
+  }
+  R fcom = dh * elj + dcc * ec;
+  R fp[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    R t = hh * fsite[0][k];
+    acc.fs[0][k] += t;
+    R sum = t;
+#pragma unroll
+    for (int a = 1; a <= M::NQ; ++a) {
+      R u = scc * fsite[a][k];
+      acc.fs[a][k] += u;
+      sum += u;
+    }
+    R c = fcom * d[k];
+    acc.fc[k] += c;
+    fp[k] = sum + c;
+  }
+  acc.e += hh * elj + scc * ec;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) acc.w[3 * a + b] += d[a] * fp[b];
+}
+
+__device__ __forceinline__ double shfl_xor_d(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+template <int LPI>
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int m = LPI / 2; m >= 1; m >>= 1) v += shfl_xor_d(v, m);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// k_force: neighbour-list force kernel.
+// ---------------------------------------------------------------------------
+template <class M, bool MIXED, int LPI>
+__global__ void __launch_bounds__(128) k_force(ForceArgs a) {
+  using R = typename std::conditional<MIXED, float, double>::type;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt / LPI;
+  const int sub = gt % LPI;
+  const bool valid = i < a.n;
+  const int n = a.n;
+
+  Acc<M, R> acc;
+  acc.zero();
+  R ri[M::NQ + 1][3];
+  int npin = 0;
+  if (valid) {
+    const int r = a.rep.mol_rep[i];
+    double Ld[3], iLd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { Ld[k] = a.rep.L[3 * r + k]; iLd[k] = a.rep.invL[3 * r + k]; }
+    const double* pi = a.pk64 + (size_t)i * M::W64;
+    double ci[3] = {pi[0], pi[1], pi[2]};
+    const int nn = a.nnb[i];
+    const int* row = a.nbr + (size_t)i * a.cap;
+    if (MIXED) {
+      float wi[4 * M::NPK];
+#pragma unroll
+      for (int q = 0; q < M::NPK; ++q) {
+        float4 t = a.pk32[(size_t)i * M::NPK + q];
+        wi[4 * q] = t.x; wi[4 * q + 1] = t.y; wi[4 * q + 2] = t.z; wi[4 * q + 3] = t.w;
+      }
+      const uint32_t xi = __float_as_uint(wi[0]), yi = __float_as_uint(wi[1]), zi = __float_as_uint(wi[2]);
+#pragma unroll
+      for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ri[s][k] = (R)wi[3 + 3 * s + k];
+      const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
+      const float rout2 = a.cc.frout2;
+      const float band = 1e-3f;   // |dd32 - dd64| is below 1e-4 A^2 for boxes up to 1000 A
+      for (int k = sub; k < nn; k += LPI) {
+        const int j = row[k];
+        float wj[4 * M::NPK];
+#pragma unroll
+        for (int q = 0; q < M::NPK; ++q) {
+          float4 t = a.pk32[(size_t)j * M::NPK + q];
+          wj[4 * q] = t.x; wj[4 * q + 1] = t.y; wj[4 * q + 2] = t.z; wj[4 * q + 3] = t.w;
+        }
+        float d[3];
+        d[0] = (float)(int)(xi - __float_as_uint(wj[0])) * sx;
+        d[1] = (float)(int)(yi - __float_as_uint(wj[1])) * sy;
+        d[2] = (float)(int)(zi - __float_as_uint(wj[2])) * sz;
+        float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        bool in = dd < rout2;
+        if (fabsf(dd - rout2) < band) {
+          // borderline: decide with the reference's FP64 arithmetic
+          const double* pj = a.pk64 + (size_t)j * M::W64;
+          double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
+          in = exact_dd(ci, cj, Ld, iLd, o, dx) < a.cc.rout2;
+        }
+        if (!in) continue;
+        ++npin;
+        R rj[M::NQ + 1][3];
+#pragma unroll
+        for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) rj[s][q] = (R)wj[3 + 3 * s + q];
+        R dr[3] = {(R)d[0], (R)d[1], (R)d[2]};
+        pair_math<M, R>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.frin2, (R)a.cc.frin, (R)a.cc.frout, (R)a.cc.fc1,
+                        (R)a.cc.fc2, (R)a.pc.frl, (R)a.pc.fru, (R)a.pc.fw3, acc);
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ri[s][k] = (R)pi[3 + 3 * s + k];
+      for (int k = sub; k < nn; k += LPI) {
+        const int j = row[k];
+        const double* pj = a.pk64 + (size_t)j * M::W64;
+        double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
+        double dd = exact_dd(ci, cj, Ld, iLd, o, dx);
+        if (!(dd < a.cc.rout2)) continue;
+        ++npin;
+        R rj[M::NQ + 1][3];
+#pragma unroll
+        for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) rj[s][q] = (R)pj[3 + 3 * s + q];
+        R dr[3] = {(R)dx[0], (R)dx[1], (R)dx[2]};
+        pair_math<M, R>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1, (R)a.cc.c2,
+                        (R)a.pc.rl, (R)a.pc.ru, (R)a.pc.w3, acc);
+      }
+    }
+  }
+  // rigid_collectforce on the lane partials, then combine the LPI lanes in FP64
+  double v[16];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    R s = acc.fc[k];
+#pragma unroll
+    for (int q = 0; q <= M::NQ; ++q) s += acc.fs[q][k];
+    v[k] = (double)s;
+  }
+  {
+    R tx = 0, ty = 0, tz = 0;
+#pragma unroll
+    for (int q = 0; q <= M::NQ; ++q) {
+      tx += ri[q][1] * acc.fs[q][2] - ri[q][2] * acc.fs[q][1];
+      ty += ri[q][2] * acc.fs[q][0] - ri[q][0] * acc.fs[q][2];
+      tz += ri[q][0] * acc.fs[q][1] - ri[q][1] * acc.fs[q][0];
+    }
+    v[3] = (double)tx; v[4] = (double)ty; v[5] = (double)tz;
+  }
+  v[6] = (double)acc.e;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) v[7 + k] = (double)acc.w[k];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = group_sum<LPI>(v[k]);
+  int np_tot = npin;
+#pragma unroll
+  for (int m = LPI / 2; m >= 1; m >>= 1) np_tot += __shfl_xor_sync(0xffffffffu, np_tot, m);
+  if (valid && sub == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
+    a.emol[i] = 0.5 * v[6];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
+    if (a.npair_in) a.npair_in[i] = np_tot;
+  }
+}
+
+template <class M, bool MIXED, int LPI>
+static cudaError_t launch_force_t(const ForceArgs& a, cudaStream_t s) {
+  const int threads = 128;
+  const long long total = (long long)a.n * LPI;
+  const int blocks = (int)((total + threads - 1) / threads);
+  if (blocks == 0) return cudaSuccess;
+  k_force<M, MIXED, LPI><<<blocks, threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <class M, bool MIXED>
+static cudaError_t launch_force_l(const ForceArgs& a, int lpi, cudaStream_t s) {
+  switch (lpi) {
+    case 4: return launch_force_t<M, MIXED, 4>(a, s);
+    case 8: return launch_force_t<M, MIXED, 8>(a, s);
+    case 16: return launch_force_t<M, MIXED, 16>(a, s);
+    default: return launch_force_t<M, MIXED, 32>(a, s);
+  }
+}
+
+template <class M>
+static cudaError_t launch_force_m(const ForceArgs& a, bool mixed, int lpi, cudaStream_t s) {
+  return mixed ? launch_force_l<M, true>(a, lpi, s) : launch_force_l<M, false>(a, lpi, s);
+}
+
+cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cudaStream_t s) {
+  if (model == G6_TIP4P) return launch_force_m<MT<3, false>>(a, mixed, lpi, s);
+  if (a.pc.taper) return launch_force_m<MT<4, true>>(a, mixed, lpi, s);
+  return launch_force_m<MT<4, false>>(a, mixed, lpi, s);
+}
+
+int pk64_width(int model) { return model == G6_TIP4P ? MT<3, false>::W64 : MT<4, false>::W64; }
+int pk32_width(int model) { return model == G6_TIP4P ? MT<3, false>::NPK : MT<4, false>::NPK; }
+
+// ---------------------------------------------------------------------------
+// Pair-list kernels for the reference-facing calls g6_force_sites and
+// g6_pair_potential: one thread per pair of the caller's compressed list,
+// absolute FP64 site positions (site%x of the reference), site forces
+// scattered with FP64 atomics (i: +, j: -), per-pair ep, block-reduced virial.
+// ---------------------------------------------------------------------------
+
+template <int NQ, bool TAPER>
+__global__ void __launch_bounds__(128) k_force_sites(SitesArgs a) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (k < a.npair) {
+    const int ns = a.nsite, last = ns - 1;
+    const int ii = a.pi[k] * ns, jj = a.pj[k] * ns;
+    const double ox = a.ox[k], oy = a.oy[k], oz = a.oz[k];
+    const double hh = a.hh[k], dh = a.with_force ? a.dh[k] : 0.0;
+    double d[3] = {a.x[ii + last] - a.x[jj + last] - ox, a.y[ii + last] - a.y[jj + last] - oy,
+                   a.z[ii + last] - a.z[jj + last] - oz};
+    double fi[NQ + 2][3], fj[NQ + 2][3];
+#pragma unroll
+    for (int s = 0; s < NQ + 2; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fi[s][c] = fj[s][c] = 0.0;
+    // LJ site pair
+    double vx = a.x[ii] - a.x[jj] - ox, vy = a.y[ii] - a.y[jj] - oy, vz = a.z[ii] - a.z[jj] - oz;
+    double inv = 1.0 / (vx * vx + vy * vy + vz * vz);
+    double d6 = inv * inv * inv, d12 = d6 * d6;
+    double elj = a.pc.aa * d12 + a.pc.bb * d6;
+    double flj = inv * (a.pc.aa * 12.0 * d12 + a.pc.bb * 6.0 * d6);
+    fi[0][0] = fj[0][0] = vx * flj; fi[0][1] = fj[0][1] = vy * flj; fi[0][2] = fj[0][2] = vz * flj;
+    double ec = 0;
+#pragma unroll
+    for (int p = 1; p <= NQ; ++p)
+#pragma unroll
+      for (int q = 1; q <= NQ; ++q) {
+        double x = a.x[ii + p] - a.x[jj + q] - ox, y = a.y[ii + p] - a.y[jj + q] - oy,
+               z = a.z[ii + p] - a.z[jj + q] - oz;
+        double dd = 1.0 / (x * x + y * y + z * z);
+        double ri = sqrt(dd);
+        double e0 = a.pc.qq[p - 1][q - 1] * ri;
+        double f0 = e0 * dd;
+        ec += e0;
+        fi[p][0] += x * f0; fi[p][1] += y * f0; fi[p][2] += z * f0;
+        fj[q][0] += x * f0; fj[q][1] += y * f0; fj[q][2] += z * f0;
+      }
+    double scc = hh, dcc = dh;
+    if (TAPER) {
+      double s12, ds12;
+      double d12c = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      if (d12c < a.pc.ru * a.pc.ru) {
+        if (d12c < a.pc.rl * a.pc.rl) { s12 = 0; ds12 = 0; }
+        else {
+          double r12 = sqrt(d12c);
+          s12 = (r12 - a.pc.rl) * (r12 - a.pc.rl) * (3.0 * a.pc.ru - a.pc.rl - 2.0 * r12) / a.pc.w3;
+          ds12 = -(6.0 * (r12 - a.pc.rl) * (a.pc.ru - r12) / a.pc.w3) / r12;
+        }
+      } else { s12 = 1; ds12 = 0; }
+      scc = hh * s12;
+      dcc = dh * s12 + hh * ds12;
+    }
+    a.ep[k] = hh * elj + scc * ec;
+    if (a.with_force) {
+      double fcom = dh * elj + dcc * ec;
+      double fp[3] = {0, 0, 0};
+#pragma unroll
+      for (int s = 0; s < NQ + 1; ++s) {
+        double sc = (s == 0) ? hh : scc;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { fi[s][c] *= sc; fj[s][c] *= sc; fp[c] += fi[s][c]; }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { fi[NQ + 1][c] = fcom * d[c]; fj[NQ + 1][c] = fcom * d[c]; fp[c] += fcom * d[c]; }
+      // site index of the COM is the last site; charged sites are 1..NQ; LJ site 0
+#pragma unroll
+      for (int s = 0; s < NQ + 2; ++s) {
+        int si = (s == NQ + 1) ? last : s;
+        atomicAdd(&a.fx[ii + si], fi[s][0]); atomicAdd(&a.fy[ii + si], fi[s][1]); atomicAdd(&a.fz[ii + si], fi[s][2]);
+        atomicAdd(&a.fx[jj + si], -fj[s][0]); atomicAdd(&a.fy[jj + si], -fj[s][1]); atomicAdd(&a.fz[jj + si], -fj[s][2]);
+      }
+#pragma unroll
+      for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) w[3 * p + q] = d[p] * fp[q];
+    }
+  }
+  if (a.with_force) {
+    __shared__ double sw[9][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+      double v = w[c];
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+      if (lane == 0) sw[c][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+      double v = 0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += sw[threadIdx.x][q];
+      atomicAdd(&a.vir[threadIdx.x], v);
+    }
+  }
+}
+
+cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s) {
+  const int threads = 128;
+  const long long blocks = (a.npair + threads - 1) / threads;
+  if (blocks == 0) return cudaSuccess;
+  if (model == G6_TIP4P) k_force_sites<3, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else if (a.pc.taper) k_force_sites<4, true><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else k_force_sites<4, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace g6

@@ -1,0 +1,303 @@
+// g6_internal.cuh -- shared definitions of the sm_103a rigid-water library.
+//
+// Device data layout (one context = one system of nrep replicas, n molecules
+// in replica order):
+//   st      FP64 SoA rigid state, st[c*n + i], c in [0,53): com[3], d[5][3],
+//           w[5][3], q[5][4] (the 53-double record of g6gpu.h)
+//   tmat    FP64 SoA rotation matrices (body -> lab), tmat[k*n + i]
+//   pk64    FP64 AoS packed pose per molecule for the site loop:
+//           com[3], LJ-site offset[3], charged-site offsets[3*NQ] (+pad)
+//   pk32    float4 AoS packed pose for the mixed site loop: 32-bit fixed-point
+//           COM (x,y,z as uint32 in units of L/2^32), then float offsets of
+//           the LJ site and the charged sites relative to the COM
+//   fix     uint32 SoA fixed-point COM (list building and cell-free tests)
+//   F, tl   per-molecule force and lab-frame torque (FP64 SoA)
+//   emol, wmol  per-molecule energy (1/2 of its pair sum) and virial rows
+// Cells are counting-sorted molecule ids (cell_mol) with start offsets; the
+// neighbour list is a fixed-capacity row per molecule (nbr[i*cap + k]).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/g6gpu.h"
+
+namespace g6 {
+
+constexpr int REC = 53;
+constexpr int MAXSITE = 6;  // sites per molecule including the COM site
+constexpr int MAXQ = 4;     // charged sites per molecule
+constexpr int MAXREP_PER_BLOCK = 8;
+constexpr int RED_BLOCK = 128;   // block size of the per-molecule update kernels
+constexpr int NRED = 24;         // reduced quantities per replica (see g6_md.cu)
+
+// ---------------------------------------------------------------------------
+// Model constants (host computes them from the reference formulas; the device
+// receives them by value in kernel arguments).
+// ---------------------------------------------------------------------------
+struct PairConst {
+  double qq[MAXQ][MAXQ];   // charged-site pair prefactors (already x100 internal units)
+  double aa, bb;           // LJ site pair: e = aa/r^12 + bb/r^6
+  float fqq[MAXQ][MAXQ];
+  float faa, fbb;
+  int taper;               // ST2 Coulomb taper (force_st2 / pairpotential_st2)
+  double rl, ru, w3;       // taper range and (ru-rl)^3
+  float frl, fru, fw3;
+};
+
+struct CutConst {
+  double rin, rout, rin2, rout2, c1, c2;
+  float frin, frout, frin2, frout2, fc1, fc2;
+};
+
+// Per-replica geometry of one cell grid.
+struct GridDev {
+  int ncell_total;
+  const int* nd;         // 3*nrep
+  const double* cell;    // 3*nrep cell edge
+  const double* icell;   // 3*nrep 1/cell
+  const int* cell_off;   // nrep+1
+};
+
+struct RepDev {
+  int nrep;
+  const int* off;        // nrep+1 molecule offsets
+  const int* mol_rep;    // n
+  const double* L;       // 3*nrep
+  const double* invL;    // 3*nrep
+  const float* fscale;   // 3*nrep  L / 2^32
+};
+
+// ---------------------------------------------------------------------------
+// Exact FP64 helpers: explicit round-to-nearest intrinsics are never fused
+// into FMAs, so these reproduce the reference's separate multiply/add steps.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+// Fortran dnint: round half away from zero.
+__device__ __forceinline__ double xdnint(double x) { return round(x); }
+
+// Minimum-image COM separation exactly as Interaction_Compress2
+// (InteractionModule.F90:454-465): o = dnint(delta*invL)*L, d = delta - o,
+// dd = (dx^2 + dy^2) + dz^2.
+__device__ __forceinline__ double exact_dd(const double ci[3], const double cj[3], const double L[3],
+                                           const double iL[3], double o[3], double d[3]) {
+  for (int k = 0; k < 3; ++k) {
+    double delta = xsub(ci[k], cj[k]);
+    o[k] = xmul(xdnint(xmul(delta, iL[k])), L[k]);
+    d[k] = xsub(delta, o[k]);
+  }
+  return xadd(xadd(xmul(d[0], d[0]), xmul(d[1], d[1])), xmul(d[2], d[2]));
+}
+
+// Fixed-point COM: x -> round(frac(x/L) * 2^32) as uint32.  Differences of
+// two such words, read as int32, are the minimum-image separation in units of
+// L/2^32.
+__device__ __forceinline__ uint32_t to_fixed(double x, double invL) {
+  double f = x * invL;
+  f = f - floor(f);
+  unsigned long long u = __double2ull_rn(f * 4294967296.0);
+  return (uint32_t)(u & 0xffffffffull);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11), identical to the oracle's generator.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)M0 * c[0];
+    uint64_t p1 = (uint64_t)M1 * c[2];
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += W0; k1 += W1;
+  }
+}
+// Two uniforms in (0,1] with 53-bit resolution.
+__host__ __device__ __forceinline__ void uniform2(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                  double out[2]) {
+  uint32_t c[4] = {c0, c1, c2, c3};
+  philox4x32(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    uint64_t u = ((uint64_t)(c[2 * k] >> 5) << 26) | (uint64_t)(c[2 * k + 1] >> 6);
+    out[k] = ((double)u + 1.0) * (1.0 / 9007199254740992.0);
+  }
+}
+
+// Physical constants (PhysConst.F90:4-62).
+constexpr double PI = 3.1415926535897932;
+constexpr double NA = 6.0225e23;
+constexpr double KB = 1.380066e-23;
+constexpr double RGAS = NA * KB;
+constexpr double CA = 4.184;
+constexpr double COEFF = CA * 332.17752;
+constexpr double I2J = 10.0;
+constexpr double J2I = 1.0 / 10.0;
+constexpr double J2K = 0.120273;
+constexpr double KX2X = 1000.0;
+constexpr double A2P = 101326.0;
+constexpr double ANG2M = 1e-10;
+
+// Gear coefficients, PhysConst.F90:7-15
+constexpr double G50 = 3.0 / 16.0, G51 = 251.0 / 360.0, G53 = 11.0 / 18.0, G54 = 1.0 / 6.0, G55 = 1.0 / 60.0;
+constexpr double G40 = 251.0 / 720.0, G42 = 11.0 / 12.0, G43 = 1.0 / 3.0, G44 = 1.0 / 24.0;
+
+// ---------------------------------------------------------------------------
+// Kernel argument blocks (passed by value).
+// ---------------------------------------------------------------------------
+struct ForceArgs {
+  int n, cap, stride_pk32;
+  const int* nbr;
+  const int* nnb;
+  RepDev rep;
+  const double* pk64;
+  const float4* pk32;
+  PairConst pc;
+  CutConst cc;
+  double* F;      // 3 SoA
+  double* tl;     // 3 SoA lab torque
+  double* emol;   // n
+  double* wmol;   // 9 SoA
+  int* npair_in;  // per molecule: pairs within rc (diagnostic, optional)
+};
+
+struct SitesArgs {
+  int nsite, nq;
+  long long npair;
+  const double *x, *y, *z;
+  double *fx, *fy, *fz;
+  const int *pi, *pj;
+  const double *ox, *oy, *oz, *hh, *dh;
+  double* ep;
+  double* vir;   // 9, accumulated with atomics
+  PairConst pc;
+  int with_force;
+};
+
+struct CellArgs {
+  int n;
+  RepDev rep;
+  GridDev g;
+  const double* com;   // SoA (x: com[i], y: com[n+i], z: com[2n+i])
+  int* cell;           // n
+  int* slot;           // n
+  int* count;          // ncell_total
+  const int* ctrl;     // optional: ctrl[0] == 0 -> skip (no rebuild this step)
+};
+
+struct ListArgs {
+  int n, cap;
+  RepDev rep;
+  GridDev g;
+  const int* cell;
+  const int* start;
+  const int* cellmol;
+  const uint32_t* fix;   // SoA 3n
+  const double* com;     // SoA 3n (state)
+  double* com_build;     // SoA 3n
+  float rlist2;
+  int* nbr;
+  int* nnb;
+  int* overflow;
+  const int* ctrl;
+};
+
+struct PairSetArgs {
+  int n;
+  RepDev rep;
+  GridDev g;
+  const int* cell;
+  const int* start;
+  const int* cellmol;
+  const int* sten;       // (x,y,z,kind) per entry; kind 0 half shell, 1 self-mirror (j > i)
+  const int* sten_off;   // nrep+1
+  const double* com;     // SoA 3n
+  double rout2, rin2, rin, rout, c1, c2;
+  long long* cnt;        // n+1 (pass 0 writes counts; the scan turns them into offsets)
+  const long long* off;  // pass 1
+  int pass;
+  int* pi; int* pj;
+  double *ox, *oy, *oz, *hh, *dh;
+};
+
+struct ThermoDev {
+  int kind;
+  double temp, q, dump;
+  double z[5];
+  double zsum;
+  double rate;
+};
+
+struct PlaceArgs {
+  int n, nq, npk, w64;
+  RepDev rep;
+  double body[MAXSITE][3];
+  double* st;
+  double* tmat;
+  double* pk64;
+  float4* pk32;
+  uint32_t* fix;
+};
+
+struct StepArgs {
+  PlaceArgs p;
+  double mass, I[3], dt;
+  const double* F;
+  const double* tl;
+  const double* emol;
+  const double* wmol;
+  const int* npin;
+  const double* com_build;
+  double half_skin2;
+  ThermoDev* th;
+  double* part;        // gridDim * MAXREP_PER_BLOCK * NRED
+  double* partmax;     // gridDim
+  double* red;         // nrep * NRED (finalize scratch)
+  unsigned int* done;
+  int* ctrl;           // [0] rebuild, [1] step, [2] nsteps, [3] error bits, [4] list overflow, [5] log capacity
+  double* log;         // [step][rep][G6_LOG_WIDTH]
+  unsigned long long seed;
+};
+
+struct ExchArgs {
+  int nrep, parity;
+  unsigned long long seed, counter;
+  const double* epot;   // per replica
+  double* beta;
+  ThermoDev* th;
+  int* accepted;
+  double* scale;        // per replica velocity scale (1 if unchanged)
+};
+
+// ---------------------------------------------------------------------------
+// Host-side declarations shared between translation units.
+// ---------------------------------------------------------------------------
+struct ModelHost {
+  int model = 0, nsite = 0, nq = 0;
+  double body[MAXSITE][3] = {};
+  double param[MAXSITE][3] = {};   // q, eps, sig
+  double mass = 0, I[3] = {};
+};
+bool make_model(int model, ModelHost& m);
+void make_pair_const(const ModelHost& m, int path, PairConst& pc);
+void make_cut_const(double rin, double rout, CutConst& cc);
+
+cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
+cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s);
+int pk64_width(int model);
+int pk32_width(int model);
+cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream_t s);
+cudaError_t launch_list(const ListArgs& a, cudaStream_t s);
+cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s);
+cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
+cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
+cudaError_t launch_correct_step(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s);
+cudaError_t launch_exchange(const ExchArgs& a, double* st, int n, const int* mol_rep, cudaStream_t s);
+
+}  // namespace g6

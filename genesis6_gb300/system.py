@@ -1,0 +1,146 @@
+"""Host-side owner of one device system (one g6_ctx).
+
+``RigidWater`` mirrors the set-up the reference drivers perform (Mixture.F90
+and mc2.F90: model constructor + @BOX3 + @RCOA + @VOXA, then the per-step force
+path) on top of the C ABI.  All compute goes through libg6gpu.so; there is no
+CPU fallback: without a GPU, ``RigidWater(...)`` raises G6Error.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import G6Error, Thermostat, dptr, iptr
+
+
+class RigidWater:
+    """nrep replicas of one rigid water model on one GPU."""
+
+    def __init__(self, model: str, nmol, box, *, path: str = "custom", precision: str = "fp64", rc: float = 9.0,
+                 switch: float = 2.0, cell_edge: float = 0.0, skin: float = 1.0, device: int = 0):
+        self.L = _capi.lib()
+        self.model = model
+        self.path = path
+        self.precision = precision
+        nmol = np.atleast_1d(np.asarray(nmol, dtype=np.int32))
+        box = np.ascontiguousarray(np.asarray(box, dtype=np.float64).reshape(len(nmol), 3))
+        self.nmol = nmol
+        self.box = box
+        self.nrep = len(nmol)
+        self.n = int(nmol.sum())
+        self.rc = float(rc)
+        self.rin = float(rc - switch)
+        ptr = ctypes.c_void_p()
+        st = self.L.g6_ctx_create(device, ctypes.byref(ptr))
+        if st != _capi.G6_OK:
+            raise G6Error(st, "g6_ctx_create(%d) failed (no usable CUDA device?)" % device)
+        self.ctx = ptr
+        self._check(self.L.g6_system(self.ctx, _capi.MODELS[model], _capi.PATHS[path],
+                                     _capi.PRECISIONS[precision], self.nrep, iptr(np.ascontiguousarray(nmol)),
+                                     dptr(box)))
+        self._check(self.L.g6_set_cutoff(self.ctx, self.rin, self.rc))   # cutoff_initialize(in, out)
+        self._check(self.L.g6_set_grid(self.ctx, float(cell_edge)))
+        self._check(self.L.g6_set_skin(self.ctx, float(skin)))
+        self.info = _capi.model_info(model)
+
+    # -- plumbing -------------------------------------------------------
+    def _check(self, status):
+        if status != _capi.G6_OK:
+            msg = self.L.g6_last_error(self.ctx).decode() if getattr(self, "ctx", None) else ""
+            raise G6Error(status, msg)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.g6_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state ----------------------------------------------------------
+    def upload_state(self, rec):
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        assert rec.shape == (self.n, _capi.REC)
+        self._check(self.L.g6_upload_state(self.ctx, dptr(rec)))
+
+    def download_state(self):
+        rec = np.zeros((self.n, _capi.REC))
+        self._check(self.L.g6_download_state(self.ctx, dptr(rec)))
+        return rec
+
+    def upload_poses(self, com, quat):
+        com = np.ascontiguousarray(com, dtype=np.float64)
+        quat = np.ascontiguousarray(quat, dtype=np.float64)
+        self._check(self.L.g6_upload_poses(self.ctx, dptr(com), dptr(quat)))
+
+    # -- parity surface ---------------------------------------------------
+    def cells(self):
+        c = np.zeros(self.n, dtype=np.int32)
+        self._check(self.L.g6_cells(self.ctx, iptr(c)))
+        return c
+
+    def pairsearch(self):
+        npair = ctypes.c_int64()
+        self._check(self.L.g6_pairsearch(self.ctx, ctypes.byref(npair)))
+        m = npair.value
+        pi = np.zeros(max(m, 1), np.int32); pj = np.zeros(max(m, 1), np.int32)
+        ox, oy, oz, hh, dh = (np.zeros(max(m, 1)) for _ in range(5))
+        self._check(self.L.g6_get_pairs(self.ctx, m, iptr(pi), iptr(pj), dptr(ox), dptr(oy), dptr(oz), dptr(hh),
+                                        dptr(dh)))
+        s = slice(0, m)
+        return dict(i=pi[s], j=pj[s], ox=ox[s], oy=oy[s], oz=oz[s], hh=hh[s], dh=dh[s])
+
+    def force(self):
+        """F (n,3), body torque (n,3), epot (nrep,), virial (nrep,3,3)."""
+        F = np.zeros((self.n, 3)); tau = np.zeros((self.n, 3))
+        ep = np.zeros(self.nrep); vir = np.zeros((self.nrep, 9))
+        self._check(self.L.g6_force(self.ctx, dptr(F), dptr(tau), dptr(ep), dptr(vir)))
+        return F, tau, ep, vir.reshape(self.nrep, 3, 3)
+
+    def molecule_energies(self):
+        e = np.zeros(self.n)
+        self._check(self.L.g6_molecule_energies(self.ctx, dptr(e)))
+        return e
+
+    # -- dynamics ---------------------------------------------------------
+    @staticmethod
+    def thermostats(nrep, kind="nve", temp=300.0, q=0.0, dump=0.0, rate=0.0, seed=0):
+        arr = (Thermostat * nrep)()
+        kinds = {"nve": _capi.NVE, "nose": _capi.NOSE, "andersen": _capi.ANDERSEN}
+        temps = np.broadcast_to(np.asarray(temp, dtype=np.float64), (nrep,))
+        for r in range(nrep):
+            arr[r].kind = kinds[kind]
+            arr[r].temp = float(temps[r]); arr[r].q = q; arr[r].dump = dump
+            arr[r].collision_rate = rate; arr[r].seed = seed
+        return arr
+
+    def md_run(self, dt, nsteps, thermo=None, log=True):
+        if thermo is None:
+            thermo = self.thermostats(self.nrep)
+        buf = np.zeros((nsteps, self.nrep, _capi.LOG_WIDTH)) if log else None
+        self._check(self.L.g6_md_run(self.ctx, float(dt), int(nsteps), thermo, dptr(buf)))
+        return buf
+
+    def md_step_host(self, dt, rec, thermo=None, log=None):
+        if thermo is None:
+            thermo = self.thermostats(self.nrep)
+        self._check(self.L.g6_md_step_host(self.ctx, float(dt), thermo, dptr(rec), dptr(log)))
+        return rec
+
+    def replica_exchange(self, parity, seed, counter, beta, thermo):
+        beta = np.ascontiguousarray(beta, dtype=np.float64)
+        acc = np.zeros(self.nrep, np.int32)
+        self._check(self.L.g6_replica_exchange(self.ctx, int(parity), int(seed), int(counter), dptr(beta), thermo,
+                                               iptr(acc)))
+        return beta, acc

@@ -1,0 +1,190 @@
+/*
+ * g6gpu.h -- C ABI of the GB300 (sm_103a) rigid-water force/energy library.
+ *
+ * This is the drop-in boundary for Genesis6's rigid-molecule force path.  Each
+ * entry point names the Fortran interface it replaces (file:line in the
+ * Genesis6 sources).  Conventions:
+ *   - every function returns an int status (G6_OK = 0, G6_ERR_* otherwise);
+ *     g6_last_error() gives a one-line message for the last failure;
+ *   - host pointers are borrowed for the duration of the call, never retained;
+ *   - a context owns all device memory of one system (one or more replicas);
+ *     use one context per host thread;
+ *   - calls are synchronous at return;
+ *   - indices are 0-based (the Fortran shim subtracts 1);
+ *   - arrays are row-major: com (n,3), quat (n,4), rec (n,53), F/tau (n,3);
+ *     a 3x3 virial is vir[3*a+b] = sum over pairs of d00_a * F_b, which is
+ *     the reference's vrmat(a,b).
+ *   - units are the reference's: Angstrom, ps, amu, energy in 10 J/mol.
+ */
+#ifndef G6GPU_H
+#define G6GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define G6_OK 0
+#define G6_ERR_ARG 1        /* bad argument or unsupported combination          */
+#define G6_ERR_CUDA 2       /* CUDA runtime error (message in g6_last_error)    */
+#define G6_ERR_CAPACITY 3   /* a fixed-capacity device table overflowed          */
+#define G6_ERR_NONFINITE 4  /* NaN/Inf coordinates or forces detected            */
+#define G6_ERR_TIMEOUT 5    /* a bounded device-side wait gave up                */
+#define G6_ERR_STATE 6      /* call order violated (e.g. no system defined)      */
+
+/* models: site order is the reference's, the centre of mass is the last site */
+#define G6_TIP4P 1 /* O, M, H, H, COM      TIP4PModule.F90:43-97               */
+#define G6_TIP5P 2 /* O, H, H, L, L, COM   TIP5PModule.F90:57-83, RigidModule.F90:429-477 */
+#define G6_ST2 3   /* O, H, H, M, M, COM   ST2Module.F90:10-100                */
+
+/* force path, the reference's `custom` flag (@FAST) of Interaction2.F90:19-68 */
+#define G6_PATH_STD 0    /* StdForce / StdPairPotential (LB mixing, no ST2 taper)   */
+#define G6_PATH_CUSTOM 1 /* hand kernels: interaction_force_tip4p, force_st2 (taper) */
+
+/* arithmetic of the site-site loop */
+#define G6_FP64 0  /* plain form: everything in double                              */
+#define G6_MIXED 1 /* site-site math in float, per-molecule and global sums in double */
+
+/* thermostats for g6_md_run */
+#define G6_NVE 0
+#define G6_NOSE 1     /* Nose-Hoover zeta with Gear-4, NoseModule.F90:43-87           */
+#define G6_ANDERSEN 2 /* stochastic-collision thermostat (new; the reference's Andersen is a barostat) */
+
+typedef struct g6_ctx g6_ctx;
+
+/* Per-replica thermostat parameters. */
+typedef struct g6_thermostat {
+  int kind;              /* G6_NVE, G6_NOSE or G6_ANDERSEN                            */
+  double temp;           /* target temperature [K]                                    */
+  double q;              /* Nose mass in the reference's internal form (input q times
+                            21.8852721616497249235^2, NoseModule.F90:101)            */
+  double dump;           /* Nose damping term (@NOS2 dump)                            */
+  double zeta[5];        /* Nose zeta0..zeta4                                          */
+  double zetasum;        /* running sum of zeta0 (conserved-quantity term)            */
+  double collision_rate; /* Andersen: collisions per molecule per ps                  */
+  uint64_t seed;         /* Andersen: random stream (first replica's value is used)   */
+} g6_thermostat;
+
+/* Per-step log record written by g6_md_run (doubles, 10 per replica per step). */
+#define G6_LOG_WIDTH 10
+/* [0] Epot  [1] Ekin translational  [2] Ekin rotational  (internal units)
+   [3] T [K]  [4] P [atm]  [5] H [J/mol] (Mixture.F90:2431-2453)
+   [6] pairs within rc  [7] zeta0  [8] neighbour-list rebuild flag  [9] step   */
+
+int g6_version(void);
+const char* g6_last_error(const g6_ctx* ctx);
+const char* g6_status_string(int status);
+
+/* Host-only model tables (no device work): body-frame site coordinates
+   (nsite,3), site parameters (nsite,3) = (charge, LJ eps [kJ/mol], LJ sigma [A])
+   as sStdInt%param (StdInteraction.F90:34-39), and mass, Ixx, Iyy, Izz. */
+int g6_model_info(int model, int* nsite, double* body, double* param, double* mass_inertia);
+
+int g6_ctx_create(int device, g6_ctx** out);
+int g6_ctx_destroy(g6_ctx* ctx);
+
+/* Define the system: nrep replicas of one model; replica r holds nmol[r]
+   molecules in an orthorhombic box box[3r..3r+2].  Replaces the allocation
+   done by Mol_allocate / interaction_initialize (MolModule.F90:63-113,
+   InteractionModule.F90:199-223). */
+int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const int* nmol, const double* box);
+
+/* cutoff_initialize(in, out), CutoffModule.F90:25-36 (@RCOA rc margin gives in = rc - margin). */
+int g6_set_cutoff(g6_ctx* ctx, double r_in, double r_out);
+/* Requested cell edge of the adaptive grid (@VOXA, GridModule.F90:488-501); 0 selects r_out. */
+int g6_set_grid(g6_ctx* ctx, double cell_edge);
+/* Verlet margin of the device neighbour list (>= 0).  The set of interacting
+   pairs is unchanged: every pair is re-tested against r_out each step. */
+int g6_set_skin(g6_ctx* ctx, double skin);
+/* Box of replica r (BoxModule @BOX3); invalidates the neighbour list. */
+int g6_set_box(g6_ctx* ctx, int replica, const double* L3);
+
+/* State transfer.  rec is the per-molecule rigid record (53 doubles):
+   com[3], d[5][3] (dx(1..5): Gear-5 COM stack, dx(1) = v*dt), w[5][3]
+   (angular velocity stack, body frame), q[5][4] (quaternion stack), i.e. the
+   content of sRigid1 (RigidModule.F90:14-24).  Poses only: com (n,3), quat (n,4). */
+int g6_upload_state(g6_ctx* ctx, const double* rec);
+int g6_download_state(g6_ctx* ctx, double* rec);
+int g6_upload_poses(g6_ctx* ctx, const double* com, const double* quat);
+
+/* Address_Assign (GridModule.F90:503-552): 0-based cell id of every molecule
+   under the reference grid (bit-exact with the reference FP64 arithmetic). */
+int g6_cells(g6_ctx* ctx, int* cell);
+/* Grid_Update + Address_Assign + Grid_NeighborList + Interaction_Compress2 +
+   CutOff_Dimmer2 (GridModule.F90:95, 503, 557; InteractionModule.F90:398;
+   CutoffModule.F90:220): build the exact within-cutoff pair set on the device. */
+int g6_pairsearch(g6_ctx* ctx, int64_t* npair);
+/* Copy the pair set of the last g6_pairsearch: pair_i/pair_j, image offsets
+   ox/oy/oz (iv%ox..), eratio (hh) and fratio (dh).  cap bounds every array. */
+int g6_get_pairs(g6_ctx* ctx, int64_t cap, int* pi, int* pj, double* ox, double* oy, double* oz, double* hh,
+                 double* dh);
+
+/* Full force path on the uploaded poses: rigid_setsiteposition
+   (RigidModule.F90:146) -> pair search -> switch -> force (Interaction2.F90:19)
+   -> rigid_collectforce (RigidModule.F90:159).  Outputs per-molecule COM force
+   F (n,3), body-frame torque tau (n,3), per-replica potential energy
+   epot[nrep] and virial vir[nrep*9].  Any output pointer may be NULL. */
+int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir);
+/* Per-molecule potential energy e_i = 1/2 sum_j e_ij (n) of the uploaded poses. */
+int g6_molecule_energies(g6_ctx* ctx, double* e);
+
+/* The reference `force(iv,mi,mj,site,ep,vrmat,custom,si,sj)` call,
+   Interaction2.F90:19-68, for one homogeneous component: caller-owned site
+   arrays (site%x/y/z, molecule m site s at m*nsite+s), the compressed pair
+   list with image offsets and switch factors.  Site forces are ACCUMULATED
+   into fx/fy/fz (the caller zeroes them, site_resetforce); ep[npair] and
+   vrmat[9] are outputs.  Model and path come from g6_system. */
+int g6_force_sites(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, double* fx, double* fy,
+                   double* fz, int64_t npair, const int* pair_i, const int* pair_j, const double* ox, const double* oy,
+                   const double* oz, const double* eratio, const double* fratio, double* ep, double* vrmat);
+/* The reference `PairPotential(iv,mi,mj,site,ep,custom,si,sj)`, Interaction2.F90:71-121. */
+int g6_pair_potential(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, int64_t npair,
+                      const int* pair_i, const int* pair_j, const double* ox, const double* oy, const double* oz,
+                      const double* eratio, double* ep);
+
+/* Molecular dynamics on the device-resident state: per step rigid_predict,
+   Nose_Predict, site placement, pair search, force, rigid_collectforce,
+   rigid_correct, Rigid_Ek, Nose_Correct in the order of Mixture.F90:1789-2290.
+   dt in ps.  thermo[nrep] is read at the start and written back at the end.
+   log (optional) receives nsteps*nrep*G6_LOG_WIDTH doubles, step-major.
+   The steps run as CUDA-graph launches with no host synchronisation inside. */
+int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double* log);
+
+/* g6_md_run split into its three phases so that a driver can interleave its
+   own stream work: g6_md_begin uploads the thermostats and performs the first
+   rigid_predict; g6_md_advance enqueues nsteps steps on the context's stream
+   and returns without synchronising (at most max_steps in total);
+   g6_md_end synchronises, returns thermostats/log and reports device errors. */
+int g6_md_begin(g6_ctx* ctx, double dt, int max_steps, const g6_thermostat* thermo, int want_log);
+int g6_md_advance(g6_ctx* ctx, int nsteps);
+int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log);
+/* The cudaStream_t (as void*) on which the context enqueues its work. */
+int g6_stream(g6_ctx* ctx, void** stream);
+/* Per-step kernel timing: g6_set_timing(ctx, m) arms CUDA events around the
+   force kernel of the next m MD steps (those steps launch without a CUDA
+   graph); g6_get_timing returns their durations in ms (count = steps timed).
+   g6_set_timing(ctx, 0) disarms. */
+int g6_set_timing(g6_ctx* ctx, int max_steps);
+int g6_get_timing(g6_ctx* ctx, double* ms, int cap, int* count);
+
+/* One MD step with the state in caller-owned host memory: uploads rec,
+   advances one step, downloads rec and the step's log record.  This is the
+   call a host-side driver makes when it keeps the state itself. */
+int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log);
+
+/* replica_exchange_trial (Replica.F90:7-73) for neighbouring temperatures of
+   the replicas of this context, FP64 acceptance.  beta[nrep] is in 1/K and is
+   permuted in place on acceptance (with the MD side effects of
+   Mixture.F90:1630-1653: velocities scaled by sqrt(T'/T), Nose zeta reset).
+   parity selects the pairs (r, r+1) with r % 2 == parity.  accepted[nrep]
+   (optional) gets 1 for each lower member of an accepted pair. */
+int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
+                        g6_thermostat* thermo, int* accepted);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* G6GPU_H */

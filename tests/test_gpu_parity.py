@@ -1,0 +1,200 @@
+"""GPU parity: libg6gpu.so (through its C ABI) against the FP64 oracle.
+
+Bars:
+  - cell ids and the within-cutoff pair set: bit-exact, including the image
+    offsets and the switch values hh/dh of every pair;
+  - plain FP64 mode: total energy and virial to 1e-12 relative, per-molecule
+    force/torque to 1e-12 of the RMS force/torque;
+  - mixed mode: relative RMS force error <= 1e-5 (torques <= 1e-5).
+"""
+import numpy as np
+import pytest
+
+import genesis6_gb300 as g6
+from genesis6_gb300 import config
+from genesis6_gb300.interaction import Interaction, Sites, force, pair_potential, site_positions
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "std"), ("ST2", "custom"), ("ST2", "std")]
+
+
+def _system(model, path, n, seed, prec="fp64", rc=8.5, jitter=0.4, skin=1.0, cell_edge=0.0):
+    b = config.water_box(model, n, seed, jitter=jitter)
+    s = g6.RigidWater(model, n, b["L"], path=path, precision=prec, rc=rc, skin=skin, cell_edge=cell_edge)
+    s.upload_state(b["rec"])
+    return s, b
+
+
+def _canon(p):
+    a = np.minimum(p["i"], p["j"]); b = np.maximum(p["i"], p["j"])
+    key = a.astype(np.int64) * 10 ** 7 + b
+    return key
+
+
+@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (1000, 7.0)])
+def test_cells_bitexact(orc, n, rc):
+    s, b = _system("TIP4P", "custom", n, 11 + n, rc=rc, jitter=3.0)
+    cell_gpu = s.cells()
+    cell_orc, _ = orc.pairsearch(b["com"], b["L"], [rc] * 3, rc - 2.0, rc)
+    assert np.array_equal(cell_gpu, cell_orc)
+
+
+@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (512, 9.5)])
+def test_pairset_bitexact(orc, n, rc):
+    s, b = _system("TIP4P", "custom", n, 3 + n, rc=rc, jitter=3.0)
+    pg = s.pairsearch()
+    _, po = orc.pairsearch(b["com"], b["L"], [rc] * 3, rc - 2.0, rc)
+    kg, ko = _canon(pg), _canon(po)
+    assert len(kg) == len(ko) == len(np.unique(kg))
+    og, oo = np.argsort(kg), np.argsort(ko)
+    assert np.array_equal(kg[og], ko[oo])
+    # orientation of each pair may differ; image offsets flip sign with it
+    sg = np.where(pg["i"][og] < pg["j"][og], 1.0, -1.0)
+    so = np.where(po["i"][oo] < po["j"][oo], 1.0, -1.0)
+    for k in ("ox", "oy", "oz"):
+        assert np.array_equal(pg[k][og] * sg, po[k][oo] * so)
+    for k in ("hh", "dh"):
+        assert np.array_equal(pg[k][og], po[k][oo])   # bit-exact switch values
+
+
+@pytest.mark.parametrize("model,path", CASES)
+def test_force_fp64_matches_oracle(orc, model, path):
+    n = 256 if model == "TIP4P" else 343
+    L = config.box_edge(n)
+    rc = min(8.5, 0.5 * L - 0.05)
+    s, b = _system(model, path, n, 21, rc=rc)
+    F, tau, ep, vir = s.force()
+    Fo, to, Eo, Vo, _ = orc.compute(model, path, b["com"], b["quat"], b["L"], [rc] * 3, rc - 2.0, rc)
+    assert ep[0] == pytest.approx(Eo, rel=1e-12)
+    assert np.abs(vir[0] - Vo).max() <= 1e-12 * np.abs(Vo).max()
+    frms = np.sqrt((Fo ** 2).sum(1).mean()); trms = np.sqrt((to ** 2).sum(1).mean())
+    assert np.abs(F - Fo).max() <= 1e-12 * frms
+    assert np.abs(tau - to).max() <= 1e-12 * trms
+
+
+def test_force_fp64_4096(orc):
+    s, b = _system("TIP4P", "custom", 4096, 4, rc=9.0)
+    F, tau, ep, vir = s.force()
+    Fo, to, Eo, Vo, _ = orc.compute("TIP4P", "custom", b["com"], b["quat"], b["L"], [9.0] * 3, 7.0, 9.0)
+    assert ep[0] == pytest.approx(Eo, rel=1e-12)
+    assert np.abs(vir[0] - Vo).max() <= 1e-12 * np.abs(Vo).max()
+    frms = np.sqrt((Fo ** 2).sum(1).mean())
+    assert np.abs(F - Fo).max() <= 1e-12 * frms
+
+
+@pytest.mark.parametrize("model,path", CASES)
+def test_force_mixed_rms_error(orc, model, path):
+    n = 512
+    L = config.box_edge(n)
+    rc = min(9.0, 0.5 * L - 0.05)
+    s, b = _system(model, path, n, 31, prec="mixed", rc=rc)
+    F, tau, ep, vir = s.force()
+    Fo, to, Eo, Vo, _ = orc.compute(model, path, b["com"], b["quat"], b["L"], [rc] * 3, rc - 2.0, rc)
+    ef = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    et = np.sqrt(((tau - to) ** 2).sum() / (to ** 2).sum())
+    assert ef <= 1e-5, ef
+    assert et <= 1e-5, et
+    assert ep[0] == pytest.approx(Eo, rel=1e-5)
+
+
+@pytest.mark.parametrize("model,path", CASES)
+def test_force_sites_entry_matches_reference_call(orc, model, path):
+    """g6_force_sites / g6_pair_potential mirror force()/PairPotential() on the caller's pair list."""
+    n = 216
+    L = config.box_edge(n)
+    rc = min(8.5, 0.5 * L - 0.05)
+    b = config.water_box(model, n, 41, jitter=0.4)
+    s = g6.RigidWater(model, n, b["L"], path=path, rc=rc)
+    x, y, z = orc.place_sites(model, b["com"], b["quat"])[:3]
+    _, p = orc.pairsearch(b["com"], b["L"], [rc] * 3, rc - 2.0, rc)
+    site = Sites.of(x, y, z)
+    iv = Interaction.from_pairs(p)
+    ep, vr = force(s, site, iv)
+    fx, fy, fz, epo, vro = orc.force_sites(model, path, x, y, z, p)
+    fs = np.abs(np.concatenate([fx, fy, fz])).max()
+    assert np.abs(site.fx - fx).max() <= 1e-12 * fs
+    assert np.abs(site.fy - fy).max() <= 1e-12 * fs
+    assert np.abs(site.fz - fz).max() <= 1e-12 * fs
+    assert np.abs(ep - epo).max() <= 1e-12 * np.abs(epo).max()
+    assert np.abs(vr - vro).max() <= 1e-12 * np.abs(vro).max()
+    e2 = pair_potential(s, site, iv)
+    e2o = orc.pair_potential(model, path, x, y, z, p)
+    assert np.abs(e2 - e2o).max() <= 1e-12 * np.abs(e2o).max()
+    # host-side site placement agrees with the oracle's
+    hx, hy, hz = site_positions(model, b["com"], b["quat"])
+    assert np.abs(hx - x).max() < 1e-12
+
+
+def test_md_fp64_follows_oracle(orc):
+    """Short Gear MD: the device trajectory tracks the oracle's step by step."""
+    n = 256
+    b = config.water_box("TIP4P", n, 5, temp=300.0, dt=0.002, jitter=0.2)
+    L = b["L"]
+    s = g6.RigidWater("TIP4P", n, L, path="custom", rc=8.5, skin=1.0)
+    s.upload_state(b["rec"])
+    log = s.md_run(0.002, 20)
+    rec_g = s.download_state()
+    rec_o, _, log_o = orc.md_run("TIP4P", "custom", b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 20, np.zeros(10))
+    assert np.abs(log[:, 0, 0] - log_o[:, 0]).max() <= 1e-9 * np.abs(log_o[:, 0]).max()
+    assert np.abs(log[:, 0, 5] - log_o[:, 5]).max() <= 1e-9 * np.abs(log_o[:, 5]).max()
+    assert np.abs(rec_g[:, :3] - rec_o[:, :3]).max() < 1e-9
+    assert np.abs(rec_g[:, 33:37] - rec_o[:, 33:37]).max() < 1e-9
+    assert np.array_equal(log[:, 0, 6], log_o[:, 6])   # pairs within rc, every step
+
+
+def test_md_nose_follows_oracle(orc):
+    n = 216
+    b = config.water_box("TIP4P", n, 6, temp=350.0, dt=0.002, jitter=0.2)
+    L = b["L"]
+    q = 300.0 * 0.1 ** 2 / 0.002
+    s = g6.RigidWater("TIP4P", n, L, path="custom", rc=8.5)
+    s.upload_state(b["rec"])
+    th = s.thermostats(1, "nose", temp=300.0, q=q, dump=0.0)
+    log = s.md_run(0.002, 25, th)
+    t_o = np.array([1, q, 0.0, 300.0, 0, 0, 0, 0, 0, 0], float)
+    _, t_o, log_o = orc.md_run("TIP4P", "custom", b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 25, t_o)
+    assert np.abs(log[:, 0, 7] - log_o[:, 7]).max() <= 1e-9 * max(1e-30, np.abs(log_o[:, 7]).max())
+    assert np.abs(log[:, 0, 5] - log_o[:, 5]).max() <= 1e-9 * np.abs(log_o[:, 5]).max()
+    assert th[0].zeta[0] == pytest.approx(t_o[4], rel=1e-8)
+
+
+def test_md_mixed_conserves_energy():
+    n = 512
+    b = config.water_box("TIP4P", n, 8, temp=300.0, dt=0.001, jitter=0.2)
+    s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision="mixed", rc=9.0)
+    s.upload_state(b["rec"])
+    s.md_run(0.001, 200)        # relax the lattice start
+    log = s.md_run(0.001, 400)
+    H = log[:, 0, 5]
+    ek = (log[:, 0, 1] + log[:, 0, 2]).mean() * 10.0   # J/mol
+    assert np.isfinite(H).all()
+    assert np.ptp(H) < 0.02 * ek
+
+
+def test_replicas_equal_separate_systems(orc):
+    sizes = [216, 300, 250]
+    boxes, recs = [], []
+    for k, n in enumerate(sizes):
+        b = config.water_box("TIP4P", n, 100 + k, jitter=0.3)
+        boxes.append(b["L"]); recs.append(b)
+    s = g6.RigidWater("TIP4P", sizes, np.array(boxes), path="custom", rc=8.5)
+    s.upload_state(np.concatenate([b["rec"] for b in recs]))
+    F, tau, ep, vir = s.force()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for k, b in enumerate(recs):
+        Fo, to, Eo, Vo, _ = orc.compute("TIP4P", "custom", b["com"], b["quat"], b["L"], [8.5] * 3, 6.5, 8.5)
+        assert ep[k] == pytest.approx(Eo, rel=1e-12)
+        frms = np.sqrt((Fo ** 2).sum(1).mean())
+        assert np.abs(F[off[k]:off[k + 1]] - Fo).max() <= 1e-12 * frms
+
+
+def test_nonfinite_state_is_reported():
+    b = config.water_box("TIP4P", 256, 1)
+    s = g6.RigidWater("TIP4P", 256, b["L"], rc=8.5)
+    rec = b["rec"].copy()
+    rec[7, 3:6] = np.nan      # a velocity that turns the COM into NaN after predict
+    s.upload_state(rec)
+    with pytest.raises(g6.G6Error) as e:
+        s.md_run(0.002, 3)
+    assert e.value.status == g6._capi.G6_ERR_NONFINITE
