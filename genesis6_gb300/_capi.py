@@ -32,7 +32,7 @@ SYMBOLS = [
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
     "g6_molecule_energies", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
-    "g6_set_timing", "g6_get_timing",
+    "g6_set_timing", "g6_get_timing", "g6_force_noalloc",
 ]
 
 
@@ -94,6 +94,8 @@ def lib():
     L.g6_md_advance.argtypes = [vp, ctypes.c_int]
     L.g6_md_end.argtypes = [vp, ctypes.POINTER(Thermostat), dp]
     L.g6_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.g6_force_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, vp, vp, vp, vp, vp, vp]
     L.g6_set_timing.argtypes = [vp, ctypes.c_int]
     L.g6_get_timing.argtypes = [vp, dp, ctypes.c_int, ip]
     for name in SYMBOLS:

@@ -183,6 +183,25 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
 int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
                         g6_thermostat* thermo, int* accepted);
 
+/* Force evaluation that allocates no device memory.  No counterpart in the
+   reference: it exists for callers that may not call cudaMalloc -- programs
+   whose device memory is owned by their own arena or pool, or that must not
+   grow the process's device footprint -- and that hold their own device
+   buffers.  Same computation as g6_force (sites, cell grid, neighbour list,
+   force, collect) for ONE system of at most G6_NOALLOC_MAX_MOL molecules;
+   larger n returns G6_ERR_CAPACITY.  d_com (n,3), d_quat (n,4) are device
+   inputs; d_F (n,3), d_tau (n,3, body frame) and d_epot (1) are device
+   outputs; box (3) is host memory; stream is a cudaStream_t (NULL = default).
+   Intermediate tables live in one static device array of 7,129,856 bytes (6.8 MiB) that
+   every GPU loading the library keeps until exit.  The first call on a device
+   looks up that array's address: make it before any stream capture.  All
+   calls share the array, so calls that overlap on the GPU race; serialise
+   them.  The call waits for its stream before returning. */
+#define G6_NOALLOC_MAX_MOL 4096
+int g6_force_noalloc(int model, int path, int precision, int n, const double* box, double r_in, double r_out,
+                     double skin, const double* d_com, const double* d_quat, double* d_F, double* d_tau,
+                     double* d_epot, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
