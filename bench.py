@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--no-32k", action="store_true")
     p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
     return p.parse_args()
 
 
@@ -210,34 +211,34 @@ def thermo_for(s, n=1):
 
 
 def timed_md(torch, s, steps, warmup, flush):
-    """Per-step CUDA-event timing of `steps` MD steps, L2 flushed between them."""
+    """`steps` MD steps, each a one-step CUDA graph that records events around
+    the whole step and around the fused force/integrator kernel, with a
+    256 MiB L2 flush on the same stream before every step."""
     L = s.L
     th = thermo_for(s)
+    lpi = ctypes.c_int()
+    s._check(L.g6_tune(s.ctx, ctypes.byref(lpi)))
     if warmup:
         s.md_run(DT, warmup, th, log=False)
     sp = ctypes.c_void_p()
     s._check(L.g6_stream(s.ctx, ctypes.byref(sp)))
     stream = torch.cuda.ExternalStream(sp.value)
-    s._check(L.g6_set_timing(s.ctx, steps))
     log = np.zeros((steps, 1, 10))
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    step_ms, kms = np.zeros(steps), np.zeros(steps)
+    a, b = ctypes.c_double(), ctypes.c_double()
+    s._check(L.g6_set_step_timing(s.ctx, 1))
     torch.cuda.synchronize()
     s._check(L.g6_md_begin(s.ctx, DT, steps, th, 1))
-    with torch.cuda.stream(stream):
-        flush.add_(1.0)
-        for k in range(steps):
-            ev[k][0].record(stream)
-            s._check(L.g6_md_advance(s.ctx, 1))
-            ev[k][1].record(stream)
+    for k in range(steps):
+        with torch.cuda.stream(stream):
             flush.add_(1.0)
+        s._check(L.g6_md_advance(s.ctx, 1))
+        s._check(L.g6_step_times(s.ctx, ctypes.byref(a), ctypes.byref(b)))
+        step_ms[k], kms[k] = a.value, b.value
     s._check(L.g6_md_end(s.ctx, th, log.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    s._check(L.g6_set_step_timing(s.ctx, 0))
     torch.cuda.synchronize()
-    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
-    kms = np.zeros(steps)
-    cnt = ctypes.c_int()
-    s._check(L.g6_get_timing(s.ctx, kms.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), steps, ctypes.byref(cnt)))
-    s._check(L.g6_set_timing(s.ctx, 0))
-    return step_ms, kms, log
+    return step_ms, kms, log, lpi.value
 
 
 def e2e_md(torch, s, rec, steps):
@@ -258,6 +259,156 @@ def e2e_md(torch, s, rec, steps):
     h2d = rec_b + 88 + 32                       # records, thermostat, control words
     d2h = rec_b + 32 + 4 + 88 + 24 * 8 + 80     # records, control, overflow flag, thermostat, sums, log
     return 1e3 * wall / steps, h2d, d2h
+
+
+def ess_geyer(x):
+    """Effective sample size by Geyer's initial positive sequence on autocovariances."""
+    x = np.asarray(x, float)
+    n = len(x)
+    if n < 4 or np.var(x) == 0:
+        return float(n)
+    xc = x - x.mean()
+    f = np.fft.rfft(xc, 2 * n)
+    acov = np.fft.irfft(f * np.conj(f))[:n] / n
+    rho = acov / acov[0]
+    s = 0.0
+    for k in range(0, n - 1, 2):
+        g = rho[k] + rho[k + 1]
+        if g <= 0:
+            break
+        s += g
+    tau = max(1.0, 2.0 * s - 1.0)
+    return n / tau
+
+
+def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
+    """64 TIP4P replicas (216-2,048 molecules, log-uniform), 220-360 K geometric,
+    stochastic-collision thermostat, rc 8.5 A, dt 2 fs, neighbour swaps every
+    500 steps: all replicas in one context (CUDA-graph steps) vs one context
+    per replica run one after the other.  Aggregate ns/day."""
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import config
+    R = 64
+    sizes = config.replica_sizes(R, 216, 2048, seed)
+    temps = 220.0 * (360.0 / 220.0) ** (np.arange(R) / (R - 1))
+    boxes, recs = [], []
+    for r in range(R):
+        b = config.water_box("TIP4P", int(sizes[r]), seed + 100 + r, temp=float(temps[r]), dt=DT)
+        boxes.append(b["L"]); recs.append(b["rec"])
+    rate = 1.0   # collisions per molecule per ps
+
+    def thermo(s, tr):
+        th = s.thermostats(len(tr), "andersen", temp=tr, rate=rate, seed=seed)
+        return th
+    # batched
+    s = g6.RigidWater("TIP4P", sizes, np.array(boxes), path="custom", precision="mixed", rc=8.5)
+    s.upload_state(np.concatenate(recs))
+    th = thermo(s, temps)
+    s.md_run(DT, 50, th, log=False)   # warm-up (graph capture, list build)
+    beta = 1.0 / np.array([th[r].temp for r in range(R)])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    acc = np.zeros(R)
+    done = 0
+    swap = 0
+    while done < steps:
+        k = min(500, steps - done)
+        s.md_run(DT, k, th, log=False)
+        done += k
+        if done % 500 == 0:
+            beta, a = s.replica_exchange(swap & 1, seed, swap, beta, th)
+            acc += a
+            swap += 1
+    torch.cuda.synchronize()
+    t_batched = time.perf_counter() - t0
+    agg_batched = R * steps * DT * 1e-3 * 86400.0 / t_batched
+    s.close()
+    # one replica after another
+    ctxs = []
+    for r in range(R):
+        c = g6.RigidWater("TIP4P", int(sizes[r]), boxes[r], path="custom", precision="mixed", rc=8.5)
+        c.upload_state(recs[r])
+        tc = thermo(c, [temps[r]])
+        c.md_run(DT, 20, tc, log=False)
+        ctxs.append((c, tc))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c, tc in ctxs:
+        c.md_run(DT, loop_steps, tc, log=False)
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    agg_loop = R * loop_steps * DT * 1e-3 * 86400.0 / t_loop
+    for c, _ in ctxs:
+        c.close()
+    return {"replicas": R, "molecules": int(sizes.sum()), "min_size": int(sizes.min()), "max_size": int(sizes.max()),
+            "batched_ns_per_day_aggregate": agg_batched, "loop_ns_per_day_aggregate": agg_loop,
+            "batched_over_loop": agg_batched / agg_loop, "batched_steps": steps, "loop_steps": loop_steps,
+            "swap_attempts": int(swap), "accepted_swaps": int(acc.sum()),
+            "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed"}
+
+
+def bench_mc(torch, seed=20261203, sweeps=120, records=1_000_000):
+    """32 chains x 1,024 ST2 (custom path, Coulomb taper), 260 K, rc = L/2 with a
+    2 A switch: fixed widths (0.15 A, 0.15 rad) vs widths from the MLP trained on
+    `records` plain-sampler moves.  ESS of U per GPU-second (U sampled every
+    sweep of 1,024 trials) and <U> of both."""
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import _capi, config
+    C, N = 32, 1024
+    boxes, recs = [], []
+    for c in range(C):
+        b = config.water_box("ST2", N, seed + 500 + c, temp=260.0)
+        boxes.append(b["L"]); recs.append(b["rec"])
+    L = boxes[0][0]
+    s = g6.RigidWater("ST2", [N] * C, np.array(boxes), path="custom", precision="mixed", rc=0.5 * L, skin=0.0)
+    s.upload_state(np.concatenate(recs))
+    beta = np.full(C, 1.0 / 260.0)
+    st = np.full(C, 0.15); sr = np.full(C, 0.15)
+    counts = np.zeros(2 * C, np.int64)
+    energy = np.zeros(C)
+
+    def run(ntrial, mode, counter, sample_every=0):
+        nsm = ntrial // sample_every if sample_every else 0
+        samples = np.zeros((C, max(nsm, 1)))
+        s._check(s.L.g6_mc_run(s.ctx, ntrial, seed, counter, _capi.dptr(beta), _capi.dptr(st), _capi.dptr(sr),
+                               mode, sample_every, _capi.dptr(samples) if nsm else None,
+                               counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _capi.dptr(energy), None))
+        return samples, counts.reshape(C, 2).copy()
+    run(30 * N, _capi.MC_PLAIN, 0)                                   # equilibration
+    rec_state = s.download_state()
+    ntr = records // C
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run(ntr, _capi.MC_COLLECT, 10 ** 7)                              # training records
+    loss = np.zeros(8)
+    s._check(s.L.g6_mlp_train(s.ctx, 8, 1024, 2e-3, seed, 0.15, 0.15, _capi.dptr(loss)))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    out = {}
+    for name, mode in (("fixed", _capi.MC_PLAIN), ("learned", _capi.MC_LEARNED)):
+        s.upload_state(rec_state)
+        run(2 * N, mode, 2 * 10 ** 7)                                # settle the sampler
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        samples, cnt = run(sweeps * N, mode, 3 * 10 ** 7, sample_every=N)
+        torch.cuda.synchronize()
+        gpu_s = time.perf_counter() - t0
+        ess = np.array([ess_geyer(samples[c]) for c in range(C)])
+        u = samples.mean(1)
+        var_mean = np.array([np.var(samples[c]) / max(ess[c], 1.0) for c in range(C)])
+        out[name] = {"ess_total": float(ess.sum()), "gpu_seconds": gpu_s, "ess_per_gpu_s": float(ess.sum() / gpu_s),
+                     "mean_U_internal": float(u.mean()), "stderr_U": float(np.sqrt(var_mean.sum()) / C),
+                     "acceptance": float(cnt[:, 0].sum() / cnt[:, 1].sum()), "sweeps": sweeps}
+    s.close()
+    d = abs(out["learned"]["mean_U_internal"] - out["fixed"]["mean_U_internal"])
+    sig = np.hypot(out["learned"]["stderr_U"], out["fixed"]["stderr_U"])
+    return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": 260.0,
+            "rc_A": 0.5 * L, "training_records": ntr * C, "training_loss_first_last": [float(loss[0]),
+                                                                                     float(loss[-1])],
+            "collect_and_train_seconds": t_train, "fixed": out["fixed"], "learned": out["learned"],
+            "ess_per_gpu_s_learned_over_fixed": out["learned"]["ess_per_gpu_s"] / out["fixed"]["ess_per_gpu_s"],
+            "mean_U_difference_in_sigma": float(d / sig) if sig > 0 else None,
+            "U_unit": "10 J/mol per chain (internal)"}
 
 
 def run_gpu(args, rank, world, local):
@@ -288,7 +439,7 @@ def run_gpu(args, rank, world, local):
     s.upload_state(rec_eq)
     barrier()
     with Clocks(local) as clk:
-        step_ms, kms, log = timed_md(torch, s, args.steps, args.warmup, flush)
+        step_ms, kms, log, lpi = timed_md(torch, s, args.steps, args.warmup, flush)
         barrier()
     total_ms = float(step_ms.sum())
     if dist:
@@ -301,7 +452,7 @@ def run_gpu(args, rank, world, local):
     # plain FP64 mode, same state
     s64 = make_system("TIP4P", N_MAIN, "fp64", L, rec_eq)
     k64 = max(5, min(args.steps, 60))
-    step64, kms64, log64 = timed_md(torch, s64, k64, min(args.warmup, 5), flush)
+    step64, kms64, log64, _ = timed_md(torch, s64, k64, min(args.warmup, 5), flush)
     ms64 = float(step64.mean())
 
     # e2e through the host-buffer entry point
@@ -316,9 +467,9 @@ def run_gpu(args, rank, world, local):
         sb.md_run(DT, 200, thermo_for(sb), log=False)
         rb = sb.download_state()
         kb = max(5, min(args.steps, 100))
-        stb, kmb, logb = timed_md(torch, sb, kb, min(args.warmup, 5), flush)
+        stb, kmb, logb, lpib = timed_md(torch, sb, kb, min(args.warmup, 5), flush)
         s64b = make_system("TIP4P", N_BIG, "fp64", bb["L"], rb)
-        stb64, _, _ = timed_md(torch, s64b, 5, 2, flush)
+        stb64, _, _, _ = timed_md(torch, s64b, 5, 2, flush)
         pb = float(logb[:, 0, 6].mean())
         big = {"mixed_ns_per_day": ns_per_day(float(stb.mean())), "fp64_ns_per_day": ns_per_day(float(stb64.mean())),
                "mixed_ms_per_step": float(stb.mean()), "fp64_ms_per_step": float(stb64.mean()),
@@ -341,12 +492,14 @@ def run_gpu(args, rank, world, local):
     kmean = float(kms.mean())
     achieved = FLOPS_PER_PAIR["TIP4P"] * pairs / (kmean * 1e-3) / 1e12
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "force_tip4p4096_mixed.txt")
+    tpath = os.path.join(ROOT, "profiles", "step_tip4p4096_mixed.txt")
     if os.path.exists(tpath):
         for l in open(tpath):
             if l.startswith("traffic_bytes_per_launch:"):
                 traffic = float(l.split(":")[1])
     cpu = None if args.no_cpu else cpu_md_rate(budget_s=12.0)
+    rex = None if args.no_extra else bench_replicas(torch)
+    mcb = None if args.no_extra else bench_mc(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -354,17 +507,20 @@ def run_gpu(args, rank, world, local):
         "Maxwell-Boltzmann 300 K, 2,000-step pre-equilibration)", "config": config_block(args, world),
         "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
         "tip4p_32k": big,
+        "replica_exchange": rex,
+        "mc_learned_vs_fixed": mcb,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "kernel": "k_force<TIP4P, mixed>", "flops_per_pair": FLOPS_PER_PAIR["TIP4P"],
-                     "pairs_per_launch": pairs, "kernel_ms": kmean,
+                     "kernel": "k_force<TIP4P, mixed, fused step> (site loop + Gear corrector epilogue)",
+                     "flops_per_pair": FLOPS_PER_PAIR["TIP4P"],
+                     "pairs_per_launch": pairs, "kernel_ms": kmean, "lanes_per_molecule": lpi,
                      "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run (FP32 CUDA-core "
                                     "pipe; the kernel uses no tensor cores and moves a few MB per launch)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": world * ns_per_day(e2e_ms), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "entry": "g6_md_step_host"},
-        "gpu_launches": 8 * args.steps,
+        "gpu_launches": 2 * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

@@ -22,6 +22,8 @@ PATHS = {"std": PATH_STD, "custom": PATH_CUSTOM}
 FP64, MIXED = 0, 1
 PRECISIONS = {"fp64": FP64, "mixed": MIXED}
 NVE, NOSE, ANDERSEN = 0, 1, 2
+MC_PLAIN, MC_LEARNED, MC_COLLECT = 0, 1, 2
+MLP_NPARAM, MLP_NFEAT, MLP_RECORD = 5890, 24, 51
 LOG_WIDTH = 10
 REC = 53
 
@@ -32,7 +34,8 @@ SYMBOLS = [
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
     "g6_molecule_energies", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
-    "g6_set_timing", "g6_get_timing", "g6_force_noalloc",
+    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get",
+    "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
 ]
 
 
@@ -96,8 +99,20 @@ def lib():
     L.g6_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.g6_force_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_double, vp, vp, vp, vp, vp, vp]
-    L.g6_set_timing.argtypes = [vp, ctypes.c_int]
-    L.g6_get_timing.argtypes = [vp, dp, ctypes.c_int, ip]
+    L.g6_mc_run.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp, ctypes.c_int,
+                            ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int64), dp, dp]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.g6_mlp_set.argtypes = [vp, fp, fp, fp, ctypes.c_double, ctypes.c_double]
+    L.g6_mlp_get.argtypes = [vp, fp, fp, fp]
+    L.g6_mlp_records.argtypes = [vp, fp, i64, ctypes.POINTER(i64)]
+    L.g6_mlp_grad.argtypes = [vp, fp, i64, fp, dp]
+    L.g6_mlp_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_double,
+                               ctypes.c_double, dp]
+    L.g6_time_force.argtypes = [vp, dp]
+    L.g6_set_step_timing.argtypes = [vp, ctypes.c_int]
+    L.g6_step_times.argtypes = [vp, dp, dp]
+    L.g6_tune.argtypes = [vp, ip]
+    L.g6_set_lpi.argtypes = [vp, ctypes.c_int]
     for name in SYMBOLS:
         if name not in ("g6_last_error", "g6_status_string"):
             getattr(L, name).restype = ctypes.c_int
@@ -111,6 +126,13 @@ def dptr(a):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def iptr(a):

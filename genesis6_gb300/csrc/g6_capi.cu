@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "g6_internal.cuh"
+#include "g6_mlp.cuh"
 
 namespace g6 {
 
@@ -183,11 +184,13 @@ struct g6_ctx {
   std::vector<int> off;
   std::vector<double> L;
   int lpi = 0;                    // lanes per molecule in the force kernel (0 = tune)
+  int coop_grid = 0;              // blocks of the cooperative rebuild kernel
   // device arrays
   int* d_off = nullptr; int* d_mol_rep = nullptr; double* d_L = nullptr; double* d_invL = nullptr;
   float* d_fscale = nullptr;
   double* d_st = nullptr; double* d_tmat = nullptr; double* d_pk64 = nullptr; float4* d_pk32 = nullptr;
   uint32_t* d_fix = nullptr;
+  double* d_tmat1 = nullptr; double* d_pk64_1 = nullptr; float4* d_pk32_1 = nullptr; uint32_t* d_fix1 = nullptr;
   double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
   int* d_npin = nullptr;
   double* d_stage = nullptr;      // AoS staging (53 n)
@@ -204,6 +207,17 @@ struct g6_ctx {
   unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
   ThermoDev* d_th = nullptr; double* d_scale = nullptr; double* d_beta = nullptr; int* d_acc = nullptr;
   double* d_epot_rep = nullptr;
+  // Monte Carlo and the proposal-width MLP
+  double *d_sig_t = nullptr, *d_sig_r = nullptr, *d_energy = nullptr;
+  long long* d_counts = nullptr;
+  double* d_samples = nullptr; size_t samples_cap = 0;
+  double* d_trace = nullptr; size_t trace_cap = 0;
+  float* d_rec = nullptr; size_t rec_cap = 0; long long nrec = 0;   // training records
+  float* d_mlp = nullptr;          // parameters
+  float* d_mlp_zero = nullptr;     // constant-width network (plain proposal with records)
+  float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
+  double sig0_t = 0.15, sig0_r = 0.15;
+  bool have_mlp = false;
   // pair set
   long long* d_pcnt = nullptr;
   long long npairs = -1;
@@ -228,9 +242,9 @@ struct g6_ctx {
   bool in_run = false, run_log = false;
   double run_dt = 0.0;
   int run_max = 0, run_done = 0;
-  // optional per-step CUDA events around the force kernel
-  std::vector<cudaEvent_t> tev;
-  int tcap = 0, tnext = 0;
+  cudaGraphExec_t graph1 = nullptr;   // one step, for step-by-step advancing
+  bool step_timing = false;           // graph1 carries events around the step and the kernel
+  cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 static int fail(g6_ctx* c, int code, const std::string& msg) {
@@ -256,19 +270,24 @@ static cudaError_t dalloc(g6_ctx* c, T** p, size_t count) {
   return cudaMemset(q, 0, std::max<size_t>(count, 1) * sizeof(T));
 }
 
-static void free_timing(g6_ctx* c) {
-  for (cudaEvent_t e : c->tev) cudaEventDestroy(e);
-  c->tev.clear();
-  c->tcap = 0; c->tnext = 0;
+static void drop_graphs(g6_ctx* c) {
+  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  if (c->graph1) { cudaGraphExecDestroy(c->graph1); c->graph1 = nullptr; }
 }
 
 static void free_all(g6_ctx* c) {
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-  free_timing(c);
+  drop_graphs(c);
+  for (int k = 0; k < 4; ++k)
+    if (c->sev[k]) { cudaEventDestroy(c->sev[k]); c->sev[k] = nullptr; }
+  c->step_timing = false;
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
   if (c->d_scratch) { cudaFree(c->d_scratch); c->d_scratch = nullptr; c->scratch_bytes = 0; }
   if (c->d_log) { cudaFree(c->d_log); c->d_log = nullptr; c->log_cap = 0; }
+  if (c->d_samples) { cudaFree(c->d_samples); c->d_samples = nullptr; c->samples_cap = 0; }
+  if (c->d_trace) { cudaFree(c->d_trace); c->d_trace = nullptr; c->trace_cap = 0; }
+  if (c->d_rec) { cudaFree(c->d_rec); c->d_rec = nullptr; c->rec_cap = 0; c->nrec = 0; }
+  c->have_mlp = false;
   if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
   c->gref = HostGrid(); c->glist = HostGrid();
   c->pair_capacity = 0; c->npairs = -1; c->cap = 0;
@@ -401,7 +420,7 @@ static CellArgs cell_args(g6_ctx* c, HostGrid& g, const int* ctrl) {
 static ListArgs list_args(g6_ctx* c, const int* ctrl) {
   ListArgs a;
   a.n = c->n; a.cap = c->cap; a.rep = rep_dev(c); a.g = grid_dev(c->glist); a.cell = c->glist.d_cell;
-  a.start = c->glist.d_start; a.cellmol = c->glist.d_cellmol; a.fix = c->d_fix; a.com = c->d_st;
+  a.start = c->glist.d_start; a.cellmol = c->glist.d_cellmol; a.fix = c->d_fix; a.fix1 = c->d_fix1; a.com = c->d_st;
   a.com_build = c->d_com_build;
   const double rl = c->cc.rout + effective_skin(c);
   a.rlist2 = (float)(rl * rl) + 1e-3f;   // superset margin over the fixed-point rounding
@@ -412,7 +431,8 @@ static ListArgs list_args(g6_ctx* c, const int* ctrl) {
 static ForceArgs force_args(g6_ctx* c) {
   ForceArgs a;
   a.n = c->n; a.cap = c->cap; a.stride_pk32 = c->npk; a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.rep = rep_dev(c);
-  a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
+  a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pk64_1 = c->d_pk64_1; a.pk32_1 = c->d_pk32_1; a.ctrl = nullptr;
+  a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
   a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin;
   return a;
 }
@@ -425,11 +445,12 @@ static int default_lpi(const g6_ctx* c) {
   return l;
 }
 
-// Enqueue the neighbour-list rebuild (conditional on ctrl[0] when ctrl != NULL).
+// Enqueue the neighbour-list rebuild (conditional on ctrl[0] when ctrl != NULL):
+// one cooperative launch that exits at once when no rebuild is due.
 static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl) {
+  if (ctx->coop_grid == 0) ctx->coop_grid = rebuild_grid_limit();
   CellArgs ca = cell_args(ctx, ctx->glist, ctrl);
-  CK(launch_cells(ca, ctx->glist.d_start, ctx->glist.d_cellmol, ctx->stream));
-  CK(launch_list(list_args(ctx, ctrl), ctx->stream));
+  CK(launch_rebuild(ca, list_args(ctx, ctrl), ctx->glist.d_start, ctx->glist.d_cellmol, ctx->coop_grid, ctx->stream));
   return G6_OK;
 }
 
@@ -445,6 +466,7 @@ static int force_once(g6_ctx* ctx) {
   int ovf = 0;
   CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
   if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow");
   return G6_OK;
 }
@@ -555,17 +577,28 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_st, (size_t)REC * n)); CK(dalloc(ctx, &ctx->d_tmat, 9 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_pk64, (size_t)ctx->w64 * n)); CK(dalloc(ctx, &ctx->d_pk32, (size_t)ctx->npk * n));
   CK(dalloc(ctx, &ctx->d_fix, 3 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_tmat1, 9 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_pk64_1, (size_t)ctx->w64 * n)); CK(dalloc(ctx, &ctx->d_pk32_1, (size_t)ctx->npk * n));
+  CK(dalloc(ctx, &ctx->d_fix1, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_overflow, 1));
-  ctx->nblk = (n + RED_BLOCK - 1) / RED_BLOCK;
+  ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // blocks of the fused step kernel at 32 lanes/molecule
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
   CK(dalloc(ctx, &ctx->d_partmax, ctx->nblk)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
   CK(dalloc(ctx, &ctx->d_done, 1)); CK(dalloc(ctx, &ctx->d_ctrl, 8));
   CK(dalloc(ctx, &ctx->d_th, nrep)); CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
   CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
   CK(dalloc(ctx, &ctx->d_pcnt, 2 * (size_t)n + 2));
+  CK(dalloc(ctx, &ctx->d_sig_t, nrep)); CK(dalloc(ctx, &ctx->d_sig_r, nrep)); CK(dalloc(ctx, &ctx->d_energy, nrep));
+  CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
+  CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_mlp_zero, MLP_NPARAM));
+  {
+    std::vector<float> z(MLP_NPARAM, 0.0f);
+    z[MLP_B3] = z[MLP_B3 + 1] = (float)std::log(0.25 / 0.75);   // sigma = sigma0 (0.5 + 2 * 0.25)
+    CK(cudaMemcpy(ctx->d_mlp_zero, z.data(), z.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   ctx->last_epot.assign(nrep, 0.0);
   ctx->have_system = true;
   return G6_OK;
@@ -577,7 +610,7 @@ int g6_set_cutoff(g6_ctx* ctx, double r_in, double r_out) {
   make_cut_const(r_in, r_out, ctx->cc);
   ctx->have_cut = true;
   ctx->gref.valid = false; ctx->glist.valid = false; ctx->cap = 0;
-  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  drop_graphs(ctx);
   return G6_OK;
 }
 
@@ -594,7 +627,7 @@ int g6_set_skin(g6_ctx* ctx, double skin) {
   if (!(skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
   ctx->skin = skin;
   ctx->glist.valid = false; ctx->cap = 0;
-  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  drop_graphs(ctx);
   return G6_OK;
 }
 
@@ -613,7 +646,7 @@ int g6_set_box(g6_ctx* ctx, int replica, const double* L3) {
   CK(cudaMemcpy(ctx->d_invL, invL.data(), 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_fscale, fs.data(), 3 * ctx->nrep * sizeof(float), cudaMemcpyHostToDevice));
   ctx->gref.valid = false; ctx->glist.valid = false; ctx->cap = 0;
-  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  drop_graphs(ctx);
   return G6_OK;
 }
 
@@ -861,8 +894,8 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   StepArgs a;
   std::memset(&a, 0, sizeof a);
   a.p = place_args(ctx);
+  a.tmat1 = ctx->d_tmat1; a.pk64_1 = ctx->d_pk64_1; a.pk32_1 = ctx->d_pk32_1; a.fix1 = ctx->d_fix1;
   a.mass = ctx->mh.mass; a.I[0] = ctx->mh.I[0]; a.I[1] = ctx->mh.I[1]; a.I[2] = ctx->mh.I[2]; a.dt = dt;
-  a.F = ctx->d_F; a.tl = ctx->d_tl; a.emol = ctx->d_emol; a.wmol = ctx->d_wmol; a.npin = ctx->d_npin;
   a.com_build = ctx->d_com_build;
   const double hs = 0.5 * effective_skin(ctx);
   a.half_skin2 = hs * hs;
@@ -871,14 +904,21 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   return a;
 }
 
-static int enqueue_step(g6_ctx* ctx, const StepArgs& sa) {
+// One MD step = the (conditional) neighbour-list rebuild + the fused force /
+// integrator kernel.  ev (optional, 4 events) brackets the step and the kernel.
+static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullptr) {
+  // external records become event nodes of a captured graph (queryable after launch)
+  if (ev) CK(cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal));
   int rc = enqueue_rebuild(ctx, ctx->d_ctrl);
   if (rc) return rc;
-  const bool timed = ctx->tcap > 0 && ctx->tnext < ctx->tcap;
-  if (timed) CK(cudaEventRecord(ctx->tev[2 * ctx->tnext], ctx->stream));
-  CK(launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
-  if (timed) { CK(cudaEventRecord(ctx->tev[2 * ctx->tnext + 1], ctx->stream)); ++ctx->tnext; }
-  CK(launch_correct_step(sa, ctx->stream));
+  ForceArgs fa = force_args(ctx);
+  fa.ctrl = ctx->d_ctrl;
+  if (ev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
+  CK(launch_step(fa, sa, ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
+  if (ev) {
+    CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
+    CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
+  }
   return G6_OK;
 }
 
@@ -910,7 +950,7 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
     if (ctx->d_log) { cudaFree(ctx->d_log); ctx->d_log = nullptr; ctx->log_cap = 0; }
     CK(cudaMalloc(&ctx->d_log, need_log * sizeof(double)));
     ctx->log_cap = need_log;
-    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    drop_graphs(ctx);
   }
   int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
   CK(cudaMemcpyAsync(ctx->d_ctrl, ctrl, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
@@ -919,7 +959,7 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
   (void)dt;
   if (thermo && thermo[0].seed != ctx->seed) {
     ctx->seed = thermo[0].seed;
-    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    drop_graphs(ctx);
   }
   (void)seed;
   return G6_OK;
@@ -945,6 +985,7 @@ static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log
       thermo[r].zetasum = th[r].zsum;
     }
   }
+  if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
   if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow (raise the skin or density)");
   if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");
   if (ctrl[1] != nsteps) return fail(ctx, G6_ERR_STATE, "step counter mismatch");
@@ -952,33 +993,33 @@ static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log
   return G6_OK;
 }
 
+static int capture_steps(g6_ctx* ctx, const StepArgs& sa, int k, cudaGraphExec_t* out) {
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (int q = 0; q < k; ++q) {
+    int rc = enqueue_step(ctx, sa, (k == 1 && ctx->step_timing) ? ctx->sev : nullptr);
+    if (rc) { cudaStreamEndCapture(ctx->stream, &g); return rc; }
+  }
+  CK(cudaStreamEndCapture(ctx->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphInstantiate");
+  return G6_OK;
+}
+
+// Steps run as graph launches: blocks of GRAPH_STEPS, then single steps.
 static int md_enqueue_steps(g6_ctx* ctx, int nsteps) {
   StepArgs sa = step_args(ctx, ctx->run_dt, ctx->run_log ? ctx->d_log : nullptr);
-  // with per-step kernel timing the steps are launched directly (events per step)
-  const int full = ctx->tcap > 0 ? 0 : nsteps / GRAPH_STEPS;
+  const int want_log = ctx->run_log ? 1 : 0;
+  if (ctx->graph_dt != ctx->run_dt || ctx->graph_log != want_log) drop_graphs(ctx);
+  ctx->graph_dt = ctx->run_dt; ctx->graph_log = want_log;
+  const int full = ctx->step_timing ? 0 : nsteps / GRAPH_STEPS;
   const int rest = nsteps - full * GRAPH_STEPS;
   int rc;
-  if (full > 0) {
-    const int want_log = ctx->run_log ? 1 : 0;
-    if (!ctx->graph || ctx->graph_dt != ctx->run_dt || ctx->graph_log != want_log) {
-      if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
-      cudaGraph_t g;
-      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < GRAPH_STEPS; ++k) {
-        rc = enqueue_step(ctx, sa);
-        if (rc) { cudaStreamEndCapture(ctx->stream, &g); return rc; }
-      }
-      CK(cudaStreamEndCapture(ctx->stream, &g));
-      CK(cudaGraphInstantiate(&ctx->graph, g, 0));
-      cudaGraphDestroy(g);
-      ctx->graph_dt = ctx->run_dt; ctx->graph_log = want_log;
-    }
-    for (int k = 0; k < full; ++k) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-  }
-  for (int k = 0; k < rest; ++k) {
-    rc = enqueue_step(ctx, sa);
-    if (rc) return rc;
-  }
+  if (full > 0 && !ctx->graph) { rc = capture_steps(ctx, sa, GRAPH_STEPS, &ctx->graph); if (rc) return rc; }
+  if (rest > 0 && !ctx->graph1) { rc = capture_steps(ctx, sa, 1, &ctx->graph1); if (rc) return rc; }
+  for (int k = 0; k < full; ++k) CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+  for (int k = 0; k < rest; ++k) CK(cudaGraphLaunch(ctx->graph1, ctx->stream));
   return G6_OK;
 }
 
@@ -1016,32 +1057,79 @@ int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log) {
   return G6_OK;
 }
 
-int g6_set_timing(g6_ctx* ctx, int max_steps) {
-  if (!ctx || max_steps < 0) return G6_ERR_ARG;
+int g6_set_step_timing(g6_ctx* ctx, int on) {
+  if (!ctx) return G6_ERR_ARG;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
-  free_timing(ctx);
-  for (int k = 0; k < 2 * max_steps; ++k) {
-    cudaEvent_t e;
-    CK(cudaEventCreate(&e));
-    ctx->tev.push_back(e);
-  }
-  ctx->tcap = max_steps;
-  ctx->tnext = 0;
+  for (int k = 0; k < 4; ++k)
+    if (!ctx->sev[k]) CK(cudaEventCreate(&ctx->sev[k]));
+  ctx->step_timing = on != 0;
+  drop_graphs(ctx);
   return G6_OK;
 }
 
-int g6_get_timing(g6_ctx* ctx, double* ms, int cap, int* count) {
-  if (!ctx || (cap > 0 && !ms)) return G6_ERR_ARG;
+int g6_step_times(g6_ctx* ctx, double* step_ms, double* kernel_ms) {
+  if (!ctx || !ctx->step_timing) return fail(ctx, G6_ERR_STATE, "step timing is off (g6_set_step_timing)");
   CK(cudaSetDevice(ctx->device));
-  CK(cudaStreamSynchronize(ctx->stream));
-  const int m = std::min(cap, ctx->tnext);
-  for (int k = 0; k < m; ++k) {
-    float t = 0.0f;
-    CK(cudaEventElapsedTime(&t, ctx->tev[2 * k], ctx->tev[2 * k + 1]));
-    ms[k] = t;
+  CK(cudaEventSynchronize(ctx->sev[3]));
+  float a = 0.0f, b = 0.0f;
+  CK(cudaEventElapsedTime(&a, ctx->sev[0], ctx->sev[3]));
+  CK(cudaEventElapsedTime(&b, ctx->sev[1], ctx->sev[2]));
+  if (step_ms) *step_ms = a;
+  if (kernel_ms) *kernel_ms = b;
+  return G6_OK;
+}
+
+int g6_time_force(g6_ctx* ctx, double* ms) {
+  if (!ctx || !ms) return G6_ERR_ARG;
+  if (!ctx->have_system || ctx->cap == 0 || ctx->lpi == 0) return fail(ctx, G6_ERR_STATE, "no neighbour list yet");
+  CK(cudaSetDevice(ctx->device));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  cudaError_t e = cudaEventRecord(e0, ctx->stream);
+  if (e == cudaSuccess) e = launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float t = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "g6_time_force");
+  *ms = t;
+  return G6_OK;
+}
+
+// Lanes per molecule of the force kernel: time each candidate on the current
+// configuration (3 launches each, best of) and keep the fastest.
+int g6_tune(g6_ctx* ctx, int* lpi_out) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
+  rc = force_once(ctx);
+  if (rc) return rc;
+  const int cand[4] = {4, 8, 16, 32};
+  int best = ctx->lpi;
+  double tbest = 1e30;
+  for (int k = 0; k < 4; ++k) {
+    ctx->lpi = cand[k];
+    double t = 1e30, m = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+      rc = g6_time_force(ctx, &m);
+      if (rc) return rc;
+      t = std::min(t, m);
+    }
+    if (t < tbest) { tbest = t; best = cand[k]; }
   }
-  if (count) *count = ctx->tnext;
+  ctx->lpi = best;
+  drop_graphs(ctx);
+  if (lpi_out) *lpi_out = best;
+  return G6_OK;
+}
+
+int g6_set_lpi(g6_ctx* ctx, int lpi) {
+  if (!ctx || (lpi != 4 && lpi != 8 && lpi != 16 && lpi != 32)) return G6_ERR_ARG;
+  ctx->lpi = lpi;
+  drop_graphs(ctx);
   return G6_OK;
 }
 
@@ -1111,6 +1199,243 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
     thermo[r].temp = th[r].temp;
     for (int k = 0; k < 5; ++k) thermo[r].zeta[k] = th[r].z[k];
     if (accepted) accepted[r] = acc[r];
+  }
+  return G6_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Monte Carlo and the learned proposal widths
+// ---------------------------------------------------------------------------
+static int grow(g6_ctx* ctx, void** p, size_t* cap, size_t need_bytes, bool keep) {
+  if (need_bytes <= *cap) return G6_OK;
+  void* q = nullptr;
+  CK(cudaMalloc(&q, need_bytes));
+  if (keep && *p && *cap) CK(cudaMemcpy(q, *p, *cap, cudaMemcpyDeviceToDevice));
+  if (*p) cudaFree(*p);
+  *p = q;
+  *cap = need_bytes;
+  return G6_OK;
+}
+
+static MlpDev mlp_dev(g6_ctx* ctx, bool zero) {
+  MlpDev m;
+  m.w = zero ? ctx->d_mlp_zero : ctx->d_mlp;
+  for (int k = 0; k < MLP_IN; ++k) { m.feat_mean[k] = zero ? 0.0f : ctx->h_mean[k]; m.feat_inv_std[k] = zero ? 1.0f : ctx->h_istd[k]; }
+  m.sigma0_t = ctx->sig0_t; m.sigma0_r = ctx->sig0_r;
+  return m;
+}
+
+extern "C" {
+
+int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const double* beta, const double* sigma_t,
+              const double* sigma_r, int mode, int sample_every, double* samples, int64_t* counts, double* energy,
+              double* trace) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (ntrial < 0 || !beta || (mode != G6_MC_LEARNED && (!sigma_t || !sigma_r)))
+    return fail(ctx, G6_ERR_ARG, "ntrial >= 0, beta and widths are required");
+  if (mode < G6_MC_PLAIN || mode > G6_MC_COLLECT) return fail(ctx, G6_ERR_ARG, "unknown Monte Carlo mode");
+  if (mode == G6_MC_LEARNED && !ctx->have_mlp) return fail(ctx, G6_ERR_STATE, "no trained network (g6_mlp_set / g6_mlp_train)");
+  if (sample_every < 0) return fail(ctx, G6_ERR_ARG, "sample_every must be >= 0");
+  const int R = ctx->nrep;
+  // current energies of every chain from a full force evaluation (also places the poses)
+  rc = force_once(ctx);
+  if (rc) return rc;
+  std::vector<double> e(ctx->n), etot(R, 0.0);
+  CK(cudaMemcpy(e.data(), ctx->d_emol, ctx->n * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int r = 0; r < R; ++r)
+    for (int i = ctx->off[r]; i < ctx->off[r + 1]; ++i) etot[r] += e[i];
+  std::vector<double> st(R, ctx->sig0_t), sr(R, ctx->sig0_r);
+  if (sigma_t) st.assign(sigma_t, sigma_t + R);
+  if (sigma_r) sr.assign(sigma_r, sigma_r + R);
+  CK(cudaMemcpy(ctx->d_beta, beta, R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_sig_t, st.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_sig_r, sr.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_energy, etot.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(ctx->d_counts, 0, 2 * R * sizeof(long long)));
+  const int nsamples = sample_every > 0 ? ntrial / sample_every : 0;
+  if (samples && nsamples > 0)
+    if ((rc = grow(ctx, (void**)&ctx->d_samples, &ctx->samples_cap, (size_t)R * nsamples * sizeof(double), false))) return rc;
+  if (trace && ntrial > 0)
+    if ((rc = grow(ctx, (void**)&ctx->d_trace, &ctx->trace_cap, (size_t)R * ntrial * 4 * sizeof(double), false))) return rc;
+  float* rec_out = nullptr;
+  if (mode == G6_MC_COLLECT && ntrial > 0) {
+    const size_t need = (size_t)(ctx->nrec + (long long)R * ntrial) * MLP_REC * sizeof(float);
+    if ((rc = grow(ctx, (void**)&ctx->d_rec, &ctx->rec_cap, need, true))) return rc;
+    rec_out = ctx->d_rec + (size_t)ctx->nrec * MLP_REC;
+  }
+  McArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.n = ctx->n; a.ntrial = ntrial; a.nsamples = nsamples; a.sample_every = samples ? sample_every : 0;
+  a.rep = rep_dev(ctx);
+  for (int q = 0; q < MAXSITE; ++q)
+    for (int k = 0; k < 3; ++k) a.body[q][k] = ctx->mh.body[q][k];
+  a.st = ctx->d_st; a.pk64 = ctx->d_pk64; a.pk32f = (float*)ctx->d_pk32; a.fix = ctx->d_fix;
+  a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
+  a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
+  a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
+  a.mlp = mlp_dev(ctx, mode == G6_MC_COLLECT);
+  if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode != G6_MC_PLAIN, ctx->stream));
+  std::vector<long long> cnt(2 * R);
+  CK(cudaMemcpyAsync(etot.data(), ctx->d_energy, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cnt.data(), ctx->d_counts, 2 * R * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+  if (a.samples) CK(cudaMemcpyAsync(samples, ctx->d_samples, (size_t)R * nsamples * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (a.trace) CK(cudaMemcpyAsync(trace, ctx->d_trace, (size_t)R * ntrial * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (mode == G6_MC_COLLECT) ctx->nrec += (long long)R * ntrial;
+  if (energy) for (int r = 0; r < R; ++r) energy[r] = etot[r];
+  if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
+  drop_graphs(ctx);   // poses changed outside the MD state machine
+  return G6_OK;
+}
+
+int g6_mlp_set(g6_ctx* ctx, const float* params, const float* feat_mean, const float* feat_inv_std, double sigma0_t,
+               double sigma0_r) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (!params || !feat_mean || !feat_inv_std || !(sigma0_t > 0.0) || !(sigma0_r > 0.0))
+    return fail(ctx, G6_ERR_ARG, "parameters, normalisation and positive widths are required");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(ctx->d_mlp, params, MLP_NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  std::memcpy(ctx->h_mean, feat_mean, sizeof ctx->h_mean);
+  std::memcpy(ctx->h_istd, feat_inv_std, sizeof ctx->h_istd);
+  ctx->sig0_t = sigma0_t; ctx->sig0_r = sigma0_r;
+  ctx->have_mlp = true;
+  return G6_OK;
+}
+
+int g6_mlp_get(g6_ctx* ctx, float* params, float* feat_mean, float* feat_inv_std) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  CK(cudaSetDevice(ctx->device));
+  if (params) CK(cudaMemcpy(params, ctx->d_mlp, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
+  if (feat_mean) std::memcpy(feat_mean, ctx->h_mean, sizeof ctx->h_mean);
+  if (feat_inv_std) std::memcpy(feat_inv_std, ctx->h_istd, sizeof ctx->h_istd);
+  return G6_OK;
+}
+
+int g6_mlp_records(g6_ctx* ctx, float* host, int64_t cap, int64_t* count) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  CK(cudaSetDevice(ctx->device));
+  const long long m = std::min<long long>(cap, ctx->nrec);
+  if (host && m > 0) CK(cudaMemcpy(host, ctx->d_rec, (size_t)m * MLP_REC * sizeof(float), cudaMemcpyDeviceToHost));
+  if (count) *count = ctx->nrec;
+  if (cap < 0) ctx->nrec = 0;   // cap < 0 discards the collected records
+  return G6_OK;
+}
+
+}  // extern "C"
+
+struct TrainBuffers {
+  float *X = nullptr, *H1 = nullptr, *H2 = nullptr, *Z = nullptr, *G3 = nullptr, *D2 = nullptr, *D1 = nullptr;
+  float *grad = nullptr, *m = nullptr, *v = nullptr, *mean = nullptr, *istd = nullptr;
+  double* loss = nullptr;
+  int* idx = nullptr;
+  std::vector<void*> all;
+  ~TrainBuffers() { for (void* p : all) cudaFree(p); }
+  template <class T> cudaError_t get(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) { all.push_back(*p); e = cudaMemset(*p, 0, std::max<size_t>(count, 1) * sizeof(T)); }
+    return e;
+  }
+};
+
+static int train_buffers(g6_ctx* ctx, TrainBuffers& b, int batch) {
+  const size_t rows = 2 * (size_t)batch;
+  CK(b.get(&b.X, rows * MLP_IN)); CK(b.get(&b.H1, rows * MLP_H)); CK(b.get(&b.H2, rows * MLP_H));
+  CK(b.get(&b.Z, rows * MLP_OUT)); CK(b.get(&b.G3, rows * MLP_OUT)); CK(b.get(&b.D2, rows * MLP_H));
+  CK(b.get(&b.D1, rows * MLP_H)); CK(b.get(&b.grad, MLP_NPARAM)); CK(b.get(&b.m, MLP_NPARAM));
+  CK(b.get(&b.v, MLP_NPARAM)); CK(b.get(&b.mean, MLP_IN)); CK(b.get(&b.istd, MLP_IN)); CK(b.get(&b.loss, 1));
+  CK(b.get(&b.idx, batch));
+  return G6_OK;
+}
+
+static TrainArgs train_args(g6_ctx* ctx, TrainBuffers& b, const float* rec, int nb, const int* idx) {
+  TrainArgs t;
+  t.nrows = 2 * nb; t.rec = rec; t.idx = idx; t.w = ctx->d_mlp; t.mean = b.mean; t.istd = b.istd;
+  t.s0t = ctx->sig0_t; t.s0r = ctx->sig0_r; t.X = b.X; t.H1 = b.H1; t.H2 = b.H2; t.Z = b.Z; t.G3 = b.G3;
+  t.D2 = b.D2; t.D1 = b.D1; t.grad = b.grad; t.loss = b.loss;
+  return t;
+}
+
+extern "C" {
+
+// Gradient of the training loss over caller records (host), with the current
+// parameters and normalisation: mean over records of -J (see g6_train.cu).
+int g6_mlp_grad(g6_ctx* ctx, const float* records, int64_t nrec, float* grad, double* loss) {
+  if (!ctx || !ctx->have_system || !ctx->have_mlp) return fail(ctx, G6_ERR_STATE, "no system or network");
+  if (!records || nrec <= 0 || nrec > (1 << 22)) return fail(ctx, G6_ERR_ARG, "1 <= nrec <= 2^22 records required");
+  CK(cudaSetDevice(ctx->device));
+  TrainBuffers b;
+  int rc = train_buffers(ctx, b, (int)nrec);
+  if (rc) return rc;
+  float* drec = nullptr;
+  CK(b.get(&drec, (size_t)nrec * MLP_REC));
+  CK(cudaMemcpy(drec, records, (size_t)nrec * MLP_REC * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.mean, ctx->h_mean, sizeof ctx->h_mean, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b.istd, ctx->h_istd, sizeof ctx->h_istd, cudaMemcpyHostToDevice));
+  CK(launch_mlp_grad(train_args(ctx, b, drec, (int)nrec, nullptr), 1.0f / (float)nrec, ctx->stream));
+  double l = 0.0;
+  CK(cudaMemcpyAsync(&l, b.loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (grad) CK(cudaMemcpyAsync(grad, b.grad, MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (loss) *loss = l / (double)nrec;
+  return G6_OK;
+}
+
+// Adam on the records collected by G6_MC_COLLECT runs: feature normalisation
+// from the records, seeded initialisation (constant sigma0 at start), shuffled
+// mini-batches.  loss (optional, epochs) receives the mean loss per epoch.
+int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, double sigma0_t, double sigma0_r,
+                 double* loss) {
+  if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
+  if (ctx->nrec < 2) return fail(ctx, G6_ERR_STATE, "no records (run g6_mc_run in G6_MC_COLLECT mode)");
+  if (epochs < 0 || batch < 2 || !(lr > 0.0) || !(sigma0_t > 0.0) || !(sigma0_r > 0.0))
+    return fail(ctx, G6_ERR_ARG, "bad training arguments");
+  CK(cudaSetDevice(ctx->device));
+  const long long N = ctx->nrec;
+  batch = (int)std::min<long long>(batch, N);
+  TrainBuffers b;
+  int rc = train_buffers(ctx, b, batch);
+  if (rc) return rc;
+  CK(launch_feat_stats(ctx->d_rec, N, b.mean, b.istd, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->h_mean, b.mean, sizeof ctx->h_mean, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->h_istd, b.istd, sizeof ctx->h_istd, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->sig0_t = sigma0_t; ctx->sig0_r = sigma0_r;
+  // initialisation: uniform(-a, a) with a = 1/sqrt(fan_in) from the Philox stream; output layer starts at 0
+  std::vector<float> w(MLP_NPARAM, 0.0f);
+  for (int p = 0; p < MLP_W3; ++p) {
+    const int fan = p < MLP_B1 ? MLP_IN : (p < MLP_W2 ? 1 : (p < MLP_B2 ? MLP_H : 1));
+    double u[2];
+    uniform2(seed, (uint32_t)p, 0x4d4cu, 0u, 0u, u);
+    const bool bias = (p >= MLP_B1 && p < MLP_W2) || (p >= MLP_B2 && p < MLP_W3);
+    w[p] = bias ? 0.0f : (float)((2.0 * u[0] - 1.0) / std::sqrt((double)fan));
+  }
+  w[MLP_B3] = w[MLP_B3 + 1] = (float)std::log(0.25 / 0.75);
+  CK(cudaMemcpy(ctx->d_mlp, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+  ctx->have_mlp = true;
+  std::vector<int> perm(N);
+  int t = 0;
+  for (int ep = 0; ep < epochs; ++ep) {
+    for (long long k = 0; k < N; ++k) perm[k] = (int)k;
+    for (long long k = N - 1; k > 0; --k) {   // Fisher-Yates from the Philox stream
+      double u[2];
+      uniform2(seed, (uint32_t)k, (uint32_t)ep, 0x5348u, (uint32_t)(k >> 32), u);
+      const long long j = std::min<long long>(k, (long long)(u[0] * (double)(k + 1)));
+      std::swap(perm[k], perm[j]);
+    }
+    CK(cudaMemsetAsync(b.loss, 0, sizeof(double), ctx->stream));
+    const long long nb = N / batch;
+    for (long long q = 0; q < nb; ++q) {
+      CK(cudaMemcpyAsync(b.idx, perm.data() + q * batch, batch * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+      CK(launch_mlp_grad(train_args(ctx, b, ctx->d_rec, batch, b.idx), 1.0f / (float)batch, ctx->stream));
+      CK(launch_adam(ctx->d_mlp, b.grad, b.m, b.v, (float)lr, ++t, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));   // the index buffer is reused next batch
+    }
+    double l = 0.0;
+    CK(cudaMemcpy(&l, b.loss, sizeof(double), cudaMemcpyDeviceToHost));
+    if (loss) loss[ep] = nb > 0 ? l / (double)(nb * batch) : 0.0;
   }
   return G6_OK;
 }

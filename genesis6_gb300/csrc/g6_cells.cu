@@ -19,7 +19,11 @@
 // 32-bit fixed-point COM; compacted per warp with ballots.
 #include <cuda_runtime.h>
 
+#include <cooperative_groups.h>
+
 #include "g6_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace g6 {
 
@@ -106,18 +110,47 @@ __global__ void k_cell_fill(CellArgs a, const int* start, int* cellmol) {
   if (i < a.n) cellmol[start[a.cell[i]] + a.slot[i]] = i;
 }
 
-// Residents of each cell in molecule order (insertion sort; cells are small).
+// Residents of one cell in molecule order, sorted by one warp: every lane
+// holds up to 8 ids and computes their ranks (ids are distinct); cells larger
+// than 256 fall back to an insertion sort by lane 0.
+__device__ void sort_cell_warp(int* cellmol, int b, int e, int lane) {
+  const int m = e - b;
+  if (m <= 1) return;
+  if (m <= 256) {
+    int v[8], r[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { v[c] = (lane + 32 * c < m) ? cellmol[b + lane + 32 * c] : 0x7fffffff; r[c] = 0; }
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {
+      if (32 * cc >= m) break;   // uniform across the warp
+      for (int k = 0; k < 32; ++k) {
+        const int w = __shfl_sync(0xffffffffu, v[cc], k);
+        if (32 * cc + k < m) {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) r[c] += (w < v[c]) ? 1 : 0;
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (lane + 32 * c < m) cellmol[b + r[c]] = v[c];
+    __syncwarp();
+  } else if (lane == 0) {
+    for (int k = b + 1; k < e; ++k) {
+      const int v = cellmol[k];
+      int q = k - 1;
+      while (q >= b && cellmol[q] > v) { cellmol[q + 1] = cellmol[q]; --q; }
+      cellmol[q + 1] = v;
+    }
+  }
+}
+
 __global__ void k_cell_sort(const int* start, int* cellmol, int ncell, const int* ctrl) {
   if (skip_ctrl(ctrl)) return;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  const int b = start[c], e = start[c + 1];
-  for (int k = b + 1; k < e; ++k) {
-    int v = cellmol[k];
-    int m = k - 1;
-    while (m >= b && cellmol[m] > v) { cellmol[m + 1] = cellmol[m]; --m; }
-    cellmol[m + 1] = v;
-  }
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= ncell) return;   // whole warp
+  sort_cell_warp(cellmol, start[c], start[c + 1], threadIdx.x & 31);
 }
 
 cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream_t s) {
@@ -126,25 +159,22 @@ cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream
   if (a.n > 0) k_cell_assign<<<(a.n + 255) / 256, 256, 0, s>>>(a);
   k_scan<int><<<1, 1024, 0, s>>>(a.count, start, nc, a.ctrl);
   if (a.n > 0) k_cell_fill<<<(a.n + 255) / 256, 256, 0, s>>>(a, start, cellmol);
-  k_cell_sort<<<(nc + 127) / 128, 128, 0, s>>>(start, cellmol, nc, a.ctrl);
+  k_cell_sort<<<(nc * 32 + 127) / 128, 128, 0, s>>>(start, cellmol, nc, a.ctrl);
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // Neighbour list.  One warp per molecule.
 // ---------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
-  if (skip_ctrl(a.ctrl)) return;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= a.n) return;   // whole warp leaves together
-  const int i = warp, n = a.n;
+__device__ void list_row(const ListArgs& a, int i, int lane) {
+  const int n = a.n;
   const int r = a.rep.mol_rep[i];
   const int nx = a.g.nd[3 * r], ny = a.g.nd[3 * r + 1], nz = a.g.nd[3 * r + 2];
   const int loc = a.cell[i] - a.g.cell_off[r];
   const int cx = loc % nx, cy = (loc / nx) % ny, cz = loc / (nx * ny);
-  const uint32_t xi = a.fix[i], yi = a.fix[n + i], zi = a.fix[2 * n + i];
+  // fixed-point COM of this step's pose buffer (the buffers alternate with the step parity)
+  const uint32_t* fix = (a.ctrl != nullptr && (a.ctrl[1] & 1)) ? a.fix1 : a.fix;
+  const uint32_t xi = fix[i], yi = fix[n + i], zi = fix[2 * n + i];
   const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
   // distinct neighbour offsets per dimension: {-1,0,1} (nd>=3), {0,1} (nd==2), {0} (nd==1)
   const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
@@ -167,9 +197,9 @@ __global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
           if (k < e) {
             j = a.cellmol[k];
             if (j != i) {
-              float dx = (float)(int)(xi - a.fix[j]) * sx;
-              float dy = (float)(int)(yi - a.fix[n + j]) * sy;
-              float dz = (float)(int)(zi - a.fix[2 * n + j]) * sz;
+              float dx = (float)(int)(xi - fix[j]) * sx;
+              float dy = (float)(int)(yi - fix[n + j]) * sy;
+              float dz = (float)(int)(zi - fix[2 * n + j]) * sz;
               in = dx * dx + dy * dy + dz * dz < a.rlist2;
             }
           }
@@ -190,6 +220,102 @@ __global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
     a.com_build[n + i] = a.com[n + i];
     a.com_build[2 * n + i] = a.com[2 * n + i];
   }
+}
+
+__global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
+  if (skip_ctrl(a.ctrl)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= a.n) return;   // whole warp leaves together
+  list_row(a, warp, threadIdx.x & 31);
+}
+
+// ---------------------------------------------------------------------------
+// The whole neighbour-list rebuild in one cooperative launch: clear, assign
+// and count, scan, fill, sort, list, separated by grid-wide barriers.  When
+// the rebuild flag is 0 every block returns before the first barrier (the
+// flag is written only by the kernel that runs before this one).
+// ---------------------------------------------------------------------------
+struct RebuildArgs {
+  CellArgs c;
+  ListArgs l;
+  int* start;
+  int* cellmol;
+};
+
+__global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
+  if (skip_ctrl(a.c.ctrl)) return;
+  cg::grid_group grid = cg::this_grid();
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  if (!grid.is_valid()) {   // not launched cooperatively: report, never wait
+    if (gt == 0) atomicExch(a.l.overflow, 2);
+    return;
+  }
+  const int lane = threadIdx.x & 31, gw = gt >> 5, nw = gs >> 5;
+  const int nc = a.c.g.ncell_total, n = a.c.n;
+  for (int c = gt; c <= nc; c += gs) a.c.count[c] = 0;
+  grid.sync();
+  for (int base = gt - lane; base < n; base += gs) {   // whole warps, grid-stride
+    const int i = base + lane;
+    const bool valid = i < n;
+    int c = -1;
+    if (valid) {
+      c = ref_cell(a.c.rep, a.c.g, a.c.rep.mol_rep[i], a.c.com[i], a.c.com[n + i], a.c.com[2 * n + i]);
+      a.c.cell[i] = c;
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (valid) {
+      const unsigned peers = __match_any_sync(act, c);
+      const int leader = __ffs(peers) - 1;
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      int b0 = 0;
+      if (lane == leader) b0 = atomicAdd(&a.c.count[c], __popc(peers));
+      b0 = __shfl_sync(peers, b0, leader);
+      a.c.slot[i] = b0 + rank;
+    }
+  }
+  grid.sync();
+  if (blockIdx.x == 0) {   // exclusive scan of the cell counts by one block
+    __shared__ int part[256];
+    const int t = threadIdx.x, per = (nc + 255) / 256;
+    const int b = t * per, e = min(nc, b + per);
+    int s = 0;
+    for (int k = b; k < e; ++k) s += a.c.count[k];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+      const int v = t >= off ? part[t - off] : 0;
+      __syncthreads();
+      part[t] += v;
+      __syncthreads();
+    }
+    int run = t == 0 ? 0 : part[t - 1];
+    for (int k = b; k < e; ++k) { a.start[k] = run; run += a.c.count[k]; }
+    if (t == 255) a.start[nc] = part[255];
+  }
+  grid.sync();
+  for (int i = gt; i < n; i += gs) a.cellmol[a.start[a.c.cell[i]] + a.c.slot[i]] = i;
+  grid.sync();
+  for (int c = gw; c < nc; c += nw) sort_cell_warp(a.cellmol, a.start[c], a.start[c + 1], lane);
+  grid.sync();
+  for (int i = gw; i < n; i += nw) list_row(a.l, i, lane);
+}
+
+int rebuild_grid_limit() {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild, 256, 0);
+  return sms * (per > 0 ? per : 1);
+}
+
+cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int* cellmol, int grid_limit,
+                           cudaStream_t s) {
+  RebuildArgs a;
+  a.c = c; a.l = l; a.start = start; a.cellmol = cellmol;
+  const int want = (max(c.n, c.g.ncell_total) * 32 + 255) / 256;
+  const int blocks = max(1, min(grid_limit, want));
+  void* args[] = {&a};
+  return cudaLaunchCooperativeKernel((void*)k_rebuild, dim3(blocks), dim3(256), args, 0, s);
 }
 
 cudaError_t launch_list(const ListArgs& a, cudaStream_t s) {

@@ -20,7 +20,10 @@
 //   W     += d (x) (sum of i-site forces incl. f_COM)
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "g6_internal.cuh"
+#include "g6_rigid.cuh"
 
 namespace g6 {
 
@@ -175,9 +178,14 @@ __device__ __forceinline__ double group_sum(double v) {
 // ---------------------------------------------------------------------------
 // k_force: neighbour-list force kernel.
 // ---------------------------------------------------------------------------
-template <class M, bool MIXED, int LPI>
-__global__ void __launch_bounds__(128) k_force(ForceArgs a) {
+template <class M, bool MIXED, int LPI, bool FUSED>
+__global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
   using R = typename std::conditional<MIXED, float, double>::type;
+  int step = 0;
+  if (a.ctrl) step = a.ctrl[1];
+  const bool odd = (step & 1) != 0;
+  const double* pk64 = odd ? a.pk64_1 : a.pk64;
+  const float4* pk32 = odd ? a.pk32_1 : a.pk32;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gt / LPI;
   const int sub = gt % LPI;
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
     double Ld[3], iLd[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) { Ld[k] = a.rep.L[3 * r + k]; iLd[k] = a.rep.invL[3 * r + k]; }
-    const double* pi = a.pk64 + (size_t)i * M::W64;
+    const double* pi = pk64 + (size_t)i * M::W64;
     double ci[3] = {pi[0], pi[1], pi[2]};
     const int nn = a.nnb[i];
     const int* row = a.nbr + (size_t)i * a.cap;
@@ -201,7 +209,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
       float wi[4 * M::NPK];
 #pragma unroll
       for (int q = 0; q < M::NPK; ++q) {
-        float4 t = a.pk32[(size_t)i * M::NPK + q];
+        float4 t = pk32[(size_t)i * M::NPK + q];
         wi[4 * q] = t.x; wi[4 * q + 1] = t.y; wi[4 * q + 2] = t.z; wi[4 * q + 3] = t.w;
       }
       const uint32_t xi = __float_as_uint(wi[0]), yi = __float_as_uint(wi[1]), zi = __float_as_uint(wi[2]);
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
         float wj[4 * M::NPK];
 #pragma unroll
         for (int q = 0; q < M::NPK; ++q) {
-          float4 t = a.pk32[(size_t)j * M::NPK + q];
+          float4 t = pk32[(size_t)j * M::NPK + q];
           wj[4 * q] = t.x; wj[4 * q + 1] = t.y; wj[4 * q + 2] = t.z; wj[4 * q + 3] = t.w;
         }
         float d[3];
@@ -228,7 +236,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
         bool in = dd < rout2;
         if (fabsf(dd - rout2) < band) {
           // borderline: decide with the reference's FP64 arithmetic
-          const double* pj = a.pk64 + (size_t)j * M::W64;
+          const double* pj = pk64 + (size_t)j * M::W64;
           double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
           in = exact_dd(ci, cj, Ld, iLd, o, dx) < a.cc.rout2;
         }
@@ -250,7 +258,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
         for (int k = 0; k < 3; ++k) ri[s][k] = (R)pi[3 + 3 * s + k];
       for (int k = sub; k < nn; k += LPI) {
         const int j = row[k];
-        const double* pj = a.pk64 + (size_t)j * M::W64;
+        const double* pj = pk64 + (size_t)j * M::W64;
         double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
         double dd = exact_dd(ci, cj, Ld, iLd, o, dx);
         if (!(dd < a.cc.rout2)) continue;
@@ -293,45 +301,80 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
   int np_tot = npin;
 #pragma unroll
   for (int m = LPI / 2; m >= 1; m >>= 1) np_tot += __shfl_xor_sync(0xffffffffu, np_tot, m);
-  if (valid && sub == 0) {
+  if (!FUSED) {
+    if (valid && sub == 0) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
-    a.emol[i] = 0.5 * v[6];
+      for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
+      a.emol[i] = 0.5 * v[6];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
-    if (a.npair_in) a.npair_in[i] = np_tot;
+      for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
+      if (a.npair_in) a.npair_in[i] = np_tot;
+    }
+    return;
   }
+  // fused MD step: Gear corrector, reductions and the next predict+placement
+  const bool predict_next = step + 1 < sa.ctrl[2];
+  double vv[NRED];
+#pragma unroll
+  for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
+  double dmax2 = 0.0;
+  int bad = 0, rr = -1;
+  if (valid && sub == 0) {
+    rr = a.rep.mol_rep[i];
+    const double F[3] = {v[0], v[1], v[2]}, tl[3] = {v[3], v[4], v[5]};
+    double wm[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) wm[k] = 0.5 * v[7 + k];
+    correct_one(sa, i, F, tl, 0.5 * v[6], wm, 0.5 * (double)np_tot, step, predict_next, pose_buf(sa, odd ? 1 : 0),
+                pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+  }
+  step_reduce<128>(sa, vv, rr, dmax2, bad, 128 / LPI, step, predict_next);
 }
 
-template <class M, bool MIXED, int LPI>
-static cudaError_t launch_force_t(const ForceArgs& a, cudaStream_t s) {
+template <class M, bool MIXED, int LPI, bool FUSED>
+static cudaError_t launch_force_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
   const int threads = 128;
   const long long total = (long long)a.n * LPI;
   const int blocks = (int)((total + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;
-  k_force<M, MIXED, LPI><<<blocks, threads, 0, s>>>(a);
+  k_force<M, MIXED, LPI, FUSED><<<blocks, threads, 0, s>>>(a, sa);
   return cudaGetLastError();
 }
 
-template <class M, bool MIXED>
-static cudaError_t launch_force_l(const ForceArgs& a, int lpi, cudaStream_t s) {
+template <class M, bool MIXED, bool FUSED>
+static cudaError_t launch_force_l(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
   switch (lpi) {
-    case 4: return launch_force_t<M, MIXED, 4>(a, s);
-    case 8: return launch_force_t<M, MIXED, 8>(a, s);
-    case 16: return launch_force_t<M, MIXED, 16>(a, s);
-    default: return launch_force_t<M, MIXED, 32>(a, s);
+    case 4: return launch_force_t<M, MIXED, 4, FUSED>(a, sa, s);
+    case 8: return launch_force_t<M, MIXED, 8, FUSED>(a, sa, s);
+    case 16: return launch_force_t<M, MIXED, 16, FUSED>(a, sa, s);
+    default: return launch_force_t<M, MIXED, 32, FUSED>(a, sa, s);
   }
 }
 
-template <class M>
-static cudaError_t launch_force_m(const ForceArgs& a, bool mixed, int lpi, cudaStream_t s) {
-  return mixed ? launch_force_l<M, true>(a, lpi, s) : launch_force_l<M, false>(a, lpi, s);
+template <class M, bool FUSED>
+static cudaError_t launch_force_m(const ForceArgs& a, const StepArgs& sa, bool mixed, int lpi, cudaStream_t s) {
+  return mixed ? launch_force_l<M, true, FUSED>(a, sa, lpi, s) : launch_force_l<M, false, FUSED>(a, sa, lpi, s);
 }
 
+template <bool FUSED>
+static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int model, bool mixed, int lpi,
+                                    cudaStream_t s) {
+  if (model == G6_TIP4P) return launch_force_m<MT<3, false>, FUSED>(a, sa, mixed, lpi, s);
+  if (a.pc.taper) return launch_force_m<MT<4, true>, FUSED>(a, sa, mixed, lpi, s);
+  return launch_force_m<MT<4, false>, FUSED>(a, sa, mixed, lpi, s);
+}
+
+// Force only (outputs F, lab torque, per-molecule energy and virial).
 cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cudaStream_t s) {
-  if (model == G6_TIP4P) return launch_force_m<MT<3, false>>(a, mixed, lpi, s);
-  if (a.pc.taper) return launch_force_m<MT<4, true>>(a, mixed, lpi, s);
-  return launch_force_m<MT<4, false>>(a, mixed, lpi, s);
+  StepArgs none;
+  memset(&none, 0, sizeof none);
+  return launch_force_any<false>(a, none, model, mixed, lpi, s);
+}
+
+// One fused MD step: force, then the Gear corrector, reductions and the next
+// step's predict + placement in the kernel's epilogue.
+cudaError_t launch_step(const ForceArgs& a, const StepArgs& sa, int model, bool mixed, int lpi, cudaStream_t s) {
+  return launch_force_any<true>(a, sa, model, mixed, lpi, s);
 }
 
 int pk64_width(int model) { return model == G6_TIP4P ? MT<3, false>::W64 : MT<4, false>::W64; }

@@ -28,7 +28,7 @@ constexpr int REC = 53;
 constexpr int MAXSITE = 6;  // sites per molecule including the COM site
 constexpr int MAXQ = 4;     // charged sites per molecule
 constexpr int MAXREP_PER_BLOCK = 8;
-constexpr int RED_BLOCK = 128;   // block size of the per-molecule update kernels
+constexpr int RED_BLOCK = 64;    // block size of the per-molecule update kernels (FP64-bound: spread over SMs)
 constexpr int NRED = 24;         // reduced quantities per replica (see g6_md.cu)
 
 // ---------------------------------------------------------------------------
@@ -152,6 +152,9 @@ constexpr double G40 = 251.0 / 720.0, G42 = 11.0 / 12.0, G43 = 1.0 / 3.0, G44 = 
 // ---------------------------------------------------------------------------
 struct ForceArgs {
   int n, cap, stride_pk32;
+  const double* pk64_1;   // pose buffer 1, used when ctrl != NULL and the step is odd
+  const float4* pk32_1;
+  const int* ctrl;
   const int* nbr;
   const int* nnb;
   RepDev rep;
@@ -198,6 +201,7 @@ struct ListArgs {
   const int* start;
   const int* cellmol;
   const uint32_t* fix;   // SoA 3n
+  const uint32_t* fix1;  // buffer 1 (odd steps when ctrl != NULL)
   const double* com;     // SoA 3n (state)
   double* com_build;     // SoA 3n
   float rlist2;
@@ -245,21 +249,20 @@ struct PlaceArgs {
 };
 
 struct StepArgs {
-  PlaceArgs p;
+  PlaceArgs p;         // constants, the state st and pose buffer 0
+  double* tmat1;       // pose buffer 1 (the buffers alternate with the step parity)
+  double* pk64_1;
+  float4* pk32_1;
+  uint32_t* fix1;
   double mass, I[3], dt;
-  const double* F;
-  const double* tl;
-  const double* emol;
-  const double* wmol;
-  const int* npin;
   const double* com_build;
   double half_skin2;
   ThermoDev* th;
-  double* part;        // gridDim * MAXREP_PER_BLOCK * NRED
-  double* partmax;     // gridDim
+  double* part;        // blocks * MAXREP_PER_BLOCK * NRED
+  double* partmax;     // blocks
   double* red;         // nrep * NRED (finalize scratch)
   unsigned int* done;
-  int* ctrl;           // [0] rebuild, [1] step, [2] nsteps, [3] error bits, [4] list overflow, [5] log capacity
+  int* ctrl;           // [0] rebuild, [1] step, [2] nsteps, [3] error bits, [4] -, [5] log capacity, [6] step base
   double* log;         // [step][rep][G6_LOG_WIDTH]
   unsigned long long seed;
 };
@@ -293,10 +296,15 @@ int pk64_width(int model);
 int pk32_width(int model);
 cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream_t s);
 cudaError_t launch_list(const ListArgs& a, cudaStream_t s);
+int rebuild_grid_limit();
+cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int* cellmol, int grid_limit,
+                           cudaStream_t s);
 cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
-cudaError_t launch_correct_step(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_step(const ForceArgs& f, const StepArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
+cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
+cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);
 cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s);
 cudaError_t launch_exchange(const ExchArgs& a, double* st, int n, const int* mol_rep, cudaStream_t s);
 

@@ -103,6 +103,28 @@ __device__ __forceinline__ void mlp_widths(const MlpDev& m, const float* feat, d
   }
 }
 
+struct TrainArgs {
+  int nrows;              // 2 * records in the batch (row 2i = x, row 2i+1 = x')
+  const float* rec;       // records (MLP_REC floats each)
+  const int* idx;         // optional: record index of batch entry b
+  const float* w;         // parameters
+  const float* mean;      // feature normalisation
+  const float* istd;
+  double s0t, s0r;
+  float* X;               // [rows][IN] normalised inputs
+  float* H1;              // [rows][H]
+  float* H2;              // [rows][H]
+  float* Z;               // [rows][OUT]
+  float* G3;              // [rows][OUT] dL/dz
+  float* D2;              // [rows][H]
+  float* D1;              // [rows][H]
+  float* grad;            // [NPARAM]
+  double* loss;           // accumulated sum of -J over the batch
+};
+
+cudaError_t launch_mc(const McArgs& a, int model, bool mixed, bool learned, cudaStream_t s);
+cudaError_t launch_mlp_grad(TrainArgs a, float inv_batch, cudaStream_t s);
+
 // Block-wide feature accumulation (every thread of the block calls it) for
 // molecule tg placed at COM `com` with lab site offsets `off` (index 1..NQ =
 // charged sites).  Neighbours are the other molecules i0..i1-1 of its chain.

@@ -223,14 +223,14 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
 
   ListArgs la;
   la.n = n; la.cap = CAP; la.rep = rep; la.g = g; la.cell = ca.cell; la.start = (const int*)(base + O_START);
-  la.cellmol = (const int*)(base + O_CELLMOL); la.fix = pa.fix; la.com = pa.st; la.com_build = (double*)(base + O_COMB);
+  la.cellmol = (const int*)(base + O_CELLMOL); la.fix = pa.fix; la.fix1 = pa.fix; la.com = pa.st; la.com_build = (double*)(base + O_COMB);
   la.rlist2 = (float)(rlist * rlist) + 1e-3f; la.nbr = (int*)(base + O_NBR); la.nnb = (int*)(base + O_NNB);
   la.overflow = (int*)(base + O_OVF); la.ctrl = nullptr;
 
   ForceArgs fa;
   std::memset(&fa, 0, sizeof fa);
   fa.n = n; fa.cap = CAP; fa.stride_pk32 = pa.npk; fa.nbr = la.nbr; fa.nnb = la.nnb; fa.rep = rep; fa.pk64 = pa.pk64;
-  fa.pk32 = pa.pk32;
+  fa.pk32 = pa.pk32; fa.pk64_1 = pa.pk64; fa.pk32_1 = pa.pk32; fa.ctrl = nullptr;
   make_pair_const(mh, path, fa.pc);
   make_cut_const(r_in, r_out, fa.cc);
   fa.F = (double*)(base + O_F); fa.tl = (double*)(base + O_TL); fa.emol = (double*)(base + O_EMOL);

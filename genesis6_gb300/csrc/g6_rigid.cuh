@@ -1,0 +1,435 @@
+// g6_rigid.cuh -- rigid-body Gear predictor-corrector, site placement and the
+// per-step reductions, as device functions shared by the placement kernel
+// (g6_md.cu) and the fused force+integrator step kernel (g6_force.cu).
+//
+//   predict_one   rigid_predict (RigidModule.F90:480-559)
+//   place_to      rigid_setmatrix + rigid_setsiteposition0 (RigidModule.F90:62-144):
+//                 rotation matrix and the packed poses the site loop reads
+//   correct_one   rigid_correct (RigidModule.F90:1255-1487) with Nose friction and
+//                 the stochastic-collision thermostat, the Rigid_Ek /
+//                 Rigid_PressureTensor terms (:576-619) of one molecule, then the next
+//                 step's predict + placement and the neighbour-list displacement test
+//   step_reduce   per-block, per-replica partial sums; the last block to finish sums
+//                 the partials in a fixed order, computes T, P and the conserved
+//                 quantity (Mixture.F90:2251-2264, 2431-2453), runs Nose_Correct and the
+//                 next Nose_Predict (NoseModule.F90:43-87) and sets the rebuild flag.
+// All FP64.
+#pragma once
+
+#include "g6_internal.cuh"
+
+namespace g6 {
+
+#define G6_ST(c) st[(size_t)(c) * n + i]
+
+__device__ __forceinline__ void setmatrix(const double q[4], double t[9]) {
+  const double qa = q[0], qb = q[1], qc = q[2], qd = q[3];
+  t[0] = (qa * qa + qb * qb - (qc * qc + qd * qd));
+  t[1] = -2.0 * (qa * qd + qb * qc);
+  t[2] = 2.0 * (qb * qd - qa * qc);
+  t[3] = 2.0 * (qa * qd - qb * qc);
+  t[4] = qa * qa + qc * qc - (qb * qb + qd * qd);
+  t[5] = -2.0 * (qa * qb + qc * qd);
+  t[6] = 2.0 * (qa * qc + qb * qd);
+  t[7] = 2.0 * (qa * qb - qc * qd);
+  t[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
+}
+
+__device__ __forceinline__ void predict_one(double* st, int n, int i) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double d1 = G6_ST(3 + a), d2 = G6_ST(6 + a), d3 = G6_ST(9 + a), d4 = G6_ST(12 + a), d5 = G6_ST(15 + a);
+    G6_ST(a) = G6_ST(a) + d1 + d2 + d3 + d4 + d5;
+    G6_ST(3 + a) = d1 + 2.0 * d2 + 3.0 * d3 + 4.0 * d4 + 5.0 * d5;
+    G6_ST(6 + a) = d2 + 3.0 * d3 + 6.0 * d4 + 10.0 * d5;
+    G6_ST(9 + a) = d3 + 4.0 * d4 + 10.0 * d5;
+    G6_ST(12 + a) = d4 + 5.0 * d5;
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double w1 = G6_ST(18 + a), w2 = G6_ST(21 + a), w3 = G6_ST(24 + a), w4 = G6_ST(27 + a), w5 = G6_ST(30 + a);
+    G6_ST(18 + a) = w1 + w2 + w3 + w4 + w5;
+    G6_ST(21 + a) = w2 + 2.0 * w3 + 3.0 * w4 + 4.0 * w5;
+    G6_ST(24 + a) = w3 + 3.0 * w4 + 6.0 * w5;
+    G6_ST(27 + a) = w4 + 4.0 * w5;
+  }
+  double q[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    double q1 = G6_ST(33 + a), q2 = G6_ST(37 + a), q3 = G6_ST(41 + a), q4 = G6_ST(45 + a), q5 = G6_ST(49 + a);
+    q[a] = q1 + q2 + q3 + q4 + q5;
+    G6_ST(37 + a) = q2 + 2.0 * q3 + 3.0 * q4 + 4.0 * q5;
+  }
+  double re = 1.0 / sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) G6_ST(33 + a) = q[a] * re;
+}
+
+// Placement of molecule i (its current com and q in st) into one buffer set.
+__device__ __forceinline__ void place_to(const PlaceArgs& a, int i, double* tmat, double* pk64, float4* pk32,
+                                         uint32_t* fix) {
+  const int n = a.n;
+  const double* st = a.st;
+  double q[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
+  double t[9];
+  setmatrix(q, t);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) tmat[(size_t)k * n + i] = t[k];
+  const int r = a.rep.mol_rep[i];
+  const double com[3] = {G6_ST(0), G6_ST(1), G6_ST(2)};
+  double* p64 = pk64 + (size_t)i * a.w64;
+  p64[0] = com[0]; p64[1] = com[1]; p64[2] = com[2];
+  float w[24];
+#pragma unroll
+  for (int k = 0; k < 24; ++k) w[k] = 0.0f;
+  const uint32_t fx = to_fixed(com[0], a.rep.invL[3 * r]);
+  const uint32_t fy = to_fixed(com[1], a.rep.invL[3 * r + 1]);
+  const uint32_t fz = to_fixed(com[2], a.rep.invL[3 * r + 2]);
+  fix[i] = fx; fix[n + i] = fy; fix[2 * n + i] = fz;
+  w[0] = __uint_as_float(fx); w[1] = __uint_as_float(fy); w[2] = __uint_as_float(fz);
+  for (int s = 0; s <= a.nq; ++s) {   // LJ site then charged sites; the COM site offset is zero
+    const double bx = a.body[s][0], by = a.body[s][1], bz = a.body[s][2];
+    const double o[3] = {t[0] * bx + t[1] * by + t[2] * bz, t[3] * bx + t[4] * by + t[5] * bz,
+                         t[6] * bx + t[7] * by + t[8] * bz};
+    for (int k = 0; k < 3; ++k) { p64[3 + 3 * s + k] = o[k]; w[3 + 3 * s + k] = (float)o[k]; }
+  }
+  for (int k = 3 + 3 * (a.nq + 1); k < a.w64; ++k) p64[k] = 0.0;
+  for (int q4 = 0; q4 < a.npk; ++q4)
+    pk32[(size_t)i * a.npk + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+}
+
+// (1/2) W(w) q pattern of RigidModule.F90:1337-1348
+__device__ __forceinline__ void qdot(const double w[3], const double q[4], double o[4]) {
+  o[0] = (-w[0] * q[1] + w[1] * q[2] - w[2] * q[3]);
+  o[1] = (w[0] * q[0] - w[1] * q[3] - w[2] * q[2]);
+  o[2] = (-w[0] * q[3] - w[1] * q[0] + w[2] * q[1]);
+  o[3] = (w[0] * q[2] + w[1] * q[1] + w[2] * q[0]);
+}
+
+__device__ __forceinline__ double normal_pair(double u1, double u2, double& second) {
+  double r = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  second = r * c;
+  return r * s;
+}
+
+// Buffer set (0 or 1) of the packed poses.
+struct PoseBuf {
+  double* tmat;
+  double* pk64;
+  float4* pk32;
+  uint32_t* fix;
+};
+__device__ __forceinline__ PoseBuf pose_buf(const StepArgs& a, int which) {
+  PoseBuf b;
+  if (which == 0) { b.tmat = a.p.tmat; b.pk64 = a.p.pk64; b.pk32 = a.p.pk32; b.fix = a.p.fix; }
+  else { b.tmat = a.tmat1; b.pk64 = a.pk64_1; b.pk32 = a.pk32_1; b.fix = a.fix1; }
+  return b;
+}
+
+// rigid_correct + energy/virial/kinetic terms + the next predict and placement
+// for molecule i.  F: COM force; tl: lab-frame torque; cur/next: pose buffers.
+__device__ __forceinline__ void correct_one(const StepArgs& a, int i, const double F[3], const double tl[3],
+                                            double emol, const double wmol[9], double npair_half, int step,
+                                            bool predict_next, const PoseBuf& cur, const PoseBuf& next,
+                                            double (&v)[NRED], double& dmax2, int& bad) {
+  const int n = a.p.n;
+  double* st = a.p.st;
+  const int r = a.p.rep.mol_rep[i];
+  const ThermoDev th = a.th[r];
+  const double dt = a.dt;
+  // body torque = T^T tau_lab (rigid_collectforce RigidModule.F90:305-310)
+  double t[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) t[k] = cur.tmat[(size_t)k * n + i];
+  const double tau[3] = {t[0] * tl[0] + t[3] * tl[1] + t[6] * tl[2], t[1] * tl[0] + t[4] * tl[1] + t[7] * tl[2],
+                         t[2] * tl[0] + t[5] * tl[1] + t[8] * tl[2]};
+  if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]) && isfinite(tau[0]) && isfinite(tau[1]) &&
+        isfinite(tau[2])))
+    bad = 1;
+  double ext_t = 0.0, ext_r = 0.0;
+  if (th.kind == G6_NOSE) {
+    const double nc = th.z[0] * dt;
+    ext_t = nc * 0.5;
+    ext_r = nc;
+  }
+  // COM: Gear-5
+  const double massi = 1.0 / a.mass;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double nf = F[c] * (dt * dt * 0.5 * massi);
+    nf = nf - G6_ST(3 + c) * ext_t;
+    const double delta = nf - G6_ST(6 + c);
+    G6_ST(c) = G6_ST(c) + G50 * delta;
+    G6_ST(3 + c) = G6_ST(3 + c) + G51 * delta;
+    G6_ST(6 + c) = nf;
+    G6_ST(9 + c) = G6_ST(9 + c) + G53 * delta;
+    G6_ST(12 + c) = G6_ST(12 + c) + G54 * delta;
+    G6_ST(15 + c) = G6_ST(15 + c) + G55 * delta;
+  }
+  // quaternion value
+  double q1[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
+  double w1[3] = {G6_ST(18), G6_ST(19), G6_ST(20)};
+  double nw[4];
+  qdot(w1, q1, nw);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const double dw = nw[c] * dt * 0.5 - G6_ST(37 + c);
+    q1[c] = q1[c] + G40 * dw;
+    G6_ST(33 + c) = q1[c];
+  }
+  // angular velocity: Gear-4 with Euler's equations
+  const double Ix = a.I[0], Iy = a.I[1], Iz = a.I[2];
+  double nf[3];
+  nf[0] = (tau[0] + (Iy - Iz) * w1[1] * w1[2]) * dt * (1.0 / Ix);
+  nf[1] = (tau[1] + (Iz - Ix) * w1[2] * w1[0]) * dt * (1.0 / Iy);
+  nf[2] = (tau[2] + (Ix - Iy) * w1[0] * w1[1]) * dt * (1.0 / Iz);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    nf[c] = nf[c] - w1[c] * ext_r;
+    const double delta = nf[c] - G6_ST(21 + c);
+    G6_ST(18 + c) = G6_ST(18 + c) + G40 * delta;
+    G6_ST(21 + c) = nf[c];
+    G6_ST(24 + c) = G6_ST(24 + c) + G42 * delta;
+    G6_ST(27 + c) = G6_ST(27 + c) + G43 * delta;
+    G6_ST(30 + c) = G6_ST(30 + c) + G44 * delta;
+  }
+  // stochastic collisions (new thermostat; velocity resampled from Maxwell-Boltzmann)
+  if (th.kind == G6_ANDERSEN) {
+    double u[2];
+    const uint32_t sc = (uint32_t)(a.ctrl[6] + step);
+    uniform2(a.seed, (uint32_t)i, sc, 0x41u, 0u, u);
+    if (u[0] <= th.rate * dt) {
+      const double kT = th.temp * RGAS * J2I;
+      double z[6];
+      for (int p = 0; p < 3; ++p) {
+        double g[2];
+        uniform2(a.seed, (uint32_t)i, sc, 0x41u, (uint32_t)(p + 1), g);
+        z[2 * p] = normal_pair(g[0], g[1], z[2 * p + 1]);
+      }
+      const double sv = sqrt(kT * massi) * dt;
+      for (int c = 0; c < 3; ++c) G6_ST(3 + c) = z[c] * sv;
+      G6_ST(18) = z[3] * sqrt(kT / Ix);
+      G6_ST(19) = z[4] * sqrt(kT / Iy);
+      G6_ST(20) = z[5] * sqrt(kT / Iz);
+    }
+  }
+  // quaternion derivative stacks from the corrected angular-velocity stack
+  double W[5][3], Q[5][4], tq[4], uq[4], vq[4], xq[4];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) W[k][c] = G6_ST(18 + 3 * k + c);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[0][c] = q1[c];
+  qdot(W[0], Q[0], tq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[1][c] = tq[c] * dt * 0.5;
+  qdot(W[1], Q[0], tq); qdot(W[0], Q[1], uq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[2][c] = (tq[c] + uq[c]) * dt * 0.25;
+  qdot(W[2], Q[0], tq); qdot(W[0], Q[2], uq); qdot(W[1], Q[1], vq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[3][c] = (tq[c] + uq[c] + vq[c]) * dt * (1.0 / 6.0);
+  qdot(W[3], Q[0], tq); qdot(W[2], Q[1], uq); qdot(W[1], Q[2], vq); qdot(W[0], Q[3], xq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[4][c] = (tq[c] + uq[c] + vq[c] + xq[c]) * dt * (1.0 / 8.0);
+#pragma unroll
+  for (int k = 1; k < 5; ++k)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) G6_ST(33 + 4 * k + c) = Q[k][c];
+  // reductions: Epot, virial, kinetic sums, kinetic tensor, pairs
+  const double d1[3] = {G6_ST(3), G6_ST(4), G6_ST(5)};
+  v[0] = emol;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) v[1 + k] = wmol[k];
+  v[10] = d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2];
+  v[11] = W[0][0] * W[0][0];
+  v[12] = W[0][1] * W[0][1];
+  v[13] = W[0][2] * W[0][2];
+#pragma unroll
+  for (int p = 0; p < 3; ++p)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) v[14 + 3 * p + q] = d1[p] * d1[q];
+  v[23] = npair_half;
+  if (predict_next) {
+    predict_one(st, n, i);
+    place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.fix);
+    const double dx = G6_ST(0) - a.com_build[i], dy = G6_ST(1) - a.com_build[n + i],
+                 dz = G6_ST(2) - a.com_build[2 * n + i];
+    dmax2 = dx * dx + dy * dy + dz * dz;
+    if (!isfinite(dmax2)) { bad = 1; dmax2 = 1e300; }
+  }
+}
+
+// Per-block partial sums, segmented by replica (molecules are in replica
+// order; a block spans replicas rfirst..rfirst+nslots-1 <= MAXREP_PER_BLOCK).
+// Every thread of the block calls it; r = -1 contributes nothing.
+template <int NV, int NWARP>
+__device__ void block_segmented_sum(const double (&v)[NV], int r, int rfirst, int nslots, double* out_part) {
+  __shared__ double sh[NWARP][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int s = 0; s < nslots; ++s) {
+    const bool mine = (r == rfirst + s);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = mine ? v[k] : 0.0;
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
+      if (lane == 0) sh[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+      double x = 0.0;
+      for (int w = 0; w < NWARP; ++w) x += sh[w][threadIdx.x];
+      out_part[s * NV + threadIdx.x] = x;
+    }
+    __syncthreads();
+  }
+}
+
+// Block partials, then the last block to arrive finalises the step.
+// mpb: molecules covered by one block (blocks are in molecule order).
+template <int NTHREADS>
+__device__ void step_reduce(const StepArgs& a, const double (&v)[NRED], int r, double dmax2, int bad, int mpb,
+                            int step, bool predict_next) {
+  const int n = a.p.n;
+  const int first_i = blockIdx.x * mpb;
+  const int last_i = min(n, first_i + mpb) - 1;
+  const int rfirst = a.p.rep.mol_rep[first_i];
+  const int nslots = a.p.rep.mol_rep[last_i] - rfirst + 1;
+  block_segmented_sum<NRED, NTHREADS / 32>(v, r, rfirst, nslots, a.part + (size_t)blockIdx.x * MAXREP_PER_BLOCK * NRED);
+  {
+    __shared__ double shm[NTHREADS / 32];
+    __shared__ int shbad[NTHREADS / 32];
+    double m = dmax2;
+    int b = bad;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      b |= __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { shm[threadIdx.x >> 5] = m; shbad[threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double mm = 0.0;
+      int bb = 0;
+      for (int w = 0; w < NTHREADS / 32; ++w) { mm = fmax(mm, shm[w]); bb |= shbad[w]; }
+      a.partmax[blockIdx.x] = mm;
+      if (bb) atomicOr(&a.ctrl[3], 1);
+    }
+  }
+  __shared__ int am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(a.done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  const int nrep = a.p.rep.nrep;
+  if (nrep * NRED >= NTHREADS) {
+    // many replicas: one thread per (replica, quantity), blocks summed in order
+    for (int task = threadIdx.x; task < nrep * NRED; task += NTHREADS) {
+      const int rr = task / NRED, k = task % NRED;
+      const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
+      double s = 0.0;
+      for (int b = b0; b <= b1; ++b) {
+        const int slot = rr - a.p.rep.mol_rep[b * mpb];
+        s += __ldcg(&a.part[((size_t)b * MAXREP_PER_BLOCK + slot) * NRED + k]);
+      }
+      a.red[task] = s;
+    }
+  } else {
+    // few replicas: thread t sums blocks b0+t, b0+t+NTHREADS, ... of every quantity,
+    // then a fixed-order tree per quantity
+    __shared__ double tree[NTHREADS];
+    for (int rr = 0; rr < nrep; ++rr) {
+      const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
+      double s[NRED];
+#pragma unroll
+      for (int k = 0; k < NRED; ++k) s[k] = 0.0;
+      for (int b = b0 + (int)threadIdx.x; b <= b1; b += NTHREADS) {
+        const int slot = rr - a.p.rep.mol_rep[b * mpb];
+        const double* src = a.part + ((size_t)b * MAXREP_PER_BLOCK + slot) * NRED;
+#pragma unroll
+        for (int k = 0; k < NRED; ++k) s[k] += __ldcg(src + k);
+      }
+      for (int k = 0; k < NRED; ++k) {
+        tree[threadIdx.x] = s[k];
+        __syncthreads();
+        for (int o = NTHREADS / 2; o >= 1; o >>= 1) {
+          if ((int)threadIdx.x < o) tree[threadIdx.x] += tree[threadIdx.x + o];
+          __syncthreads();
+        }
+        if (threadIdx.x == 0) a.red[rr * NRED + k] = tree[0];
+        __syncthreads();
+      }
+    }
+  }
+  __shared__ double gmaxv[NTHREADS];
+  {
+    double m = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += NTHREADS) m = fmax(m, __ldcg(&a.partmax[b]));
+    gmaxv[threadIdx.x] = m;
+  }
+  __syncthreads();
+  __shared__ double gmax;
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int t = 0; t < NTHREADS; ++t) m = fmax(m, gmaxv[t]);
+    gmax = m;
+  }
+  __syncthreads();
+  const int logcap = a.ctrl[5];
+  for (int rr = threadIdx.x; rr < nrep; rr += NTHREADS) {
+    const double* s = a.red + (size_t)rr * NRED;
+    ThermoDev& th = a.th[rr];
+    const int nm = a.p.rep.off[rr + 1] - a.p.rep.off[rr];
+    const double dof = 6.0 * nm;
+    const double dt = a.dt;
+    const double ekt = s[10] * a.mass * 0.5 * (1.0 / (dt * dt));
+    const double ekr = (s[11] * a.I[0] + s[12] * a.I[1] + s[13] * a.I[2]) * 0.5;
+    const double temperature = I2J * 2.0 * (ekt + ekr) / (RGAS * dof);
+    const double pkin = (s[14] + s[18] + s[22]) * a.mass * (1.0 / (dt * dt));
+    const double vp = pkin + s[1] + s[5] + s[9];
+    const double V = a.p.rep.L[3 * rr] * a.p.rep.L[3 * rr + 1] * a.p.rep.L[3 * rr + 2];
+    const double pressure = (vp / 3.0) * I2J * (1.0 / A2P) / (V * NA * ANG2M * ANG2M * ANG2M);
+    if (th.kind == G6_NOSE) {   // Nose_Correct
+      const double zetaf = (temperature - th.temp) / th.q - th.dump * th.z[0];
+      const double dz2 = zetaf - th.z[1];
+      th.z[0] = th.z[0] + G40 * dz2;
+      th.z[1] = zetaf;
+      th.z[2] = th.z[2] + G42 * dz2;
+      th.z[3] = th.z[3] + G43 * dz2;
+      th.z[4] = th.z[4] + G44 * dz2;
+      th.zsum = th.zsum + th.z[0];
+    }
+    double nose_ek = 0.0, nose_ep = 0.0;
+    if (th.kind == G6_NOSE) {
+      nose_ek = (th.z[0] * th.z[0] * th.q * dt * dof * 0.5) * RGAS;
+      nose_ep = (dof * th.temp * (th.zsum - 0.5 * th.z[0]) * dt) * RGAS;
+    }
+    if (a.log && step < logcap) {
+      double* lg = a.log + ((size_t)step * nrep + rr) * G6_LOG_WIDTH;
+      lg[0] = s[0]; lg[1] = ekt; lg[2] = ekr; lg[3] = temperature; lg[4] = pressure;
+      lg[5] = (s[0] + ekt + ekr) * I2J + nose_ep + nose_ek;
+      lg[6] = s[23]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
+    }
+    if (predict_next && th.kind == G6_NOSE) {   // Nose_Predict for the next step
+      th.z[0] = th.z[0] + th.z[1] + th.z[2] + th.z[3] + th.z[4];
+      th.z[1] = th.z[1] + 2.0 * th.z[2] + 3.0 * th.z[3] + 4.0 * th.z[4];
+      th.z[2] = th.z[2] + 3.0 * th.z[3] + 6.0 * th.z[4];
+      th.z[3] = th.z[3] + 4.0 * th.z[4];
+    }
+  }
+  if (threadIdx.x == 0) {
+    a.ctrl[0] = (predict_next && gmax > a.half_skin2) ? 1 : 0;
+    a.ctrl[1] = step + 1;
+    *a.done = 0u;
+  }
+}
+
+#undef G6_ST
+
+}  // namespace g6

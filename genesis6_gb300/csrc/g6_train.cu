@@ -23,24 +23,6 @@
 
 namespace g6 {
 
-struct TrainArgs {
-  int nrows;              // 2 * records in the batch (row 2i = x, row 2i+1 = x')
-  const float* rec;       // records (MLP_REC floats each), batch view
-  const int* idx;         // optional permutation: record index of batch entry b
-  const float* w;         // parameters
-  const float* mean;      // feature normalisation
-  const float* istd;
-  double s0t, s0r;
-  float* X;               // [rows][IN] normalised inputs
-  float* H1;              // [rows][H]
-  float* H2;              // [rows][H]
-  float* Z;               // [rows][OUT]
-  float* G3;              // [rows][OUT] dL/dz
-  float* D2;              // [rows][H]
-  float* D1;              // [rows][H]
-  float* grad;            // [NPARAM]
-  double* loss;           // accumulated sum of -J over the batch
-};
 
 __device__ __forceinline__ const float* row_feat(const TrainArgs& a, int row) {
   const int b = row >> 1;

@@ -162,12 +162,22 @@ int g6_md_advance(g6_ctx* ctx, int nsteps);
 int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log);
 /* The cudaStream_t (as void*) on which the context enqueues its work. */
 int g6_stream(g6_ctx* ctx, void** stream);
-/* Per-step kernel timing: g6_set_timing(ctx, m) arms CUDA events around the
-   force kernel of the next m MD steps (those steps launch without a CUDA
-   graph); g6_get_timing returns their durations in ms (count = steps timed).
-   g6_set_timing(ctx, 0) disarms. */
-int g6_set_timing(g6_ctx* ctx, int max_steps);
-int g6_get_timing(g6_ctx* ctx, double* ms, int cap, int* count);
+/* Step timing: with g6_set_step_timing(ctx, 1) every MD step runs as its own
+   one-step CUDA graph that records events around the whole step and around
+   the fused force/integrator kernel; g6_step_times waits for the last step
+   and returns both durations in ms. */
+int g6_set_step_timing(g6_ctx* ctx, int on);
+int g6_step_times(g6_ctx* ctx, double* step_ms, double* kernel_ms);
+/* Duration (ms, CUDA events on the context's stream) of one launch of the
+   force kernel on the current configuration and neighbour list. */
+int g6_time_force(g6_ctx* ctx, double* ms);
+/* Lanes cooperating on one molecule in the force kernel (4, 8, 16 or 32).
+   g6_tune times each choice on the uploaded configuration and keeps the
+   fastest; g6_set_lpi fixes it.  Without either, the first force evaluation
+   picks a value from the system size.  (Per-lane partial sums change with
+   it, so results differ at rounding level between choices.) */
+int g6_tune(g6_ctx* ctx, int* lpi);
+int g6_set_lpi(g6_ctx* ctx, int lpi);
 
 /* One MD step with the state in caller-owned host memory: uploads rec,
    advances one step, downloads rec and the step's log record.  This is the
@@ -182,6 +192,53 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
    (optional) gets 1 for each lower member of an accepted pair. */
 int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
                         g6_thermostat* thermo, int* accepted);
+
+/* Monte Carlo, mc2.F90:544-832: the replicas of the context are independent
+   chains; each advances ntrial single-molecule trials (uniform target,
+   Gaussian translation of per-axis width sigma_t [A], rotation vector of
+   per-axis width sigma_r [rad] applied with qinfrotator + qadd,
+   QuatModule.F90:108-223) under an exact Metropolis-Hastings test at
+   beta[r] [1/K] (acceptance exp(-dE*I2J*J2K*beta), mc2.F90:712-722).  dE sums
+   the PairPotential energies of the target at both poses against every other
+   molecule of its chain, so no stored pair table is needed and the chain is
+   exact; the reference's per-trial width adaptation (mc2.F90:794-810) is not
+   applied.  Modes: G6_MC_PLAIN uses sigma_t/sigma_r; G6_MC_LEARNED takes the
+   widths from the network (g6_mlp_*) evaluated at the old pose, with the
+   reverse density at the new pose in the Hastings ratio; G6_MC_COLLECT runs
+   the plain proposal and stores one training record per trial.  Draws come
+   from Philox4x32-10 (key = seed, counter = chain, trial, draw).
+   samples (optional, nrep x ntrial/sample_every) gets the running energy,
+   counts (optional, nrep x 2) accepted/attempted, energy (optional, nrep) the
+   final energies, trace (optional, nrep x ntrial x 4) per trial dE, energy,
+   accepted flag and target index. */
+#define G6_MC_PLAIN 0
+#define G6_MC_LEARNED 1
+#define G6_MC_COLLECT 2
+int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const double* beta, const double* sigma_t,
+              const double* sigma_r, int mode, int sample_every, double* samples, int64_t* counts, double* energy,
+              double* trace);
+
+/* Proposal-width network: 24 local-environment features -> 64 -> 64 (tanh)
+   -> 2 widths, sigma = sigma0 * (0.5 + 2 sigmoid(z)).  Parameters are one
+   float array of G6_MLP_NPARAM values: W1[64][24], b1[64], W2[64][64],
+   b2[64], W3[2][64], b3[2]; features are normalised with feat_mean and
+   feat_inv_std.  A training record is G6_MLP_RECORD floats: features at the
+   old and at the proposed pose, |translation|^2, |rotation vector|^2 and
+   beta*dE. */
+#define G6_MLP_NPARAM 5890
+#define G6_MLP_NFEAT 24
+#define G6_MLP_RECORD 51
+int g6_mlp_set(g6_ctx* ctx, const float* params, const float* feat_mean, const float* feat_inv_std, double sigma0_t,
+               double sigma0_r);
+int g6_mlp_get(g6_ctx* ctx, float* params, float* feat_mean, float* feat_inv_std);
+/* Copy up to cap collected records to host (count = records held); cap < 0 discards them. */
+int g6_mlp_records(g6_ctx* ctx, float* host, int64_t cap, int64_t* count);
+/* Mean loss and its gradient over caller records (host) with the current parameters. */
+int g6_mlp_grad(g6_ctx* ctx, const float* records, int64_t nrec, float* grad, double* loss);
+/* Train on the collected records with Adam (hand-written forward/backward
+   kernels); loss (optional, epochs) gets the mean loss of each epoch. */
+int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, double sigma0_t, double sigma0_r,
+                 double* loss);
 
 /* Force evaluation that allocates no device memory.  No counterpart in the
    reference: it exists for callers that may not call cudaMalloc -- programs

@@ -3,10 +3,13 @@
 The oracle is an FP64 C++ restatement of Genesis6's Fortran (g6_oracle.cpp,
 every function cites the reference file:line it follows).  It exists to check
 the CUDA library: only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline
-leg of ``bench.py`` may load it.  Parity is pinned by closed-form dimer vectors
-(tests/golden) and by the reference's own self-consistency checks restated as
-tests, because the reference ships no test vectors and its Fortran cannot be
-compiled here.
+leg of ``bench.py`` may load it.
+
+Parity unpinned: the reference ships no test vectors and its Fortran cannot be
+compiled here, so no output of the reference itself pins this restatement.  It
+is checked against independently computed closed-form dimer vectors
+(tests/golden) and the reference's own self-consistency checks restated as
+tests.
 """
 from __future__ import annotations
 
@@ -67,6 +70,8 @@ def lib():
         L.orc_molecule_energy.argtypes = [c_int, c_int, c_int, dp, dp, c_int, dp, dp, dp, c_double, c_double]
         L.orc_md_run_threaded.argtypes = [c_int, c_int, dp, dp, dp, c_double, c_double, c_double, c_int, dp, dp,
                                           c_int]
+        L.orc_mc_run.argtypes = [c_int, c_int, c_int, dp, dp, dp, c_double, c_double, c_double, c_double, c_double,
+                                 c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, dp, dp]
         L.orc_max_threads.restype = c_int
         _lib = L
     return _lib
@@ -213,6 +218,17 @@ def molecule_energy(model, path, com, quat, t, com_t, quat_t, L, rin, rc):
     com = _f64(com); quat = _f64(quat)
     return lib().orc_molecule_energy(MODEL[model], PATH[path], com.shape[0], com, quat, int(t), _f64(com_t),
                                      _f64(quat_t), _f64(L), rin, rc)
+
+
+def mc_run(model, path, com, quat, L, rin, rc, beta, sig_t, sig_r, ntrial, seed, chain, counter, energy):
+    """One Monte Carlo chain on the CPU (same draws as the device).  Returns com, quat, energy, trace (ntrial,4)."""
+    com = np.ascontiguousarray(com, dtype=np.float64).copy()
+    quat = np.ascontiguousarray(quat, dtype=np.float64).copy()
+    e = np.array([energy], dtype=np.float64)
+    trace = np.zeros((ntrial, 4))
+    lib().orc_mc_run(MODEL[model], PATH[path], com.shape[0], com, quat, _f64(L), rin, rc, beta, sig_t, sig_r, ntrial,
+                     seed, chain, counter, e, trace)
+    return com, quat, e[0], trace
 
 
 def max_threads() -> int:

@@ -4,8 +4,9 @@
 // (libg6gpu.so) is compared against.  Only tests/, __graft_entry__.smoke() and
 // the CPU-baseline leg of bench.py load it.  The product path never calls it.
 //
-// Parity pins.  Genesis6 ships no test vectors and its Fortran cannot be
-// compiled here (no Fortran compiler), so this restatement is pinned by
+// PARITY UNPINNED: Genesis6 ships no test vectors and its Fortran cannot be
+// compiled or run here (no Fortran compiler), so no output of the reference
+// itself exists to pin this restatement against.  It is checked instead by
 //   (1) dimer energies/forces computed independently in closed form
 //       (tests/golden/make_golden.py -> tests/golden/*.json),
 //   (2) the reference's own in-code self-checks restated as tests
@@ -1252,6 +1253,60 @@ int orc_md_run_threaded(int model, int n, double* rec, const double* L, const do
     }
   }
   thermo[4] = th.z0; thermo[5] = th.z1; thermo[6] = th.z2; thermo[7] = th.z3; thermo[8] = th.z4; thermo[9] = th.zsum;
+  return 0;
+}
+
+// Monte Carlo chain, the trial/accept algorithm of mc2.F90:544-832 with the
+// device's conventions: Philox draws (counter = chain, trial, draw), fixed
+// widths, dE = E(target at new pose) - E(target at old pose) over every other
+// molecule.  com (n,3) and quat (n,4) are updated in place; energy (1) is the
+// running total; trace (ntrial,4) gets dE, energy, accepted, target.
+int orc_mc_run(int model, int path, int n, double* com, double* quat, const double* L, double rin, double rc,
+               double beta, double sig_t, double sig_r, int ntrial, uint64_t seed, uint32_t chain, uint64_t counter,
+               double* energy, double* trace) {
+  Model m;
+  if (!make_model(model, m)) return 1;
+  double e = *energy;
+  for (int t = 0; t < ntrial; ++t) {
+    const uint64_t trial = counter + (uint64_t)t;
+    const uint32_t lo = (uint32_t)trial, hi = (uint32_t)(trial >> 32);
+    double u0[2];
+    uniform2(seed, chain, lo, hi, 0u, u0);
+    int tg = (int)(u0[0] * n);
+    if (tg >= n) tg = n - 1;   // mc2.F90:551 could select n+1 (1-based) when the uniform is 1
+    double rot[3], dx[3];
+    for (int k = 0; k < 3; ++k) {
+      double u[2];
+      uniform2(seed, chain, lo, hi, 1u + k, u);
+      rot[k] = random_normal(0.0, sig_r * sig_r, u[0], u[1]);
+    }
+    for (int k = 0; k < 3; ++k) {
+      double u[2];
+      uniform2(seed, chain, lo, hi, 4u + k, u);
+      dx[k] = random_normal(0.0, sig_t * sig_t, u[0], u[1]);
+    }
+    // qinfrotator (QuatModule.F90:203-211) then qadd (:108-133)
+    double a = 1.0, b = rot[0], c = rot[1], d = rot[2];
+    const double r = 1.0 / std::sqrt(a * a + b * b + c * c + d * d);
+    a *= r; b *= r; c *= r; d *= r;
+    const double* qo = quat + 4 * tg;
+    double qn[4] = {a * qo[0] - b * qo[1] - c * qo[2] - d * qo[3], a * qo[1] + b * qo[0] + c * qo[3] - d * qo[2],
+                    a * qo[2] + c * qo[0] - b * qo[3] + d * qo[1], a * qo[3] + d * qo[0] + b * qo[2] - c * qo[1]};
+    if (qn[0] < 0) for (int k = 0; k < 4; ++k) qn[k] = -qn[k];
+    double cn[3] = {com[3 * tg] + dx[0], com[3 * tg + 1] + dx[1], com[3 * tg + 2] + dx[2]};
+    const double eo = orc_molecule_energy(model, path, n, com, quat, tg, com + 3 * tg, quat + 4 * tg, L, rin, rc);
+    const double en = orc_molecule_energy(model, path, n, com, quat, tg, cn, qn, L, rin, rc);
+    const double dE = en - eo;
+    const double x = -(dE * I2J * J2K) * beta;
+    const bool acc = x >= 0.0 || u0[1] < std::exp(x);
+    if (acc) {
+      for (int k = 0; k < 3; ++k) com[3 * tg + k] = cn[k];
+      for (int k = 0; k < 4; ++k) quat[4 * tg + k] = qn[k];
+      e += dE;
+    }
+    if (trace) { trace[4 * t] = dE; trace[4 * t + 1] = e; trace[4 * t + 2] = acc ? 1.0 : 0.0; trace[4 * t + 3] = tg; }
+  }
+  *energy = e;
   return 0;
 }
 

@@ -1,0 +1,110 @@
+"""FP64 NumPy reference of the learned-proposal pieces (test infrastructure).
+
+The device computes local-environment features, the 24-64-64-2 tanh network,
+its training loss and gradients in FP32 kernels (genesis6_gb300/csrc/g6_mlp.cuh,
+g6_train.cu).  This module restates each in FP64 so the tests can check the
+kernels: the gradient here is checked against finite differences of the loss
+here, and the device gradient against this one.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+NIN, NH, NOUT = 24, 64, 2
+W1, B1 = 0, NH * NIN
+W2 = B1 + NH
+B2 = W2 + NH * NH
+W3 = B2 + NH
+B3 = W3 + NOUT * NH
+NPARAM = B3 + NOUT
+RECORD = 2 * NIN + 3
+
+
+def unpack(p):
+    p = np.asarray(p, dtype=np.float64)
+    return (p[W1:B1].reshape(NH, NIN), p[B1:W2], p[W2:B2].reshape(NH, NH), p[B2:W3], p[W3:B3].reshape(NOUT, NH),
+            p[B3:NPARAM])
+
+
+def features(com_all, L, t, com, off_charged):
+    """Features of molecule t placed at `com` with lab offsets of its charged sites (NQ,3)."""
+    f = np.zeros(NIN)
+    u = np.zeros((4, 3))
+    for s in range(min(4, len(off_charged))):
+        u[s] = off_charged[s] / np.linalg.norm(off_charged[s])
+    for j in range(len(com_all)):
+        if j == t:
+            continue
+        d = com_all[j] - com
+        d = d - np.round(d / L) * L
+        r2 = d @ d
+        if r2 > 6.5 ** 2 or r2 <= 0:
+            continue
+        r = np.sqrt(r2)
+        f[:16] += np.exp(-((r - (2.4 + 0.25 * np.arange(16))) * 4.0) ** 2)
+        g1 = np.exp(-((r - 2.9) / 0.35) ** 2)
+        g2 = np.exp(-((r - 4.5) * 2.0) ** 2)
+        c = np.maximum(u @ d / r, 0.0)
+        f[16:20] += g1 * c ** 4
+        f[20:24] += g2 * c ** 4
+    return f
+
+
+def forward(p, x):
+    """x (B,24) normalised -> z (B,2), with activations for backprop."""
+    w1, b1, w2, b2, w3, b3 = unpack(p)
+    h1 = np.tanh(x @ w1.T + b1)
+    h2 = np.tanh(h1 @ w2.T + b2)
+    z = h2 @ w3.T + b3
+    return z, (x, h1, h2)
+
+
+def widths(z, s0t, s0r):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return s0t * (0.5 + 2.0 * s[..., 0]), s0r * (0.5 + 2.0 * s[..., 1])
+
+
+def loss_and_grad(p, rec, mean, istd, s0t, s0r):
+    """Mean over records of -J (g6_train.cu) and its gradient w.r.t. the parameters."""
+    rec = np.asarray(rec, dtype=np.float64)
+    B = rec.shape[0]
+    xo = (rec[:, :NIN] - mean) * istd
+    xn = (rec[:, NIN:2 * NIN] - mean) * istd
+    d2, r2, bde = rec[:, 2 * NIN], rec[:, 2 * NIN + 1], rec[:, 2 * NIN + 2]
+    zo, ao = forward(p, xo)
+    zn, an = forward(p, xn)
+    sg_o = 1.0 / (1.0 + np.exp(-zo))
+    sg_n = 1.0 / (1.0 + np.exp(-zn))
+    so = np.stack([s0t * (0.5 + 2 * sg_o[:, 0]), s0r * (0.5 + 2 * sg_o[:, 1])], 1)
+    sn = np.stack([s0t * (0.5 + 2 * sg_n[:, 0]), s0r * (0.5 + 2 * sg_n[:, 1])], 1)
+
+    def logq(s):
+        return -3 * np.log(s[:, 0]) - d2 / (2 * s[:, 0] ** 2) - 3 * np.log(s[:, 1]) - r2 / (2 * s[:, 1] ** 2)
+
+    lq0 = -3 * np.log(s0t) - d2 / (2 * s0t ** 2) - 3 * np.log(s0r) - r2 / (2 * s0r ** 2)
+    lf = logq(so) - lq0
+    lr = logq(sn) - bde - lq0
+    use_o = lf <= lr
+    l = np.where(use_o, lf, lr)
+    D = d2 / s0t ** 2 + r2 / s0r ** 2
+    J = np.exp(np.minimum(l, 30.0)) * D
+    loss = -J.mean()
+    s_act = np.where(use_o[:, None], so, sn)
+    sg_act = np.where(use_o[:, None], sg_o, sg_n)
+    dls = np.stack([-3 / s_act[:, 0] + d2 / s_act[:, 0] ** 3, -3 / s_act[:, 1] + r2 / s_act[:, 1] ** 3], 1)
+    dsdz = np.stack([s0t, s0r])[None, :] * 2 * sg_act * (1 - sg_act)
+    gz = (-J[:, None] * dls * dsdz) / B
+    gzo = np.where(use_o[:, None], gz, 0.0)
+    gzn = np.where(use_o[:, None], 0.0, gz)
+    g = np.zeros(NPARAM)
+    w1, b1, w2, b2, w3, b3 = unpack(p)
+    for gzs, (x, h1, h2) in ((gzo, ao), (gzn, an)):
+        g[W3:B3] += (gzs.T @ h2).ravel()
+        g[B3:NPARAM] += gzs.sum(0)
+        d2h = (gzs @ w3) * (1 - h2 ** 2)
+        g[W2:B2] += (d2h.T @ h1).ravel()
+        g[B2:W3] += d2h.sum(0)
+        d1h = (d2h @ w2) * (1 - h1 ** 2)
+        g[W1:B1] += (d1h.T @ x).ravel()
+        g[B1:W2] += d1h.sum(0)
+    return loss, g

@@ -1,0 +1,139 @@
+"""GPU Monte Carlo and learned proposal widths against the CPU references.
+
+- plain MC in FP64 replays the oracle's chain (same Philox draws) trial by trial;
+- the running energy stays equal to a full recomputation (the reference's
+  incremental-vs-full check, mc2.F90:489-505);
+- training records carry the features of the reference formulas (oracle/mlp.py);
+- the device gradient of the training loss matches the FP64 reference;
+- training lowers the loss and the learned sampler keeps the energy consistent.
+"""
+import numpy as np
+import pytest
+
+import genesis6_gb300 as g6
+from genesis6_gb300 import _capi, config
+from genesis6_gb300._capi import dptr, fptr
+from oracle import mlp
+
+pytestmark = pytest.mark.gpu
+
+
+def _chains(model, nrep, n, seed, prec="fp64", jitter=0.3):
+    boxes, recs = [], []
+    for r in range(nrep):
+        b = config.water_box(model, n, seed + r, jitter=jitter)
+        boxes.append(b["L"]); recs.append(b)
+    L = boxes[0][0]
+    rc = 0.5 * L
+    s = g6.RigidWater(model, [n] * nrep, np.array(boxes), path="custom", precision=prec, rc=rc, skin=0.0)
+    s.upload_state(np.concatenate([b["rec"] for b in recs]))
+    return s, recs, rc
+
+
+def _mc(s, ntrial, seed, counter, beta, st, sr, mode=_capi.MC_PLAIN, sample_every=0):
+    R = s.nrep
+    beta = np.full(R, beta); st = np.full(R, st); sr = np.full(R, sr)
+    counts = np.zeros(2 * R, np.int64); energy = np.zeros(R); trace = np.zeros((R, ntrial, 4))
+    nsm = ntrial // sample_every if sample_every else 0
+    samples = np.zeros((R, max(nsm, 1)))
+    import ctypes
+    s._check(s.L.g6_mc_run(s.ctx, ntrial, seed, counter, dptr(beta), dptr(st), dptr(sr), mode, sample_every,
+                           dptr(samples) if nsm else None,
+                           counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(energy), dptr(trace)))
+    return counts.reshape(R, 2), energy, trace, samples
+
+
+def test_mc_fp64_replays_oracle(orc):
+    s, recs, rc = _chains("ST2", 2, 216, 40)
+    beta = 1.0 / 260.0
+    ntrial = 300
+    counts, energy, trace, _ = _mc(s, ntrial, 99, 0, beta, 0.15, 0.15)
+    rec_g = s.download_state()
+    for c, b in enumerate(recs):
+        L = b["L"]
+        E0 = orc.compute("ST2", "custom", b["com"], b["quat"], L, [rc] * 3, rc - 2.0, rc)[2]
+        com, quat, e, tr = orc.mc_run("ST2", "custom", b["com"], b["quat"], L, rc - 2.0, rc, beta, 0.15, 0.15, ntrial,
+                                      99, c, 0, E0)
+        assert np.array_equal(trace[c, :, 3], tr[:, 3])          # same targets
+        assert np.array_equal(trace[c, :, 2], tr[:, 2])          # same decisions
+        assert np.abs(trace[c, :, 0] - tr[:, 0]).max() <= 1e-9 * np.abs(tr[:, 0]).max()
+        assert energy[c] == pytest.approx(e, rel=1e-10)
+        sl = rec_g[216 * c:216 * (c + 1)]
+        assert np.abs(sl[:, :3] - com).max() < 1e-10
+        assert np.abs(sl[:, 33:37] - quat).max() < 1e-10
+        assert counts[c, 1] == ntrial and counts[c, 0] == int(tr[:, 2].sum())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_mc_running_energy_matches_full(prec):
+    s, recs, rc = _chains("ST2", 4, 343, 50, prec=prec)
+    counts, energy, trace, samples = _mc(s, 1500, 5, 0, 1.0 / 260.0, 0.15, 0.15, sample_every=100)
+    F, tau, ep, vir = s.force()
+    tol = 1e-10 if prec == "fp64" else 2e-5
+    for c in range(4):
+        assert energy[c] == pytest.approx(ep[c], rel=tol, abs=tol * 1e3)
+        assert samples[c, -1] == energy[c]
+    acc = counts[:, 0] / counts[:, 1]
+    assert (acc > 0.2).all() and (acc < 0.95).all()
+
+
+def test_collect_records_hold_reference_features(orc):
+    s, recs, rc = _chains("ST2", 1, 216, 60)
+    b = recs[0]
+    _mc(s, 1, 3, 0, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_COLLECT)
+    rec = np.zeros((4, mlp.RECORD), np.float32)
+    import ctypes
+    cnt = ctypes.c_int64()
+    s._check(s.L.g6_mlp_records(s.ctx, fptr(rec), 4, ctypes.byref(cnt)))
+    assert cnt.value == 1
+    # target and move from the same Philox draws as the device
+    u = orc.philox_uniform2(3, 0, 0, 0, 0)
+    t = min(int(u[0] * 216), 215)
+    sx, sy, sz, intra, tmat = orc.place_sites("ST2", b["com"], b["quat"])
+    fo = mlp.features(b["com"], b["L"], t, b["com"][t], intra[t, 1:5])
+    assert np.allclose(rec[0, :mlp.NIN], fo, rtol=2e-4, atol=2e-4)
+    rot = []; dx = []
+    for k in range(3):
+        a = orc.philox_uniform2(3, 0, 0, 0, 1 + k)
+        rot.append(np.sqrt(-2 * np.log(a[0])) * np.sin(2 * np.pi * a[1]) * 0.15)
+    for k in range(3):
+        a = orc.philox_uniform2(3, 0, 0, 0, 4 + k)
+        dx.append(np.sqrt(-2 * np.log(a[0])) * np.sin(2 * np.pi * a[1]) * 0.15)
+    assert rec[0, 2 * mlp.NIN] == pytest.approx(np.sum(np.square(dx)), rel=1e-5)
+    assert rec[0, 2 * mlp.NIN + 1] == pytest.approx(np.sum(np.square(rot)), rel=1e-5)
+
+
+def test_mlp_gradient_matches_reference():
+    s, recs, rc = _chains("ST2", 1, 216, 70)
+    rng = np.random.default_rng(1)
+    n = 512
+    rec = np.zeros((n, mlp.RECORD))
+    rec[:, :2 * mlp.NIN] = rng.uniform(0, 3, (n, 2 * mlp.NIN))
+    rec[:, 2 * mlp.NIN] = rng.chisquare(3, n) * 0.15 ** 2
+    rec[:, 2 * mlp.NIN + 1] = rng.chisquare(3, n) * 0.15 ** 2
+    rec[:, 2 * mlp.NIN + 2] = rng.normal(0.5, 1.5, n)
+    p = rng.normal(0, 0.2, mlp.NPARAM).astype(np.float32)
+    mean = rec[:, :mlp.NIN].mean(0).astype(np.float32); istd = (1 / rec[:, :mlp.NIN].std(0)).astype(np.float32)
+    s._check(s.L.g6_mlp_set(s.ctx, fptr(p), fptr(mean), fptr(istd), 0.15, 0.15))
+    rec32 = rec.astype(np.float32)
+    g = np.zeros(mlp.NPARAM, np.float32)
+    loss = np.zeros(1)
+    s._check(s.L.g6_mlp_grad(s.ctx, fptr(rec32), n, fptr(g), dptr(loss)))
+    lref, gref = mlp.loss_and_grad(p.astype(np.float64), rec32.astype(np.float64), mean.astype(np.float64),
+                                   istd.astype(np.float64), 0.15, 0.15)
+    assert loss[0] == pytest.approx(lref, rel=1e-4)
+    assert np.abs(g - gref).max() <= 2e-3 * np.abs(gref).max()
+
+
+def test_training_lowers_loss_and_learned_chain_is_consistent():
+    s, recs, rc = _chains("ST2", 8, 216, 80, prec="mixed")
+    _mc(s, 2000, 11, 0, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_COLLECT)
+    loss = np.zeros(6)
+    s._check(s.L.g6_mlp_train(s.ctx, 6, 256, 3e-3, 7, 0.15, 0.15, dptr(loss)))
+    assert np.isfinite(loss).all()
+    assert loss[-1] < loss[0]
+    counts, energy, trace, _ = _mc(s, 1000, 12, 10 ** 6, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_LEARNED)
+    F, tau, ep, vir = s.force()
+    for c in range(8):
+        assert energy[c] == pytest.approx(ep[c], rel=2e-5, abs=0.05)
+    assert (counts[:, 0] > 0).all()
