@@ -347,14 +347,17 @@ def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
             "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed"}
 
 
-def bench_mc(torch, seed=20261203, sweeps=120, records=1_000_000):
+def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=1500, w_energy=0.0):
     """32 chains x 1,024 ST2 (custom path, Coulomb taper), 260 K, rc = L/2 with a
-    2 A switch: fixed widths (0.15 A, 0.15 rad) vs widths from the MLP trained on
-    `records` plain-sampler moves.  ESS of U per GPU-second (U sampled every
+    2 A switch.  Chains are equilibrated from the lattice with the fixed widths,
+    then the MLP is trained on `records` plain-sampler moves and both samplers
+    run `sweeps` sweeps from the same equilibrated state: fixed widths (0.15 A,
+    0.15 rad) vs the learned widths.  ESS of U per GPU-second (U sampled every
     sweep of 1,024 trials) and <U> of both."""
     import genesis6_gb300 as g6
     from genesis6_gb300 import _capi, config
     C, N = 32, 1024
+    NF, NREC = _capi.MLP_NFEAT, _capi.MLP_RECORD
     boxes, recs = [], []
     for c in range(C):
         b = config.water_box("ST2", N, seed + 500 + c, temp=260.0)
@@ -374,38 +377,55 @@ def bench_mc(torch, seed=20261203, sweeps=120, records=1_000_000):
                                mode, sample_every, _capi.dptr(samples) if nsm else None,
                                counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _capi.dptr(energy), None))
         return samples, counts.reshape(C, 2).copy()
-    run(30 * N, _capi.MC_PLAIN, 0)                                   # equilibration
+    t0 = time.perf_counter()
+    eq, _ = run(equil_sweeps * N, _capi.MC_PLAIN, 0, sample_every=N)      # equilibration from the lattice
+    torch.cuda.synchronize()
+    t_equil = time.perf_counter() - t0
     rec_state = s.download_state()
     ntr = records // C
-    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    run(ntr, _capi.MC_COLLECT, 10 ** 7)                              # training records
+    run(ntr, _capi.MC_COLLECT, 10 ** 8)                                   # training records
     loss = np.zeros(8)
+    s._check(s.L.g6_mlp_objective(s.ctx, 1.0, w_energy))
     s._check(s.L.g6_mlp_train(s.ctx, 8, 1024, 2e-3, seed, 0.15, 0.15, _capi.dptr(loss)))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    # widths the trained network gives on the collected (plain-sampler) configurations
+    nrec = min(200_000, ntr * C)
+    rec = np.zeros((nrec, NREC), np.float32)
+    cnt = ctypes.c_int64()
+    s._check(s.L.g6_mlp_records(s.ctx, _capi.fptr(rec), nrec, ctypes.byref(cnt)))
+    feat = np.ascontiguousarray(rec[:, :NF])
+    wt = np.zeros(nrec); wr = np.zeros(nrec)
+    s._check(s.L.g6_mlp_widths(s.ctx, _capi.fptr(feat), nrec, _capi.dptr(wt), _capi.dptr(wr)))
     out = {}
     for name, mode in (("fixed", _capi.MC_PLAIN), ("learned", _capi.MC_LEARNED)):
         s.upload_state(rec_state)
-        run(2 * N, mode, 2 * 10 ** 7)                                # settle the sampler
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        samples, cnt = run(sweeps * N, mode, 3 * 10 ** 7, sample_every=N)
+        samples, cnt = run(sweeps * N, mode, 3 * 10 ** 8, sample_every=N)
         torch.cuda.synchronize()
         gpu_s = time.perf_counter() - t0
         ess = np.array([ess_geyer(samples[c]) for c in range(C)])
         u = samples.mean(1)
         var_mean = np.array([np.var(samples[c]) / max(ess[c], 1.0) for c in range(C)])
         out[name] = {"ess_total": float(ess.sum()), "gpu_seconds": gpu_s, "ess_per_gpu_s": float(ess.sum() / gpu_s),
+                     "us_per_trial": gpu_s / (sweeps * N) * 1e6,
                      "mean_U_internal": float(u.mean()), "stderr_U": float(np.sqrt(var_mean.sum()) / C),
                      "acceptance": float(cnt[:, 0].sum() / cnt[:, 1].sum()), "sweeps": sweeps}
     s.close()
     d = abs(out["learned"]["mean_U_internal"] - out["fixed"]["mean_U_internal"])
     sig = np.hypot(out["learned"]["stderr_U"], out["fixed"]["stderr_U"])
+    drift = float(eq[:, -100:].mean() - eq[:, -200:-100].mean()) / C if eq.shape[1] >= 200 else None
     return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": 260.0,
-            "rc_A": 0.5 * L, "training_records": ntr * C, "training_loss_first_last": [float(loss[0]),
-                                                                                     float(loss[-1])],
-            "collect_and_train_seconds": t_train, "fixed": out["fixed"], "learned": out["learned"],
+            "rc_A": 0.5 * L, "equilibration_sweeps": equil_sweeps, "equilibration_seconds": t_equil,
+            "U_drift_last_100_sweeps_per_chain": drift,
+            "training_records": ntr * C, "objective": {"w_move": 1.0, "w_energy": w_energy},
+            "training_loss_first_last": [float(loss[0]), float(loss[-1])],
+            "collect_and_train_seconds": t_train,
+            "learned_widths_on_records": {"sigma_t_mean": float(wt.mean()), "sigma_t_p10_p90": [float(np.percentile(wt, 10)), float(np.percentile(wt, 90))],
+                                          "sigma_r_mean": float(wr.mean()), "sigma_r_p10_p90": [float(np.percentile(wr, 10)), float(np.percentile(wr, 90))]},
+            "fixed": out["fixed"], "learned": out["learned"],
             "ess_per_gpu_s_learned_over_fixed": out["learned"]["ess_per_gpu_s"] / out["fixed"]["ess_per_gpu_s"],
             "mean_U_difference_in_sigma": float(d / sig) if sig > 0 else None,
             "U_unit": "10 J/mol per chain (internal)"}

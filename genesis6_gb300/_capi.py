@@ -34,7 +34,7 @@ SYMBOLS = [
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
     "g6_molecule_energies", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
-    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get",
+    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
     "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
 ]
 
@@ -104,6 +104,8 @@ def lib():
     fp = ctypes.POINTER(ctypes.c_float)
     L.g6_mlp_set.argtypes = [vp, fp, fp, fp, ctypes.c_double, ctypes.c_double]
     L.g6_mlp_get.argtypes = [vp, fp, fp, fp]
+    L.g6_mlp_objective.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    L.g6_mlp_widths.argtypes = [vp, fp, ctypes.c_int64, dp, dp]
     L.g6_mlp_records.argtypes = [vp, fp, i64, ctypes.POINTER(i64)]
     L.g6_mlp_grad.argtypes = [vp, fp, i64, fp, dp]
     L.g6_mlp_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_double,

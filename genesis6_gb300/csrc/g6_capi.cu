@@ -183,7 +183,8 @@ struct g6_ctx {
   double req = 0.0, skin = 1.0;
   std::vector<int> off;
   std::vector<double> L;
-  int lpi = 0;                    // lanes per molecule in the force kernel (0 = tune)
+  int lpi = 0;                    // lanes per molecule in the force kernel (0 = default)
+  int step_lpi = 0;               // lanes per molecule in the fused MD step kernel (0 = default)
   int coop_grid = 0;              // blocks of the cooperative rebuild kernel
   // device arrays
   int* d_off = nullptr; int* d_mol_rep = nullptr; double* d_L = nullptr; double* d_invL = nullptr;
@@ -201,6 +202,8 @@ struct g6_ctx {
   // neighbour list
   int cap = 0;
   int* d_nbr = nullptr; int* d_nnb = nullptr; double* d_com_build = nullptr; int* d_overflow = nullptr;
+  uint32_t* d_fix_build = nullptr;
+  float* d_stf = nullptr;   // mixed precision: small Gear terms during a run
   // reductions and control
   int nblk = 0;
   double* d_part = nullptr; double* d_partmax = nullptr; double* d_red = nullptr;
@@ -214,9 +217,11 @@ struct g6_ctx {
   double* d_trace = nullptr; size_t trace_cap = 0;
   float* d_rec = nullptr; size_t rec_cap = 0; long long nrec = 0;   // training records
   float* d_mlp = nullptr;          // parameters
-  float* d_mlp_zero = nullptr;     // constant-width network (plain proposal with records)
+  int* d_fcache = nullptr;         // per-molecule features at the current pose (Monte Carlo)
+  int* d_mcflag = nullptr;         // Monte Carlo: too many feature neighbours
   float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
   double sig0_t = 0.15, sig0_r = 0.15;
+  double obj_move = 1.0, obj_energy = 0.0;   // training objective weights (g6_mlp_objective)
   bool have_mlp = false;
   // pair set
   long long* d_pcnt = nullptr;
@@ -402,16 +407,18 @@ static int prepare_ref_grid(g6_ctx* ctx) {
 
 static PlaceArgs place_args(g6_ctx* c) {
   PlaceArgs p;
+  std::memset(&p, 0, sizeof p);
   p.n = c->n; p.nq = c->nq; p.npk = c->npk; p.w64 = c->w64;
   p.rep = rep_dev(c);
   for (int s = 0; s < MAXSITE; ++s)
-    for (int k = 0; k < 3; ++k) p.body[s][k] = c->mh.body[s][k];
+    for (int k = 0; k < 3; ++k) { p.body[s][k] = c->mh.body[s][k]; p.fbody[s][k] = (float)c->mh.body[s][k]; }
   p.st = c->d_st; p.tmat = c->d_tmat; p.pk64 = c->d_pk64; p.pk32 = c->d_pk32; p.fix = c->d_fix;
   return p;
 }
 
 static CellArgs cell_args(g6_ctx* c, HostGrid& g, const int* ctrl) {
   CellArgs a;
+  std::memset(&a, 0, sizeof a);
   a.n = c->n; a.rep = rep_dev(c); a.g = grid_dev(g); a.com = c->d_st;
   a.cell = g.d_cell; a.slot = g.d_slot; a.count = g.d_count; a.ctrl = ctrl;
   return a;
@@ -419,9 +426,11 @@ static CellArgs cell_args(g6_ctx* c, HostGrid& g, const int* ctrl) {
 
 static ListArgs list_args(g6_ctx* c, const int* ctrl) {
   ListArgs a;
+  std::memset(&a, 0, sizeof a);
   a.n = c->n; a.cap = c->cap; a.rep = rep_dev(c); a.g = grid_dev(c->glist); a.cell = c->glist.d_cell;
   a.start = c->glist.d_start; a.cellmol = c->glist.d_cellmol; a.fix = c->d_fix; a.fix1 = c->d_fix1; a.com = c->d_st;
   a.com_build = c->d_com_build;
+  a.fix_build = c->d_fix_build;
   const double rl = c->cc.rout + effective_skin(c);
   a.rlist2 = (float)(rl * rl) + 1e-3f;   // superset margin over the fixed-point rounding
   a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.overflow = c->d_overflow; a.ctrl = ctrl;
@@ -430,6 +439,7 @@ static ListArgs list_args(g6_ctx* c, const int* ctrl) {
 
 static ForceArgs force_args(g6_ctx* c) {
   ForceArgs a;
+  std::memset(&a, 0, sizeof a);
   a.n = c->n; a.cap = c->cap; a.stride_pk32 = c->npk; a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.rep = rep_dev(c);
   a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pk64_1 = c->d_pk64_1; a.pk32_1 = c->d_pk32_1; a.ctrl = nullptr;
   a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
@@ -584,6 +594,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_overflow, 1));
+  CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
   ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // blocks of the fused step kernel at 32 lanes/molecule
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
   CK(dalloc(ctx, &ctx->d_partmax, ctx->nblk)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
@@ -593,12 +604,8 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_pcnt, 2 * (size_t)n + 2));
   CK(dalloc(ctx, &ctx->d_sig_t, nrep)); CK(dalloc(ctx, &ctx->d_sig_r, nrep)); CK(dalloc(ctx, &ctx->d_energy, nrep));
   CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
-  CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_mlp_zero, MLP_NPARAM));
-  {
-    std::vector<float> z(MLP_NPARAM, 0.0f);
-    z[MLP_B3] = z[MLP_B3 + 1] = (float)std::log(0.25 / 0.75);   // sigma = sigma0 (0.5 + 2 * 0.25)
-    CK(cudaMemcpy(ctx->d_mlp_zero, z.data(), z.size() * sizeof(float), cudaMemcpyHostToDevice));
-  }
+  CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_fcache, (size_t)n * MLP_IN));
+  CK(dalloc(ctx, &ctx->d_mcflag, 1));
   ctx->last_epot.assign(nrep, 0.0);
   ctx->have_system = true;
   return G6_OK;
@@ -897,6 +904,8 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   a.tmat1 = ctx->d_tmat1; a.pk64_1 = ctx->d_pk64_1; a.pk32_1 = ctx->d_pk32_1; a.fix1 = ctx->d_fix1;
   a.mass = ctx->mh.mass; a.I[0] = ctx->mh.I[0]; a.I[1] = ctx->mh.I[1]; a.I[2] = ctx->mh.I[2]; a.dt = dt;
   a.com_build = ctx->d_com_build;
+  a.fix_build = ctx->d_fix_build;
+  a.stf = ctx->d_stf;
   const double hs = 0.5 * effective_skin(ctx);
   a.half_skin2 = hs * hs;
   a.th = ctx->d_th; a.part = ctx->d_part; a.partmax = ctx->d_partmax; a.red = ctx->d_red; a.done = ctx->d_done;
@@ -914,7 +923,7 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
   ForceArgs fa = force_args(ctx);
   fa.ctrl = ctx->d_ctrl;
   if (ev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
-  CK(launch_step(fa, sa, ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
+  CK(launch_step(fa, sa, ctx->model, ctx->prec == G6_MIXED, ctx->step_lpi, ctx->stream));
   if (ev) {
     CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
     CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
@@ -924,13 +933,33 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
 
 static const int GRAPH_STEPS = 16;
 
+// First predict + placement of a run.  Mixed runs first move the small Gear
+// terms into the float SoA; md_stop moves them back so that the FP64 state is
+// the complete record outside a run.
+static int md_start(g6_ctx* ctx) {
+  if (ctx->prec == G6_MIXED) {
+    CK(launch_stf_move(ctx->d_st, ctx->d_stf, ctx->n, 1, ctx->stream));
+    CK(launch_begin_mixed(place_args(ctx), ctx->d_stf, ctx->d_th, ctx->stream));
+  } else {
+    CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
+  }
+  return G6_OK;
+}
+
+static int md_stop(g6_ctx* ctx) {
+  if (ctx->prec == G6_MIXED) CK(launch_stf_move(ctx->d_st, ctx->d_stf, ctx->n, 0, ctx->stream));
+  return G6_OK;
+}
+
 static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log, uint64_t seed) {
   int rc = prepare_list(ctx);
   if (rc) return rc;
-  if (ctx->lpi == 0) {
+  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
+  if (ctx->step_lpi == 0) {
     const char* env = std::getenv("G6_LPI");
-    ctx->lpi = env ? std::atoi(env) : default_lpi(ctx);
-    if (ctx->lpi != 4 && ctx->lpi != 8 && ctx->lpi != 16 && ctx->lpi != 32) ctx->lpi = default_lpi(ctx);
+    ctx->step_lpi = env ? std::atoi(env) : default_lpi(ctx);
+    if (ctx->step_lpi != 4 && ctx->step_lpi != 8 && ctx->step_lpi != 16 && ctx->step_lpi != 32)
+      ctx->step_lpi = default_lpi(ctx);
   }
   std::vector<ThermoDev> th(ctx->nrep);
   for (int r = 0; r < ctx->nrep; ++r) {
@@ -1030,8 +1059,7 @@ int g6_md_begin(g6_ctx* ctx, double dt, int max_steps, const g6_thermostat* ther
   rc = md_prepare(ctx, dt, max_steps, const_cast<g6_thermostat*>(thermo), want_log != 0, 0);
   if (rc) return rc;
   ctx->run_dt = dt; ctx->run_log = want_log != 0; ctx->run_max = max_steps; ctx->run_done = 0; ctx->in_run = true;
-  CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
-  return G6_OK;
+  return md_start(ctx);
 }
 
 int g6_md_advance(g6_ctx* ctx, int nsteps) {
@@ -1048,7 +1076,9 @@ int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log) {
   if (!ctx || !ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_md_end without g6_md_begin");
   ctx->in_run = false;
   CK(cudaSetDevice(ctx->device));
-  int rc = md_finish(ctx, ctx->run_done, thermo, ctx->run_log ? log : nullptr);
+  int rc = md_stop(ctx);
+  if (rc) return rc;
+  rc = md_finish(ctx, ctx->run_done, thermo, ctx->run_log ? log : nullptr);
   if (rc) return rc;
   // every step but the last predicts the next one; the state is a corrected
   // (reference-consistent) state only after exactly max_steps steps
@@ -1104,10 +1134,12 @@ int g6_time_force(g6_ctx* ctx, double* ms) {
 int g6_tune(g6_ctx* ctx, int* lpi_out) {
   int rc = check_ready(ctx, true);
   if (rc) return rc;
+  if (ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_tune inside g6_md_begin/g6_md_end");
   if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
   rc = force_once(ctx);
   if (rc) return rc;
   const int cand[4] = {4, 8, 16, 32};
+  // force-only kernel
   int best = ctx->lpi;
   double tbest = 1e30;
   for (int k = 0; k < 4; ++k) {
@@ -1121,14 +1153,48 @@ int g6_tune(g6_ctx* ctx, int* lpi_out) {
     if (t < tbest) { tbest = t; best = cand[k]; }
   }
   ctx->lpi = best;
+  // fused MD step: short NVE runs from the current state, which is restored after
+  const size_t bytes = (size_t)REC * ctx->n * sizeof(double);
+  CK(cudaMemcpyAsync(ctx->d_stage, ctx->d_st, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  const unsigned long long steps0 = ctx->steps_done;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int sbest = ctx->step_lpi ? ctx->step_lpi : best;
+  float sb = 1e30f;
+  for (int k = 0; k < 4 && rc == G6_OK; ++k) {
+    ctx->step_lpi = cand[k];
+    drop_graphs(ctx);
+    const int warm = 2, timed = 10;
+    rc = g6_md_begin(ctx, 0.001, warm + timed, nullptr, 0);
+    if (rc == G6_OK) rc = g6_md_advance(ctx, warm);
+    if (rc == G6_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
+    if (rc == G6_OK) rc = g6_md_advance(ctx, timed);
+    if (rc == G6_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
+    if (ctx->in_run) { int r2 = g6_md_end(ctx, nullptr, nullptr); if (rc == G6_OK) rc = r2; }
+    if (rc == G6_OK) {
+      float ms = 0.0f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        rc = fail(ctx, G6_ERR_CUDA, "event timing");
+      else if (ms < sb) { sb = ms; sbest = cand[k]; }
+    }
+    cudaMemcpyAsync(ctx->d_st, ctx->d_stage, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->steps_done = steps0;
+  ctx->step_lpi = sbest;
   drop_graphs(ctx);
-  if (lpi_out) *lpi_out = best;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (rc) return rc;
+  if (lpi_out) *lpi_out = sbest;
   return G6_OK;
 }
 
 int g6_set_lpi(g6_ctx* ctx, int lpi) {
   if (!ctx || (lpi != 4 && lpi != 8 && lpi != 16 && lpi != 32)) return G6_ERR_ARG;
   ctx->lpi = lpi;
+  ctx->step_lpi = lpi;
   drop_graphs(ctx);
   return G6_OK;
 }
@@ -1144,7 +1210,7 @@ int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double*
   int rc = g6_md_begin(ctx, dt, nsteps, thermo, log != nullptr);
   if (rc) return rc;
   rc = g6_md_advance(ctx, nsteps);
-  if (rc) { ctx->in_run = false; cudaStreamSynchronize(ctx->stream); return rc; }
+  if (rc) { ctx->in_run = false; md_stop(ctx); cudaStreamSynchronize(ctx->stream); return rc; }
   return g6_md_end(ctx, thermo, log);
 }
 
@@ -1160,9 +1226,10 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   rc = md_prepare(ctx, dt, 1, thermo, log != nullptr, 0);
   if (rc) return rc;
   StepArgs sa = step_args(ctx, dt, log ? ctx->d_log : nullptr);
-  CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
+  if ((rc = md_start(ctx))) return rc;
   rc = enqueue_step(ctx, sa);
   if (rc) return rc;
+  if ((rc = md_stop(ctx))) return rc;
   CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
   CK(cudaMemcpyAsync(rec, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return md_finish(ctx, 1, thermo, log);
@@ -1219,10 +1286,10 @@ static int grow(g6_ctx* ctx, void** p, size_t* cap, size_t need_bytes, bool keep
   return G6_OK;
 }
 
-static MlpDev mlp_dev(g6_ctx* ctx, bool zero) {
+static MlpDev mlp_dev(g6_ctx* ctx) {
   MlpDev m;
-  m.w = zero ? ctx->d_mlp_zero : ctx->d_mlp;
-  for (int k = 0; k < MLP_IN; ++k) { m.feat_mean[k] = zero ? 0.0f : ctx->h_mean[k]; m.feat_inv_std[k] = zero ? 1.0f : ctx->h_istd[k]; }
+  m.w = ctx->d_mlp;
+  for (int k = 0; k < MLP_IN; ++k) { m.feat_mean[k] = ctx->h_mean[k]; m.feat_inv_std[k] = ctx->h_istd[k]; }
   m.sigma0_t = ctx->sig0_t; m.sigma0_r = ctx->sig0_r;
   return m;
 }
@@ -1276,9 +1343,13 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
   a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
   a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
-  a.mlp = mlp_dev(ctx, mode == G6_MC_COLLECT);
-  if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode != G6_MC_PLAIN, ctx->stream));
+  a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag;
+  a.mlp = mlp_dev(ctx);
+  CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
+  if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode, ctx->stream));
   std::vector<long long> cnt(2 * R);
+  int mcflag = 0;
+  CK(cudaMemcpyAsync(&mcflag, ctx->d_mcflag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(etot.data(), ctx->d_energy, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(cnt.data(), ctx->d_counts, 2 * R * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
   if (a.samples) CK(cudaMemcpyAsync(samples, ctx->d_samples, (size_t)R * nsamples * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1286,6 +1357,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   CK(cudaStreamSynchronize(ctx->stream));
   if (mode == G6_MC_COLLECT) ctx->nrec += (long long)R * ntrial;
   if (energy) for (int r = 0; r < R; ++r) energy[r] = etot[r];
+  if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 256 molecules within 6.5 A of a Monte Carlo pose");
   if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
   drop_graphs(ctx);   // poses changed outside the MD state machine
   return G6_OK;
@@ -1302,6 +1374,38 @@ int g6_mlp_set(g6_ctx* ctx, const float* params, const float* feat_mean, const f
   std::memcpy(ctx->h_istd, feat_inv_std, sizeof ctx->h_istd);
   ctx->sig0_t = sigma0_t; ctx->sig0_r = sigma0_r;
   ctx->have_mlp = true;
+  return G6_OK;
+}
+
+int g6_mlp_widths(g6_ctx* ctx, const float* features, int64_t n, double* sigma_t, double* sigma_r) {
+  if (!ctx || !ctx->have_system || !ctx->have_mlp) return fail(ctx, G6_ERR_STATE, "no system or network");
+  if (n < 0 || (n > 0 && (!features || !sigma_t || !sigma_r))) return fail(ctx, G6_ERR_ARG, "bad arguments");
+  if (n == 0) return G6_OK;
+  CK(cudaSetDevice(ctx->device));
+  float *df = nullptr, *dm = nullptr;
+  double* dw = nullptr;
+  cudaError_t e = cudaMalloc(&df, (size_t)n * MLP_IN * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dm, 2 * MLP_IN * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&dw, 2 * (size_t)n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpy(df, features, (size_t)n * MLP_IN * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dm, ctx->h_mean, MLP_IN * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dm + MLP_IN, ctx->h_istd, MLP_IN * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = launch_mlp_eval(df, n, ctx->d_mlp, dm, dm + MLP_IN, ctx->sig0_t, ctx->sig0_r, dw, dw + n, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(sigma_t, dw, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sigma_r, dw + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(df); cudaFree(dm); cudaFree(dw);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "g6_mlp_widths");
+  return G6_OK;
+}
+
+int g6_mlp_objective(g6_ctx* ctx, double w_move, double w_energy) {
+  if (!ctx) return G6_ERR_ARG;
+  if (!(w_move >= 0.0) || !(w_energy >= 0.0) || !(w_move + w_energy > 0.0))
+    return fail(ctx, G6_ERR_ARG, "objective weights must be >= 0 and not both 0");
+  ctx->obj_move = w_move;
+  ctx->obj_energy = w_energy;
   return G6_OK;
 }
 
@@ -1340,20 +1444,20 @@ struct TrainBuffers {
   }
 };
 
-static int train_buffers(g6_ctx* ctx, TrainBuffers& b, int batch) {
+static int train_buffers(g6_ctx* ctx, TrainBuffers& b, int batch, long long nidx) {
   const size_t rows = 2 * (size_t)batch;
   CK(b.get(&b.X, rows * MLP_IN)); CK(b.get(&b.H1, rows * MLP_H)); CK(b.get(&b.H2, rows * MLP_H));
   CK(b.get(&b.Z, rows * MLP_OUT)); CK(b.get(&b.G3, rows * MLP_OUT)); CK(b.get(&b.D2, rows * MLP_H));
   CK(b.get(&b.D1, rows * MLP_H)); CK(b.get(&b.grad, MLP_NPARAM)); CK(b.get(&b.m, MLP_NPARAM));
   CK(b.get(&b.v, MLP_NPARAM)); CK(b.get(&b.mean, MLP_IN)); CK(b.get(&b.istd, MLP_IN)); CK(b.get(&b.loss, 1));
-  CK(b.get(&b.idx, batch));
+  CK(b.get(&b.idx, (size_t)std::max<long long>(nidx, batch)));
   return G6_OK;
 }
 
 static TrainArgs train_args(g6_ctx* ctx, TrainBuffers& b, const float* rec, int nb, const int* idx) {
   TrainArgs t;
   t.nrows = 2 * nb; t.rec = rec; t.idx = idx; t.w = ctx->d_mlp; t.mean = b.mean; t.istd = b.istd;
-  t.s0t = ctx->sig0_t; t.s0r = ctx->sig0_r; t.X = b.X; t.H1 = b.H1; t.H2 = b.H2; t.Z = b.Z; t.G3 = b.G3;
+  t.s0t = ctx->sig0_t; t.s0r = ctx->sig0_r; t.w_move = ctx->obj_move; t.w_energy = ctx->obj_energy; t.X = b.X; t.H1 = b.H1; t.H2 = b.H2; t.Z = b.Z; t.G3 = b.G3;
   t.D2 = b.D2; t.D1 = b.D1; t.grad = b.grad; t.loss = b.loss;
   return t;
 }
@@ -1367,7 +1471,7 @@ int g6_mlp_grad(g6_ctx* ctx, const float* records, int64_t nrec, float* grad, do
   if (!records || nrec <= 0 || nrec > (1 << 22)) return fail(ctx, G6_ERR_ARG, "1 <= nrec <= 2^22 records required");
   CK(cudaSetDevice(ctx->device));
   TrainBuffers b;
-  int rc = train_buffers(ctx, b, (int)nrec);
+  int rc = train_buffers(ctx, b, (int)nrec, 0);
   if (rc) return rc;
   float* drec = nullptr;
   CK(b.get(&drec, (size_t)nrec * MLP_REC));
@@ -1396,7 +1500,7 @@ int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, d
   const long long N = ctx->nrec;
   batch = (int)std::min<long long>(batch, N);
   TrainBuffers b;
-  int rc = train_buffers(ctx, b, batch);
+  int rc = train_buffers(ctx, b, batch, N);
   if (rc) return rc;
   CK(launch_feat_stats(ctx->d_rec, N, b.mean, b.istd, ctx->stream));
   CK(cudaMemcpyAsync(ctx->h_mean, b.mean, sizeof ctx->h_mean, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1412,7 +1516,10 @@ int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, d
     const bool bias = (p >= MLP_B1 && p < MLP_W2) || (p >= MLP_B2 && p < MLP_W3);
     w[p] = bias ? 0.0f : (float)((2.0 * u[0] - 1.0) / std::sqrt((double)fan));
   }
-  w[MLP_B3] = w[MLP_B3 + 1] = (float)std::log(0.25 / 0.75);
+  {   // output bias: sigma = sigma0 before training
+    const double p0 = (1.0 - MLP_SMIN) / MLP_SSPAN;
+    w[MLP_B3] = w[MLP_B3 + 1] = (float)std::log(p0 / (1.0 - p0));
+  }
   CK(cudaMemcpy(ctx->d_mlp, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
   ctx->have_mlp = true;
   std::vector<int> perm(N);
@@ -1426,12 +1533,13 @@ int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, d
       std::swap(perm[k], perm[j]);
     }
     CK(cudaMemsetAsync(b.loss, 0, sizeof(double), ctx->stream));
+    // the epoch's permutation goes up once; the host vector is refilled only
+    // after the copy has completed (the loss read-back below synchronises)
+    CK(cudaMemcpyAsync(b.idx, perm.data(), N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     const long long nb = N / batch;
     for (long long q = 0; q < nb; ++q) {
-      CK(cudaMemcpyAsync(b.idx, perm.data() + q * batch, batch * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-      CK(launch_mlp_grad(train_args(ctx, b, ctx->d_rec, batch, b.idx), 1.0f / (float)batch, ctx->stream));
+      CK(launch_mlp_grad(train_args(ctx, b, ctx->d_rec, batch, b.idx + q * batch), 1.0f / (float)batch, ctx->stream));
       CK(launch_adam(ctx->d_mlp, b.grad, b.m, b.v, (float)lr, ++t, ctx->stream));
-      CK(cudaStreamSynchronize(ctx->stream));   // the index buffer is reused next batch
     }
     double l = 0.0;
     CK(cudaMemcpy(&l, b.loss, sizeof(double), cudaMemcpyDeviceToHost));

@@ -219,6 +219,11 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
     a.com_build[i] = a.com[i];
     a.com_build[n + i] = a.com[n + i];
     a.com_build[2 * n + i] = a.com[2 * n + i];
+    if (a.fix_build) {
+      a.fix_build[i] = xi;
+      a.fix_build[n + i] = yi;
+      a.fix_build[2 * n + i] = zi;
+    }
   }
 }
 

@@ -83,26 +83,27 @@ template <> struct Prm<float> {
 
 // Site-site loop of one molecule pair.  ri/rj: site offsets from their COM
 // (index 0 = LJ site, 1..NQ = charged sites).  Adds i-side results to acc.
-template <class M, class R>
+// NW = 9: full 3x3 molecular virial; NW = 1: its trace only (MD step).
+template <class M, class R, int NW>
 struct Acc {
   R fs[M::NQ + 1][3];
   R fc[3];
   R e;
-  R w[9];
+  R w[NW];
   __device__ void zero() {
 #pragma unroll
     for (int s = 0; s <= M::NQ; ++s) fs[s][0] = fs[s][1] = fs[s][2] = R(0);
     fc[0] = fc[1] = fc[2] = R(0);
     e = R(0);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) w[k] = R(0);
+    for (int k = 0; k < NW; ++k) w[k] = R(0);
   }
 };
 
-template <class M, class R>
+template <class M, class R, int NW>
 __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::NQ + 1][3],
                                           const R (&rj)[M::NQ + 1][3], const PairConst& pc, R rin2, R rin, R rout,
-                                          R c1, R c2, R trl, R tru, R tw3, Acc<M, R>& acc) {
+                                          R c1, R c2, R trl, R tru, R tw3, Acc<M, R, NW>& acc) {
   R hh, dh;
   switch_fn<R>(dd, rin2, rin, rout, c1, c2, hh, dh);
   // LJ site pair (site 0 - site 0)
@@ -160,10 +161,14 @@ __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::N
     fp[k] = sum + c;
   }
   acc.e += hh * elj + scc * ec;
+  if constexpr (NW == 9) {
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) acc.w[3 * a + b] += d[a] * fp[b];
+      for (int b = 0; b < 3; ++b) acc.w[3 * a + b] += d[a] * fp[b];
+  } else {
+    acc.w[0] += d[0] * fp[0] + d[1] * fp[1] + d[2] * fp[2];
+  }
 }
 
 __device__ __forceinline__ double shfl_xor_d(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
@@ -178,9 +183,24 @@ __device__ __forceinline__ double group_sum(double v) {
 // ---------------------------------------------------------------------------
 // k_force: neighbour-list force kernel.
 // ---------------------------------------------------------------------------
+// Molecules per block of the fused step kernel: the block is MPB x LPI
+// threads and warp 0 runs the integrator with one molecule per lane.  Small
+// blocks let several blocks share an SM, so one block's integrator epilogue
+// overlaps the site loops of the others; 8 molecules per epilogue warp keep the
+// FP64 instruction count low.  The mixed kernel is capped at 128 registers.
+template <bool MIXED, int LPI>
+struct StepShape {
+  static constexpr int MPB = (64 / LPI) > 8 ? (64 / LPI) : 8;
+  static constexpr int THREADS = MPB * LPI;
+  static constexpr int MINB = MIXED ? 65536 / (THREADS * 128) : 1;
+};
+
 template <class M, bool MIXED, int LPI, bool FUSED>
-__global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
+__global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
+                                  FUSED ? StepShape<MIXED, LPI>::MINB : 1)
+    k_force(ForceArgs a, StepArgs sa) {
   using R = typename std::conditional<MIXED, float, double>::type;
+  constexpr int NW = FUSED ? 1 : 9;
   int step = 0;
   if (a.ctrl) step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
@@ -192,7 +212,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
   const bool valid = i < a.n;
   const int n = a.n;
 
-  Acc<M, R> acc;
+  Acc<M, R, NW> acc;
   acc.zero();
   R ri[M::NQ + 1][3];
   int npin = 0;
@@ -220,13 +240,23 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
       const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
       const float rout2 = a.cc.frout2;
       const float band = 1e-3f;   // |dd32 - dd64| is below 1e-4 A^2 for boxes up to 1000 A
+      // the next neighbour's index and packed pose are loaded one iteration ahead
+      int jn = sub < nn ? row[sub] : 0;
+      float4 tn[M::NPK];
+#pragma unroll
+      for (int q = 0; q < M::NPK; ++q) tn[q] = sub < nn ? pk32[(size_t)jn * M::NPK + q] : make_float4(0.f, 0.f, 0.f, 0.f);
       for (int k = sub; k < nn; k += LPI) {
-        const int j = row[k];
+        const int j = jn;
         float wj[4 * M::NPK];
 #pragma unroll
         for (int q = 0; q < M::NPK; ++q) {
-          float4 t = pk32[(size_t)j * M::NPK + q];
+          const float4 t = tn[q];
           wj[4 * q] = t.x; wj[4 * q + 1] = t.y; wj[4 * q + 2] = t.z; wj[4 * q + 3] = t.w;
+        }
+        if (k + LPI < nn) {
+          jn = row[k + LPI];
+#pragma unroll
+          for (int q = 0; q < M::NPK; ++q) tn[q] = pk32[(size_t)jn * M::NPK + q];
         }
         float d[3];
         d[0] = (float)(int)(xi - __float_as_uint(wj[0])) * sx;
@@ -248,7 +278,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
 #pragma unroll
           for (int q = 0; q < 3; ++q) rj[s][q] = (R)wj[3 + 3 * s + q];
         R dr[3] = {(R)d[0], (R)d[1], (R)d[2]};
-        pair_math<M, R>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.frin2, (R)a.cc.frin, (R)a.cc.frout, (R)a.cc.fc1,
+        pair_math<M, R, NW>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.frin2, (R)a.cc.frin, (R)a.cc.frout, (R)a.cc.fc1,
                         (R)a.cc.fc2, (R)a.pc.frl, (R)a.pc.fru, (R)a.pc.fw3, acc);
       }
     } else {
@@ -269,19 +299,19 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
 #pragma unroll
           for (int q = 0; q < 3; ++q) rj[s][q] = (R)pj[3 + 3 * s + q];
         R dr[3] = {(R)dx[0], (R)dx[1], (R)dx[2]};
-        pair_math<M, R>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1, (R)a.cc.c2,
+        pair_math<M, R, NW>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1, (R)a.cc.c2,
                         (R)a.pc.rl, (R)a.pc.ru, (R)a.pc.w3, acc);
       }
     }
   }
-  // rigid_collectforce on the lane partials, then combine the LPI lanes in FP64
-  double v[16];
+  // rigid_collectforce on the lane partials: F, lab torque, energy, virial
+  R fo[3], to[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    R s = acc.fc[k];
+    R t = acc.fc[k];
 #pragma unroll
-    for (int q = 0; q <= M::NQ; ++q) s += acc.fs[q][k];
-    v[k] = (double)s;
+    for (int q = 0; q <= M::NQ; ++q) t += acc.fs[q][k];
+    fo[k] = t;
   }
   {
     R tx = 0, ty = 0, tz = 0;
@@ -291,17 +321,21 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
       ty += ri[q][2] * acc.fs[q][0] - ri[q][0] * acc.fs[q][2];
       tz += ri[q][0] * acc.fs[q][1] - ri[q][1] * acc.fs[q][0];
     }
-    v[3] = (double)tx; v[4] = (double)ty; v[5] = (double)tz;
+    to[0] = tx; to[1] = ty; to[2] = tz;
   }
-  v[6] = (double)acc.e;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) v[7 + k] = (double)acc.w[k];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = group_sum<LPI>(v[k]);
   int np_tot = npin;
 #pragma unroll
   for (int m = LPI / 2; m >= 1; m >>= 1) np_tot += __shfl_xor_sync(0xffffffffu, np_tot, m);
-  if (!FUSED) {
+  if constexpr (!FUSED) {
+    // combine the LPI lanes in FP64
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { v[k] = (double)fo[k]; v[3 + k] = (double)to[k]; }
+    v[6] = (double)acc.e;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[7 + k] = (double)acc.w[k];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = group_sum<LPI>(v[k]);
     if (valid && sub == 0) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
@@ -310,30 +344,91 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a, StepArgs sa) {
       for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
       if (a.npair_in) a.npair_in[i] = np_tot;
     }
-    return;
-  }
-  // fused MD step: Gear corrector, reductions and the next predict+placement
-  const bool predict_next = step + 1 < sa.ctrl[2];
-  double vv[NRED];
+  } else if constexpr (MIXED) {
+    // fused mixed step: error-free float-pair combine of the lanes, then warp 0
+    // runs the integrator for the block's MPB molecules (one per lane)
+    constexpr int MPB = StepShape<MIXED, LPI>::MPB;
+    const bool predict_next = step + 1 < sa.ctrl[2];
+    FF q8[8];
 #pragma unroll
-  for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
-  double dmax2 = 0.0;
-  int bad = 0, rr = -1;
-  if (valid && sub == 0) {
-    rr = a.rep.mol_rep[i];
-    const double F[3] = {v[0], v[1], v[2]}, tl[3] = {v[3], v[4], v[5]};
-    double wm[9];
+    for (int k = 0; k < 3; ++k) { q8[k] = FF{fo[k], 0.0f}; q8[3 + k] = FF{to[k], 0.0f}; }
+    q8[6] = FF{acc.e, 0.0f};
+    q8[7] = FF{acc.w[0], 0.0f};
 #pragma unroll
-    for (int k = 0; k < 9; ++k) wm[k] = 0.5 * v[7 + k];
-    correct_one(sa, i, F, tl, 0.5 * v[6], wm, 0.5 * (double)np_tot, step, predict_next, pose_buf(sa, odd ? 1 : 0),
-                pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+      for (int m = LPI / 2; m >= 1; m >>= 1) q8[k] = ff_add(q8[k], red_shfl(q8[k], m));
+    __shared__ FF smf[MPB][8];
+    __shared__ int smn[MPB];
+    if (sub == 0) {
+      const int m = threadIdx.x / LPI;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) smf[m][k] = q8[k];
+      smn[m] = np_tot;
+    }
+    __syncthreads();
+    FF vv[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = FF{0.0f, 0.0f};
+    float dmax2 = 0.0f;
+    int bad = 0, rr = -1;
+    if (threadIdx.x < MPB) {
+      const int m = threadIdx.x;
+      const int im = blockIdx.x * MPB + m;
+      if (im < n) {
+        rr = a.rep.mol_rep[im];
+        const float F[3] = {smf[m][0].hi + smf[m][0].lo, smf[m][1].hi + smf[m][1].lo, smf[m][2].hi + smf[m][2].lo};
+        const float tl[3] = {smf[m][3].hi + smf[m][3].lo, smf[m][4].hi + smf[m][4].lo, smf[m][5].hi + smf[m][5].lo};
+        float ekt2, ekr2;
+        correct_mixed<M::NQ>(sa, im, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
+        vv[0] = FF{0.5f * smf[m][6].hi, 0.5f * smf[m][6].lo};
+        vv[1] = FF{0.5f * smf[m][7].hi, 0.5f * smf[m][7].lo};
+        vv[2] = FF{ekt2, 0.0f};
+        vv[3] = FF{ekr2, 0.0f};
+        vv[4] = FF{0.5f * (float)smn[m], 0.0f};
+      }
+    }
+    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step, predict_next);
+  } else {
+    // fused FP64 step: FP64 lane combine, FP64 integrator in warp 0
+    constexpr int MPB = StepShape<MIXED, LPI>::MPB;
+    const bool predict_next = step + 1 < sa.ctrl[2];
+    double v8[8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { v8[k] = group_sum<LPI>((double)fo[k]); v8[3 + k] = group_sum<LPI>((double)to[k]); }
+    v8[6] = group_sum<LPI>((double)acc.e);
+    v8[7] = group_sum<LPI>((double)acc.w[0]);
+    __shared__ double smd[MPB][9];
+    if (sub == 0) {
+      const int m = threadIdx.x / LPI;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) smd[m][k] = v8[k];
+      smd[m][8] = (double)np_tot;
+    }
+    __syncthreads();
+    double vv[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
+    double dmax2 = 0.0;
+    int bad = 0, rr = -1;
+    if (threadIdx.x < MPB) {
+      const int m = threadIdx.x;
+      const int im = blockIdx.x * MPB + m;
+      if (im < n) {
+        rr = a.rep.mol_rep[im];
+        const double F[3] = {smd[m][0], smd[m][1], smd[m][2]}, tl[3] = {smd[m][3], smd[m][4], smd[m][5]};
+        correct_one(sa, im, F, tl, 0.5 * smd[m][6], 0.5 * smd[m][7], 0.5 * smd[m][8], step, predict_next,
+                    pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+      }
+    }
+    step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step, predict_next);
   }
-  step_reduce<128>(sa, vv, rr, dmax2, bad, 128 / LPI, step, predict_next);
 }
 
 template <class M, bool MIXED, int LPI, bool FUSED>
 static cudaError_t launch_force_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
-  const int threads = 128;
+  // force only: 128 threads; fused step: MPB molecules (MPB x LPI threads) per block
+  const int threads = FUSED ? StepShape<MIXED, LPI>::THREADS : 128;
   const long long total = (long long)a.n * LPI;
   const int blocks = (int)((total + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;

@@ -29,7 +29,10 @@ constexpr int MAXSITE = 6;  // sites per molecule including the COM site
 constexpr int MAXQ = 4;     // charged sites per molecule
 constexpr int MAXREP_PER_BLOCK = 8;
 constexpr int RED_BLOCK = 64;    // block size of the per-molecule update kernels (FP64-bound: spread over SMs)
-constexpr int NRED = 24;         // reduced quantities per replica (see g6_md.cu)
+constexpr int NRED = 5;          // reduced quantities per replica: Epot, virial trace, sum |d1|^2, sum I w^2, pairs
+// Mixed-precision MD keeps the small Gear terms in a float SoA (stf[c*n + i]):
+// d2..d5 (com), w2..w5 (angular velocity) and the quaternion stacks q2..q5.
+constexpr int STF_D2 = 0, STF_W2 = 12, STF_Q2 = 24, STF_COLS = 40;
 
 // ---------------------------------------------------------------------------
 // Model constants (host computes them from the reference formulas; the device
@@ -204,6 +207,7 @@ struct ListArgs {
   const uint32_t* fix1;  // buffer 1 (odd steps when ctrl != NULL)
   const double* com;     // SoA 3n (state)
   double* com_build;     // SoA 3n
+  uint32_t* fix_build;   // SoA 3n fixed-point COM at the build
   float rlist2;
   int* nbr;
   int* nnb;
@@ -241,6 +245,7 @@ struct PlaceArgs {
   int n, nq, npk, w64;
   RepDev rep;
   double body[MAXSITE][3];
+  float fbody[MAXSITE][3];
   double* st;
   double* tmat;
   double* pk64;
@@ -256,6 +261,8 @@ struct StepArgs {
   uint32_t* fix1;
   double mass, I[3], dt;
   const double* com_build;
+  const uint32_t* fix_build;
+  float* stf;          // mixed precision: float SoA of the small Gear terms (STF_*)
   double half_skin2;
   ThermoDev* th;
   double* part;        // blocks * MAXREP_PER_BLOCK * NRED
@@ -302,6 +309,8 @@ cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int
 cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
+cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s);
+cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, cudaStream_t s);
 cudaError_t launch_step(const ForceArgs& f, const StepArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);

@@ -2,38 +2,58 @@
 //
 // One CTA advances one chain (= one replica of the context) through ntrial
 // sequential trials.  Per trial:
-//   thread 0   picks the target (uniform), draws the rotation vector and the
-//              translation (Gaussian, the sine branch of Random_Normal,
-//              RandomModule.F90:20-28), builds the new quaternion with
-//              qinfrotator + qadd (QuatModule.F90:108-133, 203-223) and the new
-//              site offsets (rigid_setsiteposition);
-//   all        sum e(new, j) - e(old, j) over every other molecule j of the
-//              chain with the PairPotential arithmetic (strict rc test, COM
-//              switch, ST2 Coulomb taper on the custom path), per-thread
-//              partials combined in FP64 in a fixed order;
-//   thread 0   Metropolis test exp(-dE * I2J * J2K * beta) (mc2.F90:712-722),
-//              and on acceptance writes the new pose.
+//   warp 0   reads the trial's draws (target, Gaussian rotation vector and
+//            translation: the sine branch of Random_Normal, RandomModule.F90:20-28)
+//            from a shared-memory batch that all threads fill in parallel once
+//            per 256 trials, scales them by the widths, and builds the new
+//            quaternion with qinfrotator + qadd (QuatModule.F90:108-133, 203-223)
+//            and the new site offsets (rigid_setsiteposition);
+//   all      sum e(new, j) - e(old, j) over every other molecule j of the chain
+//            with the PairPotential arithmetic (strict rc test, COM switch, ST2
+//            Coulomb taper on the custom path), one molecule j per thread;
+//   warp 0   Metropolis test (mc2.F90:712-722) as log(u) < -dE*I2J*J2K*beta
+//            (+ the Hastings term), and on acceptance writes the new pose.
 // Unlike mc2 (which subtracts stored pair energies of the neighbours of the
 // new pose only and adapts the step width after every trial), dE runs over all
 // neighbours of both poses and the widths are fixed, so the Markov chain is
 // exactly Metropolis-Hastings for the chosen widths.  The draws come from the
 // same Philox stream as the oracle (counter = chain, trial, draw), so short
-// chains can be replayed step by step on the CPU.
+// FP64 chains replay the CPU chain trial by trial.
 //
-// Learned widths (LEARNED = true): the proposal widths come from a 24-64-64-2
-// MLP on local-environment features, evaluated at the old pose before the draw
-// and at the new pose after it; the Hastings ratio includes both densities.
+// Mixed precision: the trial pose and the pair energies are FP32; the FP64
+// state (COM, quaternion, FP64 offsets) is rebuilt from the FP64 draws only
+// when a trial is accepted, and the FP32 offsets the trial used are the ones
+// stored in the packed pose, so later trials see exactly the pose whose energy
+// was accepted.
+//
+// Learned widths (G6_MC_LEARNED): the proposal widths come from a 24-64-64-2
+// MLP on local-environment features.  The features of every molecule at its
+// current pose are kept in an integer cache (exact sums, see g6_mlp.cuh): the
+// widths at the old pose come from the cache, the features at the new pose
+// are summed in the same pass as the energies, and an accepted move updates
+// the cache of the moved molecule and of its neighbours.  The Hastings ratio
+// uses the widths of both poses.  G6_MC_COLLECT runs the fixed widths and
+// writes one training record per trial.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "g6_internal.cuh"
 #include "g6_mlp.cuh"
 
 namespace g6 {
 
+constexpr int MC_NT = 512;            // threads per chain
+constexpr int MC_NB = 256;            // trials per batch of pre-computed draws
+constexpr float FEAT_Q = 1048576.0f;  // feature terms are integers of 2^-20
+constexpr float FEAT_IQ = 1.0f / 1048576.0f;
+constexpr float FEAT_RC2 = 6.5f * 6.5f;
+constexpr int MC_QMAX = 256;          // feature neighbours per pose (about 40 in liquid water)
+
 template <int NQ, bool TAPER, class R>
 __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 1][3], const R (&rj)[NQ + 1][3],
-                                         const PairConst& pc, R rin2, R rin, R rout, R c1, R c2) {
-  R hh, dh;
+                                         const PairConst& pc, R rin2, R rin, R rout, R c1) {
+  R hh;
   if (dd > rin2) {
     R r = sqrt(dd);
     R u = r - rout, l = r - rin, uu = u * u, ll = l * l;
@@ -41,7 +61,6 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
   } else {
     hh = R(1);
   }
-  (void)dh;
   R v[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) v[k] = d[k] + ri[0][k] - rj[0][k];
@@ -77,238 +96,631 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
   return hh * elj + scc * ec;
 }
 
-// QuatModule.F90:108-133: a1 <- a1 (x) a2, then the shorter of the two signs.
-__device__ __forceinline__ void qadd(double q1[4], const double q2[4]) {
-  const double a1 = q1[0], b1 = q1[1], c1 = q1[2], d1 = q1[3];
-  const double a2 = q2[0], b2 = q2[1], c2 = q2[2], d2 = q2[3];
-  double a3 = a1 * a2 - b1 * b2 - c1 * c2 - d1 * d2;
-  double b3 = a1 * b2 + b1 * a2 + c1 * d2 - d1 * c2;
-  double c3 = a1 * c2 + c1 * a2 - b1 * d2 + d1 * b2;
-  double d3 = a1 * d2 + d1 * a2 + b1 * c2 - c1 * b2;
-  if (a3 < 0) { a3 = -a3; b3 = -b3; c3 = -c3; d3 = -d3; }
+// QuatModule.F90:108-133: a1 <- a1 (x) a2, then the sign with a >= 0.
+template <class R>
+__device__ __forceinline__ void qadd(R q1[4], const R q2[4]) {
+  const R a1 = q1[0], b1 = q1[1], c1 = q1[2], d1 = q1[3];
+  const R a2 = q2[0], b2 = q2[1], c2 = q2[2], d2 = q2[3];
+  R a3 = a1 * a2 - b1 * b2 - c1 * c2 - d1 * d2;
+  R b3 = a1 * b2 + b1 * a2 + c1 * d2 - d1 * c2;
+  R c3 = a1 * c2 + c1 * a2 - b1 * d2 + d1 * b2;
+  R d3 = a1 * d2 + d1 * a2 + b1 * c2 - c1 * b2;
+  if (a3 < R(0)) { a3 = -a3; b3 = -b3; c3 = -c3; d3 = -d3; }
   q1[0] = a3; q1[1] = b3; q1[2] = c3; q1[3] = d3;
 }
 
-__device__ __forceinline__ double mc_normal(uint64_t seed, uint32_t chain, uint64_t trial, uint32_t k, double var) {
-  double u[2];
-  uniform2(seed, chain, (uint32_t)trial, (uint32_t)(trial >> 32), k, u);
-  return sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]) * sqrt(var);
+// qinfrotator (QuatModule.F90:203-223) composed with the old orientation, the
+// rotation matrix of rigid_setmatrix and the lab offsets of sites 0..NQ.
+template <class R, int NQ>
+__device__ __forceinline__ void trial_rotation(const R rot[3], const double* qold, const double (&body)[MAXSITE][3],
+                                               R qn[4], R (&off)[NQ + 1][3]) {
+  R qr[4] = {R(1), rot[0], rot[1], rot[2]};
+  const R rn = R(1) / sqrt(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qr[k] *= rn;
+  R qo[4] = {(R)qold[0], (R)qold[1], (R)qold[2], (R)qold[3]};
+  qadd(qr, qo);
+  const R qa = qr[0], qb = qr[1], qc = qr[2], qd = qr[3];
+  R tm[9];
+  tm[0] = (qa * qa + qb * qb - (qc * qc + qd * qd)); tm[1] = -R(2) * (qa * qd + qb * qc);
+  tm[2] = R(2) * (qb * qd - qa * qc); tm[3] = R(2) * (qa * qd - qb * qc);
+  tm[4] = qa * qa + qc * qc - (qb * qb + qd * qd); tm[5] = -R(2) * (qa * qb + qc * qd);
+  tm[6] = R(2) * (qa * qc + qb * qd); tm[7] = R(2) * (qa * qb - qc * qd);
+  tm[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qn[k] = qr[k];
+#pragma unroll
+  for (int s = 0; s <= NQ; ++s) {
+    const R bx = (R)body[s][0], by = (R)body[s][1], bz = (R)body[s][2];
+    off[s][0] = tm[0] * bx + tm[1] * by + tm[2] * bz;
+    off[s][1] = tm[3] * bx + tm[4] * by + tm[5] * bz;
+    off[s][2] = tm[6] * bx + tm[7] * by + tm[8] * bz;
+  }
 }
 
-struct McShared {
-  double com_new[3], q_new[4], off_new[MAXQ + 1][3];
-  double com_old[3], off_old[MAXQ + 1][3];
-  float off_new_f[MAXQ + 1][3];
-  uint32_t fix_new[3];
-  int target;
-  double sig_t, sig_r, logq_fwd;
-  double rot[3], dx[3];
-  float feat_old[MLP_IN], feat_new[MLP_IN];
-  double part[32];
-  double dE;
-  int accept;
+// ---------------------------------------------------------------------------
+// Features with correctly rounded single operations only (no contraction), so
+// the same pair gives the same integer terms at every call site.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float dot3_rn(const float a[3], const float b[3]) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a[0], b[0]), __fmul_rn(a[1], b[1])), __fmul_rn(a[2], b[2]));
+}
+__device__ __forceinline__ float gauss_rn(float t) { return exp2f(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)); }
+__device__ __forceinline__ int feat_q(float x) { return __float2int_rn(__fmul_rn(x, FEAT_Q)); }
+
+// Unit directions of the charged sites 1..NQ from their offsets o[(NQ+1)*3].
+template <int NQ>
+__device__ __forceinline__ void site_dirs(const float* o, float (&u)[4][3]) {
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    if (s < NQ) {
+      const float v[3] = {o[3 * (s + 1)], o[3 * (s + 1) + 1], o[3 * (s + 1) + 2]};
+      const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3_rn(v, v)));
+#pragma unroll
+      for (int k = 0; k < 3; ++k) u[s][k] = __fmul_rn(v[k], inv);
+    } else {
+      u[s][0] = u[s][1] = u[s][2] = 0.0f;
+    }
+  }
+}
+
+// Integer feature terms of one neighbour at e (molecule -> neighbour, |e|^2 = r2).
+__device__ __forceinline__ void feat_terms(const float e[3], float r2, const float (&u)[4][3], int sign,
+                                           int (&f)[MLP_IN]) {
+  const float r = __fsqrt_rn(r2), ir = __fdiv_rn(1.0f, r);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) f[k] += sign * feat_q(gauss_rn(__fmul_rn(__fsub_rn(r, 2.4f + 0.25f * k), 4.0f)));
+  const float g1 = gauss_rn(__fmul_rn(__fsub_rn(r, 2.9f), 1.0f / 0.35f));
+  const float g2 = gauss_rn(__fmul_rn(__fsub_rn(r, 4.5f), 2.0f));
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    float c = __fmul_rn(dot3_rn(u[s], e), ir);
+    c = fmaxf(c, 0.0f);
+    const float c2 = __fmul_rn(c, c), c4 = __fmul_rn(c2, c2);
+    f[16 + s] += sign * feat_q(__fmul_rn(g1, c4));
+    f[20 + s] += sign * feat_q(__fmul_rn(g2, c4));
+  }
+}
+
+// Separation a -> b of two molecules: fixed-point COMs (mixed) or the FP64
+// minimum image (plain), as float.
+__device__ __forceinline__ float fvec_fix(const uint32_t a[3], const uint32_t b[3], const float fs[3], float e[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) e[k] = __fmul_rn((float)(int)(b[k] - a[k]), fs[k]);
+  return dot3_rn(e, e);
+}
+__device__ __forceinline__ float fvec_64(const double a[3], const double b[3], const double L[3], const double iL[3],
+                                         float e[3]) {
+  double o[3], d[3];
+  exact_dd(b, a, L, iL, o, d);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) e[k] = (float)d[k];
+  return dot3_rn(e, e);
+}
+
+template <int NQ, bool MIXED>
+struct PoseRead {
+  static constexpr int W64 = ((6 + 3 * NQ) + 1) / 2 * 2;
+  static constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
+  // float offsets of sites 0..NQ of molecule j as the trial energies see them
+  __device__ static void offsets(const McArgs& a, int j, float (&o)[(NQ + 1) * 3]) {
+#pragma unroll
+    for (int k = 0; k < (NQ + 1) * 3; ++k)
+      o[k] = MIXED ? a.pk32f[(size_t)j * 4 * NPK + 3 + k] : (float)a.pk64[(size_t)j * W64 + 3 + k];
+  }
+  __device__ static void fix(const McArgs& a, int j, uint32_t (&f)[3]) {
+    f[0] = a.fix[j]; f[1] = a.fix[a.n + j]; f[2] = a.fix[2 * a.n + j];
+  }
+  __device__ static void com(const McArgs& a, int j, double (&c)[3]) {
+    const double* p = a.pk64 + (size_t)j * W64;
+    c[0] = p[0]; c[1] = p[1]; c[2] = p[2];
+  }
 };
 
-template <int NQ, bool TAPER, bool MIXED, bool LEARNED>
-__global__ void __launch_bounds__(256) k_mc(McArgs a) {
+// Features of every molecule of the chain at its current pose (integer cache).
+template <int NQ, bool MIXED>
+__device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3], const double L[3],
+                              const double iL[3]) {
+  using P = PoseRead<NQ, MIXED>;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    float o[(NQ + 1) * 3], u[4][3];
+    P::offsets(a, i, o);
+    site_dirs<NQ>(o, u);
+    int f[MLP_IN];
+#pragma unroll
+    for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
+    uint32_t fi[3];
+    double ci[3];
+    if (MIXED) P::fix(a, i, fi); else P::com(a, i, ci);
+    for (int j = i0; j < i1; ++j) {
+      if (j == i) continue;
+      float e[3], r2;
+      if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fi, fj, fs, e); }
+      else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(ci, cj, L, iL, e); }
+      if (r2 < FEAT_RC2 && r2 > 0.0f) feat_terms(e, r2, u, 1, f);
+    }
+#pragma unroll
+    for (int k = 0; k < MLP_IN; ++k) a.fcache[(size_t)i * MLP_IN + k] = f[k];
+  }
+}
+
+// The proposal-width network in shared memory, transposed for conflict-free
+// reads (lane o reads column o).
+struct MlpShared {
+  float w1t[MLP_IN][MLP_H];
+  float b1[MLP_H];
+  float w2t[MLP_H][MLP_H];
+  float b2[MLP_H];
+  float w3[MLP_OUT][MLP_H];
+  float b3[MLP_OUT];
+  float mean[MLP_IN], istd[MLP_IN];
+  float x[2][MLP_IN];   // per-warp scratch (warps 0 and 1 evaluate the network concurrently)
+  float h[2][MLP_H];
+};
+
+__device__ void mlp_load(MlpShared& m, const MlpDev& d) {
+  for (int p = threadIdx.x; p < MLP_H * MLP_IN; p += blockDim.x) {
+    const int o = p / MLP_IN, k = p % MLP_IN;
+    m.w1t[k][o] = d.w[MLP_W1 + p];
+  }
+  for (int p = threadIdx.x; p < MLP_H * MLP_H; p += blockDim.x) {
+    const int o = p / MLP_H, k = p % MLP_H;
+    m.w2t[k][o] = d.w[MLP_W2 + p];
+  }
+  for (int p = threadIdx.x; p < MLP_H; p += blockDim.x) {
+    m.b1[p] = d.w[MLP_B1 + p];
+    m.b2[p] = d.w[MLP_B2 + p];
+    m.w3[0][p] = d.w[MLP_W3 + p];
+    m.w3[1][p] = d.w[MLP_W3 + MLP_H + p];
+  }
+  if (threadIdx.x < MLP_OUT) m.b3[threadIdx.x] = d.w[MLP_B3 + threadIdx.x];
+  if (threadIdx.x < MLP_IN) { m.mean[threadIdx.x] = d.feat_mean[threadIdx.x]; m.istd[threadIdx.x] = d.feat_inv_std[threadIdx.x]; }
+}
+
+// Widths from integer features feat[] (one whole warp; lane 0's result is the
+// one used).  w selects the warp's scratch rows.
+__device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, double s0t, double s0r,
+                                                double& st, double& sr) {
+  const int lane = threadIdx.x & 31;
+  float* xs = m.x[w];
+  float* hs = m.h[w];
+  if (lane < MLP_IN) xs[lane] = ((float)feat[lane] * FEAT_IQ - m.mean[lane]) * m.istd[lane];
+  __syncwarp();
+  float h1[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int o = lane + 32 * u;
+    float s0 = m.b1[o], s1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MLP_IN; k += 2) {
+      s0 = fmaf(m.w1t[k][o], xs[k], s0);
+      s1 = fmaf(m.w1t[k + 1][o], xs[k + 1], s1);
+    }
+    h1[u] = tanhf(s0 + s1);
+  }
+  __syncwarp();
+  hs[lane] = h1[0];
+  hs[lane + 32] = h1[1];
+  __syncwarp();
+  float h2[2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int o = lane + 32 * u;
+    float s0 = m.b2[o], s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < MLP_H; k += 4) {
+      s0 = fmaf(m.w2t[k][o], hs[k], s0);
+      s1 = fmaf(m.w2t[k + 1][o], hs[k + 1], s1);
+      s2 = fmaf(m.w2t[k + 2][o], hs[k + 2], s2);
+      s3 = fmaf(m.w2t[k + 3][o], hs[k + 3], s3);
+    }
+    h2[u] = tanhf((s0 + s1) + (s2 + s3));
+  }
+  float z[MLP_OUT];
+#pragma unroll
+  for (int q = 0; q < MLP_OUT; ++q) {
+    float s = m.w3[q][lane] * h2[0] + m.w3[q][lane + 32] * h2[1];
+#pragma unroll
+    for (int mm = 16; mm >= 1; mm >>= 1) s += __shfl_xor_sync(0xffffffffu, s, mm);
+    z[q] = __shfl_sync(0xffffffffu, s, 0) + m.b3[q];
+  }
+  __syncwarp();
+  st = s0t * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[0]));
+  sr = s0r * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[1]));
+}
+
+// log of the proposal density of a move (up to a constant): isotropic
+// Gaussians in the translation and in the rotation vector.
+__device__ __forceinline__ float log_q(float st, float sr, float d2, float r2) {
+  return -3.0f * __logf(st) - d2 / (2.0f * st * st) - 3.0f * __logf(sr) - r2 / (2.0f * sr * sr);
+}
+
+// Queues of the molecules within the feature radius of the old (0) and new
+// (1) pose of the target.  Control warp w owns segment w of each queue and
+// appends with ballots only (no atomics); seg_n[p][w] is its length.
+__device__ __forceinline__ void queue_append(int* seg, int& cnt, bool in, int j, int qseg, int* overflow) {
+  const unsigned m = __ballot_sync(0xffffffffu, in);
+  if (in) {
+    const int pos = cnt + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
+    if (pos < qseg) seg[pos] = j;
+    else *overflow = 1;
+  }
+  cnt += __popc(m);
+}
+
+template <int NQ, bool TAPER, bool MIXED, int MODE>
+__global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   using R = typename std::conditional<MIXED, float, double>::type;
-  constexpr int W64 = ((6 + 3 * NQ) + 1) / 2 * 2;
-  constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
-  __shared__ McShared sh;
+  using P = PoseRead<NQ, MIXED>;
+  constexpr bool FEAT = MODE != G6_MC_PLAIN;
+  constexpr bool LEARN = MODE == G6_MC_LEARNED;
+  // warps 0 (and 1) find the feature neighbours, sum the new-pose features
+  // and run the network while the other warps sum the energies
+  constexpr int NCTRL = LEARN ? 2 : (FEAT ? 1 : 0);
+  constexpr int E0 = 32 * NCTRL, NE = MC_NT - E0, NEW = NE / 32;
+  constexpr int W64 = P::W64, NPK = P::NPK;
+  __shared__ double s_lu[MC_NB];
+  __shared__ double s_g[6][MC_NB];
+  __shared__ int s_tg[MC_NB];
+  __shared__ R s_on[NQ + 1][3], s_oo[NQ + 1][3];
+  __shared__ double s_cn[3], s_co[3];
+  __shared__ uint32_t s_fn[3], s_fo[3];
+  __shared__ float s_un[4][3];
+  __shared__ int s_feat[MLP_IN];
+  __shared__ R s_part[NEW > 0 ? NEW : 1];
+  constexpr int QSEG = NCTRL > 0 ? MC_QMAX / NCTRL : 1;
+  __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
+  __shared__ int s_nq[2][NCTRL > 0 ? NCTRL : 1];
+  __shared__ double s_sig_new[2], s_spec[2];
+  __shared__ int s_spec_tg;
+  __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
+
   const int c = blockIdx.x;
   const int i0 = a.rep.off[c], i1 = a.rep.off[c + 1], nc = i1 - i0;
   const int n = a.n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double L[3], iL[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) { L[k] = a.rep.L[3 * c + k]; iL[k] = a.rep.invL[3 * c + k]; }
   const float fs[3] = {a.rep.fscale[3 * c], a.rep.fscale[3 * c + 1], a.rep.fscale[3 * c + 2]};
   const double beta = a.beta[c];
+  // fixed widths enter as sqrt(sigma^2), the variance form of mc2's Random_Normal call
+  const double sig_t_fixed = sqrt(a.sigma_t[c] * a.sigma_t[c]);
+  const double sig_r_fixed = sqrt(a.sigma_r[c] * a.sigma_r[c]);
+  if constexpr (LEARN) mlp_load(s_mlp, a.mlp);
+  if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL);
+  if (threadIdx.x == 0) s_spec_tg = -1;
+  __syncthreads();
+
+  const R rin2 = MIXED ? (R)a.cc.frin2 : (R)a.cc.rin2, rin = MIXED ? (R)a.cc.frin : (R)a.cc.rin;
+  const R rout = MIXED ? (R)a.cc.frout : (R)a.cc.rout, c1 = MIXED ? (R)a.cc.fc1 : (R)a.cc.c1;
   double energy = a.energy[c];
   long long nacc = 0;
   int nsample = 0;
+  // lane-0 registers carried from the pose build to the acceptance step
+  double rot_d[3] = {0, 0, 0}, dx_d[3] = {0, 0, 0}, st_old = 0.0, sr_old = 0.0;
+  R qn_trial[4] = {0, 0, 0, 0};
+  float d2f = 0.0f, r2f = 0.0f;
+
   for (int t = 0; t < a.ntrial; ++t) {
-    const uint64_t trial = a.counter + (uint64_t)t;
-    if (threadIdx.x == 0) {
-      double u[2];
-      uniform2(a.seed, (uint32_t)c, (uint32_t)trial, (uint32_t)(trial >> 32), 0u, u);
-      int tg = (int)(u[0] * nc);
-      if (tg >= nc) tg = nc - 1;   // u = 1 would select nc (mc2.F90:551 quirk)
-      sh.target = i0 + tg;
-      sh.sig_t = a.sigma_t[c];
-      sh.sig_r = a.sigma_r[c];
+    const int tb = t % MC_NB;
+    if (tb == 0) {   // draws of the next MC_NB trials, one trial per thread
+      __syncthreads();
+      const int tt = t + (int)threadIdx.x;
+      if (threadIdx.x < MC_NB && tt < a.ntrial) {
+        const uint64_t trial = a.counter + (uint64_t)tt;
+        const uint32_t lo = (uint32_t)trial, hi = (uint32_t)(trial >> 32);
+        double u[2];
+        uniform2(a.seed, (uint32_t)c, lo, hi, 0u, u);
+        int tg = (int)(u[0] * nc);
+        if (tg >= nc) tg = nc - 1;   // u = 1 would select nc (mc2.F90:551 quirk)
+        s_tg[threadIdx.x] = tg;
+        s_lu[threadIdx.x] = log(u[1]);
+#pragma unroll 1
+        for (int k = 0; k < 6; ++k) {
+          uniform2(a.seed, (uint32_t)c, lo, hi, 1u + k, u);
+          s_g[k][threadIdx.x] = sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]);
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    const int tg = sh.target;
-    if (LEARNED) {
-      if (threadIdx.x == 0) {
-        const double* po = a.pk64 + (size_t)tg * W64;
-        for (int k = 0; k < 3; ++k) sh.com_old[k] = po[k];
+    const int tg = i0 + s_tg[tb];
+    // ---- warp 0: widths at the old pose and the trial pose ----
+    if (warp == 0) {
+      double st_w = sig_t_fixed, sr_w = sig_r_fixed;
+      if constexpr (LEARN) {
+        if (s_spec_tg == tg) { st_w = s_spec[0]; sr_w = s_spec[1]; }
+        else mlp_widths_warp(s_mlp, 0, a.fcache + (size_t)tg * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st_w, sr_w);
+        st_old = st_w; sr_old = sr_w;
+      }
+      if (lane == 0) {
+        R rot[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          rot_d[k] = s_g[k][tb] * sr_w;
+          dx_d[k] = s_g[3 + k][tb] * st_w;
+          rot[k] = (R)rot_d[k];
+        }
+        d2f = (float)(dx_d[0] * dx_d[0] + dx_d[1] * dx_d[1] + dx_d[2] * dx_d[2]);
+        r2f = (float)(rot_d[0] * rot_d[0] + rot_d[1] * rot_d[1] + rot_d[2] * rot_d[2]);
+        double qold[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
+        R off[NQ + 1][3];
+        trial_rotation<R, NQ>(rot, qold, a.body, qn_trial, off);
+        float oo[(NQ + 1) * 3];
+        if (MIXED) P::offsets(a, tg, oo);
+#pragma unroll
         for (int s = 0; s <= NQ; ++s)
-          for (int k = 0; k < 3; ++k) sh.off_old[s][k] = po[3 + 3 * s + k];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            s_on[s][k] = off[s][k];
+            s_oo[s][k] = MIXED ? (R)oo[3 * s + k] : (R)a.pk64[(size_t)tg * W64 + 3 + 3 * s + k];
+          }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          s_co[k] = a.st[(size_t)k * n + tg];
+          s_cn[k] = s_co[k] + dx_d[k];
+          s_fo[k] = a.fix[(size_t)k * n + tg];
+          s_fn[k] = to_fixed(s_cn[k], iL[k]);
+        }
+        if (FEAT) {
+          float on[(NQ + 1) * 3];
+#pragma unroll
+          for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) on[3 * s + k] = (float)off[s][k];
+          float u[4][3];
+          site_dirs<NQ>(on, u);
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s_un[s][k] = u[s][k];
+        }
       }
-      __syncthreads();
-      mc_features<NQ>(a, tg, sh.com_old, sh.off_old, sh.feat_old, i0, i1, L, iL);   // block-wide
-      if (threadIdx.x < 32) mlp_widths(a.mlp, sh.feat_old, &sh.sig_t, &sh.sig_r);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      const double sr = sh.sig_r, st = sh.sig_t;
-      double rot[3], dx[3];
-      for (int k = 0; k < 3; ++k) rot[k] = mc_normal(a.seed, c, trial, 1u + k, sr * sr);
-      for (int k = 0; k < 3; ++k) dx[k] = mc_normal(a.seed, c, trial, 4u + k, st * st);
-      // qinfrotator: normalise (1, x, y, z)
-      double qr[4] = {1.0, rot[0], rot[1], rot[2]};
-      const double rn = 1.0 / sqrt(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
-      for (int k = 0; k < 4; ++k) qr[k] *= rn;
-      double qo[4];
-      for (int k = 0; k < 4; ++k) qo[k] = a.st[(size_t)(33 + k) * n + tg];
-      qadd(qr, qo);
-      double tm[9];
-      {
-        const double qa = qr[0], qb = qr[1], qc = qr[2], qd = qr[3];
-        tm[0] = (qa * qa + qb * qb - (qc * qc + qd * qd)); tm[1] = -2.0 * (qa * qd + qb * qc);
-        tm[2] = 2.0 * (qb * qd - qa * qc); tm[3] = 2.0 * (qa * qd - qb * qc);
-        tm[4] = qa * qa + qc * qc - (qb * qb + qd * qd); tm[5] = -2.0 * (qa * qb + qc * qd);
-        tm[6] = 2.0 * (qa * qc + qb * qd); tm[7] = 2.0 * (qa * qb - qc * qd);
-        tm[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
-      }
-      for (int k = 0; k < 4; ++k) sh.q_new[k] = qr[k];
-      for (int k = 0; k < 3; ++k) { sh.com_new[k] = a.st[(size_t)k * n + tg] + dx[k]; sh.rot[k] = rot[k]; sh.dx[k] = dx[k]; }
-      for (int s = 0; s <= NQ; ++s) {
-        const double bx = a.body[s][0], by = a.body[s][1], bz = a.body[s][2];
-        const double o[3] = {tm[0] * bx + tm[1] * by + tm[2] * bz, tm[3] * bx + tm[4] * by + tm[5] * bz,
-                             tm[6] * bx + tm[7] * by + tm[8] * bz};
-        for (int k = 0; k < 3; ++k) { sh.off_new[s][k] = o[k]; sh.off_new_f[s][k] = (float)o[k]; }
-      }
-      for (int k = 0; k < 3; ++k) sh.fix_new[k] = to_fixed(sh.com_new[k], iL[k]);
     }
     __syncthreads();
-    // dE over all other molecules of the chain
-    double part = 0.0;
-    {
-      const double* po = a.pk64 + (size_t)tg * W64;
-      double co[3] = {po[0], po[1], po[2]};
+    if ((int)threadIdx.x >= E0) {
+      // ---- energy warps: dE over every other molecule of the chain ----
+      R acc = R(0);
       R ro[NQ + 1][3], rn[NQ + 1][3];
-      uint32_t fo[3] = {a.fix[tg], a.fix[n + tg], a.fix[2 * n + tg]};
 #pragma unroll
       for (int s = 0; s <= NQ; ++s)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          ro[s][k] = MIXED ? (R)a.pk32f[(size_t)tg * 4 * NPK + 3 + 3 * s + k] : (R)po[3 + 3 * s + k];
-          rn[s][k] = MIXED ? (R)sh.off_new_f[s][k] : (R)sh.off_new[s][k];
-        }
-      const R rin2 = MIXED ? (R)a.cc.frin2 : (R)a.cc.rin2, rin = MIXED ? (R)a.cc.frin : (R)a.cc.rin;
-      const R rout = MIXED ? (R)a.cc.frout : (R)a.cc.rout;
-      const R c1 = MIXED ? (R)a.cc.fc1 : (R)a.cc.c1, c2 = MIXED ? (R)a.cc.fc2 : (R)a.cc.c2;
-      R acc = R(0);
-      for (int j = i0 + threadIdx.x; j < i1; j += blockDim.x) {
+        for (int k = 0; k < 3; ++k) { ro[s][k] = s_oo[s][k]; rn[s][k] = s_on[s][k]; }
+      const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
+      const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
+      for (int j = i0 + (int)threadIdx.x - E0; j < i1; j += NE) {
         if (j == tg) continue;
-        const double* pj = a.pk64 + (size_t)j * W64;
-        R rj[NQ + 1][3];
-        for (int pose = 0; pose < 2; ++pose) {
-          R d[3];
-          R dd;
-          bool in;
-          if (MIXED) {
-            const uint32_t* f = pose ? sh.fix_new : fo;
-            d[0] = (R)((float)(int)(f[0] - a.fix[j]) * fs[0]);
-            d[1] = (R)((float)(int)(f[1] - a.fix[n + j]) * fs[1]);
-            d[2] = (R)((float)(int)(f[2] - a.fix[2 * n + j]) * fs[2]);
-            dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-            in = dd < (R)a.cc.frout2;
-            if (fabs((double)dd - a.cc.rout2) < 1e-3) {
-              double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
-              in = exact_dd(pose ? sh.com_new : co, cj, L, iL, o, dx) < a.cc.rout2;
-            }
-          } else {
-            double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
-            const double ddd = exact_dd(pose ? sh.com_new : co, cj, L, iL, o, dx);
-            in = ddd < a.cc.rout2;
-            d[0] = (R)dx[0]; d[1] = (R)dx[1]; d[2] = (R)dx[2];
-            dd = (R)ddd;
+        R dO[3], dN[3], ddO, ddN;
+        bool inO, inN;
+        if (MIXED) {
+          uint32_t fj[3];
+          P::fix(a, j, fj);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            dO[k] = (R)((float)(int)(fo[k] - fj[k]) * fs[k]);
+            dN[k] = (R)((float)(int)(fn[k] - fj[k]) * fs[k]);
           }
-          if (!in) continue;
+          ddO = dO[0] * dO[0] + dO[1] * dO[1] + dO[2] * dO[2];
+          ddN = dN[0] * dN[0] + dN[1] * dN[1] + dN[2] * dN[2];
+          inO = ddO < (R)a.cc.frout2;
+          inN = ddN < (R)a.cc.frout2;
+          const bool bandO = fabsf((float)ddO - a.cc.frout2) < 1e-3f, bandN = fabsf((float)ddN - a.cc.frout2) < 1e-3f;
+          if (bandO || bandN) {   // borderline: the reference's FP64 test
+            double cj[3], o[3], dx[3];
+            P::com(a, j, cj);
+            if (bandO) inO = exact_dd(co, cj, L, iL, o, dx) < a.cc.rout2;
+            if (bandN) inN = exact_dd(cn, cj, L, iL, o, dx) < a.cc.rout2;
+          }
+        } else {
+          double cj[3], o[3], dx[3];
+          P::com(a, j, cj);
+          const double d0 = exact_dd(co, cj, L, iL, o, dx);
+          dO[0] = dx[0]; dO[1] = dx[1]; dO[2] = dx[2];
+          ddO = (R)d0;
+          inO = d0 < a.cc.rout2;
+          const double d1 = exact_dd(cn, cj, L, iL, o, dx);
+          dN[0] = dx[0]; dN[1] = dx[1]; dN[2] = dx[2];
+          ddN = (R)d1;
+          inN = d1 < a.cc.rout2;
+        }
+        if (inO || inN) {
+          R rj[NQ + 1][3];
 #pragma unroll
           for (int s = 0; s <= NQ; ++s)
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-              rj[s][k] = MIXED ? (R)a.pk32f[(size_t)j * 4 * NPK + 3 + 3 * s + k] : (R)pj[3 + 3 * s + k];
-          const R e = pose ? pair_energy<NQ, TAPER, R>(d, dd, rn, rj, a.pc, rin2, rin, rout, c1, c2)
-                           : pair_energy<NQ, TAPER, R>(d, dd, ro, rj, a.pc, rin2, rin, rout, c1, c2);
-          acc += pose ? e : -e;
+              rj[s][k] = MIXED ? (R)a.pk32f[(size_t)j * 4 * NPK + 3 + 3 * s + k] : (R)a.pk64[(size_t)j * W64 + 3 + 3 * s + k];
+          if (inO) acc -= pair_energy<NQ, TAPER, R>(dO, ddO, ro, rj, a.pc, rin2, rin, rout, c1);
+          if (inN) acc += pair_energy<NQ, TAPER, R>(dN, ddN, rn, rj, a.pc, rin2, rin, rout, c1);
         }
       }
-      part = (double)acc;
-    }
-    // fixed-order block reduction in FP64
 #pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) part += __shfl_xor_sync(0xffffffffu, part, m);
-    if ((threadIdx.x & 31) == 0) sh.part[threadIdx.x >> 5] = part;
-    if (LEARNED) mc_features<NQ>(a, tg, sh.com_new, sh.off_new, sh.feat_new, i0, i1, L, iL);
+      for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+      if (lane == 0) s_part[warp - NCTRL] = acc;
+    } else if constexpr (FEAT) {
+      // ---- control warps: feature neighbours of both poses, new-pose features ----
+      const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
+      const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
+      int cnt[2] = {0, 0};
+      for (int j0 = i0; j0 < i1; j0 += E0) {
+        const int j = j0 + (int)threadIdx.x;
+        bool qo = false, qn = false;
+        if (j < i1 && j != tg) {
+          float e[3];
+          if (MIXED) {
+            uint32_t fj[3];
+            P::fix(a, j, fj);
+            const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
+            qo = r2o < FEAT_RC2 && r2o > 0.0f;
+            qn = r2n < FEAT_RC2 && r2n > 0.0f;
+          } else {
+            double cj[3];
+            P::com(a, j, cj);
+            const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
+            qo = r2o < FEAT_RC2 && r2o > 0.0f;
+            qn = r2n < FEAT_RC2 && r2n > 0.0f;
+          }
+        }
+        queue_append(&s_q[0][warp * QSEG], cnt[0], qo, j, QSEG, a.flag);
+        queue_append(&s_q[1][warp * QSEG], cnt[1], qn, j, QSEG, a.flag);
+      }
+      if (lane == 0) { s_nq[0][warp] = min(cnt[0], QSEG); s_nq[1][warp] = min(cnt[1], QSEG); }
+      __syncwarp();
+      if (NCTRL > 1) asm volatile("bar.sync 1, %0;" ::"n"(32 * NCTRL));
+      if (warp == 0) {
+        // features of the target at the new pose: terms of every queued neighbour
+        int f[MLP_IN];
+#pragma unroll
+        for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
+        float un[4][3];
+#pragma unroll
+        for (int s = 0; s < 4; ++s)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) un[s][k] = s_un[s][k];
+        const int n0 = s_nq[1][0], nn = n0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
+        for (int p = lane; p < nn; p += 32) {
+          const int j = p < n0 ? s_q[1][p] : s_q[1][QSEG + p - n0];
+          float e[3], r2;
+          if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fn, fj, fs, e); }
+          else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cn, cj, L, iL, e); }
+          feat_terms(e, r2, un, 1, f);
+        }
+#pragma unroll
+        for (int k = 0; k < MLP_IN; ++k) {
+          const int v = __reduce_add_sync(0xffffffffu, f[k]);
+          if (lane == k) s_feat[k] = v;
+        }
+        __syncwarp();
+        if constexpr (LEARN) {
+          double st2, sr2;
+          mlp_widths_warp(s_mlp, 0, s_feat, a.mlp.sigma0_t, a.mlp.sigma0_r, st2, sr2);
+          if (lane == 0) { s_sig_new[0] = st2; s_sig_new[1] = sr2; }
+        }
+      } else if constexpr (LEARN) {
+        // warp 1: widths of the next trial's target at its current pose
+        // (used unless this trial's move changes its features)
+        if (tb + 1 < MC_NB && t + 1 < a.ntrial) {
+          const int tg1 = i0 + s_tg[tb + 1];
+          double st1, sr1;
+          mlp_widths_warp(s_mlp, 1, a.fcache + (size_t)tg1 * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st1, sr1);
+          if (lane == 0) { s_spec[0] = st1; s_spec[1] = sr1; s_spec_tg = tg1; }
+        } else if (lane == 0) {
+          s_spec_tg = -1;
+        }
+      }
+    }
     __syncthreads();
-    if (LEARNED && threadIdx.x < 32) {
-      double st2, sr2;
-      mlp_widths(a.mlp, sh.feat_new, &st2, &sr2);
-      if (threadIdx.x == 0) {
-        // log q(old|new) - log q(new|old) for isotropic Gaussians in translation and rotation vector
-        double d2 = sh.dx[0] * sh.dx[0] + sh.dx[1] * sh.dx[1] + sh.dx[2] * sh.dx[2];
-        double r2 = sh.rot[0] * sh.rot[0] + sh.rot[1] * sh.rot[1] + sh.rot[2] * sh.rot[2];
-        const double lf = -3.0 * log(sh.sig_t) - d2 / (2.0 * sh.sig_t * sh.sig_t) - 3.0 * log(sh.sig_r) -
-                          r2 / (2.0 * sh.sig_r * sh.sig_r);
-        const double lr = -3.0 * log(st2) - d2 / (2.0 * st2 * st2) - 3.0 * log(sr2) - r2 / (2.0 * sr2 * sr2);
-        sh.logq_fwd = lr - lf;
+    // ---- warp 0: acceptance, state update, feature cache ----
+    if (warp == 0) {
+      R v = lane < NEW ? s_part[lane] : R(0);
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+      const double dE = (double)__shfl_sync(0xffffffffu, v, 0);
+      int acc_flag = 0;
+      if (lane == 0) {
+        float logh = 0.0f;
+        if (LEARN)
+          logh = log_q((float)s_sig_new[0], (float)s_sig_new[1], d2f, r2f) - log_q((float)st_old, (float)sr_old, d2f, r2f);
+        const double x = -(dE * I2J * J2K) * beta + (double)logh;
+        const bool ok = x >= 0.0 || s_lu[tb] < x;
+        acc_flag = ok ? 1 : 0;
+        if (a.trace) a.trace[((size_t)c * a.ntrial + t) * 4 + 0] = dE;
+        if (ok) {
+          double qn[4];
+          double* p = a.pk64 + (size_t)tg * W64;
+          if (MIXED) {   // FP64 orientation and offsets from the FP64 draws
+            double off64[NQ + 1][3];
+            double qold[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
+            trial_rotation<double, NQ>(rot_d, qold, a.body, qn, off64);
+#pragma unroll
+            for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = off64[s][k];
+          } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qn[k] = (double)qn_trial[k];
+#pragma unroll
+            for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = (double)s_on[s][k];
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) a.st[(size_t)(33 + k) * n + tg] = qn[k];
+          float* pf = a.pk32f + (size_t)tg * 4 * NPK;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            a.st[(size_t)k * n + tg] = s_cn[k];
+            p[k] = s_cn[k];
+            pf[k] = __uint_as_float(s_fn[k]);
+            a.fix[(size_t)k * n + tg] = s_fn[k];
+          }
+#pragma unroll
+          for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) pf[3 + 3 * s + k] = (float)s_on[s][k];
+          energy += dE;
+          ++nacc;
+        }
+        if (a.trace) {
+          double* tr = a.trace + ((size_t)c * a.ntrial + t) * 4;
+          tr[1] = energy; tr[2] = (double)acc_flag; tr[3] = (double)(tg - i0);
+        }
+        if (a.samples && a.sample_every > 0 && (t + 1) % a.sample_every == 0)
+          a.samples[(size_t)c * a.nsamples + nsample] = energy;
       }
-    }
-    if (threadIdx.x == 0) {
-      double dE = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) dE += sh.part[w];
-      double u[2];
-      uniform2(a.seed, (uint32_t)c, (uint32_t)trial, (uint32_t)(trial >> 32), 0u, u);
-      const double logh = LEARNED ? sh.logq_fwd : 0.0;
-      bool acc = false;
-      const double x = -(dE * I2J * J2K) * beta + logh;
-      if (x >= 0.0) acc = true;
-      else acc = u[1] < exp(x);
-      sh.accept = acc ? 1 : 0;
-      sh.dE = dE;
-      if (LEARNED && a.records) {   // training record of this trial
-        float* rr = a.records + ((size_t)c * a.ntrial + t) * MLP_REC;
-        for (int k = 0; k < MLP_IN; ++k) { rr[k] = sh.feat_old[k]; rr[MLP_IN + k] = sh.feat_new[k]; }
-        rr[2 * MLP_IN] = (float)(sh.dx[0] * sh.dx[0] + sh.dx[1] * sh.dx[1] + sh.dx[2] * sh.dx[2]);
-        rr[2 * MLP_IN + 1] = (float)(sh.rot[0] * sh.rot[0] + sh.rot[1] * sh.rot[1] + sh.rot[2] * sh.rot[2]);
-        rr[2 * MLP_IN + 2] = (float)(dE * I2J * J2K * beta);
+      acc_flag = __shfl_sync(0xffffffffu, acc_flag, 0);
+      if constexpr (FEAT) {
+        if (MODE == G6_MC_COLLECT && a.records) {   // training record of this trial
+          float* rr = a.records + ((size_t)c * a.ntrial + t) * MLP_REC;
+          if (lane < MLP_IN) {
+            rr[lane] = (float)a.fcache[(size_t)tg * MLP_IN + lane] * FEAT_IQ;
+            rr[MLP_IN + lane] = (float)s_feat[lane] * FEAT_IQ;
+          }
+          if (lane == 0) {
+            rr[2 * MLP_IN] = d2f;
+            rr[2 * MLP_IN + 1] = r2f;
+            rr[2 * MLP_IN + 2] = (float)(dE * I2J * J2K * beta);
+          }
+        }
+        const int o0 = s_nq[0][0], no = o0 + (NCTRL > 1 ? s_nq[0][NCTRL - 1] : 0);
+        const int m0 = s_nq[1][0], nn = m0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
+        if (acc_flag) {
+          __syncwarp();
+          if (lane < MLP_IN) a.fcache[(size_t)tg * MLP_IN + lane] = s_feat[lane];
+          // neighbours of both poses: remove the old term, add the new one
+          const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
+          const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
+          bool hit = false;
+          for (int p = lane; p < no + nn; p += 32) {
+            const bool old_pose = p < no;
+            const int po = old_pose ? p : p - no;
+            const int j = old_pose ? (po < o0 ? s_q[0][po] : s_q[0][QSEG + po - o0])
+                                   : (po < m0 ? s_q[1][po] : s_q[1][QSEG + po - m0]);
+            hit = hit || j == s_spec_tg;
+            float e[3], r2;
+            if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
+            else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
+            float o[(NQ + 1) * 3], u[4][3];
+            P::offsets(a, j, o);
+            site_dirs<NQ>(o, u);
+            int g[MLP_IN];
+#pragma unroll
+            for (int k = 0; k < MLP_IN; ++k) g[k] = 0;
+            feat_terms(e, r2, u, old_pose ? -1 : 1, g);
+            int* fc = a.fcache + (size_t)j * MLP_IN;
+#pragma unroll
+            for (int k = 0; k < MLP_IN; ++k)
+              if (g[k] != 0) atomicAdd(fc + k, g[k]);
+          }
+          if (LEARN && (__any_sync(0xffffffffu, hit) || s_spec_tg == tg) && lane == 0) s_spec_tg = -1;
+        }
       }
-      if (a.trace) a.trace[((size_t)c * a.ntrial + t) * 4 + 0] = dE;
-    }
-    __syncthreads();
-    if (sh.accept) {
-      // write the new pose (state, packed poses, fixed point); one thread per field group
-      if (threadIdx.x == 0) {
-        for (int k = 0; k < 3; ++k) a.st[(size_t)k * n + tg] = sh.com_new[k];
-        for (int k = 0; k < 4; ++k) a.st[(size_t)(33 + k) * n + tg] = sh.q_new[k];
-        double* p = a.pk64 + (size_t)tg * W64;
-        for (int k = 0; k < 3; ++k) p[k] = sh.com_new[k];
-        for (int s = 0; s <= NQ; ++s)
-          for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = sh.off_new[s][k];
-        float* pf = a.pk32f + (size_t)tg * 4 * NPK;
-        for (int k = 0; k < 3; ++k) pf[k] = __uint_as_float(sh.fix_new[k]);
-        for (int s = 0; s <= NQ; ++s)
-          for (int k = 0; k < 3; ++k) pf[3 + 3 * s + k] = sh.off_new_f[s][k];
-        for (int k = 0; k < 3; ++k) a.fix[(size_t)k * n + tg] = sh.fix_new[k];
-      }
-      energy += sh.dE;
-      ++nacc;
-    }
-    if (threadIdx.x == 0 && a.trace) {
-      a.trace[((size_t)c * a.ntrial + t) * 4 + 1] = energy;
-      a.trace[((size_t)c * a.ntrial + t) * 4 + 2] = (double)sh.accept;
-      a.trace[((size_t)c * a.ntrial + t) * 4 + 3] = (double)(tg - i0);
-    }
-    if (a.samples && a.sample_every > 0 && (t + 1) % a.sample_every == 0 && threadIdx.x == 0) {
-      a.samples[(size_t)c * a.nsamples + nsample] = energy;
     }
     if (a.sample_every > 0 && (t + 1) % a.sample_every == 0) ++nsample;
-    __syncthreads();
   }
   if (threadIdx.x == 0) {
     a.energy[c] = energy;
@@ -317,23 +729,24 @@ __global__ void __launch_bounds__(256) k_mc(McArgs a) {
   }
 }
 
-template <int NQ, bool TAPER>
-static cudaError_t launch_mc_t(const McArgs& a, bool mixed, bool learned, cudaStream_t s) {
+template <int NQ, bool TAPER, bool MIXED>
+static cudaError_t launch_mc_m(const McArgs& a, int mode, cudaStream_t s) {
   const int nb = a.rep.nrep;
-  if (mixed) {
-    if (learned) k_mc<NQ, TAPER, true, true><<<nb, 256, 0, s>>>(a);
-    else k_mc<NQ, TAPER, true, false><<<nb, 256, 0, s>>>(a);
-  } else {
-    if (learned) k_mc<NQ, TAPER, false, true><<<nb, 256, 0, s>>>(a);
-    else k_mc<NQ, TAPER, false, false><<<nb, 256, 0, s>>>(a);
-  }
+  if (mode == G6_MC_LEARNED) k_mc<NQ, TAPER, MIXED, G6_MC_LEARNED><<<nb, MC_NT, 0, s>>>(a);
+  else if (mode == G6_MC_COLLECT) k_mc<NQ, TAPER, MIXED, G6_MC_COLLECT><<<nb, MC_NT, 0, s>>>(a);
+  else k_mc<NQ, TAPER, MIXED, G6_MC_PLAIN><<<nb, MC_NT, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mc(const McArgs& a, int model, bool mixed, bool learned, cudaStream_t s) {
-  if (model == G6_TIP4P) return launch_mc_t<3, false>(a, mixed, learned, s);
-  if (a.pc.taper) return launch_mc_t<4, true>(a, mixed, learned, s);
-  return launch_mc_t<4, false>(a, mixed, learned, s);
+template <int NQ, bool TAPER>
+static cudaError_t launch_mc_t(const McArgs& a, bool mixed, int mode, cudaStream_t s) {
+  return mixed ? launch_mc_m<NQ, TAPER, true>(a, mode, s) : launch_mc_m<NQ, TAPER, false>(a, mode, s);
+}
+
+cudaError_t launch_mc(const McArgs& a, int model, bool mixed, int mode, cudaStream_t s) {
+  if (model == G6_TIP4P) return launch_mc_t<3, false>(a, mixed, mode, s);
+  if (a.pc.taper) return launch_mc_t<4, true>(a, mixed, mode, s);
+  return launch_mc_t<4, false>(a, mixed, mode, s);
 }
 
 }  // namespace g6

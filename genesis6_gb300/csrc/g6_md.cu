@@ -5,7 +5,8 @@
 //   per thread, writing pose buffer 0, plus the first Nose_Predict of a run.
 // The Gear corrector and the per-step reductions run in the epilogue of the
 // fused force kernel (g6_force.cu) through the device functions of g6_rigid.cuh.
-// Everything here is FP64.
+// k_stf_move / k_begin_mixed: state moves and the first step of a
+// mixed-precision run (float SoA for the small Gear terms).
 #include <cuda_runtime.h>
 
 #include "g6_internal.cuh"
@@ -37,6 +38,55 @@ cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* 
                                  cudaStream_t s) {
   const int blocks = a.n > 0 ? (a.n + 127) / 128 : 1;
   k_predict_place<<<blocks, 128, 0, s>>>(a, do_predict, th, nose_predict);
+  return cudaGetLastError();
+}
+
+// Mixed-precision runs: the small Gear terms move from the FP64 state into
+// the float SoA at the start of a run (to_float) and back at its end, so the
+// FP64 state is the complete rigid record whenever no run is active.
+__global__ void k_stf_move(double* st, float* stf, int n, int to_float) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * STF_COLS) return;
+  const int c = (int)(t / n), i = (int)(t % n);
+  int sc;   // state column of float column c
+  if (c < STF_W2) sc = 6 + c;                      // d2..d5
+  else if (c < STF_Q2) sc = 21 + (c - STF_W2);     // w2..w5
+  else sc = 37 + (c - STF_Q2);                     // q2..q5 stacks
+  if (to_float) stf[t] = (float)st[(size_t)sc * n + i];
+  else st[(size_t)sc * n + i] = (double)stf[t];
+}
+
+// First predict + placement of a mixed run (plus the first Nose_Predict).
+__global__ void k_begin_mixed(PlaceArgs a, float* stf, ThermoDev* th) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0) {
+    for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
+      ThermoDev& T = th[r];
+      if (T.kind == G6_NOSE) {
+        T.z[0] = T.z[0] + T.z[1] + T.z[2] + T.z[3] + T.z[4];
+        T.z[1] = T.z[1] + 2.0 * T.z[2] + 3.0 * T.z[3] + 4.0 * T.z[4];
+        T.z[2] = T.z[2] + 3.0 * T.z[3] + 6.0 * T.z[4];
+        T.z[3] = T.z[3] + 4.0 * T.z[4];
+      }
+    }
+  }
+  if (i >= a.n) return;
+  double x[3], q[4];
+  predict_mixed(a.st, stf, a.n, i, x, q);
+  if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.fix);
+  else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.fix);
+}
+
+cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s) {
+  const long long total = (long long)n * STF_COLS;
+  if (total == 0) return cudaSuccess;
+  k_stf_move<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(st, stf, n, to_float);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, cudaStream_t s) {
+  const int blocks = a.n > 0 ? (a.n + 127) / 128 : 1;
+  k_begin_mixed<<<blocks, 128, 0, s>>>(a, stf, th);
   return cudaGetLastError();
 }
 

@@ -213,7 +213,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   PlaceArgs pa;
   pa.n = n; pa.nq = mh.nq; pa.npk = pk32_width(model); pa.w64 = pk64_width(model); pa.rep = rep;
   for (int q = 0; q < MAXSITE; ++q)
-    for (int k = 0; k < 3; ++k) pa.body[q][k] = mh.body[q][k];
+    for (int k = 0; k < 3; ++k) { pa.body[q][k] = mh.body[q][k]; pa.fbody[q][k] = (float)mh.body[q][k]; }
   pa.st = (double*)(base + O_ST); pa.tmat = (double*)(base + O_TMAT); pa.pk64 = (double*)(base + O_PK64);
   pa.pk32 = (float4*)(base + O_PK32); pa.fix = (uint32_t*)(base + O_FIX);
 
@@ -222,6 +222,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   ca.count = (int*)(base + O_COUNT); ca.ctrl = nullptr;
 
   ListArgs la;
+  std::memset(&la, 0, sizeof la);   // fix_build stays NULL: no displacement bookkeeping here
   la.n = n; la.cap = CAP; la.rep = rep; la.g = g; la.cell = ca.cell; la.start = (const int*)(base + O_START);
   la.cellmol = (const int*)(base + O_CELLMOL); la.fix = pa.fix; la.fix1 = pa.fix; la.com = pa.st; la.com_build = (double*)(base + O_COMB);
   la.rlist2 = (float)(rlist * rlist) + 1e-3f; la.nbr = (int*)(base + O_NBR); la.nnb = (int*)(base + O_NNB);

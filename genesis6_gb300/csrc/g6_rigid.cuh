@@ -13,7 +13,8 @@
 //                 the partials in a fixed order, computes T, P and the conserved
 //                 quantity (Mixture.F90:2251-2264, 2431-2453), runs Nose_Correct and the
 //                 next Nose_Predict (NoseModule.F90:43-87) and sets the rebuild flag.
-// All FP64.
+// The plain path is all FP64; the mixed path (correct_mixed, predict_mixed,
+// place_mixed) keeps FP64 for com, d1, w1 and q and float for the rest.
 #pragma once
 
 #include "g6_internal.cuh"
@@ -131,7 +132,7 @@ __device__ __forceinline__ PoseBuf pose_buf(const StepArgs& a, int which) {
 // rigid_correct + energy/virial/kinetic terms + the next predict and placement
 // for molecule i.  F: COM force; tl: lab-frame torque; cur/next: pose buffers.
 __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const double F[3], const double tl[3],
-                                            double emol, const double wmol[9], double npair_half, int step,
+                                            double emol, double wtr, double npair_half, int step,
                                             bool predict_next, const PoseBuf& cur, const PoseBuf& next,
                                             double (&v)[NRED], double& dmax2, int& bad) {
   const int n = a.p.n;
@@ -239,20 +240,13 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
   for (int k = 1; k < 5; ++k)
 #pragma unroll
     for (int c = 0; c < 4; ++c) G6_ST(33 + 4 * k + c) = Q[k][c];
-  // reductions: Epot, virial, kinetic sums, kinetic tensor, pairs
+  // reductions: Epot, virial trace, kinetic sums (Rigid_Ek), pairs
   const double d1[3] = {G6_ST(3), G6_ST(4), G6_ST(5)};
   v[0] = emol;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) v[1 + k] = wmol[k];
-  v[10] = d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2];
-  v[11] = W[0][0] * W[0][0];
-  v[12] = W[0][1] * W[0][1];
-  v[13] = W[0][2] * W[0][2];
-#pragma unroll
-  for (int p = 0; p < 3; ++p)
-#pragma unroll
-    for (int q = 0; q < 3; ++q) v[14 + 3 * p + q] = d1[p] * d1[q];
-  v[23] = npair_half;
+  v[1] = wtr;
+  v[2] = d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2];
+  v[3] = a.I[0] * (W[0][0] * W[0][0]) + a.I[1] * (W[0][1] * W[0][1]) + a.I[2] * (W[0][2] * W[0][2]);
+  v[4] = npair_half;
   if (predict_next) {
     predict_one(st, n, i);
     place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.fix);
@@ -263,61 +257,304 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
   }
 }
 
-// Per-block partial sums, segmented by replica (molecules are in replica
-// order; a block spans replicas rfirst..rfirst+nslots-1 <= MAXREP_PER_BLOCK).
-// Every thread of the block calls it; r = -1 contributes nothing.
-template <int NV, int NWARP>
-__device__ void block_segmented_sum(const double (&v)[NV], int r, int rfirst, int nslots, double* out_part) {
-  __shared__ double sh[NWARP][NV];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int s = 0; s < nslots; ++s) {
-    const bool mine = (r == rfirst + s);
+// ---------------------------------------------------------------------------
+// Mixed precision: the FP64 state holds com, d1, w1 and q; the small Gear
+// terms live in the float SoA stf.  Every FP64 instruction here is one the
+// update of a FP64 quantity needs (GB300 issues FP64 at 1/64 of the FP32 rate).
+// ---------------------------------------------------------------------------
+#define G6_SF(c) stf[(size_t)(c) * n + i]
+
+__device__ __forceinline__ void setmatrix_f(const float q[4], float t[9]) {
+  const float qa = q[0], qb = q[1], qc = q[2], qd = q[3];
+  t[0] = (qa * qa + qb * qb - (qc * qc + qd * qd));
+  t[1] = -2.0f * (qa * qd + qb * qc);
+  t[2] = 2.0f * (qb * qd - qa * qc);
+  t[3] = 2.0f * (qa * qd - qb * qc);
+  t[4] = qa * qa + qc * qc - (qb * qb + qd * qd);
+  t[5] = -2.0f * (qa * qb + qc * qd);
+  t[6] = 2.0f * (qa * qc + qb * qd);
+  t[7] = 2.0f * (qa * qb - qc * qd);
+  t[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
+}
+
+__device__ __forceinline__ void qdot_f(const float w[3], const float q[4], float o[4]) {
+  o[0] = (-w[0] * q[1] + w[1] * q[2] - w[2] * q[3]);
+  o[1] = (w[0] * q[0] - w[1] * q[3] - w[2] * q[2]);
+  o[2] = (-w[0] * q[3] - w[1] * q[0] + w[2] * q[1]);
+  o[3] = (w[0] * q[2] + w[1] * q[1] + w[2] * q[0]);
+}
+
+// Uniform in (0, 1] from one Philox output word, and a float normal pair.
+__device__ __forceinline__ float uniform_f(uint32_t x) { return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f); }
+
+// Placement into a pose buffer from the FP64 com and (normalised) q:
+// fixed-point com (x * 2^32 / L, wrapped), float site offsets, FP64 com.
+template <int NQ>
+__device__ __forceinline__ void place_mixed(const PlaceArgs& a, int i, const double x[3], const double q[4],
+                                            double* pk64, float4* pk32, uint32_t* fix) {
+  constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
+  const int n = a.n;
+  const int r = a.rep.mol_rep[i];
+  const float qf[4] = {(float)q[0], (float)q[1], (float)q[2], (float)q[3]};
+  float t[9];
+  setmatrix_f(qf, t);
+  float w[24];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double x = mine ? v[k] : 0.0;
+  for (int k = 0; k < 24; ++k) w[k] = 0.0f;
 #pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
-      if (lane == 0) sh[warp][k] = x;
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t f = (uint32_t)(unsigned long long)__double2ll_rn(x[k] * (a.rep.invL[3 * r + k] * 4294967296.0));
+    fix[(size_t)k * n + i] = f;
+    w[k] = __uint_as_float(f);
+    pk64[(size_t)i * a.w64 + k] = x[k];
+  }
+#pragma unroll
+  for (int s = 0; s <= NQ; ++s) {
+    const float bx = a.fbody[s][0], by = a.fbody[s][1], bz = a.fbody[s][2];
+    w[3 + 3 * s] = t[0] * bx + t[1] * by + t[2] * bz;
+    w[4 + 3 * s] = t[3] * bx + t[4] * by + t[5] * bz;
+    w[5 + 3 * s] = t[6] * bx + t[7] * by + t[8] * bz;
+  }
+#pragma unroll
+  for (int q4 = 0; q4 < NPK; ++q4)
+    pk32[(size_t)i * NPK + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+}
+
+// rigid_predict (RigidModule.F90:480-559) with the small terms in float.
+__device__ __forceinline__ void predict_mixed(double* st, float* stf, int n, int i, double x[3], double q[4]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float d2 = G6_SF(STF_D2 + c), d3 = G6_SF(STF_D2 + 3 + c), d4 = G6_SF(STF_D2 + 6 + c),
+                d5 = G6_SF(STF_D2 + 9 + c);
+    const double d1 = G6_ST(3 + c);
+    x[c] = G6_ST(c) + d1 + (double)(d2 + d3 + d4 + d5);
+    G6_ST(c) = x[c];
+    G6_ST(3 + c) = d1 + (double)(2.0f * d2 + 3.0f * d3 + 4.0f * d4 + 5.0f * d5);
+    G6_SF(STF_D2 + c) = d2 + 3.0f * d3 + 6.0f * d4 + 10.0f * d5;
+    G6_SF(STF_D2 + 3 + c) = d3 + 4.0f * d4 + 10.0f * d5;
+    G6_SF(STF_D2 + 6 + c) = d4 + 5.0f * d5;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float w2 = G6_SF(STF_W2 + c), w3 = G6_SF(STF_W2 + 3 + c), w4 = G6_SF(STF_W2 + 6 + c),
+                w5 = G6_SF(STF_W2 + 9 + c);
+    G6_ST(18 + c) = G6_ST(18 + c) + (double)(w2 + w3 + w4 + w5);
+    G6_SF(STF_W2 + c) = w2 + 2.0f * w3 + 3.0f * w4 + 4.0f * w5;
+    G6_SF(STF_W2 + 3 + c) = w3 + 3.0f * w4 + 6.0f * w5;
+    G6_SF(STF_W2 + 6 + c) = w4 + 4.0f * w5;
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float q2 = G6_SF(STF_Q2 + c), q3 = G6_SF(STF_Q2 + 4 + c), q4 = G6_SF(STF_Q2 + 8 + c),
+                q5 = G6_SF(STF_Q2 + 12 + c);
+    q[c] = G6_ST(33 + c) + (double)(q2 + q3 + q4 + q5);
+    G6_SF(STF_Q2 + c) = q2 + 2.0f * q3 + 3.0f * q4 + 4.0f * q5;
+  }
+  // 1/|q|: float estimate, one Newton step in FP64 (|q|^2 = 1 + O(1e-6))
+  const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  double re = (double)rsqrtf((float)n2);
+  re = re * (1.5 - 0.5 * n2 * re * re);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) { q[c] *= re; G6_ST(33 + c) = q[c]; }
+}
+
+// rigid_correct (RigidModule.F90:1255-1487) with FP64 updates of com, d1, w1
+// and q only.  F: COM force, tl: lab torque (float); outputs the kinetic sums.
+template <int NQ>
+__device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const float F[3], const float tl[3], int step,
+                                              bool predict_next, const PoseBuf& next, float& ekt2, float& ekr2,
+                                              float& dmax2, int& bad) {
+  const int n = a.p.n;
+  double* st = a.p.st;
+  float* stf = a.stf;
+  const int r = a.p.rep.mol_rep[i];
+  const ThermoDev th = a.th[r];
+  const float dt = (float)a.dt;
+  double qd[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
+  const float qf[4] = {(float)qd[0], (float)qd[1], (float)qd[2], (float)qd[3]};
+  float t[9];
+  setmatrix_f(qf, t);
+  const float tau[3] = {t[0] * tl[0] + t[3] * tl[1] + t[6] * tl[2], t[1] * tl[0] + t[4] * tl[1] + t[7] * tl[2],
+                        t[2] * tl[0] + t[5] * tl[1] + t[8] * tl[2]};
+  if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]) && isfinite(tau[0]) && isfinite(tau[1]) &&
+        isfinite(tau[2])))
+    bad = 1;
+  float ext_t = 0.0f, ext_r = 0.0f;
+  if (th.kind == G6_NOSE) {
+    ext_r = (float)(th.z[0] * a.dt);
+    ext_t = 0.5f * ext_r;
+  }
+  // COM: Gear-5
+  const float cf = (float)(a.dt * a.dt * 0.5 / a.mass);
+  double d1d[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    d1d[c] = G6_ST(3 + c);
+    const float nf = F[c] * cf - (float)d1d[c] * ext_t;
+    const float delta = nf - G6_SF(STF_D2 + c);
+    G6_ST(c) = G6_ST(c) + (double)((float)G50 * delta);
+    d1d[c] = d1d[c] + (double)((float)G51 * delta);
+    G6_SF(STF_D2 + c) = nf;
+    G6_SF(STF_D2 + 3 + c) += (float)G53 * delta;
+    G6_SF(STF_D2 + 6 + c) += (float)G54 * delta;
+    G6_SF(STF_D2 + 9 + c) += (float)G55 * delta;
+  }
+  // quaternion value
+  double w1d[3] = {G6_ST(18), G6_ST(19), G6_ST(20)};
+  const float w1f[3] = {(float)w1d[0], (float)w1d[1], (float)w1d[2]};
+  float nw[4];
+  qdot_f(w1f, qf, nw);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float dw = nw[c] * dt * 0.5f - G6_SF(STF_Q2 + c);
+    qd[c] = qd[c] + (double)((float)G40 * dw);
+    G6_ST(33 + c) = qd[c];
+  }
+  // angular velocity: Gear-4 with Euler's equations
+  const float Ix = (float)a.I[0], Iy = (float)a.I[1], Iz = (float)a.I[2];
+  float nf[3];
+  nf[0] = (tau[0] + (Iy - Iz) * w1f[1] * w1f[2]) * dt / Ix - w1f[0] * ext_r;
+  nf[1] = (tau[1] + (Iz - Ix) * w1f[2] * w1f[0]) * dt / Iy - w1f[1] * ext_r;
+  nf[2] = (tau[2] + (Ix - Iy) * w1f[0] * w1f[1]) * dt / Iz - w1f[2] * ext_r;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float delta = nf[c] - G6_SF(STF_W2 + c);
+    w1d[c] = w1d[c] + (double)((float)G40 * delta);
+    G6_SF(STF_W2 + c) = nf[c];
+    G6_SF(STF_W2 + 3 + c) += (float)G42 * delta;
+    G6_SF(STF_W2 + 6 + c) += (float)G43 * delta;
+    G6_SF(STF_W2 + 9 + c) += (float)G44 * delta;
+  }
+  if (th.kind == G6_ANDERSEN) {   // stochastic collisions (float draws)
+    uint32_t ctr[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, 0u};
+    philox4x32(ctr, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+    if (uniform_f(ctr[0]) <= (float)(th.rate * a.dt)) {
+      const float kT = (float)(th.temp * RGAS * J2I);
+      float z[6];
+      for (int p = 0; p < 3; ++p) {
+        uint32_t g[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, (uint32_t)(p + 1)};
+        philox4x32(g, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+        const float rr = sqrtf(-2.0f * logf(uniform_f(g[0])));
+        float sn, cs;
+        sincospif(2.0f * uniform_f(g[1]), &sn, &cs);
+        z[2 * p] = rr * sn;
+        z[2 * p + 1] = rr * cs;
+      }
+      const float sv = sqrtf(kT / (float)a.mass) * dt;
+      for (int c = 0; c < 3; ++c) d1d[c] = (double)(z[c] * sv);
+      w1d[0] = (double)(z[3] * sqrtf(kT / Ix));
+      w1d[1] = (double)(z[4] * sqrtf(kT / Iy));
+      w1d[2] = (double)(z[5] * sqrtf(kT / Iz));
     }
-    __syncthreads();
-    if (threadIdx.x < NV) {
-      double x = 0.0;
-      for (int w = 0; w < NWARP; ++w) x += sh[w][threadIdx.x];
-      out_part[s * NV + threadIdx.x] = x;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { G6_ST(3 + c) = d1d[c]; G6_ST(18 + c) = w1d[c]; }
+  // quaternion stacks from the corrected angular-velocity stack
+  float W[5][3], Q[5][4], tq[4], uq[4], vq[4], xq[4];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    W[0][c] = (float)w1d[c];
+#pragma unroll
+    for (int k = 1; k < 5; ++k) W[k][c] = G6_SF(STF_W2 + 3 * (k - 1) + c);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[0][c] = (float)qd[c];
+  qdot_f(W[0], Q[0], tq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[1][c] = tq[c] * dt * 0.5f;
+  qdot_f(W[1], Q[0], tq); qdot_f(W[0], Q[1], uq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[2][c] = (tq[c] + uq[c]) * dt * 0.25f;
+  qdot_f(W[2], Q[0], tq); qdot_f(W[0], Q[2], uq); qdot_f(W[1], Q[1], vq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[3][c] = (tq[c] + uq[c] + vq[c]) * dt * (1.0f / 6.0f);
+  qdot_f(W[3], Q[0], tq); qdot_f(W[2], Q[1], uq); qdot_f(W[1], Q[2], vq); qdot_f(W[0], Q[3], xq);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) Q[4][c] = (tq[c] + uq[c] + vq[c] + xq[c]) * dt * (1.0f / 8.0f);
+#pragma unroll
+  for (int k = 1; k < 5; ++k)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) G6_SF(STF_Q2 + 4 * (k - 1) + c) = Q[k][c];
+  // kinetic sums (Rigid_Ek)
+  const float d1f[3] = {(float)d1d[0], (float)d1d[1], (float)d1d[2]};
+  ekt2 = d1f[0] * d1f[0] + d1f[1] * d1f[1] + d1f[2] * d1f[2];
+  ekr2 = Ix * (W[0][0] * W[0][0]) + Iy * (W[0][1] * W[0][1]) + Iz * (W[0][2] * W[0][2]);
+  if (predict_next) {
+    double x[3], q[4];
+    predict_mixed(st, stf, n, i, x, q);
+    place_mixed<NQ>(a.p, i, x, q, next.pk64, next.pk32, next.fix);
+    const float* fs = a.p.rep.fscale + 3 * r;
+    float dd = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float e = (float)(int)(next.fix[(size_t)c * n + i] - a.fix_build[(size_t)c * n + i]) * fs[c];
+      dd += e * e;
     }
-    __syncthreads();
+    dmax2 = dd;
+    if (!isfinite(dd) || !isfinite(x[0]) || !isfinite(x[1]) || !isfinite(x[2])) { bad = 1; dmax2 = 3.0e38f; }
   }
 }
 
-// Block partials, then the last block to arrive finalises the step.
-// mpb: molecules covered by one block (blocks are in molecule order).
-template <int NTHREADS>
-__device__ void step_reduce(const StepArgs& a, const double (&v)[NRED], int r, double dmax2, int bad, int mpb,
-                            int step, bool predict_next) {
+#undef G6_SF
+
+// ---------------------------------------------------------------------------
+// Per-step reductions.  Warp 0 of each block holds one molecule per lane; it
+// sums the NRED quantities per replica slot (FP64 in the plain path, float
+// pairs with error-free addition in the mixed path), writes the block
+// partials, and the last block to arrive sums the partials in a fixed order.
+// ---------------------------------------------------------------------------
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (b.hi - bp);
+  const float t = e + (a.lo + b.lo);
+  const float h = s + t;
+  return FF{h, t - (h - s)};
+}
+__device__ __forceinline__ FF red_zero(FF) { return FF{0.0f, 0.0f}; }
+__device__ __forceinline__ double red_zero(double) { return 0.0; }
+__device__ __forceinline__ FF red_add(FF a, FF b) { return ff_add(a, b); }
+__device__ __forceinline__ double red_add(double a, double b) { return a + b; }
+__device__ __forceinline__ FF red_shfl(FF v, int m) {
+  return FF{__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+}
+__device__ __forceinline__ double red_shfl(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double red_double(FF v) { return (double)v.hi + (double)v.lo; }
+__device__ __forceinline__ double red_double(double v) { return v; }
+
+template <class V>
+__device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step,
+                            bool predict_next) {
   const int n = a.p.n;
-  const int first_i = blockIdx.x * mpb;
-  const int last_i = min(n, first_i + mpb) - 1;
-  const int rfirst = a.p.rep.mol_rep[first_i];
-  const int nslots = a.p.rep.mol_rep[last_i] - rfirst + 1;
-  block_segmented_sum<NRED, NTHREADS / 32>(v, r, rfirst, nslots, a.part + (size_t)blockIdx.x * MAXREP_PER_BLOCK * NRED);
-  {
-    __shared__ double shm[NTHREADS / 32];
-    __shared__ int shbad[NTHREADS / 32];
-    double m = dmax2;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int first_i = blockIdx.x * mpb;
+    const int last_i = min(n, first_i + mpb) - 1;
+    const int rfirst = a.p.rep.mol_rep[first_i];
+    const int nslots = a.p.rep.mol_rep[last_i] - rfirst + 1;
+    for (int s = 0; s < nslots; ++s) {
+      const bool mine = (r == rfirst + s);
+#pragma unroll
+      for (int k = 0; k < NRED; ++k) {
+        V x = mine ? v[k] : red_zero(v[k]);
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) x = red_add(x, red_shfl(x, m));
+        if (lane == 0) a.part[((size_t)blockIdx.x * MAXREP_PER_BLOCK + s) * NRED + k] = red_double(x);
+      }
+    }
+    float m = dmax2;
     int b = bad;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
-      m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+      m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
       b |= __shfl_xor_sync(0xffffffffu, b, o);
     }
-    if ((threadIdx.x & 31) == 0) { shm[threadIdx.x >> 5] = m; shbad[threadIdx.x >> 5] = b; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double mm = 0.0;
-      int bb = 0;
-      for (int w = 0; w < NTHREADS / 32; ++w) { mm = fmax(mm, shm[w]); bb |= shbad[w]; }
-      a.partmax[blockIdx.x] = mm;
-      if (bb) atomicOr(&a.ctrl[3], 1);
+    if (lane == 0) {
+      a.partmax[blockIdx.x] = (double)m;
+      if (b) atomicOr(&a.ctrl[3], 1);
     }
   }
   __shared__ int am_last;
@@ -325,76 +562,48 @@ __device__ void step_reduce(const StepArgs& a, const double (&v)[NRED], int r, d
   __syncthreads();
   if (threadIdx.x == 0) am_last = (atomicAdd(a.done, 1u) == gridDim.x - 1);
   __syncthreads();
-  if (!am_last) return;
+  if (!am_last || threadIdx.x >= 32) return;
   __threadfence();
+  const int lane = threadIdx.x;
   const int nrep = a.p.rep.nrep;
-  if (nrep * NRED >= NTHREADS) {
-    // many replicas: one thread per (replica, quantity), blocks summed in order
-    for (int task = threadIdx.x; task < nrep * NRED; task += NTHREADS) {
-      const int rr = task / NRED, k = task % NRED;
-      const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
-      double s = 0.0;
-      for (int b = b0; b <= b1; ++b) {
-        const int slot = rr - a.p.rep.mol_rep[b * mpb];
-        s += __ldcg(&a.part[((size_t)b * MAXREP_PER_BLOCK + slot) * NRED + k]);
-      }
-      a.red[task] = s;
+  for (int rr = 0; rr < nrep; ++rr) {
+    const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
+    double s[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) s[k] = 0.0;
+    for (int b = b0 + lane; b <= b1; b += 32) {
+      const int slot = rr - a.p.rep.mol_rep[b * mpb];
+      const double* src = a.part + ((size_t)b * MAXREP_PER_BLOCK + slot) * NRED;
+#pragma unroll
+      for (int k = 0; k < NRED; ++k) s[k] += __ldcg(src + k);
     }
-  } else {
-    // few replicas: thread t sums blocks b0+t, b0+t+NTHREADS, ... of every quantity,
-    // then a fixed-order tree per quantity
-    __shared__ double tree[NTHREADS];
-    for (int rr = 0; rr < nrep; ++rr) {
-      const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
-      double s[NRED];
 #pragma unroll
-      for (int k = 0; k < NRED; ++k) s[k] = 0.0;
-      for (int b = b0 + (int)threadIdx.x; b <= b1; b += NTHREADS) {
-        const int slot = rr - a.p.rep.mol_rep[b * mpb];
-        const double* src = a.part + ((size_t)b * MAXREP_PER_BLOCK + slot) * NRED;
+    for (int k = 0; k < NRED; ++k) {
+      double x = s[k];
 #pragma unroll
-        for (int k = 0; k < NRED; ++k) s[k] += __ldcg(src + k);
-      }
-      for (int k = 0; k < NRED; ++k) {
-        tree[threadIdx.x] = s[k];
-        __syncthreads();
-        for (int o = NTHREADS / 2; o >= 1; o >>= 1) {
-          if ((int)threadIdx.x < o) tree[threadIdx.x] += tree[threadIdx.x + o];
-          __syncthreads();
-        }
-        if (threadIdx.x == 0) a.red[rr * NRED + k] = tree[0];
-        __syncthreads();
-      }
+      for (int m = 16; m >= 1; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
+      if (lane == 0) a.red[rr * NRED + k] = x;
     }
   }
-  __shared__ double gmaxv[NTHREADS];
-  {
-    double m = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += NTHREADS) m = fmax(m, __ldcg(&a.partmax[b]));
-    gmaxv[threadIdx.x] = m;
-  }
-  __syncthreads();
-  __shared__ double gmax;
-  if (threadIdx.x == 0) {
-    double m = 0.0;
-    for (int t = 0; t < NTHREADS; ++t) m = fmax(m, gmaxv[t]);
-    gmax = m;
-  }
-  __syncthreads();
+  double gm = 0.0;
+  for (int b = lane; b < (int)gridDim.x; b += 32) gm = fmax(gm, __ldcg(&a.partmax[b]));
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) gm = fmax(gm, __shfl_xor_sync(0xffffffffu, gm, m));
+  __syncwarp();
   const int logcap = a.ctrl[5];
-  for (int rr = threadIdx.x; rr < nrep; rr += NTHREADS) {
+  for (int rr = lane; rr < nrep; rr += 32) {
     const double* s = a.red + (size_t)rr * NRED;
     ThermoDev& th = a.th[rr];
     const int nm = a.p.rep.off[rr + 1] - a.p.rep.off[rr];
     const double dof = 6.0 * nm;
     const double dt = a.dt;
-    const double ekt = s[10] * a.mass * 0.5 * (1.0 / (dt * dt));
-    const double ekr = (s[11] * a.I[0] + s[12] * a.I[1] + s[13] * a.I[2]) * 0.5;
+    const double ekt = s[2] * a.mass * 0.5 * (1.0 / (dt * dt));
+    const double ekr = s[3] * 0.5;
     const double temperature = I2J * 2.0 * (ekt + ekr) / (RGAS * dof);
-    const double pkin = (s[14] + s[18] + s[22]) * a.mass * (1.0 / (dt * dt));
-    const double vp = pkin + s[1] + s[5] + s[9];
-    const double V = a.p.rep.L[3 * rr] * a.p.rep.L[3 * rr + 1] * a.p.rep.L[3 * rr + 2];
-    const double pressure = (vp / 3.0) * I2J * (1.0 / A2P) / (V * NA * ANG2M * ANG2M * ANG2M);
+    const double pkin = s[2] * a.mass * (1.0 / (dt * dt));
+    const double vp = pkin + s[1];
+    const double vol = a.p.rep.L[3 * rr] * a.p.rep.L[3 * rr + 1] * a.p.rep.L[3 * rr + 2];
+    const double pressure = (vp / 3.0) * I2J * (1.0 / A2P) / (vol * NA * ANG2M * ANG2M * ANG2M);
     if (th.kind == G6_NOSE) {   // Nose_Correct
       const double zetaf = (temperature - th.temp) / th.q - th.dump * th.z[0];
       const double dz2 = zetaf - th.z[1];
@@ -414,7 +623,7 @@ __device__ void step_reduce(const StepArgs& a, const double (&v)[NRED], int r, d
       double* lg = a.log + ((size_t)step * nrep + rr) * G6_LOG_WIDTH;
       lg[0] = s[0]; lg[1] = ekt; lg[2] = ekr; lg[3] = temperature; lg[4] = pressure;
       lg[5] = (s[0] + ekt + ekr) * I2J + nose_ep + nose_ek;
-      lg[6] = s[23]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
+      lg[6] = s[4]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
     }
     if (predict_next && th.kind == G6_NOSE) {   // Nose_Predict for the next step
       th.z[0] = th.z[0] + th.z[1] + th.z[2] + th.z[3] + th.z[4];
@@ -423,8 +632,9 @@ __device__ void step_reduce(const StepArgs& a, const double (&v)[NRED], int r, d
       th.z[3] = th.z[3] + 4.0 * th.z[4];
     }
   }
-  if (threadIdx.x == 0) {
-    a.ctrl[0] = (predict_next && gmax > a.half_skin2) ? 1 : 0;
+  __syncwarp();
+  if (lane == 0) {
+    a.ctrl[0] = (predict_next && gm > a.half_skin2) ? 1 : 0;
     a.ctrl[1] = step + 1;
     *a.done = 0u;
   }

@@ -10,8 +10,9 @@
 //   lf = log q_s(x'|x) - log q0(x'|x),
 //   lr = log q_s(x|x') - b - log q0(x'|x),
 //   log q_s(.|x) = -3 log s_t(x) - |d|^2 / (2 s_t(x)^2) - 3 log s_r(x) - |r|^2 / (2 s_r(x)^2),
-//   D = |d|^2 / s0_t^2 + |r|^2 / s0_r^2,
-// i.e. the proposal density ratio times the MH acceptance min(1, e^-b q(x|x')/q(x'|x)).
+//   D = w_move (|d|^2 / s0_t^2 + |r|^2 / s0_r^2) + w_energy b^2,
+// i.e. the proposal density ratio times the MH acceptance min(1, e^-b q(x|x')/q(x'|x))
+// times the jump (in configuration, scaled by the fixed widths, and in energy).
 // The loss is -J.  Kernels: forward of both sides of every record (one warp
 // per row, activations stored), the loss and dL/dz of the active branch,
 // backward through the two tanh layers, weight gradients as reductions over
@@ -67,6 +68,40 @@ __global__ void k_mlp_forward(TrainArgs a) {
   }
 }
 
+// Widths of the network for n raw feature rows (one thread per row; a
+// diagnostic evaluation, e.g. of the width distribution over a sample).
+__global__ void k_mlp_eval(const float* feat, long long n, const float* w, const float* mean, const float* istd,
+                           double s0t, double s0r, double* st, double* sr) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float x[MLP_IN], h1[MLP_H];
+#pragma unroll
+  for (int k = 0; k < MLP_IN; ++k) x[k] = (feat[r * MLP_IN + k] - mean[k]) * istd[k];
+  for (int o = 0; o < MLP_H; ++o) {
+    float t = w[MLP_B1 + o];
+#pragma unroll
+    for (int k = 0; k < MLP_IN; ++k) t = fmaf(w[MLP_W1 + o * MLP_IN + k], x[k], t);
+    h1[o] = tanhf(t);
+  }
+  float z0 = w[MLP_B3], z1 = w[MLP_B3 + 1];
+  for (int o = 0; o < MLP_H; ++o) {
+    float t = w[MLP_B2 + o];
+    for (int k = 0; k < MLP_H; ++k) t = fmaf(w[MLP_W2 + o * MLP_H + k], h1[k], t);
+    const float h2 = tanhf(t);
+    z0 = fmaf(w[MLP_W3 + o], h2, z0);
+    z1 = fmaf(w[MLP_W3 + MLP_H + o], h2, z1);
+  }
+  st[r] = s0t * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z0));
+  sr[r] = s0r * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z1));
+}
+
+cudaError_t launch_mlp_eval(const float* feat, long long n, const float* w, const float* mean, const float* istd,
+                            double s0t, double s0r, double* st, double* sr, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_mlp_eval<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(feat, n, w, mean, istd, s0t, s0r, st, sr);
+  return cudaGetLastError();
+}
+
 // Loss and dL/dz, one thread per record (both rows).
 __global__ void k_mlp_loss(TrainArgs a, float inv_batch) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,8 +116,8 @@ __global__ void k_mlp_loss(TrainArgs a, float inv_batch) {
         const double z = a.Z[(size_t)(2 * b + side) * MLP_OUT + q];
         const double sgm = 1.0 / (1.0 + exp(-z));
         const double s0 = q == 0 ? a.s0t : a.s0r;
-        s[side][q] = s0 * (0.5 + 2.0 * sgm);
-        sg[side][q] = s0 * 2.0 * sgm * (1.0 - sgm);   // ds/dz
+        s[side][q] = s0 * (MLP_SMIN + MLP_SSPAN * sgm);
+        sg[side][q] = s0 * MLP_SSPAN * sgm * (1.0 - sgm);   // ds/dz
       }
     auto logq = [&](int side) {
       return -3.0 * log(s[side][0]) - d2 / (2.0 * s[side][0] * s[side][0]) - 3.0 * log(s[side][1]) -
@@ -93,7 +128,7 @@ __global__ void k_mlp_loss(TrainArgs a, float inv_batch) {
     const double lr = logq(1) - bde - lq0;
     const int side = lf <= lr ? 0 : 1;
     const double l = side == 0 ? lf : lr;
-    const double D = d2 / (a.s0t * a.s0t) + r2 / (a.s0r * a.s0r);
+    const double D = a.w_move * (d2 / (a.s0t * a.s0t) + r2 / (a.s0r * a.s0r)) + a.w_energy * bde * bde;
     const double J = exp(fmin(l, 30.0)) * D;
     lossv = -J;
     // d(-J)/dz_q on the active side = -J * dl/ds_q * ds/dz_q

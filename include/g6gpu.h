@@ -171,11 +171,14 @@ int g6_step_times(g6_ctx* ctx, double* step_ms, double* kernel_ms);
 /* Duration (ms, CUDA events on the context's stream) of one launch of the
    force kernel on the current configuration and neighbour list. */
 int g6_time_force(g6_ctx* ctx, double* ms);
-/* Lanes cooperating on one molecule in the force kernel (4, 8, 16 or 32).
-   g6_tune times each choice on the uploaded configuration and keeps the
-   fastest; g6_set_lpi fixes it.  Without either, the first force evaluation
-   picks a value from the system size.  (Per-lane partial sums change with
-   it, so results differ at rounding level between choices.) */
+/* Lanes cooperating on one molecule in the force kernel and in the fused MD
+   step kernel (4, 8, 16 or 32).  g6_tune times each choice on the uploaded
+   configuration -- the force kernel alone, and the MD step in a short NVE run
+   whose state is restored afterwards -- and keeps the fastest of each (lpi
+   gets the MD choice); g6_set_lpi fixes both.  Without either, the first
+   force evaluation or run picks a value from the system size.  (Per-lane
+   partial sums change with it, so results differ at rounding level between
+   choices.) */
 int g6_tune(g6_ctx* ctx, int* lpi);
 int g6_set_lpi(g6_ctx* ctx, int lpi);
 
@@ -198,14 +201,17 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
    Gaussian translation of per-axis width sigma_t [A], rotation vector of
    per-axis width sigma_r [rad] applied with qinfrotator + qadd,
    QuatModule.F90:108-223) under an exact Metropolis-Hastings test at
-   beta[r] [1/K] (acceptance exp(-dE*I2J*J2K*beta), mc2.F90:712-722).  dE sums
+   beta[r] [1/K] (acceptance exp(-dE*I2J*J2K*beta), mc2.F90:712-722, tested
+   as log(u) < -dE*I2J*J2K*beta).  dE sums
    the PairPotential energies of the target at both poses against every other
    molecule of its chain, so no stored pair table is needed and the chain is
    exact; the reference's per-trial width adaptation (mc2.F90:794-810) is not
    applied.  Modes: G6_MC_PLAIN uses sigma_t/sigma_r; G6_MC_LEARNED takes the
    widths from the network (g6_mlp_*) evaluated at the old pose, with the
    reverse density at the new pose in the Hastings ratio; G6_MC_COLLECT runs
-   the plain proposal and stores one training record per trial.  Draws come
+   the plain proposal and stores one training record per trial.  Precision
+   follows the context: mixed contexts evaluate trial poses and pair energies
+   in FP32 and keep the state in FP64.  Draws come
    from Philox4x32-10 (key = seed, counter = chain, trial, draw).
    samples (optional, nrep x ntrial/sample_every) gets the running energy,
    counts (optional, nrep x 2) accepted/attempted, energy (optional, nrep) the
@@ -219,7 +225,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
               double* trace);
 
 /* Proposal-width network: 24 local-environment features -> 64 -> 64 (tanh)
-   -> 2 widths, sigma = sigma0 * (0.5 + 2 sigmoid(z)).  Parameters are one
+   -> 2 widths, sigma = sigma0 * (0.1 + 2.9 sigmoid(z)).  Parameters are one
    float array of G6_MLP_NPARAM values: W1[64][24], b1[64], W2[64][64],
    b2[64], W3[2][64], b3[2]; features are normalised with feat_mean and
    feat_inv_std.  A training record is G6_MLP_RECORD floats: features at the
@@ -235,6 +241,15 @@ int g6_mlp_get(g6_ctx* ctx, float* params, float* feat_mean, float* feat_inv_std
 int g6_mlp_records(g6_ctx* ctx, float* host, int64_t cap, int64_t* count);
 /* Mean loss and its gradient over caller records (host) with the current parameters. */
 int g6_mlp_grad(g6_ctx* ctx, const float* records, int64_t nrec, float* grad, double* loss);
+/* Training objective: the mean over records of
+   min(q(x'|x), exp(-beta dE) q(x|x')) / q0(x'|x) * (w_move * D + w_energy * (beta dE)^2),
+   the expected jump of an accepted move under the network's proposal q,
+   estimated from moves drawn with the fixed widths (q0); D = |dx|^2/sigma0_t^2
+   + |rot|^2/sigma0_r^2.  Defaults: w_move = 1, w_energy = 0. */
+int g6_mlp_objective(g6_ctx* ctx, double w_move, double w_energy);
+/* Widths sigma_t[n], sigma_r[n] the current network gives for n raw feature
+   rows (n x G6_MLP_NFEAT floats, e.g. the first half of training records). */
+int g6_mlp_widths(g6_ctx* ctx, const float* features, int64_t n, double* sigma_t, double* sigma_r);
 /* Train on the collected records with Adam (hand-written forward/backward
    kernels); loss (optional, epochs) gets the mean loss of each epoch. */
 int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, double sigma0_t, double sigma0_r,

@@ -18,6 +18,7 @@ W3 = B2 + NH
 B3 = W3 + NOUT * NH
 NPARAM = B3 + NOUT
 RECORD = 2 * NIN + 3
+SMIN, SSPAN = 0.1, 2.9          # sigma = sigma0 * (SMIN + SSPAN * sigmoid(z))
 
 
 def unpack(p):
@@ -61,11 +62,15 @@ def forward(p, x):
 
 def widths(z, s0t, s0r):
     s = 1.0 / (1.0 + np.exp(-z))
-    return s0t * (0.5 + 2.0 * s[..., 0]), s0r * (0.5 + 2.0 * s[..., 1])
+    return s0t * (SMIN + SSPAN * s[..., 0]), s0r * (SMIN + SSPAN * s[..., 1])
 
 
-def loss_and_grad(p, rec, mean, istd, s0t, s0r):
-    """Mean over records of -J (g6_train.cu) and its gradient w.r.t. the parameters."""
+def loss_and_grad(p, rec, mean, istd, s0t, s0r, w_move=1.0, w_energy=0.0):
+    """Mean over records of -J (g6_train.cu) and its gradient w.r.t. the parameters.
+
+    J = min(q(x'|x), exp(-beta dE) q(x|x')) / q0(x'|x) * (w_move * D + w_energy * (beta dE)^2):
+    the expected jump of an accepted move under the network's proposal, estimated
+    from moves drawn with the fixed widths s0t, s0r."""
     rec = np.asarray(rec, dtype=np.float64)
     B = rec.shape[0]
     xo = (rec[:, :NIN] - mean) * istd
@@ -75,8 +80,8 @@ def loss_and_grad(p, rec, mean, istd, s0t, s0r):
     zn, an = forward(p, xn)
     sg_o = 1.0 / (1.0 + np.exp(-zo))
     sg_n = 1.0 / (1.0 + np.exp(-zn))
-    so = np.stack([s0t * (0.5 + 2 * sg_o[:, 0]), s0r * (0.5 + 2 * sg_o[:, 1])], 1)
-    sn = np.stack([s0t * (0.5 + 2 * sg_n[:, 0]), s0r * (0.5 + 2 * sg_n[:, 1])], 1)
+    so = np.stack([s0t * (SMIN + SSPAN * sg_o[:, 0]), s0r * (SMIN + SSPAN * sg_o[:, 1])], 1)
+    sn = np.stack([s0t * (SMIN + SSPAN * sg_n[:, 0]), s0r * (SMIN + SSPAN * sg_n[:, 1])], 1)
 
     def logq(s):
         return -3 * np.log(s[:, 0]) - d2 / (2 * s[:, 0] ** 2) - 3 * np.log(s[:, 1]) - r2 / (2 * s[:, 1] ** 2)
@@ -86,13 +91,13 @@ def loss_and_grad(p, rec, mean, istd, s0t, s0r):
     lr = logq(sn) - bde - lq0
     use_o = lf <= lr
     l = np.where(use_o, lf, lr)
-    D = d2 / s0t ** 2 + r2 / s0r ** 2
+    D = w_move * (d2 / s0t ** 2 + r2 / s0r ** 2) + w_energy * bde ** 2
     J = np.exp(np.minimum(l, 30.0)) * D
     loss = -J.mean()
     s_act = np.where(use_o[:, None], so, sn)
     sg_act = np.where(use_o[:, None], sg_o, sg_n)
     dls = np.stack([-3 / s_act[:, 0] + d2 / s_act[:, 0] ** 3, -3 / s_act[:, 1] + r2 / s_act[:, 1] ** 3], 1)
-    dsdz = np.stack([s0t, s0r])[None, :] * 2 * sg_act * (1 - sg_act)
+    dsdz = np.stack([s0t, s0r])[None, :] * SSPAN * sg_act * (1 - sg_act)
     gz = (-J[:, None] * dls * dsdz) / B
     gzo = np.where(use_o[:, None], gz, 0.0)
     gzn = np.where(use_o[:, None], 0.0, gz)

@@ -103,8 +103,63 @@ def test_collect_records_hold_reference_features(orc):
     assert rec[0, 2 * mlp.NIN + 1] == pytest.approx(np.sum(np.square(rot)), rel=1e-5)
 
 
-def test_mlp_gradient_matches_reference():
+def test_feature_cache_follows_the_chain(orc):
+    """Records carry the target's features from the device cache, which accepted
+    moves update term by term; they must equal a fresh evaluation at the state
+    the FP64 oracle chain reaches after the same number of trials."""
+    s, recs, rc = _chains("ST2", 1, 216, 61)
+    b = recs[0]
+    beta, K = 1.0 / 260.0, 400
+    counts, energy, trace, _ = _mc(s, K, 17, 0, beta, 0.15, 0.15, mode=_capi.MC_COLLECT)
+    assert counts[0, 0] > 50                      # enough accepted moves to exercise the updates
+    rec = np.zeros((K, mlp.RECORD), np.float32)
+    import ctypes
+    cnt = ctypes.c_int64()
+    s._check(s.L.g6_mlp_records(s.ctx, fptr(rec), K, ctypes.byref(cnt)))
+    assert cnt.value == K
+    E0 = orc.compute("ST2", "custom", b["com"], b["quat"], b["L"], [rc] * 3, rc - 2.0, rc)[2]
+    for k in (120, 260, K - 1):
+        com, quat, _, tr = orc.mc_run("ST2", "custom", b["com"], b["quat"], b["L"], rc - 2.0, rc, beta, 0.15, 0.15,
+                                      k, 17, 0, 0, E0)
+        assert np.array_equal(tr[:, 2], trace[0, :k, 2])
+        t = int(trace[0, k, 3])
+        sx, sy, sz, intra, tmat = orc.place_sites("ST2", com, quat)
+        fo = mlp.features(com, b["L"], t, com[t], intra[t, 1:5])
+        assert np.allclose(rec[k, :mlp.NIN], fo, rtol=2e-4, atol=2e-4), k
+
+
+def test_network_widths_match_reference():
+    s, recs, rc = _chains("ST2", 1, 216, 71)
+    rng = np.random.default_rng(5)
+    p = rng.normal(0, 0.3, mlp.NPARAM).astype(np.float32)
+    feat = rng.uniform(0, 3, (300, mlp.NIN)).astype(np.float32)
+    mean = feat.mean(0).astype(np.float32); istd = (1 / feat.std(0)).astype(np.float32)
+    s._check(s.L.g6_mlp_set(s.ctx, fptr(p), fptr(mean), fptr(istd), 0.15, 0.2))
+    st = np.zeros(300); sr = np.zeros(300)
+    s._check(s.L.g6_mlp_widths(s.ctx, fptr(feat), 300, dptr(st), dptr(sr)))
+    z, _ = mlp.forward(p.astype(np.float64), (feat.astype(np.float64) - mean) * istd)
+    wt, wr = mlp.widths(z, 0.15, 0.2)
+    assert np.allclose(st, wt, rtol=1e-5) and np.allclose(sr, wr, rtol=1e-5)
+
+
+def test_learned_chain_is_reproducible():
+    s, recs, rc = _chains("ST2", 4, 216, 81, prec="mixed")
+    _mc(s, 1500, 11, 0, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_COLLECT)
+    s._check(s.L.g6_mlp_train(s.ctx, 3, 256, 3e-3, 7, 0.15, 0.15, None))
+    rec0 = s.download_state()
+    out = []
+    for _ in range(2):
+        s.upload_state(rec0)
+        counts, energy, trace, _ = _mc(s, 800, 12, 10 ** 6, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_LEARNED)
+        out.append((counts.copy(), energy.copy(), trace.copy()))
+    assert np.array_equal(out[0][2], out[1][2])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("w_move,w_energy", [(1.0, 0.0), (1.0, 0.5)])
+def test_mlp_gradient_matches_reference(w_move, w_energy):
     s, recs, rc = _chains("ST2", 1, 216, 70)
+    s._check(s.L.g6_mlp_objective(s.ctx, w_move, w_energy))
     rng = np.random.default_rng(1)
     n = 512
     rec = np.zeros((n, mlp.RECORD))
@@ -120,7 +175,7 @@ def test_mlp_gradient_matches_reference():
     loss = np.zeros(1)
     s._check(s.L.g6_mlp_grad(s.ctx, fptr(rec32), n, fptr(g), dptr(loss)))
     lref, gref = mlp.loss_and_grad(p.astype(np.float64), rec32.astype(np.float64), mean.astype(np.float64),
-                                   istd.astype(np.float64), 0.15, 0.15)
+                                   istd.astype(np.float64), 0.15, 0.15, w_move, w_energy)
     assert loss[0] == pytest.approx(lref, rel=1e-4)
     assert np.abs(g - gref).max() <= 2e-3 * np.abs(gref).max()
 

@@ -1,6 +1,7 @@
 """CPU checks of the FP64 learned-proposal reference (oracle/mlp.py): the
 analytic gradient of the training loss against central finite differences."""
 import numpy as np
+import pytest
 
 from oracle import mlp
 
@@ -14,24 +15,26 @@ def _records(rng, n=64):
     return rec
 
 
-def test_gradient_matches_finite_differences():
+@pytest.mark.parametrize("w_move,w_energy", [(1.0, 0.0), (1.0, 0.5), (0.0, 1.0)])
+def test_gradient_matches_finite_differences(w_move, w_energy):
     rng = np.random.default_rng(0)
     p = rng.normal(0, 0.3, mlp.NPARAM)
     rec = _records(rng)
     mean = rec[:, :mlp.NIN].mean(0); istd = 1 / rec[:, :mlp.NIN].std(0)
-    loss, g = mlp.loss_and_grad(p, rec, mean, istd, 0.15, 0.15)
+    loss, g = mlp.loss_and_grad(p, rec, mean, istd, 0.15, 0.15, w_move, w_energy)
     h = 1e-6
     for k in rng.choice(mlp.NPARAM, 40, replace=False).tolist() + [mlp.B3, mlp.B3 + 1]:
         pp = p.copy(); pp[k] += h
         pm = p.copy(); pm[k] -= h
-        fd = (mlp.loss_and_grad(pp, rec, mean, istd, 0.15, 0.15)[0] -
-              mlp.loss_and_grad(pm, rec, mean, istd, 0.15, 0.15)[0]) / (2 * h)
+        fd = (mlp.loss_and_grad(pp, rec, mean, istd, 0.15, 0.15, w_move, w_energy)[0] -
+              mlp.loss_and_grad(pm, rec, mean, istd, 0.15, 0.15, w_move, w_energy)[0]) / (2 * h)
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g).max())
 
 
 def test_constant_network_gives_sigma0():
     p = np.zeros(mlp.NPARAM)
-    p[mlp.B3:] = np.log(0.25 / 0.75)
+    p0 = (1.0 - mlp.SMIN) / mlp.SSPAN      # the initial output bias of g6_mlp_train
+    p[mlp.B3:] = np.log(p0 / (1.0 - p0))
     z, _ = mlp.forward(p, np.zeros((3, mlp.NIN)))
     st, sr = mlp.widths(z, 0.15, 0.2)
     assert np.allclose(st, 0.15) and np.allclose(sr, 0.2)
