@@ -206,7 +206,8 @@ struct g6_ctx {
   float* d_stf = nullptr;   // mixed precision: small Gear terms during a run
   // reductions and control
   int nblk = 0;
-  double* d_part = nullptr; double* d_partmax = nullptr; double* d_red = nullptr;
+  double* d_part = nullptr; unsigned int* d_gmax = nullptr; double* d_red = nullptr; int* d_repcnt = nullptr;
+  double* d_rfac = nullptr;   // per replica temperature and pressure factors
   unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
   ThermoDev* d_th = nullptr; double* d_scale = nullptr; double* d_beta = nullptr; int* d_acc = nullptr;
   double* d_epot_rep = nullptr;
@@ -457,10 +458,11 @@ static int default_lpi(const g6_ctx* c) {
 
 // Enqueue the neighbour-list rebuild (conditional on ctrl[0] when ctrl != NULL):
 // one cooperative launch that exits at once when no rebuild is due.
-static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl) {
+static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl, const StepArgs* step = nullptr) {
   if (ctx->coop_grid == 0) ctx->coop_grid = rebuild_grid_limit();
   CellArgs ca = cell_args(ctx, ctx->glist, ctrl);
-  CK(launch_rebuild(ca, list_args(ctx, ctrl), ctx->glist.d_start, ctx->glist.d_cellmol, ctx->coop_grid, ctx->stream));
+  CK(launch_rebuild(ca, list_args(ctx, ctrl), ctx->glist.d_start, ctx->glist.d_cellmol, ctx->coop_grid, step,
+                    ctx->stream));
   return G6_OK;
 }
 
@@ -597,7 +599,9 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
   ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // blocks of the fused step kernel at 32 lanes/molecule
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
-  CK(dalloc(ctx, &ctx->d_partmax, ctx->nblk)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
+  CK(dalloc(ctx, &ctx->d_gmax, 2)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
+  CK(dalloc(ctx, &ctx->d_repcnt, nrep));
+  CK(dalloc(ctx, &ctx->d_rfac, 2 * (size_t)nrep));
   CK(dalloc(ctx, &ctx->d_done, 1)); CK(dalloc(ctx, &ctx->d_ctrl, 8));
   CK(dalloc(ctx, &ctx->d_th, nrep)); CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
   CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
@@ -908,7 +912,12 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   a.stf = ctx->d_stf;
   const double hs = 0.5 * effective_skin(ctx);
   a.half_skin2 = hs * hs;
-  a.th = ctx->d_th; a.part = ctx->d_part; a.partmax = ctx->d_partmax; a.red = ctx->d_red; a.done = ctx->d_done;
+  a.th = ctx->d_th; a.part = ctx->d_part; a.gmax = ctx->d_gmax; a.red = ctx->d_red; a.done = ctx->d_done;
+  a.repcnt = ctx->d_repcnt;
+  a.inv_dt2 = 1.0 / (dt * dt);
+  a.fdt = (float)dt; a.fcf = (float)(dt * dt * 0.5 / ctx->mh.mass);
+  for (int k = 0; k < 3; ++k) a.fI[k] = (float)ctx->mh.I[k];
+  a.rfac = ctx->d_rfac;
   a.ctrl = ctx->d_ctrl; a.log = log; a.seed = ctx->seed;
   return a;
 }
@@ -918,7 +927,7 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
 static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullptr) {
   // external records become event nodes of a captured graph (queryable after launch)
   if (ev) CK(cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal));
-  int rc = enqueue_rebuild(ctx, ctx->d_ctrl);
+  int rc = enqueue_rebuild(ctx, ctx->d_ctrl, &sa);
   if (rc) return rc;
   ForceArgs fa = force_args(ctx);
   fa.ctrl = ctx->d_ctrl;
@@ -969,6 +978,7 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
       t.kind = thermo[r].kind; t.temp = thermo[r].temp; t.q = thermo[r].q; t.dump = thermo[r].dump;
       for (int k = 0; k < 5; ++k) t.z[k] = thermo[r].zeta[k];
       t.zsum = thermo[r].zetasum; t.rate = thermo[r].collision_rate;
+      t.inv_q = t.q > 0.0 ? 1.0 / t.q : 0.0;
       if (t.kind == G6_NOSE && !(t.q > 0.0)) return fail(ctx, G6_ERR_ARG, "Nose q must be > 0");
       if (t.kind < G6_NVE || t.kind > G6_ANDERSEN) return fail(ctx, G6_ERR_ARG, "unknown thermostat");
     }
@@ -984,6 +994,19 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
   int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
   CK(cudaMemcpyAsync(ctx->d_ctrl, ctrl, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_gmax, 0, 2 * sizeof(unsigned), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_repcnt, 0, ctx->nrep * sizeof(int), ctx->stream));
+  {   // temperature and pressure factors of each replica (Mixture.F90:2251-2264)
+    std::vector<double> rf(2 * (size_t)ctx->nrep);
+    for (int r = 0; r < ctx->nrep; ++r) {
+      const double dof = 6.0 * (ctx->off[r + 1] - ctx->off[r]);
+      const double vol = ctx->L[3 * r] * ctx->L[3 * r + 1] * ctx->L[3 * r + 2];
+      rf[2 * r] = I2J * 2.0 / (RGAS * dof);
+      rf[2 * r + 1] = I2J / (3.0 * A2P * vol * NA * ANG2M * ANG2M * ANG2M);
+    }
+    CK(cudaMemcpyAsync(ctx->d_rfac, rf.data(), rf.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));   // rf is a local vector
+  }
   CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
   (void)dt;
   if (thermo && thermo[0].seed != ctx->seed) {

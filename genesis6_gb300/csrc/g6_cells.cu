@@ -21,7 +21,10 @@
 
 #include <cooperative_groups.h>
 
+#include <cstring>
+
 #include "g6_internal.cuh"
+#include "g6_rigid.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -245,10 +248,31 @@ struct RebuildArgs {
   ListArgs l;
   int* start;
   int* cellmol;
+  StepArgs s;
+  int with_step;   // MD step head: the rebuild decision comes from the previous step
 };
 
 __global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
-  if (skip_ctrl(a.c.ctrl)) return;
+  bool rebuild;
+  if (a.with_step) {
+    const int* ctrl = a.s.ctrl;
+    if (ctrl[4]) {
+      // the rebuild decision from the previous step's displacement test (the
+      // same in every block)
+      const int step = ctrl[1];
+      const double gmax = step_gmax(a.s);
+      rebuild = step < ctrl[2] && gmax > a.s.half_skin2;
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.s.ctrl[0] = rebuild ? 1 : 0;
+        a.s.gmax[step & 1] = 0u;   // the word of step-2, read by the previous head only
+      }
+    } else {
+      rebuild = ctrl[0] != 0;   // first step of a run: the flag set by the host
+    }
+  } else {
+    rebuild = !skip_ctrl(a.c.ctrl);
+  }
+  if (!rebuild) return;
   cg::grid_group grid = cg::this_grid();
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   if (!grid.is_valid()) {   // not launched cooperatively: report, never wait
@@ -314,9 +338,11 @@ int rebuild_grid_limit() {
 }
 
 cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int* cellmol, int grid_limit,
-                           cudaStream_t s) {
+                           const StepArgs* step, cudaStream_t s) {
   RebuildArgs a;
+  memset(&a, 0, sizeof a);
   a.c = c; a.l = l; a.start = start; a.cellmol = cellmol;
+  if (step) { a.s = *step; a.with_step = 1; }
   const int want = (max(c.n, c.g.ncell_total) * 32 + 255) / 256;
   const int blocks = max(1, min(grid_limit, want));
   void* args[] = {&a};

@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
         vv[4] = FF{0.5f * (float)smn[m], 0.0f};
       }
     }
-    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step, predict_next);
+    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step);
   } else {
     // fused FP64 step: FP64 lane combine, FP64 integrator in warp 0
     constexpr int MPB = StepShape<MIXED, LPI>::MPB;
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
                     pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
       }
     }
-    step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step, predict_next);
+    step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step);
   }
 }
 

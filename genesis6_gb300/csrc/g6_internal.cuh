@@ -235,7 +235,7 @@ struct PairSetArgs {
 
 struct ThermoDev {
   int kind;
-  double temp, q, dump;
+  double temp, q, dump, inv_q;
   double z[5];
   double zsum;
   double rate;
@@ -260,16 +260,21 @@ struct StepArgs {
   float4* pk32_1;
   uint32_t* fix1;
   double mass, I[3], dt;
+  double inv_dt2;      // 1 / dt^2
+  float fdt, fcf, fI[3];   // dt, dt^2 / (2 mass), inertia as float (mixed corrector)
+  const double* rfac;  // per replica: I2J*2/(RGAS*dof) (temperature), I2J/(3*A2P*V*NA*ANG2M^3) (pressure)
   const double* com_build;
   const uint32_t* fix_build;
   float* stf;          // mixed precision: float SoA of the small Gear terms (STF_*)
   double half_skin2;
   ThermoDev* th;
   double* part;        // blocks * MAXREP_PER_BLOCK * NRED
-  double* partmax;     // blocks
+  unsigned int* gmax;  // 2 words: largest squared displacement of the steps of each parity (float bits)
+  int* repcnt;         // per replica: blocks of the step that have written their partials
   double* red;         // nrep * NRED (finalize scratch)
   unsigned int* done;
-  int* ctrl;           // [0] rebuild, [1] step, [2] nsteps, [3] error bits, [4] -, [5] log capacity, [6] step base
+  int* ctrl;           // [0] list rebuilt at the start of this step, [1] step, [2] nsteps, [3] error bits,
+                       // [4] a step of this run has finished, [5] log capacity, [6] step base
   double* log;         // [step][rep][G6_LOG_WIDTH]
   unsigned long long seed;
 };
@@ -305,7 +310,7 @@ cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream
 cudaError_t launch_list(const ListArgs& a, cudaStream_t s);
 int rebuild_grid_limit();
 cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int* cellmol, int grid_limit,
-                           cudaStream_t s);
+                           const StepArgs* step, cudaStream_t s);
 cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);

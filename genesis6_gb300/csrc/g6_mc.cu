@@ -348,31 +348,115 @@ __device__ __forceinline__ void queue_append(int* seg, int& cnt, bool in, int j,
   cnt += __popc(m);
 }
 
+// One trial's proposal: widths, draws, the trial pose of the target and its
+// current pose.  Built by one whole warp; two of them alternate so that the
+// next trial's pose is built while the current trial's energies are summed.
+template <class R, int NQ>
+struct TrialPose {
+  R on[NQ + 1][3], oo[NQ + 1][3];   // new / old site offsets
+  double cn[3], co[3];              // new / old FP64 COM
+  double rot[3], dx[3];             // FP64 rotation vector and translation
+  double st, sr;                    // widths of the proposal (at the old pose)
+  R qn[4];                          // trial quaternion
+  uint32_t fn[3], fo[3];            // new / old fixed-point COM
+  float un[4][3];                   // charged-site directions at the new pose
+  float d2, r2;                     // |dx|^2, |rot|^2
+  int trial;                        // trial number the pose belongs to (-1: none)
+};
+
+// Warp-cooperative build of trial `trial` (target tg, unit normals g[6]).
+// The arithmetic of every quantity is the serial formula of mc2 (each lane
+// evaluates the same expressions).
+template <class R, int NQ, bool MIXED>
+__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const double* g, double st_w,
+                            double sr_w, const double iL[3]) {
+  using Pr = PoseRead<NQ, MIXED>;
+  const int lane = threadIdx.x & 31;
+  const int n = a.n;
+  // loads spread over lanes
+  double qv = 0.0, cv = 0.0;
+  uint32_t fv = 0u;
+  R ov = R(0);
+  if (lane < 4) qv = a.st[(size_t)(33 + lane) * n + tg];
+  if (lane < 3) { cv = a.st[(size_t)lane * n + tg]; fv = a.fix[(size_t)lane * n + tg]; }
+  if (lane < 3 * (NQ + 1))
+    ov = MIXED ? (R)a.pk32f[(size_t)tg * 4 * Pr::NPK + 3 + lane] : (R)a.pk64[(size_t)tg * Pr::W64 + 3 + lane];
+  double qold[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qold[k] = __shfl_sync(0xffffffffu, qv, k);
+  double rot_d[3], dx_d[3];
+  R rot[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    rot_d[k] = g[k] * sr_w;
+    dx_d[k] = g[3 + k] * st_w;
+    rot[k] = (R)rot_d[k];
+  }
+  R qn[4], off[NQ + 1][3];
+  trial_rotation<R, NQ>(rot, qold, a.body, qn, off);
+  // register arrays are indexed with constants only (selects), never by lane
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (lane == k) {
+      const double cn = cv + dx_d[k];
+      P.co[k] = cv;
+      P.cn[k] = cn;
+      P.fo[k] = fv;
+      P.fn[k] = to_fixed(cn, iL[k]);
+      P.rot[k] = rot_d[k];
+      P.dx[k] = dx_d[k];
+    }
+#pragma unroll
+  for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (lane == 3 * s + k) { P.oo[s][k] = ov; P.on[s][k] = off[s][k]; }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (lane == k) P.qn[k] = qn[k];
+  if (lane == 0) {
+    P.d2 = (float)(dx_d[0] * dx_d[0] + dx_d[1] * dx_d[1] + dx_d[2] * dx_d[2]);
+    P.r2 = (float)(rot_d[0] * rot_d[0] + rot_d[1] * rot_d[1] + rot_d[2] * rot_d[2]);
+    P.st = st_w;
+    P.sr = sr_w;
+    float on[(NQ + 1) * 3];
+#pragma unroll
+    for (int s = 0; s <= NQ; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) on[3 * s + k] = (float)off[s][k];
+    float u[4][3];
+    site_dirs<NQ>(on, u);
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) P.un[s][k] = u[s][k];
+    P.trial = trial;
+  }
+  __syncwarp();
+}
+
 template <int NQ, bool TAPER, bool MIXED, int MODE>
 __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   using R = typename std::conditional<MIXED, float, double>::type;
   using P = PoseRead<NQ, MIXED>;
+  using TP = TrialPose<R, NQ>;
   constexpr bool FEAT = MODE != G6_MC_PLAIN;
   constexpr bool LEARN = MODE == G6_MC_LEARNED;
-  // warps 0 (and 1) find the feature neighbours, sum the new-pose features
-  // and run the network while the other warps sum the energies
-  constexpr int NCTRL = LEARN ? 2 : (FEAT ? 1 : 0);
+  // control warps build the next trial's pose (and, with features, find the
+  // feature neighbours and run the network) while the others sum energies
+  constexpr int NCTRL = LEARN ? 2 : 1;
   constexpr int E0 = 32 * NCTRL, NE = MC_NT - E0, NEW = NE / 32;
   constexpr int W64 = P::W64, NPK = P::NPK;
+  constexpr int QSEG = MC_QMAX / NCTRL;
   __shared__ double s_lu[MC_NB];
   __shared__ double s_g[6][MC_NB];
   __shared__ int s_tg[MC_NB];
-  __shared__ R s_on[NQ + 1][3], s_oo[NQ + 1][3];
-  __shared__ double s_cn[3], s_co[3];
-  __shared__ uint32_t s_fn[3], s_fo[3];
-  __shared__ float s_un[4][3];
+  __shared__ TP s_pose[2];
   __shared__ int s_feat[MLP_IN];
-  __shared__ R s_part[NEW > 0 ? NEW : 1];
-  constexpr int QSEG = NCTRL > 0 ? MC_QMAX / NCTRL : 1;
+  __shared__ R s_part[NEW];
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
-  __shared__ int s_nq[2][NCTRL > 0 ? NCTRL : 1];
-  __shared__ double s_sig_new[2], s_spec[2];
-  __shared__ int s_spec_tg;
+  __shared__ int s_nq[2][NCTRL];
+  __shared__ double s_sig_new[2];
   __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
 
   const int c = blockIdx.x;
@@ -389,7 +473,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   const double sig_r_fixed = sqrt(a.sigma_r[c] * a.sigma_r[c]);
   if constexpr (LEARN) mlp_load(s_mlp, a.mlp);
   if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL);
-  if (threadIdx.x == 0) s_spec_tg = -1;
+  if (threadIdx.x == 0) { s_pose[0].trial = -1; s_pose[1].trial = -1; }
   __syncthreads();
 
   const R rin2 = MIXED ? (R)a.cc.frin2 : (R)a.cc.rin2, rin = MIXED ? (R)a.cc.frin : (R)a.cc.rin;
@@ -397,10 +481,6 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   double energy = a.energy[c];
   long long nacc = 0;
   int nsample = 0;
-  // lane-0 registers carried from the pose build to the acceptance step
-  double rot_d[3] = {0, 0, 0}, dx_d[3] = {0, 0, 0}, st_old = 0.0, sr_old = 0.0;
-  R qn_trial[4] = {0, 0, 0, 0};
-  float d2f = 0.0f, r2f = 0.0f;
 
   for (int t = 0; t < a.ntrial; ++t) {
     const int tb = t % MC_NB;
@@ -425,59 +505,16 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       __syncthreads();
     }
     const int tg = i0 + s_tg[tb];
-    // ---- warp 0: widths at the old pose and the trial pose ----
-    if (warp == 0) {
+    TP& cur = s_pose[t & 1];
+    // ---- warp 0: the trial pose, unless it was built during the previous trial ----
+    if (warp == 0 && cur.trial != t) {
       double st_w = sig_t_fixed, sr_w = sig_r_fixed;
-      if constexpr (LEARN) {
-        if (s_spec_tg == tg) { st_w = s_spec[0]; sr_w = s_spec[1]; }
-        else mlp_widths_warp(s_mlp, 0, a.fcache + (size_t)tg * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st_w, sr_w);
-        st_old = st_w; sr_old = sr_w;
-      }
-      if (lane == 0) {
-        R rot[3];
+      if constexpr (LEARN)
+        mlp_widths_warp(s_mlp, 0, a.fcache + (size_t)tg * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st_w, sr_w);
+      double gk[6];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          rot_d[k] = s_g[k][tb] * sr_w;
-          dx_d[k] = s_g[3 + k][tb] * st_w;
-          rot[k] = (R)rot_d[k];
-        }
-        d2f = (float)(dx_d[0] * dx_d[0] + dx_d[1] * dx_d[1] + dx_d[2] * dx_d[2]);
-        r2f = (float)(rot_d[0] * rot_d[0] + rot_d[1] * rot_d[1] + rot_d[2] * rot_d[2]);
-        double qold[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
-        R off[NQ + 1][3];
-        trial_rotation<R, NQ>(rot, qold, a.body, qn_trial, off);
-        float oo[(NQ + 1) * 3];
-        if (MIXED) P::offsets(a, tg, oo);
-#pragma unroll
-        for (int s = 0; s <= NQ; ++s)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            s_on[s][k] = off[s][k];
-            s_oo[s][k] = MIXED ? (R)oo[3 * s + k] : (R)a.pk64[(size_t)tg * W64 + 3 + 3 * s + k];
-          }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          s_co[k] = a.st[(size_t)k * n + tg];
-          s_cn[k] = s_co[k] + dx_d[k];
-          s_fo[k] = a.fix[(size_t)k * n + tg];
-          s_fn[k] = to_fixed(s_cn[k], iL[k]);
-        }
-        if (FEAT) {
-          float on[(NQ + 1) * 3];
-#pragma unroll
-          for (int s = 0; s <= NQ; ++s)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) on[3 * s + k] = (float)off[s][k];
-          float u[4][3];
-          site_dirs<NQ>(on, u);
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) s_un[s][k] = u[s][k];
-        }
-      }
+      for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb];
+      build_trial<R, NQ, MIXED>(a, cur, t, tg, gk, st_w, sr_w, iL);
     }
     __syncthreads();
     if ((int)threadIdx.x >= E0) {
@@ -487,9 +524,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
 #pragma unroll
       for (int s = 0; s <= NQ; ++s)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) { ro[s][k] = s_oo[s][k]; rn[s][k] = s_on[s][k]; }
-      const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
-      const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
+        for (int k = 0; k < 3; ++k) { ro[s][k] = cur.oo[s][k]; rn[s][k] = cur.on[s][k]; }
+      const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+      const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
       for (int j = i0 + (int)threadIdx.x - E0; j < i1; j += NE) {
         if (j == tg) continue;
         R dO[3], dN[3], ddO, ddN;
@@ -539,75 +576,89 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
 #pragma unroll
       for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
       if (lane == 0) s_part[warp - NCTRL] = acc;
-    } else if constexpr (FEAT) {
-      // ---- control warps: feature neighbours of both poses, new-pose features ----
-      const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
-      const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
-      int cnt[2] = {0, 0};
-      for (int j0 = i0; j0 < i1; j0 += E0) {
-        const int j = j0 + (int)threadIdx.x;
-        bool qo = false, qn = false;
-        if (j < i1 && j != tg) {
-          float e[3];
-          if (MIXED) {
-            uint32_t fj[3];
-            P::fix(a, j, fj);
-            const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
-            qo = r2o < FEAT_RC2 && r2o > 0.0f;
-            qn = r2n < FEAT_RC2 && r2n > 0.0f;
-          } else {
-            double cj[3];
-            P::com(a, j, cj);
-            const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
-            qo = r2o < FEAT_RC2 && r2o > 0.0f;
-            qn = r2n < FEAT_RC2 && r2n > 0.0f;
+    } else {
+      // ---- control warps ----
+      const bool next_in_batch = tb + 1 < MC_NB && t + 1 < a.ntrial;
+      const int tg1 = next_in_batch ? i0 + s_tg[tb + 1] : -1;
+      if constexpr (FEAT) {
+        // feature neighbours of both poses of this trial
+        const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+        const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+        int cnt[2] = {0, 0};
+        for (int j0 = i0; j0 < i1; j0 += E0) {
+          const int j = j0 + (int)threadIdx.x;
+          bool qo = false, qn = false;
+          if (j < i1 && j != tg) {
+            float e[3];
+            if (MIXED) {
+              uint32_t fj[3];
+              P::fix(a, j, fj);
+              const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
+              qo = r2o < FEAT_RC2 && r2o > 0.0f;
+              qn = r2n < FEAT_RC2 && r2n > 0.0f;
+            } else {
+              double cj[3];
+              P::com(a, j, cj);
+              const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
+              qo = r2o < FEAT_RC2 && r2o > 0.0f;
+              qn = r2n < FEAT_RC2 && r2n > 0.0f;
+            }
+          }
+          queue_append(&s_q[0][warp * QSEG], cnt[0], qo, j, QSEG, a.flag);
+          queue_append(&s_q[1][warp * QSEG], cnt[1], qn, j, QSEG, a.flag);
+        }
+        if (lane == 0) { s_nq[0][warp] = min(cnt[0], QSEG); s_nq[1][warp] = min(cnt[1], QSEG); }
+        __syncwarp();
+        if (NCTRL > 1) asm volatile("bar.sync 1, %0;" ::"n"(32 * NCTRL));
+      }
+      if (warp == 0) {
+        if constexpr (FEAT) {
+          // features of the target at the new pose: terms of every queued neighbour
+          int f[MLP_IN];
+#pragma unroll
+          for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
+          float un[4][3];
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) un[s][k] = cur.un[s][k];
+          const uint32_t fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+          const double cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+          const int n0 = s_nq[1][0], nn = n0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
+          for (int p = lane; p < nn; p += 32) {
+            const int j = p < n0 ? s_q[1][p] : s_q[1][QSEG + p - n0];
+            float e[3], r2;
+            if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fn, fj, fs, e); }
+            else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cn, cj, L, iL, e); }
+            feat_terms(e, r2, un, 1, f);
+          }
+#pragma unroll
+          for (int k = 0; k < MLP_IN; ++k) {
+            const int v = __reduce_add_sync(0xffffffffu, f[k]);
+            if (lane == k) s_feat[k] = v;
+          }
+          __syncwarp();
+          if constexpr (LEARN) {
+            double st2, sr2;
+            mlp_widths_warp(s_mlp, 0, s_feat, a.mlp.sigma0_t, a.mlp.sigma0_r, st2, sr2);
+            if (lane == 0) { s_sig_new[0] = st2; s_sig_new[1] = sr2; }
           }
         }
-        queue_append(&s_q[0][warp * QSEG], cnt[0], qo, j, QSEG, a.flag);
-        queue_append(&s_q[1][warp * QSEG], cnt[1], qn, j, QSEG, a.flag);
-      }
-      if (lane == 0) { s_nq[0][warp] = min(cnt[0], QSEG); s_nq[1][warp] = min(cnt[1], QSEG); }
-      __syncwarp();
-      if (NCTRL > 1) asm volatile("bar.sync 1, %0;" ::"n"(32 * NCTRL));
-      if (warp == 0) {
-        // features of the target at the new pose: terms of every queued neighbour
-        int f[MLP_IN];
+        if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
+          double gk[6];
 #pragma unroll
-        for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
-        float un[4][3];
-#pragma unroll
-        for (int s = 0; s < 4; ++s)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) un[s][k] = s_un[s][k];
-        const int n0 = s_nq[1][0], nn = n0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
-        for (int p = lane; p < nn; p += 32) {
-          const int j = p < n0 ? s_q[1][p] : s_q[1][QSEG + p - n0];
-          float e[3], r2;
-          if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fn, fj, fs, e); }
-          else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cn, cj, L, iL, e); }
-          feat_terms(e, r2, un, 1, f);
-        }
-#pragma unroll
-        for (int k = 0; k < MLP_IN; ++k) {
-          const int v = __reduce_add_sync(0xffffffffu, f[k]);
-          if (lane == k) s_feat[k] = v;
-        }
-        __syncwarp();
-        if constexpr (LEARN) {
-          double st2, sr2;
-          mlp_widths_warp(s_mlp, 0, s_feat, a.mlp.sigma0_t, a.mlp.sigma0_r, st2, sr2);
-          if (lane == 0) { s_sig_new[0] = st2; s_sig_new[1] = sr2; }
+          for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb + 1];
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, gk, sig_t_fixed, sig_r_fixed, iL);
         }
       } else if constexpr (LEARN) {
-        // warp 1: widths of the next trial's target at its current pose
-        // (used unless this trial's move changes its features)
-        if (tb + 1 < MC_NB && t + 1 < a.ntrial) {
-          const int tg1 = i0 + s_tg[tb + 1];
+        if (next_in_batch) {
+          // warp 1: widths of the next trial's target at its current pose and its trial pose
           double st1, sr1;
           mlp_widths_warp(s_mlp, 1, a.fcache + (size_t)tg1 * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st1, sr1);
-          if (lane == 0) { s_spec[0] = st1; s_spec[1] = sr1; s_spec_tg = tg1; }
-        } else if (lane == 0) {
-          s_spec_tg = -1;
+          double gk[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb + 1];
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, gk, st1, sr1, iL);
         }
       }
     }
@@ -622,7 +673,8 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       if (lane == 0) {
         float logh = 0.0f;
         if (LEARN)
-          logh = log_q((float)s_sig_new[0], (float)s_sig_new[1], d2f, r2f) - log_q((float)st_old, (float)sr_old, d2f, r2f);
+          logh = log_q((float)s_sig_new[0], (float)s_sig_new[1], cur.d2, cur.r2) -
+                 log_q((float)cur.st, (float)cur.sr, cur.d2, cur.r2);
         const double x = -(dE * I2J * J2K) * beta + (double)logh;
         const bool ok = x >= 0.0 || s_lu[tb] < x;
         acc_flag = ok ? 1 : 0;
@@ -635,35 +687,38 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             double qold[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
-            trial_rotation<double, NQ>(rot_d, qold, a.body, qn, off64);
+            trial_rotation<double, NQ>(cur.rot, qold, a.body, qn, off64);
 #pragma unroll
             for (int s = 0; s <= NQ; ++s)
 #pragma unroll
               for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = off64[s][k];
           } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) qn[k] = (double)qn_trial[k];
+            for (int k = 0; k < 4; ++k) qn[k] = (double)cur.qn[k];
 #pragma unroll
             for (int s = 0; s <= NQ; ++s)
 #pragma unroll
-              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = (double)s_on[s][k];
+              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = (double)cur.on[s][k];
           }
 #pragma unroll
           for (int k = 0; k < 4; ++k) a.st[(size_t)(33 + k) * n + tg] = qn[k];
           float* pf = a.pk32f + (size_t)tg * 4 * NPK;
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
-            a.st[(size_t)k * n + tg] = s_cn[k];
-            p[k] = s_cn[k];
-            pf[k] = __uint_as_float(s_fn[k]);
-            a.fix[(size_t)k * n + tg] = s_fn[k];
+            a.st[(size_t)k * n + tg] = cur.cn[k];
+            p[k] = cur.cn[k];
+            pf[k] = __uint_as_float(cur.fn[k]);
+            a.fix[(size_t)k * n + tg] = cur.fn[k];
           }
 #pragma unroll
           for (int s = 0; s <= NQ; ++s)
 #pragma unroll
-            for (int k = 0; k < 3; ++k) pf[3 + 3 * s + k] = (float)s_on[s][k];
+            for (int k = 0; k < 3; ++k) pf[3 + 3 * s + k] = (float)cur.on[s][k];
           energy += dE;
           ++nacc;
+          // the next trial's prepared pose is stale when it moves the same molecule
+          if (s_pose[(t + 1) & 1].trial == t + 1 && t + 1 < a.ntrial && s_tg[(tb + 1) % MC_NB] + i0 == tg)
+            s_pose[(t + 1) & 1].trial = -1;
         }
         if (a.trace) {
           double* tr = a.trace + ((size_t)c * a.ntrial + t) * 4;
@@ -681,44 +736,47 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             rr[MLP_IN + lane] = (float)s_feat[lane] * FEAT_IQ;
           }
           if (lane == 0) {
-            rr[2 * MLP_IN] = d2f;
-            rr[2 * MLP_IN + 1] = r2f;
+            rr[2 * MLP_IN] = cur.d2;
+            rr[2 * MLP_IN + 1] = cur.r2;
             rr[2 * MLP_IN + 2] = (float)(dE * I2J * J2K * beta);
           }
         }
-        const int o0 = s_nq[0][0], no = o0 + (NCTRL > 1 ? s_nq[0][NCTRL - 1] : 0);
-        const int m0 = s_nq[1][0], nn = m0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
         if (acc_flag) {
           __syncwarp();
           if (lane < MLP_IN) a.fcache[(size_t)tg * MLP_IN + lane] = s_feat[lane];
           // neighbours of both poses: remove the old term, add the new one
-          const uint32_t fo[3] = {s_fo[0], s_fo[1], s_fo[2]}, fn[3] = {s_fn[0], s_fn[1], s_fn[2]};
-          const double co[3] = {s_co[0], s_co[1], s_co[2]}, cn[3] = {s_cn[0], s_cn[1], s_cn[2]};
+          const int o0 = s_nq[0][0], no = o0 + (NCTRL > 1 ? s_nq[0][NCTRL - 1] : 0);
+          const int m0 = s_nq[1][0], nn = m0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
+          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+          const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+          const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
           bool hit = false;
           for (int p = lane; p < no + nn; p += 32) {
             const bool old_pose = p < no;
             const int po = old_pose ? p : p - no;
             const int j = old_pose ? (po < o0 ? s_q[0][po] : s_q[0][QSEG + po - o0])
                                    : (po < m0 ? s_q[1][po] : s_q[1][QSEG + po - m0]);
-            hit = hit || j == s_spec_tg;
+            hit = hit || j == tg1;
             float e[3], r2;
             if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
             else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
             float o[(NQ + 1) * 3], u[4][3];
             P::offsets(a, j, o);
             site_dirs<NQ>(o, u);
-            int g[MLP_IN];
+            int gq[MLP_IN];
 #pragma unroll
-            for (int k = 0; k < MLP_IN; ++k) g[k] = 0;
-            feat_terms(e, r2, u, old_pose ? -1 : 1, g);
+            for (int k = 0; k < MLP_IN; ++k) gq[k] = 0;
+            feat_terms(e, r2, u, old_pose ? -1 : 1, gq);
             int* fc = a.fcache + (size_t)j * MLP_IN;
 #pragma unroll
             for (int k = 0; k < MLP_IN; ++k)
-              if (g[k] != 0) atomicAdd(fc + k, g[k]);
+              if (gq[k] != 0) atomicAdd(fc + k, gq[k]);
           }
-          if (LEARN && (__any_sync(0xffffffffu, hit) || s_spec_tg == tg) && lane == 0) s_spec_tg = -1;
+          // learned widths of the next trial were taken from features this move changed
+          if (LEARN && __any_sync(0xffffffffu, hit) && lane == 0) s_pose[(t + 1) & 1].trial = -1;
         }
       }
+      __syncwarp();
     }
     if (a.sample_every > 0 && (t + 1) % a.sample_every == 0) ++nsample;
   }

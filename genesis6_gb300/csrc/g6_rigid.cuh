@@ -9,10 +9,12 @@
 //                 the stochastic-collision thermostat, the Rigid_Ek /
 //                 Rigid_PressureTensor terms (:576-619) of one molecule, then the next
 //                 step's predict + placement and the neighbour-list displacement test
-//   step_reduce   per-block, per-replica partial sums; the last block to finish sums
-//                 the partials in a fixed order, computes T, P and the conserved
-//                 quantity (Mixture.F90:2251-2264, 2431-2453), runs Nose_Correct and the
-//                 next Nose_Predict (NoseModule.F90:43-87) and sets the rebuild flag.
+//   step_reduce   per-block, per-replica partial sums of the step; the last block
+//                 of each replica runs finish_replica, the last block overall
+//                 advances the step counter
+//   finish_replica per-replica sums in a fixed order, T, P and the conserved
+//                 quantity (Mixture.F90:2251-2264, 2431-2453), Nose_Correct and the
+//                 next Nose_Predict (NoseModule.F90:43-87), the step log
 // The plain path is all FP64; the mixed path (correct_mixed, predict_mixed,
 // place_mixed) keeps FP64 for com, d1, w1 and q and float for the rest.
 #pragma once
@@ -369,7 +371,7 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   float* stf = a.stf;
   const int r = a.p.rep.mol_rep[i];
   const ThermoDev th = a.th[r];
-  const float dt = (float)a.dt;
+  const float dt = a.fdt;
   double qd[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
   const float qf[4] = {(float)qd[0], (float)qd[1], (float)qd[2], (float)qd[3]};
   float t[9];
@@ -385,7 +387,7 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
     ext_t = 0.5f * ext_r;
   }
   // COM: Gear-5
-  const float cf = (float)(a.dt * a.dt * 0.5 / a.mass);
+  const float cf = a.fcf;
   double d1d[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -411,7 +413,7 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
     G6_ST(33 + c) = qd[c];
   }
   // angular velocity: Gear-4 with Euler's equations
-  const float Ix = (float)a.I[0], Iy = (float)a.I[1], Iz = (float)a.I[2];
+  const float Ix = a.fI[0], Iy = a.fI[1], Iz = a.fI[2];
   float nf[3];
   nf[0] = (tau[0] + (Iy - Iz) * w1f[1] * w1f[2]) * dt / Ix - w1f[0] * ext_r;
   nf[1] = (tau[1] + (Iz - Ix) * w1f[2] * w1f[0]) * dt / Iy - w1f[1] * ext_r;
@@ -525,10 +527,92 @@ __device__ __forceinline__ double red_shfl(double v, int m) { return __shfl_xor_
 __device__ __forceinline__ double red_double(FF v) { return (double)v.hi + (double)v.lo; }
 __device__ __forceinline__ double red_double(double v) { return v; }
 
+// Reductions, thermostat and log of replica rr for the step (block-wide; run
+// by the last block of the replica to finish): the replica's block partials
+// summed in a fixed order, T, P and the conserved quantity
+// (Mixture.F90:2251-2264, 2431-2453), Nose_Correct and the next Nose_Predict
+// (NoseModule.F90:43-87).
+__device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int step) {
+  __shared__ double wsum[32][NRED];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+  const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
+  const int slot0 = rr - a.p.rep.mol_rep[b0 * mpb];   // later blocks start inside replica rr
+  double sum[NRED];
+#pragma unroll
+  for (int k = 0; k < NRED; ++k) sum[k] = 0.0;
+#pragma unroll 4
+  for (int b = b0 + (int)threadIdx.x; b <= b1; b += blockDim.x) {
+    const double* src = a.part + ((size_t)b * MAXREP_PER_BLOCK + (b == b0 ? slot0 : 0)) * NRED;
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) sum[k] += __ldcg(src + k);
+  }
+#pragma unroll
+  for (int k = 0; k < NRED; ++k) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) sum[k] += __shfl_xor_sync(0xffffffffu, sum[k], m);
+    if (lane == 0) wsum[warp][k] = sum[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) {
+      double x = 0.0;
+      for (int w = 0; w < nwarp; ++w) x += wsum[w][k];
+      s[k] = x;
+      a.red[(size_t)rr * NRED + k] = x;
+    }
+    const bool predict_next = step + 1 < a.ctrl[2];
+    ThermoDev& th = a.th[rr];
+    const double dt = a.dt;
+    const int nm = a.p.rep.off[rr + 1] - a.p.rep.off[rr];
+    const double dof = 6.0 * nm;
+    const double ekt = s[2] * a.mass * 0.5 * a.inv_dt2;
+    const double ekr = s[3] * 0.5;
+    const double temperature = (ekt + ekr) * a.rfac[2 * rr];
+    const double pkin = s[2] * a.mass * a.inv_dt2;
+    const double pressure = (pkin + s[1]) * a.rfac[2 * rr + 1];
+    if (th.kind == G6_NOSE) {   // Nose_Correct
+      const double zetaf = (temperature - th.temp) * th.inv_q - th.dump * th.z[0];
+      const double dz2 = zetaf - th.z[1];
+      th.z[0] = th.z[0] + G40 * dz2;
+      th.z[1] = zetaf;
+      th.z[2] = th.z[2] + G42 * dz2;
+      th.z[3] = th.z[3] + G43 * dz2;
+      th.z[4] = th.z[4] + G44 * dz2;
+      th.zsum = th.zsum + th.z[0];
+    }
+    double nose_ek = 0.0, nose_ep = 0.0;
+    if (th.kind == G6_NOSE) {
+      nose_ek = (th.z[0] * th.z[0] * th.q * dt * dof * 0.5) * RGAS;
+      nose_ep = (dof * th.temp * (th.zsum - 0.5 * th.z[0]) * dt) * RGAS;
+    }
+    if (a.log && step < a.ctrl[5]) {
+      double* lg = a.log + ((size_t)step * a.p.rep.nrep + rr) * G6_LOG_WIDTH;
+      lg[0] = s[0]; lg[1] = ekt; lg[2] = ekr; lg[3] = temperature; lg[4] = pressure;
+      lg[5] = (s[0] + ekt + ekr) * I2J + nose_ep + nose_ek;
+      lg[6] = s[4]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
+    }
+    if (predict_next && th.kind == G6_NOSE) {   // Nose_Predict for the next step
+      th.z[0] = th.z[0] + th.z[1] + th.z[2] + th.z[3] + th.z[4];
+      th.z[1] = th.z[1] + 2.0 * th.z[2] + 3.0 * th.z[3] + 4.0 * th.z[4];
+      th.z[2] = th.z[2] + 3.0 * th.z[3] + 6.0 * th.z[4];
+      th.z[3] = th.z[3] + 4.0 * th.z[4];
+    }
+  }
+  __syncthreads();
+}
+
+// Block partials of the step (warp 0 holds one molecule per lane): per replica
+// slot, sums over the lanes (FP64 in the plain path, float pairs with error-free
+// addition in the mixed path); the largest displacement goes to an atomic max
+// word.  The last block of each replica to arrive finishes that replica
+// (finish_replica); the last block overall advances the step counter.
 template <class V>
-__device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step,
-                            bool predict_next) {
+__device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step) {
   const int n = a.p.n;
+  __shared__ int s_rfirst, s_nslots;
+  __shared__ int s_last[MAXREP_PER_BLOCK];
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     const int first_i = blockIdx.x * mpb;
@@ -553,91 +637,39 @@ __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float 
       b |= __shfl_xor_sync(0xffffffffu, b, o);
     }
     if (lane == 0) {
-      a.partmax[blockIdx.x] = (double)m;
+      // non-negative floats order like their bit patterns: an exact, order-free maximum
+      if (m > 0.0f) atomicMax(&a.gmax[step & 1], __float_as_uint(m));
       if (b) atomicOr(&a.ctrl[3], 1);
+      s_rfirst = rfirst;
+      s_nslots = nslots;
     }
   }
-  __shared__ int am_last;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(a.done, 1u) == gridDim.x - 1);
+  if ((int)threadIdx.x < s_nslots) {
+    const int rr = s_rfirst + threadIdx.x;
+    const int nb = (a.p.rep.off[rr + 1] - 1) / mpb - a.p.rep.off[rr] / mpb + 1;
+    s_last[threadIdx.x] = atomicAdd(&a.repcnt[rr], 1) == nb - 1;
+  }
   __syncthreads();
-  if (!am_last || threadIdx.x >= 32) return;
-  __threadfence();
-  const int lane = threadIdx.x;
-  const int nrep = a.p.rep.nrep;
-  for (int rr = 0; rr < nrep; ++rr) {
-    const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
-    double s[NRED];
-#pragma unroll
-    for (int k = 0; k < NRED; ++k) s[k] = 0.0;
-    for (int b = b0 + lane; b <= b1; b += 32) {
-      const int slot = rr - a.p.rep.mol_rep[b * mpb];
-      const double* src = a.part + ((size_t)b * MAXREP_PER_BLOCK + slot) * NRED;
-#pragma unroll
-      for (int k = 0; k < NRED; ++k) s[k] += __ldcg(src + k);
-    }
-#pragma unroll
-    for (int k = 0; k < NRED; ++k) {
-      double x = s[k];
-#pragma unroll
-      for (int m = 16; m >= 1; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
-      if (lane == 0) a.red[rr * NRED + k] = x;
-    }
+  for (int sl = 0; sl < s_nslots; ++sl) {
+    if (!s_last[sl]) continue;
+    __threadfence();
+    finish_replica(a, s_rfirst + sl, mpb, step);
+    if (threadIdx.x == 0) a.repcnt[s_rfirst + sl] = 0;
   }
-  double gm = 0.0;
-  for (int b = lane; b < (int)gridDim.x; b += 32) gm = fmax(gm, __ldcg(&a.partmax[b]));
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) gm = fmax(gm, __shfl_xor_sync(0xffffffffu, gm, m));
-  __syncwarp();
-  const int logcap = a.ctrl[5];
-  for (int rr = lane; rr < nrep; rr += 32) {
-    const double* s = a.red + (size_t)rr * NRED;
-    ThermoDev& th = a.th[rr];
-    const int nm = a.p.rep.off[rr + 1] - a.p.rep.off[rr];
-    const double dof = 6.0 * nm;
-    const double dt = a.dt;
-    const double ekt = s[2] * a.mass * 0.5 * (1.0 / (dt * dt));
-    const double ekr = s[3] * 0.5;
-    const double temperature = I2J * 2.0 * (ekt + ekr) / (RGAS * dof);
-    const double pkin = s[2] * a.mass * (1.0 / (dt * dt));
-    const double vp = pkin + s[1];
-    const double vol = a.p.rep.L[3 * rr] * a.p.rep.L[3 * rr + 1] * a.p.rep.L[3 * rr + 2];
-    const double pressure = (vp / 3.0) * I2J * (1.0 / A2P) / (vol * NA * ANG2M * ANG2M * ANG2M);
-    if (th.kind == G6_NOSE) {   // Nose_Correct
-      const double zetaf = (temperature - th.temp) / th.q - th.dump * th.z[0];
-      const double dz2 = zetaf - th.z[1];
-      th.z[0] = th.z[0] + G40 * dz2;
-      th.z[1] = zetaf;
-      th.z[2] = th.z[2] + G42 * dz2;
-      th.z[3] = th.z[3] + G43 * dz2;
-      th.z[4] = th.z[4] + G44 * dz2;
-      th.zsum = th.zsum + th.z[0];
-    }
-    double nose_ek = 0.0, nose_ep = 0.0;
-    if (th.kind == G6_NOSE) {
-      nose_ek = (th.z[0] * th.z[0] * th.q * dt * dof * 0.5) * RGAS;
-      nose_ep = (dof * th.temp * (th.zsum - 0.5 * th.z[0]) * dt) * RGAS;
-    }
-    if (a.log && step < logcap) {
-      double* lg = a.log + ((size_t)step * nrep + rr) * G6_LOG_WIDTH;
-      lg[0] = s[0]; lg[1] = ekt; lg[2] = ekr; lg[3] = temperature; lg[4] = pressure;
-      lg[5] = (s[0] + ekt + ekr) * I2J + nose_ep + nose_ek;
-      lg[6] = s[4]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
-    }
-    if (predict_next && th.kind == G6_NOSE) {   // Nose_Predict for the next step
-      th.z[0] = th.z[0] + th.z[1] + th.z[2] + th.z[3] + th.z[4];
-      th.z[1] = th.z[1] + 2.0 * th.z[2] + 3.0 * th.z[3] + 4.0 * th.z[4];
-      th.z[2] = th.z[2] + 3.0 * th.z[3] + 6.0 * th.z[4];
-      th.z[3] = th.z[3] + 4.0 * th.z[4];
-    }
-  }
-  __syncwarp();
-  if (lane == 0) {
-    a.ctrl[0] = (predict_next && gm > a.half_skin2) ? 1 : 0;
+  // (every block has read ctrl[1] before it arrives at the counter)
+  if (threadIdx.x == 0 && atomicAdd(a.done, 1u) == gridDim.x - 1) {
     a.ctrl[1] = step + 1;
+    a.ctrl[4] = 1;
     *a.done = 0u;
   }
+}
+
+// Largest squared displacement since the last list build over the finished
+// step ctrl[1]-1.
+__device__ __forceinline__ double step_gmax(const StepArgs& a) {
+  return (double)__uint_as_float(__ldcg(&a.gmax[(a.ctrl[1] - 1) & 1]));
 }
 
 #undef G6_ST
