@@ -347,7 +347,7 @@ def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
             "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed"}
 
 
-def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=1500, w_energy=0.0):
+def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=3000, w_energy=0.0):
     """32 chains x 1,024 ST2 (custom path, Coulomb taper), 260 K, rc = L/2 with a
     2 A switch.  Chains are equilibrated from the lattice with the fixed widths,
     then the MLP is trained on `records` plain-sampler moves and both samplers
@@ -429,6 +429,72 @@ def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=1
             "ess_per_gpu_s_learned_over_fixed": out["learned"]["ess_per_gpu_s"] / out["fixed"]["ess_per_gpu_s"],
             "mean_U_difference_in_sigma": float(d / sig) if sig > 0 else None,
             "U_unit": "10 J/mol per chain (internal)"}
+
+
+def bench_rms(torch, rec_eq, L, snapshots=100, every=20):
+    """Relative RMS force and torque error of the mixed path on `snapshots`
+    configurations of a TIP4P-4096 Nose-Hoover trajectory (one every `every`
+    steps), against the FP64 path (which follows the FP64 oracle to 1e-12)."""
+    sm = make_system("TIP4P", N_MAIN, "mixed", L, rec_eq)
+    s64 = make_system("TIP4P", N_MAIN, "fp64", L, rec_eq)
+    th = thermo_for(sm)
+    num_f = den_f = num_t = den_t = 0.0
+    worst = 0.0
+    for k in range(snapshots):
+        sm.md_run(DT, every, th, log=False)
+        rec = sm.download_state()
+        s64.upload_state(rec)
+        Fm, tm, _, _ = sm.force()
+        F6, t6, _, _ = s64.force()
+        num_f += float(np.sum((Fm - F6) ** 2)); den_f += float(np.sum(F6 ** 2))
+        num_t += float(np.sum((tm - t6) ** 2)); den_t += float(np.sum(t6 ** 2))
+        worst = max(worst, float(np.sqrt(np.sum((Fm - F6) ** 2) / np.sum(F6 ** 2))))
+    sm.close(); s64.close()
+    return {"snapshots": snapshots, "every_steps": every, "rms_force_rel": float(np.sqrt(num_f / den_f)),
+            "rms_torque_rel": float(np.sqrt(num_t / den_t)), "worst_snapshot_force_rel": worst,
+            "against": "the FP64 path on the same configurations"}
+
+
+def bench_tip5p(torch, seed=20261205, melt=2000, steps=5000):
+    """32,768 TIP5P at 1.0 g/cm^3, rc 9 A (2 A switch), dt 1 fs: lattice melted
+    2,000 steps at 400 K (Nose-Hoover), velocities redrawn at 300 K, then NVE
+    for `steps` steps in mixed precision and in FP64 from the same state.
+    Energy drift = slope of a least-squares line through H per molecule
+    (kJ/mol) against time (ns)."""
+    from genesis6_gb300 import config
+    dt = 0.001
+    n = N_BIG
+    b = config.water_box("TIP5P", n, seed, temp=400.0, dt=dt)
+    s = make_system("TIP5P", n, "mixed", b["L"], b["rec"])
+    q = 400.0 * TAU_NOSE ** 2 / dt
+    s.md_run(dt, melt, s.thermostats(1, "nose", temp=400.0, q=q, dump=0.0), log=False)
+    rec = s.download_state()
+    rng = np.random.default_rng(seed + 1)
+    v, w = config.maxwell_boltzmann(n, 300.0, b["mass"], b["inertia"], rng)
+    start = config.rigid_records(rec[:, 0:3], rec[:, 33:37], v, w, dt)
+    out = {"molecules": n, "dt_fs": 1.0, "melt_steps_400K": melt, "nve_steps": steps}
+    for prec in ("mixed", "fp64"):
+        if prec == "fp64":
+            s.close()
+            s = make_system("TIP5P", n, "fp64", b["L"], start)
+        else:
+            s.upload_state(start)
+        th = s.thermostats(1, "nve")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        log = s.md_run(dt, steps, th)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        H = log[:, 0, 5] * 1e-3 / n                     # kJ/mol per molecule
+        tns = np.arange(steps) * dt * 1e-3              # ns
+        slope = float(np.polyfit(tns, H, 1)[0])
+        ms = 1e3 * wall / steps
+        out[prec] = {"ns_per_day": dt * 1e-3 * 86400.0 / (ms * 1e-3), "ms_per_step": ms,
+                     "drift_kJ_per_mol_per_ns": slope, "H_first_last_kJ_per_mol": [float(H[0]), float(H[-1])],
+                     "T_mean_K": float(log[:, 0, 3].mean())}
+    s.close()
+    out["timing"] = "wall clock over the NVE run (CUDA-graph steps, no L2 flush)"
+    return out
 
 
 def run_gpu(args, rank, world, local):
@@ -520,6 +586,8 @@ def run_gpu(args, rank, world, local):
     cpu = None if args.no_cpu else cpu_md_rate(budget_s=12.0)
     rex = None if args.no_extra else bench_replicas(torch)
     mcb = None if args.no_extra else bench_mc(torch)
+    rms = None if args.no_extra else bench_rms(torch, rec_eq, L)
+    t5p = None if (args.no_extra or args.no_32k) else bench_tip5p(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -527,6 +595,8 @@ def run_gpu(args, rank, world, local):
         "Maxwell-Boltzmann 300 K, 2,000-step pre-equilibration)", "config": config_block(args, world),
         "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
         "tip4p_32k": big,
+        "tip5p_32k_nve": t5p,
+        "mixed_rms_error_4096": rms,
         "replica_exchange": rex,
         "mc_learned_vs_fixed": mcb,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",

@@ -220,6 +220,7 @@ struct g6_ctx {
   float* d_mlp = nullptr;          // parameters
   int* d_fcache = nullptr;         // per-molecule features at the current pose (Monte Carlo)
   int* d_mcflag = nullptr;         // Monte Carlo: too many feature neighbours
+  float* d_udir = nullptr;         // Monte Carlo: charged-site directions per molecule
   float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
   double sig0_t = 0.15, sig0_r = 0.15;
   double obj_move = 1.0, obj_energy = 0.0;   // training objective weights (g6_mlp_objective)
@@ -609,7 +610,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_sig_t, nrep)); CK(dalloc(ctx, &ctx->d_sig_r, nrep)); CK(dalloc(ctx, &ctx->d_energy, nrep));
   CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
   CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_fcache, (size_t)n * MLP_IN));
-  CK(dalloc(ctx, &ctx->d_mcflag, 1));
+  CK(dalloc(ctx, &ctx->d_mcflag, 1)); CK(dalloc(ctx, &ctx->d_udir, (size_t)n * 12));
   ctx->last_epot.assign(nrep, 0.0);
   ctx->have_system = true;
   return G6_OK;
@@ -1366,7 +1367,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
   a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
   a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
-  a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag;
+  a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
   a.mlp = mlp_dev(ctx);
   CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
   if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode, ctx->stream));

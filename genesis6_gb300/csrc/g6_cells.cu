@@ -334,7 +334,9 @@ int rebuild_grid_limit() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebuild, 256, 0);
-  return sms * (per > 0 ? per : 1);
+  // two blocks per SM: the launch runs every step and mostly returns at once,
+  // so its block count is paid every step while a rebuild is rare
+  return sms * (per > 2 ? 2 : (per > 0 ? per : 1));
 }
 
 cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int* cellmol, int grid_limit,

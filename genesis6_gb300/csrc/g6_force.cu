@@ -184,13 +184,14 @@ __device__ __forceinline__ double group_sum(double v) {
 // k_force: neighbour-list force kernel.
 // ---------------------------------------------------------------------------
 // Molecules per block of the fused step kernel: the block is MPB x LPI
-// threads and warp 0 runs the integrator with one molecule per lane.  Small
-// blocks let several blocks share an SM, so one block's integrator epilogue
-// overlaps the site loops of the others; 8 molecules per epilogue warp keep the
-// FP64 instruction count low.  The mixed kernel is capped at 128 registers.
+// threads (128, or 256 at 32 lanes) and warp 0 runs the integrator with one
+// molecule per lane.  Small blocks let several blocks share an SM, so one
+// block's integrator epilogue overlaps the site loops of the others; at least 8
+// molecules per epilogue warp keep the FP64 instruction count low.  The mixed
+// kernel is capped at 128 registers.
 template <bool MIXED, int LPI>
 struct StepShape {
-  static constexpr int MPB = (64 / LPI) > 8 ? (64 / LPI) : 8;
+  static constexpr int MPB = (128 / LPI) > 8 ? (128 / LPI) : 8;
   static constexpr int THREADS = MPB * LPI;
   static constexpr int MINB = MIXED ? 65536 / (THREADS * 128) : 1;
 };

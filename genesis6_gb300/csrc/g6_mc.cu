@@ -44,7 +44,7 @@
 namespace g6 {
 
 constexpr int MC_NT = 512;            // threads per chain
-constexpr int MC_NB = 256;            // trials per batch of pre-computed draws
+constexpr int MC_NB = 128;            // trials per batch of pre-computed draws
 constexpr float FEAT_Q = 1048576.0f;  // feature terms are integers of 2^-20
 constexpr float FEAT_IQ = 1.0f / 1048576.0f;
 constexpr float FEAT_RC2 = 6.5f * 6.5f;
@@ -112,13 +112,13 @@ __device__ __forceinline__ void qadd(R q1[4], const R q2[4]) {
 // qinfrotator (QuatModule.F90:203-223) composed with the old orientation, the
 // rotation matrix of rigid_setmatrix and the lab offsets of sites 0..NQ.
 template <class R, int NQ>
-__device__ __forceinline__ void trial_rotation(const R rot[3], const double* qold, const double (&body)[MAXSITE][3],
+__device__ __forceinline__ void trial_rotation(const R rot[3], const R* qold, const double (&body)[MAXSITE][3],
                                                R qn[4], R (&off)[NQ + 1][3]) {
   R qr[4] = {R(1), rot[0], rot[1], rot[2]};
   const R rn = R(1) / sqrt(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
 #pragma unroll
   for (int k = 0; k < 4; ++k) qr[k] *= rn;
-  R qo[4] = {(R)qold[0], (R)qold[1], (R)qold[2], (R)qold[3]};
+  R qo[4] = {qold[0], qold[1], qold[2], qold[3]};
   qadd(qr, qo);
   const R qa = qr[0], qb = qr[1], qc = qr[2], qd = qr[3];
   R tm[9];
@@ -148,6 +148,13 @@ __device__ __forceinline__ float dot3_rn(const float a[3], const float b[3]) {
 __device__ __forceinline__ float gauss_rn(float t) { return exp2f(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)); }
 __device__ __forceinline__ int feat_q(float x) { return __float2int_rn(__fmul_rn(x, FEAT_Q)); }
 
+// Unit direction of one site offset v.
+__device__ __forceinline__ void site_dir1(const float v[3], float u[3]) {
+  const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3_rn(v, v)));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = __fmul_rn(v[k], inv);
+}
+
 // Unit directions of the charged sites 1..NQ from their offsets o[(NQ+1)*3].
 template <int NQ>
 __device__ __forceinline__ void site_dirs(const float* o, float (&u)[4][3]) {
@@ -155,9 +162,7 @@ __device__ __forceinline__ void site_dirs(const float* o, float (&u)[4][3]) {
   for (int s = 0; s < 4; ++s) {
     if (s < NQ) {
       const float v[3] = {o[3 * (s + 1)], o[3 * (s + 1) + 1], o[3 * (s + 1) + 2]};
-      const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3_rn(v, v)));
-#pragma unroll
-      for (int k = 0; k < 3; ++k) u[s][k] = __fmul_rn(v[k], inv);
+      site_dir1(v, u[s]);
     } else {
       u[s][0] = u[s][1] = u[s][2] = 0.0f;
     }
@@ -226,6 +231,10 @@ __device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3]
     float o[(NQ + 1) * 3], u[4][3];
     P::offsets(a, i, o);
     site_dirs<NQ>(o, u);
+#pragma unroll
+    for (int s = 0; s < 4; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a.udir[(size_t)i * 12 + 3 * s + k] = u[s][k];
     int f[MLP_IN];
 #pragma unroll
     for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
@@ -336,16 +345,20 @@ __device__ __forceinline__ float log_q(float st, float sr, float d2, float r2) {
 }
 
 // Queues of the molecules within the feature radius of the old (0) and new
-// (1) pose of the target.  Control warp w owns segment w of each queue and
-// appends with ballots only (no atomics); seg_n[p][w] is its length.
-__device__ __forceinline__ void queue_append(int* seg, int& cnt, bool in, int j, int qseg, int* overflow) {
+// (1) pose of the target: whole warps append with one ballot and one shared
+// atomic per warp.
+__device__ __forceinline__ void queue_push(int* q, int* count, bool in, int j, int* overflow) {
   const unsigned m = __ballot_sync(0xffffffffu, in);
+  if (m == 0u) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
   if (in) {
-    const int pos = cnt + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
-    if (pos < qseg) seg[pos] = j;
+    const int pos = base + __popc(m & ((1u << lane) - 1u));
+    if (pos < MC_QMAX) q[pos] = j;
     else *overflow = 1;
   }
-  cnt += __popc(m);
 }
 
 // One trial's proposal: widths, draws, the trial pose of the target and its
@@ -364,48 +377,52 @@ struct TrialPose {
   int trial;                        // trial number the pose belongs to (-1: none)
 };
 
-// Warp-cooperative build of trial `trial` (target tg, unit normals g[6]).
-// The arithmetic of every quantity is the serial formula of mc2 (each lane
-// evaluates the same expressions).
+// Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot]).
+// The arithmetic of every quantity is the serial formula of mc2; FP64 work is
+// done by the lanes that own it (component k on lane k), since the FP64 pipe's
+// cost grows with the active lanes.
 template <class R, int NQ, bool MIXED>
-__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const double* g, double st_w,
-                            double sr_w, const double iL[3]) {
+__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const double (*g)[MC_NB],
+                            int slot, double st_w, double sr_w, const double iL[3]) {
   using Pr = PoseRead<NQ, MIXED>;
   const int lane = threadIdx.x & 31;
   const int n = a.n;
-  // loads spread over lanes
-  double qv = 0.0, cv = 0.0;
+  double qv = 0.0, cv = 0.0, rk = 0.0, dk = 0.0;
   uint32_t fv = 0u;
   R ov = R(0);
   if (lane < 4) qv = a.st[(size_t)(33 + lane) * n + tg];
-  if (lane < 3) { cv = a.st[(size_t)lane * n + tg]; fv = a.fix[(size_t)lane * n + tg]; }
+  if (lane < 3) {
+    cv = a.st[(size_t)lane * n + tg];
+    fv = a.fix[(size_t)lane * n + tg];
+    rk = g[lane][slot] * sr_w;
+    dk = g[3 + lane][slot] * st_w;
+  }
   if (lane < 3 * (NQ + 1))
     ov = MIXED ? (R)a.pk32f[(size_t)tg * 4 * Pr::NPK + 3 + lane] : (R)a.pk64[(size_t)tg * Pr::W64 + 3 + lane];
-  double qold[4];
+  const R qr = (R)qv, rr = (R)rk;   // conversions on the owning lanes only
+  R qold[4], rot[3];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) qold[k] = __shfl_sync(0xffffffffu, qv, k);
-  double rot_d[3], dx_d[3];
-  R rot[3];
+  for (int k = 0; k < 4; ++k) qold[k] = __shfl_sync(0xffffffffu, qr, k);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    rot_d[k] = g[k] * sr_w;
-    dx_d[k] = g[3 + k] * st_w;
-    rot[k] = (R)rot_d[k];
-  }
+  for (int k = 0; k < 3; ++k) rot[k] = __shfl_sync(0xffffffffu, rr, k);
   R qn[4], off[NQ + 1][3];
   trial_rotation<R, NQ>(rot, qold, a.body, qn, off);
+  if (lane < 3) {
+    const double il = lane == 0 ? iL[0] : (lane == 1 ? iL[1] : iL[2]);
+    const double cn = cv + dk;
+    P.co[lane] = cv;
+    P.cn[lane] = cn;
+    P.fo[lane] = fv;
+    P.fn[lane] = to_fixed(cn, il);
+    P.rot[lane] = rk;
+    P.dx[lane] = dk;
+  }
+  const double d2k = dk * dk, r2k = rk * rk;   // nonzero on lanes 0-2 only
+  const double d2a = __shfl_sync(0xffffffffu, d2k, 0), d2b = __shfl_sync(0xffffffffu, d2k, 1),
+               d2c = __shfl_sync(0xffffffffu, d2k, 2);
+  const double r2a = __shfl_sync(0xffffffffu, r2k, 0), r2b = __shfl_sync(0xffffffffu, r2k, 1),
+               r2c = __shfl_sync(0xffffffffu, r2k, 2);
   // register arrays are indexed with constants only (selects), never by lane
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-    if (lane == k) {
-      const double cn = cv + dx_d[k];
-      P.co[k] = cv;
-      P.cn[k] = cn;
-      P.fo[k] = fv;
-      P.fn[k] = to_fixed(cn, iL[k]);
-      P.rot[k] = rot_d[k];
-      P.dx[k] = dx_d[k];
-    }
 #pragma unroll
   for (int s = 0; s <= NQ; ++s)
 #pragma unroll
@@ -414,22 +431,23 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     if (lane == k) P.qn[k] = qn[k];
+  // unit directions of the charged sites at the new pose, one site per lane
+#pragma unroll
+  for (int s = 0; s < 4; ++s)
+    if (lane == 8 + s) {
+      float u[3] = {0.0f, 0.0f, 0.0f};
+      if (s < NQ) {
+        const float v[3] = {(float)off[s + 1][0], (float)off[s + 1][1], (float)off[s + 1][2]};
+        site_dir1(v, u);
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) P.un[s][k] = u[k];
+    }
   if (lane == 0) {
-    P.d2 = (float)(dx_d[0] * dx_d[0] + dx_d[1] * dx_d[1] + dx_d[2] * dx_d[2]);
-    P.r2 = (float)(rot_d[0] * rot_d[0] + rot_d[1] * rot_d[1] + rot_d[2] * rot_d[2]);
+    P.d2 = (float)(d2a + d2b + d2c);
+    P.r2 = (float)(r2a + r2b + r2c);
     P.st = st_w;
     P.sr = sr_w;
-    float on[(NQ + 1) * 3];
-#pragma unroll
-    for (int s = 0; s <= NQ; ++s)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) on[3 * s + k] = (float)off[s][k];
-    float u[4][3];
-    site_dirs<NQ>(on, u);
-#pragma unroll
-    for (int s = 0; s < 4; ++s)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) P.un[s][k] = u[s][k];
     P.trial = trial;
   }
   __syncwarp();
@@ -444,10 +462,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   constexpr bool LEARN = MODE == G6_MC_LEARNED;
   // control warps build the next trial's pose (and, with features, find the
   // feature neighbours and run the network) while the others sum energies
-  constexpr int NCTRL = LEARN ? 2 : 1;
+  constexpr int NCTRL = LEARN ? 2 : (FEAT ? 1 : 0);
   constexpr int E0 = 32 * NCTRL, NE = MC_NT - E0, NEW = NE / 32;
   constexpr int W64 = P::W64, NPK = P::NPK;
-  constexpr int QSEG = MC_QMAX / NCTRL;
   __shared__ double s_lu[MC_NB];
   __shared__ double s_g[6][MC_NB];
   __shared__ int s_tg[MC_NB];
@@ -455,7 +472,8 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   __shared__ int s_feat[MLP_IN];
   __shared__ R s_part[NEW];
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
-  __shared__ int s_nq[2][NCTRL];
+  __shared__ int s_nq[2];
+  __shared__ int s_accept, s_hit;
   __shared__ double s_sig_new[2];
   __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
 
@@ -506,15 +524,13 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
     }
     const int tg = i0 + s_tg[tb];
     TP& cur = s_pose[t & 1];
+    if (FEAT && threadIdx.x == 0) { s_nq[0] = 0; s_nq[1] = 0; }
     // ---- warp 0: the trial pose, unless it was built during the previous trial ----
     if (warp == 0 && cur.trial != t) {
       double st_w = sig_t_fixed, sr_w = sig_r_fixed;
       if constexpr (LEARN)
         mlp_widths_warp(s_mlp, 0, a.fcache + (size_t)tg * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st_w, sr_w);
-      double gk[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb];
-      build_trial<R, NQ, MIXED>(a, cur, t, tg, gk, st_w, sr_w, iL);
+      build_trial<R, NQ, MIXED>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL);
     }
     __syncthreads();
     if ((int)threadIdx.x >= E0) {
@@ -527,6 +543,34 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         for (int k = 0; k < 3; ++k) { ro[s][k] = cur.oo[s][k]; rn[s][k] = cur.on[s][k]; }
       const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
       const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+      if constexpr (FEAT) {
+        // feature neighbours of both poses (whole warps, ballots into this warp's
+        // segments), then release the control warps
+        const int ew = warp - NCTRL;
+        for (int j0 = i0 + 32 * ew; j0 < i1; j0 += NE) {
+          const int j = j0 + lane;
+          bool qo = false, qn = false;
+          if (j < i1 && j != tg) {
+            float e[3];
+            if (MIXED) {
+              uint32_t fj[3];
+              P::fix(a, j, fj);
+              const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
+              qo = r2o < FEAT_RC2 && r2o > 0.0f;
+              qn = r2n < FEAT_RC2 && r2n > 0.0f;
+            } else {
+              double cj[3];
+              P::com(a, j, cj);
+              const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
+              qo = r2o < FEAT_RC2 && r2o > 0.0f;
+              qn = r2n < FEAT_RC2 && r2n > 0.0f;
+            }
+          }
+          queue_push(s_q[0], &s_nq[0], qo, j, a.flag);
+          queue_push(s_q[1], &s_nq[1], qn, j, a.flag);
+        }
+        asm volatile("bar.arrive 1, %0;" ::"n"(NE + 32));
+      }
       for (int j = i0 + (int)threadIdx.x - E0; j < i1; j += NE) {
         if (j == tg) continue;
         R dO[3], dN[3], ddO, ddN;
@@ -580,40 +624,10 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       // ---- control warps ----
       const bool next_in_batch = tb + 1 < MC_NB && t + 1 < a.ntrial;
       const int tg1 = next_in_batch ? i0 + s_tg[tb + 1] : -1;
-      if constexpr (FEAT) {
-        // feature neighbours of both poses of this trial
-        const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-        const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-        int cnt[2] = {0, 0};
-        for (int j0 = i0; j0 < i1; j0 += E0) {
-          const int j = j0 + (int)threadIdx.x;
-          bool qo = false, qn = false;
-          if (j < i1 && j != tg) {
-            float e[3];
-            if (MIXED) {
-              uint32_t fj[3];
-              P::fix(a, j, fj);
-              const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
-              qo = r2o < FEAT_RC2 && r2o > 0.0f;
-              qn = r2n < FEAT_RC2 && r2n > 0.0f;
-            } else {
-              double cj[3];
-              P::com(a, j, cj);
-              const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
-              qo = r2o < FEAT_RC2 && r2o > 0.0f;
-              qn = r2n < FEAT_RC2 && r2n > 0.0f;
-            }
-          }
-          queue_append(&s_q[0][warp * QSEG], cnt[0], qo, j, QSEG, a.flag);
-          queue_append(&s_q[1][warp * QSEG], cnt[1], qn, j, QSEG, a.flag);
-        }
-        if (lane == 0) { s_nq[0][warp] = min(cnt[0], QSEG); s_nq[1][warp] = min(cnt[1], QSEG); }
-        __syncwarp();
-        if (NCTRL > 1) asm volatile("bar.sync 1, %0;" ::"n"(32 * NCTRL));
-      }
       if (warp == 0) {
         if constexpr (FEAT) {
           // features of the target at the new pose: terms of every queued neighbour
+          asm volatile("bar.sync 1, %0;" ::"n"(NE + 32));   // the energy warps' queues are complete
           int f[MLP_IN];
 #pragma unroll
           for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
@@ -624,9 +638,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             for (int k = 0; k < 3; ++k) un[s][k] = cur.un[s][k];
           const uint32_t fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
           const double cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-          const int n0 = s_nq[1][0], nn = n0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
+          const int nn = min(s_nq[1], MC_QMAX);
           for (int p = lane; p < nn; p += 32) {
-            const int j = p < n0 ? s_q[1][p] : s_q[1][QSEG + p - n0];
+            const int j = s_q[1][p];
             float e[3], r2;
             if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fn, fj, fs, e); }
             else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cn, cj, L, iL, e); }
@@ -645,20 +659,14 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
         }
         if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
-          double gk[6];
-#pragma unroll
-          for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb + 1];
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, gk, sig_t_fixed, sig_r_fixed, iL);
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL);
         }
       } else if constexpr (LEARN) {
         if (next_in_batch) {
           // warp 1: widths of the next trial's target at its current pose and its trial pose
           double st1, sr1;
           mlp_widths_warp(s_mlp, 1, a.fcache + (size_t)tg1 * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st1, sr1);
-          double gk[6];
-#pragma unroll
-          for (int k = 0; k < 6; ++k) gk[k] = s_g[k][tb + 1];
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, gk, st1, sr1, iL);
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL);
         }
       }
     }
@@ -687,7 +695,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             double qold[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
-            trial_rotation<double, NQ>(cur.rot, qold, a.body, qn, off64);
+            trial_rotation<double, NQ>(cur.rot, qold, a.body, qn, off64);   // lane 0 only
 #pragma unroll
             for (int s = 0; s <= NQ; ++s)
 #pragma unroll
@@ -741,42 +749,49 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             rr[2 * MLP_IN + 2] = (float)(dE * I2J * J2K * beta);
           }
         }
-        if (acc_flag) {
-          __syncwarp();
-          if (lane < MLP_IN) a.fcache[(size_t)tg * MLP_IN + lane] = s_feat[lane];
-          // neighbours of both poses: remove the old term, add the new one
-          const int o0 = s_nq[0][0], no = o0 + (NCTRL > 1 ? s_nq[0][NCTRL - 1] : 0);
-          const int m0 = s_nq[1][0], nn = m0 + (NCTRL > 1 ? s_nq[1][NCTRL - 1] : 0);
-          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-          const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-          const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
-          bool hit = false;
-          for (int p = lane; p < no + nn; p += 32) {
-            const bool old_pose = p < no;
-            const int po = old_pose ? p : p - no;
-            const int j = old_pose ? (po < o0 ? s_q[0][po] : s_q[0][QSEG + po - o0])
-                                   : (po < m0 ? s_q[1][po] : s_q[1][QSEG + po - m0]);
-            hit = hit || j == tg1;
-            float e[3], r2;
-            if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
-            else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
-            float o[(NQ + 1) * 3], u[4][3];
-            P::offsets(a, j, o);
-            site_dirs<NQ>(o, u);
-            int gq[MLP_IN];
-#pragma unroll
-            for (int k = 0; k < MLP_IN; ++k) gq[k] = 0;
-            feat_terms(e, r2, u, old_pose ? -1 : 1, gq);
-            int* fc = a.fcache + (size_t)j * MLP_IN;
-#pragma unroll
-            for (int k = 0; k < MLP_IN; ++k)
-              if (gq[k] != 0) atomicAdd(fc + k, gq[k]);
-          }
-          // learned widths of the next trial were taken from features this move changed
-          if (LEARN && __any_sync(0xffffffffu, hit) && lane == 0) s_pose[(t + 1) & 1].trial = -1;
-        }
+        if (lane == 0) s_accept = acc_flag;
       }
       __syncwarp();
+    }
+    if constexpr (FEAT) {
+      // ---- accepted move: feature cache of the molecule and of the neighbours of
+      //      both poses (old term removed, new term added), one entry per thread ----
+      __syncthreads();
+      if (s_accept) {
+        const int no = min(s_nq[0], MC_QMAX), ntot = no + min(s_nq[1], MC_QMAX);
+        const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+        const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+        const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
+        if (threadIdx.x == 0) s_hit = 0;
+        if ((int)threadIdx.x < MLP_IN) a.fcache[(size_t)tg * MLP_IN + threadIdx.x] = s_feat[threadIdx.x];
+        else if ((int)threadIdx.x < MLP_IN + 12) {
+          const int q = threadIdx.x - MLP_IN;
+          a.udir[(size_t)tg * 12 + q] = cur.un[q / 3][q % 3];
+        }
+        __syncthreads();
+        for (int p = threadIdx.x; p < ntot; p += blockDim.x) {
+          const bool old_pose = p < no;
+          const int j = old_pose ? s_q[0][p] : s_q[1][p - no];
+          if (j == tg1) s_hit = 1;
+          float e[3], r2;
+          if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
+          else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
+          float u[4][3];
+#pragma unroll
+          for (int q = 0; q < 12; ++q) u[q / 3][q % 3] = a.udir[(size_t)j * 12 + q];
+          int gq[MLP_IN];
+#pragma unroll
+          for (int k = 0; k < MLP_IN; ++k) gq[k] = 0;
+          feat_terms(e, r2, u, old_pose ? -1 : 1, gq);
+          int* fc = a.fcache + (size_t)j * MLP_IN;
+#pragma unroll
+          for (int k = 0; k < MLP_IN; ++k)
+            if (gq[k] != 0) atomicAdd(fc + k, gq[k]);
+        }
+        __syncthreads();
+        // learned widths of the next trial were taken from features this move changed
+        if (LEARN && threadIdx.x == 0 && s_hit) s_pose[(t + 1) & 1].trial = -1;
+      }
     }
     if (a.sample_every > 0 && (t + 1) % a.sample_every == 0) ++nsample;
   }

@@ -63,6 +63,7 @@ struct McArgs {
   float* records;         // optional: per chain per trial training record (MLP_REC floats)
   int* fcache;            // features of every molecule at its current pose (MLP_IN integers each)
   int* flag;              // set to 1 when a pose has more than MC_QMAX feature neighbours
+  float* udir;            // unit directions of every molecule's charged sites (12 floats each)
   unsigned long long seed, counter;
   MlpDev mlp;
 };

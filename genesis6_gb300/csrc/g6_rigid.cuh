@@ -644,6 +644,7 @@ __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float 
       s_nslots = nslots;
     }
   }
+  // publish the partials, then count the block in for each of its replicas
   __threadfence();
   __syncthreads();
   if ((int)threadIdx.x < s_nslots) {
