@@ -208,6 +208,7 @@ struct g6_ctx {
   int nblk = 0;
   double* d_part = nullptr; unsigned int* d_gmax = nullptr; double* d_red = nullptr; int* d_repcnt = nullptr;
   double* d_rfac = nullptr;   // per replica temperature and pressure factors
+  double* d_fixs = nullptr;   // per replica and axis 2^32 / L
   unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
   ThermoDev* d_th = nullptr; double* d_scale = nullptr; double* d_beta = nullptr; int* d_acc = nullptr;
   double* d_epot_rep = nullptr;
@@ -602,7 +603,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
   CK(dalloc(ctx, &ctx->d_gmax, 2)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
   CK(dalloc(ctx, &ctx->d_repcnt, nrep));
-  CK(dalloc(ctx, &ctx->d_rfac, 2 * (size_t)nrep));
+  CK(dalloc(ctx, &ctx->d_rfac, 2 * (size_t)nrep)); CK(dalloc(ctx, &ctx->d_fixs, 3 * (size_t)nrep));
   CK(dalloc(ctx, &ctx->d_done, 1)); CK(dalloc(ctx, &ctx->d_ctrl, 8));
   CK(dalloc(ctx, &ctx->d_th, nrep)); CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
   CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
@@ -916,9 +917,9 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   a.th = ctx->d_th; a.part = ctx->d_part; a.gmax = ctx->d_gmax; a.red = ctx->d_red; a.done = ctx->d_done;
   a.repcnt = ctx->d_repcnt;
   a.inv_dt2 = 1.0 / (dt * dt);
-  a.fdt = (float)dt; a.fcf = (float)(dt * dt * 0.5 / ctx->mh.mass);
+  a.fdt = (float)dt; a.fcf = (float)(dt * dt * 0.5 / ctx->mh.mass); a.fmass = (float)ctx->mh.mass;
   for (int k = 0; k < 3; ++k) a.fI[k] = (float)ctx->mh.I[k];
-  a.rfac = ctx->d_rfac;
+  a.rfac = ctx->d_rfac; a.fixs = ctx->d_fixs;
   a.ctrl = ctx->d_ctrl; a.log = log; a.seed = ctx->seed;
   return a;
 }
@@ -946,10 +947,10 @@ static const int GRAPH_STEPS = 16;
 // First predict + placement of a run.  Mixed runs first move the small Gear
 // terms into the float SoA; md_stop moves them back so that the FP64 state is
 // the complete record outside a run.
-static int md_start(g6_ctx* ctx) {
+static int md_start(g6_ctx* ctx, double dt) {
   if (ctx->prec == G6_MIXED) {
     CK(launch_stf_move(ctx->d_st, ctx->d_stf, ctx->n, 1, ctx->stream));
-    CK(launch_begin_mixed(place_args(ctx), ctx->d_stf, ctx->d_th, ctx->stream));
+    CK(launch_begin_mixed(place_args(ctx), ctx->d_stf, ctx->d_th, dt, ctx->stream));
   } else {
     CK(launch_predict_place(place_args(ctx), 1, ctx->d_th, 1, ctx->stream));
   }
@@ -980,6 +981,9 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
       for (int k = 0; k < 5; ++k) t.z[k] = thermo[r].zeta[k];
       t.zsum = thermo[r].zetasum; t.rate = thermo[r].collision_rate;
       t.inv_q = t.q > 0.0 ? 1.0 / t.q : 0.0;
+      t.fext = (float)(t.z[0] * dt);
+      t.fkT = (float)(t.temp * RGAS * J2I);
+      t.frdt = (float)(t.rate * dt);
       if (t.kind == G6_NOSE && !(t.q > 0.0)) return fail(ctx, G6_ERR_ARG, "Nose q must be > 0");
       if (t.kind < G6_NVE || t.kind > G6_ANDERSEN) return fail(ctx, G6_ERR_ARG, "unknown thermostat");
     }
@@ -1005,11 +1009,13 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
       rf[2 * r] = I2J * 2.0 / (RGAS * dof);
       rf[2 * r + 1] = I2J / (3.0 * A2P * vol * NA * ANG2M * ANG2M * ANG2M);
     }
+    std::vector<double> fx(3 * (size_t)ctx->nrep);
+    for (int k = 0; k < 3 * ctx->nrep; ++k) fx[k] = (1.0 / ctx->L[k]) * 4294967296.0;
     CK(cudaMemcpyAsync(ctx->d_rfac, rf.data(), rf.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));   // rf is a local vector
+    CK(cudaMemcpyAsync(ctx->d_fixs, fx.data(), fx.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));   // rf, fx are local vectors
   }
   CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
-  (void)dt;
   if (thermo && thermo[0].seed != ctx->seed) {
     ctx->seed = thermo[0].seed;
     drop_graphs(ctx);
@@ -1083,7 +1089,7 @@ int g6_md_begin(g6_ctx* ctx, double dt, int max_steps, const g6_thermostat* ther
   rc = md_prepare(ctx, dt, max_steps, const_cast<g6_thermostat*>(thermo), want_log != 0, 0);
   if (rc) return rc;
   ctx->run_dt = dt; ctx->run_log = want_log != 0; ctx->run_max = max_steps; ctx->run_done = 0; ctx->in_run = true;
-  return md_start(ctx);
+  return md_start(ctx, dt);
 }
 
 int g6_md_advance(g6_ctx* ctx, int nsteps) {
@@ -1250,7 +1256,7 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   rc = md_prepare(ctx, dt, 1, thermo, log != nullptr, 0);
   if (rc) return rc;
   StepArgs sa = step_args(ctx, dt, log ? ctx->d_log : nullptr);
-  if ((rc = md_start(ctx))) return rc;
+  if ((rc = md_start(ctx, dt))) return rc;
   rc = enqueue_step(ctx, sa);
   if (rc) return rc;
   if ((rc = md_stop(ctx))) return rc;

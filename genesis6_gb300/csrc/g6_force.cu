@@ -184,8 +184,8 @@ __device__ __forceinline__ double group_sum(double v) {
 // k_force: neighbour-list force kernel.
 // ---------------------------------------------------------------------------
 // Molecules per block of the fused step kernel: the block is MPB x LPI
-// threads (128, or 256 at 32 lanes) and warp 0 runs the integrator with one
-// molecule per lane.  Small blocks let several blocks share an SM, so one
+// threads (128, or 256 at 32 lanes) and one of its warps runs the integrator
+// with one molecule per lane.  Small blocks let several blocks share an SM, so one
 // block's integrator epilogue overlaps the site loops of the others; at least 8
 // molecules per epilogue warp keep the FP64 instruction count low.  The mixed
 // kernel is capped at 128 registers.
@@ -373,8 +373,11 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
     for (int k = 0; k < NRED; ++k) vv[k] = FF{0.0f, 0.0f};
     float dmax2 = 0.0f;
     int bad = 0, rr = -1;
-    if (threadIdx.x < MPB) {
-      const int m = threadIdx.x;
+    // the integrator warp rotates with the block so that the blocks resident on an
+    // SM spread their FP64 work over its four schedulers
+    const int ew = blockIdx.x % (StepShape<MIXED, LPI>::THREADS / 32);
+    if ((int)(threadIdx.x >> 5) == ew && (threadIdx.x & 31) < MPB) {
+      const int m = threadIdx.x & 31;
       const int im = blockIdx.x * MPB + m;
       if (im < n) {
         rr = a.rep.mol_rep[im];
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
         vv[4] = FF{0.5f * (float)smn[m], 0.0f};
       }
     }
-    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step);
+    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step, ew);
   } else {
     // fused FP64 step: FP64 lane combine, FP64 integrator in warp 0
     constexpr int MPB = StepShape<MIXED, LPI>::MPB;
@@ -412,8 +415,11 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
     for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
     double dmax2 = 0.0;
     int bad = 0, rr = -1;
-    if (threadIdx.x < MPB) {
-      const int m = threadIdx.x;
+    // the integrator warp rotates with the block so that the blocks resident on an
+    // SM spread their FP64 work over its four schedulers
+    const int ew = blockIdx.x % (StepShape<MIXED, LPI>::THREADS / 32);
+    if ((int)(threadIdx.x >> 5) == ew && (threadIdx.x & 31) < MPB) {
+      const int m = threadIdx.x & 31;
       const int im = blockIdx.x * MPB + m;
       if (im < n) {
         rr = a.rep.mol_rep[im];
@@ -422,7 +428,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
                     pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
       }
     }
-    step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step);
+    step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step, ew);
   }
 }
 

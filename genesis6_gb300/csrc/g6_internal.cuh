@@ -236,6 +236,8 @@ struct PairSetArgs {
 struct ThermoDev {
   int kind;
   double temp, q, dump, inv_q;
+  float fext;        // zeta0 * dt of the current step (mixed corrector)
+  float fkT, frdt;   // kT and collision probability per step (mixed corrector)
   double z[5];
   double zsum;
   double rate;
@@ -261,8 +263,9 @@ struct StepArgs {
   uint32_t* fix1;
   double mass, I[3], dt;
   double inv_dt2;      // 1 / dt^2
-  float fdt, fcf, fI[3];   // dt, dt^2 / (2 mass), inertia as float (mixed corrector)
+  float fdt, fcf, fmass, fI[3];   // dt, dt^2 / (2 mass), mass, inertia as float (mixed corrector)
   const double* rfac;  // per replica: I2J*2/(RGAS*dof) (temperature), I2J/(3*A2P*V*NA*ANG2M^3) (pressure)
+  const double* fixs;  // per replica and axis: 2^32 / L (fixed-point COM scale)
   const double* com_build;
   const uint32_t* fix_build;
   float* stf;          // mixed precision: float SoA of the small Gear terms (STF_*)
@@ -315,7 +318,7 @@ cudaError_t launch_pairset_count(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
 cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s);
-cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, cudaStream_t s);
+cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, double dt, cudaStream_t s);
 cudaError_t launch_step(const ForceArgs& f, const StepArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);

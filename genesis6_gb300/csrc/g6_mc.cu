@@ -371,6 +371,7 @@ struct TrialPose {
   double rot[3], dx[3];             // FP64 rotation vector and translation
   double st, sr;                    // widths of the proposal (at the old pose)
   R qn[4];                          // trial quaternion
+  float qi[4];                      // qinfrotator(rot) - (1,0,0,0), components accurate in float
   uint32_t fn[3], fo[3];            // new / old fixed-point COM
   float un[4][3];                   // charged-site directions at the new pose
   float d2, r2;                     // |dx|^2, |rot|^2
@@ -407,6 +408,14 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
   for (int k = 0; k < 3; ++k) rot[k] = __shfl_sync(0xffffffffu, rr, k);
   R qn[4], off[NQ + 1][3];
   trial_rotation<R, NQ>(rot, qold, a.body, qn, off);
+  if (MIXED && lane == 0) {
+    // increment of the normalised (1, rot) over the identity, with 1/sqrt(1+s) - 1
+    // written without cancellation: -s / (sqrt(1+s) (1 + sqrt(1+s)))
+    const float r0 = (float)rot[0], r1 = (float)rot[1], r2 = (float)rot[2];
+    const float s2 = r0 * r0 + r1 * r1 + r2 * r2, rs = sqrtf(1.0f + s2), inv = 1.0f / rs;
+    P.qi[0] = -s2 / (rs * (1.0f + rs));
+    P.qi[1] = r0 * inv; P.qi[2] = r1 * inv; P.qi[3] = r2 * inv;
+  }
   if (lane < 3) {
     const double il = lane == 0 ? iL[0] : (lane == 1 ? iL[1] : iL[2]);
     const double cn = cv + dk;
@@ -690,16 +699,32 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         if (ok) {
           double qn[4];
           double* p = a.pk64 + (size_t)tg * W64;
-          if (MIXED) {   // FP64 orientation and offsets from the FP64 draws
-            double off64[NQ + 1][3];
-            double qold[4];
+          if (MIXED) {
+            // FP64 orientation: the trial's rotation applied to the FP64 quaternion as
+            // a float increment (qadd of QuatModule.F90:108-133 minus the old value),
+            // the sign with a >= 0, then |q| = 1 restored.  Every FP64 or conversion
+            // instruction costs a warp 64 cycles, so only these few are FP64.  The FP64
+            // site offsets of the packed pose are not kept during a run: the Monte
+            // Carlo kernel reads only the COM of pk64, and every other caller places
+            // the molecules again from the state.
+            double qo[4];
+            float of[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) qold[k] = a.st[(size_t)(33 + k) * n + tg];
-            trial_rotation<double, NQ>(cur.rot, qold, a.body, qn, off64);   // lane 0 only
+            for (int k = 0; k < 4; ++k) { qo[k] = a.st[(size_t)(33 + k) * n + tg]; of[k] = (float)qo[k]; }
+            const float m0 = cur.qi[0], b1 = cur.qi[1], c1 = cur.qi[2], d1 = cur.qi[3];
+            const float dq[4] = {m0 * of[0] - b1 * of[1] - c1 * of[2] - d1 * of[3],
+                                 m0 * of[1] + b1 * of[0] + c1 * of[3] - d1 * of[2],
+                                 m0 * of[2] + c1 * of[0] - b1 * of[3] + d1 * of[1],
+                                 m0 * of[3] + d1 * of[0] + b1 * of[2] - c1 * of[1]};
 #pragma unroll
-            for (int s = 0; s <= NQ; ++s)
+            for (int k = 0; k < 4; ++k) qn[k] = qo[k] + (double)dq[k];
+            if (of[0] + dq[0] < 0.0f)
 #pragma unroll
-              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = off64[s][k];
+              for (int k = 0; k < 4; ++k) qn[k] = __longlong_as_double(__double_as_longlong(qn[k]) ^ (long long)0x8000000000000000ULL);
+            const float ef = (float)((qn[0] * qn[0] + qn[1] * qn[1] + qn[2] * qn[2] + qn[3] * qn[3]) - 1.0);
+            const double cd = (double)(ef * (-0.5f + 0.375f * ef));
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qn[k] = qn[k] + qn[k] * cd;
           } else {
 #pragma unroll
             for (int k = 0; k < 4; ++k) qn[k] = (double)cur.qn[k];

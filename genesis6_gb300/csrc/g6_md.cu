@@ -57,7 +57,7 @@ __global__ void k_stf_move(double* st, float* stf, int n, int to_float) {
 }
 
 // First predict + placement of a mixed run (plus the first Nose_Predict).
-__global__ void k_begin_mixed(PlaceArgs a, float* stf, ThermoDev* th) {
+__global__ void k_begin_mixed(PlaceArgs a, float* stf, ThermoDev* th, double dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (blockIdx.x == 0) {
     for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
@@ -67,6 +67,7 @@ __global__ void k_begin_mixed(PlaceArgs a, float* stf, ThermoDev* th) {
         T.z[1] = T.z[1] + 2.0 * T.z[2] + 3.0 * T.z[3] + 4.0 * T.z[4];
         T.z[2] = T.z[2] + 3.0 * T.z[3] + 6.0 * T.z[4];
         T.z[3] = T.z[3] + 4.0 * T.z[4];
+        T.fext = (float)(T.z[0] * dt);
       }
     }
   }
@@ -84,9 +85,9 @@ cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStr
   return cudaGetLastError();
 }
 
-cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, cudaStream_t s) {
+cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, double dt, cudaStream_t s) {
   const int blocks = a.n > 0 ? (a.n + 127) / 128 : 1;
-  k_begin_mixed<<<blocks, 128, 0, s>>>(a, stf, th);
+  k_begin_mixed<<<blocks, 128, 0, s>>>(a, stf, th, dt);
   return cudaGetLastError();
 }
 

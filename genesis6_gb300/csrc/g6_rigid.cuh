@@ -360,8 +360,12 @@ __device__ __forceinline__ void predict_mixed(double* st, float* stf, int n, int
   for (int c = 0; c < 4; ++c) { q[c] *= re; G6_ST(33 + c) = q[c]; }
 }
 
-// rigid_correct (RigidModule.F90:1255-1487) with FP64 updates of com, d1, w1
-// and q only.  F: COM force, tl: lab torque (float); outputs the kinetic sums.
+// rigid_correct (RigidModule.F90:1255-1487) followed by the next step's
+// rigid_predict (:480-559), with FP64 only for com, d1, w1 and q.  Every FP64
+// or conversion instruction costs a warp 64 cycles on GB300, so the float
+// increments of the corrector and of the predictor are summed in float and
+// each FP64 quantity receives them in one FP64 addition.  F: COM force, tl: lab
+// torque (float); outputs the kinetic sums and the displacement test.
 template <int NQ>
 __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const float F[3], const float tl[3], int step,
                                               bool predict_next, const PoseBuf& next, float& ekt2, float& ekr2,
@@ -370,10 +374,19 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   double* st = a.p.st;
   float* stf = a.stf;
   const int r = a.p.rep.mol_rep[i];
-  const ThermoDev th = a.th[r];
+  const ThermoDev& th = a.th[r];
+  const int kind = th.kind;
   const float dt = a.fdt;
-  double qd[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
-  const float qf[4] = {(float)qd[0], (float)qd[1], (float)qd[2], (float)qd[3]};
+  double xd[3], d1d[3], w1d[3], qd[4];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { xd[c] = G6_ST(c); d1d[c] = G6_ST(3 + c); w1d[c] = G6_ST(18 + c); }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) qd[c] = G6_ST(33 + c);
+  float d1f[3], w1f[3], qf[4];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { d1f[c] = (float)d1d[c]; w1f[c] = (float)w1d[c]; }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) qf[c] = (float)qd[c];
   float t[9];
   setmatrix_f(qf, t);
   const float tau[3] = {t[0] * tl[0] + t[3] * tl[1] + t[6] * tl[2], t[1] * tl[0] + t[4] * tl[1] + t[7] * tl[2],
@@ -381,57 +394,49 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]) && isfinite(tau[0]) && isfinite(tau[1]) &&
         isfinite(tau[2])))
     bad = 1;
-  float ext_t = 0.0f, ext_r = 0.0f;
-  if (th.kind == G6_NOSE) {
-    ext_r = (float)(th.z[0] * a.dt);
-    ext_t = 0.5f * ext_r;
-  }
-  // COM: Gear-5
-  const float cf = a.fcf;
-  double d1d[3];
+  const float ext_r = kind == G6_NOSE ? th.fext : 0.0f, ext_t = 0.5f * ext_r;
+  // COM: Gear-5 corrector (float increments of x and d1)
+  float D[4][3], dx_c[3], dd1_c[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    d1d[c] = G6_ST(3 + c);
-    const float nf = F[c] * cf - (float)d1d[c] * ext_t;
+    const float nf = F[c] * a.fcf - d1f[c] * ext_t;
     const float delta = nf - G6_SF(STF_D2 + c);
-    G6_ST(c) = G6_ST(c) + (double)((float)G50 * delta);
-    d1d[c] = d1d[c] + (double)((float)G51 * delta);
-    G6_SF(STF_D2 + c) = nf;
-    G6_SF(STF_D2 + 3 + c) += (float)G53 * delta;
-    G6_SF(STF_D2 + 6 + c) += (float)G54 * delta;
-    G6_SF(STF_D2 + 9 + c) += (float)G55 * delta;
+    dx_c[c] = (float)G50 * delta;
+    dd1_c[c] = (float)G51 * delta;
+    D[0][c] = nf;
+    D[1][c] = G6_SF(STF_D2 + 3 + c) + (float)G53 * delta;
+    D[2][c] = G6_SF(STF_D2 + 6 + c) + (float)G54 * delta;
+    D[3][c] = G6_SF(STF_D2 + 9 + c) + (float)G55 * delta;
   }
   // quaternion value
-  double w1d[3] = {G6_ST(18), G6_ST(19), G6_ST(20)};
-  const float w1f[3] = {(float)w1d[0], (float)w1d[1], (float)w1d[2]};
-  float nw[4];
+  float nw[4], dq_c[4];
   qdot_f(w1f, qf, nw);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const float dw = nw[c] * dt * 0.5f - G6_SF(STF_Q2 + c);
-    qd[c] = qd[c] + (double)((float)G40 * dw);
-    G6_ST(33 + c) = qd[c];
-  }
+  for (int c = 0; c < 4; ++c) dq_c[c] = (float)G40 * (nw[c] * dt * 0.5f - G6_SF(STF_Q2 + c));
   // angular velocity: Gear-4 with Euler's equations
   const float Ix = a.fI[0], Iy = a.fI[1], Iz = a.fI[2];
-  float nf[3];
-  nf[0] = (tau[0] + (Iy - Iz) * w1f[1] * w1f[2]) * dt / Ix - w1f[0] * ext_r;
-  nf[1] = (tau[1] + (Iz - Ix) * w1f[2] * w1f[0]) * dt / Iy - w1f[1] * ext_r;
-  nf[2] = (tau[2] + (Ix - Iy) * w1f[0] * w1f[1]) * dt / Iz - w1f[2] * ext_r;
+  float nfw[3], Wk[4][3], dw1_c[3];
+  nfw[0] = (tau[0] + (Iy - Iz) * w1f[1] * w1f[2]) * dt / Ix - w1f[0] * ext_r;
+  nfw[1] = (tau[1] + (Iz - Ix) * w1f[2] * w1f[0]) * dt / Iy - w1f[1] * ext_r;
+  nfw[2] = (tau[2] + (Ix - Iy) * w1f[0] * w1f[1]) * dt / Iz - w1f[2] * ext_r;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float delta = nf[c] - G6_SF(STF_W2 + c);
-    w1d[c] = w1d[c] + (double)((float)G40 * delta);
-    G6_SF(STF_W2 + c) = nf[c];
-    G6_SF(STF_W2 + 3 + c) += (float)G42 * delta;
-    G6_SF(STF_W2 + 6 + c) += (float)G43 * delta;
-    G6_SF(STF_W2 + 9 + c) += (float)G44 * delta;
+    const float delta = nfw[c] - G6_SF(STF_W2 + c);
+    dw1_c[c] = (float)G40 * delta;
+    Wk[0][c] = nfw[c];
+    Wk[1][c] = G6_SF(STF_W2 + 3 + c) + (float)G42 * delta;
+    Wk[2][c] = G6_SF(STF_W2 + 6 + c) + (float)G43 * delta;
+    Wk[3][c] = G6_SF(STF_W2 + 9 + c) + (float)G44 * delta;
   }
-  if (th.kind == G6_ANDERSEN) {   // stochastic collisions (float draws)
+  // corrected d1, w1 in float (kinetic sums, quaternion stacks)
+  float d1c[3], w1c[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { d1c[c] = d1f[c] + dd1_c[c]; w1c[c] = w1f[c] + dw1_c[c]; }
+  if (kind == G6_ANDERSEN) {   // stochastic collisions (float draws)
     uint32_t ctr[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, 0u};
     philox4x32(ctr, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
-    if (uniform_f(ctr[0]) <= (float)(th.rate * a.dt)) {
-      const float kT = (float)(th.temp * RGAS * J2I);
+    if (uniform_f(ctr[0]) <= th.frdt) {
+      const float kT = th.fkT;
       float z[6];
       for (int p = 0; p < 3; ++p) {
         uint32_t g[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, (uint32_t)(p + 1)};
@@ -442,25 +447,24 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
         z[2 * p] = rr * sn;
         z[2 * p + 1] = rr * cs;
       }
-      const float sv = sqrtf(kT / (float)a.mass) * dt;
-      for (int c = 0; c < 3; ++c) d1d[c] = (double)(z[c] * sv);
-      w1d[0] = (double)(z[3] * sqrtf(kT / Ix));
-      w1d[1] = (double)(z[4] * sqrtf(kT / Iy));
-      w1d[2] = (double)(z[5] * sqrtf(kT / Iz));
+      const float sv = sqrtf(kT / a.fmass) * dt;
+      for (int c = 0; c < 3; ++c) { d1c[c] = z[c] * sv; d1d[c] = 0.0; dd1_c[c] = d1c[c]; }
+      w1c[0] = z[3] * sqrtf(kT / Ix);
+      w1c[1] = z[4] * sqrtf(kT / Iy);
+      w1c[2] = z[5] * sqrtf(kT / Iz);
+      for (int c = 0; c < 3; ++c) { w1d[c] = 0.0; dw1_c[c] = w1c[c]; }
     }
   }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) { G6_ST(3 + c) = d1d[c]; G6_ST(18 + c) = w1d[c]; }
   // quaternion stacks from the corrected angular-velocity stack
   float W[5][3], Q[5][4], tq[4], uq[4], vq[4], xq[4];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    W[0][c] = (float)w1d[c];
+    W[0][c] = w1c[c];
 #pragma unroll
-    for (int k = 1; k < 5; ++k) W[k][c] = G6_SF(STF_W2 + 3 * (k - 1) + c);
+    for (int k = 1; k < 5; ++k) W[k][c] = Wk[k - 1][c];
   }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) Q[0][c] = (float)qd[c];
+  for (int c = 0; c < 4; ++c) Q[0][c] = qf[c] + dq_c[c];
   qdot_f(W[0], Q[0], tq);
 #pragma unroll
   for (int c = 0; c < 4; ++c) Q[1][c] = tq[c] * dt * 0.5f;
@@ -473,28 +477,93 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   qdot_f(W[3], Q[0], tq); qdot_f(W[2], Q[1], uq); qdot_f(W[1], Q[2], vq); qdot_f(W[0], Q[3], xq);
 #pragma unroll
   for (int c = 0; c < 4; ++c) Q[4][c] = (tq[c] + uq[c] + vq[c] + xq[c]) * dt * (1.0f / 8.0f);
-#pragma unroll
-  for (int k = 1; k < 5; ++k)
-#pragma unroll
-    for (int c = 0; c < 4; ++c) G6_SF(STF_Q2 + 4 * (k - 1) + c) = Q[k][c];
   // kinetic sums (Rigid_Ek)
-  const float d1f[3] = {(float)d1d[0], (float)d1d[1], (float)d1d[2]};
-  ekt2 = d1f[0] * d1f[0] + d1f[1] * d1f[1] + d1f[2] * d1f[2];
+  ekt2 = d1c[0] * d1c[0] + d1c[1] * d1c[1] + d1c[2] * d1c[2];
   ekr2 = Ix * (W[0][0] * W[0][0]) + Iy * (W[0][1] * W[0][1]) + Iz * (W[0][2] * W[0][2]);
-  if (predict_next) {
-    double x[3], q[4];
-    predict_mixed(st, stf, n, i, x, q);
-    place_mixed<NQ>(a.p, i, x, q, next.pk64, next.pk32, next.fix);
-    const float* fs = a.p.rep.fscale + 3 * r;
-    float dd = 0.0f;
+  if (!predict_next) {   // last step of a run: the corrected state
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float e = (float)(int)(next.fix[(size_t)c * n + i] - a.fix_build[(size_t)c * n + i]) * fs[c];
-      dd += e * e;
+      G6_ST(c) = xd[c] + (double)dx_c[c];
+      G6_ST(3 + c) = d1d[c] + (double)dd1_c[c];
+      G6_ST(18 + c) = w1d[c] + (double)dw1_c[c];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { G6_SF(STF_D2 + 3 * k + c) = D[k][c]; G6_SF(STF_W2 + 3 * k + c) = W[k + 1][c]; }
     }
-    dmax2 = dd;
-    if (!isfinite(dd) || !isfinite(x[0]) || !isfinite(x[1]) || !isfinite(x[2])) { bad = 1; dmax2 = 3.0e38f; }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      G6_ST(33 + c) = qd[c] + (double)dq_c[c];
+#pragma unroll
+      for (int k = 1; k < 5; ++k) G6_SF(STF_Q2 + 4 * (k - 1) + c) = Q[k][c];
+    }
+    return;
   }
+  // the next step's prediction, added to the corrected state in one FP64 add each
+  double x[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float dsum = D[0][c] + D[1][c] + D[2][c] + D[3][c];
+    x[c] = (xd[c] + d1d[c]) + (double)(dx_c[c] + dd1_c[c] + dsum);
+    G6_ST(c) = x[c];
+    G6_ST(3 + c) = d1d[c] + (double)(dd1_c[c] + 2.0f * D[0][c] + 3.0f * D[1][c] + 4.0f * D[2][c] + 5.0f * D[3][c]);
+    G6_SF(STF_D2 + c) = D[0][c] + 3.0f * D[1][c] + 6.0f * D[2][c] + 10.0f * D[3][c];
+    G6_SF(STF_D2 + 3 + c) = D[1][c] + 4.0f * D[2][c] + 10.0f * D[3][c];
+    G6_SF(STF_D2 + 6 + c) = D[2][c] + 5.0f * D[3][c];
+    G6_SF(STF_D2 + 9 + c) = D[3][c];
+    G6_ST(18 + c) = w1d[c] + (double)(dw1_c[c] + W[1][c] + W[2][c] + W[3][c] + W[4][c]);
+    G6_SF(STF_W2 + c) = W[1][c] + 2.0f * W[2][c] + 3.0f * W[3][c] + 4.0f * W[4][c];
+    G6_SF(STF_W2 + 3 + c) = W[2][c] + 3.0f * W[3][c] + 6.0f * W[4][c];
+    G6_SF(STF_W2 + 6 + c) = W[3][c] + 4.0f * W[4][c];
+    G6_SF(STF_W2 + 9 + c) = W[4][c];
+  }
+  double q[4];
+  float qp[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float qsum = dq_c[c] + Q[1][c] + Q[2][c] + Q[3][c] + Q[4][c];
+    q[c] = qd[c] + (double)qsum;
+    qp[c] = qf[c] + qsum;
+    G6_SF(STF_Q2 + c) = Q[1][c] + 2.0f * Q[2][c] + 3.0f * Q[3][c] + 4.0f * Q[4][c];
+    G6_SF(STF_Q2 + 4 + c) = Q[2][c];
+    G6_SF(STF_Q2 + 8 + c) = Q[3][c];
+    G6_SF(STF_Q2 + 12 + c) = Q[4][c];
+  }
+  // 1/|q| = 1 - e/2 + 3e^2/8 for |q|^2 = 1 + e (|e| ~ 1e-6): the small factor in float
+  const double e2 = (q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) - 1.0;
+  const float ef = (float)e2;
+  const float cfac = ef * (-0.5f + 0.375f * ef);
+  const double cd = (double)cfac;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) { q[c] = q[c] + q[c] * cd; G6_ST(33 + c) = q[c]; qp[c] = qp[c] + qp[c] * cfac; }
+  // placement of the predicted pose: fixed-point COM, FP64 COM, float offsets
+  constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
+  float tp[9];
+  setmatrix_f(qp, tp);
+  float w[24];
+#pragma unroll
+  for (int k = 0; k < 24; ++k) w[k] = 0.0f;
+  const float* fs = a.p.rep.fscale + 3 * r;
+  float dd = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const uint32_t fw = (uint32_t)(unsigned long long)__double2ll_rn(x[c] * a.fixs[3 * r + c]);
+    next.fix[(size_t)c * n + i] = fw;
+    w[c] = __uint_as_float(fw);
+    next.pk64[(size_t)i * a.p.w64 + c] = x[c];
+    const float e = (float)(int)(fw - a.fix_build[(size_t)c * n + i]) * fs[c];
+    dd += e * e;
+  }
+#pragma unroll
+  for (int s = 0; s <= NQ; ++s) {
+    const float bx = a.p.fbody[s][0], by = a.p.fbody[s][1], bz = a.p.fbody[s][2];
+    w[3 + 3 * s] = tp[0] * bx + tp[1] * by + tp[2] * bz;
+    w[4 + 3 * s] = tp[3] * bx + tp[4] * by + tp[5] * bz;
+    w[5 + 3 * s] = tp[6] * bx + tp[7] * by + tp[8] * bz;
+  }
+#pragma unroll
+  for (int q4 = 0; q4 < NPK; ++q4)
+    next.pk32[(size_t)i * NPK + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+  dmax2 = dd;
+  if (!isfinite(dd)) { bad = 1; dmax2 = 3.0e38f; }
 }
 
 #undef G6_SF
@@ -598,23 +667,25 @@ __device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int st
       th.z[1] = th.z[1] + 2.0 * th.z[2] + 3.0 * th.z[3] + 4.0 * th.z[4];
       th.z[2] = th.z[2] + 3.0 * th.z[3] + 6.0 * th.z[4];
       th.z[3] = th.z[3] + 4.0 * th.z[4];
+      th.fext = (float)(th.z[0] * dt);
     }
   }
   __syncthreads();
 }
 
-// Block partials of the step (warp 0 holds one molecule per lane): per replica
+// Block partials of the step (warp ew holds one molecule per lane): per replica
 // slot, sums over the lanes (FP64 in the plain path, float pairs with error-free
 // addition in the mixed path); the largest displacement goes to an atomic max
 // word.  The last block of each replica to arrive finishes that replica
 // (finish_replica); the last block overall advances the step counter.
 template <class V>
-__device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step) {
+__device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step,
+                            int ew) {
   const int n = a.p.n;
   __shared__ int s_rfirst, s_nslots;
   __shared__ int s_last[MAXREP_PER_BLOCK];
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
+  if ((int)(threadIdx.x >> 5) == ew) {
+    const int lane = threadIdx.x & 31;
     const int first_i = blockIdx.x * mpb;
     const int last_i = min(n, first_i + mpb) - 1;
     const int rfirst = a.p.rep.mol_rep[first_i];
