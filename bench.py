@@ -56,6 +56,10 @@ def parse():
     p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
+    p.add_argument("--profile", choices=["md", "mc"], default=None,
+                   help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
+                        "TIP4P-4096 (mixed, Nose 300 K, one g6_md_run), 'mc' = two runs of --steps trials on "
+                        "32 chains x 1,024 ST2 (fixed widths)")
     return p.parse_args()
 
 
@@ -347,46 +351,56 @@ def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
             "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed"}
 
 
-def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=3000, w_energy=0.0):
-    """32 chains x 1,024 ST2 (custom path, Coulomb taper), 260 K, rc = L/2 with a
-    2 A switch.  Chains are equilibrated from the lattice with the fixed widths,
-    then the MLP is trained on `records` plain-sampler moves and both samplers
-    run `sweeps` sweeps from the same equilibrated state: fixed widths (0.15 A,
-    0.15 rad) vs the learned widths.  ESS of U per GPU-second (U sampled every
-    sweep of 1,024 trials) and <U> of both."""
+def mc_chains(C=32, N=1024, T=260.0, rc=9.0, seed=20261203, melt_steps=5000, md_steps=30000):
+    """32 chains x 1,024 ST2 at 1.0 g/cm^3: seeded lattices melted by MD at 400 K,
+    then MD at T (stochastic-collision thermostat, rc 9 A with a 2 A switch, dt
+    2 fs), all chains in one replica context.  Returns boxes and records."""
     import genesis6_gb300 as g6
-    from genesis6_gb300 import _capi, config
-    C, N = 32, 1024
-    NF, NREC = _capi.MLP_NFEAT, _capi.MLP_RECORD
+    from genesis6_gb300 import config
     boxes, recs = [], []
     for c in range(C):
-        b = config.water_box("ST2", N, seed + 500 + c, temp=260.0)
+        b = config.water_box("ST2", N, seed + 500 + c, temp=400.0)
         boxes.append(b["L"]); recs.append(b["rec"])
-    L = boxes[0][0]
-    s = g6.RigidWater("ST2", [N] * C, np.array(boxes), path="custom", precision="mixed", rc=0.5 * L, skin=0.0)
+    s = g6.RigidWater("ST2", [N] * C, np.array(boxes), path="custom", precision="mixed", rc=rc, switch=2.0, skin=1.0)
     s.upload_state(np.concatenate(recs))
-    beta = np.full(C, 1.0 / 260.0)
-    st = np.full(C, 0.15); sr = np.full(C, 0.15)
-    counts = np.zeros(2 * C, np.int64)
-    energy = np.zeros(C)
+    s.md_run(DT, melt_steps, s.thermostats(C, "andersen", temp=400.0, rate=5.0, seed=seed), log=False)
+    log = s.md_run(DT, md_steps, s.thermostats(C, "andersen", temp=T, rate=5.0, seed=seed + 1))
+    rec = s.download_state()
+    s.close()
+    q = max(md_steps // 4, 1)
+    return np.array(boxes), rec, {"md_U_last_quarters": [float(log[k * q:(k + 1) * q, :, 0].mean()) for k in range(4)],
+                                  "md_T_last_quarter": float(log[3 * q:, :, 3].mean())}
 
-    def run(ntrial, mode, counter, sample_every=0):
-        nsm = ntrial // sample_every if sample_every else 0
-        samples = np.zeros((C, max(nsm, 1)))
-        s._check(s.L.g6_mc_run(s.ctx, ntrial, seed, counter, _capi.dptr(beta), _capi.dptr(st), _capi.dptr(sr),
-                               mode, sample_every, _capi.dptr(samples) if nsm else None,
-                               counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _capi.dptr(energy), None))
-        return samples, counts.reshape(C, 2).copy()
+
+def bench_mc(torch, seed=20261203, sweeps=1000, records=1_000_000, equil_sweeps=1000, w_move=1.0, w_energy=0.0,
+             T=260.0, rc=9.0, md_steps=30000):
+    """32 chains x 1,024 ST2 (custom path, Coulomb taper), T = 260 K, rc 9 A with
+    a 2 A switch.  Chains start from MD-equilibrated liquid (melt at 400 K, then
+    MD at T), are equilibrated further by the fixed-width sampler, then the MLP
+    is trained on `records` plain-sampler moves and both samplers run `sweeps`
+    sweeps from the same state: fixed widths (0.15 A, 0.15 rad) vs the learned
+    widths.  ESS of U per GPU-second (U sampled every sweep of 1,024 trials),
+    <U> of both, and the running energies against a full recomputation."""
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import _capi
+    C, N = 32, 1024
+    NF, NREC = _capi.MLP_NFEAT, _capi.MLP_RECORD
     t0 = time.perf_counter()
-    eq, _ = run(equil_sweeps * N, _capi.MC_PLAIN, 0, sample_every=N)      # equilibration from the lattice
+    boxes, rec0, md = mc_chains(C, N, T, rc, seed, md_steps=md_steps)
+    t_md = time.perf_counter() - t0
+    s = g6.RigidWater("ST2", [N] * C, boxes, path="custom", precision="mixed", rc=rc, switch=2.0, skin=0.0)
+    s.upload_state(rec0)
+    beta = 1.0 / T
+    t0 = time.perf_counter()
+    eq = s.mc_run(equil_sweeps * N, seed, 0, beta, 0.15, 0.15, sample_every=N)["samples"]
     torch.cuda.synchronize()
     t_equil = time.perf_counter() - t0
     rec_state = s.download_state()
     ntr = records // C
     t0 = time.perf_counter()
-    run(ntr, _capi.MC_COLLECT, 10 ** 8)                                   # training records
+    s.mc_run(ntr, seed, 10 ** 8, beta, 0.15, 0.15, mode="collect")       # training records
     loss = np.zeros(8)
-    s._check(s.L.g6_mlp_objective(s.ctx, 1.0, w_energy))
+    s._check(s.L.g6_mlp_objective(s.ctx, w_move, w_energy))
     s._check(s.L.g6_mlp_train(s.ctx, 8, 1024, 2e-3, seed, 0.15, 0.15, _capi.dptr(loss)))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
@@ -399,28 +413,35 @@ def bench_mc(torch, seed=20261203, sweeps=400, records=1_000_000, equil_sweeps=3
     wt = np.zeros(nrec); wr = np.zeros(nrec)
     s._check(s.L.g6_mlp_widths(s.ctx, _capi.fptr(feat), nrec, _capi.dptr(wt), _capi.dptr(wr)))
     out = {}
-    for name, mode in (("fixed", _capi.MC_PLAIN), ("learned", _capi.MC_LEARNED)):
+    for name in ("plain", "learned"):
         s.upload_state(rec_state)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        samples, cnt = run(sweeps * N, mode, 3 * 10 ** 8, sample_every=N)
+        r = s.mc_run(sweeps * N, seed, 3 * 10 ** 8, beta, 0.15, 0.15, mode=name, sample_every=N)
         torch.cuda.synchronize()
         gpu_s = time.perf_counter() - t0
+        samples = r["samples"]
+        F, tau, ep, vir = s.force()
         ess = np.array([ess_geyer(samples[c]) for c in range(C)])
         u = samples.mean(1)
         var_mean = np.array([np.var(samples[c]) / max(ess[c], 1.0) for c in range(C)])
-        out[name] = {"ess_total": float(ess.sum()), "gpu_seconds": gpu_s, "ess_per_gpu_s": float(ess.sum() / gpu_s),
-                     "us_per_trial": gpu_s / (sweeps * N) * 1e6,
-                     "mean_U_internal": float(u.mean()), "stderr_U": float(np.sqrt(var_mean.sum()) / C),
-                     "acceptance": float(cnt[:, 0].sum() / cnt[:, 1].sum()), "sweeps": sweeps}
+        half = samples.shape[1] // 2
+        out["fixed" if name == "plain" else name] = {
+            "ess_total": float(ess.sum()), "gpu_seconds": gpu_s, "ess_per_gpu_s": float(ess.sum() / gpu_s),
+            "us_per_trial": gpu_s / (sweeps * N) * 1e6,
+            "mean_U_internal": float(u.mean()), "stderr_U": float(np.sqrt(var_mean.sum()) / C),
+            "mean_U_first_second_half": [float(samples[:, :half].mean()), float(samples[:, half:].mean())],
+            "acceptance": float(r["accepted"].sum() / r["trials"].sum()), "sweeps": sweeps,
+            "running_minus_full_energy_rel": float(np.abs(r["energy"] - ep).max() / np.abs(ep).max())}
     s.close()
     d = abs(out["learned"]["mean_U_internal"] - out["fixed"]["mean_U_internal"])
     sig = np.hypot(out["learned"]["stderr_U"], out["fixed"]["stderr_U"])
-    drift = float(eq[:, -100:].mean() - eq[:, -200:-100].mean()) / C if eq.shape[1] >= 200 else None
-    return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": 260.0,
-            "rc_A": 0.5 * L, "equilibration_sweeps": equil_sweeps, "equilibration_seconds": t_equil,
-            "U_drift_last_100_sweeps_per_chain": drift,
-            "training_records": ntr * C, "objective": {"w_move": 1.0, "w_energy": w_energy},
+    q = max(equil_sweeps // 4, 1)
+    return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": T,
+            "rc_A": rc, "start": "lattice, MD melt 5,000 steps at 400 K, MD %d steps at %g K (%.1f s)" % (md_steps, T, t_md),
+            "md": md, "equilibration_sweeps": equil_sweeps, "equilibration_seconds": t_equil,
+            "equilibration_U_quarters": [float(eq[:, k * q:(k + 1) * q].mean()) for k in range(4)],
+            "training_records": ntr * C, "objective": {"w_move": w_move, "w_energy": w_energy},
             "training_loss_first_last": [float(loss[0]), float(loss[-1])],
             "collect_and_train_seconds": t_train,
             "learned_widths_on_records": {"sigma_t_mean": float(wt.mean()), "sigma_t_p10_p90": [float(np.percentile(wt, 10)), float(np.percentile(wt, 90))],
@@ -616,9 +637,36 @@ def run_gpu(args, rank, world, local):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    """Workloads for ncu captures: nothing is timed and no JSON line is printed."""
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import config
+    if args.profile == "md":
+        b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
+        s = make_system("TIP4P", N_MAIN, "mixed", b["L"], b["rec"])
+        log = s.md_run(DT, args.steps, thermo_for(s))
+        print("md ok: %d steps, last T %.1f K" % (args.steps, float(log[-1, 0, 3])))
+    else:
+        C, N, seed = 32, 1024, 20261203
+        boxes, recs = [], []
+        for c in range(C):
+            b = config.water_box("ST2", N, seed + 500 + c, temp=260.0)
+            boxes.append(b["L"]); recs.append(b["rec"])
+        s = g6.RigidWater("ST2", [N] * C, np.array(boxes), path="custom", precision="mixed", rc=9.0, switch=2.0,
+                          skin=0.0)
+        s.upload_state(np.concatenate(recs))
+        for rep in range(2):
+            r = s.mc_run(args.steps, seed, rep * args.steps, 1.0 / 260.0)
+        print("mc ok: acceptance %.3f" % (r["accepted"].sum() / r["trials"].sum()))
+    s.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

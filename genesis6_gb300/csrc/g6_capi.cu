@@ -1368,12 +1368,13 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   a.n = ctx->n; a.ntrial = ntrial; a.nsamples = nsamples; a.sample_every = samples ? sample_every : 0;
   a.rep = rep_dev(ctx);
   for (int q = 0; q < MAXSITE; ++q)
-    for (int k = 0; k < 3; ++k) a.body[q][k] = ctx->mh.body[q][k];
+    for (int k = 0; k < 3; ++k) { a.body[q][k] = ctx->mh.body[q][k]; a.fbody[q][k] = (float)ctx->mh.body[q][k]; }
   a.st = ctx->d_st; a.pk64 = ctx->d_pk64; a.pk32f = (float*)ctx->d_pk32; a.fix = ctx->d_fix;
   a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
   a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
   a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
   a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
+  for (int r = 0; r < R; ++r) a.ncmax = std::max(a.ncmax, ctx->off[r + 1] - ctx->off[r]);
   a.mlp = mlp_dev(ctx);
   CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
   if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode, ctx->stream));

@@ -42,10 +42,11 @@ struct MT {
 template <class R>
 __device__ __forceinline__ void switch_fn(R dd, R rin2, R rin, R rout, R c1, R c2, R& hh, R& dh) {
   if (dd > rin2) {
-    R r = sqrt(dd);
+    R r, ir;
+    root_r(dd, r, ir);
     R u = r - rout, l = r - rin, uu = u * u, ll = l * l;
     hh = c1 * uu * u * (R(10) * ll - R(5) * u * l + uu);
-    dh = -c2 * uu * ll / r;
+    dh = div_r(-c2 * uu * ll, r, ir);
   } else {
     hh = R(1);
     dh = R(0);
@@ -57,17 +58,15 @@ __device__ __forceinline__ void taper_fn(R d12, R rl, R ru, R w3, R& s12, R& ds1
     if (d12 < rl * rl) {
       s12 = R(0); ds12 = R(0);
     } else {
-      R r12 = sqrt(d12);
+      R r12, ir12;
+      root_r(d12, r12, ir12);
       s12 = (r12 - rl) * (r12 - rl) * (R(3) * ru - rl - R(2) * r12) / w3;
-      ds12 = -(R(6) * (r12 - rl) * (ru - r12) / w3) / r12;
+      ds12 = div_r(-(R(6) * (r12 - rl) * (ru - r12) / w3), r12, ir12);
     }
   } else {
     s12 = R(1); ds12 = R(0);
   }
 }
-
-__device__ __forceinline__ float rsqrt_r(float x) { return rsqrtf(x); }
-__device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
 
 template <class R> struct Prm;
 template <> struct Prm<double> {
@@ -110,7 +109,7 @@ __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::N
   R v[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) v[k] = d[k] + ri[0][k] - rj[0][k];
-  R inv = R(1) / (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  R inv = rcp_r(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
   R d6 = inv * inv * inv, d12 = d6 * d6;
   const R aa = Prm<R>::aa(pc), bb = Prm<R>::bb(pc);
   R elj = aa * d12 + bb * d6;

@@ -81,6 +81,31 @@ __device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a,
 // Fortran dnint: round half away from zero.
 __device__ __forceinline__ double xdnint(double x) { return round(x); }
 
+// ---------------------------------------------------------------------------
+// Reciprocal, reciprocal square root and square root in either precision.  The
+// FP32 (mixed) site loops use the single hardware instructions (PTX
+// rcp/rsqrt.approx.ftz: about one ulp, no subnormal handling; squared site
+// separations are far from the subnormal range); the FP64 mode keeps IEEE
+// division and sqrt.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float rsqrt_r(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ double rsqrt_r(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rcp_r(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ double rcp_r(double x) { return 1.0 / x; }
+// r from r^2, and y / r
+__device__ __forceinline__ void root_r(float x, float& r, float& ir) { ir = rsqrt_r(x); r = x * ir; }
+__device__ __forceinline__ void root_r(double x, double& r, double& ir) { r = sqrt(x); ir = 0.0; }
+__device__ __forceinline__ float div_r(float y, float, float ir) { return y * ir; }
+__device__ __forceinline__ double div_r(double y, double r, double) { return y / r; }
+
 // Minimum-image COM separation exactly as Interaction_Compress2
 // (InteractionModule.F90:454-465): o = dnint(delta*invL)*L, d = delta - o,
 // dd = (dx^2 + dy^2) + dz^2.

@@ -5,10 +5,12 @@
 //   warp 0   reads the trial's draws (target, Gaussian rotation vector and
 //            translation: the sine branch of Random_Normal, RandomModule.F90:20-28)
 //            from a shared-memory batch that all threads fill in parallel once
-//            per 256 trials, scales them by the widths, and builds the new
+//            per MC_NB trials, scales them by the widths, and builds the new
 //            quaternion with qinfrotator + qadd (QuatModule.F90:108-133, 203-223)
-//            and the new site offsets (rigid_setsiteposition);
-//   all      sum e(new, j) - e(old, j) over every other molecule j of the chain
+//            and the new site offsets (rigid_setsiteposition) -- normally one
+//            trial ahead, while the previous trial's energies are summed, and
+//            again here only when the previous acceptance made that pose stale;
+//   others   sum e(new, j) - e(old, j) over every other molecule j of the chain
 //            with the PairPotential arithmetic (strict rc test, COM switch, ST2
 //            Coulomb taper on the custom path), one molecule j per thread;
 //   warp 0   Metropolis test (mc2.F90:712-722) as log(u) < -dE*I2J*J2K*beta
@@ -55,7 +57,8 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
                                          const PairConst& pc, R rin2, R rin, R rout, R c1) {
   R hh;
   if (dd > rin2) {
-    R r = sqrt(dd);
+    R r, ir;
+    root_r(dd, r, ir);
     R u = r - rout, l = r - rin, uu = u * u, ll = l * l;
     hh = c1 * uu * u * (R(10) * ll - R(5) * u * l + uu);
   } else {
@@ -64,7 +67,7 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
   R v[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) v[k] = d[k] + ri[0][k] - rj[0][k];
-  const R inv = R(1) / (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  const R inv = rcp_r(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
   const R d6 = inv * inv * inv;
   const R aa = sizeof(R) == 8 ? (R)pc.aa : (R)pc.faa, bb = sizeof(R) == 8 ? (R)pc.bb : (R)pc.fbb;
   const R elj = aa * d6 * d6 + bb * d6;
@@ -75,7 +78,7 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
     for (int b = 1; b <= NQ; ++b) {
       R x = d[0] + ri[a][0] - rj[b][0], y = d[1] + ri[a][1] - rj[b][1], z = d[2] + ri[a][2] - rj[b][2];
       const R q = sizeof(R) == 8 ? (R)pc.qq[a - 1][b - 1] : (R)pc.fqq[a - 1][b - 1];
-      ec += q * (sizeof(R) == 8 ? (R)rsqrt((double)(x * x + y * y + z * z)) : (R)rsqrtf((float)(x * x + y * y + z * z)));
+      ec += q * rsqrt_r(x * x + y * y + z * z);
     }
   R scc = hh;
   if (TAPER) {
@@ -85,7 +88,8 @@ __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 
     if (dd < ru * ru) {
       if (dd < rl * rl) s12 = R(0);
       else {
-        R r12 = sqrt(dd);
+        R r12, ir12;
+        root_r(dd, r12, ir12);
         s12 = (r12 - rl) * (r12 - rl) * (R(3) * ru - rl - R(2) * r12) / w3;
       }
     } else {
@@ -111,11 +115,14 @@ __device__ __forceinline__ void qadd(R q1[4], const R q2[4]) {
 
 // qinfrotator (QuatModule.F90:203-223) composed with the old orientation, the
 // rotation matrix of rigid_setmatrix and the lab offsets of sites 0..NQ.
-template <class R, int NQ>
-__device__ __forceinline__ void trial_rotation(const R rot[3], const R* qold, const double (&body)[MAXSITE][3],
+template <class R, int NQ, class B>
+__device__ __forceinline__ void trial_rotation(const R rot[3], const R* qold, const B (&body)[MAXSITE][3],
                                                R qn[4], R (&off)[NQ + 1][3]) {
   R qr[4] = {R(1), rot[0], rot[1], rot[2]};
-  const R rn = R(1) / sqrt(qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3]);
+  const R nn = qr[0] * qr[0] + qr[1] * qr[1] + qr[2] * qr[2] + qr[3] * qr[3];
+  R rn;
+  if constexpr (sizeof(R) == 4) rn = rsqrtf(nn);   // FP32 trial poses: the hardware reciprocal square root
+  else rn = R(1) / sqrt(nn);
 #pragma unroll
   for (int k = 0; k < 4; ++k) qr[k] *= rn;
   R qo[4] = {qold[0], qold[1], qold[2], qold[3]};
@@ -148,9 +155,10 @@ __device__ __forceinline__ float dot3_rn(const float a[3], const float b[3]) {
 __device__ __forceinline__ float gauss_rn(float t) { return exp2f(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)); }
 __device__ __forceinline__ int feat_q(float x) { return __float2int_rn(__fmul_rn(x, FEAT_Q)); }
 
-// Unit direction of one site offset v.
+// Unit direction of one site offset v.  rsqrtf is a fixed function of its
+// argument, so every call site gets the same bits for the same v.
 __device__ __forceinline__ void site_dir1(const float v[3], float u[3]) {
-  const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot3_rn(v, v)));
+  const float inv = rsqrtf(dot3_rn(v, v));
 #pragma unroll
   for (int k = 0; k < 3; ++k) u[k] = __fmul_rn(v[k], inv);
 }
@@ -169,21 +177,80 @@ __device__ __forceinline__ void site_dirs(const float* o, float (&u)[4][3]) {
   }
 }
 
+// The single terms of one neighbour at distance r (1/r = ir) along e.  Every
+// call site builds a term from these helpers, so a pair gives the same integer
+// whichever molecule of the pair is being updated.
+__device__ __forceinline__ void feat_r(float r2, float& r, float& ir) {
+  ir = rsqrtf(r2);
+  r = __fmul_rn(r2, ir);
+}
+template <int K>
+__device__ __forceinline__ int feat_radial(float r) {
+  return feat_q(gauss_rn(__fmul_rn(__fsub_rn(r, 2.4f + 0.25f * K), 4.0f)));
+}
+__device__ __forceinline__ float feat_g1(float r) { return gauss_rn(__fmul_rn(__fsub_rn(r, 2.9f), 1.0f / 0.35f)); }
+__device__ __forceinline__ float feat_g2(float r) { return gauss_rn(__fmul_rn(__fsub_rn(r, 4.5f), 2.0f)); }
+__device__ __forceinline__ float feat_c4(const float u[3], const float e[3], float ir) {
+  const float c = fmaxf(__fmul_rn(dot3_rn(u, e), ir), 0.0f);
+  const float c2 = __fmul_rn(c, c);
+  return __fmul_rn(c2, c2);
+}
+template <int K0, int NK>
+__device__ __forceinline__ void feat_radials(float r, int sign, int (&f)[MLP_IN]) {
+  if constexpr (NK > 0) {
+    f[K0] += sign * feat_radial<K0>(r);
+    feat_radials<K0 + 1, NK - 1>(r, sign, f);
+  }
+}
+
 // Integer feature terms of one neighbour at e (molecule -> neighbour, |e|^2 = r2).
 __device__ __forceinline__ void feat_terms(const float e[3], float r2, const float (&u)[4][3], int sign,
                                            int (&f)[MLP_IN]) {
-  const float r = __fsqrt_rn(r2), ir = __fdiv_rn(1.0f, r);
-#pragma unroll
-  for (int k = 0; k < 16; ++k) f[k] += sign * feat_q(gauss_rn(__fmul_rn(__fsub_rn(r, 2.4f + 0.25f * k), 4.0f)));
-  const float g1 = gauss_rn(__fmul_rn(__fsub_rn(r, 2.9f), 1.0f / 0.35f));
-  const float g2 = gauss_rn(__fmul_rn(__fsub_rn(r, 4.5f), 2.0f));
+  float r, ir;
+  feat_r(r2, r, ir);
+  feat_radials<0, 16>(r, sign, f);
+  const float g1 = feat_g1(r), g2 = feat_g2(r);
 #pragma unroll
   for (int s = 0; s < 4; ++s) {
-    float c = __fmul_rn(dot3_rn(u[s], e), ir);
-    c = fmaxf(c, 0.0f);
-    const float c2 = __fmul_rn(c, c), c4 = __fmul_rn(c2, c2);
+    const float c4 = feat_c4(u[s], e, ir);
     f[16 + s] += sign * feat_q(__fmul_rn(g1, c4));
     f[20 + s] += sign * feat_q(__fmul_rn(g2, c4));
+  }
+}
+
+// A quarter of the terms of one neighbour added into fc (shared or global):
+// part 0 and 1 the radial shells 0-7 and 8-15, part 2 and 3 the direction terms
+// of charged sites 0-1 and 2-3 (u = the molecule's 12 site-direction floats).
+__device__ __forceinline__ void feat_add_part(int part, const float e[3], float r2, const float* u, int sign,
+                                              int* fc) {
+  float r, ir;
+  feat_r(r2, r, ir);
+  int f[MLP_IN];
+  if (part == 0) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) f[k] = 0;
+    feat_radials<0, 8>(r, sign, f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (f[k] != 0) atomicAdd(fc + k, f[k]);
+  } else if (part == 1) {
+#pragma unroll
+    for (int k = 8; k < 16; ++k) f[k] = 0;
+    feat_radials<8, 8>(r, sign, f);
+#pragma unroll
+    for (int k = 8; k < 16; ++k)
+      if (f[k] != 0) atomicAdd(fc + k, f[k]);
+  } else {
+    const float g1 = feat_g1(r), g2 = feat_g2(r);
+    const int s0 = 2 * (part - 2);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float us[3] = {u[3 * (s0 + q)], u[3 * (s0 + q) + 1], u[3 * (s0 + q) + 2]};
+      const float c4 = feat_c4(us, e, ir);
+      const int a1 = sign * feat_q(__fmul_rn(g1, c4)), a2 = sign * feat_q(__fmul_rn(g2, c4));
+      if (a1 != 0) atomicAdd(fc + 16 + s0 + q, a1);
+      if (a2 != 0) atomicAdd(fc + 20 + s0 + q, a2);
+    }
   }
 }
 
@@ -225,7 +292,7 @@ struct PoseRead {
 // Features of every molecule of the chain at its current pose (integer cache).
 template <int NQ, bool MIXED>
 __device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3], const double L[3],
-                              const double iL[3]) {
+                              const double iL[3], int* fcl) {
   using P = PoseRead<NQ, MIXED>;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     float o[(NQ + 1) * 3], u[4][3];
@@ -249,7 +316,7 @@ __device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3]
       if (r2 < FEAT_RC2 && r2 > 0.0f) feat_terms(e, r2, u, 1, f);
     }
 #pragma unroll
-    for (int k = 0; k < MLP_IN; ++k) a.fcache[(size_t)i * MLP_IN + k] = f[k];
+    for (int k = 0; k < MLP_IN; ++k) fcl[(size_t)(i - i0) * MLP_IN + k] = f[k];
   }
 }
 
@@ -265,6 +332,8 @@ struct MlpShared {
   float mean[MLP_IN], istd[MLP_IN];
   float x[2][MLP_IN];   // per-warp scratch (warps 0 and 1 evaluate the network concurrently)
   float h[2][MLP_H];
+  float s0t, s0r;       // reference widths sigma0
+  double s0t_d, s0r_d;
 };
 
 __device__ void mlp_load(MlpShared& m, const MlpDev& d) {
@@ -284,12 +353,13 @@ __device__ void mlp_load(MlpShared& m, const MlpDev& d) {
   }
   if (threadIdx.x < MLP_OUT) m.b3[threadIdx.x] = d.w[MLP_B3 + threadIdx.x];
   if (threadIdx.x < MLP_IN) { m.mean[threadIdx.x] = d.feat_mean[threadIdx.x]; m.istd[threadIdx.x] = d.feat_inv_std[threadIdx.x]; }
+  if (threadIdx.x == 0) { m.s0t = (float)d.sigma0_t; m.s0r = (float)d.sigma0_r; m.s0t_d = d.sigma0_t; m.s0r_d = d.sigma0_r; }
 }
 
 // Widths from integer features feat[] (one whole warp; lane 0's result is the
-// one used).  w selects the warp's scratch rows.
-__device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, double s0t, double s0r,
-                                                double& st, double& sr) {
+// one used).  w selects the warp's scratch rows.  R: the pose precision.
+template <class R>
+__device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, R& st, R& sr) {
   const int lane = threadIdx.x & 31;
   float* xs = m.x[w];
   float* hs = m.h[w];
@@ -334,8 +404,13 @@ __device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* 
     z[q] = __shfl_sync(0xffffffffu, s, 0) + m.b3[q];
   }
   __syncwarp();
-  st = s0t * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[0]));
-  sr = s0r * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[1]));
+  if constexpr (sizeof(R) == 4) {
+    st = m.s0t * ((float)MLP_SMIN + (float)MLP_SSPAN * mlp_sigmoid(z[0]));
+    sr = m.s0r * ((float)MLP_SMIN + (float)MLP_SSPAN * mlp_sigmoid(z[1]));
+  } else {
+    st = m.s0t_d * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[0]));
+    sr = m.s0r_d * (MLP_SMIN + MLP_SSPAN * (double)mlp_sigmoid(z[1]));
+  }
 }
 
 // log of the proposal density of a move (up to a constant): isotropic
@@ -368,29 +443,33 @@ template <class R, int NQ>
 struct TrialPose {
   R on[NQ + 1][3], oo[NQ + 1][3];   // new / old site offsets
   double cn[3], co[3];              // new / old FP64 COM
-  double rot[3], dx[3];             // FP64 rotation vector and translation
-  double st, sr;                    // widths of the proposal (at the old pose)
-  R qn[4];                          // trial quaternion
-  float qi[4];                      // qinfrotator(rot) - (1,0,0,0), components accurate in float
+  R rot[3], dx[3];                  // rotation vector and translation
+  float stf, srf;                   // widths of the proposal (at the old pose), FP32
+  R qn[4];                          // trial quaternion (the pose's precision)
+  double qo64[4];                   // FP64 quaternion before the move
+  double q64[4];                    // FP64 quaternion after the move (FP64 mode; mixed: made on acceptance)
   uint32_t fn[3], fo[3];            // new / old fixed-point COM
   float un[4][3];                   // charged-site directions at the new pose
   float d2, r2;                     // |dx|^2, |rot|^2
   int trial;                        // trial number the pose belongs to (-1: none)
 };
 
-// Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot]).
-// The arithmetic of every quantity is the serial formula of mc2; FP64 work is
-// done by the lanes that own it (component k on lane k), since the FP64 pipe's
-// cost grows with the active lanes.
+// Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot],
+// widths st_w, sr_w).  Register arrays are indexed with constants only
+// (selects), never by lane.  Mixed precision builds the pose in FP32 with no
+// FP64 arithmetic but the trial COM (the FP64 quaternion is made on
+// acceptance); the FP64 mode follows mc2's serial formulas in FP64, component
+// k on lane k, since an FP64 warp instruction costs the same whatever the
+// number of active lanes.
 template <class R, int NQ, bool MIXED>
-__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const double (*g)[MC_NB],
-                            int slot, double st_w, double sr_w, const double iL[3]) {
+__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const R (*g)[MC_NB], int slot,
+                            R st_w, R sr_w, const double iL[3], const float fsi[3]) {
   using Pr = PoseRead<NQ, MIXED>;
   const int lane = threadIdx.x & 31;
   const int n = a.n;
-  double qv = 0.0, cv = 0.0, rk = 0.0, dk = 0.0;
+  double qv = 0.0, cv = 0.0;
+  R rk = R(0), dk = R(0), ov = R(0);
   uint32_t fv = 0u;
-  R ov = R(0);
   if (lane < 4) qv = a.st[(size_t)(33 + lane) * n + tg];
   if (lane < 3) {
     cv = a.st[(size_t)lane * n + tg];
@@ -400,66 +479,104 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
   }
   if (lane < 3 * (NQ + 1))
     ov = MIXED ? (R)a.pk32f[(size_t)tg * 4 * Pr::NPK + 3 + lane] : (R)a.pk64[(size_t)tg * Pr::W64 + 3 + lane];
-  const R qr = (R)qv, rr = (R)rk;   // conversions on the owning lanes only
+  const R qr = (R)qv;   // the conversion on the owning lanes only
   R qold[4], rot[3];
 #pragma unroll
   for (int k = 0; k < 4; ++k) qold[k] = __shfl_sync(0xffffffffu, qr, k);
 #pragma unroll
-  for (int k = 0; k < 3; ++k) rot[k] = __shfl_sync(0xffffffffu, rr, k);
+  for (int k = 0; k < 3; ++k) rot[k] = __shfl_sync(0xffffffffu, rk, k);
   R qn[4], off[NQ + 1][3];
-  trial_rotation<R, NQ>(rot, qold, a.body, qn, off);
-  if (MIXED && lane == 0) {
-    // increment of the normalised (1, rot) over the identity, with 1/sqrt(1+s) - 1
-    // written without cancellation: -s / (sqrt(1+s) (1 + sqrt(1+s)))
-    const float r0 = (float)rot[0], r1 = (float)rot[1], r2 = (float)rot[2];
-    const float s2 = r0 * r0 + r1 * r1 + r2 * r2, rs = sqrtf(1.0f + s2), inv = 1.0f / rs;
-    P.qi[0] = -s2 / (rs * (1.0f + rs));
-    P.qi[1] = r0 * inv; P.qi[2] = r1 * inv; P.qi[3] = r2 * inv;
+  if constexpr (MIXED) trial_rotation<R, NQ>(rot, qold, a.fbody, qn, off);
+  else trial_rotation<R, NQ>(rot, qold, a.body, qn, off);
+  if (lane < 4) {
+    P.qo64[lane] = qv;
+    if (!MIXED) P.q64[lane] = (double)(lane == 0 ? qn[0] : (lane == 1 ? qn[1] : (lane == 2 ? qn[2] : qn[3])));
   }
   if (lane < 3) {
-    const double il = lane == 0 ? iL[0] : (lane == 1 ? iL[1] : iL[2]);
-    const double cn = cv + dk;
+    const double cn = cv + (double)dk;
     P.co[lane] = cv;
     P.cn[lane] = cn;
     P.fo[lane] = fv;
-    P.fn[lane] = to_fixed(cn, il);
+    if (MIXED) {
+      // the fixed-point trial COM: old word + rounded translation, so that the
+      // reverse move (-dk) returns to the same word
+      const float s = lane == 0 ? fsi[0] : (lane == 1 ? fsi[1] : fsi[2]);
+      P.fn[lane] = fv + (uint32_t)__float2int_rn((float)dk * s);
+    } else {
+      const double il = lane == 0 ? iL[0] : (lane == 1 ? iL[1] : iL[2]);
+      P.fn[lane] = to_fixed(cn, il);
+    }
     P.rot[lane] = rk;
     P.dx[lane] = dk;
   }
-  const double d2k = dk * dk, r2k = rk * rk;   // nonzero on lanes 0-2 only
-  const double d2a = __shfl_sync(0xffffffffu, d2k, 0), d2b = __shfl_sync(0xffffffffu, d2k, 1),
-               d2c = __shfl_sync(0xffffffffu, d2k, 2);
-  const double r2a = __shfl_sync(0xffffffffu, r2k, 0), r2b = __shfl_sync(0xffffffffu, r2k, 1),
-               r2c = __shfl_sync(0xffffffffu, r2k, 2);
-  // register arrays are indexed with constants only (selects), never by lane
+  R d2 = dk * dk, r2 = rk * rk;   // nonzero on lanes 0-2 only
+  d2 += __shfl_xor_sync(0xffffffffu, d2, 1);
+  r2 += __shfl_xor_sync(0xffffffffu, r2, 1);
+  d2 += __shfl_sync(0xffffffffu, d2, 2);
+  r2 += __shfl_sync(0xffffffffu, r2, 2);
+  // old and new offsets: value 3s+k on lane 3s+k
+  R onv = R(0);
 #pragma unroll
   for (int s = 0; s <= NQ; ++s)
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      if (lane == 3 * s + k) { P.oo[s][k] = ov; P.on[s][k] = off[s][k]; }
+      if (lane == 3 * s + k) onv = off[s][k];
+  if (lane < 3 * (NQ + 1)) {
+    (&P.oo[0][0])[lane] = ov;
+    (&P.on[0][0])[lane] = onv;
+  }
+  if (lane < 4) P.qn[lane] = lane == 0 ? qn[0] : (lane == 1 ? qn[1] : (lane == 2 ? qn[2] : qn[3]));
+  // unit direction of charged site s at the new pose on lane 16 + 3s .. 16 + 3s + 2
+  {
+    const int s = (lane - 16) / 3;
+    float v[3] = {1.0f, 0.0f, 0.0f};
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (lane == k) P.qn[k] = qn[k];
-  // unit directions of the charged sites at the new pose, one site per lane
-#pragma unroll
-  for (int s = 0; s < 4; ++s)
-    if (lane == 8 + s) {
-      float u[3] = {0.0f, 0.0f, 0.0f};
-      if (s < NQ) {
-        const float v[3] = {(float)off[s + 1][0], (float)off[s + 1][1], (float)off[s + 1][2]};
-        site_dir1(v, u);
-      }
-#pragma unroll
-      for (int k = 0; k < 3; ++k) P.un[s][k] = u[k];
+    for (int q = 0; q < NQ; ++q)
+      if (s == q) { v[0] = (float)off[q + 1][0]; v[1] = (float)off[q + 1][1]; v[2] = (float)off[q + 1][2]; }
+    float u[3];
+    site_dir1(v, u);
+    if (lane >= 16 && lane < 28) {
+      const int k = (lane - 16) - 3 * s;
+      (&P.un[0][0])[lane - 16] = s < NQ ? (k == 0 ? u[0] : (k == 1 ? u[1] : u[2])) : 0.0f;
     }
+  }
   if (lane == 0) {
-    P.d2 = (float)(d2a + d2b + d2c);
-    P.r2 = (float)(r2a + r2b + r2c);
-    P.st = st_w;
-    P.sr = sr_w;
+    P.d2 = (float)d2;
+    P.r2 = (float)r2;
+    P.stf = (float)st_w;
+    P.srf = (float)sr_w;
     P.trial = trial;
   }
   __syncwarp();
+}
+
+// FP64 quaternion of an accepted mixed-precision trial, component `lane` on
+// lanes 0-3 (all lanes call): qadd of QuatModule.F90:108-133 applied to the
+// FP64 quaternion as a float increment (qinfrotator(rot) - identity) (x) q_old,
+// with 1/sqrt(1+s) - 1 written without cancellation as
+// -s / (sqrt(1+s) (1 + sqrt(1+s))); then the sign with a >= 0 and |q| = 1
+// restored by the factor 1 - e/2 + 3e^2/8.
+template <class TP>
+__device__ __forceinline__ double accepted_q64(const TP& P, int lane) {
+  const double qv = lane < 4 ? P.qo64[lane & 3] : 0.0;
+  const float qf = (float)qv;
+  const float of0 = __shfl_sync(0xffffffffu, qf, 0), of1 = __shfl_sync(0xffffffffu, qf, 1);
+  const float of2 = __shfl_sync(0xffffffffu, qf, 2), of3 = __shfl_sync(0xffffffffu, qf, 3);
+  const float r0 = (float)P.rot[0], r1 = (float)P.rot[1], r2 = (float)P.rot[2];
+  const float s2 = r0 * r0 + r1 * r1 + r2 * r2, rs = sqrtf(1.0f + s2), inv = 1.0f / rs;
+  const float m0 = -s2 / (rs * (1.0f + rs)), b1 = r0 * inv, c1 = r1 * inv, d1 = r2 * inv;
+  const float dq0 = m0 * of0 - b1 * of1 - c1 * of2 - d1 * of3;
+  const float dq1 = m0 * of1 + b1 * of0 + c1 * of3 - d1 * of2;
+  const float dq2 = m0 * of2 + c1 * of0 - b1 * of3 + d1 * of1;
+  const float dq3 = m0 * of3 + d1 * of0 + b1 * of2 - c1 * of1;
+  const float dq = lane == 0 ? dq0 : (lane == 1 ? dq1 : (lane == 2 ? dq2 : dq3));
+  double q64 = qv + (double)dq;
+  if (of0 + dq0 < 0.0f) q64 = -q64;
+  double sq = lane < 4 ? q64 * q64 : 0.0;
+  sq += __shfl_xor_sync(0xffffffffu, sq, 1);
+  sq += __shfl_xor_sync(0xffffffffu, sq, 2);
+  const float ef = (float)(sq - 1.0);
+  return q64 + q64 * (double)(ef * (-0.5f + 0.375f * ef));
 }
 
 template <int NQ, bool TAPER, bool MIXED, int MODE>
@@ -471,11 +588,11 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   constexpr bool LEARN = MODE == G6_MC_LEARNED;
   // control warps build the next trial's pose (and, with features, find the
   // feature neighbours and run the network) while the others sum energies
-  constexpr int NCTRL = LEARN ? 2 : (FEAT ? 1 : 0);
+  constexpr int NCTRL = LEARN ? 2 : 1;
   constexpr int E0 = 32 * NCTRL, NE = MC_NT - E0, NEW = NE / 32;
   constexpr int W64 = P::W64, NPK = P::NPK;
-  __shared__ double s_lu[MC_NB];
-  __shared__ double s_g[6][MC_NB];
+  __shared__ typename std::conditional<MIXED, float, double>::type s_lu[MC_NB];   // log of the test uniform
+  __shared__ R s_g[6][MC_NB];   // unit normals of the rotation (0-2) and translation (3-5)
   __shared__ int s_tg[MC_NB];
   __shared__ TP s_pose[2];
   __shared__ int s_feat[MLP_IN];
@@ -483,7 +600,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
   __shared__ int s_nq[2];
   __shared__ int s_accept, s_hit;
-  __shared__ double s_sig_new[2];
+  __shared__ float s_sig_new[2];   // learned widths at the trial pose
   __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
 
   const int c = blockIdx.x;
@@ -495,11 +612,16 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   for (int k = 0; k < 3; ++k) { L[k] = a.rep.L[3 * c + k]; iL[k] = a.rep.invL[3 * c + k]; }
   const float fs[3] = {a.rep.fscale[3 * c], a.rep.fscale[3 * c + 1], a.rep.fscale[3 * c + 2]};
   const double beta = a.beta[c];
+  const float fbeta_e = (float)(I2J * J2K * beta);   // mixed test: x = -dE * fbeta_e + log Hastings
   // fixed widths enter as sqrt(sigma^2), the variance form of mc2's Random_Normal call
-  const double sig_t_fixed = sqrt(a.sigma_t[c] * a.sigma_t[c]);
-  const double sig_r_fixed = sqrt(a.sigma_r[c] * a.sigma_r[c]);
+  const R sig_t_fixed = (R)sqrt(a.sigma_t[c] * a.sigma_t[c]);
+  const R sig_r_fixed = (R)sqrt(a.sigma_r[c] * a.sigma_r[c]);
+  const float fsi[3] = {(float)(4294967296.0 * iL[0]), (float)(4294967296.0 * iL[1]), (float)(4294967296.0 * iL[2])};
   if constexpr (LEARN) mlp_load(s_mlp, a.mlp);
-  if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL);
+  // the chain's feature cache: shared memory when it fits, else its rows of a.fcache
+  extern __shared__ int s_fcdyn[];
+  int* const fcl = a.fc_smem ? s_fcdyn : a.fcache + (size_t)i0 * MLP_IN;
+  if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
   if (threadIdx.x == 0) { s_pose[0].trial = -1; s_pose[1].trial = -1; }
   __syncthreads();
 
@@ -522,11 +644,11 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         int tg = (int)(u[0] * nc);
         if (tg >= nc) tg = nc - 1;   // u = 1 would select nc (mc2.F90:551 quirk)
         s_tg[threadIdx.x] = tg;
-        s_lu[threadIdx.x] = log(u[1]);
+        s_lu[threadIdx.x] = (R)log(u[1]);
 #pragma unroll 1
         for (int k = 0; k < 6; ++k) {
           uniform2(a.seed, (uint32_t)c, lo, hi, 1u + k, u);
-          s_g[k][threadIdx.x] = sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]);
+          s_g[k][threadIdx.x] = (R)(sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]));
         }
       }
       __syncthreads();
@@ -536,10 +658,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
     if (FEAT && threadIdx.x == 0) { s_nq[0] = 0; s_nq[1] = 0; }
     // ---- warp 0: the trial pose, unless it was built during the previous trial ----
     if (warp == 0 && cur.trial != t) {
-      double st_w = sig_t_fixed, sr_w = sig_r_fixed;
-      if constexpr (LEARN)
-        mlp_widths_warp(s_mlp, 0, a.fcache + (size_t)tg * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st_w, sr_w);
-      build_trial<R, NQ, MIXED>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL);
+      R st_w = sig_t_fixed, sr_w = sig_r_fixed;
+      if constexpr (LEARN) mlp_widths_warp<R>(s_mlp, 0, fcl + (size_t)(tg - i0) * MLP_IN, st_w, sr_w);
+      build_trial<R, NQ, MIXED>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL, fsi);
     }
     __syncthreads();
     if ((int)threadIdx.x >= E0) {
@@ -662,20 +783,20 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
           __syncwarp();
           if constexpr (LEARN) {
-            double st2, sr2;
-            mlp_widths_warp(s_mlp, 0, s_feat, a.mlp.sigma0_t, a.mlp.sigma0_r, st2, sr2);
-            if (lane == 0) { s_sig_new[0] = st2; s_sig_new[1] = sr2; }
+            R st2, sr2;
+            mlp_widths_warp<R>(s_mlp, 0, s_feat, st2, sr2);
+            if (lane == 0) { s_sig_new[0] = (float)st2; s_sig_new[1] = (float)sr2; }
           }
         }
         if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL);
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL, fsi);
         }
       } else if constexpr (LEARN) {
         if (next_in_batch) {
           // warp 1: widths of the next trial's target at its current pose and its trial pose
-          double st1, sr1;
-          mlp_widths_warp(s_mlp, 1, a.fcache + (size_t)tg1 * MLP_IN, a.mlp.sigma0_t, a.mlp.sigma0_r, st1, sr1);
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL);
+          R st1, sr1;
+          mlp_widths_warp<R>(s_mlp, 1, fcl + (size_t)(tg1 - i0) * MLP_IN, st1, sr1);
+          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL, fsi);
         }
       }
     }
@@ -685,93 +806,77 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       R v = lane < NEW ? s_part[lane] : R(0);
 #pragma unroll
       for (int m = 16; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
-      const double dE = (double)__shfl_sync(0xffffffffu, v, 0);
+      const R dEr = __shfl_sync(0xffffffffu, v, 0);
       int acc_flag = 0;
       if (lane == 0) {
         float logh = 0.0f;
         if (LEARN)
-          logh = log_q((float)s_sig_new[0], (float)s_sig_new[1], cur.d2, cur.r2) -
-                 log_q((float)cur.st, (float)cur.sr, cur.d2, cur.r2);
-        const double x = -(dE * I2J * J2K) * beta + (double)logh;
-        const bool ok = x >= 0.0 || s_lu[tb] < x;
+          logh = log_q(s_sig_new[0], s_sig_new[1], cur.d2, cur.r2) - log_q(cur.stf, cur.srf, cur.d2, cur.r2);
+        // Metropolis-Hastings test in the precision of the energies
+        bool ok;
+        if (MIXED) {
+          const float x = fmaf(-(float)dEr, fbeta_e, logh);
+          ok = x >= 0.0f || (float)s_lu[tb] < x;
+        } else {
+          const double x = -((double)dEr * I2J * J2K) * beta + (double)logh;
+          ok = x >= 0.0 || (double)s_lu[tb] < x;
+        }
         acc_flag = ok ? 1 : 0;
-        if (a.trace) a.trace[((size_t)c * a.ntrial + t) * 4 + 0] = dE;
-        if (ok) {
-          double qn[4];
-          double* p = a.pk64 + (size_t)tg * W64;
-          if (MIXED) {
-            // FP64 orientation: the trial's rotation applied to the FP64 quaternion as
-            // a float increment (qadd of QuatModule.F90:108-133 minus the old value),
-            // the sign with a >= 0, then |q| = 1 restored.  Every FP64 or conversion
-            // instruction costs a warp 64 cycles, so only these few are FP64.  The FP64
-            // site offsets of the packed pose are not kept during a run: the Monte
-            // Carlo kernel reads only the COM of pk64, and every other caller places
-            // the molecules again from the state.
-            double qo[4];
-            float of[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) { qo[k] = a.st[(size_t)(33 + k) * n + tg]; of[k] = (float)qo[k]; }
-            const float m0 = cur.qi[0], b1 = cur.qi[1], c1 = cur.qi[2], d1 = cur.qi[3];
-            const float dq[4] = {m0 * of[0] - b1 * of[1] - c1 * of[2] - d1 * of[3],
-                                 m0 * of[1] + b1 * of[0] + c1 * of[3] - d1 * of[2],
-                                 m0 * of[2] + c1 * of[0] - b1 * of[3] + d1 * of[1],
-                                 m0 * of[3] + d1 * of[0] + b1 * of[2] - c1 * of[1]};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) qn[k] = qo[k] + (double)dq[k];
-            if (of[0] + dq[0] < 0.0f)
-#pragma unroll
-              for (int k = 0; k < 4; ++k) qn[k] = __longlong_as_double(__double_as_longlong(qn[k]) ^ (long long)0x8000000000000000ULL);
-            const float ef = (float)((qn[0] * qn[0] + qn[1] * qn[1] + qn[2] * qn[2] + qn[3] * qn[3]) - 1.0);
-            const double cd = (double)(ef * (-0.5f + 0.375f * ef));
-#pragma unroll
-            for (int k = 0; k < 4; ++k) qn[k] = qn[k] + qn[k] * cd;
-          } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) qn[k] = (double)cur.qn[k];
-#pragma unroll
-            for (int s = 0; s <= NQ; ++s)
-#pragma unroll
-              for (int k = 0; k < 3; ++k) p[3 + 3 * s + k] = (double)cur.on[s][k];
-          }
-#pragma unroll
-          for (int k = 0; k < 4; ++k) a.st[(size_t)(33 + k) * n + tg] = qn[k];
-          float* pf = a.pk32f + (size_t)tg * 4 * NPK;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            a.st[(size_t)k * n + tg] = cur.cn[k];
-            p[k] = cur.cn[k];
-            pf[k] = __uint_as_float(cur.fn[k]);
-            a.fix[(size_t)k * n + tg] = cur.fn[k];
-          }
-#pragma unroll
-          for (int s = 0; s <= NQ; ++s)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) pf[3 + 3 * s + k] = (float)cur.on[s][k];
+      }
+      acc_flag = __shfl_sync(0xffffffffu, acc_flag, 0);
+      const double dE = (double)dEr;
+      if (acc_flag) {
+        // the accepted pose, one component per lane.  In mixed precision the FP64
+        // site offsets of the packed pose are not kept during a run: the Monte
+        // Carlo kernel reads only the COM of pk64, and every other caller places
+        // the molecules again from the state.
+        double q64;
+        if constexpr (MIXED) q64 = accepted_q64(cur, lane);
+        else q64 = cur.q64[lane & 3];
+        double* p = a.pk64 + (size_t)tg * W64;
+        float* pf = a.pk32f + (size_t)tg * 4 * NPK;
+        if (lane < 4) a.st[(size_t)(33 + lane) * n + tg] = q64;
+        if (lane < 3) {
+          const double cn = cur.cn[lane];
+          const uint32_t fw = cur.fn[lane];
+          a.st[(size_t)lane * n + tg] = cn;
+          p[lane] = cn;
+          pf[lane] = __uint_as_float(fw);
+          a.fix[(size_t)lane * n + tg] = fw;
+        }
+        if (lane < 3 * (NQ + 1)) {
+          const R o = (&cur.on[0][0])[lane];
+          pf[3 + lane] = (float)o;
+          if (!MIXED) p[3 + lane] = (double)o;
+        }
+        if (lane == 0) {
           energy += dE;
           ++nacc;
           // the next trial's prepared pose is stale when it moves the same molecule
           if (s_pose[(t + 1) & 1].trial == t + 1 && t + 1 < a.ntrial && s_tg[(tb + 1) % MC_NB] + i0 == tg)
             s_pose[(t + 1) & 1].trial = -1;
         }
+      }
+      if (lane == 0) {
         if (a.trace) {
           double* tr = a.trace + ((size_t)c * a.ntrial + t) * 4;
-          tr[1] = energy; tr[2] = (double)acc_flag; tr[3] = (double)(tg - i0);
+          tr[0] = dE; tr[1] = energy; tr[2] = (double)acc_flag; tr[3] = (double)(tg - i0);
         }
         if (a.samples && a.sample_every > 0 && (t + 1) % a.sample_every == 0)
           a.samples[(size_t)c * a.nsamples + nsample] = energy;
       }
-      acc_flag = __shfl_sync(0xffffffffu, acc_flag, 0);
+      __syncwarp();
       if constexpr (FEAT) {
         if (MODE == G6_MC_COLLECT && a.records) {   // training record of this trial
           float* rr = a.records + ((size_t)c * a.ntrial + t) * MLP_REC;
           if (lane < MLP_IN) {
-            rr[lane] = (float)a.fcache[(size_t)tg * MLP_IN + lane] * FEAT_IQ;
+            rr[lane] = (float)fcl[(size_t)(tg - i0) * MLP_IN + lane] * FEAT_IQ;
             rr[MLP_IN + lane] = (float)s_feat[lane] * FEAT_IQ;
           }
           if (lane == 0) {
             rr[2 * MLP_IN] = cur.d2;
             rr[2 * MLP_IN + 1] = cur.r2;
-            rr[2 * MLP_IN + 2] = (float)(dE * I2J * J2K * beta);
+            rr[2 * MLP_IN + 2] = (float)((double)dEr * I2J * J2K * beta);
           }
         }
         if (lane == 0) s_accept = acc_flag;
@@ -788,30 +893,22 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
         const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
         if (threadIdx.x == 0) s_hit = 0;
-        if ((int)threadIdx.x < MLP_IN) a.fcache[(size_t)tg * MLP_IN + threadIdx.x] = s_feat[threadIdx.x];
+        if ((int)threadIdx.x < MLP_IN) fcl[(size_t)(tg - i0) * MLP_IN + threadIdx.x] = s_feat[threadIdx.x];
         else if ((int)threadIdx.x < MLP_IN + 12) {
           const int q = threadIdx.x - MLP_IN;
           a.udir[(size_t)tg * 12 + q] = cur.un[q / 3][q % 3];
         }
         __syncthreads();
-        for (int p = threadIdx.x; p < ntot; p += blockDim.x) {
-          const bool old_pose = p < no;
-          const int j = old_pose ? s_q[0][p] : s_q[1][p - no];
+        // four threads per neighbour entry, each adding a quarter of its terms
+        for (int p = threadIdx.x; p < 4 * ntot; p += blockDim.x) {
+          const int q = p >> 2, part = p & 3;
+          const bool old_pose = q < no;
+          const int j = old_pose ? s_q[0][q] : s_q[1][q - no];
           if (j == tg1) s_hit = 1;
           float e[3], r2;
           if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
           else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
-          float u[4][3];
-#pragma unroll
-          for (int q = 0; q < 12; ++q) u[q / 3][q % 3] = a.udir[(size_t)j * 12 + q];
-          int gq[MLP_IN];
-#pragma unroll
-          for (int k = 0; k < MLP_IN; ++k) gq[k] = 0;
-          feat_terms(e, r2, u, old_pose ? -1 : 1, gq);
-          int* fc = a.fcache + (size_t)j * MLP_IN;
-#pragma unroll
-          for (int k = 0; k < MLP_IN; ++k)
-            if (gq[k] != 0) atomicAdd(fc + k, gq[k]);
+          feat_add_part(part, e, r2, a.udir + (size_t)j * 12, old_pose ? -1 : 1, fcl + (size_t)(j - i0) * MLP_IN);
         }
         __syncthreads();
         // learned widths of the next trial were taken from features this move changed
@@ -827,13 +924,30 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   }
 }
 
+// Shared memory a CTA may give to its chain's feature cache (the rest of the
+// 227 KB stays with the L1 that holds the chain's packed poses).
+constexpr size_t MC_FC_SMEM_MAX = 100 * 1024;
+
+template <int NQ, bool TAPER, bool MIXED, int MODE>
+static cudaError_t launch_mc_k(McArgs a, cudaStream_t s) {
+  const size_t fc_bytes = (size_t)a.ncmax * MLP_IN * sizeof(int);
+  size_t dyn = 0;
+  if (MODE != G6_MC_PLAIN && fc_bytes <= MC_FC_SMEM_MAX) {
+    dyn = fc_bytes;
+    cudaError_t e = cudaFuncSetAttribute(k_mc<NQ, TAPER, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  a.fc_smem = dyn > 0;
+  k_mc<NQ, TAPER, MIXED, MODE><<<a.rep.nrep, MC_NT, dyn, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int NQ, bool TAPER, bool MIXED>
 static cudaError_t launch_mc_m(const McArgs& a, int mode, cudaStream_t s) {
-  const int nb = a.rep.nrep;
-  if (mode == G6_MC_LEARNED) k_mc<NQ, TAPER, MIXED, G6_MC_LEARNED><<<nb, MC_NT, 0, s>>>(a);
-  else if (mode == G6_MC_COLLECT) k_mc<NQ, TAPER, MIXED, G6_MC_COLLECT><<<nb, MC_NT, 0, s>>>(a);
-  else k_mc<NQ, TAPER, MIXED, G6_MC_PLAIN><<<nb, MC_NT, 0, s>>>(a);
-  return cudaGetLastError();
+  if (mode == G6_MC_LEARNED) return launch_mc_k<NQ, TAPER, MIXED, G6_MC_LEARNED>(a, s);
+  if (mode == G6_MC_COLLECT) return launch_mc_k<NQ, TAPER, MIXED, G6_MC_COLLECT>(a, s);
+  return launch_mc_k<NQ, TAPER, MIXED, G6_MC_PLAIN>(a, s);
 }
 
 template <int NQ, bool TAPER>

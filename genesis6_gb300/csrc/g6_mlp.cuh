@@ -47,6 +47,7 @@ struct McArgs {
   int n, ntrial, nsamples, sample_every;
   RepDev rep;
   double body[MAXSITE][3];
+  float fbody[MAXSITE][3];   // the same in FP32 (mixed trial poses)
   double* st;
   double* pk64;
   float* pk32f;           // the float4 packed poses viewed as floats
@@ -64,6 +65,8 @@ struct McArgs {
   int* fcache;            // features of every molecule at its current pose (MLP_IN integers each)
   int* flag;              // set to 1 when a pose has more than MC_QMAX feature neighbours
   float* udir;            // unit directions of every molecule's charged sites (12 floats each)
+  int ncmax;              // molecules of the largest chain
+  int fc_smem;            // set by launch_mc: each chain's feature cache lives in shared memory
   unsigned long long seed, counter;
   MlpDev mlp;
 };

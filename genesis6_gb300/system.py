@@ -138,6 +138,30 @@ class RigidWater:
         self._check(self.L.g6_md_step_host(self.ctx, float(dt), thermo, dptr(rec), dptr(log)))
         return rec
 
+    # -- Monte Carlo (mc2.F90 trial/accept loop, one chain per replica) --------
+    def mc_run(self, ntrial, seed, counter, beta, sigma_t=0.15, sigma_r=0.15, mode="plain", sample_every=0,
+               trace=False):
+        """`ntrial` single-molecule trials on every chain.  beta, sigma_t, sigma_r
+        are scalars or per-chain arrays; mode is "plain" (fixed widths),
+        "learned" (widths from the network) or "collect" (fixed widths, training
+        records kept on the device).  Returns a dict with accepted/trial counts,
+        the running energies, the energy every `sample_every` trials and, with
+        trace=True, (dE, energy, accepted, target) per trial."""
+        R = self.nrep
+        per = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (R,)))
+        beta, st, sr = per(beta), per(sigma_t), per(sigma_r)
+        modes = {"plain": _capi.MC_PLAIN, "learned": _capi.MC_LEARNED, "collect": _capi.MC_COLLECT}
+        counts = np.zeros(2 * R, np.int64)
+        energy = np.zeros(R)
+        nsm = ntrial // sample_every if sample_every else 0
+        samples = np.zeros((R, max(nsm, 1)))
+        tr = np.zeros((R, ntrial, 4)) if trace else None
+        self._check(self.L.g6_mc_run(self.ctx, int(ntrial), int(seed), int(counter), dptr(beta), dptr(st), dptr(sr),
+                                     modes[mode], int(sample_every), dptr(samples) if nsm else None,
+                                     counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(energy), dptr(tr)))
+        return {"accepted": counts[0::2].copy(), "trials": counts[1::2].copy(), "energy": energy,
+                "samples": samples[:, :nsm], "trace": tr}
+
     def replica_exchange(self, parity, seed, counter, beta, thermo):
         beta = np.ascontiguousarray(beta, dtype=np.float64)
         acc = np.zeros(self.nrep, np.int32)
