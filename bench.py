@@ -214,10 +214,12 @@ def thermo_for(s, n=1):
     return s.thermostats(n, "nose", temp=TEMP, q=q, dump=0.0)
 
 
-def timed_md(torch, s, steps, warmup, flush):
+def timed_md(torch, s, steps, warmup, flush, kernel_steps=50):
     """`steps` MD steps, each a one-step CUDA graph that records events around
-    the whole step and around the fused force/integrator kernel, with a
-    256 MiB L2 flush on the same stream before every step."""
+    the whole step, with a 256 MiB L2 flush on the same stream before every
+    step.  The fused force/integrator kernel is timed on `kernel_steps` further
+    steps with events around the kernel as well (event nodes between the
+    kernels add latency of their own, so they stay out of the step timing)."""
     L = s.L
     th = thermo_for(s)
     lpi = ctypes.c_int()
@@ -227,21 +229,26 @@ def timed_md(torch, s, steps, warmup, flush):
     sp = ctypes.c_void_p()
     s._check(L.g6_stream(s.ctx, ctypes.byref(sp)))
     stream = torch.cuda.ExternalStream(sp.value)
-    log = np.zeros((steps, 1, 10))
-    step_ms, kms = np.zeros(steps), np.zeros(steps)
     a, b = ctypes.c_double(), ctypes.c_double()
-    s._check(L.g6_set_step_timing(s.ctx, 1))
-    torch.cuda.synchronize()
-    s._check(L.g6_md_begin(s.ctx, DT, steps, th, 1))
-    for k in range(steps):
-        with torch.cuda.stream(stream):
-            flush.add_(1.0)
-        s._check(L.g6_md_advance(s.ctx, 1))
-        s._check(L.g6_step_times(s.ctx, ctypes.byref(a), ctypes.byref(b)))
-        step_ms[k], kms[k] = a.value, b.value
-    s._check(L.g6_md_end(s.ctx, th, log.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
-    s._check(L.g6_set_step_timing(s.ctx, 0))
-    torch.cuda.synchronize()
+
+    def run(mode, nst):
+        log = np.zeros((nst, 1, 10))
+        step_ms, kms = np.zeros(nst), np.zeros(nst)
+        s._check(L.g6_set_step_timing(s.ctx, mode))
+        torch.cuda.synchronize()
+        s._check(L.g6_md_begin(s.ctx, DT, nst, th, 1))
+        for k in range(nst):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            s._check(L.g6_md_advance(s.ctx, 1))
+            s._check(L.g6_step_times(s.ctx, ctypes.byref(a), ctypes.byref(b)))
+            step_ms[k], kms[k] = a.value, b.value
+        s._check(L.g6_md_end(s.ctx, th, log.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        s._check(L.g6_set_step_timing(s.ctx, 0))
+        torch.cuda.synchronize()
+        return step_ms, kms, log
+    step_ms, _, log = run(1, steps)
+    _, kms, _ = run(2, max(1, min(kernel_steps, steps)))
     return step_ms, kms, log, lpi.value
 
 
@@ -372,7 +379,7 @@ def mc_chains(C=32, N=1024, T=260.0, rc=9.0, seed=20261203, melt_steps=5000, md_
                                   "md_T_last_quarter": float(log[3 * q:, :, 3].mean())}
 
 
-def bench_mc(torch, seed=20261203, sweeps=1000, records=1_000_000, equil_sweeps=1000, w_move=1.0, w_energy=0.0,
+def bench_mc(torch, seed=20261203, sweeps=2000, records=1_000_000, equil_sweeps=1000, w_move=0.0, w_energy=1.0,
              T=260.0, rc=9.0, md_steps=30000):
     """32 chains x 1,024 ST2 (custom path, Coulomb taper), T = 260 K, rc 9 A with
     a 2 A switch.  Chains start from MD-equilibrated liquid (melt at 400 K, then

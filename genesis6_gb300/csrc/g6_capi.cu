@@ -222,6 +222,9 @@ struct g6_ctx {
   int* d_fcache = nullptr;         // per-molecule features at the current pose (Monte Carlo)
   int* d_mcflag = nullptr;         // Monte Carlo: too many feature neighbours
   float* d_udir = nullptr;         // Monte Carlo: charged-site directions per molecule
+  int* d_flist = nullptr;          // Monte Carlo: feature-neighbour rows (MC_FL_CAP per molecule)
+  int* d_fnum = nullptr;
+  uint32_t* d_flfix = nullptr;
   float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
   double sig0_t = 0.15, sig0_r = 0.15;
   double obj_move = 1.0, obj_energy = 0.0;   // training objective weights (g6_mlp_objective)
@@ -251,7 +254,7 @@ struct g6_ctx {
   double run_dt = 0.0;
   int run_max = 0, run_done = 0;
   cudaGraphExec_t graph1 = nullptr;   // one step, for step-by-step advancing
-  bool step_timing = false;           // graph1 carries events around the step and the kernel
+  int step_timing = 0;                // 1: graph1 carries events around the step; 2: and around the kernel
   cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -287,7 +290,7 @@ static void free_all(g6_ctx* c) {
   drop_graphs(c);
   for (int k = 0; k < 4; ++k)
     if (c->sev[k]) { cudaEventDestroy(c->sev[k]); c->sev[k] = nullptr; }
-  c->step_timing = false;
+  c->step_timing = 0;
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
   if (c->d_scratch) { cudaFree(c->d_scratch); c->d_scratch = nullptr; c->scratch_bytes = 0; }
@@ -612,6 +615,8 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
   CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_fcache, (size_t)n * MLP_IN));
   CK(dalloc(ctx, &ctx->d_mcflag, 1)); CK(dalloc(ctx, &ctx->d_udir, (size_t)n * 12));
+  CK(dalloc(ctx, &ctx->d_flist, (size_t)n * MC_FL_CAP)); CK(dalloc(ctx, &ctx->d_fnum, (size_t)n));
+  CK(dalloc(ctx, &ctx->d_flfix, (size_t)n * 3));
   ctx->last_epot.assign(nrep, 0.0);
   ctx->have_system = true;
   return G6_OK;
@@ -928,17 +933,18 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
 // integrator kernel.  ev (optional, 4 events) brackets the step and the kernel.
 static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullptr) {
   // external records become event nodes of a captured graph (queryable after launch)
+  // the kernel's own events only in mode 2: event nodes between the kernels add
+  // their own latency to the step
+  const bool kev = ev && ctx->step_timing == 2;
   if (ev) CK(cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal));
   int rc = enqueue_rebuild(ctx, ctx->d_ctrl, &sa);
   if (rc) return rc;
   ForceArgs fa = force_args(ctx);
   fa.ctrl = ctx->d_ctrl;
-  if (ev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
+  if (kev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
   CK(launch_step(fa, sa, ctx->model, ctx->prec == G6_MIXED, ctx->step_lpi, ctx->stream));
-  if (ev) {
-    CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
-    CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
-  }
+  if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
+  if (ev) CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
   return G6_OK;
 }
 
@@ -1122,7 +1128,8 @@ int g6_set_step_timing(g6_ctx* ctx, int on) {
   CK(cudaSetDevice(ctx->device));
   for (int k = 0; k < 4; ++k)
     if (!ctx->sev[k]) CK(cudaEventCreate(&ctx->sev[k]));
-  ctx->step_timing = on != 0;
+  if (on < 0 || on > 2) return fail(ctx, G6_ERR_ARG, "step timing mode is 0, 1 or 2");
+  ctx->step_timing = on;
   drop_graphs(ctx);
   return G6_OK;
 }
@@ -1133,7 +1140,7 @@ int g6_step_times(g6_ctx* ctx, double* step_ms, double* kernel_ms) {
   CK(cudaEventSynchronize(ctx->sev[3]));
   float a = 0.0f, b = 0.0f;
   CK(cudaEventElapsedTime(&a, ctx->sev[0], ctx->sev[3]));
-  CK(cudaEventElapsedTime(&b, ctx->sev[1], ctx->sev[2]));
+  if (ctx->step_timing == 2) CK(cudaEventElapsedTime(&b, ctx->sev[1], ctx->sev[2]));
   if (step_ms) *step_ms = a;
   if (kernel_ms) *kernel_ms = b;
   return G6_OK;
@@ -1374,6 +1381,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
   a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
   a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
+  a.flist = ctx->d_flist; a.fnum = ctx->d_fnum; a.flfix = ctx->d_flfix;
   for (int r = 0; r < R; ++r) a.ncmax = std::max(a.ncmax, ctx->off[r + 1] - ctx->off[r]);
   a.mlp = mlp_dev(ctx);
   CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));

@@ -32,7 +32,9 @@
 // MLP on local-environment features.  The features of every molecule at its
 // current pose are kept in an integer cache (exact sums, see g6_mlp.cuh): the
 // widths at the old pose come from the cache, the features at the new pose
-// are summed in the same pass as the energies, and an accepted move updates
+// are summed by a control warp from the molecules of the target's feature row
+// (molecules within 6.5 A + a skin, rebuilt when molecules have moved far
+// enough) while the other warps sum the energies, and an accepted move updates
 // the cache of the moved molecule and of its neighbours.  The Hastings ratio
 // uses the widths of both poses.  G6_MC_COLLECT runs the fixed widths and
 // writes one training record per trial.
@@ -320,6 +322,41 @@ __device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3]
   }
 }
 
+// Feature-neighbour rows of every molecule of the chain: the molecules within
+// 6.5 A + MC_FL_SKIN of its fixed-point COM now, which is kept as the row's
+// reference position.  A row holds every molecule within 6.5 A of the
+// molecule as long as the two have moved by less than MC_FL_SKIN in total
+// since the build; the kernel checks that before every trial.
+__device__ void build_flists(const McArgs& a, int i0, int i1, const float fs[3]) {
+  constexpr float R2 = (6.5f + MC_FL_SKIN) * (6.5f + MC_FL_SKIN);
+  const int n = a.n;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const uint32_t fi[3] = {a.fix[i], a.fix[n + i], a.fix[2 * n + i]};
+    int* row = a.flist + (size_t)i * MC_FL_CAP;
+    int cnt = 0;
+    for (int j = i0; j < i1; ++j) {
+      if (j == i) continue;
+      const uint32_t fj[3] = {a.fix[j], a.fix[n + j], a.fix[2 * n + j]};
+      float e[3];
+      if (fvec_fix(fi, fj, fs, e) < R2) {
+        if (cnt < MC_FL_CAP) row[cnt] = j;
+        ++cnt;
+      }
+    }
+    if (cnt > MC_FL_CAP) { atomicExch(a.flag, 1); cnt = MC_FL_CAP; }
+    a.fnum[i] = cnt;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a.flfix[(size_t)k * n + i] = fi[k];
+  }
+}
+
+// Distance moved since the feature rows were built (fixed-point COM).
+__device__ __forceinline__ float fl_moved(const McArgs& a, int i, const uint32_t f[3], const float fs[3]) {
+  const uint32_t b[3] = {a.flfix[i], a.flfix[a.n + i], a.flfix[2 * a.n + i]};
+  float e[3];
+  return sqrtf(fvec_fix(b, f, fs, e));
+}
+
 // The proposal-width network in shared memory, transposed for conflict-free
 // reads (lane o reads column o).
 struct MlpShared {
@@ -413,10 +450,15 @@ __device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* 
   }
 }
 
-// log of the proposal density of a move (up to a constant): isotropic
-// Gaussians in the translation and in the rotation vector.
-__device__ __forceinline__ float log_q(float st, float sr, float d2, float r2) {
-  return -3.0f * __logf(st) - d2 / (2.0f * st * st) - 3.0f * __logf(sr) - r2 / (2.0f * sr * sr);
+// The proposal density of a move (isotropic Gaussians in the translation and
+// in the rotation vector) as three numbers of its widths, so that the log of
+// the density, -3 ln st - 3 ln sr - d2/(2 st^2) - r2/(2 sr^2), is
+// lq - d2 * it - r2 * ir.
+struct QForm {
+  float lq, it, ir;
+};
+__device__ __forceinline__ QForm q_form(float st, float sr) {
+  return QForm{-3.0f * (__logf(st) + __logf(sr)), 0.5f / (st * st), 0.5f / (sr * sr)};
 }
 
 // Queues of the molecules within the feature radius of the old (0) and new
@@ -444,7 +486,7 @@ struct TrialPose {
   R on[NQ + 1][3], oo[NQ + 1][3];   // new / old site offsets
   double cn[3], co[3];              // new / old FP64 COM
   R rot[3], dx[3];                  // rotation vector and translation
-  float stf, srf;                   // widths of the proposal (at the old pose), FP32
+  QForm qf;                         // proposal density form of the widths at the old pose
   R qn[4];                          // trial quaternion (the pose's precision)
   double qo64[4];                   // FP64 quaternion before the move
   double q64[4];                    // FP64 quaternion after the move (FP64 mode; mixed: made on acceptance)
@@ -452,7 +494,19 @@ struct TrialPose {
   float un[4][3];                   // charged-site directions at the new pose
   float d2, r2;                     // |dx|^2, |rot|^2
   int trial;                        // trial number the pose belongs to (-1: none)
+  float fl_mo, fl_mn;               // distance of the old / new pose from the target's feature-row reference
+  int fl_epoch;                     // feature-row build the two distances refer to
 };
+
+// Distances of a pose's old and new COM from its target's feature-row
+// reference position (one thread).
+template <class TP>
+__device__ __forceinline__ void fl_distances(const McArgs& a, TP& P, int tg, const float fs[3], int epoch) {
+  const uint32_t fo[3] = {P.fo[0], P.fo[1], P.fo[2]}, fn[3] = {P.fn[0], P.fn[1], P.fn[2]};
+  P.fl_mo = fl_moved(a, tg, fo, fs);
+  P.fl_mn = fl_moved(a, tg, fn, fs);
+  P.fl_epoch = epoch;
+}
 
 // Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot],
 // widths st_w, sr_w).  Register arrays are indexed with constants only
@@ -543,8 +597,7 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
   if (lane == 0) {
     P.d2 = (float)d2;
     P.r2 = (float)r2;
-    P.stf = (float)st_w;
-    P.srf = (float)sr_w;
+    P.qf = q_form((float)st_w, (float)sr_w);
     P.trial = trial;
   }
   __syncwarp();
@@ -600,7 +653,11 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
   __shared__ int s_nq[2];
   __shared__ int s_accept, s_hit;
-  __shared__ float s_sig_new[2];   // learned widths at the trial pose
+  __shared__ float s_fl_moved;   // largest distance any molecule moved since the feature rows were built
+  __shared__ int s_fl_mode;      // 0: the target's feature row covers both poses; 1: rebuild the rows first;
+                                 // 2: the trial move alone exceeds the skin, scan the whole chain
+  __shared__ int s_fl_epoch;     // feature-row builds so far
+  __shared__ QForm s_qf_new;   // proposal density form of the learned widths at the trial pose
   __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
 
   const int c = blockIdx.x;
@@ -621,7 +678,11 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   // the chain's feature cache: shared memory when it fits, else its rows of a.fcache
   extern __shared__ int s_fcdyn[];
   int* const fcl = a.fc_smem ? s_fcdyn : a.fcache + (size_t)i0 * MLP_IN;
-  if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
+  if constexpr (FEAT) {
+    init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
+    build_flists(a, i0, i1, fs);
+    if (threadIdx.x == 0) { s_fl_moved = 0.0f; s_fl_epoch = 0; }
+  }
   if (threadIdx.x == 0) { s_pose[0].trial = -1; s_pose[1].trial = -1; }
   __syncthreads();
 
@@ -655,14 +716,41 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
     }
     const int tg = i0 + s_tg[tb];
     TP& cur = s_pose[t & 1];
-    if (FEAT && threadIdx.x == 0) { s_nq[0] = 0; s_nq[1] = 0; }
     // ---- warp 0: the trial pose, unless it was built during the previous trial ----
     if (warp == 0 && cur.trial != t) {
       R st_w = sig_t_fixed, sr_w = sig_r_fixed;
       if constexpr (LEARN) mlp_widths_warp<R>(s_mlp, 0, fcl + (size_t)(tg - i0) * MLP_IN, st_w, sr_w);
       build_trial<R, NQ, MIXED>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL, fsi);
+      if (FEAT && lane == 0) fl_distances(a, cur, tg, fs, s_fl_epoch);
+    }
+    if constexpr (FEAT) {
+      // the target's feature row holds every molecule within 6.5 A of both poses
+      // while the pose and any other molecule have moved less than the skin in
+      // total since the rows were built (margin for the FP32 distances)
+      if (warp == 0 && lane == 0) {
+        if (cur.fl_epoch != s_fl_epoch) fl_distances(a, cur, tg, fs, s_fl_epoch);
+        constexpr float LIM = MC_FL_SKIN - 0.01f;
+        int mode = 0;
+        if (s_fl_moved + fmaxf(cur.fl_mo, cur.fl_mn) >= LIM) {
+          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+          float e[3];
+          mode = sqrtf(fvec_fix(fo, fn, fs, e)) < LIM ? 1 : 2;
+        }
+        s_fl_mode = mode;
+      }
     }
     __syncthreads();
+    if constexpr (FEAT) {
+      if (s_fl_mode == 1) {
+        build_flists(a, i0, i1, fs);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          s_fl_moved = 0.0f;
+          ++s_fl_epoch;
+        }
+        __syncthreads();
+      }
+    }
     if ((int)threadIdx.x >= E0) {
       // ---- energy warps: dE over every other molecule of the chain ----
       R acc = R(0);
@@ -673,34 +761,6 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         for (int k = 0; k < 3; ++k) { ro[s][k] = cur.oo[s][k]; rn[s][k] = cur.on[s][k]; }
       const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
       const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-      if constexpr (FEAT) {
-        // feature neighbours of both poses (whole warps, ballots into this warp's
-        // segments), then release the control warps
-        const int ew = warp - NCTRL;
-        for (int j0 = i0 + 32 * ew; j0 < i1; j0 += NE) {
-          const int j = j0 + lane;
-          bool qo = false, qn = false;
-          if (j < i1 && j != tg) {
-            float e[3];
-            if (MIXED) {
-              uint32_t fj[3];
-              P::fix(a, j, fj);
-              const float r2o = fvec_fix(fj, fo, fs, e), r2n = fvec_fix(fj, fn, fs, e);
-              qo = r2o < FEAT_RC2 && r2o > 0.0f;
-              qn = r2n < FEAT_RC2 && r2n > 0.0f;
-            } else {
-              double cj[3];
-              P::com(a, j, cj);
-              const float r2o = fvec_64(cj, co, L, iL, e), r2n = fvec_64(cj, cn, L, iL, e);
-              qo = r2o < FEAT_RC2 && r2o > 0.0f;
-              qn = r2n < FEAT_RC2 && r2n > 0.0f;
-            }
-          }
-          queue_push(s_q[0], &s_nq[0], qo, j, a.flag);
-          queue_push(s_q[1], &s_nq[1], qn, j, a.flag);
-        }
-        asm volatile("bar.arrive 1, %0;" ::"n"(NE + 32));
-      }
       for (int j = i0 + (int)threadIdx.x - E0; j < i1; j += NE) {
         if (j == tg) continue;
         R dO[3], dN[3], ddO, ddN;
@@ -756,8 +816,55 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       const int tg1 = next_in_batch ? i0 + s_tg[tb + 1] : -1;
       if (warp == 0) {
         if constexpr (FEAT) {
-          // features of the target at the new pose: terms of every queued neighbour
-          asm volatile("bar.sync 1, %0;" ::"n"(NE + 32));   // the energy warps' queues are complete
+          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
+          const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+          // queues of the molecules within 6.5 A of the old (0) and new (1) pose, from
+          // the target's feature row (or, when the move alone exceeds the skin, from
+          // the whole chain)
+          {
+            const bool all = s_fl_mode == 2;
+            const int* row = a.flist + (size_t)tg * MC_FL_CAP;
+            const int m = all ? nc : a.fnum[tg];
+            int cnt0 = 0, cnt1 = 0;
+            for (int p0 = 0; p0 < m; p0 += 32) {
+              const int p = p0 + lane;
+              bool qo = false, qn = false;
+              int j = -1;
+              if (p < m) {
+                j = all ? i0 + p : row[p];
+                if (j != tg) {
+                  float e[3], r2o, r2n;
+                  if (MIXED) {
+                    uint32_t fj[3];
+                    P::fix(a, j, fj);
+                    r2o = fvec_fix(fj, fo, fs, e);
+                    r2n = fvec_fix(fj, fn, fs, e);
+                  } else {
+                    double cj[3];
+                    P::com(a, j, cj);
+                    r2o = fvec_64(cj, co, L, iL, e);
+                    r2n = fvec_64(cj, cn, L, iL, e);
+                  }
+                  qo = r2o < FEAT_RC2 && r2o > 0.0f;
+                  qn = r2n < FEAT_RC2 && r2n > 0.0f;
+                }
+              }
+              const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
+              const unsigned lt = (1u << lane) - 1u;
+              if (qo) {
+                const int pos = cnt0 + __popc(mo & lt);
+                if (pos < MC_QMAX) s_q[0][pos] = j; else *a.flag = 1;
+              }
+              if (qn) {
+                const int pos = cnt1 + __popc(mn & lt);
+                if (pos < MC_QMAX) s_q[1][pos] = j; else *a.flag = 1;
+              }
+              cnt0 += __popc(mo);
+              cnt1 += __popc(mn);
+            }
+            if (lane == 0) { s_nq[0] = cnt0; s_nq[1] = cnt1; }
+            __syncwarp();
+          }
           int f[MLP_IN];
 #pragma unroll
           for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
@@ -766,8 +873,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           for (int s = 0; s < 4; ++s)
 #pragma unroll
             for (int k = 0; k < 3; ++k) un[s][k] = cur.un[s][k];
-          const uint32_t fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-          const double cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
+          // features of the target at the new pose: terms of every queued neighbour
           const int nn = min(s_nq[1], MC_QMAX);
           for (int p = lane; p < nn; p += 32) {
             const int j = s_q[1][p];
@@ -785,11 +891,12 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           if constexpr (LEARN) {
             R st2, sr2;
             mlp_widths_warp<R>(s_mlp, 0, s_feat, st2, sr2);
-            if (lane == 0) { s_sig_new[0] = (float)st2; s_sig_new[1] = (float)sr2; }
+            if (lane == 0) s_qf_new = q_form((float)st2, (float)sr2);
           }
         }
         if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
           build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL, fsi);
+          if (FEAT && lane == 0) fl_distances(a, s_pose[(t + 1) & 1], tg1, fs, s_fl_epoch);
         }
       } else if constexpr (LEARN) {
         if (next_in_batch) {
@@ -797,6 +904,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           R st1, sr1;
           mlp_widths_warp<R>(s_mlp, 1, fcl + (size_t)(tg1 - i0) * MLP_IN, st1, sr1);
           build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL, fsi);
+          if (lane == 0) fl_distances(a, s_pose[(t + 1) & 1], tg1, fs, s_fl_epoch);
         }
       }
     }
@@ -811,7 +919,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       if (lane == 0) {
         float logh = 0.0f;
         if (LEARN)
-          logh = log_q(s_sig_new[0], s_sig_new[1], cur.d2, cur.r2) - log_q(cur.stf, cur.srf, cur.d2, cur.r2);
+          logh = (s_qf_new.lq - cur.qf.lq) - cur.d2 * (s_qf_new.it - cur.qf.it) - cur.r2 * (s_qf_new.ir - cur.qf.ir);
         // Metropolis-Hastings test in the precision of the energies
         bool ok;
         if (MIXED) {
@@ -852,6 +960,10 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         if (lane == 0) {
           energy += dE;
           ++nacc;
+          if constexpr (FEAT) {   // the moved molecule's distance from its feature-row reference
+            if (cur.fl_epoch != s_fl_epoch) fl_distances(a, cur, tg, fs, s_fl_epoch);
+            s_fl_moved = fmaxf(s_fl_moved, cur.fl_mn);
+          }
           // the next trial's prepared pose is stale when it moves the same molecule
           if (s_pose[(t + 1) & 1].trial == t + 1 && t + 1 < a.ntrial && s_tg[(tb + 1) % MC_NB] + i0 == tg)
             s_pose[(t + 1) & 1].trial = -1;

@@ -163,9 +163,10 @@ int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log);
 /* The cudaStream_t (as void*) on which the context enqueues its work. */
 int g6_stream(g6_ctx* ctx, void** stream);
 /* Step timing: with g6_set_step_timing(ctx, 1) every MD step runs as its own
-   one-step CUDA graph that records events around the whole step and around
-   the fused force/integrator kernel; g6_step_times waits for the last step
-   and returns both durations in ms. */
+   one-step CUDA graph that records events around the whole step; with mode 2
+   also around the fused force/integrator kernel (the extra event nodes add
+   their own latency to the step).  g6_step_times waits for the last step and
+   returns both durations in ms (kernel_ms = 0 in mode 1); 0 turns it off. */
 int g6_set_step_timing(g6_ctx* ctx, int on);
 int g6_step_times(g6_ctx* ctx, double* step_ms, double* kernel_ms);
 /* Duration (ms, CUDA events on the context's stream) of one launch of the
