@@ -240,7 +240,10 @@ struct g6_ctx {
   // log buffer
   double* d_log = nullptr; size_t log_cap = 0;
   // pinned host staging for g6_md_step_host
-  double* h_pinned = nullptr; size_t pinned_bytes = 0;
+  // pinned host block for the small per-run transfers (thermostats, control
+  // words, per-replica factors, read-backs), so that they are asynchronous
+  char* h_pinned = nullptr; size_t pinned_bytes = 0;
+  cudaEvent_t pin_ev = nullptr;   // the last uploads from the block have been read
   // graph of a block of MD steps
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
@@ -300,6 +303,7 @@ static void free_all(g6_ctx* c) {
   if (c->d_rec) { cudaFree(c->d_rec); c->d_rec = nullptr; c->rec_cap = 0; c->nrec = 0; }
   c->have_mlp = false;
   if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
+  if (c->pin_ev) { cudaEventDestroy(c->pin_ev); c->pin_ev = nullptr; }
   c->gref = HostGrid(); c->glist = HostGrid();
   c->pair_capacity = 0; c->npairs = -1; c->cap = 0;
 }
@@ -547,6 +551,11 @@ int g6_ctx_destroy(g6_ctx* ctx) {
   return G6_OK;
 }
 
+// Bytes of the pinned host block of a context with nrep replicas (its regions: pinned_runs).
+static size_t pinned_runs_bytes(int nrep) {
+  return 2 * (size_t)nrep * sizeof(ThermoDev) + (size_t)nrep * (NRED + 2 + 3) * sizeof(double) + 24 * sizeof(int);
+}
+
 int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const int* nmol, const double* box) {
   if (!ctx) return G6_ERR_ARG;
   if (nrep < 1 || !nmol || !box) return fail(ctx, G6_ERR_ARG, "nrep, nmol and box are required");
@@ -618,6 +627,10 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_flist, (size_t)n * MC_FL_CAP)); CK(dalloc(ctx, &ctx->d_fnum, (size_t)n));
   CK(dalloc(ctx, &ctx->d_flfix, (size_t)n * 3));
   ctx->last_epot.assign(nrep, 0.0);
+  ctx->pinned_bytes = pinned_runs_bytes(nrep);
+  CK(cudaMallocHost((void**)&ctx->h_pinned, ctx->pinned_bytes));
+  CK(cudaEventCreateWithFlags(&ctx->pin_ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
   ctx->have_system = true;
   return G6_OK;
 }
@@ -968,6 +981,32 @@ static int md_stop(g6_ctx* ctx) {
   return G6_OK;
 }
 
+// Regions of the pinned host block: uploads (thermostats, control words,
+// factors) and read-backs kept apart, since an upload may still be pending
+// while a read-back is enqueued.
+struct PinnedRuns {
+  ThermoDev* th_up;
+  ThermoDev* th_dn;
+  double* red;
+  double* rf;
+  double* fx;
+  int* ctrl_up;
+  int* ctrl_dn;
+  int* ovf;
+};
+static PinnedRuns pinned_runs(g6_ctx* ctx) {
+  const int R = ctx->nrep;
+  char* b = ctx->h_pinned;
+  PinnedRuns p;
+  p.th_up = (ThermoDev*)b; b += (size_t)R * sizeof(ThermoDev);
+  p.th_dn = (ThermoDev*)b; b += (size_t)R * sizeof(ThermoDev);
+  p.red = (double*)b; b += (size_t)R * NRED * sizeof(double);
+  p.rf = (double*)b; b += 2 * (size_t)R * sizeof(double);
+  p.fx = (double*)b; b += 3 * (size_t)R * sizeof(double);
+  p.ctrl_up = (int*)b; p.ctrl_dn = p.ctrl_up + 8; p.ovf = p.ctrl_up + 16;
+  return p;
+}
+
 static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log, uint64_t seed) {
   int rc = prepare_list(ctx);
   if (rc) return rc;
@@ -978,7 +1017,10 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
     if (ctx->step_lpi != 4 && ctx->step_lpi != 8 && ctx->step_lpi != 16 && ctx->step_lpi != 32)
       ctx->step_lpi = default_lpi(ctx);
   }
-  std::vector<ThermoDev> th(ctx->nrep);
+  // the previous uploads from the pinned block have been read before it is refilled
+  CK(cudaEventSynchronize(ctx->pin_ev));
+  const PinnedRuns pr = pinned_runs(ctx);
+  ThermoDev* th = pr.th_up;
   for (int r = 0; r < ctx->nrep; ++r) {
     ThermoDev& t = th[r];
     std::memset(&t, 0, sizeof t);
@@ -994,7 +1036,7 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
       if (t.kind < G6_NVE || t.kind > G6_ANDERSEN) return fail(ctx, G6_ERR_ARG, "unknown thermostat");
     }
   }
-  CK(cudaMemcpyAsync(ctx->d_th, th.data(), th.size() * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_th, th, ctx->nrep * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
   const size_t need_log = want_log ? (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH : 0;
   if (need_log > ctx->log_cap) {
     if (ctx->d_log) { cudaFree(ctx->d_log); ctx->d_log = nullptr; ctx->log_cap = 0; }
@@ -1002,25 +1044,26 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
     ctx->log_cap = need_log;
     drop_graphs(ctx);
   }
-  int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
-  CK(cudaMemcpyAsync(ctx->d_ctrl, ctrl, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
+  const int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
+  std::memcpy(pr.ctrl_up, ctrl, sizeof ctrl);
+  CK(cudaMemcpyAsync(ctx->d_ctrl, pr.ctrl_up, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_gmax, 0, 2 * sizeof(unsigned), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_repcnt, 0, ctx->nrep * sizeof(int), ctx->stream));
   {   // temperature and pressure factors of each replica (Mixture.F90:2251-2264)
-    std::vector<double> rf(2 * (size_t)ctx->nrep);
+    double* rf = pr.rf;
     for (int r = 0; r < ctx->nrep; ++r) {
       const double dof = 6.0 * (ctx->off[r + 1] - ctx->off[r]);
       const double vol = ctx->L[3 * r] * ctx->L[3 * r + 1] * ctx->L[3 * r + 2];
       rf[2 * r] = I2J * 2.0 / (RGAS * dof);
       rf[2 * r + 1] = I2J / (3.0 * A2P * vol * NA * ANG2M * ANG2M * ANG2M);
     }
-    std::vector<double> fx(3 * (size_t)ctx->nrep);
+    double* fx = pr.fx;
     for (int k = 0; k < 3 * ctx->nrep; ++k) fx[k] = (1.0 / ctx->L[k]) * 4294967296.0;
-    CK(cudaMemcpyAsync(ctx->d_rfac, rf.data(), rf.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_fixs, fx.data(), fx.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));   // rf, fx are local vectors
+    CK(cudaMemcpyAsync(ctx->d_rfac, rf, 2 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_fixs, fx, 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   }
+  CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
   CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
   if (thermo && thermo[0].seed != ctx->seed) {
     ctx->seed = thermo[0].seed;
@@ -1031,13 +1074,15 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
 }
 
 static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log) {
-  int ctrl[8], ovf = 0;
-  std::vector<ThermoDev> th(ctx->nrep);
-  std::vector<double> red((size_t)ctx->nrep * NRED);
-  CK(cudaMemcpyAsync(ctrl, ctx->d_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(th.data(), ctx->d_th, th.size() * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(red.data(), ctx->d_red, red.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  const PinnedRuns pr = pinned_runs(ctx);
+  const int* ctrl = pr.ctrl_dn;
+  const ThermoDev* th = pr.th_dn;
+  const double* red = pr.red;
+  CK(cudaMemcpyAsync(pr.ctrl_dn, ctx->d_ctrl, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(pr.ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(pr.th_dn, ctx->d_th, ctx->nrep * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(pr.red, ctx->d_red, (size_t)ctx->nrep * NRED * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
   if (log && nsteps > 0)
     CK(cudaMemcpyAsync(log, ctx->d_log, (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH * sizeof(double),
                        cudaMemcpyDeviceToHost, ctx->stream));
@@ -1050,6 +1095,7 @@ static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log
       thermo[r].zetasum = th[r].zsum;
     }
   }
+  const int ovf = *pr.ovf;
   if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
   if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow (raise the skin or density)");
   if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");

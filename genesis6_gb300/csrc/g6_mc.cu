@@ -52,7 +52,7 @@ constexpr int MC_NB = 128;            // trials per batch of pre-computed draws
 constexpr float FEAT_Q = 1048576.0f;  // feature terms are integers of 2^-20
 constexpr float FEAT_IQ = 1.0f / 1048576.0f;
 constexpr float FEAT_RC2 = 6.5f * 6.5f;
-constexpr int MC_QMAX = 256;          // feature neighbours per pose (about 40 in liquid water)
+constexpr int MC_QMAX = 128;          // feature neighbours per pose (about 40 in liquid water)
 
 template <int NQ, bool TAPER, class R>
 __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 1][3], const R (&rj)[NQ + 1][3],
@@ -154,7 +154,13 @@ __device__ __forceinline__ void trial_rotation(const R rot[3], const R* qold, co
 __device__ __forceinline__ float dot3_rn(const float a[3], const float b[3]) {
   return __fadd_rn(__fadd_rn(__fmul_rn(a[0], b[0]), __fmul_rn(a[1], b[1])), __fmul_rn(a[2], b[2]));
 }
-__device__ __forceinline__ float gauss_rn(float t) { return exp2f(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)); }
+// exp(-t^2) with the single hardware base-2 exponential (PTX ex2.approx.ftz:
+// results below 2^-126 flush to zero, far below the 2^-20 quantum of a term)
+__device__ __forceinline__ float gauss_rn(float t) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)));
+  return y;
+}
 __device__ __forceinline__ int feat_q(float x) { return __float2int_rn(__fmul_rn(x, FEAT_Q)); }
 
 // Unit direction of one site offset v.  rsqrtf is a fixed function of its
@@ -360,33 +366,35 @@ __device__ __forceinline__ float fl_moved(const McArgs& a, int i, const uint32_t
 // The proposal-width network in shared memory, transposed for conflict-free
 // reads (lane o reads column o).
 struct MlpShared {
-  float w1t[MLP_IN][MLP_H];
-  float b1[MLP_H];
-  float w2t[MLP_H][MLP_H];
-  float b2[MLP_H];
-  float w3[MLP_OUT][MLP_H];
+  float2 w1p[MLP_IN][MLP_H / 2];   // lane l holds outputs 2l, 2l+1: w1p[k][l] = (W1[2l][k], W1[2l+1][k])
+  float2 b1p[MLP_H / 2];
+  float2 w2p[MLP_H][MLP_H / 2];
+  float2 b2p[MLP_H / 2];
+  float2 w3p[MLP_OUT][MLP_H / 2];
   float b3[MLP_OUT];
   float mean[MLP_IN], istd[MLP_IN];
-  float x[2][MLP_IN];   // per-warp scratch (warps 0 and 1 evaluate the network concurrently)
-  float h[2][MLP_H];
-  float s0t, s0r;       // reference widths sigma0
+  float4 x[2][MLP_IN / 4];   // per-warp scratch (warps 0 and 1 evaluate the network concurrently)
+  float4 h[2][MLP_H / 4];
+  float s0t, s0r;            // reference widths sigma0
   double s0t_d, s0r_d;
 };
 
 __device__ void mlp_load(MlpShared& m, const MlpDev& d) {
   for (int p = threadIdx.x; p < MLP_H * MLP_IN; p += blockDim.x) {
     const int o = p / MLP_IN, k = p % MLP_IN;
-    m.w1t[k][o] = d.w[MLP_W1 + p];
+    float* w = reinterpret_cast<float*>(&m.w1p[k][o >> 1]);
+    w[o & 1] = d.w[MLP_W1 + p];
   }
   for (int p = threadIdx.x; p < MLP_H * MLP_H; p += blockDim.x) {
     const int o = p / MLP_H, k = p % MLP_H;
-    m.w2t[k][o] = d.w[MLP_W2 + p];
+    float* w = reinterpret_cast<float*>(&m.w2p[k][o >> 1]);
+    w[o & 1] = d.w[MLP_W2 + p];
   }
   for (int p = threadIdx.x; p < MLP_H; p += blockDim.x) {
-    m.b1[p] = d.w[MLP_B1 + p];
-    m.b2[p] = d.w[MLP_B2 + p];
-    m.w3[0][p] = d.w[MLP_W3 + p];
-    m.w3[1][p] = d.w[MLP_W3 + MLP_H + p];
+    reinterpret_cast<float*>(m.b1p)[p] = d.w[MLP_B1 + p];
+    reinterpret_cast<float*>(m.b2p)[p] = d.w[MLP_B2 + p];
+    reinterpret_cast<float*>(m.w3p[0])[p] = d.w[MLP_W3 + p];
+    reinterpret_cast<float*>(m.w3p[1])[p] = d.w[MLP_W3 + MLP_H + p];
   }
   if (threadIdx.x < MLP_OUT) m.b3[threadIdx.x] = d.w[MLP_B3 + threadIdx.x];
   if (threadIdx.x < MLP_IN) { m.mean[threadIdx.x] = d.feat_mean[threadIdx.x]; m.istd[threadIdx.x] = d.feat_inv_std[threadIdx.x]; }
@@ -394,51 +402,56 @@ __device__ void mlp_load(MlpShared& m, const MlpDev& d) {
 }
 
 // Widths from integer features feat[] (one whole warp; lane 0's result is the
-// one used).  w selects the warp's scratch rows.  R: the pose precision.
+// one used).  w selects the warp's scratch rows.  R: the pose precision.  Lane
+// l computes hidden units 2l and 2l+1 with one 8-byte weight load per input
+// and four independent partial sums per unit; inputs are read four at a time.
 template <class R>
 __device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, R& st, R& sr) {
   const int lane = threadIdx.x & 31;
-  float* xs = m.x[w];
-  float* hs = m.h[w];
+  float* xs = reinterpret_cast<float*>(m.x[w]);
   if (lane < MLP_IN) xs[lane] = ((float)feat[lane] * FEAT_IQ - m.mean[lane]) * m.istd[lane];
   __syncwarp();
-  float h1[2];
+  float a0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, a1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int o = lane + 32 * u;
-    float s0 = m.b1[o], s1 = 0.0f;
+  for (int k4 = 0; k4 < MLP_IN / 4; ++k4) {
+    const float4 x = m.x[w][k4];
+    const float xv[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
-    for (int k = 0; k < MLP_IN; k += 2) {
-      s0 = fmaf(m.w1t[k][o], xs[k], s0);
-      s1 = fmaf(m.w1t[k + 1][o], xs[k + 1], s1);
+    for (int u = 0; u < 4; ++u) {
+      const float2 wt = m.w1p[4 * k4 + u][lane];
+      a0[u] = fmaf(wt.x, xv[u], a0[u]);
+      a1[u] = fmaf(wt.y, xv[u], a1[u]);
     }
-    h1[u] = tanhf(s0 + s1);
   }
+  const float2 b1 = m.b1p[lane];
+  const float h1a = tanhf(b1.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
+  const float h1b = tanhf(b1.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
+  reinterpret_cast<float2*>(m.h[w])[lane] = make_float2(h1a, h1b);
   __syncwarp();
-  hs[lane] = h1[0];
-  hs[lane + 32] = h1[1];
-  __syncwarp();
-  float h2[2];
 #pragma unroll
-  for (int u = 0; u < 2; ++u) {
-    const int o = lane + 32 * u;
-    float s0 = m.b2[o], s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+  for (int u = 0; u < 4; ++u) { a0[u] = 0.0f; a1[u] = 0.0f; }
 #pragma unroll
-    for (int k = 0; k < MLP_H; k += 4) {
-      s0 = fmaf(m.w2t[k][o], hs[k], s0);
-      s1 = fmaf(m.w2t[k + 1][o], hs[k + 1], s1);
-      s2 = fmaf(m.w2t[k + 2][o], hs[k + 2], s2);
-      s3 = fmaf(m.w2t[k + 3][o], hs[k + 3], s3);
+  for (int k4 = 0; k4 < MLP_H / 4; ++k4) {
+    const float4 x = m.h[w][k4];
+    const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float2 wt = m.w2p[4 * k4 + u][lane];
+      a0[u] = fmaf(wt.x, xv[u], a0[u]);
+      a1[u] = fmaf(wt.y, xv[u], a1[u]);
     }
-    h2[u] = tanhf((s0 + s1) + (s2 + s3));
   }
+  const float2 b2 = m.b2p[lane];
+  const float h2a = tanhf(b2.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
+  const float h2b = tanhf(b2.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
   float z[MLP_OUT];
 #pragma unroll
   for (int q = 0; q < MLP_OUT; ++q) {
-    float s = m.w3[q][lane] * h2[0] + m.w3[q][lane + 32] * h2[1];
+    const float2 w3 = m.w3p[q][lane];
+    float s = w3.x * h2a + w3.y * h2b;
 #pragma unroll
     for (int mm = 16; mm >= 1; mm >>= 1) s += __shfl_xor_sync(0xffffffffu, s, mm);
-    z[q] = __shfl_sync(0xffffffffu, s, 0) + m.b3[q];
+    z[q] = __shfl_sync(0xffffffffu, s, 0) + m.b3[q];   // lane 0's sum on every lane
   }
   __syncwarp();
   if constexpr (sizeof(R) == 4) {
@@ -459,23 +472,6 @@ struct QForm {
 };
 __device__ __forceinline__ QForm q_form(float st, float sr) {
   return QForm{-3.0f * (__logf(st) + __logf(sr)), 0.5f / (st * st), 0.5f / (sr * sr)};
-}
-
-// Queues of the molecules within the feature radius of the old (0) and new
-// (1) pose of the target: whole warps append with one ballot and one shared
-// atomic per warp.
-__device__ __forceinline__ void queue_push(int* q, int* count, bool in, int j, int* overflow) {
-  const unsigned m = __ballot_sync(0xffffffffu, in);
-  if (m == 0u) return;
-  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(count, __popc(m));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (in) {
-    const int pos = base + __popc(m & ((1u << lane) - 1u));
-    if (pos < MC_QMAX) q[pos] = j;
-    else *overflow = 1;
-  }
 }
 
 // One trial's proposal: widths, draws, the trial pose of the target and its
@@ -505,6 +501,15 @@ __device__ __forceinline__ void fl_distances(const McArgs& a, TP& P, int tg, con
   const uint32_t fo[3] = {P.fo[0], P.fo[1], P.fo[2]}, fn[3] = {P.fn[0], P.fn[1], P.fn[2]};
   P.fl_mo = fl_moved(a, tg, fo, fs);
   P.fl_mn = fl_moved(a, tg, fn, fs);
+  P.fl_epoch = epoch;
+}
+// The same from the reference position b, loaded ahead by the caller.
+template <class TP>
+__device__ __forceinline__ void fl_distances_from(TP& P, const uint32_t (&b)[3], const float fs[3], int epoch) {
+  const uint32_t fo[3] = {P.fo[0], P.fo[1], P.fo[2]}, fn[3] = {P.fn[0], P.fn[1], P.fn[2]};
+  float e[3];
+  P.fl_mo = sqrtf(fvec_fix(b, fo, fs, e));
+  P.fl_mn = sqrtf(fvec_fix(b, fn, fs, e));
   P.fl_epoch = epoch;
 }
 
@@ -651,6 +656,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   __shared__ int s_feat[MLP_IN];
   __shared__ R s_part[NEW];
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
+  __shared__ float s_qe[2][FEAT ? MC_QMAX : 1][3];   // their separations neighbour -> target pose
   __shared__ int s_nq[2];
   __shared__ int s_accept, s_hit;
   __shared__ float s_fl_moved;   // largest distance any molecule moved since the feature rows were built
@@ -705,17 +711,23 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         int tg = (int)(u[0] * nc);
         if (tg >= nc) tg = nc - 1;   // u = 1 would select nc (mc2.F90:551 quirk)
         s_tg[threadIdx.x] = tg;
-        s_lu[threadIdx.x] = (R)log(u[1]);
+        // Box-Muller normals (sine branch): FP32 functions for the FP32 trial poses
+        // of mixed precision (FP64 transcendentals cost tens of 64-cycle FP64
+        // instructions each), FP64 in the FP64 mode that replays the oracle
+        if constexpr (MIXED) s_lu[threadIdx.x] = logf((float)u[1]);
+        else s_lu[threadIdx.x] = log(u[1]);
 #pragma unroll 1
         for (int k = 0; k < 6; ++k) {
           uniform2(a.seed, (uint32_t)c, lo, hi, 1u + k, u);
-          s_g[k][threadIdx.x] = (R)(sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]));
+          if constexpr (MIXED) s_g[k][threadIdx.x] = sqrtf(-2.0f * logf((float)u[0])) * sinpif(2.0f * (float)u[1]);
+          else s_g[k][threadIdx.x] = sqrt(-2.0 * log(u[0])) * sin(2.0 * PI * u[1]);
         }
       }
       __syncthreads();
     }
     const int tg = i0 + s_tg[tb];
     TP& cur = s_pose[t & 1];
+    if (FEAT && threadIdx.x == 0) s_hit = 0;
     // ---- warp 0: the trial pose, unless it was built during the previous trial ----
     if (warp == 0 && cur.trial != t) {
       R st_w = sig_t_fixed, sr_w = sig_r_fixed;
@@ -818,53 +830,6 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         if constexpr (FEAT) {
           const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
           const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-          // queues of the molecules within 6.5 A of the old (0) and new (1) pose, from
-          // the target's feature row (or, when the move alone exceeds the skin, from
-          // the whole chain)
-          {
-            const bool all = s_fl_mode == 2;
-            const int* row = a.flist + (size_t)tg * MC_FL_CAP;
-            const int m = all ? nc : a.fnum[tg];
-            int cnt0 = 0, cnt1 = 0;
-            for (int p0 = 0; p0 < m; p0 += 32) {
-              const int p = p0 + lane;
-              bool qo = false, qn = false;
-              int j = -1;
-              if (p < m) {
-                j = all ? i0 + p : row[p];
-                if (j != tg) {
-                  float e[3], r2o, r2n;
-                  if (MIXED) {
-                    uint32_t fj[3];
-                    P::fix(a, j, fj);
-                    r2o = fvec_fix(fj, fo, fs, e);
-                    r2n = fvec_fix(fj, fn, fs, e);
-                  } else {
-                    double cj[3];
-                    P::com(a, j, cj);
-                    r2o = fvec_64(cj, co, L, iL, e);
-                    r2n = fvec_64(cj, cn, L, iL, e);
-                  }
-                  qo = r2o < FEAT_RC2 && r2o > 0.0f;
-                  qn = r2n < FEAT_RC2 && r2n > 0.0f;
-                }
-              }
-              const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
-              const unsigned lt = (1u << lane) - 1u;
-              if (qo) {
-                const int pos = cnt0 + __popc(mo & lt);
-                if (pos < MC_QMAX) s_q[0][pos] = j; else *a.flag = 1;
-              }
-              if (qn) {
-                const int pos = cnt1 + __popc(mn & lt);
-                if (pos < MC_QMAX) s_q[1][pos] = j; else *a.flag = 1;
-              }
-              cnt0 += __popc(mo);
-              cnt1 += __popc(mn);
-            }
-            if (lane == 0) { s_nq[0] = cnt0; s_nq[1] = cnt1; }
-            __syncwarp();
-          }
           int f[MLP_IN];
 #pragma unroll
           for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
@@ -873,14 +838,91 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           for (int s = 0; s < 4; ++s)
 #pragma unroll
             for (int k = 0; k < 3; ++k) un[s][k] = cur.un[s][k];
-          // features of the target at the new pose: terms of every queued neighbour
-          const int nn = min(s_nq[1], MC_QMAX);
-          for (int p = lane; p < nn; p += 32) {
-            const int j = s_q[1][p];
-            float e[3], r2;
-            if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fn, fj, fs, e); }
-            else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cn, cj, L, iL, e); }
-            feat_terms(e, r2, un, 1, f);
+          // Queues of the molecules within 6.5 A of the old (0) and new (1) pose, with
+          // their separations from the molecule's side (j -> target, kept for the
+          // cache update and for the features of the target at the new pose).  The candidates
+          // are the target's feature row, loaded a whole row at a time, or, when the
+          // move alone exceeds the skin, the whole chain.
+          {
+            int cnt0 = 0, cnt1 = 0;
+            // fj: the candidate's fixed-point COM, loaded by the caller (mixed)
+            auto take = [&](int j, bool valid, const uint32_t (&fj)[3]) {
+              bool qo = false, qn = false;
+              float eo[3] = {0.0f, 0.0f, 0.0f}, en[3] = {0.0f, 0.0f, 0.0f};
+              if (valid && j != tg) {
+                float r2o, r2n;
+                if (MIXED) {
+                  r2o = fvec_fix(fj, fo, fs, eo);
+                  r2n = fvec_fix(fj, fn, fs, en);
+                } else {
+                  double cj[3];
+                  P::com(a, j, cj);
+                  r2o = fvec_64(cj, co, L, iL, eo);
+                  r2n = fvec_64(cj, cn, L, iL, en);
+                }
+                qo = r2o < FEAT_RC2 && r2o > 0.0f;
+                qn = r2n < FEAT_RC2 && r2n > 0.0f;
+              }
+              const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
+              const unsigned lt = (1u << lane) - 1u;
+              if (qo) {
+                const int pos = cnt0 + __popc(mo & lt);
+                if (pos < MC_QMAX) {
+                  s_q[0][pos] = j;
+                  s_qe[0][pos][0] = eo[0]; s_qe[0][pos][1] = eo[1]; s_qe[0][pos][2] = eo[2];
+                } else {
+                  *a.flag = 1;
+                }
+              }
+              if (qn) {
+                const int pos = cnt1 + __popc(mn & lt);
+                if (pos < MC_QMAX) {
+                  s_q[1][pos] = j;
+                  s_qe[1][pos][0] = en[0]; s_qe[1][pos][1] = en[1]; s_qe[1][pos][2] = en[2];
+                } else {
+                  *a.flag = 1;
+                }
+              }
+              cnt0 += __popc(mo);
+              cnt1 += __popc(mn);
+            };
+            if (s_fl_mode == 2) {
+              for (int p0 = 0; p0 < nc; p0 += 32) {
+                const int j = i0 + p0 + lane;
+                uint32_t fj[3] = {0u, 0u, 0u};
+                if (MIXED && p0 + lane < nc) P::fix(a, j, fj);
+                take(j, p0 + lane < nc, fj);
+              }
+            } else {
+              // the whole row (its slots beyond fnum are ignored) and then the
+              // candidates' COMs, so that the loads are two round trips in all
+              constexpr int U = MC_FL_CAP / 32;
+              const int* row = a.flist + (size_t)tg * MC_FL_CAP;
+              int jr[U];
+#pragma unroll
+              for (int u = 0; u < U; ++u) jr[u] = row[32 * u + lane];
+              const int m = a.fnum[tg];
+              uint32_t fr[U][3];
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const bool ok = 32 * u + lane < m;
+                jr[u] = ok ? jr[u] : -1;
+                if (MIXED && ok) P::fix(a, jr[u], fr[u]);
+                else fr[u][0] = fr[u][1] = fr[u][2] = 0u;
+              }
+#pragma unroll
+              for (int u = 0; u < U; ++u)
+                if (32 * u < m) take(jr[u], jr[u] >= 0, fr[u]);
+            }
+            if (lane == 0) { s_nq[0] = cnt0; s_nq[1] = cnt1; }
+            __syncwarp();
+            // features of the target at the new pose, one queued neighbour per lane
+            // (target -> j is the exact negation of the stored separation)
+            const int nq1 = min(cnt1, MC_QMAX);
+            for (int p = lane; p < nq1; p += 32) {
+              const float et[3] = {-s_qe[1][p][0], -s_qe[1][p][1], -s_qe[1][p][2]};
+              feat_terms(et, dot3_rn(et, et), un, 1, f);
+            }
           }
 #pragma unroll
           for (int k = 0; k < MLP_IN; ++k) {
@@ -895,16 +937,20 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
         }
         if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
+          uint32_t b[3] = {0u, 0u, 0u};
+          if (FEAT && lane == 0) { b[0] = a.flfix[tg1]; b[1] = a.flfix[n + tg1]; b[2] = a.flfix[2 * n + tg1]; }
           build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL, fsi);
-          if (FEAT && lane == 0) fl_distances(a, s_pose[(t + 1) & 1], tg1, fs, s_fl_epoch);
+          if (FEAT && lane == 0) fl_distances_from(s_pose[(t + 1) & 1], b, fs, s_fl_epoch);
         }
       } else if constexpr (LEARN) {
         if (next_in_batch) {
           // warp 1: widths of the next trial's target at its current pose and its trial pose
+          uint32_t b[3] = {0u, 0u, 0u};
+          if (lane == 0) { b[0] = a.flfix[tg1]; b[1] = a.flfix[n + tg1]; b[2] = a.flfix[2 * n + tg1]; }
           R st1, sr1;
           mlp_widths_warp<R>(s_mlp, 1, fcl + (size_t)(tg1 - i0) * MLP_IN, st1, sr1);
           build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL, fsi);
-          if (lane == 0) fl_distances(a, s_pose[(t + 1) & 1], tg1, fs, s_fl_epoch);
+          if (lane == 0) fl_distances_from(s_pose[(t + 1) & 1], b, fs, s_fl_epoch);
         }
       }
     }
@@ -992,6 +1038,10 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
         }
         if (lane == 0) s_accept = acc_flag;
+        if (acc_flag) {   // the moved molecule's own cache entries: its new-pose features and site directions
+          if (lane < MLP_IN) fcl[(size_t)(tg - i0) * MLP_IN + lane] = s_feat[lane];
+          if (lane < 12) a.udir[(size_t)tg * 12 + lane] = cur.un[lane / 3][lane % 3];
+        }
       }
       __syncwarp();
     }
@@ -1001,26 +1051,17 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       __syncthreads();
       if (s_accept) {
         const int no = min(s_nq[0], MC_QMAX), ntot = no + min(s_nq[1], MC_QMAX);
-        const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-        const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
         const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
-        if (threadIdx.x == 0) s_hit = 0;
-        if ((int)threadIdx.x < MLP_IN) fcl[(size_t)(tg - i0) * MLP_IN + threadIdx.x] = s_feat[threadIdx.x];
-        else if ((int)threadIdx.x < MLP_IN + 12) {
-          const int q = threadIdx.x - MLP_IN;
-          a.udir[(size_t)tg * 12 + q] = cur.un[q / 3][q % 3];
-        }
-        __syncthreads();
         // four threads per neighbour entry, each adding a quarter of its terms
         for (int p = threadIdx.x; p < 4 * ntot; p += blockDim.x) {
           const int q = p >> 2, part = p & 3;
           const bool old_pose = q < no;
           const int j = old_pose ? s_q[0][q] : s_q[1][q - no];
           if (j == tg1) s_hit = 1;
-          float e[3], r2;
-          if (MIXED) { uint32_t fj[3]; P::fix(a, j, fj); r2 = fvec_fix(fj, old_pose ? fo : fn, fs, e); }
-          else { double cj[3]; P::com(a, j, cj); r2 = fvec_64(cj, old_pose ? co : cn, L, iL, e); }
-          feat_add_part(part, e, r2, a.udir + (size_t)j * 12, old_pose ? -1 : 1, fcl + (size_t)(j - i0) * MLP_IN);
+          const float* ep = old_pose ? s_qe[0][q] : s_qe[1][q - no];
+          const float e[3] = {ep[0], ep[1], ep[2]};
+          feat_add_part(part, e, dot3_rn(e, e), a.udir + (size_t)j * 12, old_pose ? -1 : 1,
+                        fcl + (size_t)(j - i0) * MLP_IN);
         }
         __syncthreads();
         // learned widths of the next trial were taken from features this move changed

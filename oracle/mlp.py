@@ -113,3 +113,71 @@ def loss_and_grad(p, rec, mean, istd, s0t, s0r, w_move=1.0, w_energy=0.0):
         g[W1:B1] += (d1h.T @ x).ravel()
         g[B1:W2] += d1h.sum(0)
     return loss, g
+
+
+def mc_run_learned(orc, model, path, com, quat, L, rin, rc, beta, p, mean, istd, s0t, s0r, ntrial, seed, chain,
+                   counter):
+    """Monte Carlo chain with learned widths on the CPU, the device's G6_MC_LEARNED
+    trial in FP64: the widths at the old pose from the features of the current
+    configuration, Gaussian rotation vector and translation scaled by them (same
+    Philox draws as the device: counter = chain, trial, draw), the widths at the
+    new pose, and the Metropolis-Hastings test
+    log u < -beta dE + log q(x|x') - log q(x'|x) with the isotropic Gaussian
+    densities of the two widths.  `orc` is the oracle module (energies, draws,
+    site placement).  Returns com, quat and a trace (ntrial, 4): dE, accepted,
+    target, log Hastings ratio."""
+    com = np.array(com, dtype=np.float64)
+    quat = np.array(quat, dtype=np.float64)
+    n = com.shape[0]
+    K = orc.constants()
+    conv = K["I2J"] * K["J2K"]
+    p = np.asarray(p, dtype=np.float64)
+    mean = np.asarray(mean, dtype=np.float64)
+    istd = np.asarray(istd, dtype=np.float64)
+    nq = orc.model_info(model)["nsite"] - 1
+
+    def widths_at(t, c, q):
+        intra = orc.place_sites(model, c[None, :], q[None, :])[3][0]
+        f = features(com, L, t, c, intra[1:1 + nq][:4])
+        z, _ = forward(p, ((f - mean) * istd)[None, :])
+        st, sr = widths(z, s0t, s0r)
+        return float(st[0]), float(sr[0])
+
+    def logq(st, sr, d2, r2):
+        return -3.0 * (np.log(st) + np.log(sr)) - d2 / (2 * st * st) - r2 / (2 * sr * sr)
+
+    trace = np.zeros((ntrial, 4))
+    for k in range(ntrial):
+        trial = counter + k
+        lo, hi = trial & 0xffffffff, trial >> 32
+        u0 = orc.philox_uniform2(seed, chain, lo, hi, 0)
+        t = min(int(u0[0] * n), n - 1)
+        g = []
+        for d in range(6):
+            a = orc.philox_uniform2(seed, chain, lo, hi, 1 + d)
+            g.append(np.sqrt(-2.0 * np.log(a[0])) * np.sin(2.0 * np.pi * a[1]))
+        st, sr = widths_at(t, com[t], quat[t])
+        rot = np.array(g[:3]) * sr
+        dx = np.array(g[3:]) * st
+        qr = np.array([1.0, rot[0], rot[1], rot[2]])
+        qr = qr / np.sqrt(qr @ qr)
+        a_, b_, c_, d_ = qr
+        qo = quat[t]
+        qn = np.array([a_ * qo[0] - b_ * qo[1] - c_ * qo[2] - d_ * qo[3], a_ * qo[1] + b_ * qo[0] + c_ * qo[3] - d_ * qo[2],
+                       a_ * qo[2] + c_ * qo[0] - b_ * qo[3] + d_ * qo[1], a_ * qo[3] + d_ * qo[0] + b_ * qo[2] - c_ * qo[1]])
+        if qn[0] < 0:
+            qn = -qn
+        cn = com[t] + dx
+        st2, sr2 = widths_at(t, cn, qn)
+        d2, r2 = float(dx @ dx), float(rot @ rot)
+        logh = logq(st2, sr2, d2, r2) - logq(st, sr, d2, r2)
+        eo = orc.molecule_energy(model, path, com, quat, t, com[t], quat[t], L, rin, rc)
+        en = orc.molecule_energy(model, path, com, quat, t, cn, qn, L, rin, rc)
+        dE = en - eo
+        x = -(dE * conv) * beta + logh
+        acc = x >= 0.0 or np.log(u0[1]) < x
+        if acc:
+            com[t] = cn
+            quat[t] = qn
+        trace[k] = (dE, 1.0 if acc else 0.0, t, logh)
+    return com, quat, trace

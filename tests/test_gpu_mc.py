@@ -192,3 +192,30 @@ def test_training_lowers_loss_and_learned_chain_is_consistent():
     for c in range(8):
         assert energy[c] == pytest.approx(ep[c], rel=2e-5, abs=0.05)
     assert (counts[:, 0] > 0).all()
+
+
+def test_learned_fp64_chain_replays_reference(orc):
+    """The FP64 learned-width chain (widths at both poses, Hastings term) follows
+    the CPU restatement trial by trial: same targets, same decisions, same end
+    state.  The network is random, so the widths vary from molecule to molecule
+    and from pose to pose."""
+    s, recs, rc = _chains("ST2", 2, 216, 90)
+    rng = np.random.default_rng(9)
+    p = rng.normal(0, 0.3, mlp.NPARAM).astype(np.float32)
+    mean = np.full(mlp.NIN, 0.5, np.float32); istd = np.full(mlp.NIN, 1.0, np.float32)
+    s._check(s.L.g6_mlp_set(s.ctx, fptr(p), fptr(mean), fptr(istd), 0.1, 0.1))
+    beta, ntrial = 1.0 / 260.0, 250
+    counts, energy, trace, _ = _mc(s, ntrial, 31, 0, beta, 0.1, 0.1, mode=_capi.MC_LEARNED)
+    rec_g = s.download_state()
+    for c, b in enumerate(recs):
+        com, quat, tr = mlp.mc_run_learned(orc, "ST2", "custom", b["com"], b["quat"], b["L"], rc - 2.0, rc, beta,
+                                           p, mean, istd, 0.1, 0.1, ntrial, 31, c, 0)
+        assert np.array_equal(trace[c, :, 3], tr[:, 2])          # same targets
+        assert np.array_equal(trace[c, :, 2], tr[:, 1])          # same decisions
+        assert 0 < tr[:, 1].sum() < ntrial
+        # the widths come from FP32 features and an FP32 network on the device
+        # (about 1e-6 relative), so the moves and their dE differ at that level
+        assert np.abs(trace[c, :, 0] - tr[:, 0]).max() <= 2e-5 * np.abs(tr[:, 0]).max()
+        sl = rec_g[216 * c:216 * (c + 1)]
+        assert np.abs(sl[:, :3] - com).max() < 1e-5
+        assert np.abs(sl[:, 33:37] - quat).max() < 1e-5

@@ -172,6 +172,32 @@ def test_md_mixed_conserves_energy():
     assert np.ptp(H) < 0.02 * ek
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_host_buffer_step_equals_device_step(prec):
+    """g6_md_step_host (state in a host buffer, copied in and out) gives the
+    same state, log and thermostat as one device-resident step from the same
+    state, on two calls in a row."""
+    n = 343
+    b = config.water_box("TIP4P", n, 12, temp=300.0, dt=0.002, jitter=0.2)
+    s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision=prec, rc=8.5)
+    s.upload_state(b["rec"])
+    s.md_run(0.002, 50, s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002))
+    rec = s.download_state()
+    th_a = s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002)
+    th_b = s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002)
+    host = rec.copy()
+    for _ in range(2):
+        ref_in = host.copy()
+        s.upload_state(ref_in)
+        log_a = s.md_run(0.002, 1, th_a)
+        want = s.download_state()
+        lg = np.zeros(10)
+        s.md_step_host(0.002, host, th_b, lg)
+        assert np.array_equal(host, want)
+        assert np.array_equal(lg, log_a[0, 0])
+        assert list(th_a[0].zeta) == list(th_b[0].zeta)
+
+
 def test_replicas_equal_separate_systems(orc):
     sizes = [216, 300, 250]
     boxes, recs = [], []
