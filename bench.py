@@ -483,17 +483,17 @@ def bench_rms(torch, rec_eq, L, snapshots=100, every=20):
             "against": "the FP64 path on the same configurations"}
 
 
-def bench_tip5p(torch, seed=20261205, melt=2000, steps=5000):
-    """32,768 TIP5P at 1.0 g/cm^3, rc 9 A (2 A switch), dt 1 fs: lattice melted
-    2,000 steps at 400 K (Nose-Hoover), velocities redrawn at 300 K, then NVE
-    for `steps` steps in mixed precision and in FP64 from the same state.
-    Energy drift = slope of a least-squares line through H per molecule
-    (kJ/mol) against time (ns)."""
+def bench_nve32k(torch, model="TIP5P", seed=20261205, melt=2000, steps=5000):
+    """32,768 molecules of `model` at 1.0 g/cm^3, rc 9 A (2 A switch), dt 1 fs:
+    lattice melted 2,000 steps at 400 K (Nose-Hoover), velocities redrawn at
+    300 K, then NVE for `steps` steps in mixed precision and in FP64 from the
+    same state.  Energy drift = slope of a least-squares line through H per
+    molecule (kJ/mol) against time (ns)."""
     from genesis6_gb300 import config
     dt = 0.001
     n = N_BIG
-    b = config.water_box("TIP5P", n, seed, temp=400.0, dt=dt)
-    s = make_system("TIP5P", n, "mixed", b["L"], b["rec"])
+    b = config.water_box(model, n, seed, temp=400.0, dt=dt)
+    s = make_system(model, n, "mixed", b["L"], b["rec"])
     q = 400.0 * TAU_NOSE ** 2 / dt
     s.md_run(dt, melt, s.thermostats(1, "nose", temp=400.0, q=q, dump=0.0), log=False)
     rec = s.download_state()
@@ -504,7 +504,7 @@ def bench_tip5p(torch, seed=20261205, melt=2000, steps=5000):
     for prec in ("mixed", "fp64"):
         if prec == "fp64":
             s.close()
-            s = make_system("TIP5P", n, "fp64", b["L"], start)
+            s = make_system(model, n, "fp64", b["L"], start)
         else:
             s.upload_state(start)
         th = s.thermostats(1, "nve")
@@ -615,7 +615,8 @@ def run_gpu(args, rank, world, local):
     rex = None if args.no_extra else bench_replicas(torch)
     mcb = None if args.no_extra else bench_mc(torch)
     rms = None if args.no_extra else bench_rms(torch, rec_eq, L)
-    t5p = None if (args.no_extra or args.no_32k) else bench_tip5p(torch)
+    t5p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP5P")
+    t4p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP4P", seed=20261206)
     line = {
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -624,6 +625,7 @@ def run_gpu(args, rank, world, local):
         "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
         "tip4p_32k": big,
         "tip5p_32k_nve": t5p,
+        "tip4p_32k_nve": t4p,
         "mixed_rms_error_4096": rms,
         "replica_exchange": rex,
         "mc_learned_vs_fixed": mcb,
