@@ -485,7 +485,7 @@ struct TrialPose {
   QForm qf;                         // proposal density form of the widths at the old pose
   R qn[4];                          // trial quaternion (the pose's precision)
   double qo64[4];                   // FP64 quaternion before the move
-  double q64[4];                    // FP64 quaternion after the move (FP64 mode; mixed: made on acceptance)
+  double q64[4];                    // FP64 quaternion after the move
   uint32_t fn[3], fo[3];            // new / old fixed-point COM
   float un[4][3];                   // charged-site directions at the new pose
   float d2, r2;                     // |dx|^2, |rot|^2
@@ -513,13 +513,42 @@ __device__ __forceinline__ void fl_distances_from(TP& P, const uint32_t (&b)[3],
   P.fl_epoch = epoch;
 }
 
+// FP64 quaternion of an accepted mixed-precision trial, component `lane` on
+// lanes 0-3 (all lanes call): qadd of QuatModule.F90:108-133 applied to the
+// FP64 quaternion as a float increment (qinfrotator(rot) - identity) (x) q_old,
+// with 1/sqrt(1+s) - 1 written without cancellation as
+// -s / (sqrt(1+s) (1 + sqrt(1+s))); then the sign with a >= 0 and |q| = 1
+// restored by the factor 1 - e/2 + 3e^2/8.
+template <class TP>
+__device__ __forceinline__ double accepted_q64(const TP& P, int lane) {
+  const double qv = lane < 4 ? P.qo64[lane & 3] : 0.0;
+  const float qf = (float)qv;
+  const float of0 = __shfl_sync(0xffffffffu, qf, 0), of1 = __shfl_sync(0xffffffffu, qf, 1);
+  const float of2 = __shfl_sync(0xffffffffu, qf, 2), of3 = __shfl_sync(0xffffffffu, qf, 3);
+  const float r0 = (float)P.rot[0], r1 = (float)P.rot[1], r2 = (float)P.rot[2];
+  const float s2 = r0 * r0 + r1 * r1 + r2 * r2, rs = sqrtf(1.0f + s2), inv = 1.0f / rs;
+  const float m0 = -s2 / (rs * (1.0f + rs)), b1 = r0 * inv, c1 = r1 * inv, d1 = r2 * inv;
+  const float dq0 = m0 * of0 - b1 * of1 - c1 * of2 - d1 * of3;
+  const float dq1 = m0 * of1 + b1 * of0 + c1 * of3 - d1 * of2;
+  const float dq2 = m0 * of2 + c1 * of0 - b1 * of3 + d1 * of1;
+  const float dq3 = m0 * of3 + d1 * of0 + b1 * of2 - c1 * of1;
+  const float dq = lane == 0 ? dq0 : (lane == 1 ? dq1 : (lane == 2 ? dq2 : dq3));
+  double q64 = qv + (double)dq;
+  if (of0 + dq0 < 0.0f) q64 = -q64;
+  double sq = lane < 4 ? q64 * q64 : 0.0;
+  sq += __shfl_xor_sync(0xffffffffu, sq, 1);
+  sq += __shfl_xor_sync(0xffffffffu, sq, 2);
+  const float ef = (float)(sq - 1.0);
+  return q64 + q64 * (double)(ef * (-0.5f + 0.375f * ef));
+}
+
 // Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot],
 // widths st_w, sr_w).  Register arrays are indexed with constants only
 // (selects), never by lane.  Mixed precision builds the pose in FP32 with no
-// FP64 arithmetic but the trial COM (the FP64 quaternion is made on
-// acceptance); the FP64 mode follows mc2's serial formulas in FP64, component
-// k on lane k, since an FP64 warp instruction costs the same whatever the
-// number of active lanes.
+// FP64 arithmetic but the trial COM and the FP64 quaternion an acceptance
+// would write (accepted_q64); the FP64 mode follows mc2's serial formulas in
+// FP64, component k on lane k, since an FP64 warp instruction costs the same
+// whatever the number of active lanes.
 template <class R, int NQ, bool MIXED>
 __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const R (*g)[MC_NB], int slot,
                             R st_w, R sr_w, const double iL[3], const float fsi[3]) {
@@ -606,35 +635,11 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
     P.trial = trial;
   }
   __syncwarp();
-}
-
-// FP64 quaternion of an accepted mixed-precision trial, component `lane` on
-// lanes 0-3 (all lanes call): qadd of QuatModule.F90:108-133 applied to the
-// FP64 quaternion as a float increment (qinfrotator(rot) - identity) (x) q_old,
-// with 1/sqrt(1+s) - 1 written without cancellation as
-// -s / (sqrt(1+s) (1 + sqrt(1+s))); then the sign with a >= 0 and |q| = 1
-// restored by the factor 1 - e/2 + 3e^2/8.
-template <class TP>
-__device__ __forceinline__ double accepted_q64(const TP& P, int lane) {
-  const double qv = lane < 4 ? P.qo64[lane & 3] : 0.0;
-  const float qf = (float)qv;
-  const float of0 = __shfl_sync(0xffffffffu, qf, 0), of1 = __shfl_sync(0xffffffffu, qf, 1);
-  const float of2 = __shfl_sync(0xffffffffu, qf, 2), of3 = __shfl_sync(0xffffffffu, qf, 3);
-  const float r0 = (float)P.rot[0], r1 = (float)P.rot[1], r2 = (float)P.rot[2];
-  const float s2 = r0 * r0 + r1 * r1 + r2 * r2, rs = sqrtf(1.0f + s2), inv = 1.0f / rs;
-  const float m0 = -s2 / (rs * (1.0f + rs)), b1 = r0 * inv, c1 = r1 * inv, d1 = r2 * inv;
-  const float dq0 = m0 * of0 - b1 * of1 - c1 * of2 - d1 * of3;
-  const float dq1 = m0 * of1 + b1 * of0 + c1 * of3 - d1 * of2;
-  const float dq2 = m0 * of2 + c1 * of0 - b1 * of3 + d1 * of1;
-  const float dq3 = m0 * of3 + d1 * of0 + b1 * of2 - c1 * of1;
-  const float dq = lane == 0 ? dq0 : (lane == 1 ? dq1 : (lane == 2 ? dq2 : dq3));
-  double q64 = qv + (double)dq;
-  if (of0 + dq0 < 0.0f) q64 = -q64;
-  double sq = lane < 4 ? q64 * q64 : 0.0;
-  sq += __shfl_xor_sync(0xffffffffu, sq, 1);
-  sq += __shfl_xor_sync(0xffffffffu, sq, 2);
-  const float ef = (float)(sq - 1.0);
-  return q64 + q64 * (double)(ef * (-0.5f + 0.375f * ef));
+  if (MIXED) {   // the FP64 quaternion an acceptance writes, prepared off the acceptance path
+    const double q = accepted_q64(P, lane);
+    if (lane < 4) P.q64[lane] = q;
+    __syncwarp();
+  }
 }
 
 template <int NQ, bool TAPER, bool MIXED, int MODE>
@@ -684,6 +689,10 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   // the chain's feature cache: shared memory when it fits, else its rows of a.fcache
   extern __shared__ int s_fcdyn[];
   int* const fcl = a.fc_smem ? s_fcdyn : a.fcache + (size_t)i0 * MLP_IN;
+  // with the cache in shared memory, the site directions of the queued
+  // neighbours are copied there too (asynchronously, while the control warps
+  // work), for the cache update of an acceptance: 2 x MC_QMAX rows of 12 floats
+  float* const s_ud = reinterpret_cast<float*>(s_fcdyn + (size_t)a.ncmax * MLP_IN);
   if constexpr (FEAT) {
     init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
     build_flists(a, i0, i1, fs);
@@ -865,11 +874,23 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
               }
               const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
               const unsigned lt = (1u << lane) - 1u;
+              // with the cache in shared memory, the neighbour's site directions are
+              // copied next to the queue (asynchronously) for the cache update
+              auto stage_dirs = [&](int slot) {
+                if (a.fc_smem) {
+                  const unsigned dst = (unsigned)__cvta_generic_to_shared(s_ud + (size_t)slot * 12);
+                  const float* src = a.udir + (size_t)j * 12;
+                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 16), "l"(src + 4) : "memory");
+                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 32), "l"(src + 8) : "memory");
+                }
+              };
               if (qo) {
                 const int pos = cnt0 + __popc(mo & lt);
                 if (pos < MC_QMAX) {
                   s_q[0][pos] = j;
                   s_qe[0][pos][0] = eo[0]; s_qe[0][pos][1] = eo[1]; s_qe[0][pos][2] = eo[2];
+                  stage_dirs(pos);
                 } else {
                   *a.flag = 1;
                 }
@@ -879,6 +900,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
                 if (pos < MC_QMAX) {
                   s_q[1][pos] = j;
                   s_qe[1][pos][0] = en[0]; s_qe[1][pos][1] = en[1]; s_qe[1][pos][2] = en[2];
+                  stage_dirs(MC_QMAX + pos);
                 } else {
                   *a.flag = 1;
                 }
@@ -916,6 +938,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
             }
             if (lane == 0) { s_nq[0] = cnt0; s_nq[1] = cnt1; }
             __syncwarp();
+            if (a.fc_smem) asm volatile("cp.async.commit_group;" ::: "memory");
             // features of the target at the new pose, one queued neighbour per lane
             // (target -> j is the exact negation of the stored separation)
             const int nq1 = min(cnt1, MC_QMAX);
@@ -984,9 +1007,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         // site offsets of the packed pose are not kept during a run: the Monte
         // Carlo kernel reads only the COM of pk64, and every other caller places
         // the molecules again from the state.
-        double q64;
-        if constexpr (MIXED) q64 = accepted_q64(cur, lane);
-        else q64 = cur.q64[lane & 3];
+        const double q64 = cur.q64[lane & 3];
         double* p = a.pk64 + (size_t)tg * W64;
         float* pf = a.pk32f + (size_t)tg * 4 * NPK;
         if (lane < 4) a.st[(size_t)(33 + lane) * n + tg] = q64;
@@ -1038,6 +1059,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
         }
         if (lane == 0) s_accept = acc_flag;
+        if (a.fc_smem) asm volatile("cp.async.wait_all;" ::: "memory");   // the staged directions have landed
         if (acc_flag) {   // the moved molecule's own cache entries: its new-pose features and site directions
           if (lane < MLP_IN) fcl[(size_t)(tg - i0) * MLP_IN + lane] = s_feat[lane];
           if (lane < 12) a.udir[(size_t)tg * 12 + lane] = cur.un[lane / 3][lane % 3];
@@ -1060,8 +1082,8 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           if (j == tg1) s_hit = 1;
           const float* ep = old_pose ? s_qe[0][q] : s_qe[1][q - no];
           const float e[3] = {ep[0], ep[1], ep[2]};
-          feat_add_part(part, e, dot3_rn(e, e), a.udir + (size_t)j * 12, old_pose ? -1 : 1,
-                        fcl + (size_t)(j - i0) * MLP_IN);
+          const float* u = a.fc_smem ? s_ud + (size_t)(old_pose ? q : MC_QMAX + (q - no)) * 12 : a.udir + (size_t)j * 12;
+          feat_add_part(part, e, dot3_rn(e, e), u, old_pose ? -1 : 1, fcl + (size_t)(j - i0) * MLP_IN);
         }
         __syncthreads();
         // learned widths of the next trial were taken from features this move changed
@@ -1086,7 +1108,7 @@ static cudaError_t launch_mc_k(McArgs a, cudaStream_t s) {
   const size_t fc_bytes = (size_t)a.ncmax * MLP_IN * sizeof(int);
   size_t dyn = 0;
   if (MODE != G6_MC_PLAIN && fc_bytes <= MC_FC_SMEM_MAX) {
-    dyn = fc_bytes;
+    dyn = fc_bytes + (size_t)2 * MC_QMAX * 12 * sizeof(float);   // cache + staged site directions
     cudaError_t e = cudaFuncSetAttribute(k_mc<NQ, TAPER, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)dyn);
     if (e != cudaSuccess) return e;
