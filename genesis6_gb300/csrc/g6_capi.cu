@@ -390,7 +390,8 @@ static int prepare_list(g6_ctx* ctx) {
   if (ctx->glist.valid && ctx->cap > 0) return G6_OK;
   const double skin = effective_skin(ctx);
   const double rlist = ctx->cc.rout + skin;
-  int rc = build_grid(ctx, ctx->glist, rlist, false);
+  // cells of at least half the list radius (list_row visits two cells each way)
+  int rc = build_grid(ctx, ctx->glist, 0.5 * rlist, false);
   if (rc) return rc;
   double rho = 0.0;
   for (int r = 0; r < ctx->nrep; ++r) {

@@ -167,8 +167,12 @@ cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream
 }
 
 // ---------------------------------------------------------------------------
-// Neighbour list.  One warp per molecule.
-// ---------------------------------------------------------------------------
+// Neighbour list.  One warp per molecule.  The list grid has cells of at least
+// half the list radius, so the neighbours lie within two cells in every
+// dimension: the 5 x 5 stencil rows of 5 consecutive x-cells are contiguous in
+// the cell-sorted molecule array (two ranges where a row wraps), and a warp
+// scans each row range 32 candidates at a time.  A dimension of fewer than 5
+// cells is scanned whole.
 __device__ void list_row(const ListArgs& a, int i, int lane) {
   const int n = a.n;
   const int r = a.rep.mol_rep[i];
@@ -179,20 +183,28 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
   const uint32_t* fix = (a.ctrl != nullptr && (a.ctrl[1] & 1)) ? a.fix1 : a.fix;
   const uint32_t xi = fix[i], yi = fix[n + i], zi = fix[2 * n + i];
   const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
-  // distinct neighbour offsets per dimension: {-1,0,1} (nd>=3), {0,1} (nd==2), {0} (nd==1)
-  const int lox = nx >= 3 ? -1 : 0, hix = nx >= 2 ? 1 : 0;
-  const int loy = ny >= 3 ? -1 : 0, hiy = ny >= 2 ? 1 : 0;
-  const int loz = nz >= 3 ? -1 : 0, hiz = nz >= 2 ? 1 : 0;
+  // the cells of y and z to visit: cy-2..cy+2 (mod n) or every cell of a short dimension
+  const int y0 = ny >= 5 ? cy - 2 : 0, y1 = ny >= 5 ? cy + 2 : ny - 1;
+  const int z0 = nz >= 5 ? cz - 2 : 0, z1 = nz >= 5 ? cz + 2 : nz - 1;
+  // x-ranges of a row: [xa, xb] and, after a wrap, [0, xc]
+  int xa, xb, xc = -1;
+  if (nx >= 5) {
+    xa = cx - 2; xb = cx + 2;
+    if (xa < 0) { xc = xb; xa += nx; xb = nx - 1; }
+    else if (xb >= nx) { xc = xb - nx; xb = nx - 1; }
+  } else {
+    xa = 0; xb = nx - 1;
+  }
   int* row = a.nbr + (size_t)i * a.cap;
   int cnt = 0;
-  for (int oz = loz; oz <= hiz; ++oz) {
-    const int zz = (cz + oz + nz) % nz;
-    for (int oy = loy; oy <= hiy; ++oy) {
-      const int yy = (cy + oy + ny) % ny;
-      for (int ox = lox; ox <= hix; ++ox) {
-        const int xx = (cx + ox + nx) % nx;
-        const int c = a.g.cell_off[r] + (zz * ny + yy) * nx + xx;
-        const int b = a.start[c], e = a.start[c + 1];
+  for (int oz = z0; oz <= z1; ++oz) {
+    const int zz = (oz + nz) % nz;
+    for (int oy = y0; oy <= y1; ++oy) {
+      const int yy = (oy + ny) % ny;
+      const int base = a.g.cell_off[r] + (zz * ny + yy) * nx;
+      for (int part = 0; part < 2; ++part) {
+        if (part == 1 && xc < 0) break;
+        const int b = a.start[base + (part == 0 ? xa : 0)], e = a.start[base + (part == 0 ? xb : xc) + 1];
         for (int k0 = b; k0 < e; k0 += 32) {
           const int k = k0 + lane;
           bool in = false;
