@@ -166,6 +166,7 @@ struct HostGrid {
   int ncell = 0;
   int* d_nd = nullptr; double* d_edge = nullptr; double* d_icell = nullptr; int* d_cell_off = nullptr;
   int* d_cell = nullptr; int* d_slot = nullptr; int* d_count = nullptr; int* d_start = nullptr; int* d_cellmol = nullptr;
+  uint4* d_cellfix = nullptr;
   bool valid = false;
 };
 
@@ -343,7 +344,7 @@ static int build_grid(g6_ctx* ctx, HostGrid& g, double edge, bool with_stencil) 
   if (!g.d_nd) {
     CK(dalloc(ctx, &g.d_nd, 3 * R)); CK(dalloc(ctx, &g.d_edge, 3 * R)); CK(dalloc(ctx, &g.d_icell, 3 * R));
     CK(dalloc(ctx, &g.d_cell_off, R + 1)); CK(dalloc(ctx, &g.d_cell, n)); CK(dalloc(ctx, &g.d_slot, n));
-    CK(dalloc(ctx, &g.d_cellmol, n));
+    CK(dalloc(ctx, &g.d_cellmol, n)); CK(dalloc(ctx, &g.d_cellfix, n));
   }
   // cell-count arrays are sized per grid (re-allocated if the grid grows)
   CK(dalloc(ctx, &g.d_count, g.ncell + 1));
@@ -440,6 +441,7 @@ static ListArgs list_args(g6_ctx* c, const int* ctrl) {
   std::memset(&a, 0, sizeof a);
   a.n = c->n; a.cap = c->cap; a.rep = rep_dev(c); a.g = grid_dev(c->glist); a.cell = c->glist.d_cell;
   a.start = c->glist.d_start; a.cellmol = c->glist.d_cellmol; a.fix = c->d_fix; a.fix1 = c->d_fix1; a.com = c->d_st;
+  a.cellfix = c->glist.d_cellfix;
   a.com_build = c->d_com_build;
   a.fix_build = c->d_fix_build;
   const double rl = c->cc.rout + effective_skin(c);

@@ -113,13 +113,21 @@ __global__ void k_cell_fill(CellArgs a, const int* start, int* cellmol) {
   if (i < a.n) cellmol[start[a.cell[i]] + a.slot[i]] = i;
 }
 
+// (fixed-point COM, molecule) of cell-sorted slot k, so that the row scan reads
+// one coalesced 16-byte word per candidate instead of an index and a gather.
+__device__ __forceinline__ void fill_cellfix(const ListArgs& a, int k) {
+  const uint32_t* fix = (a.ctrl != nullptr && (a.ctrl[1] & 1)) ? a.fix1 : a.fix;
+  const int j = a.cellmol[k];
+  a.cellfix[k] = make_uint4(fix[j], fix[a.n + j], fix[2 * a.n + j], (uint32_t)j);
+}
+
 // Residents of one cell in molecule order, sorted by one warp: every lane
 // holds up to 8 ids and computes their ranks (ids are distinct); cells larger
 // than 256 fall back to an insertion sort by lane 0.
-__device__ void sort_cell_warp(int* cellmol, int b, int e, int lane) {
+__device__ void sort_cell_warp(int* cellmol, int b, int e, int lane, const ListArgs* fill = nullptr) {
   const int m = e - b;
-  if (m <= 1) return;
-  if (m <= 256) {
+  if (m <= 1) {
+  } else if (m <= 256) {
     int v[8], r[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) { v[c] = (lane + 32 * c < m) ? cellmol[b + lane + 32 * c] : 0x7fffffff; r[c] = 0; }
@@ -147,6 +155,10 @@ __device__ void sort_cell_warp(int* cellmol, int b, int e, int lane) {
       cellmol[q + 1] = v;
     }
   }
+  if (fill) {   // the cell's (fixed-point COM, molecule) words in sorted order
+    __syncwarp();
+    for (int k = b + lane; k < e; k += 32) fill_cellfix(*fill, k);
+  }
 }
 
 __global__ void k_cell_sort(const int* start, int* cellmol, int ncell, const int* ctrl) {
@@ -169,10 +181,12 @@ cudaError_t launch_cells(const CellArgs& a, int* start, int* cellmol, cudaStream
 // ---------------------------------------------------------------------------
 // Neighbour list.  One warp per molecule.  The list grid has cells of at least
 // half the list radius, so the neighbours lie within two cells in every
-// dimension: the 5 x 5 stencil rows of 5 consecutive x-cells are contiguous in
-// the cell-sorted molecule array (two ranges where a row wraps), and a warp
-// scans each row range 32 candidates at a time.  A dimension of fewer than 5
-// cells is scanned whole.
+// dimension: the (at most) 5 x 5 stencil rows of 5 consecutive x-cells, each
+// contiguous in the cell-sorted arrays (two ranges where a row wraps); a
+// dimension of fewer than 5 cells is taken whole.  Lane r scans row r on its
+// own (independent loads, so several are in flight at once): a counting pass,
+// a warp prefix sum of the counts, and a writing pass.  The row order of the
+// result is stencil row by stencil row, each in cell-sorted order.
 __device__ void list_row(const ListArgs& a, int i, int lane) {
   const int n = a.n;
   const int r = a.rep.mol_rep[i];
@@ -183,9 +197,8 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
   const uint32_t* fix = (a.ctrl != nullptr && (a.ctrl[1] & 1)) ? a.fix1 : a.fix;
   const uint32_t xi = fix[i], yi = fix[n + i], zi = fix[2 * n + i];
   const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
-  // the cells of y and z to visit: cy-2..cy+2 (mod n) or every cell of a short dimension
-  const int y0 = ny >= 5 ? cy - 2 : 0, y1 = ny >= 5 ? cy + 2 : ny - 1;
-  const int z0 = nz >= 5 ? cz - 2 : 0, z1 = nz >= 5 ? cz + 2 : nz - 1;
+  const int ky = ny >= 5 ? 5 : ny, kz = nz >= 5 ? 5 : nz;   // rows of y and z to visit
+  const int y0 = ny >= 5 ? cy - 2 : 0, z0 = nz >= 5 ? cz - 2 : 0;
   // x-ranges of a row: [xa, xb] and, after a wrap, [0, xc]
   int xa, xb, xc = -1;
   if (nx >= 5) {
@@ -195,42 +208,46 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
   } else {
     xa = 0; xb = nx - 1;
   }
-  int* row = a.nbr + (size_t)i * a.cap;
+  // this lane's stencil row
+  int b0 = 0, e0 = 0, b1 = 0, e1 = 0;
+  if (lane < ky * kz) {
+    const int yy = (y0 + lane % ky + ny) % ny, zz = (z0 + lane / ky + nz) % nz;
+    const int base = a.g.cell_off[r] + (zz * ny + yy) * nx;
+    b0 = a.start[base + xa]; e0 = a.start[base + xb + 1];
+    if (xc >= 0) { b1 = a.start[base]; e1 = a.start[base + xc + 1]; }
+  }
+  auto near = [&](const uint4& q) {
+    const float dx = (float)(int)(xi - q.x) * sx;
+    const float dy = (float)(int)(yi - q.y) * sy;
+    const float dz = (float)(int)(zi - q.z) * sz;
+    return (int)q.w != i && dx * dx + dy * dy + dz * dz < a.rlist2;
+  };
   int cnt = 0;
-  for (int oz = z0; oz <= z1; ++oz) {
-    const int zz = (oz + nz) % nz;
-    for (int oy = y0; oy <= y1; ++oy) {
-      const int yy = (oy + ny) % ny;
-      const int base = a.g.cell_off[r] + (zz * ny + yy) * nx;
-      for (int part = 0; part < 2; ++part) {
-        if (part == 1 && xc < 0) break;
-        const int b = a.start[base + (part == 0 ? xa : 0)], e = a.start[base + (part == 0 ? xb : xc) + 1];
-        for (int k0 = b; k0 < e; k0 += 32) {
-          const int k = k0 + lane;
-          bool in = false;
-          int j = -1;
-          if (k < e) {
-            j = a.cellmol[k];
-            if (j != i) {
-              float dx = (float)(int)(xi - fix[j]) * sx;
-              float dy = (float)(int)(yi - fix[n + j]) * sy;
-              float dz = (float)(int)(zi - fix[2 * n + j]) * sz;
-              in = dx * dx + dy * dy + dz * dz < a.rlist2;
-            }
-          }
-          const unsigned m = __ballot_sync(0xffffffffu, in);
-          if (in) {
-            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-            if (pos < a.cap) row[pos] = j;
-          }
-          cnt += __popc(m);
-        }
-      }
-    }
+#pragma unroll 4
+  for (int k = b0; k < e0; ++k) cnt += near(a.cellfix[k]) ? 1 : 0;
+#pragma unroll 4
+  for (int k = b1; k < e1; ++k) cnt += near(a.cellfix[k]) ? 1 : 0;
+  int pre = cnt;   // inclusive warp prefix sum
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, pre, d);
+    if (lane >= d) pre += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, pre, 31);
+  int pos = pre - cnt;
+  int* row = a.nbr + (size_t)i * a.cap;
+  for (int k = b0; k < e0; ++k) {
+    const uint4 q = a.cellfix[k];
+    if (near(q)) { if (pos < a.cap) row[pos] = (int)q.w; ++pos; }
+  }
+  for (int k = b1; k < e1; ++k) {
+    const uint4 q = a.cellfix[k];
+    if (near(q)) { if (pos < a.cap) row[pos] = (int)q.w; ++pos; }
   }
   if (lane == 0) {
-    if (cnt > a.cap) { atomicExch(a.overflow, 1); cnt = a.cap; }
-    a.nnb[i] = cnt;
+    int c = total;
+    if (c > a.cap) { atomicExch(a.overflow, 1); c = a.cap; }
+    a.nnb[i] = c;
     a.com_build[i] = a.com[i];
     a.com_build[n + i] = a.com[n + i];
     a.com_build[2 * n + i] = a.com[2 * n + i];
@@ -240,6 +257,12 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
       a.fix_build[2 * n + i] = zi;
     }
   }
+}
+
+__global__ void k_cell_fix(ListArgs a) {
+  if (skip_ctrl(a.ctrl)) return;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < a.n) fill_cellfix(a, k);
 }
 
 __global__ void __launch_bounds__(128) k_list_build(ListArgs a) {
@@ -336,7 +359,7 @@ __global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
   grid.sync();
   for (int i = gt; i < n; i += gs) a.cellmol[a.start[a.c.cell[i]] + a.c.slot[i]] = i;
   grid.sync();
-  for (int c = gw; c < nc; c += nw) sort_cell_warp(a.cellmol, a.start[c], a.start[c + 1], lane);
+  for (int c = gw; c < nc; c += nw) sort_cell_warp(a.cellmol, a.start[c], a.start[c + 1], lane, &a.l);
   grid.sync();
   for (int i = gw; i < n; i += nw) list_row(a.l, i, lane);
 }
@@ -366,6 +389,7 @@ cudaError_t launch_rebuild(const CellArgs& c, const ListArgs& l, int* start, int
 cudaError_t launch_list(const ListArgs& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   const long long threads = (long long)a.n * 32;
+  k_cell_fix<<<(a.n + 255) / 256, 256, 0, s>>>(a);
   k_list_build<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(a);
   return cudaGetLastError();
 }

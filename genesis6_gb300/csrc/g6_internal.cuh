@@ -238,6 +238,7 @@ struct ListArgs {
   int* nnb;
   int* overflow;
   const int* ctrl;
+  uint4* cellfix;        // n: (fixed-point COM, molecule) of each cell-sorted slot, filled before the rows
 };
 
 struct PairSetArgs {

@@ -11,7 +11,7 @@
 // What it does: the same kernels as g6_force (site placement, cell build,
 // neighbour list, force, collect) on one system of at most
 // G6_NOALLOC_MAX_MOL molecules.  All intermediate tables live in one
-// file-scope __device__ array (g6_noalloc_scratch, 7,129,856 bytes (6.8 MiB)), which every
+// file-scope __device__ array (g6_noalloc_scratch, 7,195,392 bytes (6.9 MiB)), which every
 // GPU that loads the library holds until the process exits.  Inputs and
 // outputs are device pointers owned by the caller.
 //
@@ -75,7 +75,8 @@ constexpr size_t O_CELLMOL = O_START + al((size_t)(MAXCELL + 1) * 4);
 constexpr size_t O_NBR = O_CELLMOL + al((size_t)MAXN * 4);
 constexpr size_t O_NNB = O_NBR + al((size_t)MAXN * CAP * 4);
 constexpr size_t O_COMB = O_NNB + al((size_t)MAXN * 4);
-constexpr size_t O_OVF = O_COMB + al(3ull * MAXN * 8);
+constexpr size_t O_CFIX = O_COMB + al(3ull * MAXN * 8);
+constexpr size_t O_OVF = O_CFIX + al((size_t)MAXN * 16);
 constexpr size_t BYTES = O_OVF + al(4);
 
 }  // namespace noalloc
@@ -226,7 +227,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   la.n = n; la.cap = CAP; la.rep = rep; la.g = g; la.cell = ca.cell; la.start = (const int*)(base + O_START);
   la.cellmol = (const int*)(base + O_CELLMOL); la.fix = pa.fix; la.fix1 = pa.fix; la.com = pa.st; la.com_build = (double*)(base + O_COMB);
   la.rlist2 = (float)(rlist * rlist) + 1e-3f; la.nbr = (int*)(base + O_NBR); la.nnb = (int*)(base + O_NNB);
-  la.overflow = (int*)(base + O_OVF); la.ctrl = nullptr;
+  la.overflow = (int*)(base + O_OVF); la.ctrl = nullptr; la.cellfix = (uint4*)(base + O_CFIX);
 
   ForceArgs fa;
   std::memset(&fa, 0, sizeof fa);

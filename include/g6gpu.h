@@ -265,7 +265,7 @@ int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, d
    larger n returns G6_ERR_CAPACITY.  d_com (n,3), d_quat (n,4) are device
    inputs; d_F (n,3), d_tau (n,3, body frame) and d_epot (1) are device
    outputs; box (3) is host memory; stream is a cudaStream_t (NULL = default).
-   Intermediate tables live in one static device array of 7,129,856 bytes (6.8 MiB) that
+   Intermediate tables live in one static device array of 7,195,392 bytes (6.9 MiB) that
    every GPU loading the library keeps until exit.  The first call on a device
    looks up that array's address: make it before any stream capture.  All
    calls share the array, so calls that overlap on the GPU race; serialise
