@@ -56,10 +56,11 @@ def parse():
     p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
-    p.add_argument("--profile", choices=["md", "mc"], default=None,
+    p.add_argument("--profile", choices=["md", "mc", "mc-learned"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
-                        "TIP4P-4096 (mixed, Nose 300 K, one g6_md_run), 'mc' = two runs of --steps trials on "
-                        "32 chains x 1,024 ST2 (fixed widths)")
+                        "TIP4P-4096 (mixed, Nose 300 K, one g6_md_run); 'mc' = two runs of --steps trials on "
+                        "32 chains x 1,024 ST2 (fixed widths) from a short MD start; 'mc-learned' = the same "
+                        "with the network trained on 32,768 records first, then learned widths")
     return p.parse_args()
 
 
@@ -657,16 +658,18 @@ def run_profile(args):
         print("md ok: %d steps, last T %.1f K" % (args.steps, float(log[-1, 0, 3])))
     else:
         C, N, seed = 32, 1024, 20261203
-        boxes, recs = [], []
-        for c in range(C):
-            b = config.water_box("ST2", N, seed + 500 + c, temp=260.0)
-            boxes.append(b["L"]); recs.append(b["rec"])
-        s = g6.RigidWater("ST2", [N] * C, np.array(boxes), path="custom", precision="mixed", rc=9.0, switch=2.0,
-                          skin=0.0)
-        s.upload_state(np.concatenate(recs))
-        for rep in range(2):
-            r = s.mc_run(args.steps, seed, rep * args.steps, 1.0 / 260.0)
-        print("mc ok: acceptance %.3f" % (r["accepted"].sum() / r["trials"].sum()))
+        boxes, rec0, _ = mc_chains(C, N, 260.0, 9.0, seed, melt_steps=1000, md_steps=2000)
+        s = g6.RigidWater("ST2", [N] * C, boxes, path="custom", precision="mixed", rc=9.0, switch=2.0, skin=0.0)
+        s.upload_state(rec0)
+        mode = "plain"
+        if args.profile == "mc-learned":
+            s.mc_run(1024, seed, 10 ** 8, 1.0 / 260.0, mode="collect")
+            s._check(s.L.g6_mlp_objective(s.ctx, 0.0, 1.0))
+            s._check(s.L.g6_mlp_train(s.ctx, 1, 1024, 2e-3, seed, 0.15, 0.15, None))
+            mode = "learned"
+        for k in range(2):
+            r = s.mc_run(args.steps, seed, k * args.steps, 1.0 / 260.0, mode=mode)
+        print("mc ok (%s): acceptance %.3f" % (mode, r["accepted"].sum() / r["trials"].sum()))
     s.close()
 
 
