@@ -53,6 +53,7 @@ constexpr float FEAT_Q = 1048576.0f;  // feature terms are integers of 2^-20
 constexpr float FEAT_IQ = 1.0f / 1048576.0f;
 constexpr float FEAT_RC2 = 6.5f * 6.5f;
 constexpr int MC_QMAX = 128;          // feature neighbours per pose (about 40 in liquid water)
+constexpr int MC_SEG = 96;            // molecules within rc kept per energy warp and trial
 
 template <int NQ, bool TAPER, class R>
 __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 1][3], const R (&rj)[NQ + 1][3],
@@ -660,6 +661,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   __shared__ TP s_pose[2];
   __shared__ int s_feat[MLP_IN];
   __shared__ R s_part[NEW];
+  __shared__ int s_seg[NEW][MC_SEG];   // each energy warp's molecules within rc of either pose
   __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
   __shared__ float s_qe[2][FEAT ? MC_QMAX : 1][3];   // their separations neighbour -> target pose
   __shared__ int s_nq[2];
@@ -782,10 +784,8 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         for (int k = 0; k < 3; ++k) { ro[s][k] = cur.oo[s][k]; rn[s][k] = cur.on[s][k]; }
       const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
       const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-      for (int j = i0 + (int)threadIdx.x - E0; j < i1; j += NE) {
-        if (j == tg) continue;
-        R dO[3], dN[3], ddO, ddN;
-        bool inO, inN;
+      // separation of molecule j from both poses and the strict rc tests
+      auto separations = [&](int j, R (&dO)[3], R (&dN)[3], R& ddO, R& ddN, bool& inO, bool& inN) {
         if (MIXED) {
           uint32_t fj[3];
           P::fix(a, j, fj);
@@ -817,16 +817,51 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           ddN = (R)d1;
           inN = d1 < a.cc.rout2;
         }
-        if (inO || inN) {
-          R rj[NQ + 1][3];
+      };
+      // e(new, j) - e(old, j)
+      auto pair_dE = [&](int j, const R (&dO)[3], const R (&dN)[3], R ddO, R ddN, bool inO, bool inN) {
+        R rj[NQ + 1][3];
 #pragma unroll
-          for (int s = 0; s <= NQ; ++s)
+        for (int s = 0; s <= NQ; ++s)
 #pragma unroll
-            for (int k = 0; k < 3; ++k)
-              rj[s][k] = MIXED ? (R)a.pk32f[(size_t)j * 4 * NPK + 3 + 3 * s + k] : (R)a.pk64[(size_t)j * W64 + 3 + 3 * s + k];
-          if (inO) acc -= pair_energy<NQ, TAPER, R>(dO, ddO, ro, rj, a.pc, rin2, rin, rout, c1);
-          if (inN) acc += pair_energy<NQ, TAPER, R>(dN, ddN, rn, rj, a.pc, rin2, rin, rout, c1);
+          for (int k = 0; k < 3; ++k)
+            rj[s][k] = MIXED ? (R)a.pk32f[(size_t)j * 4 * NPK + 3 + 3 * s + k] : (R)a.pk64[(size_t)j * W64 + 3 + 3 * s + k];
+        R v = R(0);
+        if (inO) v -= pair_energy<NQ, TAPER, R>(dO, ddO, ro, rj, a.pc, rin2, rin, rout, c1);
+        if (inN) v += pair_energy<NQ, TAPER, R>(dN, ddN, rn, rj, a.pc, rin2, rin, rout, c1);
+        return v;
+      };
+      // Pass 1: the rc tests for this warp's molecules, the ones within rc of
+      // either pose appended (ballot order) to the warp's segment, so that the
+      // pair energies below run with full lanes instead of one site-loop pass
+      // per 32 molecules with a few lanes each.  Entries beyond the segment's
+      // capacity are summed at once.  Both passes run in a fixed order.
+      const int ew = warp - NCTRL;
+      int* seg = s_seg[ew];
+      int nseg = 0;
+      for (int j0 = i0 + 32 * ew; j0 < i1; j0 += NE) {
+        const int j = j0 + lane;
+        R dO[3], dN[3], ddO = R(0), ddN = R(0);
+        bool inO = false, inN = false;
+        if (j < i1 && j != tg) separations(j, dO, dN, ddO, ddN, inO, inN);
+        const bool take = inO || inN;
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (take) {
+          const int pos = nseg + __popc(m & ((1u << lane) - 1u));
+          if (pos < MC_SEG) seg[pos] = j;
+          else acc += pair_dE(j, dO, dN, ddO, ddN, inO, inN);
         }
+        nseg += __popc(m);
+      }
+      __syncwarp();
+      // Pass 2: the segment, one molecule per lane
+      const int ns = min(nseg, MC_SEG);
+      for (int q = lane; q < ns; q += 32) {
+        const int j = seg[q];
+        R dO[3], dN[3], ddO, ddN;
+        bool inO, inN;
+        separations(j, dO, dN, ddO, ddN, inO, inN);
+        acc += pair_dE(j, dO, dN, ddO, ddN, inO, inN);
       }
 #pragma unroll
       for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
