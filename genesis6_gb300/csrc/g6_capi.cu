@@ -198,6 +198,7 @@ struct g6_ctx {
   double* d_stage = nullptr;      // AoS staging (53 n)
   // grids
   HostGrid gref, glist;
+  bool list_valid = false;   // the device neighbour list matches glist (built since the grid was made)
   std::vector<int> sten, sten_off;
   int* d_sten = nullptr; int* d_sten_off = nullptr;
   // neighbour list
@@ -258,6 +259,10 @@ struct g6_ctx {
   double run_dt = 0.0;
   int run_max = 0, run_done = 0;
   cudaGraphExec_t graph1 = nullptr;   // one step, for step-by-step advancing
+  // g6_md_step_host with a pinned host record: the whole call as one graph,
+  // for one record pointer, dt, log choice and lane width
+  cudaGraphExec_t graph_host = nullptr;
+  const double* ghost_rec = nullptr; double ghost_dt = 0.0; bool ghost_log = false; int ghost_lpi = 0;
   int step_timing = 0;                // 1: graph1 carries events around the step; 2: and around the kernel
   cudaEvent_t sev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -288,6 +293,7 @@ static cudaError_t dalloc(g6_ctx* c, T** p, size_t count) {
 static void drop_graphs(g6_ctx* c) {
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   if (c->graph1) { cudaGraphExecDestroy(c->graph1); c->graph1 = nullptr; }
+  if (c->graph_host) { cudaGraphExecDestroy(c->graph_host); c->graph_host = nullptr; }
 }
 
 static void free_all(g6_ctx* c) {
@@ -306,6 +312,7 @@ static void free_all(g6_ctx* c) {
   if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
   if (c->pin_ev) { cudaEventDestroy(c->pin_ev); c->pin_ev = nullptr; }
   c->gref = HostGrid(); c->glist = HostGrid();
+  c->list_valid = false;
   c->pair_capacity = 0; c->npairs = -1; c->cap = 0;
 }
 
@@ -389,6 +396,7 @@ static int check_ready(g6_ctx* ctx, bool need_state) {
 // Neighbour-list grid, capacity and buffers for the current box/cutoff/skin.
 static int prepare_list(g6_ctx* ctx) {
   if (ctx->glist.valid && ctx->cap > 0) return G6_OK;
+  ctx->list_valid = false;
   const double skin = effective_skin(ctx);
   const double rlist = ctx->cc.rout + skin;
   // cells of at least half the list radius (list_row visits two cells each way)
@@ -556,7 +564,8 @@ int g6_ctx_destroy(g6_ctx* ctx) {
 
 // Bytes of the pinned host block of a context with nrep replicas (its regions: pinned_runs).
 static size_t pinned_runs_bytes(int nrep) {
-  return 2 * (size_t)nrep * sizeof(ThermoDev) + (size_t)nrep * (NRED + 2 + 3) * sizeof(double) + 24 * sizeof(int);
+  return 2 * (size_t)nrep * sizeof(ThermoDev) + (size_t)nrep * (NRED + 2 + 3 + G6_LOG_WIDTH) * sizeof(double) +
+         24 * sizeof(int);
 }
 
 int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const int* nmol, const double* box) {
@@ -996,6 +1005,7 @@ struct PinnedRuns {
   int* ctrl_up;
   int* ctrl_dn;
   int* ovf;
+  double* log1;   // one step's log (g6_md_step_host)
 };
 static PinnedRuns pinned_runs(g6_ctx* ctx) {
   const int R = ctx->nrep;
@@ -1006,11 +1016,16 @@ static PinnedRuns pinned_runs(g6_ctx* ctx) {
   p.red = (double*)b; b += (size_t)R * NRED * sizeof(double);
   p.rf = (double*)b; b += 2 * (size_t)R * sizeof(double);
   p.fx = (double*)b; b += 3 * (size_t)R * sizeof(double);
+  p.log1 = (double*)b; b += (size_t)R * G6_LOG_WIDTH * sizeof(double);
   p.ctrl_up = (int*)b; p.ctrl_dn = p.ctrl_up + 8; p.ovf = p.ctrl_up + 16;
   return p;
 }
 
-static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log, uint64_t seed) {
+// Host part of a run's set-up: list buffers, lane widths, the log buffer and
+// the thermostat / control / factor words written into the pinned block
+// (whose previous uploads must have been read: callers wait on pin_ev or the
+// stream first).
+static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log) {
   int rc = prepare_list(ctx);
   if (rc) return rc;
   if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
@@ -1020,8 +1035,6 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
     if (ctx->step_lpi != 4 && ctx->step_lpi != 8 && ctx->step_lpi != 16 && ctx->step_lpi != 32)
       ctx->step_lpi = default_lpi(ctx);
   }
-  // the previous uploads from the pinned block have been read before it is refilled
-  CK(cudaEventSynchronize(ctx->pin_ev));
   const PinnedRuns pr = pinned_runs(ctx);
   ThermoDev* th = pr.th_up;
   for (int r = 0; r < ctx->nrep; ++r) {
@@ -1039,7 +1052,6 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
       if (t.kind < G6_NVE || t.kind > G6_ANDERSEN) return fail(ctx, G6_ERR_ARG, "unknown thermostat");
     }
   }
-  CK(cudaMemcpyAsync(ctx->d_th, th, ctx->nrep * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
   const size_t need_log = want_log ? (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH : 0;
   if (need_log > ctx->log_cap) {
     if (ctx->d_log) { cudaFree(ctx->d_log); ctx->d_log = nullptr; ctx->log_cap = 0; }
@@ -1047,40 +1059,54 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
     ctx->log_cap = need_log;
     drop_graphs(ctx);
   }
-  const int ctrl[8] = {1, 0, nsteps, 0, 0, want_log ? nsteps : 0, (int)(ctx->steps_done & 0x3fffffffULL), 0};
+  // first step: rebuild the list (1), or let the step head test the displacements
+  // since the last build (2) when a list for this grid exists
+  const int ctrl[8] = {ctx->list_valid ? 2 : 1, 0, nsteps, 0, 0, want_log ? nsteps : 0,
+                       (int)(ctx->steps_done & 0x3fffffffULL), 0};
   std::memcpy(pr.ctrl_up, ctrl, sizeof ctrl);
-  CK(cudaMemcpyAsync(ctx->d_ctrl, pr.ctrl_up, sizeof ctrl, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_gmax, 0, 2 * sizeof(unsigned), ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_repcnt, 0, ctx->nrep * sizeof(int), ctx->stream));
-  {   // temperature and pressure factors of each replica (Mixture.F90:2251-2264)
-    double* rf = pr.rf;
-    for (int r = 0; r < ctx->nrep; ++r) {
-      const double dof = 6.0 * (ctx->off[r + 1] - ctx->off[r]);
-      const double vol = ctx->L[3 * r] * ctx->L[3 * r + 1] * ctx->L[3 * r + 2];
-      rf[2 * r] = I2J * 2.0 / (RGAS * dof);
-      rf[2 * r + 1] = I2J / (3.0 * A2P * vol * NA * ANG2M * ANG2M * ANG2M);
-    }
-    double* fx = pr.fx;
-    for (int k = 0; k < 3 * ctx->nrep; ++k) fx[k] = (1.0 / ctx->L[k]) * 4294967296.0;
-    CK(cudaMemcpyAsync(ctx->d_rfac, rf, 2 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->d_fixs, fx, 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // temperature and pressure factors of each replica (Mixture.F90:2251-2264)
+  for (int r = 0; r < ctx->nrep; ++r) {
+    const double dof = 6.0 * (ctx->off[r + 1] - ctx->off[r]);
+    const double vol = ctx->L[3 * r] * ctx->L[3 * r + 1] * ctx->L[3 * r + 2];
+    pr.rf[2 * r] = I2J * 2.0 / (RGAS * dof);
+    pr.rf[2 * r + 1] = I2J / (3.0 * A2P * vol * NA * ANG2M * ANG2M * ANG2M);
   }
-  CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  for (int k = 0; k < 3 * ctx->nrep; ++k) pr.fx[k] = (1.0 / ctx->L[k]) * 4294967296.0;
   if (thermo && thermo[0].seed != ctx->seed) {
     ctx->seed = thermo[0].seed;
     drop_graphs(ctx);
   }
+  return G6_OK;
+}
+
+// Device part of a run's set-up: the uploads from the pinned block and the clears.
+static int md_upload(g6_ctx* ctx) {
+  const PinnedRuns pr = pinned_runs(ctx);
+  CK(cudaMemcpyAsync(ctx->d_th, pr.th_up, ctx->nrep * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_ctrl, pr.ctrl_up, 8 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_gmax, 0, 2 * sizeof(unsigned), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_repcnt, 0, ctx->nrep * sizeof(int), ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_rfac, pr.rf, 2 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_fixs, pr.fx, 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  return G6_OK;
+}
+
+static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log, uint64_t seed) {
+  // the previous uploads from the pinned block have been read before it is refilled
+  CK(cudaEventSynchronize(ctx->pin_ev));
+  int rc = md_fill(ctx, dt, nsteps, thermo, want_log);
+  if (rc) return rc;
+  if ((rc = md_upload(ctx))) return rc;
+  CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
   (void)seed;
   return G6_OK;
 }
 
-static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log) {
+// Read-backs of a run into the pinned block (and the log into `log`, host memory).
+static int md_readback(g6_ctx* ctx, int nsteps, double* log) {
   const PinnedRuns pr = pinned_runs(ctx);
-  const int* ctrl = pr.ctrl_dn;
-  const ThermoDev* th = pr.th_dn;
-  const double* red = pr.red;
   CK(cudaMemcpyAsync(pr.ctrl_dn, ctx->d_ctrl, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(pr.ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(pr.th_dn, ctx->d_th, ctx->nrep * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1089,7 +1115,15 @@ static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log
   if (log && nsteps > 0)
     CK(cudaMemcpyAsync(log, ctx->d_log, (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH * sizeof(double),
                        cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  return G6_OK;
+}
+
+// After the stream has finished: thermostat state back to the caller, errors.
+static int md_check(g6_ctx* ctx, int nsteps, g6_thermostat* thermo) {
+  const PinnedRuns pr = pinned_runs(ctx);
+  const int* ctrl = pr.ctrl_dn;
+  const ThermoDev* th = pr.th_dn;
+  const double* red = pr.red;
   for (int r = 0; r < ctx->nrep; ++r) {
     ctx->last_epot[r] = red[(size_t)r * NRED];
     if (thermo) {
@@ -1104,7 +1138,15 @@ static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log
   if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");
   if (ctrl[1] != nsteps) return fail(ctx, G6_ERR_STATE, "step counter mismatch");
   ctx->steps_done += (unsigned long long)nsteps;
+  ctx->list_valid = true;   // every step leaves the list valid for its positions
   return G6_OK;
+}
+
+static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log) {
+  int rc = md_readback(ctx, nsteps, log);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return md_check(ctx, nsteps, thermo);
 }
 
 static int capture_steps(g6_ctx* ctx, const StepArgs& sa, int k, cudaGraphExec_t* out) {
@@ -1300,25 +1342,65 @@ int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double*
   return g6_md_end(ctx, thermo, log);
 }
 
-int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log) {
-  int rc = check_ready(ctx, false);
-  if (rc) return rc;
-  if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
+// Enqueue the whole host-buffer step on the context's stream (used directly,
+// or captured once into graph_host).  log_dst: host destination of the log.
+static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log) {
   const int n = ctx->n;
   const size_t bytes = (size_t)REC * n * sizeof(double);
   CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
   CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));
-  ctx->have_state = true;
-  rc = md_prepare(ctx, dt, 1, thermo, log != nullptr, 0);
+  int rc = md_upload(ctx);
   if (rc) return rc;
-  StepArgs sa = step_args(ctx, dt, log ? ctx->d_log : nullptr);
+  StepArgs sa = step_args(ctx, dt, want_log ? ctx->d_log : nullptr);
   if ((rc = md_start(ctx, dt))) return rc;
-  rc = enqueue_step(ctx, sa);
-  if (rc) return rc;
+  if ((rc = enqueue_step(ctx, sa))) return rc;
   if ((rc = md_stop(ctx))) return rc;
   CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
   CK(cudaMemcpyAsync(rec, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  return md_finish(ctx, 1, thermo, log);
+  return md_readback(ctx, 1, want_log ? log_dst : nullptr);
+}
+
+int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log) {
+  int rc = check_ready(ctx, false);
+  if (rc) return rc;
+  if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
+  // the pinned block is free: every earlier use ended with a stream synchronisation or pin_ev
+  CK(cudaEventSynchronize(ctx->pin_ev));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if ((rc = md_fill(ctx, dt, 1, thermo, log != nullptr))) return rc;
+  ctx->have_state = true;
+  // a page-locked record: the call runs as one cached graph (launch overhead of
+  // the dozen copies and kernels paid once); otherwise the same work is enqueued
+  // operation by operation
+  cudaPointerAttributes at;
+  bool pinned = cudaPointerGetAttributes(&at, rec) == cudaSuccess && at.type == cudaMemoryTypeHost;
+  if (!pinned) cudaGetLastError();   // clear the lookup's status for a pageable pointer
+  const PinnedRuns pr = pinned_runs(ctx);
+  if (pinned) {
+    const bool want_log = log != nullptr;
+    if (ctx->graph_host && (ctx->ghost_rec != rec || ctx->ghost_dt != dt || ctx->ghost_log != want_log ||
+                            ctx->ghost_lpi != ctx->step_lpi)) {
+      cudaGraphExecDestroy(ctx->graph_host);
+      ctx->graph_host = nullptr;
+    }
+    if (!ctx->graph_host) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_step_host(ctx, dt, rec, pr.log1, want_log);
+      if (rc) { cudaStreamEndCapture(ctx->stream, &g); return rc; }
+      CK(cudaStreamEndCapture(ctx->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&ctx->graph_host, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) { ctx->graph_host = nullptr; return cuda_fail(ctx, e, "cudaGraphInstantiate"); }
+      ctx->ghost_rec = rec; ctx->ghost_dt = dt; ctx->ghost_log = want_log; ctx->ghost_lpi = ctx->step_lpi;
+    }
+    CK(cudaGraphLaunch(ctx->graph_host, ctx->stream));
+  } else {
+    if ((rc = enqueue_step_host(ctx, dt, rec, log, log != nullptr))) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (pinned && log) std::memcpy(log, pr.log1, (size_t)ctx->nrep * G6_LOG_WIDTH * sizeof(double));
+  return md_check(ctx, 1, thermo);
 }
 
 int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta, g6_thermostat* thermo,

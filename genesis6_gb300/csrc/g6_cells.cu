@@ -301,6 +301,34 @@ __global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
         a.s.ctrl[0] = rebuild ? 1 : 0;
         a.s.gmax[step & 1] = 0u;   // the word of step-2, read by the previous head only
       }
+    } else if (ctrl[0] == 2) {
+      // first step of a run over a list built earlier: rebuild only if some
+      // molecule has moved more than half the skin since that build (the
+      // same test as between steps, on the fixed-point COM)
+      cg::grid_group grid = cg::this_grid();
+      if (!grid.is_valid()) {   // not launched cooperatively: report, never wait
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(a.l.overflow, 2);
+        return;
+      }
+      const int n = a.l.n;
+      const uint32_t* fx = (ctrl[1] & 1) ? a.l.fix1 : a.l.fix;
+      float dmax = 0.0f;
+      for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int r = a.l.rep.mol_rep[i];
+        float dd = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float e = (float)(int)(fx[(size_t)k * n + i] - a.l.fix_build[(size_t)k * n + i]) * a.l.rep.fscale[3 * r + k];
+          dd += e * e;
+        }
+        dmax = fmaxf(dmax, dd);
+      }
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, m));
+      if ((threadIdx.x & 31) == 0) atomicMax(&a.s.gmax[1], __float_as_uint(dmax));   // the word is 0 at run start
+      grid.sync();
+      rebuild = (double)__uint_as_float(__ldcg(&a.s.gmax[1])) > a.s.half_skin2;
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.s.ctrl[0] = rebuild ? 1 : 0;
     } else {
       rebuild = ctrl[0] != 0;   // first step of a run: the flag set by the host
     }

@@ -185,7 +185,12 @@ int g6_set_lpi(g6_ctx* ctx, int lpi);
 
 /* One MD step with the state in caller-owned host memory: uploads rec,
    advances one step, downloads rec and the step's log record.  This is the
-   call a host-side driver makes when it keeps the state itself. */
+   call a host-side driver makes when it keeps the state itself.  With rec in
+   page-locked memory the whole call runs as one CUDA graph, captured on the
+   first call for that rec pointer, dt, log choice and lane width (so that
+   first call must not come during a stream capture); pageable rec works
+   too, operation by operation.  The neighbour list of the previous call is
+   kept when no molecule moved more than half the skin since it was built. */
 int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log);
 
 /* replica_exchange_trial (Replica.F90:7-73) for neighbouring temperatures of

@@ -172,11 +172,12 @@ def test_md_mixed_conserves_energy():
     assert np.ptp(H) < 0.02 * ek
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_host_buffer_step_equals_device_step(prec):
-    """g6_md_step_host (state in a host buffer, copied in and out) gives the
-    same state, log and thermostat as one device-resident step from the same
-    state, on two calls in a row."""
+@pytest.mark.parametrize("prec,pinned", [("fp64", False), ("mixed", False), ("mixed", True)])
+def test_host_buffer_step_equals_device_step(prec, pinned):
+    """g6_md_step_host (state in a host buffer, copied in and out; a page-locked
+    buffer takes the cached-graph route) gives the same state, log and
+    thermostat as one device-resident step from the same state, on two calls in
+    a row."""
     n = 343
     b = config.water_box("TIP4P", n, 12, temp=300.0, dt=0.002, jitter=0.2)
     s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision=prec, rc=8.5)
@@ -185,7 +186,12 @@ def test_host_buffer_step_equals_device_step(prec):
     rec = s.download_state()
     th_a = s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002)
     th_b = s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002)
-    host = rec.copy()
+    if pinned:
+        import torch
+        host = torch.empty(rec.shape, dtype=torch.float64, pin_memory=True).numpy()
+        host[:] = rec
+    else:
+        host = rec.copy()
     for _ in range(2):
         ref_in = host.copy()
         s.upload_state(ref_in)
