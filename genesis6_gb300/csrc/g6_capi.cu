@@ -1527,7 +1527,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   CK(cudaStreamSynchronize(ctx->stream));
   if (mode == G6_MC_COLLECT) ctx->nrec += (long long)R * ntrial;
   if (energy) for (int r = 0; r < R; ++r) energy[r] = etot[r];
-  if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 256 molecules within 6.5 A of a Monte Carlo pose");
+  if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 128 molecules within 6.5 A of a Monte Carlo pose, or a feature row over its capacity");
   if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
   drop_graphs(ctx);   // poses changed outside the MD state machine
   return G6_OK;
