@@ -126,16 +126,18 @@ def test_force_sites_entry_matches_reference_call(orc, model, path):
     assert np.abs(hx - x).max() < 1e-12
 
 
-def test_md_fp64_follows_oracle(orc):
+@pytest.mark.parametrize("model,path", [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "custom"), ("ST2", "custom"),
+                                        ("ST2", "std")])
+def test_md_fp64_follows_oracle(orc, model, path):
     """Short Gear MD: the device trajectory tracks the oracle's step by step."""
     n = 256
-    b = config.water_box("TIP4P", n, 5, temp=300.0, dt=0.002, jitter=0.2)
+    b = config.water_box(model, n, 5, temp=300.0, dt=0.002, jitter=0.2)
     L = b["L"]
-    s = g6.RigidWater("TIP4P", n, L, path="custom", rc=8.5, skin=1.0)
+    s = g6.RigidWater(model, n, L, path=path, rc=8.5, skin=1.0)
     s.upload_state(b["rec"])
     log = s.md_run(0.002, 20)
     rec_g = s.download_state()
-    rec_o, _, log_o = orc.md_run("TIP4P", "custom", b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 20, np.zeros(10))
+    rec_o, _, log_o = orc.md_run(model, path, b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 20, np.zeros(10))
     assert np.abs(log[:, 0, 0] - log_o[:, 0]).max() <= 1e-9 * np.abs(log_o[:, 0]).max()
     assert np.abs(log[:, 0, 5] - log_o[:, 5]).max() <= 1e-9 * np.abs(log_o[:, 5]).max()
     assert np.abs(rec_g[:, :3] - rec_o[:, :3]).max() < 1e-9
