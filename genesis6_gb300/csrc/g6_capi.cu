@@ -224,9 +224,6 @@ struct g6_ctx {
   int* d_fcache = nullptr;         // per-molecule features at the current pose (Monte Carlo)
   int* d_mcflag = nullptr;         // Monte Carlo: too many feature neighbours
   float* d_udir = nullptr;         // Monte Carlo: charged-site directions per molecule
-  int* d_flist = nullptr;          // Monte Carlo: feature-neighbour rows (MC_FL_CAP per molecule)
-  int* d_fnum = nullptr;
-  uint32_t* d_flfix = nullptr;
   float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
   double sig0_t = 0.15, sig0_r = 0.15;
   double obj_move = 1.0, obj_energy = 0.0;   // training objective weights (g6_mlp_objective)
@@ -636,8 +633,6 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
   CK(dalloc(ctx, &ctx->d_mlp, MLP_NPARAM)); CK(dalloc(ctx, &ctx->d_fcache, (size_t)n * MLP_IN));
   CK(dalloc(ctx, &ctx->d_mcflag, 1)); CK(dalloc(ctx, &ctx->d_udir, (size_t)n * 12));
-  CK(dalloc(ctx, &ctx->d_flist, (size_t)n * MC_FL_CAP)); CK(dalloc(ctx, &ctx->d_fnum, (size_t)n));
-  CK(dalloc(ctx, &ctx->d_flfix, (size_t)n * 3));
   ctx->last_epot.assign(nrep, 0.0);
   ctx->pinned_bytes = pinned_runs_bytes(nrep);
   CK(cudaMallocHost((void**)&ctx->h_pinned, ctx->pinned_bytes));
@@ -1512,7 +1507,6 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
   a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
   a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
-  a.flist = ctx->d_flist; a.fnum = ctx->d_fnum; a.flfix = ctx->d_flfix;
   for (int r = 0; r < R; ++r) a.ncmax = std::max(a.ncmax, ctx->off[r + 1] - ctx->off[r]);
   a.mlp = mlp_dev(ctx);
   CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
@@ -1527,7 +1521,7 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   CK(cudaStreamSynchronize(ctx->stream));
   if (mode == G6_MC_COLLECT) ctx->nrec += (long long)R * ntrial;
   if (energy) for (int r = 0; r < R; ++r) energy[r] = etot[r];
-  if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 128 molecules within 6.5 A of a Monte Carlo pose, or a feature row over its capacity");
+  if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 64 molecules within 6 A of a Monte Carlo pose");
   if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
   drop_graphs(ctx);   // poses changed outside the MD state machine
   return G6_OK;

@@ -31,13 +31,15 @@
 // Learned widths (G6_MC_LEARNED): the proposal widths come from a 24-64-64-2
 // MLP on local-environment features.  The features of every molecule at its
 // current pose are kept in an integer cache (exact sums, see g6_mlp.cuh): the
-// widths at the old pose come from the cache, the features at the new pose
-// are summed by a control warp from the molecules of the target's feature row
-// (molecules within 6.5 A + a skin, rebuilt when molecules have moved far
-// enough) while the other warps sum the energies, and an accepted move updates
-// the cache of the moved molecule and of its neighbours.  The Hastings ratio
-// uses the widths of both poses.  G6_MC_COLLECT runs the fixed widths and
-// writes one training record per trial.
+// widths at the old pose come from the cache.  The energy warps, which test
+// every molecule against both poses anyway, keep the molecules within 6 A of
+// either pose, add the target's terms of the new-pose ones into its new
+// features and prepare each neighbour's own terms of the pair; they then
+// signal warp 0 (named barrier 1), which runs the network on the new features
+// while they sum the pair energies.  An accepted move writes the moved
+// molecule's new features and adds the prepared terms to its neighbours'
+// rows.  The Hastings ratio uses the widths of both poses.  G6_MC_COLLECT runs
+// the fixed widths and writes one training record per trial.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -51,9 +53,9 @@ constexpr int MC_NT = 512;            // threads per chain
 constexpr int MC_NB = 128;            // trials per batch of pre-computed draws
 constexpr float FEAT_Q = 1048576.0f;  // feature terms are integers of 2^-20
 constexpr float FEAT_IQ = 1.0f / 1048576.0f;
-constexpr float FEAT_RC2 = 6.5f * 6.5f;
-constexpr int MC_QMAX = 128;          // feature neighbours per pose (about 40 in liquid water)
+constexpr float FEAT_RC2 = 6.0f * 6.0f;
 constexpr int MC_SEG = 96;            // molecules within rc kept per energy warp and trial
+constexpr int MC_POOL = 64;           // feature neighbours kept per pose (about 31 in liquid water)
 
 template <int NQ, bool TAPER, class R>
 __device__ __forceinline__ R pair_energy(const R d[3], R dd, const R (&ri)[NQ + 1][3], const R (&rj)[NQ + 1][3],
@@ -195,7 +197,7 @@ __device__ __forceinline__ void feat_r(float r2, float& r, float& ir) {
 }
 template <int K>
 __device__ __forceinline__ int feat_radial(float r) {
-  return feat_q(gauss_rn(__fmul_rn(__fsub_rn(r, 2.4f + 0.25f * K), 4.0f)));
+  return feat_q(gauss_rn(__fmul_rn(__fsub_rn(r, 2.4f + 0.225f * K), 4.0f)));
 }
 __device__ __forceinline__ float feat_g1(float r) { return gauss_rn(__fmul_rn(__fsub_rn(r, 2.9f), 1.0f / 0.35f)); }
 __device__ __forceinline__ float feat_g2(float r) { return gauss_rn(__fmul_rn(__fsub_rn(r, 4.5f), 2.0f)); }
@@ -227,28 +229,27 @@ __device__ __forceinline__ void feat_terms(const float e[3], float r2, const flo
   }
 }
 
-// A quarter of the terms of one neighbour added into fc (shared or global):
-// part 0 and 1 the radial shells 0-7 and 8-15, part 2 and 3 the direction terms
-// of charged sites 0-1 and 2-3 (u = the molecule's 12 site-direction floats).
-__device__ __forceinline__ void feat_add_part(int part, const float e[3], float r2, const float* u, int sign,
-                                              int* fc) {
+// A quarter of the terms of one neighbour: part 0 and 1 the radial shells 0-7
+// and 8-15, part 2 and 3 the direction terms of charged sites 0-1 and 2-3 (u =
+// the molecule's 12 site-direction floats).  v[q] is the term of feature
+// part_index(part, q); parts 2 and 3 fill v[0..3].
+__device__ __forceinline__ int part_index(int part, int q) {
+  return part < 2 ? 8 * part + q : 16 + 4 * (q >> 1) + 2 * (part - 2) + (q & 1);
+}
+__device__ __forceinline__ void feat_part(int part, const float e[3], float r2, const float* u, int (&v)[8]) {
   float r, ir;
   feat_r(r2, r, ir);
   int f[MLP_IN];
+#pragma unroll
+  for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
   if (part == 0) {
+    feat_radials<0, 8>(r, 1, f);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) f[k] = 0;
-    feat_radials<0, 8>(r, sign, f);
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      if (f[k] != 0) atomicAdd(fc + k, f[k]);
+    for (int q = 0; q < 8; ++q) v[q] = f[q];
   } else if (part == 1) {
+    feat_radials<8, 8>(r, 1, f);
 #pragma unroll
-    for (int k = 8; k < 16; ++k) f[k] = 0;
-    feat_radials<8, 8>(r, sign, f);
-#pragma unroll
-    for (int k = 8; k < 16; ++k)
-      if (f[k] != 0) atomicAdd(fc + k, f[k]);
+    for (int q = 0; q < 8; ++q) v[q] = f[8 + q];
   } else {
     const float g1 = feat_g1(r), g2 = feat_g2(r);
     const int s0 = 2 * (part - 2);
@@ -256,12 +257,25 @@ __device__ __forceinline__ void feat_add_part(int part, const float e[3], float 
     for (int q = 0; q < 2; ++q) {
       const float us[3] = {u[3 * (s0 + q)], u[3 * (s0 + q) + 1], u[3 * (s0 + q) + 2]};
       const float c4 = feat_c4(us, e, ir);
-      const int a1 = sign * feat_q(__fmul_rn(g1, c4)), a2 = sign * feat_q(__fmul_rn(g2, c4));
-      if (a1 != 0) atomicAdd(fc + 16 + s0 + q, a1);
-      if (a2 != 0) atomicAdd(fc + 20 + s0 + q, a2);
+      v[q] = feat_q(__fmul_rn(g1, c4));
+      v[2 + q] = feat_q(__fmul_rn(g2, c4));
     }
+#pragma unroll
+    for (int q = 4; q < 8; ++q) v[q] = 0;
   }
 }
+
+// One feature neighbour of a trial pose as an energy warp keeps it: the
+// neighbour's site directions (copied asynchronously), the separation
+// neighbour -> target pose, the neighbour, and the neighbour's own terms of the
+// pair, added to (new pose) or subtracted from (old pose) its cache row when
+// the move is accepted.  160 bytes, so that u stays 16-byte aligned.
+struct FeEntry {
+  float u[12];
+  float e[3];
+  int j;
+  int d[MLP_IN];
+};
 
 // Separation a -> b of two molecules: fixed-point COMs (mixed) or the FP64
 // minimum image (plain), as float.
@@ -300,7 +314,7 @@ struct PoseRead {
 
 // Features of every molecule of the chain at its current pose (integer cache).
 template <int NQ, bool MIXED>
-__device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3], const double L[3],
+__device__ __noinline__ void init_features(const McArgs& a, int i0, int i1, const float fs[3], const double L[3],
                               const double iL[3], int* fcl) {
   using P = PoseRead<NQ, MIXED>;
   for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
@@ -327,41 +341,6 @@ __device__ void init_features(const McArgs& a, int i0, int i1, const float fs[3]
 #pragma unroll
     for (int k = 0; k < MLP_IN; ++k) fcl[(size_t)(i - i0) * MLP_IN + k] = f[k];
   }
-}
-
-// Feature-neighbour rows of every molecule of the chain: the molecules within
-// 6.5 A + MC_FL_SKIN of its fixed-point COM now, which is kept as the row's
-// reference position.  A row holds every molecule within 6.5 A of the
-// molecule as long as the two have moved by less than MC_FL_SKIN in total
-// since the build; the kernel checks that before every trial.
-__device__ void build_flists(const McArgs& a, int i0, int i1, const float fs[3]) {
-  constexpr float R2 = (6.5f + MC_FL_SKIN) * (6.5f + MC_FL_SKIN);
-  const int n = a.n;
-  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-    const uint32_t fi[3] = {a.fix[i], a.fix[n + i], a.fix[2 * n + i]};
-    int* row = a.flist + (size_t)i * MC_FL_CAP;
-    int cnt = 0;
-    for (int j = i0; j < i1; ++j) {
-      if (j == i) continue;
-      const uint32_t fj[3] = {a.fix[j], a.fix[n + j], a.fix[2 * n + j]};
-      float e[3];
-      if (fvec_fix(fi, fj, fs, e) < R2) {
-        if (cnt < MC_FL_CAP) row[cnt] = j;
-        ++cnt;
-      }
-    }
-    if (cnt > MC_FL_CAP) { atomicExch(a.flag, 1); cnt = MC_FL_CAP; }
-    a.fnum[i] = cnt;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) a.flfix[(size_t)k * n + i] = fi[k];
-  }
-}
-
-// Distance moved since the feature rows were built (fixed-point COM).
-__device__ __forceinline__ float fl_moved(const McArgs& a, int i, const uint32_t f[3], const float fs[3]) {
-  const uint32_t b[3] = {a.flfix[i], a.flfix[a.n + i], a.flfix[2 * a.n + i]};
-  float e[3];
-  return sqrtf(fvec_fix(b, f, fs, e));
 }
 
 // The proposal-width network in shared memory, transposed for conflict-free
@@ -406,8 +385,25 @@ __device__ void mlp_load(MlpShared& m, const MlpDev& d) {
 // one used).  w selects the warp's scratch rows.  R: the pose precision.  Lane
 // l computes hidden units 2l and 2l+1 with one 8-byte weight load per input
 // and four independent partial sums per unit; inputs are read four at a time.
+// Not inlined (nor are build_trial and init_features): one copy of the code
+// serves every call site, which keeps the kernel's instruction footprint small
+// (about 7% faster per trial than inlined copies).
+// tanh of a hidden unit: the single-instruction approximation (PTX
+// tanh.approx.f32) for mixed-precision chains, tanhf for the FP64 chains that
+// replay the FP64 reference.
 template <class R>
-__device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, R& st, R& sr) {
+__device__ __forceinline__ float mlp_tanh(float x) {
+  if constexpr (sizeof(R) == 4) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+  } else {
+    return tanhf(x);
+  }
+}
+
+template <class R>
+__device__ __noinline__ void mlp_widths_warp(MlpShared& m, int w, const int* feat, R& st, R& sr) {
   const int lane = threadIdx.x & 31;
   float* xs = reinterpret_cast<float*>(m.x[w]);
   if (lane < MLP_IN) xs[lane] = ((float)feat[lane] * FEAT_IQ - m.mean[lane]) * m.istd[lane];
@@ -425,8 +421,8 @@ __device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* 
     }
   }
   const float2 b1 = m.b1p[lane];
-  const float h1a = tanhf(b1.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
-  const float h1b = tanhf(b1.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
+  const float h1a = mlp_tanh<R>(b1.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
+  const float h1b = mlp_tanh<R>(b1.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
   reinterpret_cast<float2*>(m.h[w])[lane] = make_float2(h1a, h1b);
   __syncwarp();
 #pragma unroll
@@ -443,8 +439,8 @@ __device__ __forceinline__ void mlp_widths_warp(MlpShared& m, int w, const int* 
     }
   }
   const float2 b2 = m.b2p[lane];
-  const float h2a = tanhf(b2.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
-  const float h2b = tanhf(b2.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
+  const float h2a = mlp_tanh<R>(b2.x + ((a0[0] + a0[1]) + (a0[2] + a0[3])));
+  const float h2b = mlp_tanh<R>(b2.y + ((a1[0] + a1[1]) + (a1[2] + a1[3])));
   float z[MLP_OUT];
 #pragma unroll
   for (int q = 0; q < MLP_OUT; ++q) {
@@ -491,28 +487,7 @@ struct TrialPose {
   float un[4][3];                   // charged-site directions at the new pose
   float d2, r2;                     // |dx|^2, |rot|^2
   int trial;                        // trial number the pose belongs to (-1: none)
-  float fl_mo, fl_mn;               // distance of the old / new pose from the target's feature-row reference
-  int fl_epoch;                     // feature-row build the two distances refer to
 };
-
-// Distances of a pose's old and new COM from its target's feature-row
-// reference position (one thread).
-template <class TP>
-__device__ __forceinline__ void fl_distances(const McArgs& a, TP& P, int tg, const float fs[3], int epoch) {
-  const uint32_t fo[3] = {P.fo[0], P.fo[1], P.fo[2]}, fn[3] = {P.fn[0], P.fn[1], P.fn[2]};
-  P.fl_mo = fl_moved(a, tg, fo, fs);
-  P.fl_mn = fl_moved(a, tg, fn, fs);
-  P.fl_epoch = epoch;
-}
-// The same from the reference position b, loaded ahead by the caller.
-template <class TP>
-__device__ __forceinline__ void fl_distances_from(TP& P, const uint32_t (&b)[3], const float fs[3], int epoch) {
-  const uint32_t fo[3] = {P.fo[0], P.fo[1], P.fo[2]}, fn[3] = {P.fn[0], P.fn[1], P.fn[2]};
-  float e[3];
-  P.fl_mo = sqrtf(fvec_fix(b, fo, fs, e));
-  P.fl_mn = sqrtf(fvec_fix(b, fn, fs, e));
-  P.fl_epoch = epoch;
-}
 
 // FP64 quaternion of an accepted mixed-precision trial, component `lane` on
 // lanes 0-3 (all lanes call): qadd of QuatModule.F90:108-133 applied to the
@@ -546,12 +521,12 @@ __device__ __forceinline__ double accepted_q64(const TP& P, int lane) {
 // Warp-cooperative build of trial `trial` (target tg, unit normals g[0..5][slot],
 // widths st_w, sr_w).  Register arrays are indexed with constants only
 // (selects), never by lane.  Mixed precision builds the pose in FP32 with no
-// FP64 arithmetic but the trial COM and the FP64 quaternion an acceptance
-// would write (accepted_q64); the FP64 mode follows mc2's serial formulas in
+// FP64 arithmetic but the trial COM and, with Q64, the FP64 quaternion an
+// acceptance would write (accepted_q64); the FP64 mode follows mc2's serial formulas in
 // FP64, component k on lane k, since an FP64 warp instruction costs the same
 // whatever the number of active lanes.
-template <class R, int NQ, bool MIXED>
-__device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const R (*g)[MC_NB], int slot,
+template <class R, int NQ, bool MIXED, bool Q64>
+__device__ __noinline__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int tg, const R (*g)[MC_NB], int slot,
                             R st_w, R sr_w, const double iL[3], const float fsi[3]) {
   using Pr = PoseRead<NQ, MIXED>;
   const int lane = threadIdx.x & 31;
@@ -636,12 +611,16 @@ __device__ void build_trial(const McArgs& a, TrialPose<R, NQ>& P, int trial, int
     P.trial = trial;
   }
   __syncwarp();
-  if (MIXED) {   // the FP64 quaternion an acceptance writes, prepared off the acceptance path
+  if constexpr (Q64) {   // the FP64 quaternion an acceptance writes, prepared off the acceptance path
     const double q = accepted_q64(P, lane);
     if (lane < 4) P.q64[lane] = q;
     __syncwarp();
   }
 }
+
+// Control warps of a chain's CTA (they build poses and run the network; the
+// others are energy warps).
+__host__ __device__ constexpr int mc_ctrl_warps(int mode) { return mode == G6_MC_LEARNED ? 2 : 1; }
 
 template <int NQ, bool TAPER, bool MIXED, int MODE>
 __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
@@ -650,26 +629,22 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   using TP = TrialPose<R, NQ>;
   constexpr bool FEAT = MODE != G6_MC_PLAIN;
   constexpr bool LEARN = MODE == G6_MC_LEARNED;
-  // control warps build the next trial's pose (and, with features, find the
-  // feature neighbours and run the network) while the others sum energies
-  constexpr int NCTRL = LEARN ? 2 : 1;
+  // the FP64 quaternion an acceptance writes is prepared with the pose
+  constexpr bool Q64 = MIXED;
+  // control warps build the next trial's pose (and, with learned widths, run
+  // the network) while the others sum energies
+  constexpr int NCTRL = mc_ctrl_warps(MODE);
   constexpr int E0 = 32 * NCTRL, NE = MC_NT - E0, NEW = NE / 32;
   constexpr int W64 = P::W64, NPK = P::NPK;
   __shared__ typename std::conditional<MIXED, float, double>::type s_lu[MC_NB];   // log of the test uniform
   __shared__ R s_g[6][MC_NB];   // unit normals of the rotation (0-2) and translation (3-5)
   __shared__ int s_tg[MC_NB];
   __shared__ TP s_pose[2];
-  __shared__ int s_feat[MLP_IN];
+  __shared__ int s_feat[MLP_IN];   // the target's features at the trial pose
   __shared__ R s_part[NEW];
   __shared__ int s_seg[NEW][MC_SEG];   // each energy warp's molecules within rc of either pose
-  __shared__ int s_q[2][FEAT ? MC_QMAX : 1];   // feature neighbours of the old (0) and new (1) pose
-  __shared__ float s_qe[2][FEAT ? MC_QMAX : 1][3];   // their separations neighbour -> target pose
-  __shared__ int s_nq[2];
+  __shared__ int s_pool;   // feature neighbours kept so far: new pose (low 16 bits), old pose (high 16 bits)
   __shared__ int s_accept, s_hit;
-  __shared__ float s_fl_moved;   // largest distance any molecule moved since the feature rows were built
-  __shared__ int s_fl_mode;      // 0: the target's feature row covers both poses; 1: rebuild the rows first;
-                                 // 2: the trial move alone exceeds the skin, scan the whole chain
-  __shared__ int s_fl_epoch;     // feature-row builds so far
   __shared__ QForm s_qf_new;   // proposal density form of the learned widths at the trial pose
   __shared__ typename std::conditional<LEARN, MlpShared, int>::type s_mlp;
 
@@ -688,18 +663,14 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
   const R sig_r_fixed = (R)sqrt(a.sigma_r[c] * a.sigma_r[c]);
   const float fsi[3] = {(float)(4294967296.0 * iL[0]), (float)(4294967296.0 * iL[1]), (float)(4294967296.0 * iL[2])};
   if constexpr (LEARN) mlp_load(s_mlp, a.mlp);
-  // the chain's feature cache: shared memory when it fits, else its rows of a.fcache
-  extern __shared__ int s_fcdyn[];
-  int* const fcl = a.fc_smem ? s_fcdyn : a.fcache + (size_t)i0 * MLP_IN;
-  // with the cache in shared memory, the site directions of the queued
-  // neighbours are copied there too (asynchronously, while the control warps
-  // work), for the cache update of an acceptance: 2 x MC_QMAX rows of 12 floats
-  float* const s_ud = reinterpret_cast<float*>(s_fcdyn + (size_t)a.ncmax * MLP_IN);
-  if constexpr (FEAT) {
-    init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
-    build_flists(a, i0, i1, fs);
-    if (threadIdx.x == 0) { s_fl_moved = 0.0f; s_fl_epoch = 0; }
-  }
+  // dynamic shared memory: the chain's feature cache when it fits (else its rows
+  // of a.fcache), then the feature neighbours of the new pose and of the old pose
+  // (MC_POOL entries each)
+  extern __shared__ __align__(16) int s_dyn[];
+  int* const fcl = a.fc_smem ? s_dyn : a.fcache + (size_t)i0 * MLP_IN;
+  FeEntry* const pool_new = reinterpret_cast<FeEntry*>(s_dyn + (a.fc_smem ? (size_t)a.ncmax * MLP_IN : 0));
+  FeEntry* const pool_old = pool_new + MC_POOL;
+  if constexpr (FEAT) init_features<NQ, MIXED>(a, i0, i1, fs, L, iL, fcl);
   if (threadIdx.x == 0) { s_pose[0].trial = -1; s_pose[1].trial = -1; }
   __syncthreads();
 
@@ -738,42 +709,17 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
     }
     const int tg = i0 + s_tg[tb];
     TP& cur = s_pose[t & 1];
-    if (FEAT && threadIdx.x == 0) s_hit = 0;
+    const bool next_in_batch = tb + 1 < MC_NB && t + 1 < a.ntrial;
+    const int tg1 = next_in_batch ? i0 + s_tg[tb + 1] : -1;   // the next trial's target
+    if (FEAT && threadIdx.x == 0) { s_hit = 0; s_pool = 0; }
+    if (FEAT && threadIdx.x < MLP_IN) s_feat[threadIdx.x] = 0;
     // ---- warp 0: the trial pose, unless it was built during the previous trial ----
     if (warp == 0 && cur.trial != t) {
       R st_w = sig_t_fixed, sr_w = sig_r_fixed;
       if constexpr (LEARN) mlp_widths_warp<R>(s_mlp, 0, fcl + (size_t)(tg - i0) * MLP_IN, st_w, sr_w);
-      build_trial<R, NQ, MIXED>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL, fsi);
-      if (FEAT && lane == 0) fl_distances(a, cur, tg, fs, s_fl_epoch);
-    }
-    if constexpr (FEAT) {
-      // the target's feature row holds every molecule within 6.5 A of both poses
-      // while the pose and any other molecule have moved less than the skin in
-      // total since the rows were built (margin for the FP32 distances)
-      if (warp == 0 && lane == 0) {
-        if (cur.fl_epoch != s_fl_epoch) fl_distances(a, cur, tg, fs, s_fl_epoch);
-        constexpr float LIM = MC_FL_SKIN - 0.01f;
-        int mode = 0;
-        if (s_fl_moved + fmaxf(cur.fl_mo, cur.fl_mn) >= LIM) {
-          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-          float e[3];
-          mode = sqrtf(fvec_fix(fo, fn, fs, e)) < LIM ? 1 : 2;
-        }
-        s_fl_mode = mode;
-      }
+      build_trial<R, NQ, MIXED, Q64>(a, cur, t, tg, s_g, tb, st_w, sr_w, iL, fsi);
     }
     __syncthreads();
-    if constexpr (FEAT) {
-      if (s_fl_mode == 1) {
-        build_flists(a, i0, i1, fs);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          s_fl_moved = 0.0f;
-          ++s_fl_epoch;
-        }
-        __syncthreads();
-      }
-    }
     if ((int)threadIdx.x >= E0) {
       // ---- energy warps: dE over every other molecule of the chain ----
       R acc = R(0);
@@ -784,7 +730,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         for (int k = 0; k < 3; ++k) { ro[s][k] = cur.oo[s][k]; rn[s][k] = cur.on[s][k]; }
       const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
       const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-      // separation of molecule j from both poses and the strict rc tests
+      // separation of molecule j from both poses (j -> pose) and the strict rc tests
       auto separations = [&](int j, R (&dO)[3], R (&dN)[3], R& ddO, R& ddN, bool& inO, bool& inN) {
         if (MIXED) {
           uint32_t fj[3];
@@ -831,19 +777,33 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         if (inN) v += pair_energy<NQ, TAPER, R>(dN, ddN, rn, rj, a.pc, rin2, rin, rout, c1);
         return v;
       };
+      const int ew = warp - NCTRL;
+      // a feature neighbour kept in slot pos: its separation and, asynchronously,
+      // its site directions
+      auto keep = [&](FeEntry* base, int pos, int j, const float (&e)[3]) {
+        FeEntry& E = base[pos];
+        E.j = j;
+        E.e[0] = e[0]; E.e[1] = e[1]; E.e[2] = e[2];
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(E.u);
+        const float* src = a.udir + (size_t)j * 12;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 16), "l"(src + 4) : "memory");
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 32), "l"(src + 8) : "memory");
+      };
       // Pass 1: the rc tests for this warp's molecules, the ones within rc of
       // either pose appended (ballot order) to the warp's segment, so that the
       // pair energies below run with full lanes instead of one site-loop pass
       // per 32 molecules with a few lanes each.  Entries beyond the segment's
-      // capacity are summed at once.  Both passes run in a fixed order.
-      const int ew = warp - NCTRL;
+      // capacity are summed at once.  Both passes run in a fixed order.  With
+      // features, the molecules within 6 A of either pose are kept as well.
       int* seg = s_seg[ew];
       int nseg = 0;
       for (int j0 = i0 + 32 * ew; j0 < i1; j0 += NE) {
         const int j = j0 + lane;
-        R dO[3], dN[3], ddO = R(0), ddN = R(0);
+        R dO[3] = {R(0), R(0), R(0)}, dN[3] = {R(0), R(0), R(0)}, ddO = R(0), ddN = R(0);
         bool inO = false, inN = false;
-        if (j < i1 && j != tg) separations(j, dO, dN, ddO, ddN, inO, inN);
+        const bool valid = j < i1 && j != tg;
+        if (valid) separations(j, dO, dN, ddO, ddN, inO, inN);
         const bool take = inO || inN;
         const unsigned m = __ballot_sync(0xffffffffu, take);
         if (take) {
@@ -852,6 +812,81 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           else acc += pair_dE(j, dO, dN, ddO, ddN, inO, inN);
         }
         nseg += __popc(m);
+        if constexpr (FEAT) {
+          // the same separations as float: bitwise those of the cache's own
+          // evaluation (fvec_fix / fvec_64), tested with the exactly rounded |e|^2
+          const float eo[3] = {(float)dO[0], (float)dO[1], (float)dO[2]};
+          const float en[3] = {(float)dN[0], (float)dN[1], (float)dN[2]};
+          bool qo = false, qn = false;
+          if (valid) {
+            const float r2o = dot3_rn(eo, eo), r2n = dot3_rn(en, en);
+            qo = r2o < FEAT_RC2 && r2o > 0.0f;
+            qn = r2n < FEAT_RC2 && r2n > 0.0f;
+          }
+          const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
+          const unsigned lt = (1u << lane) - 1u;
+          if ((qo || qn) && j == tg1) s_hit = 1;
+          if (mn | mo) {   // slots in both pools from one shared atomic per chunk
+            int b = 0;
+            if (lane == 0) b = atomicAdd(&s_pool, __popc(mn) + (__popc(mo) << 16));
+            b = __shfl_sync(0xffffffffu, b, 0);
+            const int bn = (b & 0xffff) + __popc(mn & lt), bo = (b >> 16) + __popc(mo & lt);
+            if (qn) {
+              if (bn < MC_POOL) keep(pool_new, bn, j, en); else *a.flag = 1;
+            }
+            if (qo) {
+              if (bo < MC_POOL) keep(pool_old, bo, j, eo); else *a.flag = 1;
+            }
+          }
+        }
+      }
+      if constexpr (FEAT) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        // every energy warp's entries are complete (named barrier 2, energy warps only)
+        asm volatile("bar.sync 2, %0;" ::"n"(NE) : "memory");
+        const int nn = min(s_pool & 0xffff, MC_POOL), no = min(s_pool >> 16, MC_POOL);
+        // The terms of the kept pairs, one kind of term per warp and one pair per
+        // lane (no divergence): for the new pose the radial shells (the same for
+        // both molecules of a pair: into the target's features and the
+        // neighbour's entry), the target's direction terms and the neighbour's;
+        // for the old pose the neighbour's radial and direction terms.
+        const int bn = (nn + 31) >> 5, bo = (no + 31) >> 5;
+        auto task = [&](int wt) {
+          const bool nw = wt < 6 * bn;
+          const int kind = nw ? wt / bn : 6 + (wt - 6 * bn) / bo;
+          const int q = 32 * (nw ? wt % bn : (wt - 6 * bn) % bo) + lane;
+          const bool ok = q < (nw ? nn : no);
+          FeEntry& E = nw ? pool_new[ok ? q : 0] : pool_old[ok ? q : 0];
+          float e[3] = {E.e[0], E.e[1], E.e[2]};
+          const bool tgt = kind == 2 || kind == 3;   // the target's terms: e from the target's side
+          if (tgt) { e[0] = -e[0]; e[1] = -e[1]; e[2] = -e[2]; }
+          const int part = kind < 6 ? (kind < 2 ? kind : (kind < 4 ? kind : kind - 2)) : kind - 6;
+          int v[8];
+          feat_part(part, e, dot3_rn(e, e), tgt ? &cur.un[0][0] : E.u, v);
+          const int nv = part < 2 ? 8 : 4;
+          if (ok && kind != 2 && kind != 3) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (k < nv) E.d[part_index(part, k)] = v[k];
+          }
+          if (kind < 4) {   // into the target's features: a warp sum per feature
+            int mine = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const int sum = __reduce_add_sync(0xffffffffu, ok ? v[k] : 0);
+              if (lane == k) mine = sum;
+            }
+            if (lane < nv && mine != 0) atomicAdd(s_feat + part_index(part, lane), mine);
+          }
+        };
+        // the target's terms (kinds 0-3) first, on the warps with the fewest
+        // molecules in pass 1; each warp signals warp 0 once its share of them is
+        // done, and then takes its neighbours' terms
+        int wt = NEW - 1 - ew;
+        for (; wt < 4 * bn; wt += NEW) task(wt);
+        // the target's new features are complete once every energy warp has arrived
+        if constexpr (LEARN) asm volatile("bar.arrive 1, %0;" ::"n"(32 + NE) : "memory");
+        for (; wt < 6 * bn + 4 * bo; wt += NEW) task(wt);
       }
       __syncwarp();
       // Pass 2: the segment, one molecule per lane
@@ -866,154 +901,27 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
 #pragma unroll
       for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
       if (lane == 0) s_part[warp - NCTRL] = acc;
-    } else {
-      // ---- control warps ----
-      const bool next_in_batch = tb + 1 < MC_NB && t + 1 < a.ntrial;
-      const int tg1 = next_in_batch ? i0 + s_tg[tb + 1] : -1;
-      if (warp == 0) {
-        if constexpr (FEAT) {
-          const uint32_t fo[3] = {cur.fo[0], cur.fo[1], cur.fo[2]}, fn[3] = {cur.fn[0], cur.fn[1], cur.fn[2]};
-          const double co[3] = {cur.co[0], cur.co[1], cur.co[2]}, cn[3] = {cur.cn[0], cur.cn[1], cur.cn[2]};
-          int f[MLP_IN];
-#pragma unroll
-          for (int k = 0; k < MLP_IN; ++k) f[k] = 0;
-          float un[4][3];
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) un[s][k] = cur.un[s][k];
-          // Queues of the molecules within 6.5 A of the old (0) and new (1) pose, with
-          // their separations from the molecule's side (j -> target, kept for the
-          // cache update and for the features of the target at the new pose).  The candidates
-          // are the target's feature row, loaded a whole row at a time, or, when the
-          // move alone exceeds the skin, the whole chain.
-          {
-            int cnt0 = 0, cnt1 = 0;
-            // fj: the candidate's fixed-point COM, loaded by the caller (mixed)
-            auto take = [&](int j, bool valid, const uint32_t (&fj)[3]) {
-              bool qo = false, qn = false;
-              float eo[3] = {0.0f, 0.0f, 0.0f}, en[3] = {0.0f, 0.0f, 0.0f};
-              if (valid && j != tg) {
-                float r2o, r2n;
-                if (MIXED) {
-                  r2o = fvec_fix(fj, fo, fs, eo);
-                  r2n = fvec_fix(fj, fn, fs, en);
-                } else {
-                  double cj[3];
-                  P::com(a, j, cj);
-                  r2o = fvec_64(cj, co, L, iL, eo);
-                  r2n = fvec_64(cj, cn, L, iL, en);
-                }
-                qo = r2o < FEAT_RC2 && r2o > 0.0f;
-                qn = r2n < FEAT_RC2 && r2n > 0.0f;
-              }
-              const unsigned mo = __ballot_sync(0xffffffffu, qo), mn = __ballot_sync(0xffffffffu, qn);
-              const unsigned lt = (1u << lane) - 1u;
-              // with the cache in shared memory, the neighbour's site directions are
-              // copied next to the queue (asynchronously) for the cache update
-              auto stage_dirs = [&](int slot) {
-                if (a.fc_smem) {
-                  const unsigned dst = (unsigned)__cvta_generic_to_shared(s_ud + (size_t)slot * 12);
-                  const float* src = a.udir + (size_t)j * 12;
-                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 16), "l"(src + 4) : "memory");
-                  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst + 32), "l"(src + 8) : "memory");
-                }
-              };
-              if (qo) {
-                const int pos = cnt0 + __popc(mo & lt);
-                if (pos < MC_QMAX) {
-                  s_q[0][pos] = j;
-                  s_qe[0][pos][0] = eo[0]; s_qe[0][pos][1] = eo[1]; s_qe[0][pos][2] = eo[2];
-                  stage_dirs(pos);
-                } else {
-                  *a.flag = 1;
-                }
-              }
-              if (qn) {
-                const int pos = cnt1 + __popc(mn & lt);
-                if (pos < MC_QMAX) {
-                  s_q[1][pos] = j;
-                  s_qe[1][pos][0] = en[0]; s_qe[1][pos][1] = en[1]; s_qe[1][pos][2] = en[2];
-                  stage_dirs(MC_QMAX + pos);
-                } else {
-                  *a.flag = 1;
-                }
-              }
-              cnt0 += __popc(mo);
-              cnt1 += __popc(mn);
-            };
-            if (s_fl_mode == 2) {
-              for (int p0 = 0; p0 < nc; p0 += 32) {
-                const int j = i0 + p0 + lane;
-                uint32_t fj[3] = {0u, 0u, 0u};
-                if (MIXED && p0 + lane < nc) P::fix(a, j, fj);
-                take(j, p0 + lane < nc, fj);
-              }
-            } else {
-              // the whole row (its slots beyond fnum are ignored) and then the
-              // candidates' COMs, so that the loads are two round trips in all
-              constexpr int U = MC_FL_CAP / 32;
-              const int* row = a.flist + (size_t)tg * MC_FL_CAP;
-              int jr[U];
-#pragma unroll
-              for (int u = 0; u < U; ++u) jr[u] = row[32 * u + lane];
-              const int m = a.fnum[tg];
-              uint32_t fr[U][3];
-#pragma unroll
-              for (int u = 0; u < U; ++u) {
-                const bool ok = 32 * u + lane < m;
-                jr[u] = ok ? jr[u] : -1;
-                if (MIXED && ok) P::fix(a, jr[u], fr[u]);
-                else fr[u][0] = fr[u][1] = fr[u][2] = 0u;
-              }
-#pragma unroll
-              for (int u = 0; u < U; ++u)
-                if (32 * u < m) take(jr[u], jr[u] >= 0, fr[u]);
-            }
-            if (lane == 0) { s_nq[0] = cnt0; s_nq[1] = cnt1; }
-            __syncwarp();
-            if (a.fc_smem) asm volatile("cp.async.commit_group;" ::: "memory");
-            // features of the target at the new pose, one queued neighbour per lane
-            // (target -> j is the exact negation of the stored separation)
-            const int nq1 = min(cnt1, MC_QMAX);
-            for (int p = lane; p < nq1; p += 32) {
-              const float et[3] = {-s_qe[1][p][0], -s_qe[1][p][1], -s_qe[1][p][2]};
-              feat_terms(et, dot3_rn(et, et), un, 1, f);
-            }
-          }
-#pragma unroll
-          for (int k = 0; k < MLP_IN; ++k) {
-            const int v = __reduce_add_sync(0xffffffffu, f[k]);
-            if (lane == k) s_feat[k] = v;
-          }
-          __syncwarp();
-          if constexpr (LEARN) {
-            R st2, sr2;
-            mlp_widths_warp<R>(s_mlp, 0, s_feat, st2, sr2);
-            if (lane == 0) s_qf_new = q_form((float)st2, (float)sr2);
-          }
-        }
-        if (!LEARN && next_in_batch) {   // the next trial's pose (fixed widths)
-          uint32_t b[3] = {0u, 0u, 0u};
-          if (FEAT && lane == 0) { b[0] = a.flfix[tg1]; b[1] = a.flfix[n + tg1]; b[2] = a.flfix[2 * n + tg1]; }
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL, fsi);
-          if (FEAT && lane == 0) fl_distances_from(s_pose[(t + 1) & 1], b, fs, s_fl_epoch);
-        }
-      } else if constexpr (LEARN) {
-        if (next_in_batch) {
-          // warp 1: widths of the next trial's target at its current pose and its trial pose
-          uint32_t b[3] = {0u, 0u, 0u};
-          if (lane == 0) { b[0] = a.flfix[tg1]; b[1] = a.flfix[n + tg1]; b[2] = a.flfix[2 * n + tg1]; }
-          R st1, sr1;
-          mlp_widths_warp<R>(s_mlp, 1, fcl + (size_t)(tg1 - i0) * MLP_IN, st1, sr1);
-          build_trial<R, NQ, MIXED>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL, fsi);
-          if (lane == 0) fl_distances_from(s_pose[(t + 1) & 1], b, fs, s_fl_epoch);
-        }
+    } else if (warp == 0) {
+      if constexpr (LEARN) {
+        // ---- warp 0: widths at the trial pose from the energy warps' features ----
+        asm volatile("bar.sync 1, %0;" ::"n"(32 + NE) : "memory");
+        R st2, sr2;
+        mlp_widths_warp<R>(s_mlp, 0, s_feat, st2, sr2);
+        if (lane == 0) s_qf_new = q_form((float)st2, (float)sr2);
+      } else if (next_in_batch) {   // the next trial's pose (fixed widths)
+        build_trial<R, NQ, MIXED, Q64>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, sig_t_fixed, sig_r_fixed, iL,
+                                       fsi);
+      }
+    } else if constexpr (LEARN) {
+      // ---- warp 1: widths of the next trial's target at its current pose, and its trial pose ----
+      if (next_in_batch) {
+        R st1, sr1;
+        mlp_widths_warp<R>(s_mlp, 1, fcl + (size_t)(tg1 - i0) * MLP_IN, st1, sr1);
+        build_trial<R, NQ, MIXED, Q64>(a, s_pose[(t + 1) & 1], t + 1, tg1, s_g, tb + 1, st1, sr1, iL, fsi);
       }
     }
     __syncthreads();
-    // ---- warp 0: acceptance, state update, feature cache ----
+    // ---- warp 0: acceptance, state update, the moved molecule's cache row ----
     if (warp == 0) {
       R v = lane < NEW ? s_part[lane] : R(0);
 #pragma unroll
@@ -1062,13 +970,9 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
         if (lane == 0) {
           energy += dE;
           ++nacc;
-          if constexpr (FEAT) {   // the moved molecule's distance from its feature-row reference
-            if (cur.fl_epoch != s_fl_epoch) fl_distances(a, cur, tg, fs, s_fl_epoch);
-            s_fl_moved = fmaxf(s_fl_moved, cur.fl_mn);
-          }
-          // the next trial's prepared pose is stale when it moves the same molecule
-          if (s_pose[(t + 1) & 1].trial == t + 1 && t + 1 < a.ntrial && s_tg[(tb + 1) % MC_NB] + i0 == tg)
-            s_pose[(t + 1) & 1].trial = -1;
+          // the next trial's prepared pose is stale when it moves the same molecule,
+          // or, with learned widths, when its widths came from a cache row this move changes
+          if (s_pose[(t + 1) & 1].trial == t + 1 && (tg1 == tg || (LEARN && s_hit))) s_pose[(t + 1) & 1].trial = -1;
         }
       }
       if (lane == 0) {
@@ -1094,7 +998,7 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
           }
         }
         if (lane == 0) s_accept = acc_flag;
-        if (a.fc_smem) asm volatile("cp.async.wait_all;" ::: "memory");   // the staged directions have landed
+        __syncwarp();
         if (acc_flag) {   // the moved molecule's own cache entries: its new-pose features and site directions
           if (lane < MLP_IN) fcl[(size_t)(tg - i0) * MLP_IN + lane] = s_feat[lane];
           if (lane < 12) a.udir[(size_t)tg * 12 + lane] = cur.un[lane / 3][lane % 3];
@@ -1103,27 +1007,20 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
       __syncwarp();
     }
     if constexpr (FEAT) {
-      // ---- accepted move: feature cache of the molecule and of the neighbours of
-      //      both poses (old term removed, new term added), one entry per thread ----
+      // ---- accepted move: the neighbours' prepared terms (new pose added, old
+      //      pose subtracted) added to their cache rows, one term per thread ----
       __syncthreads();
       if (s_accept) {
-        const int no = min(s_nq[0], MC_QMAX), ntot = no + min(s_nq[1], MC_QMAX);
-        const int tg1 = (t + 1 < a.ntrial && tb + 1 < MC_NB) ? i0 + s_tg[tb + 1] : -1;
-        // four threads per neighbour entry, each adding a quarter of its terms
-        for (int p = threadIdx.x; p < 4 * ntot; p += blockDim.x) {
-          const int q = p >> 2, part = p & 3;
-          const bool old_pose = q < no;
-          const int j = old_pose ? s_q[0][q] : s_q[1][q - no];
-          if (j == tg1) s_hit = 1;
-          const float* ep = old_pose ? s_qe[0][q] : s_qe[1][q - no];
-          const float e[3] = {ep[0], ep[1], ep[2]};
-          const float* u = a.fc_smem ? s_ud + (size_t)(old_pose ? q : MC_QMAX + (q - no)) * 12 : a.udir + (size_t)j * 12;
-          feat_add_part(part, e, dot3_rn(e, e), u, old_pose ? -1 : 1, fcl + (size_t)(j - i0) * MLP_IN);
+        const int nn = min(s_pool & 0xffff, MC_POOL), no = min(s_pool >> 16, MC_POOL);
+        for (int p = threadIdx.x; p < MLP_IN * (nn + no); p += MC_NT) {
+          const int q = p / MLP_IN, k = p - q * MLP_IN;
+          const bool nw = q < nn;
+          const FeEntry& E = nw ? pool_new[q] : pool_old[q - nn];
+          const int v = E.d[k];
+          if (v != 0) atomicAdd(fcl + (size_t)(E.j - i0) * MLP_IN + k, nw ? v : -v);
         }
-        __syncthreads();
-        // learned widths of the next trial were taken from features this move changed
-        if (LEARN && threadIdx.x == 0 && s_hit) s_pose[(t + 1) & 1].trial = -1;
       }
+      __syncthreads();
     }
     if (a.sample_every > 0 && (t + 1) % a.sample_every == 0) ++nsample;
   }
@@ -1135,20 +1032,22 @@ __global__ void __launch_bounds__(MC_NT) k_mc(McArgs a) {
 }
 
 // Shared memory a CTA may give to its chain's feature cache (the rest of the
-// 227 KB stays with the L1 that holds the chain's packed poses).
+// 227 KB holds the energy warps' feature neighbours, the network and the L1
+// that caches the chain's packed poses).
 constexpr size_t MC_FC_SMEM_MAX = 100 * 1024;
 
 template <int NQ, bool TAPER, bool MIXED, int MODE>
 static cudaError_t launch_mc_k(McArgs a, cudaStream_t s) {
   const size_t fc_bytes = (size_t)a.ncmax * MLP_IN * sizeof(int);
   size_t dyn = 0;
-  if (MODE != G6_MC_PLAIN && fc_bytes <= MC_FC_SMEM_MAX) {
-    dyn = fc_bytes + (size_t)2 * MC_QMAX * 12 * sizeof(float);   // cache + staged site directions
+  a.fc_smem = 0;
+  if (MODE != G6_MC_PLAIN) {
+    a.fc_smem = fc_bytes <= MC_FC_SMEM_MAX;
+    dyn = (a.fc_smem ? fc_bytes : 0) + (size_t)2 * MC_POOL * sizeof(FeEntry);
     cudaError_t e = cudaFuncSetAttribute(k_mc<NQ, TAPER, MIXED, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)dyn);
     if (e != cudaSuccess) return e;
   }
-  a.fc_smem = dyn > 0;
   k_mc<NQ, TAPER, MIXED, MODE><<<a.rep.nrep, MC_NT, dyn, s>>>(a);
   return cudaGetLastError();
 }

@@ -3,7 +3,7 @@
 //
 // Features of a molecule at a pose (24 floats):
 //   [0,16)  radial shells: sum_j exp(-((r_j - c_k)/0.25)^2) for neighbour COMs
-//           within 6.5 A, centres c_k = 2.4 + 0.25 k;
+//           within 6 A, centres c_k = 2.4 + 0.225 k;
 //   [16,24) tetrahedral-direction occupancy: for each of (up to) four charged
 //           sites s with lab direction u_s, sum_j g(r_j) max(0, u_s . e_j)^4
 //           where e_j is the unit vector towards neighbour j and g a first-
@@ -63,21 +63,13 @@ struct McArgs {
   double* trace;          // optional: per chain per trial (dE, energy, accepted, target)
   float* records;         // optional: per chain per trial training record (MLP_REC floats)
   int* fcache;            // features of every molecule at its current pose (MLP_IN integers each)
-  int* flag;              // set to 1 when a pose has more than MC_QMAX feature neighbours
+  int* flag;              // set to 1 when a pose has more than MC_POOL feature neighbours
   float* udir;            // unit directions of every molecule's charged sites (12 floats each)
-  int* flist;             // per molecule: molecules within the feature radius + skin (MC_FL_CAP slots)
-  int* fnum;              // entries of each flist row
-  uint32_t* flfix;        // fixed-point COM of each molecule when its row was built (3*n)
   int ncmax;              // molecules of the largest chain
   int fc_smem;            // set by launch_mc: each chain's feature cache lives in shared memory
   unsigned long long seed, counter;
   MlpDev mlp;
 };
-
-// Feature-neighbour rows of the Monte Carlo kernel: molecules within
-// 6.5 A + MC_FL_SKIN of each molecule when the rows were built.
-constexpr int MC_FL_CAP = 128;
-constexpr float MC_FL_SKIN = 1.0f;
 
 constexpr int MLP_REC = 2 * MLP_IN + 3;   // x_old, x_new, |dx|^2, |rot|^2, beta*dE (reduced units)
 

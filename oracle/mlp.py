@@ -39,10 +39,10 @@ def features(com_all, L, t, com, off_charged):
         d = com_all[j] - com
         d = d - np.round(d / L) * L
         r2 = d @ d
-        if r2 > 6.5 ** 2 or r2 <= 0:
+        if r2 >= 6.0 ** 2 or r2 <= 0:
             continue
         r = np.sqrt(r2)
-        f[:16] += np.exp(-((r - (2.4 + 0.25 * np.arange(16))) * 4.0) ** 2)
+        f[:16] += np.exp(-((r - (2.4 + 0.225 * np.arange(16))) * 4.0) ** 2)
         g1 = np.exp(-((r - 2.9) / 0.35) ** 2)
         g2 = np.exp(-((r - 4.5) * 2.0) ** 2)
         c = np.maximum(u @ d / r, 0.0)
