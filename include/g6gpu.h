@@ -222,7 +222,9 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
    samples (optional, nrep x ntrial/sample_every) gets the running energy,
    counts (optional, nrep x 2) accepted/attempted, energy (optional, nrep) the
    final energies, trace (optional, nrep x ntrial x 4) per trial dE, energy,
-   accepted flag and target index. */
+   accepted flag and target index.  G6_MC_LEARNED and G6_MC_COLLECT return
+   G6_ERR_CAPACITY when a pose has more than 64 molecules within the 6 A
+   feature radius (about 31 in liquid water at 1 g/cm^3). */
 #define G6_MC_PLAIN 0
 #define G6_MC_LEARNED 1
 #define G6_MC_COLLECT 2
@@ -254,7 +256,10 @@ int g6_mlp_grad(g6_ctx* ctx, const float* records, int64_t nrec, float* grad, do
    + |rot|^2/sigma0_r^2.  Defaults: w_move = 1, w_energy = 0. */
 int g6_mlp_objective(g6_ctx* ctx, double w_move, double w_energy);
 /* Widths sigma_t[n], sigma_r[n] the current network gives for n raw feature
-   rows (n x G6_MLP_NFEAT floats, e.g. the first half of training records). */
+   rows (n x G6_MLP_NFEAT floats, e.g. the first half of training records).
+   This evaluation uses tanhf; the Monte Carlo kernel of a mixed context uses
+   the hardware tanh approximation (relative error below 2^-10), the same
+   function for both poses of a trial, so its chains stay exact. */
 int g6_mlp_widths(g6_ctx* ctx, const float* features, int64_t n, double* sigma_t, double* sigma_r);
 /* Train on the collected records with Adam (hand-written forward/backward
    kernels); loss (optional, epochs) gets the mean loss of each epoch. */
