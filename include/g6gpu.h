@@ -58,8 +58,9 @@ typedef struct g6_ctx g6_ctx;
 typedef struct g6_thermostat {
   int kind;              /* G6_NVE, G6_NOSE or G6_ANDERSEN                            */
   double temp;           /* target temperature [K]                                    */
-  double q;              /* Nose mass in the reference's internal form (input q times
-                            21.8852721616497249235^2, NoseModule.F90:101)            */
+  double q;              /* Nose mass as the reference holds it during a run: the @NOS2
+                            value times dt (Mixture.F90:1206); @NOSE values are first
+                            scaled by 21.8852721616497249235^2 (NoseModule.F90:101) */
   double dump;           /* Nose damping term (@NOS2 dump)                            */
   double zeta[5];        /* Nose zeta0..zeta4                                          */
   double zetasum;        /* running sum of zeta0 (conserved-quantity term)            */
