@@ -40,9 +40,54 @@ static void five_site(ModelHost& m, double theta, double phi, double l1, double 
 static const double ST2_QM = (double)(-0.2357f), ST2_QH = (double)(+0.2357f);
 static const double ST2_EPS = (double)(0.52605e-21f) * NA * 1e-3, ST2_SIG = 3.100;
 
+// The kernels' layout is the reference's for TIP4P, TIP5P and ST2 (LJ site,
+// charged sites, COM).  SPC/E (SPCEModule.F90:28-71: O carries the LJ site and
+// a charge) becomes LJ O, charged O, H, H for the kernels.
+static void reference_layout(ModelHost& m) {
+  m.nref = m.nsite;
+  for (int s = 0; s < MAXSITE; ++s) {
+    m.site[s] = s;
+    for (int k = 0; k < 3; ++k) { m.rbody[s][k] = m.body[s][k]; m.rparam[s][k] = m.param[s][k]; }
+  }
+}
+
+static bool make_model_sites(int model, ModelHost& m);
+
 bool make_model(int model, ModelHost& m) {
+  if (!make_model_sites(model, m)) return false;
+  if (model != G6_SPCE) reference_layout(m);
+  return true;
+}
+
+static bool make_model_sites(int model, ModelHost& m) {
   m = ModelHost();
   m.model = model;
+  if (model == G6_SPCE) {
+    const double theta = 109.5 * PI / 180.0, l1 = 1.0, hmass = 1.0, omass = 16.0;
+    double y[4] = {0.0, l1 * std::sin(0.5 * theta), -l1 * std::sin(0.5 * theta), 0.0};
+    double z[4] = {0.0, l1 * std::cos(0.5 * theta), l1 * std::cos(0.5 * theta), 0.0};
+    const double zshift = z[1] * 2.0 * hmass / (2.0 * hmass + omass);
+    for (int i = 0; i < 3; ++i) z[i] = z[i] - zshift;
+    m.nref = 4;
+    for (int s = 0; s < 4; ++s) { m.rbody[s][0] = 0.0; m.rbody[s][1] = y[s]; m.rbody[s][2] = z[s]; }
+    const double qo = -0.8476, qh = 0.4238, eps = 78.208 / J2K * 1e-3, sig = 3.166;
+    m.rparam[0][0] = qo; m.rparam[0][1] = eps; m.rparam[0][2] = sig;
+    m.rparam[1][0] = qh; m.rparam[2][0] = qh;
+    m.I[0] = omass * (y[0] * y[0] + z[0] * z[0]) + hmass * (y[1] * y[1] + z[1] * z[1]) * 2.0;
+    m.I[1] = omass * (z[0] * z[0]) + hmass * (z[1] * z[1]) * 2.0;
+    m.I[2] = omass * (y[0] * y[0]) + hmass * (y[1] * y[1]) * 2.0;
+    m.mass = 2.0 * hmass + omass;
+    // kernel layout: LJ O, charged O, H, H, COM
+    const int map[5] = {0, 0, 1, 2, 3};
+    m.nsite = 5; m.nq = 3;
+    for (int s = 0; s < 5; ++s) {
+      m.site[s] = map[s];
+      for (int k = 0; k < 3; ++k) m.body[s][k] = m.rbody[map[s]][k];
+    }
+    m.param[0][1] = eps; m.param[0][2] = sig;
+    m.param[1][0] = qo; m.param[2][0] = qh; m.param[3][0] = qh;
+    return true;
+  }
   if (model == G6_TIP4P) {
     m.nsite = 5; m.nq = 3;
     const double y[5] = {0.0, 0.0, 7.56950327263661182e-01, -7.56950327263661182e-01, 0.0};
@@ -522,11 +567,11 @@ const char* g6_status_string(int s) {
 int g6_model_info(int model, int* nsite, double* body, double* param, double* mass_inertia) {
   ModelHost m;
   if (!make_model(model, m)) return G6_ERR_ARG;
-  if (nsite) *nsite = m.nsite;
-  for (int s = 0; s < m.nsite; ++s)
+  if (nsite) *nsite = m.nref;
+  for (int s = 0; s < m.nref; ++s)
     for (int k = 0; k < 3; ++k) {
-      if (body) body[3 * s + k] = m.body[s][k];
-      if (param) param[3 * s + k] = m.param[s][k];
+      if (body) body[3 * s + k] = m.rbody[s][k];
+      if (param) param[3 * s + k] = m.rparam[s][k];
     }
   if (mass_inertia) { mass_inertia[0] = m.mass; mass_inertia[1] = m.I[0]; mass_inertia[2] = m.I[1]; mass_inertia[3] = m.I[2]; }
   return G6_OK;
@@ -853,11 +898,11 @@ static int pairlist_call(g6_ctx* ctx, int nsites, const double* x, const double*
                          double* vrmat, bool with_force) {
   if (!ctx || !ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system");
   if (nsites < 0 || npair < 0) return fail(ctx, G6_ERR_ARG, "negative size");
-  if (nsites % ctx->mh.nsite != 0) return fail(ctx, G6_ERR_ARG, "nsites is not a multiple of the model's sites");
+  if (nsites % ctx->mh.nref != 0) return fail(ctx, G6_ERR_ARG, "nsites is not a multiple of the model's sites");
   if (!x || !y || !z || (npair > 0 && (!pi || !pj || !ox || !oy || !oz || !er || !ep)))
     return fail(ctx, G6_ERR_ARG, "NULL array");
   if (with_force && (!fx || !fy || !fz || !vrmat || (npair > 0 && !fr))) return fail(ctx, G6_ERR_ARG, "NULL array");
-  const int nmol = nsites / ctx->mh.nsite;
+  const int nmol = nsites / ctx->mh.nref;
   for (int64_t k = 0; k < npair; ++k)
     if (pi[k] < 0 || pi[k] >= nmol || pj[k] < 0 || pj[k] >= nmol)
       return fail(ctx, G6_ERR_ARG, "pair index out of range");
@@ -896,7 +941,8 @@ static int pairlist_call(g6_ctx* ctx, int nsites, const double* x, const double*
   CK(cudaMemsetAsync(dvir, 0, 9 * 8, s));
   SitesArgs a;
   std::memset(&a, 0, sizeof a);
-  a.nsite = ctx->mh.nsite; a.nq = ctx->nq; a.npair = npair; a.x = dx; a.y = dy; a.z = dz;
+  a.nsite = ctx->mh.nref; a.nq = ctx->nq; a.npair = npair; a.x = dx; a.y = dy; a.z = dz;
+  for (int s = 0; s < MAXSITE; ++s) a.site[s] = ctx->mh.site[s];
   a.fx = dfx; a.fy = dfy; a.fz = dfz; a.pi = dpi; a.pj = dpj; a.ox = dox; a.oy = doy; a.oz = doz; a.hh = dhh;
   a.dh = ddh; a.ep = dep; a.vir = dvir; a.pc = ctx->pc; a.with_force = with_force ? 1 : 0;
   CK(launch_force_sites(a, ctx->model, s));

@@ -460,7 +460,7 @@ static cudaError_t launch_force_m(const ForceArgs& a, const StepArgs& sa, bool m
 template <bool FUSED>
 static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int model, bool mixed, int lpi,
                                     cudaStream_t s) {
-  if (model == G6_TIP4P) return launch_force_m<MT<3, false>, FUSED>(a, sa, mixed, lpi, s);
+  if (model_nq(model) == 3) return launch_force_m<MT<3, false>, FUSED>(a, sa, mixed, lpi, s);
   if (a.pc.taper) return launch_force_m<MT<4, true>, FUSED>(a, sa, mixed, lpi, s);
   return launch_force_m<MT<4, false>, FUSED>(a, sa, mixed, lpi, s);
 }
@@ -478,8 +478,8 @@ cudaError_t launch_step(const ForceArgs& a, const StepArgs& sa, int model, bool 
   return launch_force_any<true>(a, sa, model, mixed, lpi, s);
 }
 
-int pk64_width(int model) { return model == G6_TIP4P ? MT<3, false>::W64 : MT<4, false>::W64; }
-int pk32_width(int model) { return model == G6_TIP4P ? MT<3, false>::NPK : MT<4, false>::NPK; }
+int pk64_width(int model) { return model_nq(model) == 3 ? MT<3, false>::W64 : MT<4, false>::W64; }
+int pk32_width(int model) { return model_nq(model) == 3 ? MT<3, false>::NPK : MT<4, false>::NPK; }
 
 // ---------------------------------------------------------------------------
 // Pair-list kernels for the reference-facing calls g6_force_sites and
@@ -495,6 +495,9 @@ __global__ void __launch_bounds__(128) k_force_sites(SitesArgs a) {
   if (k < a.npair) {
     const int ns = a.nsite, last = ns - 1;
     const int ii = a.pi[k] * ns, jj = a.pj[k] * ns;
+    int st[NQ + 1];   // reference site of the LJ site and of each charged site
+#pragma unroll
+    for (int s = 0; s <= NQ; ++s) st[s] = a.site[s];
     const double ox = a.ox[k], oy = a.oy[k], oz = a.oz[k];
     const double hh = a.hh[k], dh = a.with_force ? a.dh[k] : 0.0;
     double d[3] = {a.x[ii + last] - a.x[jj + last] - ox, a.y[ii + last] - a.y[jj + last] - oy,
@@ -505,7 +508,8 @@ __global__ void __launch_bounds__(128) k_force_sites(SitesArgs a) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) fi[s][c] = fj[s][c] = 0.0;
     // LJ site pair
-    double vx = a.x[ii] - a.x[jj] - ox, vy = a.y[ii] - a.y[jj] - oy, vz = a.z[ii] - a.z[jj] - oz;
+    double vx = a.x[ii + st[0]] - a.x[jj + st[0]] - ox, vy = a.y[ii + st[0]] - a.y[jj + st[0]] - oy,
+           vz = a.z[ii + st[0]] - a.z[jj + st[0]] - oz;
     double inv = 1.0 / (vx * vx + vy * vy + vz * vz);
     double d6 = inv * inv * inv, d12 = d6 * d6;
     double elj = a.pc.aa * d12 + a.pc.bb * d6;
@@ -516,8 +520,8 @@ __global__ void __launch_bounds__(128) k_force_sites(SitesArgs a) {
     for (int p = 1; p <= NQ; ++p)
 #pragma unroll
       for (int q = 1; q <= NQ; ++q) {
-        double x = a.x[ii + p] - a.x[jj + q] - ox, y = a.y[ii + p] - a.y[jj + q] - oy,
-               z = a.z[ii + p] - a.z[jj + q] - oz;
+        double x = a.x[ii + st[p]] - a.x[jj + st[q]] - ox, y = a.y[ii + st[p]] - a.y[jj + st[q]] - oy,
+               z = a.z[ii + st[p]] - a.z[jj + st[q]] - oz;
         double dd = 1.0 / (x * x + y * y + z * z);
         double ri = sqrt(dd);
         double e0 = a.pc.qq[p - 1][q - 1] * ri;
@@ -553,10 +557,10 @@ __global__ void __launch_bounds__(128) k_force_sites(SitesArgs a) {
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) { fi[NQ + 1][c] = fcom * d[c]; fj[NQ + 1][c] = fcom * d[c]; fp[c] += fcom * d[c]; }
-      // site index of the COM is the last site; charged sites are 1..NQ; LJ site 0
+      // the COM is the last reference site; the others map through st
 #pragma unroll
       for (int s = 0; s < NQ + 2; ++s) {
-        int si = (s == NQ + 1) ? last : s;
+        int si = (s == NQ + 1) ? last : st[s];
         atomicAdd(&a.fx[ii + si], fi[s][0]); atomicAdd(&a.fy[ii + si], fi[s][1]); atomicAdd(&a.fz[ii + si], fi[s][2]);
         atomicAdd(&a.fx[jj + si], -fj[s][0]); atomicAdd(&a.fy[jj + si], -fj[s][1]); atomicAdd(&a.fz[jj + si], -fj[s][2]);
       }
@@ -589,7 +593,7 @@ cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s) {
   const int threads = 128;
   const long long blocks = (a.npair + threads - 1) / threads;
   if (blocks == 0) return cudaSuccess;
-  if (model == G6_TIP4P) k_force_sites<3, false><<<(unsigned)blocks, threads, 0, s>>>(a);
+  if (model_nq(model) == 3) k_force_sites<3, false><<<(unsigned)blocks, threads, 0, s>>>(a);
   else if (a.pc.taper) k_force_sites<4, true><<<(unsigned)blocks, threads, 0, s>>>(a);
   else k_force_sites<4, false><<<(unsigned)blocks, threads, 0, s>>>(a);
   return cudaGetLastError();

@@ -199,6 +199,7 @@ struct ForceArgs {
 
 struct SitesArgs {
   int nsite, nq;
+  int site[MAXSITE];   // reference site index of kernel site s (LJ site, charged sites)
   long long npair;
   const double *x, *y, *z;
   double *fx, *fy, *fz;
@@ -321,12 +322,21 @@ struct ExchArgs {
 // ---------------------------------------------------------------------------
 // Host-side declarations shared between translation units.
 // ---------------------------------------------------------------------------
+// body/param: the kernels' site layout (LJ site, then the nq charged sites);
+// rbody/rparam: the reference's site arrays (nref sites, the last one the COM);
+// site[s]: reference index of kernel site s (SPC/E: the oxygen is both the LJ
+// site and a charged site).
 struct ModelHost {
-  int model = 0, nsite = 0, nq = 0;
+  int model = 0, nsite = 0, nq = 0, nref = 0;
   double body[MAXSITE][3] = {};
   double param[MAXSITE][3] = {};   // q, eps, sig
+  double rbody[MAXSITE][3] = {};
+  double rparam[MAXSITE][3] = {};
+  int site[MAXSITE] = {};
   double mass = 0, I[3] = {};
 };
+// charged sites of a model's kernels: 3 (TIP4P, SPC/E) or 4 (TIP5P, ST2)
+inline int model_nq(int model) { return (model == G6_TIP4P || model == G6_SPCE) ? 3 : 4; }
 bool make_model(int model, ModelHost& m);
 void make_pair_const(const ModelHost& m, int path, PairConst& pc);
 void make_cut_const(double rin, double rout, CutConst& cc);

@@ -1065,7 +1065,7 @@ static cudaError_t launch_mc_t(const McArgs& a, bool mixed, int mode, cudaStream
 }
 
 cudaError_t launch_mc(const McArgs& a, int model, bool mixed, int mode, cudaStream_t s) {
-  if (model == G6_TIP4P) return launch_mc_t<3, false>(a, mixed, mode, s);
+  if (model_nq(model) == 3) return launch_mc_t<3, false>(a, mixed, mode, s);
   if (a.pc.taper) return launch_mc_t<4, true>(a, mixed, mode, s);
   return launch_mc_t<4, false>(a, mixed, mode, s);
 }

@@ -43,7 +43,7 @@ import numpy as np
 
 REC = 53
 NOSE_OLD_UNIT = 21.8852721616497249235   # NoseModule.F90:101 (@NOSE q scale, squared)
-MODEL_IDS = {"TIP4P": "TIP4P   ", "TIP5P": "TIP5P   ", "ST2": "ST2_____"}   # RigidSetup.F90:33-58
+MODEL_IDS = {"TIP4P": "TIP4P   ", "TIP5P": "TIP5P   ", "ST2": "ST2_____", "SPCE": "SPC_E   "}   # RigidSetup.F90:33-58; SPCEModule.F90:19
 ID_MODELS = {v.strip("_ ").upper(): k for k, v in MODEL_IDS.items()}
 
 

@@ -38,6 +38,7 @@ extern "C" {
 #define G6_TIP4P 1 /* O, M, H, H, COM      TIP4PModule.F90:43-97               */
 #define G6_TIP5P 2 /* O, H, H, L, L, COM   TIP5PModule.F90:57-83, RigidModule.F90:429-477 */
 #define G6_ST2 3   /* O, H, H, M, M, COM   ST2Module.F90:10-100                */
+#define G6_SPCE 4  /* O, H, H, COM         SPCEModule.F90:8-71 (StdForce path only) */
 
 /* force path, the reference's `custom` flag (@FAST) of Interaction2.F90:19-68 */
 #define G6_PATH_STD 0    /* StdForce / StdPairPotential (LB mixing, no ST2 taper)   */

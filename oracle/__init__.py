@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "g6_oracle.cpp")
 LIB = os.path.join(HERE, "libg6oracle.so")
 
-MODEL = {"TIP4P": 1, "TIP5P": 2, "ST2": 3}
+MODEL = {"TIP4P": 1, "TIP5P": 2, "ST2": 3, "SPCE": 4}
 PATH = {"std": 0, "custom": 1}
 REC = 53  # per-molecule rigid record: com[3], d[5][3], w[5][3], q[5][4]
 

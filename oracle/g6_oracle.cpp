@@ -82,7 +82,7 @@ inline double dnint(double x) { return std::round(x); }
 // ---------------------------------------------------------------------------
 // Models
 // ---------------------------------------------------------------------------
-enum { M_TIP4P = 1, M_TIP5P = 2, M_ST2 = 3 };
+enum { M_TIP4P = 1, M_TIP5P = 2, M_ST2 = 3, M_SPCE = 4 };
 enum { P_STD = 0, P_CUSTOM = 1 };
 const int MAXS = 8;
 
@@ -146,11 +146,34 @@ void model_st2(Model& m) {
   m.eps[0] = ST2_EPS; m.sig[0] = ST2_SIG;
 }
 
+// SPC/E: Rigid_SPCE_Constructor SPCEModule.F90:44-71, spce_setinteraction :24-43
+// (the oxygen carries both the charge and the LJ site; StdForce only).
+void model_spce(Model& m) {
+  m.id = M_SPCE; m.nsite = 4;
+  const double theta = 109.5 * PI / 180.0, l1 = 1.0, hmass = 1.0, omass = 16.0;
+  m.molx[0] = 0; m.moly[0] = 0; m.molz[0] = 0;
+  m.molx[1] = 0; m.moly[1] = l1 * std::sin(0.5 * theta); m.molz[1] = l1 * std::cos(0.5 * theta);
+  m.molx[2] = 0; m.moly[2] = -l1 * std::sin(0.5 * theta); m.molz[2] = l1 * std::cos(0.5 * theta);
+  double zshift = m.molz[1] * 2.0 * hmass / (2.0 * hmass + omass);
+  for (int i = 0; i < 3; ++i) m.molz[i] = m.molz[i] - zshift;
+  m.molx[3] = m.moly[3] = m.molz[3] = 0;
+  m.Ixx = omass * (m.moly[0] * m.moly[0] + m.molz[0] * m.molz[0]) +
+          hmass * (m.moly[1] * m.moly[1] + m.molz[1] * m.molz[1]) * 2.0;
+  m.Iyy = omass * (m.molz[0] * m.molz[0] + m.molx[0] * m.molx[0]) +
+          hmass * (m.molz[1] * m.molz[1] + m.molx[1] * m.molx[1]) * 2.0;
+  m.Izz = omass * (m.molx[0] * m.molx[0] + m.moly[0] * m.moly[0]) +
+          hmass * (m.molx[1] * m.molx[1] + m.moly[1] * m.moly[1]) * 2.0;
+  m.mass = 2.0 * hmass + omass;
+  m.q[0] = -0.8476; m.q[1] = 0.4238; m.q[2] = 0.4238;
+  m.eps[0] = 78.208 / J2K * 1e-3; m.sig[0] = 3.166;
+}
+
 bool make_model(int id, Model& m) {
   m = Model();
   if (id == M_TIP4P) model_tip4p(m);
   else if (id == M_TIP5P) model_tip5p(m);
   else if (id == M_ST2) model_st2(m);
+  else if (id == M_SPCE) model_spce(m);
   else return false;
   return true;
 }

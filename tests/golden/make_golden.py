@@ -3,7 +3,7 @@
 Genesis6 ships no test vectors, so these are computed here independently of
 the oracle: a direct Python statement of the model definitions (site geometry
 and parameters of TIP4PModule.F90:43-97, TIP5PModule.F90:38-83,
-RigidModule.F90:429-477, ST2Module.F90:10-100) and of the pair energy (site
+RigidModule.F90:429-477, ST2Module.F90:10-100, SPCEModule.F90:8-71) and of the pair energy (site
 sums of Coulomb and 12-6 LJ scaled by the centre-of-mass switch of
 CutoffModule.F90:38-59, and for ST2 the Coulomb taper of ST2Module.F90:206-225).
 Forces and torques come from 4th-order central finite differences of that
@@ -38,6 +38,12 @@ def geometry(model):
         q = [0, -1.04, 0.52, 0.52, 0]
         eps, sig = 0.15504166666666666666666 * CA, 3.15357794197649532464
         return np.array(body, float), np.array(q, float), eps, sig
+    if model == "SPCE":   # the oxygen carries both the LJ site and a charge
+        th = 109.5 * PI / 180
+        s, c = math.sin(0.5 * th), math.cos(0.5 * th)
+        body = np.array([[0, 0, 0], [0, s, c], [0, -s, c], [0, 0, 0]], float)
+        body[:3, 2] -= body[1, 2] * 2.0 / 18.0
+        return body, np.array([-0.8476, 0.4238, 0.4238, 0.0]), 78.208 / 0.120273 * 1e-3, 3.166
     if model == "TIP5P":
         theta, phi, l1, l2 = 104.52 * PI / 180, 109.47 * PI / 180, 0.9572, 0.70
         q = [0, 0.2410, 0.2410, -0.2410, -0.2410, 0]
@@ -100,8 +106,10 @@ def dimer_energy(model, custom, off_i, off_j, ci, cj, L, rin, rout):
         qq = lambda a, b: q[a] * q[b] * COEFF * 100.0
     ns = len(q)
     ecoul = 0.0
-    for a in range(1, ns - 1):
-        for b in range(1, ns - 1):
+    for a in range(0, ns - 1):          # every charged site (site 0 only for SPC/E)
+        for b in range(0, ns - 1):
+            if q[a] == 0.0 or q[b] == 0.0:
+                continue
             v = d + off_i[a] - off_j[b]
             ecoul += qq(a, b) / math.sqrt(v @ v)
     v = d + off_i[0] - off_j[0]
@@ -158,8 +166,8 @@ def dimers():
     L = np.array([20.0, 20.0, 20.0])
     seps = [("full", [2.9, 0.3, -0.2]), ("switch", [7.3, 0.4, 0.5]), ("image", [-17.0, 0.3, 0.2]),
             ("outside", [8.6, 0.3, 0.0])]
-    for model in ["TIP4P", "TIP5P", "ST2"]:
-        for custom in ([True, False] if model != "TIP5P" else [False]):
+    for model in ["TIP4P", "TIP5P", "ST2", "SPCE"]:
+        for custom in ([True, False] if model in ("TIP4P", "ST2") else [False]):
             for name, sep in seps:
                 quat = [unit(rng.standard_normal(4)), unit(rng.standard_normal(4))]
                 c0 = np.array([0.5, -0.3, 0.2])

@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_model_tables_match_oracle(orc):
-    for m in ("TIP4P", "TIP5P", "ST2"):
+    for m in ("TIP4P", "TIP5P", "ST2", "SPCE"):
         a = g6.model_info(m)
         b = orc.model_info(m)
         assert a["nsite"] == b["nsite"]

@@ -43,16 +43,17 @@ def _mc(s, ntrial, seed, counter, beta, st, sr, mode=_capi.MC_PLAIN, sample_ever
     return counts.reshape(R, 2), energy, trace, samples
 
 
-def test_mc_fp64_replays_oracle(orc):
-    s, recs, rc = _chains("ST2", 2, 216, 40)
+@pytest.mark.parametrize("model", ["ST2", "TIP4P", "SPCE"])
+def test_mc_fp64_replays_oracle(orc, model):
+    s, recs, rc = _chains(model, 2, 216, 40)
     beta = 1.0 / 260.0
     ntrial = 300
     counts, energy, trace, _ = _mc(s, ntrial, 99, 0, beta, 0.15, 0.15)
     rec_g = s.download_state()
     for c, b in enumerate(recs):
         L = b["L"]
-        E0 = orc.compute("ST2", "custom", b["com"], b["quat"], L, [rc] * 3, rc - 2.0, rc)[2]
-        com, quat, e, tr = orc.mc_run("ST2", "custom", b["com"], b["quat"], L, rc - 2.0, rc, beta, 0.15, 0.15, ntrial,
+        E0 = orc.compute(model, "custom", b["com"], b["quat"], L, [rc] * 3, rc - 2.0, rc)[2]
+        com, quat, e, tr = orc.mc_run(model, "custom", b["com"], b["quat"], L, rc - 2.0, rc, beta, 0.15, 0.15, ntrial,
                                       99, c, 0, E0)
         assert np.array_equal(trace[c, :, 3], tr[:, 3])          # same targets
         assert np.array_equal(trace[c, :, 2], tr[:, 2])          # same decisions

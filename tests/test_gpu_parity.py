@@ -16,7 +16,7 @@ from genesis6_gb300.interaction import Interaction, Sites, force, pair_potential
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "std"), ("ST2", "custom"), ("ST2", "std")]
+CASES = [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "std"), ("ST2", "custom"), ("ST2", "std"), ("SPCE", "std")]
 
 
 def _system(model, path, n, seed, prec="fp64", rc=8.5, jitter=0.4, skin=1.0, cell_edge=0.0):
@@ -126,7 +126,7 @@ def test_force_sites_entry_matches_reference_call(orc, model, path):
     assert np.abs(hx - x).max() < 1e-12
 
 
-@pytest.mark.parametrize("model,path", [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "custom"), ("ST2", "custom"),
+@pytest.mark.parametrize("model,path", [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "custom"), ("ST2", "custom"), ("SPCE", "std"),
                                         ("ST2", "std")])
 def test_md_fp64_follows_oracle(orc, model, path):
     """Short Gear MD: the device trajectory tracks the oracle's step by step."""
