@@ -460,6 +460,38 @@ def bench_mc(torch, seed=20261203, sweeps=2000, records=1_000_000, equil_sweeps=
             "U_unit": "10 J/mol per chain (internal)"}
 
 
+def bench_rdf(torch, n=N_BIG, rc=9.0, nbin=200, width=0.05, reps=5, seed=20261207):
+    """Site-site distance histogram of a 32,768-molecule TIP4P configuration
+    (g6_rdf: pair search, FP64 site positions, shared-memory histogram, read
+    back) against the oracle's numpy counting of the same configuration on one
+    host core; the two histograms must be equal."""
+    import genesis6_gb300 as g6
+    from genesis6_gb300 import config
+    from oracle import analysis as orc_analysis
+    b = config.water_box("TIP4P", n, seed, temp=TEMP, dt=DT)
+    s = make_system("TIP4P", n, "mixed", b["L"], b["rec"])
+    s.md_run(DT, 200, thermo_for(s), log=False)
+    rec = s.download_state()
+    s.rdf_counts(nbin, width)                      # warm-up (allocations, first launch)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        h = s.rdf_counts(nbin, width)
+    gpu_ms = (time.perf_counter() - t0) / reps * 1e3
+    npair = ctypes.c_int64()
+    s._check(s.L.g6_pairsearch(s.ctx, ctypes.byref(npair)))
+    s.close()
+    com, quat = rec[:, 0:3], rec[:, 33:37]
+    t0 = time.perf_counter()
+    ho = orc_analysis.rdf_counts("TIP4P", com, quat, np.asarray(b["L"], float), rc, nbin, width)
+    cpu_s = time.perf_counter() - t0
+    return {"molecules": n, "pairs_within_rc": int(npair.value), "site_pairs_per_pair": 25, "nbin": nbin,
+            "binwidth_A": width, "gpu_ms_per_call": gpu_ms,
+            "cpu_baseline": {"s_per_call": cpu_s, "kind": "port", "cores": 1,
+                             "sample": "the same configuration, oracle pair search + numpy counting"},
+            "equal_to_cpu": bool(np.array_equal(h[0], ho)),
+            "timing": "wall clock per g6_rdf call (pair search + positions + histogram + read-back)"}
+
+
 def bench_rms(torch, rec_eq, L, snapshots=100, every=20):
     """Relative RMS force and torque error of the mixed path on `snapshots`
     configurations of a TIP4P-4096 Nose-Hoover trajectory (one every `every`
@@ -618,6 +650,7 @@ def run_gpu(args, rank, world, local):
     rms = None if args.no_extra else bench_rms(torch, rec_eq, L)
     t5p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP5P")
     t4p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP4P", seed=20261206)
+    rdf = None if (args.no_extra or args.no_32k) else bench_rdf(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -630,6 +663,7 @@ def run_gpu(args, rank, world, local):
         "mixed_rms_error_4096": rms,
         "replica_exchange": rex,
         "mc_learned_vs_fixed": mcb,
+        "rdf_32k": rdf,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
                      "kernel": "k_force<TIP4P, mixed, fused step> (site loop + Gear corrector epilogue)",

@@ -892,6 +892,50 @@ static int ensure_scratch(g6_ctx* ctx, size_t bytes) {
   return G6_OK;
 }
 
+// radialdistrib (RDFModule.F90:101-137) on the device pair set of the uploaded
+// poses: FP64 site positions, then one shared-memory histogram per block.
+int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* hist) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!hist || nbin <= 0 || !(binwidth > 0.0)) return fail(ctx, G6_ERR_ARG, "hist, nbin > 0 and binwidth > 0 are needed");
+  const int ns = ctx->mh.nref;
+  const size_t smem = rdf_smem_bytes(ctx->nrep, ns, nbin);
+  if (smem > 200 * 1024)
+    return fail(ctx, G6_ERR_CAPACITY, "histogram of all replicas exceeds 200 KB of shared memory (nrep x nsite^2 x nbin x 4)");
+  int64_t np = 0;
+  rc = g6_pairsearch(ctx, &np);
+  if (rc) return rc;
+  const size_t nh = (size_t)ctx->nrep * ns * ns * nbin;
+  const size_t pos_bytes = ((size_t)ctx->n * ns * 3 * sizeof(double) + 255) & ~(size_t)255;
+  const size_t off_bytes = ((size_t)ctx->n * ns * 3 * sizeof(float) + 255) & ~(size_t)255;
+  rc = ensure_scratch(ctx, pos_bytes + off_bytes + nh * sizeof(unsigned long long));
+  if (rc) return rc;
+  double* pos = (double*)ctx->d_scratch;
+  float* off = (float*)((char*)ctx->d_scratch + pos_bytes);
+  unsigned long long* dh = (unsigned long long*)((char*)ctx->d_scratch + pos_bytes + off_bytes);
+  SitePosArgs sp;
+  std::memset(&sp, 0, sizeof sp);
+  sp.n = ctx->n; sp.nsite = ns; sp.st = ctx->d_st; sp.pos = pos; sp.off = off;
+  for (int s = 0; s < ns; ++s)
+    for (int k = 0; k < 3; ++k) sp.body[s][k] = ctx->mh.rbody[s][k];
+  CK(launch_site_positions(sp, ctx->stream));
+  CK(cudaMemsetAsync(dh, 0, nh * sizeof(unsigned long long), ctx->stream));
+  RdfArgs ra;
+  std::memset(&ra, 0, sizeof ra);
+  ra.npair = np; ra.nrep = ctx->nrep; ra.nsite = ns; ra.nbin = nbin; ra.binwidth = binwidth; ra.minvalue = minvalue;
+  ra.off_rep = ctx->d_off; ra.pi = ctx->d_pi; ra.pj = ctx->d_pj; ra.ox = ctx->d_ox; ra.oy = ctx->d_oy; ra.oz = ctx->d_oz;
+  ra.pos = pos; ra.off = off; ra.st = ctx->d_st; ra.n = ctx->n; ra.hist = dh;
+  ra.fp64_only = ctx->cc.rout > 30.0;   // the FP32 distance bound holds for separations below 32 A
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+  CK(launch_rdf(ra, nsm, ctx->stream));
+  std::vector<unsigned long long> h(nh);
+  CK(cudaMemcpyAsync(h.data(), dh, nh * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t k = 0; k < nh; ++k) hist[k] += (int64_t)h[k];
+  return G6_OK;
+}
+
 static int pairlist_call(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, double* fx,
                          double* fy, double* fz, int64_t npair, const int* pi, const int* pj, const double* ox,
                          const double* oy, const double* oz, const double* er, const double* fr, double* ep,

@@ -322,6 +322,33 @@ struct ExchArgs {
 // ---------------------------------------------------------------------------
 // Host-side declarations shared between translation units.
 // ---------------------------------------------------------------------------
+// FP64 site positions of every molecule in the reference's site layout.
+struct SitePosArgs {
+  int n, nsite;
+  double body[MAXSITE][3];
+  const double* st;
+  double* pos;   // (n, nsite, 3)
+  float* off;    // (n, nsite, 3): R(q) body, the offsets of pos from the COM, in FP32
+};
+// Site-site distance histograms over a pair set (g6_analysis.cu).
+struct RdfArgs {
+  long long npair;
+  int nrep, nsite, nbin;
+  double binwidth, minvalue;
+  const int* off_rep;             // replica offsets (nrep + 1)
+  const int *pi, *pj;
+  const double *ox, *oy, *oz;
+  const double* pos;
+  const float* off;
+  const double* st;               // COM: st[0..2][i]
+  int n;
+  int fp64_only;                  // every distance in FP64 (cutoffs beyond the FP32 bound)
+  unsigned long long* hist;       // (nrep, nsite, nsite, nbin), a <= b only
+};
+cudaError_t launch_site_positions(const SitePosArgs& a, cudaStream_t s);
+cudaError_t launch_rdf(const RdfArgs& a, int num_sms, cudaStream_t s);
+size_t rdf_smem_bytes(int nrep, int nsite, int nbin);
+
 // body/param: the kernels' site layout (LJ site, then the nq charged sites);
 // rbody/rparam: the reference's site arrays (nref sites, the last one the COM);
 // site[s]: reference index of kernel site s (SPC/E: the oxygen is both the LJ

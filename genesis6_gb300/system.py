@@ -113,6 +113,16 @@ class RigidWater:
         self._check(self.L.g6_molecule_energies(self.ctx, dptr(e)))
         return e
 
+    def rdf_counts(self, nbin, binwidth, minvalue=0.0):
+        """Site-site distance counts of the uploaded poses (radialdistrib,
+        RDFModule.F90:101-137): (nrep, nsite, nsite, nbin) int64, site pair
+        a <= b counted over both orders of each molecule pair within the cutoff."""
+        ns = self.info["nsite"]
+        h = np.zeros((self.nrep, ns, ns, int(nbin)), dtype=np.int64)
+        self._check(self.L.g6_rdf(self.ctx, int(nbin), float(binwidth), float(minvalue),
+                                  h.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return h
+
     # -- dynamics ---------------------------------------------------------
     @staticmethod
     def thermostats(nrep, kind="nve", temp=300.0, q=0.0, dump=0.0, rate=0.0, seed=0):

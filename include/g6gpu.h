@@ -131,6 +131,17 @@ int g6_get_pairs(g6_ctx* ctx, int64_t cap, int* pi, int* pj, double* ox, double*
 int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir);
 /* Per-molecule potential energy e_i = 1/2 sum_j e_ij (n) of the uploaded poses. */
 int g6_molecule_energies(g6_ctx* ctx, double* e);
+/* Site-site distance histograms of the uploaded poses, radialdistrib
+   (RDFModule.F90:101-137): over the within-cutoff pair set (g6_pairsearch),
+   for each replica r and each pair of reference sites a <= b (nsite of
+   g6_model_info, COM included), the molecule pairs with site a of one molecule
+   and site b of the other (either order) at distance r go to bin
+   nint((r - minvalue) / binwidth) when 0 <= bin < nbin (Histogram_Accumulate,
+   DistribModule.F90:149-158).  Counts are ADDED to hist[((r*nsite + a)*nsite
+   + b)*nbin + bin]; entries with a > b stay untouched.  Positions and distances
+   are FP64.  G6_ERR_CAPACITY when nrep * nsite^2 * nbin * 4 bytes exceeds
+   200 KB. */
+int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* hist);
 
 /* The reference `force(iv,mi,mj,site,ep,vrmat,custom,si,sj)` call,
    Interaction2.F90:19-68, for one homogeneous component: caller-owned site
