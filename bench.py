@@ -479,17 +479,30 @@ def bench_rdf(torch, n=N_BIG, rc=9.0, nbin=200, width=0.05, reps=5, seed=2026120
     gpu_ms = (time.perf_counter() - t0) / reps * 1e3
     npair = ctypes.c_int64()
     s._check(s.L.g6_pairsearch(s.ctx, ctypes.byref(npair)))
+    s.hbonds()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        hb = s.hbonds()
+    hb_ms = (time.perf_counter() - t0) / reps * 1e3
     s.close()
     com, quat = rec[:, 0:3], rec[:, 33:37]
     t0 = time.perf_counter()
     ho = orc_analysis.rdf_counts("TIP4P", com, quat, np.asarray(b["L"], float), rc, nbin, width)
     cpu_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hbo = orc_analysis.hbonds("TIP4P", com, quat, np.asarray(b["L"], float), rc)
+    hb_cpu_s = time.perf_counter() - t0
+    hb_equal = set(map(tuple, hb.tolist())) == set(map(tuple, hbo.tolist()))
     return {"molecules": n, "pairs_within_rc": int(npair.value), "site_pairs_per_pair": 25, "nbin": nbin,
             "binwidth_A": width, "gpu_ms_per_call": gpu_ms,
             "cpu_baseline": {"s_per_call": cpu_s, "kind": "port", "cores": 1,
                              "sample": "the same configuration, oracle pair search + numpy counting"},
             "equal_to_cpu": bool(np.array_equal(h[0], ho)),
-            "timing": "wall clock per g6_rdf call (pair search + positions + histogram + read-back)"}
+            "timing": "wall clock per g6_rdf call (pair search + positions + histogram + read-back)",
+            "hbonds": {"bonds": int(len(hb)), "gpu_ms_per_call": hb_ms, "cpu_baseline_s_per_call": hb_cpu_s,
+                       "equal_to_cpu": bool(hb_equal),
+                       "timing": "wall clock per RigidWater.hbonds call (pair search, positions, "
+                                 "O-H test, compaction, read-back of the bonds)"}}
 
 
 def bench_rms(torch, rec_eq, L, snapshots=100, every=20):

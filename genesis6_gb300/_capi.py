@@ -32,7 +32,7 @@ SYMBOLS = [
     "g6_version", "g6_last_error", "g6_status_string", "g6_model_info", "g6_ctx_create", "g6_ctx_destroy",
     "g6_system", "g6_set_cutoff", "g6_set_grid", "g6_set_skin", "g6_set_box", "g6_upload_state",
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
-    "g6_molecule_energies", "g6_rdf", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
+    "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
     "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
     "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
@@ -88,6 +88,7 @@ def lib():
     L.g6_force.argtypes = [vp, dp, dp, dp, dp]
     L.g6_molecule_energies.argtypes = [vp, dp]
     L.g6_rdf.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(i64)]
+    L.g6_hbonds.argtypes = [vp, i64, ip, ip, ip, ctypes.POINTER(i64)]
     L.g6_force_sites.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, i64, ip, ip, dp, dp, dp, dp, dp, dp, dp]
     L.g6_pair_potential.argtypes = [vp, ctypes.c_int, dp, dp, dp, i64, ip, ip, dp, dp, dp, dp, dp]
     L.g6_md_run.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Thermostat), dp]

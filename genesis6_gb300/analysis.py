@@ -52,3 +52,15 @@ def rdf(counts, model: str, nmol: int, volume: float, nconf: int, binwidth: floa
             K = nconf * nmol * len(groups[A]) * len(groups[B]) * (nmol - 1) / (2.0 * volume)
             out[(A, B)] = s_ab / (K * shell) / (2.0 if A != B else 1.0)
     return r, out
+
+
+def graph_text(bonds, nmol: int, kind: str = "NGPH") -> str:
+    """@NGPH (donor, acceptor) or @WGPH (donor, acceptor, hydrogen) lines of
+    interaction_SaveGraph (InteractionModule.F90:783-823): 0-based molecules in
+    '(99i5)' fields, terminated by -1 entries."""
+    bonds = np.asarray(bonds).reshape(-1, 3)
+    out = ["@" + kind, " %d" % nmol]
+    for f, w, t in bonds:
+        out.append("%5d%5d" % (f, t) + ("%5d" % w if kind == "WGPH" else ""))
+    out.append("%5d%5d" % (-1, -1) + ("%5d" % -1 if kind == "WGPH" else ""))
+    return "\n".join(out) + "\n"

@@ -118,6 +118,62 @@ __global__ void __launch_bounds__(256) k_rdf(RdfArgs a) {
     if (s_hist[k]) atomicAdd(&a.hist[k], (unsigned long long)s_hist[k]);
 }
 
+// interaction_hb_by_oh_distance (InteractionModule.F90:682-777), one pair per
+// thread: the squared O-H distances O(i)-H1(j), O(i)-H2(j), O(j)-H1(i),
+// O(j)-H2(i) in that order (dx = x - x - o in FP64, the reference's order), the
+// first strict minimum; below 2.5^2 A^2 the molecule whose hydrogen it is, is
+// the donor (from), the other the acceptor (to).  Bonds are appended to the
+// output (one atomic per warp), so their order is not the pair order.
+__global__ void __launch_bounds__(256) k_hbonds(HbArgs a) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  bool bond = false;
+  int f = -1, w = 0, t = -1;
+  if (k < a.npair) {
+  const int i = a.pi[k], j = a.pj[k], ns = a.nsite;
+  const double o[3] = {a.ox[k], a.oy[k], a.oz[k]};
+  double dmin = 1e10;
+  int pmin = 0, wmin = 0, p = 0;
+  for (int blk = 0; blk < 2; ++blk) {
+    const int mo = blk == 0 ? i : j, mh = blk == 0 ? j : i;   // molecule of the O, of the H
+    const double* xo = a.pos + ((size_t)mo * ns + a.osite) * 3;
+    for (int h = 0; h < 2; ++h) {
+      const double* xh = a.pos + ((size_t)mh * ns + a.hsite[h]) * 3;
+      // the reference's dx = x(ii) - x(jj) - ox with ii on molecule i, jj on molecule j
+      const double* xi = blk == 0 ? xo : xh;
+      const double* xj = blk == 0 ? xh : xo;
+      const double dx = sub(sub(xi[0], xj[0]), o[0]);
+      const double dy = sub(sub(xi[1], xj[1]), o[1]);
+      const double dz = sub(sub(xi[2], xj[2]), o[2]);
+      const double d = add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz));
+      ++p;
+      if (d < dmin) { dmin = d; pmin = p; wmin = h + 1; }
+    }
+  }
+  if (dmin < 6.25) {
+    bond = true;
+    f = pmin <= 2 ? j : i;
+    w = wmin;
+    t = pmin <= 2 ? i : j;
+  }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, bond);
+  if (m == 0u) return;
+  unsigned long long base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(a.count, (unsigned long long)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  if (bond) {
+    const long long pos = (long long)base + __popc(m & ((1u << lane) - 1u));
+    if (pos < a.cap) { a.from[pos] = f; a.which[pos] = w; a.to[pos] = t; }
+  }
+}
+
+cudaError_t launch_hbonds(const HbArgs& a, cudaStream_t s) {
+  if (a.npair == 0) return cudaSuccess;
+  k_hbonds<<<(unsigned)((a.npair + 255) / 256), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_site_positions(const SitePosArgs& a, cudaStream_t s) {
   if (a.n == 0) return cudaSuccess;
   k_site_positions<<<(a.n + 127) / 128, 128, 0, s>>>(a);

@@ -936,6 +936,56 @@ int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* his
   return G6_OK;
 }
 
+// interaction_hb_by_oh_distance (InteractionModule.F90:682-777) on the device
+// pair set: the bonds (donor, its hydrogen 1/2, acceptor), compacted.
+int g6_hbonds(g6_ctx* ctx, int64_t cap, int* from, int* which, int* to, int64_t* nbond) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (cap > 0 && (!from || !which || !to)) return fail(ctx, G6_ERR_ARG, "from, which and to are needed");
+  const int ns = ctx->mh.nref;
+  // the oxygen and the two hydrogens in the reference's site names (TIP4PConst.F90:22,
+  // TIP5PModule.F90:51, ST2Module.F90:26, SPCEModule.F90:18)
+  const int osite = 0, h1 = ctx->mh.model == G6_TIP4P ? 2 : 1, h2 = h1 + 1;
+  int64_t np = 0;
+  rc = g6_pairsearch(ctx, &np);
+  if (rc) return rc;
+  const int64_t capd = std::max<int64_t>(std::min<int64_t>(cap, np), 0);
+  const size_t pos_bytes = ((size_t)ctx->n * ns * 3 * sizeof(double) + 255) & ~(size_t)255;
+  const size_t off_bytes = ((size_t)ctx->n * ns * 3 * sizeof(float) + 255) & ~(size_t)255;
+  const size_t out_bytes = ((size_t)capd * sizeof(int) + 255) & ~(size_t)255;
+  rc = ensure_scratch(ctx, pos_bytes + off_bytes + 3 * out_bytes + 256);
+  if (rc) return rc;
+  char* base = (char*)ctx->d_scratch;
+  SitePosArgs sp;
+  std::memset(&sp, 0, sizeof sp);
+  sp.n = ctx->n; sp.nsite = ns; sp.st = ctx->d_st; sp.pos = (double*)base; sp.off = (float*)(base + pos_bytes);
+  for (int s = 0; s < ns; ++s)
+    for (int k = 0; k < 3; ++k) sp.body[s][k] = ctx->mh.rbody[s][k];
+  CK(launch_site_positions(sp, ctx->stream));
+  HbArgs ha;
+  std::memset(&ha, 0, sizeof ha);
+  ha.npair = np; ha.nsite = ns; ha.osite = osite; ha.hsite[0] = h1; ha.hsite[1] = h2;
+  ha.pi = ctx->d_pi; ha.pj = ctx->d_pj; ha.ox = ctx->d_ox; ha.oy = ctx->d_oy; ha.oz = ctx->d_oz; ha.pos = sp.pos;
+  char* outp = base + pos_bytes + off_bytes;
+  ha.cap = capd;
+  ha.from = (int*)outp; ha.which = (int*)(outp + out_bytes); ha.to = (int*)(outp + 2 * out_bytes);
+  ha.count = (unsigned long long*)(outp + 3 * out_bytes);
+  CK(cudaMemsetAsync(ha.count, 0, sizeof(unsigned long long), ctx->stream));
+  CK(launch_hbonds(ha, ctx->stream));
+  unsigned long long total = 0;
+  CK(cudaMemcpyAsync(&total, ha.count, sizeof total, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (nbond) *nbond = (int64_t)total;
+  const size_t m = (size_t)std::min<int64_t>(capd, (int64_t)total);
+  if (m > 0) {
+    CK(cudaMemcpyAsync(from, ha.from, m * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(which, ha.which, m * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(to, ha.to, m * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return G6_OK;
+}
+
 static int pairlist_call(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, double* fx,
                          double* fy, double* fz, int64_t npair, const int* pi, const int* pj, const double* ox,
                          const double* oy, const double* oz, const double* er, const double* fr, double* ep,

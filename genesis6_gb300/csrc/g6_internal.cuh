@@ -345,6 +345,18 @@ struct RdfArgs {
   int fp64_only;                  // every distance in FP64 (cutoffs beyond the FP32 bound)
   unsigned long long* hist;       // (nrep, nsite, nsite, nbin), a <= b only
 };
+// Hydrogen bonds by O-H distance on a pair set (g6_analysis.cu).
+struct HbArgs {
+  long long npair;
+  int nsite, osite, hsite[2];     // reference sites: the oxygen and the two hydrogens
+  const int *pi, *pj;
+  const double *ox, *oy, *oz;
+  const double* pos;
+  long long cap;                  // bonds the output arrays hold
+  unsigned long long* count;      // bonds found (may exceed cap)
+  int *from, *which, *to;         // per bond: donor, its hydrogen (1, 2), acceptor
+};
+cudaError_t launch_hbonds(const HbArgs& a, cudaStream_t s);
 cudaError_t launch_site_positions(const SitePosArgs& a, cudaStream_t s);
 cudaError_t launch_rdf(const RdfArgs& a, int num_sms, cudaStream_t s);
 size_t rdf_smem_bytes(int nrep, int nsite, int nbin);

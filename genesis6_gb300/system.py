@@ -113,6 +113,21 @@ class RigidWater:
         self._check(self.L.g6_molecule_energies(self.ctx, dptr(e)))
         return e
 
+    def hbonds(self):
+        """Hydrogen bonds by O-H distance (interaction_hb_by_oh_distance,
+        InteractionModule.F90:682-777): donor, hydrogen (1, 2), acceptor for
+        each pair that forms one (0-based molecules), as an (m, 3) array."""
+        cap = 4 * self.n
+        while True:
+            f = np.zeros(cap, np.int32); w = np.zeros(cap, np.int32); t = np.zeros(cap, np.int32)
+            nb = ctypes.c_int64()
+            self._check(self.L.g6_hbonds(self.ctx, cap, iptr(f), iptr(w), iptr(t), ctypes.byref(nb)))
+            if nb.value <= cap:
+                break
+            cap = nb.value
+        out = np.stack([f[:nb.value], w[:nb.value], t[:nb.value]], axis=1)
+        return out[np.lexsort((out[:, 2], out[:, 0]))]   # by donor, then acceptor
+
     def rdf_counts(self, nbin, binwidth, minvalue=0.0):
         """Site-site distance counts of the uploaded poses (radialdistrib,
         RDFModule.F90:101-137): (nrep, nsite, nsite, nbin) int64, site pair

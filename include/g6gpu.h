@@ -142,6 +142,16 @@ int g6_molecule_energies(g6_ctx* ctx, double* e);
    are FP64.  G6_ERR_CAPACITY when nrep * nsite^2 * nbin * 4 bytes exceeds
    200 KB. */
 int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* hist);
+/* Hydrogen bonds of the uploaded poses by O-H distance,
+   interaction_hb_by_oh_distance (InteractionModule.F90:682-777): for every
+   pair of the within-cutoff pair set the shortest of the four intermolecular
+   O-H distances (FP64, first strict minimum); below 2.5 A the pair is a bond
+   with donor from[b] (the molecule that owns the hydrogen), which[b] (1 or 2)
+   its hydrogen and acceptor to[b] (0-based molecules).  Only bonds are
+   written, at most cap of them, in no particular order (the reference writes
+   one entry per pair, zeros for pairs without a bond); nbond gets the number
+   of bonds, which may exceed cap. */
+int g6_hbonds(g6_ctx* ctx, int64_t cap, int* from, int* which, int* to, int64_t* nbond);
 
 /* The reference `force(iv,mi,mj,site,ep,vrmat,custom,si,sj)` call,
    Interaction2.F90:19-68, for one homogeneous component: caller-owned site

@@ -44,3 +44,32 @@ def rdf_counts(model, com, quat, L, rc, nbin, binwidth, minvalue=0.0):
             lo, hi = min(a, b), max(a, b)
             hist[lo, hi] += np.bincount(k[ok].astype(np.int64), minlength=nbin)
     return hist
+
+
+def hbonds(model, com, quat, L, rc):
+    """interaction_hb_by_oh_distance (InteractionModule.F90:682-777) over the
+    oracle's pair set: the four squared distances O(i)-H1(j), O(i)-H2(j),
+    O(j)-H1(i), O(j)-H2(i) (dx = x(ii) - x(jj) - ox, ii on molecule i), the first
+    strict minimum, a bond below 2.5^2 A^2 from the hydrogen's molecule.
+    Returns (m, 3) rows (donor, hydrogen 1/2, acceptor), 0-based."""
+    ns = model_info(model)["nsite"]
+    osite, h1 = 0, (2 if model == "TIP4P" else 1)
+    x, y, z = place_sites(model, com, quat)[:3]
+    _, p = pairsearch(com, L, [rc] * 3, rc - 2.0, rc)
+    i, j = p["i"].astype(np.int64), p["j"].astype(np.int64)
+    d = []
+    for blk in range(2):
+        for h in range(2):
+            ii = i * ns + (osite if blk == 0 else h1 + h)
+            jj = j * ns + (h1 + h if blk == 0 else osite)
+            dx = (x[ii] - x[jj]) - p["ox"]
+            dy = (y[ii] - y[jj]) - p["oy"]
+            dz = (z[ii] - z[jj]) - p["oz"]
+            d.append(dx * dx + dy * dy + dz * dz)
+    d = np.stack(d, axis=1)
+    k = np.argmin(d, axis=1)                      # first minimum, as the strict sequential test
+    dmin = d[np.arange(len(k)), k]
+    ok = dmin < 6.25
+    donor = np.where(k <= 1, j, i)
+    acceptor = np.where(k <= 1, i, j)
+    return np.stack([donor[ok], (k % 2 + 1)[ok], acceptor[ok]], axis=1)

@@ -93,3 +93,63 @@ def test_device_counts_per_replica(orc):
     for k, bx in enumerate(boxes):
         ho = A.rdf_counts("TIP4P", bx["com"], bx["quat"], np.asarray(bx["L"], float), 8.0, 120, 0.07, 0.5)
         assert np.array_equal(h[k], ho)
+
+
+def brute_hbonds(orc, model, com, quat, L, rc):
+    """A direct loop over molecule pairs of the reference's O-H test."""
+    ns = orc.model_info(model)["nsite"]
+    h1 = 2 if model == "TIP4P" else 1
+    x, y, z = orc.place_sites(model, com, quat)[:3]
+    out = set()
+    n = len(com)
+    for i in range(n):
+        for j in range(i + 1, n):
+            d = com[i] - com[j]
+            shift = L * np.array([math.copysign(math.floor(abs(v) / Lk + 0.5), v) for v, Lk in zip(d, L)])
+            dd = d - shift
+            if (dd[0] * dd[0] + dd[1] * dd[1]) + dd[2] * dd[2] >= rc * rc:
+                continue
+            best, pb, wb, pnum = 1e10, 0, 0, 0
+            for blk in range(2):
+                for h in range(2):
+                    a = i * ns + (0 if blk == 0 else h1 + h)
+                    b = j * ns + (h1 + h if blk == 0 else 0)
+                    v = np.array([x[a] - x[b], y[a] - y[b], z[a] - z[b]]) - shift
+                    dist = v[0] ** 2 + v[1] ** 2 + v[2] ** 2
+                    pnum += 1
+                    if dist < best:
+                        best, pb, wb = dist, pnum, h + 1
+            if best < 6.25:
+                out.add((j, wb, i) if pb <= 2 else (i, wb, j))
+    return out
+
+
+@pytest.mark.parametrize("model", ["TIP4P", "ST2"])
+def test_oracle_hbonds_follow_the_definition(orc, model):
+    b = config.water_box(model, 64, 4, jitter=0.3)
+    L = np.asarray(b["L"], float)
+    hb = A.hbonds(model, b["com"], b["quat"], L, 6.0)
+    assert len(hb) > 10
+    assert set(map(tuple, hb.tolist())) == brute_hbonds(orc, model, b["com"], b["quat"], L, 6.0)
+
+
+def test_graph_text_layout():
+    txt = analysis.graph_text([[3, 1, 7], [10, 2, 4]], 16, "WGPH")
+    assert txt.splitlines() == ["@WGPH", " 16", "    3    7    1", "   10    4    2", "   -1   -1   -1"]
+    assert analysis.graph_text([[3, 1, 7]], 16).splitlines()[-2:] == ["    3    7", "   -1   -1"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model,n,prec", [("TIP4P", 4096, "mixed"), ("ST2", 512, "fp64"), ("SPCE", 343, "mixed")])
+def test_device_hbonds_equal_oracle(orc, model, n, prec):
+    import genesis6_gb300 as g6
+    b = config.water_box(model, n, 23, temp=300.0, dt=0.002, jitter=0.3)
+    s = g6.RigidWater(model, n, b["L"], path="std", precision=prec, rc=8.5)
+    s.upload_state(b["rec"])
+    # a few short steps away from the lattice (random orientations start hot)
+    s.md_run(0.0005, 40, s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 ** 2 / 0.0005), log=False)
+    rec = s.download_state()
+    hb = s.hbonds()
+    ho = A.hbonds(model, rec[:, 0:3], rec[:, 33:37], np.asarray(b["L"], float), 8.5)
+    assert len(hb) > n // 10
+    assert set(map(tuple, hb.tolist())) == set(map(tuple, ho.tolist()))
