@@ -220,3 +220,18 @@ def test_learned_fp64_chain_replays_reference(orc):
         sl = rec_g[216 * c:216 * (c + 1)]
         assert np.abs(sl[:, :3] - com).max() < 1e-5
         assert np.abs(sl[:, 33:37] - quat).max() < 1e-5
+
+
+def test_feature_pool_overflow_is_reported():
+    """More than 64 molecules within 6 A of a pose (a compressed cluster) ends the
+    run with G6_ERR_CAPACITY instead of silently dropping feature neighbours."""
+    b = config.water_box("ST2", 216, 70, jitter=0.0)
+    rec = b["rec"].copy()
+    c0 = rec[:100, 0:3].mean(axis=0)
+    rec[:100, 0:3] = c0 + (rec[:100, 0:3] - c0) * 0.3      # 100 molecules squeezed into a few A
+    s = g6.RigidWater("ST2", 216, b["L"], path="custom", precision="mixed", rc=0.5 * b["L"][0] - 0.05, skin=0.0)
+    s.upload_state(rec)
+    with pytest.raises(g6.G6Error) as e:
+        _mc(s, 64, 5, 0, 1.0 / 260.0, 0.15, 0.15, mode=_capi.MC_COLLECT)
+    assert e.value.status == _capi.G6_ERR_CAPACITY
+    assert "within 6 A" in str(e.value)
