@@ -33,7 +33,7 @@ SYMBOLS = [
     "g6_system", "g6_set_cutoff", "g6_set_grid", "g6_set_skin", "g6_set_box", "g6_upload_state",
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
     "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
-    "g6_replica_exchange", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
+    "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
     "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
     "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
 ]
@@ -95,6 +95,8 @@ def lib():
     L.g6_md_step_host.argtypes = [vp, ctypes.c_double, ctypes.POINTER(Thermostat), dp, dp]
     L.g6_replica_exchange.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,
                                       ctypes.POINTER(Thermostat), ip]
+    L.g6_replica_exchange_umbrella.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,
+                                               ctypes.POINTER(Thermostat), ctypes.c_int, dp, dp, ip]
     L.g6_md_begin.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Thermostat), ctypes.c_int]
     L.g6_md_advance.argtypes = [vp, ctypes.c_int]
     L.g6_md_end.argtypes = [vp, ctypes.POINTER(Thermostat), dp]

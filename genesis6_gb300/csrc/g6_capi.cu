@@ -1538,13 +1538,24 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   return md_check(ctx, 1, thermo);
 }
 
-int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta, g6_thermostat* thermo,
-                        int* accepted) {
+static int replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
+                            g6_thermostat* thermo, int numb, double* umbrella, const double* op, int* accepted) {
   int rc = check_ready(ctx, true);
   if (rc) return rc;
   if (!beta || !thermo) return fail(ctx, G6_ERR_ARG, "beta and thermo are required");
   if (parity != 0 && parity != 1) return fail(ctx, G6_ERR_ARG, "parity must be 0 or 1");
+  if (numb < 0 || (numb > 0 && (!umbrella || !op))) return fail(ctx, G6_ERR_ARG, "umbrella and op are required");
   const int R = ctx->nrep;
+  double* d_umb = nullptr;
+  double* d_op = nullptr;
+  if (numb > 0) {
+    rc = ensure_scratch(ctx, (size_t)R * numb * 3 * sizeof(double));
+    if (rc) return rc;
+    d_umb = (double*)ctx->d_scratch;
+    d_op = d_umb + (size_t)R * numb * 2;
+    CK(cudaMemcpyAsync(d_umb, umbrella, (size_t)R * numb * 2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_op, op, (size_t)R * numb * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
   std::vector<ThermoDev> th(R);
   for (int r = 0; r < R; ++r) {
     std::memset(&th[r], 0, sizeof(ThermoDev));
@@ -1559,7 +1570,10 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
   ExchArgs ea;
   ea.nrep = R; ea.parity = parity; ea.seed = seed; ea.counter = counter; ea.epot = ctx->d_epot_rep; ea.beta = ctx->d_beta;
   ea.th = ctx->d_th; ea.accepted = ctx->d_acc; ea.scale = ctx->d_scale;
+  ea.numb = numb; ea.umb = d_umb; ea.op = d_op;
   CK(launch_exchange(ea, ctx->d_st, ctx->n, ctx->d_mol_rep, ctx->stream));
+  if (numb > 0)
+    CK(cudaMemcpyAsync(umbrella, d_umb, (size_t)R * numb * 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   std::vector<int> acc(R);
   CK(cudaMemcpyAsync(beta, ctx->d_beta, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaMemcpyAsync(th.data(), ctx->d_th, R * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1571,6 +1585,17 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
     if (accepted) accepted[r] = acc[r];
   }
   return G6_OK;
+}
+
+int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta, g6_thermostat* thermo,
+                        int* accepted) {
+  return replica_exchange(ctx, parity, seed, counter, beta, thermo, 0, nullptr, nullptr, accepted);
+}
+
+int g6_replica_exchange_umbrella(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
+                                 g6_thermostat* thermo, int numbrella, double* umbrella, const double* op,
+                                 int* accepted) {
+  return replica_exchange(ctx, parity, seed, counter, beta, thermo, numbrella, umbrella, op, accepted);
 }
 
 }  // extern "C"

@@ -317,6 +317,9 @@ struct ExchArgs {
   ThermoDev* th;
   int* accepted;
   double* scale;        // per replica velocity scale (1 if unchanged)
+  int numb;             // parabolic umbrellas per replica (Umbrella.F90), 0 for none
+  double* umb;          // (nrep, numb, 2): center, coefficient; swapped with beta on acceptance
+  const double* op;     // (nrep, numb): the order parameters the umbrellas act on
 };
 
 // ---------------------------------------------------------------------------

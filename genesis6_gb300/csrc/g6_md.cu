@@ -102,9 +102,27 @@ __global__ void k_exchange(ExchArgs a) {
   for (int r = threadIdx.x; r + 1 < a.nrep; r += blockDim.x) {
     if ((r & 1) != a.parity) continue;
     const int r1 = r + 1;
-    const double a0 = a.epot[r], a1 = a.epot[r1];
     const double b0 = a.beta[r], b1 = a.beta[r1];
+    // replica_exchange_trial (Replica.F90:7-73): energies plus the umbrella
+    // potentials coeffi (op - center)^2 (Umbrella.F90:11-16), before and after
+    // the replicas trade temperatures and umbrellas
+    double a0 = a.epot[r], a1 = a.epot[r1];
+    for (int k = 0; k < a.numb; ++k) {
+      const double* u0 = a.umb + ((size_t)r * a.numb + k) * 2;
+      const double* u1 = a.umb + ((size_t)r1 * a.numb + k) * 2;
+      const double o0 = a.op[(size_t)r * a.numb + k], o1 = a.op[(size_t)r1 * a.numb + k];
+      a0 = a0 + u0[1] * ((o0 - u0[0]) * (o0 - u0[0]));
+      a1 = a1 + u1[1] * ((o1 - u1[0]) * (o1 - u1[0]));
+    }
     const double acc0 = -(a0 * b0 + a1 * b1) * I2J * J2K;
+    a0 = a.epot[r]; a1 = a.epot[r1];
+    for (int k = 0; k < a.numb; ++k) {
+      const double* u0 = a.umb + ((size_t)r * a.numb + k) * 2;
+      const double* u1 = a.umb + ((size_t)r1 * a.numb + k) * 2;
+      const double o0 = a.op[(size_t)r * a.numb + k], o1 = a.op[(size_t)r1 * a.numb + k];
+      a0 = a0 + u1[1] * ((o0 - u1[0]) * (o0 - u1[0]));
+      a1 = a1 + u0[1] * ((o1 - u0[0]) * (o1 - u0[0]));
+    }
     const double acc1 = -(a0 * b1 + a1 * b0) * I2J * J2K;
     bool accept = false;
     if (acc0 < acc1) accept = true;
@@ -116,6 +134,11 @@ __global__ void k_exchange(ExchArgs a) {
     if (a.accepted) a.accepted[r] = accept ? 1 : 0;
     if (accept) {
       a.beta[r] = b1; a.beta[r1] = b0;
+      for (int k = 0; k < 2 * a.numb; ++k) {
+        const double t = a.umb[(size_t)r * a.numb * 2 + k];
+        a.umb[(size_t)r * a.numb * 2 + k] = a.umb[(size_t)r1 * a.numb * 2 + k];
+        a.umb[(size_t)r1 * a.numb * 2 + k] = t;
+      }
       const double t0 = a.th[r].temp, t1 = a.th[r1].temp;
       a.scale[r] = sqrt(t1 / t0);
       a.scale[r1] = sqrt(t0 / t1);

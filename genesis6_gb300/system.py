@@ -187,9 +187,18 @@ class RigidWater:
         return {"accepted": counts[0::2].copy(), "trials": counts[1::2].copy(), "energy": energy,
                 "samples": samples[:, :nsm], "trace": tr}
 
-    def replica_exchange(self, parity, seed, counter, beta, thermo):
+    def replica_exchange(self, parity, seed, counter, beta, thermo, umbrella=None, op=None):
+        """Neighbour exchange (Replica.F90:7-73).  With umbrella (nrep, k, 2) =
+        (center, coeffi) and op (nrep, k), the umbrella-aware test; the umbrellas
+        are swapped with beta on acceptance and returned as well."""
         beta = np.ascontiguousarray(beta, dtype=np.float64)
         acc = np.zeros(self.nrep, np.int32)
-        self._check(self.L.g6_replica_exchange(self.ctx, int(parity), int(seed), int(counter), dptr(beta), thermo,
-                                               iptr(acc)))
-        return beta, acc
+        if umbrella is None:
+            self._check(self.L.g6_replica_exchange(self.ctx, int(parity), int(seed), int(counter), dptr(beta),
+                                                   thermo, iptr(acc)))
+            return beta, acc
+        umb = np.ascontiguousarray(umbrella, dtype=np.float64).reshape(self.nrep, -1, 2).copy()
+        opv = np.ascontiguousarray(op, dtype=np.float64).reshape(self.nrep, umb.shape[1])
+        self._check(self.L.g6_replica_exchange_umbrella(self.ctx, int(parity), int(seed), int(counter), dptr(beta),
+                                                        thermo, umb.shape[1], dptr(umb), dptr(opv), iptr(acc)))
+        return beta, acc, umb

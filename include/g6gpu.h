@@ -224,6 +224,14 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
    (optional) gets 1 for each lower member of an accepted pair. */
 int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
                         g6_thermostat* thermo, int* accepted);
+/* The same with numbrella parabolic umbrellas per replica on order parameters
+   the caller computes (Replica.F90:20-62, Umbrella.F90:11-16): each side of the
+   test adds coeffi (op - center)^2 for its umbrellas; umbrella[nrep][numbrella][2]
+   = (center, coeffi) is swapped between the replicas of an accepted pair
+   together with beta; op[nrep][numbrella] is read only. */
+int g6_replica_exchange_umbrella(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
+                                 g6_thermostat* thermo, int numbrella, double* umbrella, const double* op,
+                                 int* accepted);
 
 /* Monte Carlo, mc2.F90:544-832: the replicas of the context are independent
    chains; each advances ntrial single-molecule trials (uniform target,
