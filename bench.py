@@ -56,11 +56,12 @@ def parse():
     p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
-    p.add_argument("--profile", choices=["md", "mc", "mc-learned"], default=None,
+    p.add_argument("--profile", choices=["md", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
                         "TIP4P-4096 (mixed, Nose 300 K, one g6_md_run); 'mc' = two runs of --steps trials on "
                         "32 chains x 1,024 ST2 (fixed widths) from a short MD start; 'mc-learned' = the same "
-                        "with the network trained on 32,768 records first, then learned widths")
+                        "with the network trained on 32,768 records first, then learned widths; 'rdf' = --steps "
+                        "g6_rdf calls on TIP4P-32768")
     return p.parse_args()
 
 
@@ -698,7 +699,13 @@ def run_profile(args):
     """Workloads for ncu captures: nothing is timed and no JSON line is printed."""
     import genesis6_gb300 as g6
     from genesis6_gb300 import config
-    if args.profile == "md":
+    if args.profile == "rdf":   # --steps calls of g6_rdf on 32,768 TIP4P (lattice start)
+        b = config.water_box("TIP4P", N_BIG, 20261207, temp=TEMP, dt=DT)
+        s = make_system("TIP4P", N_BIG, "mixed", b["L"], b["rec"])
+        for _ in range(args.steps):
+            h = s.rdf_counts(200, 0.05)
+        print("rdf ok: %d counts" % int(h.sum()))
+    elif args.profile == "md":
         b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
         s = make_system("TIP4P", N_MAIN, "mixed", b["L"], b["rec"])
         log = s.md_run(DT, args.steps, thermo_for(s))

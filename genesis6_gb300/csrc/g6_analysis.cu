@@ -13,13 +13,15 @@
 // rotation matrix of rigid_setmatrix (RigidModule.F90:62-83) and every product
 // and sum rounded separately (no contraction), the order of the CPU reference.
 //
-// The bin of a site pair comes from FP32 arithmetic (COM difference in FP64,
-// rounded once to FP32, then FP32 site offsets): for separations below 32 A
-// (cutoffs up to ~30 A) that distance is within 1e-5 A of the FP64 one (three
-// roundings of at most half an FP32 ulp of 32 A per component, plus the norm),
-// so the bin is the FP64 bin unless the distance lies within RDF_TOL = 5e-5 A
-// of a bin boundary, where the FP64 distance of the reference's formula
-// decides.  An FP64 instruction issues at 1/64 of the FP32 rate on this GPU.
+// The bin of a site pair comes from FP32 arithmetic: the COM difference is the
+// exact difference of 32-bit fixed-point COM words (the minimum image by
+// wrap-around) converted once to FP32, then the FP32 site offsets are added.
+// For separations below 32 A (cutoffs up to ~30 A) that distance is within
+// 1e-5 A of the FP64 one, so the bin is the FP64 bin unless the distance lies
+// within RDF_TOL = 5e-5 A of a bin boundary.  Those cases (~0.2% at 0.05 A
+// bins) are queued per block and then decided by the FP64 distance of the
+// reference's formula, one case per thread, so that an FP64 instruction (1/64
+// of the FP32 issue rate on this GPU) serves 32 of them.
 #include <cuda_runtime.h>
 
 #include "g6_internal.cuh"
@@ -51,9 +53,13 @@ __global__ void k_site_positions(SitePosArgs a) {
     for (int k = 0; k < 3; ++k) {
       const double o = add(add(mul(t[3 * k], bx), mul(t[3 * k + 1], by)), mul(t[3 * k + 2], bz));
       a.pos[((size_t)i * a.nsite + s) * 3 + k] = add(c[k], o);
-      a.off[((size_t)i * a.nsite + s) * 3 + k] = (float)o;
+      if (s + 1 < a.nsite) a.off[(size_t)i * 16 + 3 * s + k] = (float)o;   // the COM site's offset is 0
     }
   }
+  for (int k = 3 * (a.nsite - 1); k < 16; ++k) a.off[(size_t)i * 16 + k] = 0.0f;
+  const int r = a.rep.mol_rep[i];
+  for (int k = 0; k < 3; ++k) a.fixc[(size_t)i * 4 + k] = to_fixed(c[k], a.rep.invL[3 * r + k]);
+  a.fixc[(size_t)i * 4 + 3] = 0u;
 }
 
 // replica of molecule i: the last r with off[r] <= i
@@ -69,49 +75,85 @@ __device__ __forceinline__ int replica_of(const int* off, int nrep, int i) {
 // One pair per thread (grid-stride); counts in a shared histogram of all
 // replicas, added to the global int64 counts at the end of the block.
 constexpr float RDF_TOL = 5e-5f;   // A: FP32 distance error bound (1e-5 A) with margin
+constexpr int RDF_Q = 1024;        // queued boundary cases per block
 
+__device__ __forceinline__ int rdf_bin64(const RdfArgs& a, long long p, int sa, int sb) {
+  const int i = a.pi[p], j = a.pj[p], ns = a.nsite;
+  const double* xi = a.pos + ((size_t)i * ns + sa) * 3;
+  const double* xj = a.pos + ((size_t)j * ns + sb) * 3;
+  const double dx = sub(sub(xi[0], xj[0]), a.ox[p]);
+  const double dy = sub(sub(xi[1], xj[1]), a.oy[p]);
+  const double dz = sub(sub(xi[2], xj[2]), a.oz[p]);
+  const double rr = __dsqrt_rn(add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz)));
+  return (int)round(__ddiv_rn(sub(rr, a.minvalue), a.binwidth));   // nint: half away from zero
+}
+
+// NS sites per molecule; each molecule's FP32 offsets are 16 floats (four
+// 16-byte loads) and its fixed-point COM one 16-byte load.
+template <int NS>
 __global__ void __launch_bounds__(256) k_rdf(RdfArgs a) {
   extern __shared__ unsigned int s_hist[];
-  const int ns = a.nsite, nb = a.nbin;
-  const int per_rep = ns * ns * nb, total = a.nrep * per_rep;
+  __shared__ int s_nq;
+  __shared__ int2 s_q[RDF_Q];   // (pair, 16 sa + sb)
+  const int nb = a.nbin;
+  const int per_rep = NS * NS * nb, total = a.nrep * per_rep;
   for (int k = threadIdx.x; k < total; k += blockDim.x) s_hist[k] = 0u;
+  if (threadIdx.x == 0) s_nq = 0;
   __syncthreads();
-  const double w = a.binwidth;   // divided by, as the reference does
-  const float fw = (float)w, finv = (float)(1.0 / w), fmin = (float)a.minvalue;
-  const int n = a.n;
+  const float fw = (float)a.binwidth, finv = (float)(1.0 / a.binwidth), fmin = (float)a.minvalue;
+  const float fnb = (float)nb + 1.0f;
+  auto count = [&](int r, int sa, int sb, int bin) {
+    if (bin >= 0 && bin < nb) {
+      const int lo = sa < sb ? sa : sb, hi = sa < sb ? sb : sa;
+      atomicAdd(&s_hist[(size_t)r * per_rep + (lo * NS + hi) * nb + bin], 1u);
+    }
+  };
+  const uint4* fix4 = reinterpret_cast<const uint4*>(a.fixc);
+  const float4* off4 = reinterpret_cast<const float4*>(a.off);
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.npair;
        p += (long long)gridDim.x * blockDim.x) {
     const int i = a.pi[p], j = a.pj[p];
+    const uint4 ci = fix4[i], cj = fix4[j];
+    // offsets of sites 0..NS-2, then the COM site's zero offset
+    float oi[3 * NS > 16 ? 3 * NS : 16], oj[3 * NS > 16 ? 3 * NS : 16];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 u = off4[(size_t)i * 4 + q], v = off4[(size_t)j * 4 + q];
+      oi[4 * q] = u.x; oi[4 * q + 1] = u.y; oi[4 * q + 2] = u.z; oi[4 * q + 3] = u.w;
+      oj[4 * q] = v.x; oj[4 * q + 1] = v.y; oj[4 * q + 2] = v.z; oj[4 * q + 3] = v.w;
+    }
+#pragma unroll
+    for (int k = 3 * (NS - 1); k < 3 * NS; ++k) { oi[k] = 0.0f; oj[k] = 0.0f; }
     const int r = replica_of(a.off_rep, a.nrep, i);
-    const double ox = a.ox[p], oy = a.oy[p], oz = a.oz[p];
-    const float dc[3] = {(float)sub(sub(a.st[i], a.st[j]), ox), (float)sub(sub(a.st[n + i], a.st[n + j]), oy),
-                         (float)sub(sub(a.st[2 * n + i], a.st[2 * n + j]), oz)};
-    const float* fi = a.off + (size_t)i * ns * 3;
-    const float* fj = a.off + (size_t)j * ns * 3;
-    for (int sa = 0; sa < ns; ++sa) {
-      const float ua[3] = {dc[0] + fi[3 * sa], dc[1] + fi[3 * sa + 1], dc[2] + fi[3 * sa + 2]};
-      for (int sb = 0; sb < ns; ++sb) {
-        const float ex = ua[0] - fj[3 * sb], ey = ua[1] - fj[3 * sb + 1], ez = ua[2] - fj[3 * sb + 2];
+    const float dc[3] = {i32_to_f32((int)(ci.x - cj.x)) * a.fscale[3 * r],
+                         i32_to_f32((int)(ci.y - cj.y)) * a.fscale[3 * r + 1],
+                         i32_to_f32((int)(ci.z - cj.z)) * a.fscale[3 * r + 2]};
+#pragma unroll
+    for (int sa = 0; sa < NS; ++sa) {
+      const float ua[3] = {dc[0] + oi[3 * sa], dc[1] + oi[3 * sa + 1], dc[2] + oi[3 * sa + 2]};
+#pragma unroll
+      for (int sb = 0; sb < NS; ++sb) {
+        const float ex = ua[0] - oj[3 * sb], ey = ua[1] - oj[3 * sb + 1], ez = ua[2] - oj[3 * sb + 2];
         const float t = (sqrtf(ex * ex + ey * ey + ez * ez) - fmin) * finv;
-        const float fl = floorf(t);
-        int bin;
-        if (!a.fp64_only && fabsf(t - fl - 0.5f) * fw > RDF_TOL) {
-          bin = (int)fl + (t - fl > 0.5f ? 1 : 0);
-        } else {   // near a bin boundary: the reference's FP64 distance decides
-          const double* xi = a.pos + ((size_t)i * ns + sa) * 3;
-          const double* xj = a.pos + ((size_t)j * ns + sb) * 3;
-          const double dx = sub(sub(xi[0], xj[0]), ox);
-          const double dy = sub(sub(xi[1], xj[1]), oy);
-          const double dz = sub(sub(xi[2], xj[2]), oz);
-          const double rr = __dsqrt_rn(add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz)));
-          bin = (int)round(__ddiv_rn(sub(rr, a.minvalue), w));   // nint: half away from zero
-        }
-        if (bin >= 0 && bin < nb) {
-          const int lo = sa < sb ? sa : sb, hi = sa < sb ? sb : sa;
-          atomicAdd(&s_hist[(size_t)r * per_rep + (lo * ns + hi) * nb + bin], 1u);
+        if (!(t > -1.0f && t < fnb)) continue;   // far outside the histogram
+        float rf;
+        const int bin = nearest_i32(t, rf);
+        if (!a.fp64_only && (0.5f - fabsf(t - rf)) * fw > RDF_TOL) {
+          count(r, sa, sb, bin);
+        } else {   // near a bin boundary: queued for the reference's FP64 distance
+          const int slot = atomicAdd(&s_nq, 1);
+          if (slot < RDF_Q) s_q[slot] = make_int2((int)p, 16 * sa + sb);
+          else count(r, sa, sb, rdf_bin64(a, p, sa, sb));
         }
       }
     }
+  }
+  __syncthreads();
+  const int nq = min(s_nq, RDF_Q);
+  for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+    const int2 e = s_q[q];
+    const int sa = e.y >> 4, sb = e.y & 15;
+    count(replica_of(a.off_rep, a.nrep, a.pi[e.x]), sa, sb, rdf_bin64(a, e.x, sa, sb));
   }
   __syncthreads();
   for (int k = threadIdx.x; k < total; k += blockDim.x)
@@ -187,12 +229,18 @@ size_t rdf_smem_bytes(int nrep, int nsite, int nbin) {
 cudaError_t launch_rdf(const RdfArgs& a, int num_sms, cudaStream_t s) {
   if (a.npair == 0) return cudaSuccess;
   const size_t smem = rdf_smem_bytes(a.nrep, a.nsite, a.nbin);
-  cudaError_t e = cudaFuncSetAttribute(k_rdf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
   const long long want = (a.npair + 255) / 256;
   const int blocks = (int)(want < 4LL * num_sms ? want : 4LL * num_sms);   // a few blocks per SM
-  k_rdf<<<blocks, 256, smem, s>>>(a);
-  return cudaGetLastError();
+  auto go = [&](auto kern) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<blocks, 256, smem, s>>>(a);
+    return cudaGetLastError();
+  };
+  if (a.nsite == 4) return go(k_rdf<4>);
+  if (a.nsite == 5) return go(k_rdf<5>);
+  if (a.nsite == 6) return go(k_rdf<6>);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace g6

@@ -907,15 +907,17 @@ int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* his
   if (rc) return rc;
   const size_t nh = (size_t)ctx->nrep * ns * ns * nbin;
   const size_t pos_bytes = ((size_t)ctx->n * ns * 3 * sizeof(double) + 255) & ~(size_t)255;
-  const size_t off_bytes = ((size_t)ctx->n * ns * 3 * sizeof(float) + 255) & ~(size_t)255;
-  rc = ensure_scratch(ctx, pos_bytes + off_bytes + nh * sizeof(unsigned long long));
+  const size_t off_bytes = ((size_t)ctx->n * 16 * sizeof(float) + 255) & ~(size_t)255;
+  const size_t fix_bytes = ((size_t)ctx->n * 4 * sizeof(uint32_t) + 255) & ~(size_t)255;
+  rc = ensure_scratch(ctx, pos_bytes + off_bytes + fix_bytes + nh * sizeof(unsigned long long));
   if (rc) return rc;
   double* pos = (double*)ctx->d_scratch;
   float* off = (float*)((char*)ctx->d_scratch + pos_bytes);
-  unsigned long long* dh = (unsigned long long*)((char*)ctx->d_scratch + pos_bytes + off_bytes);
+  uint32_t* fixc = (uint32_t*)((char*)ctx->d_scratch + pos_bytes + off_bytes);
+  unsigned long long* dh = (unsigned long long*)((char*)ctx->d_scratch + pos_bytes + off_bytes + fix_bytes);
   SitePosArgs sp;
   std::memset(&sp, 0, sizeof sp);
-  sp.n = ctx->n; sp.nsite = ns; sp.st = ctx->d_st; sp.pos = pos; sp.off = off;
+  sp.n = ctx->n; sp.nsite = ns; sp.st = ctx->d_st; sp.pos = pos; sp.off = off; sp.fixc = fixc; sp.rep = rep_dev(ctx);
   for (int s = 0; s < ns; ++s)
     for (int k = 0; k < 3; ++k) sp.body[s][k] = ctx->mh.rbody[s][k];
   CK(launch_site_positions(sp, ctx->stream));
@@ -924,7 +926,7 @@ int g6_rdf(g6_ctx* ctx, int nbin, double binwidth, double minvalue, int64_t* his
   std::memset(&ra, 0, sizeof ra);
   ra.npair = np; ra.nrep = ctx->nrep; ra.nsite = ns; ra.nbin = nbin; ra.binwidth = binwidth; ra.minvalue = minvalue;
   ra.off_rep = ctx->d_off; ra.pi = ctx->d_pi; ra.pj = ctx->d_pj; ra.ox = ctx->d_ox; ra.oy = ctx->d_oy; ra.oz = ctx->d_oz;
-  ra.pos = pos; ra.off = off; ra.st = ctx->d_st; ra.n = ctx->n; ra.hist = dh;
+  ra.pos = pos; ra.off = off; ra.fixc = fixc; ra.fscale = ctx->d_fscale; ra.n = ctx->n; ra.hist = dh;
   ra.fp64_only = ctx->cc.rout > 30.0;   // the FP32 distance bound holds for separations below 32 A
   int nsm = 0;
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
@@ -951,14 +953,16 @@ int g6_hbonds(g6_ctx* ctx, int64_t cap, int* from, int* which, int* to, int64_t*
   if (rc) return rc;
   const int64_t capd = std::max<int64_t>(std::min<int64_t>(cap, np), 0);
   const size_t pos_bytes = ((size_t)ctx->n * ns * 3 * sizeof(double) + 255) & ~(size_t)255;
-  const size_t off_bytes = ((size_t)ctx->n * ns * 3 * sizeof(float) + 255) & ~(size_t)255;
+  const size_t off_bytes = ((size_t)ctx->n * 16 * sizeof(float) + 255) & ~(size_t)255;
   const size_t out_bytes = ((size_t)capd * sizeof(int) + 255) & ~(size_t)255;
-  rc = ensure_scratch(ctx, pos_bytes + off_bytes + 3 * out_bytes + 256);
+  const size_t fix_bytes = ((size_t)ctx->n * 4 * sizeof(uint32_t) + 255) & ~(size_t)255;
+  rc = ensure_scratch(ctx, pos_bytes + off_bytes + fix_bytes + 3 * out_bytes + 256);
   if (rc) return rc;
   char* base = (char*)ctx->d_scratch;
   SitePosArgs sp;
   std::memset(&sp, 0, sizeof sp);
   sp.n = ctx->n; sp.nsite = ns; sp.st = ctx->d_st; sp.pos = (double*)base; sp.off = (float*)(base + pos_bytes);
+  sp.fixc = (uint32_t*)(base + pos_bytes + off_bytes); sp.rep = rep_dev(ctx);
   for (int s = 0; s < ns; ++s)
     for (int k = 0; k < 3; ++k) sp.body[s][k] = ctx->mh.rbody[s][k];
   CK(launch_site_positions(sp, ctx->stream));
@@ -966,7 +970,7 @@ int g6_hbonds(g6_ctx* ctx, int64_t cap, int* from, int* which, int* to, int64_t*
   std::memset(&ha, 0, sizeof ha);
   ha.npair = np; ha.nsite = ns; ha.osite = osite; ha.hsite[0] = h1; ha.hsite[1] = h2;
   ha.pi = ctx->d_pi; ha.pj = ctx->d_pj; ha.ox = ctx->d_ox; ha.oy = ctx->d_oy; ha.oz = ctx->d_oz; ha.pos = sp.pos;
-  char* outp = base + pos_bytes + off_bytes;
+  char* outp = base + pos_bytes + off_bytes + fix_bytes;
   ha.cap = capd;
   ha.from = (int*)outp; ha.which = (int*)(outp + out_bytes); ha.to = (int*)(outp + 2 * out_bytes);
   ha.count = (unsigned long long*)(outp + 3 * out_bytes);

@@ -122,6 +122,22 @@ __device__ __forceinline__ double exact_dd(const double ci[3], const double cj[3
 // Fixed-point COM: x -> round(frac(x/L) * 2^32) as uint32.  Differences of
 // two such words, read as int32, are the minimum-image separation in units of
 // L/2^32.
+// int32 -> float rounded once, without a conversion instruction (conversions
+// issue on the FP64 pipe of this GPU): the two 16-bit halves are exact floats
+// through the 1.5 * 2^23 and 2^23 bit patterns, then hi * 2^16 + lo in one fma.
+__device__ __forceinline__ float i32_to_f32(int x) {
+  const float fh = __int_as_float(0x4B400000 + (x >> 16)) - 12582912.0f;
+  const float fl = __int_as_float(0x4B000000 + (x & 0xFFFF)) - 8388608.0f;
+  return fmaf(fh, 65536.0f, fl);
+}
+// Nearest integer of |t| < 2^22 as an int and as a float (ties to even),
+// without a conversion instruction.
+__device__ __forceinline__ int nearest_i32(float t, float& rf) {
+  const float m = t + 12582912.0f;
+  rf = m - 12582912.0f;
+  return __float_as_int(m) - 0x4B400000;
+}
+
 __device__ __forceinline__ uint32_t to_fixed(double x, double invL) {
   double f = x * invL;
   f = f - floor(f);
@@ -331,7 +347,9 @@ struct SitePosArgs {
   double body[MAXSITE][3];
   const double* st;
   double* pos;   // (n, nsite, 3)
-  float* off;    // (n, nsite, 3): R(q) body, the offsets of pos from the COM, in FP32
+  float* off;    // (n, 16): R(q) body of sites 0..nsite-2 (3 floats each; the COM site's is 0) in FP32, zero padded
+  uint32_t* fixc;   // (n, 4): the COM as 32-bit fixed point of its replica's box, zero padded
+  RepDev rep;
 };
 // Site-site distance histograms over a pair set (g6_analysis.cu).
 struct RdfArgs {
@@ -343,7 +361,8 @@ struct RdfArgs {
   const double *ox, *oy, *oz;
   const double* pos;
   const float* off;
-  const double* st;               // COM: st[0..2][i]
+  const uint32_t* fixc;           // COM fixed point (n, 4)
+  const float* fscale;            // per replica: box edge / 2^32 (3 floats)
   int n;
   int fp64_only;                  // every distance in FP64 (cutoffs beyond the FP32 bound)
   unsigned long long* hist;       // (nrep, nsite, nsite, nbin), a <= b only
