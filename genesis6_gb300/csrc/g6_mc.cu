@@ -164,7 +164,12 @@ __device__ __forceinline__ float gauss_rn(float t) {
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__fmul_rn(-__fmul_rn(t, t), 1.44269504f)));
   return y;
 }
-__device__ __forceinline__ int feat_q(float x) { return __float2int_rn(__fmul_rn(x, FEAT_Q)); }
+// Nearest integer (ties to even, as __float2int_rn) of the term in units of
+// 2^-20 by the 1.5 * 2^23 bit pattern (exact below 2^22; terms are in [0, 1]):
+// a float-to-int conversion issues on the FP64 pipe of this GPU.
+__device__ __forceinline__ int feat_q(float x) {
+  return __float_as_int(__fadd_rn(__fmul_rn(x, FEAT_Q), 12582912.0f)) - 0x4B400000;
+}
 
 // Unit direction of one site offset v.  rsqrtf is a fixed function of its
 // argument, so every call site gets the same bits for the same v.
