@@ -509,3 +509,65 @@ def state_from_system(s, thermo, st: State, nstep: Optional[int] = None) -> Stat
         t = thermo[0]
         out.nose = Nose(t.temp, t.q, t.dump, tuple(t.zeta[k] for k in range(5)), t.zetasum)
     return out
+
+
+# ---------------------------------------------------------------------------
+# JSON form of a configuration: one key per tag, the tag's values as on file
+# ---------------------------------------------------------------------------
+def state_to_json(st: State, poses_only: bool = False) -> str:
+    """{"DTPS": dt, "BOX3": [...], "RCOA": [rc, width], "VOXA": [...], "NOS2": [temp, q/dt, dump,
+    zeta0..4, zetasum], "MDLP"/"NLOG"/"ASTP": n, "components": [{"ID08": id, "FIXC": bool,
+    "NX4A": [[com, quat], ...]} or {..., "WTG2": [[53 values], ...]}]}: the values the text and
+    binary forms carry, with the records in this library's internal units (poses_only keeps
+    com and quaternion only)."""
+    import json
+    d: Dict[str, object] = {}
+    if st.dt is not None:
+        d["DTPS"] = st.dt
+    if st.box is not None:
+        d["BOX3"] = [float(x) for x in st.box]
+    if st.rc:
+        d["RCOA"] = [st.rc, st.switch]
+    if st.voxa is not None:
+        d["VOXA"] = [float(x) for x in st.voxa]
+    if st.nose is not None:
+        n = st.nose
+        d["NOS2"] = [n.temp, n.q / _dt_or_fail(st), n.dump, *n.zeta, n.zetasum]
+    for tag, key in (("MDLP", "nloop"), ("NLOG", "nlog"), ("ASTP", "nstep")):
+        if getattr(st, key) is not None:
+            d[tag] = int(getattr(st, key))
+    comps = []
+    for c in st.components:
+        e: Dict[str, object] = {"ID08": c.id.strip(), "FIXC": bool(c.fixed)}
+        if poses_only:
+            e["NX4A"] = np.concatenate([c.rec[:, 0:3], c.rec[:, 33:37]], axis=1).tolist()
+        else:
+            e["WTG2"] = np.asarray(c.rec).tolist()
+        comps.append(e)
+    d["components"] = comps
+    return json.dumps(d)
+
+
+def state_from_json(text: str) -> State:
+    import json
+    d = json.loads(text)
+    st = State()
+    st.dt = d.get("DTPS")
+    if "BOX3" in d:
+        st.box = np.asarray(d["BOX3"], dtype=np.float64)
+    if "RCOA" in d and d["RCOA"][0] > 0:
+        st.rc, st.switch = (float(v) for v in d["RCOA"])
+    if "VOXA" in d and d["VOXA"][0] > 0:
+        st.voxa = np.asarray(d["VOXA"], dtype=np.float64)
+    if "NOS2" in d and d["NOS2"][0] >= 0:
+        v = d["NOS2"]
+        st.nose = Nose(v[0], v[1] * _dt_or_fail(st), v[2], tuple(v[3:8]), v[8])
+    st.nloop, st.nlog, st.nstep = d.get("MDLP"), d.get("NLOG"), d.get("ASTP")
+    for e in d.get("components", []):
+        if "WTG2" in e:
+            rec = np.asarray(e["WTG2"], dtype=np.float64).reshape(-1, REC)
+        else:
+            a = np.asarray(e["NX4A"], dtype=np.float64).reshape(-1, 7)
+            rec = record_from_poses(a[:, 0:3], a[:, 3:7])
+        st.components.append(Component(str(e["ID08"]).ljust(8)[:8], rec, bool(e.get("FIXC", False))))
+    return st

@@ -216,3 +216,15 @@ def test_md_resumes_from_a_restart_file(precision):
     np.testing.assert_allclose(rec_b[:, 0:3], rec_a[:, 0:3], rtol=0, atol=tol)
     np.testing.assert_allclose(rec_b[:, 33:37], rec_a[:, 33:37], rtol=0, atol=tol)
     np.testing.assert_allclose(log_b[-1, 0, 5], log_a[-1, 0, 5], rtol=tol)   # H, with the Nose terms
+
+
+def test_json_form_round_trips_through_the_restart():
+    r = random_records(9, 6)
+    st = F.State(box=np.array([20.0, 21.0, 22.0]), rc=9.0, switch=2.0, dt=0.002, nstep=5, nloop=100, nlog=2,
+                 nose=F.Nose(300.0, 2.5, 0.0, (1e-3, 0, 0, 0, 0), 0.5), components=[F.Component("TIP5P   ", r)])
+    back = F.read_restart(F.write_restart(F.state_from_json(F.state_to_json(st))))
+    np.testing.assert_allclose(back.components[0].rec, r, rtol=1e-15, atol=0)
+    assert back.components[0].model == "TIP5P" and back.nose.q == pytest.approx(2.5) and back.nstep == 5
+    poses = F.state_from_json(F.state_to_json(st, poses_only=True)).components[0].rec
+    assert np.array_equal(poses[:, 0:3], r[:, 0:3]) and np.array_equal(poses[:, 33:37], r[:, 33:37])
+    assert not poses[:, 3:33].any()
