@@ -134,11 +134,12 @@ def mc_run_learned(orc, model, path, com, quat, L, rin, rc, beta, p, mean, istd,
     p = np.asarray(p, dtype=np.float64)
     mean = np.asarray(mean, dtype=np.float64)
     istd = np.asarray(istd, dtype=np.float64)
-    nq = orc.model_info(model)["nsite"] - 1
+    # the charged sites, in site order: their directions are the direction features
+    charged = np.nonzero(orc.model_info(model)["param"][:, 0] != 0.0)[0]
 
     def widths_at(t, c, q):
         intra = orc.place_sites(model, c[None, :], q[None, :])[3][0]
-        f = features(com, L, t, c, intra[1:1 + nq][:4])
+        f = features(com, L, t, c, intra[charged][:4])
         z, _ = forward(p, ((f - mean) * istd)[None, :])
         st, sr = widths(z, s0t, s0r)
         return float(st[0]), float(sr[0])

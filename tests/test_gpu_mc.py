@@ -195,12 +195,13 @@ def test_training_lowers_loss_and_learned_chain_is_consistent():
     assert (counts[:, 0] > 0).all()
 
 
-def test_learned_fp64_chain_replays_reference(orc):
+@pytest.mark.parametrize("model", ["ST2", "TIP4P", "SPCE"])
+def test_learned_fp64_chain_replays_reference(orc, model):
     """The FP64 learned-width chain (widths at both poses, Hastings term) follows
     the CPU restatement trial by trial: same targets, same decisions, same end
     state.  The network is random, so the widths vary from molecule to molecule
     and from pose to pose."""
-    s, recs, rc = _chains("ST2", 2, 216, 90)
+    s, recs, rc = _chains(model, 2, 216, 90)
     rng = np.random.default_rng(9)
     p = rng.normal(0, 0.3, mlp.NPARAM).astype(np.float32)
     mean = np.full(mlp.NIN, 0.5, np.float32); istd = np.full(mlp.NIN, 1.0, np.float32)
@@ -209,7 +210,7 @@ def test_learned_fp64_chain_replays_reference(orc):
     counts, energy, trace, _ = _mc(s, ntrial, 31, 0, beta, 0.1, 0.1, mode=_capi.MC_LEARNED)
     rec_g = s.download_state()
     for c, b in enumerate(recs):
-        com, quat, tr = mlp.mc_run_learned(orc, "ST2", "custom", b["com"], b["quat"], b["L"], rc - 2.0, rc, beta,
+        com, quat, tr = mlp.mc_run_learned(orc, model, "custom", b["com"], b["quat"], b["L"], rc - 2.0, rc, beta,
                                            p, mean, istd, 0.1, 0.1, ntrial, 31, c, 0)
         assert np.array_equal(trace[c, :, 3], tr[:, 2])          # same targets
         assert np.array_equal(trace[c, :, 2], tr[:, 1])          # same decisions
