@@ -254,6 +254,7 @@ struct g6_ctx {
   // reductions and control
   int nblk = 0;
   double* d_part = nullptr; unsigned int* d_gmax = nullptr; double* d_red = nullptr; int* d_repcnt = nullptr;
+  char* d_ctl = nullptr;   // the control block (ctl_layout); the pointers around it point into it
   double* d_rfac = nullptr;   // per replica temperature and pressure factors
   double* d_fixs = nullptr;   // per replica and axis 2^32 / L
   unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
@@ -605,9 +606,34 @@ int g6_ctx_destroy(g6_ctx* ctx) {
 }
 
 // Bytes of the pinned host block of a context with nrep replicas (its regions: pinned_runs).
+// The control block of a run, one device allocation mirrored by two pinned
+// copies (up, down) so that a run uploads its inputs in one copy and reads its
+// results back in one copy: thermostats, temperature / pressure factors,
+// fixed-point scales, control words, counters the upload zeroes (done flag,
+// per-axis maxima, overflow flag, per-replica counts), reductions.
+struct CtlLayout {
+  size_t th, rf, fx, ctrl, done, gmax, ovf, repcnt, up_bytes, red, bytes;
+};
+static CtlLayout ctl_layout(int R) {
+  auto al = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  CtlLayout L;
+  size_t o = 0;
+  L.th = o; o = al(o + (size_t)R * sizeof(ThermoDev));
+  L.rf = o; o = al(o + 2 * (size_t)R * sizeof(double));
+  L.fx = o; o = al(o + 3 * (size_t)R * sizeof(double));
+  L.ctrl = o; o = al(o + 8 * sizeof(int));
+  L.done = o; o += 4 * sizeof(unsigned);
+  L.gmax = o; o += 4 * sizeof(unsigned);
+  L.ovf = o; o += 4 * sizeof(int);
+  L.repcnt = o; o = al(o + (size_t)R * sizeof(int));
+  L.up_bytes = o;
+  L.red = o; o = al(o + (size_t)R * NRED * sizeof(double));
+  L.bytes = o;
+  return L;
+}
+
 static size_t pinned_runs_bytes(int nrep) {
-  return 2 * (size_t)nrep * sizeof(ThermoDev) + (size_t)nrep * (NRED + 2 + 3 + G6_LOG_WIDTH) * sizeof(double) +
-         24 * sizeof(int);
+  return 2 * ctl_layout(nrep).bytes + (size_t)nrep * G6_LOG_WIDTH * sizeof(double);
 }
 
 int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const int* nmol, const double* box) {
@@ -663,15 +689,21 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
-  CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_overflow, 1));
+  CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
   ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // blocks of the fused step kernel at 32 lanes/molecule
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
-  CK(dalloc(ctx, &ctx->d_gmax, 2)); CK(dalloc(ctx, &ctx->d_red, (size_t)nrep * NRED));
-  CK(dalloc(ctx, &ctx->d_repcnt, nrep));
-  CK(dalloc(ctx, &ctx->d_rfac, 2 * (size_t)nrep)); CK(dalloc(ctx, &ctx->d_fixs, 3 * (size_t)nrep));
-  CK(dalloc(ctx, &ctx->d_done, 1)); CK(dalloc(ctx, &ctx->d_ctrl, 8));
-  CK(dalloc(ctx, &ctx->d_th, nrep)); CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
+  {
+    const CtlLayout cl = ctl_layout(nrep);
+    char* blk = nullptr;
+    CK(dalloc(ctx, &blk, cl.bytes));
+    ctx->d_ctl = blk;
+    ctx->d_th = (ThermoDev*)(blk + cl.th); ctx->d_rfac = (double*)(blk + cl.rf); ctx->d_fixs = (double*)(blk + cl.fx);
+    ctx->d_ctrl = (int*)(blk + cl.ctrl); ctx->d_done = (unsigned int*)(blk + cl.done);
+    ctx->d_gmax = (unsigned int*)(blk + cl.gmax); ctx->d_overflow = (int*)(blk + cl.ovf);
+    ctx->d_repcnt = (int*)(blk + cl.repcnt); ctx->d_red = (double*)(blk + cl.red);
+  }
+  CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
   CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
   CK(dalloc(ctx, &ctx->d_pcnt, 2 * (size_t)n + 2));
   CK(dalloc(ctx, &ctx->d_sig_t, nrep)); CK(dalloc(ctx, &ctx->d_sig_r, nrep)); CK(dalloc(ctx, &ctx->d_energy, nrep));
@@ -681,6 +713,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   ctx->last_epot.assign(nrep, 0.0);
   ctx->pinned_bytes = pinned_runs_bytes(nrep);
   CK(cudaMallocHost((void**)&ctx->h_pinned, ctx->pinned_bytes));
+  std::memset(ctx->h_pinned, 0, ctx->pinned_bytes);   // the up block's counters stay zero
   CK(cudaEventCreateWithFlags(&ctx->pin_ev, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
   ctx->have_system = true;
@@ -1136,6 +1169,8 @@ static int md_stop(g6_ctx* ctx) {
 // factors) and read-backs kept apart, since an upload may still be pending
 // while a read-back is enqueued.
 struct PinnedRuns {
+  char* up;       // mirror of the device control block: inputs (and zero counters)
+  char* dn;       // mirror of the device control block: results
   ThermoDev* th_up;
   ThermoDev* th_dn;
   double* red;
@@ -1149,14 +1184,16 @@ struct PinnedRuns {
 static PinnedRuns pinned_runs(g6_ctx* ctx) {
   const int R = ctx->nrep;
   char* b = ctx->h_pinned;
+  const CtlLayout cl = ctl_layout(R);
   PinnedRuns p;
-  p.th_up = (ThermoDev*)b; b += (size_t)R * sizeof(ThermoDev);
-  p.th_dn = (ThermoDev*)b; b += (size_t)R * sizeof(ThermoDev);
-  p.red = (double*)b; b += (size_t)R * NRED * sizeof(double);
-  p.rf = (double*)b; b += 2 * (size_t)R * sizeof(double);
-  p.fx = (double*)b; b += 3 * (size_t)R * sizeof(double);
-  p.log1 = (double*)b; b += (size_t)R * G6_LOG_WIDTH * sizeof(double);
-  p.ctrl_up = (int*)b; p.ctrl_dn = p.ctrl_up + 8; p.ovf = p.ctrl_up + 16;
+  char* up = b;
+  char* dn = b + cl.bytes;
+  p.up = up; p.dn = dn;
+  p.th_up = (ThermoDev*)(up + cl.th); p.rf = (double*)(up + cl.rf); p.fx = (double*)(up + cl.fx);
+  p.ctrl_up = (int*)(up + cl.ctrl);
+  p.th_dn = (ThermoDev*)(dn + cl.th); p.ctrl_dn = (int*)(dn + cl.ctrl); p.ovf = (int*)(dn + cl.ovf);
+  p.red = (double*)(dn + cl.red);
+  p.log1 = (double*)(b + 2 * cl.bytes);
   return p;
 }
 
@@ -1221,14 +1258,8 @@ static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bo
 // Device part of a run's set-up: the uploads from the pinned block and the clears.
 static int md_upload(g6_ctx* ctx) {
   const PinnedRuns pr = pinned_runs(ctx);
-  CK(cudaMemcpyAsync(ctx->d_th, pr.th_up, ctx->nrep * sizeof(ThermoDev), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_ctrl, pr.ctrl_up, 8 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_done, 0, sizeof(unsigned), ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_gmax, 0, 2 * sizeof(unsigned), ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_repcnt, 0, ctx->nrep * sizeof(int), ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_rfac, pr.rf, 2 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->d_fixs, pr.fx, 3 * ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  // thermostats, factors, scales, control words and the zeroed counters in one copy
+  CK(cudaMemcpyAsync(ctx->d_ctl, pr.up, ctl_layout(ctx->nrep).up_bytes, cudaMemcpyHostToDevice, ctx->stream));
   return G6_OK;
 }
 
@@ -1246,11 +1277,8 @@ static int md_prepare(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo,
 // Read-backs of a run into the pinned block (and the log into `log`, host memory).
 static int md_readback(g6_ctx* ctx, int nsteps, double* log) {
   const PinnedRuns pr = pinned_runs(ctx);
-  CK(cudaMemcpyAsync(pr.ctrl_dn, ctx->d_ctrl, 8 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(pr.ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(pr.th_dn, ctx->d_th, ctx->nrep * sizeof(ThermoDev), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(pr.red, ctx->d_red, (size_t)ctx->nrep * NRED * sizeof(double), cudaMemcpyDeviceToHost,
-                     ctx->stream));
+  // control words, overflow flag, thermostats and reductions in one copy
+  CK(cudaMemcpyAsync(pr.dn, ctx->d_ctl, ctl_layout(ctx->nrep).bytes, cudaMemcpyDeviceToHost, ctx->stream));
   if (log && nsteps > 0)
     CK(cudaMemcpyAsync(log, ctx->d_log, (size_t)nsteps * ctx->nrep * G6_LOG_WIDTH * sizeof(double),
                        cudaMemcpyDeviceToHost, ctx->stream));
