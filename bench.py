@@ -53,7 +53,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-32k", action="store_true")
-    p.add_argument("--equil", type=int, default=EQUIL_STEPS, help="untimed pre-equilibration steps")
+    p.add_argument("--equil", type=int, default=0,
+                   help="extra untimed steps after the stored equilibrated state (which already holds %d steps)"
+                        % EQUIL_STEPS)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
     p.add_argument("--profile", choices=["md", "mc", "mc-learned", "rdf"], default=None,
@@ -72,66 +74,80 @@ def dist_info():
     return rank, world, local
 
 
-def config_block(args, world):
+def config_block(args, world, precision="mixed (fp32 site math, fp64 sums)",
+                 l2="flushed between timed steps (256 MiB write)"):
     return {"workload": "TIP4P-4096 rigid water, NVT Nose-Hoover 300 K, dt 2 fs, rc 9.0 A (2 A switch)",
             "molecules": N_MAIN, "box_A": round((N_MAIN / 0.033456) ** (1 / 3), 3), "cutoff_A": RC,
+            "start": "tests/golden/tip4p4096_eq.npz (lattice + 2,000 FP64 Nose-Hoover steps at 300 K)",
             "parallelism": "replicas" if world > 1 else "single",
-            "l2": "flushed between timed steps (256 MiB write)", "precision": "mixed (fp32 site math, fp64 sums)"}
+            "l2": l2, "precision": precision}
+
+
+START = os.path.join(ROOT, "tests", "golden", "tip4p4096_eq.npz")
+REFERENCE_UNAVAILABLE = ("Genesis6's Fortran cannot be built: no Fortran compiler on the GPU box "
+                         "(gfortran, flang, ifort, ifx, nvfortran, lfortran, f95 probed: all absent)")
+
+
+def equilibrated_start():
+    """The stored equilibrated TIP4P-4096 state that both arms start from."""
+    from genesis6_gb300 import config
+    return config.load_start(START, DT)
 
 
 # ---------------------------------------------------------------------------
-# CPU side (reference arm and cpu_baseline): oracle restatement, all host cores
+# CPU side (reference arm and cpu_baseline): oracle restatement, all host cores.
+# Nothing here loads libg6gpu.so: model tables come from the oracle.
 # ---------------------------------------------------------------------------
-def cpu_md_rate(nsteps_max=None, budget_s=15.0, rec=None):
-    import oracle
-    from genesis6_gb300 import config
-    oracle.build()
-    b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
-    rec = b["rec"] if rec is None else rec
-    threads = os.cpu_count() or 1
+def nose_thermo_cpu():
     q = TEMP * TAU_NOSE ** 2 / DT
-    th = np.array([1, q, 0.0, TEMP, 0, 0, 0, 0, 0, 0], float)
-    t0 = time.perf_counter()
-    r, th, _ = oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, 2, th, threads)
-    probe = (time.perf_counter() - t0) / 2
-    n = max(2, int(budget_s / max(probe, 1e-6)))
-    if nsteps_max:
-        n = min(n, nsteps_max)
-    t0 = time.perf_counter()
-    oracle.md_run_threaded("TIP4P", r, b["L"], [RC] * 3, RC - SWITCH, RC, DT, n, th, threads)
-    dt_s = time.perf_counter() - t0
-    ms = 1e3 * dt_s / n
-    return {"value": ns_per_day(ms), "unit": "ns/day", "cores": threads, "kind": "port",
-            "sample": "%d MD steps of TIP4P-4096 (oracle restatement, OpenMP force and pair search, %d threads, "
-                      "g++ -O2)" % (n, threads), "ms_per_step": ms}
+    return np.array([1, q, 0.0, TEMP, 0, 0, 0, 0, 0, 0], float)
 
 
-def run_reference(args, rank, world):
-    if rank != 0:
-        return
+def cpu_md_run(steps, warmup, threads=None):
+    """`warmup` untimed and `steps` timed MD steps of the oracle (FP64, OpenMP
+    force and pair search) from the stored equilibrated state.  Returns
+    (ms per step, threads, Epot of the first step)."""
     import oracle
-    from genesis6_gb300 import config
     oracle.build()
-    b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
-    threads = os.cpu_count() or 1
-    q = TEMP * TAU_NOSE ** 2 / DT
-    th = np.array([1, q, 0.0, TEMP, 0, 0, 0, 0, 0, 0], float)
+    b = equilibrated_start()
+    threads = threads or os.cpu_count() or 1
+    th = nose_thermo_cpu()
     rec = b["rec"]
-    if args.warmup:
-        rec, th, _ = oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, args.warmup, th,
-                                            threads)
-    steps = max(1, min(args.steps, 400))
+    rec, th, log = oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, max(1, warmup), th,
+                                          threads)
+    first_epot = float(log[0, 0])
     t0 = time.perf_counter()
     oracle.md_run_threaded("TIP4P", rec, b["L"], [RC] * 3, RC - SWITCH, RC, DT, steps, th, threads)
     wall = time.perf_counter() - t0
-    ms = 1e3 * wall / steps
+    return 1e3 * wall / steps, threads, first_epot
+
+
+def cpu_md_rate(steps=200, warmup=3):
+    ms, threads, e0 = cpu_md_run(steps, warmup)
+    return {"value": ns_per_day(ms), "unit": "ns/day", "cores": threads, "kind": "port",
+            "sample": "%d MD steps of TIP4P-4096 from the stored equilibrated state (oracle restatement of the "
+                      "reference, FP64, OpenMP force and pair search, %d threads, g++ -O2)" % (steps, threads),
+            "ms_per_step": ms, "first_step_epot": e0}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores: the FP64 restatement of
+    Genesis6's MD step (the Fortran itself has no compiler here or on the GPU
+    box), from the same stored state as the GPU arm, >= 200 timed steps."""
+    if rank != 0:
+        return
+    steps = min(max(args.steps, 200), 2000)
+    ms, threads, e0 = cpu_md_run(steps, max(args.warmup, 3))
     v = ns_per_day(ms)
     line = {"metric": METRIC, "value": v, "unit": "ns/day", "impl": "reference", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_block(args, world),
+            "steps": steps, "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(args, world, precision="fp64 (the reference's arithmetic)",
+                                   l2="host cores (no GPU)"),
+            "first_step_epot": e0,
             "cpu_baseline": {"value": v, "unit": "ns/day", "cores": threads, "kind": "port",
-                             "sample": "%d MD steps of TIP4P-4096 on %d host threads (Fortran reference not "
-                                       "compilable: no Fortran compiler; CPU restatement used)" % (steps, threads)},
+                             "sample": "%d MD steps of TIP4P-4096 on %d host threads; %s, so the CPU restatement "
+                                       "of its MD step is timed" % (steps, threads, REFERENCE_UNAVAILABLE)},
             "e2e": {"value": v, "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -582,11 +598,13 @@ def run_gpu(args, rank, world, local):
     import genesis6_gb300 as g6
     from genesis6_gb300 import config
     g6.lib()
-    b = config.water_box("TIP4P", N_MAIN, 20261203 + rank, temp=TEMP, dt=DT)
+    b = equilibrated_start()
     L = b["L"]
-    # pre-equilibration (untimed): 2,000 steps from the lattice start
     s = make_system("TIP4P", N_MAIN, "mixed", L, b["rec"])
-    if args.equil:
+    # the first step from the stored state, for comparison with the reference arm's
+    first_epot = float(s.md_run(DT, 1, thermo_for(s))[0, 0, 0])
+    s.upload_state(b["rec"])
+    if args.equil:   # optional extra untimed steps
         s.md_run(DT, args.equil, thermo_for(s), log=False)
     rec_eq = s.download_state()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
@@ -658,7 +676,7 @@ def run_gpu(args, rank, world, local):
         for l in open(tpath):
             if l.startswith("traffic_bytes_per_launch:"):
                 traffic = float(l.split(":")[1])
-    cpu = None if args.no_cpu else cpu_md_rate(budget_s=12.0)
+    cpu = None if args.no_cpu else cpu_md_rate()
     rex = None if args.no_extra else bench_replicas(torch)
     mcb = None if args.no_extra else bench_mc(torch)
     rms = None if args.no_extra else bench_rms(torch, rec_eq, L)
@@ -669,8 +687,10 @@ def run_gpu(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 site math / f64 accumulation", "data": "synthetic (seeded lattice, random quaternions, "
-        "Maxwell-Boltzmann 300 K, 2,000-step pre-equilibration)", "config": config_block(args, world),
+        "Maxwell-Boltzmann 300 K, then 2,000 FP64 Nose-Hoover steps: the stored state both arms start from)", "config": config_block(args, world),
         "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
+        "first_step_epot": first_epot,
+        "fp64_gpu_over_fp64_cpu": None if cpu is None else ns_per_day(ms64) / cpu["value"],
         "tip4p_32k": big,
         "tip5p_32k_nve": t5p,
         "tip4p_32k_nve": t4p,

@@ -61,9 +61,15 @@ def maxwell_boltzmann(n: int, temp: float, mass: float, inertia, rng: np.random.
 
 
 def water_box(model: str, n: int, seed: int, temp: float = 300.0, dt: float = 0.002, density: float = DENSITY,
-              jitter: float = 0.0):
-    """Seeded lattice configuration.  Returns dict(L=(3,), com, quat, rec)."""
-    info = _capi.model_info(model)
+              jitter: float = 0.0, info=None):
+    """Seeded lattice configuration.  Returns dict(L=(3,), com, quat, rec).
+
+    ``info`` (a dict with "mass" and "inertia") supplies the model's mass and
+    principal moments; without it they come from g6_model_info in
+    libg6gpu.so.  A caller that must not load the library (a CPU-only timing
+    of the same workload) passes its own tables."""
+    if info is None:
+        info = _capi.model_info(model)
     rng = np.random.default_rng(seed)
     L = box_edge(n, density)
     com = lattice(n, L)
@@ -73,6 +79,16 @@ def water_box(model: str, n: int, seed: int, temp: float = 300.0, dt: float = 0.
     v, w = maxwell_boltzmann(n, temp, info["mass"], info["inertia"], rng)
     return {"L": np.array([L, L, L]), "com": com, "quat": quat, "rec": rigid_records(com, quat, v, w, dt),
             "mass": info["mass"], "inertia": info["inertia"]}
+
+
+def load_start(path: str, dt: float):
+    """A stored starting state (npz with L, com, quat, d1 = v * dt_file, w1 and
+    dt_file) as 53-double records for time step dt; the higher Gear terms are
+    zero.  Returns dict(L=(3,), com, quat, rec)."""
+    z = np.load(path)
+    vel = z["d1"] / float(z["dt"])
+    rec = rigid_records(z["com"], z["quat"], vel, z["w1"], dt)
+    return {"L": np.asarray(z["L"], float), "com": rec[:, 0:3].copy(), "quat": rec[:, 33:37].copy(), "rec": rec}
 
 
 def replica_sizes(nrep: int, lo: int, hi: int, seed: int) -> np.ndarray:
