@@ -2,19 +2,23 @@
 """Throughput of the rigid-water MD path on GB300: ns/day of TIP4P water.
 
 Workload (N=1): 4,096 rigid TIP4P waters at 1.0 g/cm^3 (L = 49.655 A), seeded
-lattice with random quaternions, pre-equilibrated 2,000 steps, cutoff 9.0 A
-with a 2 A switch, Nose-Hoover NVT at 300 K, dt = 2 fs.  One step = one full
-MD step (Gear predict, placement, neighbour-list upkeep, force, collect,
-correct, reductions, thermostat).  ``value`` is the mixed-precision ns/day;
-the plain FP64 mode and the 32,768-molecule system are reported beside it.
+lattice with random quaternions, pre-equilibrated 2,000 steps (the stored state
+tests/golden/tip4p4096_eq.npz), cutoff 9.0 A with a 2 A switch, Nose-Hoover
+NVT at 300 K, dt = 2 fs.  One step = one full MD step (Gear predict,
+placement, neighbour-list upkeep, force, collect, correct, reductions,
+thermostat).  ``value`` is the mixed-precision ns/day; the plain FP64 mode and
+the 32,768-molecule TIP4P/TIP5P systems are reported beside it.
 
 Timing: per-step CUDA events on the library's stream, an L2 flush (256 MiB
 write) between timed steps, W untimed warm-up steps, barrier + synchronize on
 both sides, max over ranks.  ``e2e`` runs the host-buffer entry point
 g6_md_step_host (state uploaded from pinned host memory and read back every
 step).  ``--impl reference`` times the CPU restatement of the reference on all
-host cores.  With --gpus N each rank runs an independent replica (the
-single-system path does not shard).
+host cores.  With --gpus N the ranks form a replica-exchange ensemble: rank r
+runs its own TIP4P-4096 replica at 300 K * 1.01^r, and between four chunks of
+the timed steps the ranks gather (E, beta, T) over a gloo group and apply the
+same exchange decisions (genesis6_gb300.replicas); `value` sums the ranks'
+ns/day and the exchange attempts are inside the timed total.
 """
 from __future__ import annotations
 
@@ -58,9 +62,10 @@ def parse():
                         % EQUIL_STEPS)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
+    p.add_argument("--n", type=int, default=N_MAIN, help="molecules of the 'md' profiling case")
     p.add_argument("--profile", choices=["md", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
-                        "TIP4P-4096 (mixed, Nose 300 K, one g6_md_run); 'mc' = two runs of --steps trials on "
+                        "--n TIP4P molecules (mixed, Nose 300 K, one g6_md_run after a 20-step start); 'mc' = two runs of --steps trials on "
                         "32 chains x 1,024 ST2 (fixed widths) from a short MD start; 'mc-learned' = the same "
                         "with the network trained on 32,768 records first, then learned widths; 'rdf' = --steps "
                         "g6_rdf calls on TIP4P-32768")
@@ -79,7 +84,7 @@ def config_block(args, world, precision="mixed (fp32 site math, fp64 sums)",
     return {"workload": "TIP4P-4096 rigid water, NVT Nose-Hoover 300 K, dt 2 fs, rc 9.0 A (2 A switch)",
             "molecules": N_MAIN, "box_A": round((N_MAIN / 0.033456) ** (1 / 3), 3), "cutoff_A": RC,
             "start": "tests/golden/tip4p4096_eq.npz (lattice + 2,000 FP64 Nose-Hoover steps at 300 K)",
-            "parallelism": "replicas" if world > 1 else "single",
+            "parallelism": "replica-exchange ensemble, one replica per rank" if world > 1 else "single",
             "l2": l2, "precision": precision}
 
 
@@ -227,21 +232,25 @@ def make_system(model, n, prec, L, rec):
     return s
 
 
-def thermo_for(s, n=1):
-    q = TEMP * TAU_NOSE ** 2 / DT
-    return s.thermostats(n, "nose", temp=TEMP, q=q, dump=0.0)
+def thermo_for(s, n=1, temp=TEMP):
+    q = temp * TAU_NOSE ** 2 / DT
+    return s.thermostats(n, "nose", temp=temp, q=q, dump=0.0)
 
 
-def timed_md(torch, s, steps, warmup, flush, kernel_steps=50):
+def timed_md(torch, s, steps, warmup, flush, kernel_steps=50, temp=TEMP, exchange=None, chunks=1):
     """`steps` MD steps, each a one-step CUDA graph that records events around
     the whole step, with a 256 MiB L2 flush on the same stream before every
-    step.  The fused force/integrator kernel is timed on `kernel_steps` further
-    steps with events around the kernel as well (event nodes between the
-    kernels add latency of their own, so they stay out of the step timing)."""
+    step.  The pair kernel is timed on `kernel_steps` further steps with events
+    around the kernel as well (event nodes between the kernels add latency of
+    their own, so they stay out of the step timing).  With `exchange` (a
+    callable taking the chunk index and the thermostats, returning its wall
+    time in ms) the timed steps run in `chunks` runs with a replica-exchange
+    attempt after each; step_ms then includes those attempts."""
+    from genesis6_gb300 import _capi
     L = s.L
-    th = thermo_for(s)
-    lpi = ctypes.c_int()
-    s._check(L.g6_tune(s.ctx, ctypes.byref(lpi)))
+    th = thermo_for(s, temp=temp)
+    shape = _capi.Shape()
+    s._check(L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))
     if warmup:
         s.md_run(DT, warmup, th, log=False)
     sp = ctypes.c_void_p()
@@ -265,9 +274,18 @@ def timed_md(torch, s, steps, warmup, flush, kernel_steps=50):
         s._check(L.g6_set_step_timing(s.ctx, 0))
         torch.cuda.synchronize()
         return step_ms, kms, log
-    step_ms, _, log = run(1, steps)
+    if exchange is None or chunks <= 1:
+        step_ms, _, log = run(1, steps)
+    else:
+        parts, logs = [], []
+        bounds = np.linspace(0, steps, chunks + 1).astype(int)
+        for c in range(chunks):
+            st, _, lg = run(1, int(bounds[c + 1] - bounds[c]))
+            st[-1] += exchange(c, th)
+            parts.append(st); logs.append(lg)
+        step_ms, log = np.concatenate(parts), np.concatenate(logs)
     _, kms, _ = run(2, max(1, min(kernel_steps, steps)))
-    return step_ms, kms, log, lpi.value
+    return step_ms, kms, log, shape.as_dict()
 
 
 def e2e_md(torch, s, rec, steps):
@@ -546,45 +564,142 @@ def bench_rms(torch, rec_eq, L, snapshots=100, every=20):
             "against": "the FP64 path on the same configurations"}
 
 
-def bench_nve32k(torch, model="TIP5P", seed=20261205, melt=2000, steps=5000):
-    """32,768 molecules of `model` at 1.0 g/cm^3, rc 9 A (2 A switch), dt 1 fs:
-    lattice melted 2,000 steps at 400 K (Nose-Hoover), velocities redrawn at
-    300 K, then NVE for `steps` steps in mixed precision and in FP64 from the
-    same state.  Energy drift = slope of a least-squares line through H per
-    molecule (kJ/mol) against time (ns)."""
+def c3_state(model, seed, melt=2000, equil=2000, dt=0.001):
+    """32,768 molecules of `model` at 1.0 g/cm^3 (L = 99.309 A), rc 9 A with the
+    2 A switch, dt 1 fs: the seeded random-quaternion lattice melted for `melt`
+    steps at 400 K, then `equil` steps at 300 K (both with the stochastic-collision
+    thermostat, 5 collisions per molecule per ps), in mixed precision.  The 300 K
+    stage makes the NVE run that follows start in equilibrium at 300 K.
+    Returns (box, records)."""
     from genesis6_gb300 import config
+    b = config.water_box(model, N_BIG, seed, temp=400.0, dt=dt)
+    s = make_system(model, N_BIG, "mixed", b["L"], b["rec"])
+    s.md_run(dt, melt, s.thermostats(1, "andersen", temp=400.0, rate=5.0, seed=seed), log=False)
+    s.md_run(dt, equil, s.thermostats(1, "andersen", temp=300.0, rate=5.0, seed=seed + 1), log=False)
+    rec = s.download_state()
+    s.close()
+    return b["L"], rec
+
+
+def drift(log, n, dt):
+    """Least-squares slope of H per molecule (kJ/mol) against time (ns)."""
+    H = log[:, 0, 5] * 1e-3 / n
+    tns = np.arange(len(H)) * dt * 1e-3
+    return float(np.polyfit(tns, H, 1)[0])
+
+
+def bench_c3(torch, flush, model="TIP4P", seed=20261205, steps=5000, snapshots=20, every=100, timed_steps=100):
+    """The 32,768-molecule configuration: `model` at 1.0 g/cm^3, rc 9 A, dt 1 fs,
+    lattice melted 2,000 steps at 400 K and equilibrated 2,000 steps at 300 K.
+    Reported: device-timed ns/day of the mixed and FP64 steps (per-step CUDA
+    events, L2 flushed, NVE); NVE energy drift over `steps` steps of each from
+    the same start (wall clock gives their ns/day of a production run); and the
+    relative RMS force and torque error of the mixed path against the FP64 path
+    on `snapshots` configurations of the mixed NVE trajectory (one every `every`
+    steps)."""
     dt = 0.001
     n = N_BIG
-    b = config.water_box(model, n, seed, temp=400.0, dt=dt)
-    s = make_system(model, n, "mixed", b["L"], b["rec"])
-    q = 400.0 * TAU_NOSE ** 2 / dt
-    s.md_run(dt, melt, s.thermostats(1, "nose", temp=400.0, q=q, dump=0.0), log=False)
-    rec = s.download_state()
-    rng = np.random.default_rng(seed + 1)
-    v, w = config.maxwell_boltzmann(n, 300.0, b["mass"], b["inertia"], rng)
-    start = config.rigid_records(rec[:, 0:3], rec[:, 33:37], v, w, dt)
-    out = {"molecules": n, "dt_fs": 1.0, "melt_steps_400K": melt, "nve_steps": steps}
-    for prec in ("mixed", "fp64"):
-        if prec == "fp64":
-            s.close()
-            s = make_system(model, n, "fp64", b["L"], start)
-        else:
-            s.upload_state(start)
-        th = s.thermostats(1, "nve")
+    L, start = c3_state(model, seed)
+    out = {"model": model, "molecules": n, "dt_fs": 1.0,
+           "start": "lattice, 2,000 steps at 400 K, 2,000 steps at 300 K (stochastic collisions)", "nve_steps": steps}
+    sm = make_system(model, n, "mixed", L, start)
+    s64 = make_system(model, n, "fp64", L, start)
+    # RMS force/torque error on snapshots of the mixed trajectory
+    num_f = den_f = num_t = den_t = 0.0
+    for k in range(snapshots):
+        sm.md_run(dt, every, sm.thermostats(1, "nve"), log=False)
+        rec = sm.download_state()
+        s64.upload_state(rec)
+        Fm, tm, _, _ = sm.force()
+        F6, t6, _, _ = s64.force()
+        num_f += float(np.sum((Fm - F6) ** 2)); den_f += float(np.sum(F6 ** 2))
+        num_t += float(np.sum((tm - t6) ** 2)); den_t += float(np.sum(t6 ** 2))
+    out["rms_force_rel"] = float(np.sqrt(num_f / den_f))
+    out["rms_torque_rel"] = float(np.sqrt(num_t / den_t))
+    out["rms_snapshots"] = {"count": snapshots, "every_steps": every, "against": "the FP64 path (oracle-pinned to 1e-12)"}
+    # device-timed steps (NVE, one-step graphs with events, L2 flushed between steps)
+    nve = lambda s: s.thermostats(1, "nve")
+    for prec, s, k in (("mixed", sm, timed_steps), ("fp64", s64, max(5, timed_steps // 10))):
+        s.upload_state(start)
+        from genesis6_gb300 import _capi
+        shape = _capi.Shape()
+        s._check(s.L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))
+        st, km, lg = timed_nve(torch, s, dt, k, 3, flush)
+        out[prec + "_ms_per_step"] = float(st.mean())
+        out[prec + "_ns_per_day"] = ns_per_day(float(st.mean()), dt)
+        if prec == "mixed":
+            pairs = float(lg[:, 0, 6].mean())
+            out["pairs_within_rc"] = pairs
+            out["force_kernel_ms"] = float(km.mean())
+            out["force_tflops"] = FLOPS_PER_PAIR[model] * pairs / (float(km.mean()) * 1e-3) / 1e12
+            out["shape"] = shape.as_dict()
+    out["mixed_over_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
+    # NVE drift from the same start
+    for prec, s in (("mixed", sm), ("fp64", s64)):
+        s.upload_state(start)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        log = s.md_run(dt, steps, th)
+        log = s.md_run(dt, steps, nve(s))
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        H = log[:, 0, 5] * 1e-3 / n                     # kJ/mol per molecule
-        tns = np.arange(steps) * dt * 1e-3              # ns
-        slope = float(np.polyfit(tns, H, 1)[0])
-        ms = 1e3 * wall / steps
-        out[prec] = {"ns_per_day": dt * 1e-3 * 86400.0 / (ms * 1e-3), "ms_per_step": ms,
-                     "drift_kJ_per_mol_per_ns": slope, "H_first_last_kJ_per_mol": [float(H[0]), float(H[-1])],
-                     "T_mean_K": float(log[:, 0, 3].mean())}
-    s.close()
-    out["timing"] = "wall clock over the NVE run (CUDA-graph steps, no L2 flush)"
+        out[prec + "_nve"] = {"drift_kJ_per_mol_per_ns": drift(log, n, dt), "T_mean_K": float(log[:, 0, 3].mean()),
+                              "ns_per_day_wall": ns_per_day(1e3 * wall / steps, dt)}
+    sm.close(); s64.close()
+    out["timing"] = ("ns_per_day: per-step CUDA events, L2 flushed between steps; ns_per_day_wall: wall clock of "
+                     "the 5,000-step NVE run (16-step CUDA graphs, no flush)")
+    return out
+
+
+def timed_nve(torch, s, dt, steps, warmup, flush):
+    """Like timed_md for an NVE run at time step dt."""
+    L = s.L
+    th = s.thermostats(1, "nve")
+    s.md_run(dt, warmup, th, log=False)
+    sp = ctypes.c_void_p()
+    s._check(L.g6_stream(s.ctx, ctypes.byref(sp)))
+    stream = torch.cuda.ExternalStream(sp.value)
+    a, b = ctypes.c_double(), ctypes.c_double()
+    log = np.zeros((steps, 1, 10))
+    step_ms, kms = np.zeros(steps), np.zeros(steps)
+    s._check(L.g6_set_step_timing(s.ctx, 2))
+    torch.cuda.synchronize()
+    s._check(L.g6_md_begin(s.ctx, dt, steps, th, 1))
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+        s._check(L.g6_md_advance(s.ctx, 1))
+        s._check(L.g6_step_times(s.ctx, ctypes.byref(a), ctypes.byref(b)))
+        step_ms[k], kms[k] = a.value, b.value
+    s._check(L.g6_md_end(s.ctx, th, log.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    s._check(L.g6_set_step_timing(s.ctx, 0))
+    torch.cuda.synchronize()
+    return step_ms, kms, log
+
+
+def nve_drift_4096(torch, steps=5000, dt=0.001):
+    """NVE energy drift of TIP4P-4096 from the stored equilibrated state, dt 1 fs,
+    `steps` steps: the GPU's mixed and FP64 paths and, as the CPU baseline of the
+    drift, the oracle's FP64 restatement of the reference MD step (StdForce
+    arithmetic, all host cores) from the same start."""
+    import oracle
+    from genesis6_gb300 import config
+    b = config.load_start(START, dt)
+    n = N_MAIN
+    out = {"molecules": n, "dt_fs": 1.0, "steps": steps, "start": "tests/golden/tip4p4096_eq.npz"}
+    for prec in ("mixed", "fp64"):
+        s = make_system("TIP4P", n, prec, b["L"], b["rec"])
+        log = s.md_run(dt, steps, s.thermostats(1, "nve"))
+        out[prec] = {"drift_kJ_per_mol_per_ns": drift(log, n, dt), "T_mean_K": float(log[:, 0, 3].mean())}
+        s.close()
+    oracle.build()
+    th = np.zeros(10)
+    t0 = time.perf_counter()
+    _, _, lo = oracle.md_run_threaded("TIP4P", b["rec"], b["L"], [RC] * 3, RC - SWITCH, RC, dt, steps, th,
+                                      os.cpu_count() or 1)
+    wall = time.perf_counter() - t0
+    out["cpu_baseline_oracle"] = {"drift_kJ_per_mol_per_ns": drift(lo[:, None, :], n, dt),
+                                  "T_mean_K": float(lo[:, 3].mean()), "seconds": wall,
+                                  "kind": "port", "cores": os.cpu_count() or 1}
     return out
 
 
@@ -616,9 +731,29 @@ def run_gpu(args, rank, world, local):
         torch.cuda.synchronize()
 
     s.upload_state(rec_eq)
+    # N > 1: a replica-exchange ensemble sharded over the ranks -- rank r runs its
+    # own TIP4P-4096 system at T_r = 300 K * 1.01^r and the ranks attempt
+    # neighbour exchanges (gathered over a gloo group) between chunks of steps
+    exchange, temp_r = None, TEMP
+    if world > 1:
+        from genesis6_gb300 import replicas
+        temp_r = TEMP * 1.01 ** rank
+        host_group = dist.new_group(backend="gloo")
+        shard = replicas.ShardedExchange(1, group=host_group)
+        beta_r = [1.0 / temp_r]
+        accepted = []
+
+        def exchange(c, th):
+            t0 = time.perf_counter()
+            res = shard.attempt(c & 1, 20261203, c, s.last_epot(), beta_r, [th[0].temp])
+            replicas.apply_exchange(s, th, res)
+            beta_r[0] = float(res["beta"][0])
+            accepted.append(int(res["accepted_global"].sum()))
+            return 1e3 * (time.perf_counter() - t0)
     barrier()
     with Clocks(local) as clk:
-        step_ms, kms, log, lpi = timed_md(torch, s, args.steps, args.warmup, flush)
+        step_ms, kms, log, shape = timed_md(torch, s, args.steps, args.warmup, flush, temp=temp_r, exchange=exchange,
+                                            chunks=4 if exchange else 1)
         barrier()
     total_ms = float(step_ms.sum())
     if dist:
@@ -639,24 +774,7 @@ def run_gpu(args, rank, world, local):
     e2e_steps = max(10, min(args.steps, 200))
     e2e_ms, h2d, d2h = e2e_md(torch, s, rec_eq, e2e_steps)
 
-    big = None
-    if not args.no_32k:
-        bb = config.water_box("TIP4P", N_BIG, 7 + rank, temp=TEMP, dt=DT)
-        sb = make_system("TIP4P", N_BIG, "mixed", bb["L"], bb["rec"])
-        sb.md_run(DT, 200, thermo_for(sb), log=False)
-        rb = sb.download_state()
-        kb = max(5, min(args.steps, 100))
-        stb, kmb, logb, lpib = timed_md(torch, sb, kb, min(args.warmup, 5), flush)
-        s64b = make_system("TIP4P", N_BIG, "fp64", bb["L"], rb)
-        stb64, _, _, _ = timed_md(torch, s64b, 5, 2, flush)
-        pb = float(logb[:, 0, 6].mean())
-        big = {"mixed_ns_per_day": ns_per_day(float(stb.mean())), "fp64_ns_per_day": ns_per_day(float(stb64.mean())),
-               "mixed_ms_per_step": float(stb.mean()), "fp64_ms_per_step": float(stb64.mean()),
-               "mixed_over_fp64": float(stb64.mean() / stb.mean()), "force_kernel_ms": float(kmb.mean()),
-               "pairs_within_rc": pb,
-               "force_tflops": FLOPS_PER_PAIR["TIP4P"] * pb / (float(kmb.mean()) * 1e-3) / 1e12,
-               "note": "lattice start + 200 untimed steps (no 2,000-step melt)"}
-        sb.close(); s64b.close()
+    big = None if args.no_32k else bench_c3(torch, flush, "TIP4P")
 
     if rank != 0:
         return
@@ -680,8 +798,8 @@ def run_gpu(args, rank, world, local):
     rex = None if args.no_extra else bench_replicas(torch)
     mcb = None if args.no_extra else bench_mc(torch)
     rms = None if args.no_extra else bench_rms(torch, rec_eq, L)
-    t5p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP5P")
-    t4p = None if (args.no_extra or args.no_32k) else bench_nve32k(torch, "TIP4P", seed=20261206)
+    t5p = None if (args.no_extra or args.no_32k) else bench_c3(torch, flush, "TIP5P", seed=20261206)
+    drift4k = None if (args.no_extra or args.no_cpu) else nve_drift_4096(torch)
     rdf = None if (args.no_extra or args.no_32k) else bench_rdf(torch)
     line = {
         "metric": METRIC, "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps,
@@ -692,24 +810,25 @@ def run_gpu(args, rank, world, local):
         "first_step_epot": first_epot,
         "fp64_gpu_over_fp64_cpu": None if cpu is None else ns_per_day(ms64) / cpu["value"],
         "tip4p_32k": big,
-        "tip5p_32k_nve": t5p,
-        "tip4p_32k_nve": t4p,
+        "tip5p_32k": t5p,
+        "nve_drift_4096": drift4k,
         "mixed_rms_error_4096": rms,
         "replica_exchange": rex,
         "mc_learned_vs_fixed": mcb,
         "rdf_32k": rdf,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "kernel": "k_force<TIP4P, mixed, fused step> (site loop + Gear corrector epilogue)",
+                     "kernel": "k_pairs<TIP4P, mixed, MD step> (in-range compaction of the Verlet rows + FP32 "
+                               "site loops; the Gear corrector runs in k_integrate_mixed)",
                      "flops_per_pair": FLOPS_PER_PAIR["TIP4P"],
-                     "pairs_per_launch": pairs, "kernel_ms": kmean, "lanes_per_molecule": lpi,
+                     "pairs_per_launch": pairs, "kernel_ms": kmean, "shape": shape,
                      "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run (FP32 CUDA-core "
                                     "pipe; the kernel uses no tensor cores and moves a few MB per launch)",
                      "hbm_peak_gbs": peaks.get("hbm_gbs")},
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": world * ns_per_day(e2e_ms), "unit": "ns/day", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "entry": "g6_md_step_host"},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))
@@ -726,8 +845,16 @@ def run_profile(args):
             h = s.rdf_counts(200, 0.05)
         print("rdf ok: %d counts" % int(h.sum()))
     elif args.profile == "md":
-        b = config.water_box("TIP4P", N_MAIN, 20261203, temp=TEMP, dt=DT)
-        s = make_system("TIP4P", N_MAIN, "mixed", b["L"], b["rec"])
+        if args.n == N_MAIN:
+            b = equilibrated_start()
+        else:
+            b = config.water_box("TIP4P", args.n, 20261203, temp=TEMP, dt=DT)
+        s = make_system("TIP4P", args.n, "mixed", b["L"], b["rec"])
+        s.md_run(DT, 20, thermo_for(s), log=False)
+        from genesis6_gb300 import _capi
+        shape = _capi.Shape()
+        s._check(s.L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))
+        print("shape:", shape.as_dict())
         log = s.md_run(DT, args.steps, thermo_for(s))
         print("md ok: %d steps, last T %.1f K" % (args.steps, float(log[-1, 0, 3])))
     else:

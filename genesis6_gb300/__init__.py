@@ -5,8 +5,9 @@ include/g6gpu.h).  This package is the host side: the ctypes binding, the
 system owner (RigidWater), the reference-facing pair-list calls, synthetic
 configurations and the build script.
 """
-from . import _capi, analysis, config, formats, interaction  # noqa: F401
+from . import _capi, analysis, config, formats, interaction, replicas  # noqa: F401
 from ._capi import G6Error, Thermostat, lib, model_info  # noqa: F401
 from .system import RigidWater  # noqa: F401
 
-__all__ = ["RigidWater", "G6Error", "Thermostat", "lib", "model_info", "analysis", "config", "formats", "interaction"]
+__all__ = ["RigidWater", "G6Error", "Thermostat", "lib", "model_info", "analysis", "config", "formats", "interaction",
+           "replicas"]

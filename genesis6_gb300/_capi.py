@@ -33,8 +33,9 @@ SYMBOLS = [
     "g6_system", "g6_set_cutoff", "g6_set_grid", "g6_set_skin", "g6_set_box", "g6_upload_state",
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
     "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
-    "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
-    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
+    "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_exchange_plan", "g6_replica_scale", "g6_last_epot",
+    "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
+    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_tune_shape", "g6_get_shape", "g6_set_shape", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
     "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
 ]
 
@@ -50,6 +51,16 @@ class Thermostat(ctypes.Structure):
                 ("dump", ctypes.c_double), ("zeta", ctypes.c_double * 5), ("zetasum", ctypes.c_double),
                 ("collision_rate", ctypes.c_double), ("seed", ctypes.c_uint64)]
 
+
+class Shape(ctypes.Structure):
+    _fields_ = [("lpi", ctypes.c_int), ("step_lpi", ctypes.c_int), ("step_mpw", ctypes.c_int),
+                ("skin", ctypes.c_double), ("cap", ctypes.c_int), ("step_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+TUNE_SKIN = 1
 
 _lib = None
 
@@ -97,6 +108,10 @@ def lib():
                                       ctypes.POINTER(Thermostat), ip]
     L.g6_replica_exchange_umbrella.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,
                                                ctypes.POINTER(Thermostat), ctypes.c_int, dp, dp, ip]
+    L.g6_exchange_plan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp,
+                                   ctypes.c_int, dp, dp, dp, ip]
+    L.g6_replica_scale.argtypes = [vp, dp]
+    L.g6_last_epot.argtypes = [vp, dp]
     L.g6_md_begin.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Thermostat), ctypes.c_int]
     L.g6_md_advance.argtypes = [vp, ctypes.c_int]
     L.g6_md_end.argtypes = [vp, ctypes.POINTER(Thermostat), dp]
@@ -119,6 +134,9 @@ def lib():
     L.g6_step_times.argtypes = [vp, dp, dp]
     L.g6_tune.argtypes = [vp, ip]
     L.g6_set_lpi.argtypes = [vp, ctypes.c_int]
+    L.g6_tune_shape.argtypes = [vp, ctypes.c_int, ctypes.POINTER(Shape)]
+    L.g6_get_shape.argtypes = [vp, ctypes.POINTER(Shape)]
+    L.g6_set_shape.argtypes = [vp, ctypes.POINTER(Shape)]
     for name in SYMBOLS:
         if name not in ("g6_last_error", "g6_status_string"):
             getattr(L, name).restype = ctypes.c_int

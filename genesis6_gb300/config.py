@@ -53,11 +53,31 @@ def rigid_records(com, quat, vel=None, omega=None, dt=0.002) -> np.ndarray:
 
 
 def maxwell_boltzmann(n: int, temp: float, mass: float, inertia, rng: np.random.Generator):
+    """Seeded Maxwell-Boltzmann velocities with rigid_vreset2's per-axis
+    variances (RigidModule.F90:1016-1053): COM velocity N(0, kT/m), body-frame
+    angular velocity N(0, kT/I_k), kT = temp * RGAS * J2I, from numpy's
+    normal generator; the net COM momentum is removed.  Returns v, w (n,3)."""
     kT = temp * RGAS * J2I
     v = rng.standard_normal((n, 3)) * np.sqrt(kT / mass)
     v -= v.mean(axis=0, keepdims=True)
     w = rng.standard_normal((n, 3)) * np.sqrt(kT / np.asarray(inertia))[None, :]
     return v, w
+
+
+def rigid_vreset2(temp: float, mass: float, inertia, u, dt: float):
+    """Velocities exactly as rigid_vreset2 (RigidModule.F90:1016-1053) draws
+    them from a given stream of uniforms u (n, 12) in (0, 1] (the values of
+    Random_GetNext): per molecule the COM terms dx(1), dy(1), dz(1) =
+    N(0, kT/m) * dt, then the body-frame wx(1), wy(1), wz(1) = N(0, kT/I_k),
+    each normal from two consecutive numbers by Random_Normal
+    (RandomModule.F90:28-36: sqrt(-2 log r1) sin(2 pi r2) sqrt(var)).  The
+    reference does not remove the net momentum here.  Returns d1 (n,3), w1 (n,3)."""
+    u = np.asarray(u, float).reshape(-1, 12)
+    kT = temp * RGAS * J2I
+    var = np.array([kT / mass] * 3 + [kT / float(i) for i in inertia])
+    r1, r2 = u[:, 0::2], u[:, 1::2]
+    z = np.sqrt(-2.0 * np.log(r1)) * np.sin(2.0 * 3.1415926535897932 * r2) * np.sqrt(var)[None, :]
+    return z[:, :3] * dt, z[:, 3:].copy()
 
 
 def water_box(model: str, n: int, seed: int, temp: float = 300.0, dt: float = 0.002, density: float = DENSITY,

@@ -6,7 +6,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "g6_internal.cuh"
@@ -231,6 +234,7 @@ struct g6_ctx {
   std::vector<double> L;
   int lpi = 0;                    // lanes per molecule in the force kernel (0 = default)
   int step_lpi = 0;               // lanes per molecule in the fused MD step kernel (0 = default)
+  int step_mpw = 0;               // mixed MD step: molecules per warp of the integrator kernel (0 = default)
   int coop_grid = 0;              // blocks of the cooperative rebuild kernel
   // device arrays
   int* d_off = nullptr; int* d_mol_rep = nullptr; double* d_L = nullptr; double* d_invL = nullptr;
@@ -240,6 +244,7 @@ struct g6_ctx {
   double* d_tmat1 = nullptr; double* d_pk64_1 = nullptr; float4* d_pk32_1 = nullptr; uint32_t* d_fix1 = nullptr;
   double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
   int* d_npin = nullptr;
+  float4* d_fres = nullptr;       // mixed MD step: per-molecule float-pair results of the pair kernel
   double* d_stage = nullptr;      // AoS staging (53 n)
   // grids
   HostGrid gref, glist;
@@ -260,6 +265,7 @@ struct g6_ctx {
   unsigned int* d_done = nullptr; int* d_ctrl = nullptr;
   ThermoDev* d_th = nullptr; double* d_scale = nullptr; double* d_beta = nullptr; int* d_acc = nullptr;
   double* d_epot_rep = nullptr;
+  double* d_xtemp = nullptr; int* d_slot = nullptr; int* d_moved = nullptr;   // replica-exchange scratch
   // Monte Carlo and the proposal-width MLP
   double *d_sig_t = nullptr, *d_sig_r = nullptr, *d_energy = nullptr;
   long long* d_counts = nullptr;
@@ -507,7 +513,7 @@ static ForceArgs force_args(g6_ctx* c) {
   a.n = c->n; a.cap = c->cap; a.stride_pk32 = c->npk; a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.rep = rep_dev(c);
   a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pk64_1 = c->d_pk64_1; a.pk32_1 = c->d_pk32_1; a.ctrl = nullptr;
   a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
-  a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin;
+  a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin; a.fres = c->d_fres;
   return a;
 }
 
@@ -517,6 +523,19 @@ static int default_lpi(const g6_ctx* c) {
   int l = 4;
   while (l < 32 && (long long)c->n * l < want) l *= 2;
   return l;
+}
+
+// Molecules per warp of the mixed integrator kernel: 8 spreads a small system's
+// FP64 corrector work over more schedulers, 32 issues the fewest FP64
+// instructions for a large one.
+static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 8 : (c->n <= 24576 ? 16 : 32); }
+
+// The mixed list kernel keeps each molecule's in-range row in shared memory
+// (32/lpi rows per warp): widen lpi until the rows of a block fit.
+static int fit_lpi(const g6_ctx* c, int lpi) {
+  if (c->prec != G6_MIXED) return lpi;
+  while (lpi < 32 && c->cap > pairs_max_cap(lpi)) lpi *= 2;
+  return lpi;
 }
 
 // Enqueue the neighbour-list rebuild (conditional on ctrl[0] when ctrl != NULL):
@@ -529,14 +548,20 @@ static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl, const StepArgs* step = 
   return G6_OK;
 }
 
+static void apply_cached_shape(g6_ctx* ctx);
+
 static int force_once(g6_ctx* ctx) {
   int rc = prepare_list(ctx);
   if (rc) return rc;
+  apply_cached_shape(ctx);
   if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
   CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
   CK(launch_predict_place(place_args(ctx), 0, ctx->d_th, 0, ctx->stream));
   rc = enqueue_rebuild(ctx, nullptr);
   if (rc) return rc;
+  if (ctx->prec == G6_MIXED && ctx->cap > pairs_max_cap(32))
+    return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
+  ctx->lpi = fit_lpi(ctx, ctx->lpi);
   CK(launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
   int ovf = 0;
   CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -688,6 +713,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_fix1, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
+  CK(dalloc(ctx, &ctx->d_fres, 4 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
@@ -705,6 +731,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   }
   CK(dalloc(ctx, &ctx->d_scale, nrep)); CK(dalloc(ctx, &ctx->d_beta, nrep));
   CK(dalloc(ctx, &ctx->d_acc, nrep)); CK(dalloc(ctx, &ctx->d_epot_rep, nrep));
+  CK(dalloc(ctx, &ctx->d_xtemp, nrep)); CK(dalloc(ctx, &ctx->d_slot, nrep)); CK(dalloc(ctx, &ctx->d_moved, nrep));
   CK(dalloc(ctx, &ctx->d_pcnt, 2 * (size_t)n + 2));
   CK(dalloc(ctx, &ctx->d_sig_t, nrep)); CK(dalloc(ctx, &ctx->d_sig_r, nrep)); CK(dalloc(ctx, &ctx->d_energy, nrep));
   CK(dalloc(ctx, &ctx->d_counts, 2 * (size_t)nrep));
@@ -1139,8 +1166,13 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
   ForceArgs fa = force_args(ctx);
   fa.ctrl = ctx->d_ctrl;
   if (kev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
-  CK(launch_step(fa, sa, ctx->model, ctx->prec == G6_MIXED, ctx->step_lpi, ctx->stream));
-  if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
+  if (ctx->prec == G6_MIXED) {
+    // pair kernel, then the integrator kernel; the kernel events bracket the pair kernel
+    CK(launch_step_mixed(fa, sa, ctx->model, ctx->step_lpi, ctx->step_mpw, ctx->stream, kev ? ev[2] : nullptr));
+  } else {
+    CK(launch_step(fa, sa, ctx->model, false, ctx->step_lpi, ctx->stream));
+    if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
+  }
   if (ev) CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
   return G6_OK;
 }
@@ -1204,6 +1236,7 @@ static PinnedRuns pinned_runs(g6_ctx* ctx) {
 static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bool want_log) {
   int rc = prepare_list(ctx);
   if (rc) return rc;
+  apply_cached_shape(ctx);
   if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
   if (ctx->step_lpi == 0) {
     const char* env = std::getenv("G6_LPI");
@@ -1211,6 +1244,11 @@ static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bo
     if (ctx->step_lpi != 4 && ctx->step_lpi != 8 && ctx->step_lpi != 16 && ctx->step_lpi != 32)
       ctx->step_lpi = default_lpi(ctx);
   }
+  if (ctx->prec == G6_MIXED && ctx->cap > pairs_max_cap(32))
+    return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
+  ctx->lpi = fit_lpi(ctx, ctx->lpi);
+  ctx->step_lpi = fit_lpi(ctx, ctx->step_lpi);
+  if (ctx->step_mpw == 0) ctx->step_mpw = default_mpw(ctx);
   const PinnedRuns pr = pinned_runs(ctx);
   ThermoDev* th = pr.th_up;
   for (int r = 0; r < ctx->nrep; ++r) {
@@ -1424,65 +1462,212 @@ int g6_time_force(g6_ctx* ctx, double* ms) {
   return G6_OK;
 }
 
-// Lanes per molecule of the force kernel: time each candidate on the current
-// configuration (3 launches each, best of) and keep the fastest.
-int g6_tune(g6_ctx* ctx, int* lpi_out) {
-  int rc = check_ready(ctx, true);
-  if (rc) return rc;
-  if (ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_tune inside g6_md_begin/g6_md_end");
-  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
-  rc = force_once(ctx);
-  if (rc) return rc;
-  const int cand[4] = {4, 8, 16, 32};
-  // force-only kernel
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner.  Shapes of the step kernels that change the speed but not the
+// set of pairs: lanes per molecule of the force-only and MD-step pair kernels,
+// molecules per warp of the mixed integrator kernel and, on request, the
+// Verlet skin (with the row capacity that follows from it).  Each candidate
+// is timed with CUDA events on the context's stream, on the uploaded state,
+// which is restored after every trial run.  Chosen shapes are cached per
+// system size, model, path, precision and cutoff, and a context that has not
+// been tuned or given a shape starts from the cached one.
+// ---------------------------------------------------------------------------
+namespace {
+struct ShapeKey {
+  int model, path, prec, nrep, n;
+  long long rc_milli;
+  bool operator<(const ShapeKey& o) const {
+    return std::tie(model, path, prec, nrep, n, rc_milli) < std::tie(o.model, o.path, o.prec, o.nrep, o.n, o.rc_milli);
+  }
+};
+std::map<ShapeKey, g6_shape>& shape_cache() {
+  static std::map<ShapeKey, g6_shape> m;
+  return m;
+}
+std::mutex& shape_mutex() {
+  static std::mutex m;
+  return m;
+}
+ShapeKey shape_key(const g6_ctx* c) {
+  return ShapeKey{c->model, c->path, c->prec, c->nrep, c->n, (long long)std::llround(c->cc.rout * 1000.0)};
+}
+}  // namespace
+
+static void fill_shape(const g6_ctx* ctx, g6_shape* out, double step_ms) {
+  out->lpi = ctx->lpi; out->step_lpi = ctx->step_lpi; out->step_mpw = ctx->step_mpw;
+  out->skin = ctx->skin; out->cap = ctx->cap; out->step_ms = step_ms;
+}
+
+// A context without a chosen shape takes the cached one for its size.
+static void apply_cached_shape(g6_ctx* ctx) {
+  if (ctx->lpi || ctx->step_lpi || ctx->step_mpw) return;
+  std::lock_guard<std::mutex> lk(shape_mutex());
+  auto it = shape_cache().find(shape_key(ctx));
+  if (it == shape_cache().end()) return;
+  ctx->lpi = it->second.lpi; ctx->step_lpi = it->second.step_lpi; ctx->step_mpw = it->second.step_mpw;
+}
+
+// Duration of `timed` NVE steps (after `warm` untimed ones) from the state
+// saved in d_stage, which is put back afterwards.
+static int time_md_steps(g6_ctx* ctx, int warm, int timed, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+  const size_t bytes = (size_t)REC * ctx->n * sizeof(double);
+  drop_graphs(ctx);
+  int rc = g6_md_begin(ctx, 0.001, warm + timed, nullptr, 0);
+  if (rc == G6_OK) rc = g6_md_advance(ctx, warm);
+  if (rc == G6_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
+  if (rc == G6_OK) rc = g6_md_advance(ctx, timed);
+  if (rc == G6_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
+  if (ctx->in_run) { int r2 = g6_md_end(ctx, nullptr, nullptr); if (rc == G6_OK) rc = r2; }
+  if (rc == G6_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(ms, e0, e1) != cudaSuccess))
+    rc = fail(ctx, G6_ERR_CUDA, "event timing");
+  cudaMemcpyAsync(ctx->d_st, ctx->d_stage, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+  ctx->list_valid = false;
+  return rc;
+}
+
+// Force-only lanes per molecule: each candidate's kernel, best of 3 launches.
+static int tune_force_lpi(g6_ctx* ctx) {
+  static const int cand[4] = {4, 8, 16, 32};
   int best = ctx->lpi;
   double tbest = 1e30;
   for (int k = 0; k < 4; ++k) {
+    if (fit_lpi(ctx, cand[k]) != cand[k]) continue;   // rows do not fit this width's shared memory
     ctx->lpi = cand[k];
     double t = 1e30, m = 0.0;
     for (int rep = 0; rep < 3; ++rep) {
-      rc = g6_time_force(ctx, &m);
+      int rc = g6_time_force(ctx, &m);
       if (rc) return rc;
       t = std::min(t, m);
     }
     if (t < tbest) { tbest = t; best = cand[k]; }
   }
   ctx->lpi = best;
-  // fused MD step: short NVE runs from the current state, which is restored after
+  return G6_OK;
+}
+
+// MD-step kernel shape at the current skin: every (lanes, molecules per warp)
+// pair on a short run; returns the best shape's time for `timed` steps.
+static int tune_step_shape(g6_ctx* ctx, cudaEvent_t e0, cudaEvent_t e1, float* best_ms) {
+  static const int lcand[4] = {4, 8, 16, 32};
+  static const int mcand[3] = {8, 16, 32};
+  const int nm = ctx->prec == G6_MIXED ? 3 : 1;
+  int bl = ctx->step_lpi, bm = ctx->step_mpw;
+  float sb = 1e30f;
+  for (int k = 0; k < 4; ++k) {
+    if (fit_lpi(ctx, lcand[k]) != lcand[k]) continue;
+    for (int q = 0; q < nm; ++q) {
+      ctx->step_lpi = lcand[k];
+      ctx->step_mpw = ctx->prec == G6_MIXED ? mcand[q] : 8;
+      float ms = 0.0f;
+      int rc = time_md_steps(ctx, 2, 10, e0, e1, &ms);
+      if (rc) return rc;
+      if (ms < sb) { sb = ms; bl = ctx->step_lpi; bm = ctx->step_mpw; }
+    }
+  }
+  ctx->step_lpi = bl; ctx->step_mpw = bm;
+  *best_ms = sb / 10.0f;
+  return G6_OK;
+}
+
+static int tune(g6_ctx* ctx, int flags, g6_shape* out) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (ctx->in_run) return fail(ctx, G6_ERR_STATE, "tuning inside g6_md_begin/g6_md_end");
+  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
+  if (ctx->step_lpi == 0) ctx->step_lpi = ctx->lpi;
+  if (ctx->step_mpw == 0) ctx->step_mpw = default_mpw(ctx);
   const size_t bytes = (size_t)REC * ctx->n * sizeof(double);
   CK(cudaMemcpyAsync(ctx->d_stage, ctx->d_st, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   const unsigned long long steps0 = ctx->steps_done;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  int sbest = ctx->step_lpi ? ctx->step_lpi : best;
-  float sb = 1e30f;
-  for (int k = 0; k < 4 && rc == G6_OK; ++k) {
-    ctx->step_lpi = cand[k];
-    drop_graphs(ctx);
-    const int warm = 2, timed = 10;
-    rc = g6_md_begin(ctx, 0.001, warm + timed, nullptr, 0);
-    if (rc == G6_OK) rc = g6_md_advance(ctx, warm);
-    if (rc == G6_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
-    if (rc == G6_OK) rc = g6_md_advance(ctx, timed);
-    if (rc == G6_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ctx, G6_ERR_CUDA, "event");
-    if (ctx->in_run) { int r2 = g6_md_end(ctx, nullptr, nullptr); if (rc == G6_OK) rc = r2; }
-    if (rc == G6_OK) {
-      float ms = 0.0f;
-      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
-        rc = fail(ctx, G6_ERR_CUDA, "event timing");
-      else if (ms < sb) { sb = ms; sbest = cand[k]; }
+  float step_ms = 0.0f;
+  // skin candidates (A); the requested skin alone without G6_TUNE_SKIN
+  std::vector<double> skins;
+  const double skin0 = ctx->skin;
+  if (flags & G6_TUNE_SKIN) {
+    for (double sk : {0.5, 0.75, 1.0, 1.5}) skins.push_back(sk);
+  } else {
+    skins.push_back(skin0);
+  }
+  double best_skin = skin0;
+  float best_long = 1e30f;
+  int bl = 0, bs = 0, bm = 0;
+  for (size_t k = 0; k < skins.size() && rc == G6_OK; ++k) {
+    if (skins.size() > 1) {
+      ctx->skin = skins[k]; ctx->glist.valid = false; ctx->cap = 0;
     }
-    cudaMemcpyAsync(ctx->d_st, ctx->d_stage, bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+    rc = force_once(ctx);   // list for this skin
+    if (rc == G6_OK) rc = tune_force_lpi(ctx);
+    float short_ms = 0.0f;
+    if (rc == G6_OK) rc = tune_step_shape(ctx, e0, e1, &short_ms);
+    float long_ms = short_ms;
+    if (rc == G6_OK && skins.size() > 1) {
+      // the rebuild frequency depends on the skin: a longer run per candidate
+      const int timed = 128;
+      float ms = 0.0f;
+      rc = time_md_steps(ctx, 2, timed, e0, e1, &ms);
+      long_ms = ms / timed;
+    }
+    if (rc == G6_OK && long_ms < best_long) {
+      best_long = long_ms; best_skin = ctx->skin; bl = ctx->lpi; bs = ctx->step_lpi; bm = ctx->step_mpw;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc == G6_OK) {
+    if (skins.size() > 1 && best_skin != ctx->skin) { ctx->skin = best_skin; ctx->glist.valid = false; ctx->cap = 0; }
+    ctx->lpi = bl; ctx->step_lpi = bs; ctx->step_mpw = bm;
+    step_ms = best_long;
+  } else if (skins.size() > 1) {
+    ctx->skin = skin0; ctx->glist.valid = false; ctx->cap = 0;
+  }
   ctx->steps_done = steps0;
-  ctx->step_lpi = sbest;
   drop_graphs(ctx);
+  CK(cudaMemcpyAsync(ctx->d_st, ctx->d_stage, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->list_valid = false;
   if (rc) return rc;
-  if (lpi_out) *lpi_out = sbest;
+  rc = prepare_list(ctx);   // capacity of the chosen skin
+  if (rc) return rc;
+  if (out) fill_shape(ctx, out, step_ms);
+  g6_shape sh;
+  fill_shape(ctx, &sh, step_ms);
+  std::lock_guard<std::mutex> lk(shape_mutex());
+  shape_cache()[shape_key(ctx)] = sh;
+  return G6_OK;
+}
+
+extern "C" {
+
+int g6_tune(g6_ctx* ctx, int* lpi_out) {
+  int rc = tune(ctx, 0, nullptr);
+  if (rc) return rc;
+  if (lpi_out) *lpi_out = ctx->step_lpi;
+  return G6_OK;
+}
+
+int g6_tune_shape(g6_ctx* ctx, int flags, g6_shape* shape) { return tune(ctx, flags, shape); }
+
+int g6_get_shape(g6_ctx* ctx, g6_shape* shape) {
+  if (!ctx || !shape) return G6_ERR_ARG;
+  if (!ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system defined (g6_system)");
+  fill_shape(ctx, shape, 0.0);
+  return G6_OK;
+}
+
+int g6_set_shape(g6_ctx* ctx, const g6_shape* shape) {
+  if (!ctx || !shape) return G6_ERR_ARG;
+  auto ok = [](int l) { return l == 4 || l == 8 || l == 16 || l == 32; };
+  if (!ok(shape->lpi) || !ok(shape->step_lpi) || (shape->step_mpw != 8 && shape->step_mpw != 16 && shape->step_mpw != 32))
+    return fail(ctx, G6_ERR_ARG, "lanes per molecule must be 4, 8, 16 or 32 and molecules per warp 8, 16 or 32");
+  if (!(shape->skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
+  ctx->lpi = shape->lpi; ctx->step_lpi = shape->step_lpi; ctx->step_mpw = shape->step_mpw;
+  if (shape->skin != ctx->skin) { ctx->skin = shape->skin; ctx->glist.valid = false; ctx->cap = 0; }
+  drop_graphs(ctx);
   return G6_OK;
 }
 
@@ -1490,6 +1675,7 @@ int g6_set_lpi(g6_ctx* ctx, int lpi) {
   if (!ctx || (lpi != 4 && lpi != 8 && lpi != 16 && lpi != 32)) return G6_ERR_ARG;
   ctx->lpi = lpi;
   ctx->step_lpi = lpi;
+  if (ctx->step_mpw == 0) ctx->step_mpw = default_mpw(ctx);
   drop_graphs(ctx);
   return G6_OK;
 }
@@ -1603,6 +1789,7 @@ static int replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t cou
   ea.nrep = R; ea.parity = parity; ea.seed = seed; ea.counter = counter; ea.epot = ctx->d_epot_rep; ea.beta = ctx->d_beta;
   ea.th = ctx->d_th; ea.accepted = ctx->d_acc; ea.scale = ctx->d_scale;
   ea.numb = numb; ea.umb = d_umb; ea.op = d_op;
+  ea.temp = ctx->d_xtemp; ea.slot = ctx->d_slot; ea.moved = ctx->d_moved;
   CK(launch_exchange(ea, ctx->d_st, ctx->n, ctx->d_mol_rep, ctx->stream));
   if (numb > 0)
     CK(cudaMemcpyAsync(umbrella, d_umb, (size_t)R * numb * 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1628,6 +1815,42 @@ int g6_replica_exchange_umbrella(g6_ctx* ctx, int parity, uint64_t seed, uint64_
                                  g6_thermostat* thermo, int numbrella, double* umbrella, const double* op,
                                  int* accepted) {
   return replica_exchange(ctx, parity, seed, counter, beta, thermo, numbrella, umbrella, op, accepted);
+}
+
+int g6_exchange_plan(int nrep, int parity, uint64_t seed, uint64_t counter, const double* epot, double* beta,
+                     double* temp, int numbrella, double* umbrella, const double* op, double* scale, int* accepted) {
+  if (nrep < 1 || !epot || !beta || !temp || !scale) return G6_ERR_ARG;
+  if (parity != 0 && parity != 1) return G6_ERR_ARG;
+  if (numbrella < 0 || (numbrella > 0 && (!umbrella || !op))) return G6_ERR_ARG;
+  for (int r = 0; r < nrep; ++r)
+    if (!(temp[r] > 0.0) || !std::isfinite(beta[r]) || !std::isfinite(epot[r])) return G6_ERR_ARG;
+  std::vector<int> slot(nrep), moved(nrep);
+  ExchangeIO x;
+  x.nrep = nrep; x.parity = parity; x.seed = seed; x.counter = counter; x.epot = epot; x.beta = beta; x.temp = temp;
+  x.numb = numbrella; x.umb = umbrella; x.op = op; x.slot = slot.data(); x.scale = scale; x.moved = moved.data();
+  x.accepted = accepted;
+  exchange_run(x);
+  return G6_OK;
+}
+
+int g6_replica_scale(g6_ctx* ctx, const double* scale) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!scale) return fail(ctx, G6_ERR_ARG, "scale is required");
+  if (ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_replica_scale inside g6_md_begin/g6_md_end");
+  for (int r = 0; r < ctx->nrep; ++r)
+    if (!(scale[r] > 0.0) || !std::isfinite(scale[r])) return fail(ctx, G6_ERR_ARG, "scale factors must be positive");
+  CK(cudaMemcpyAsync(ctx->d_scale, scale, ctx->nrep * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_scale_velocity(ctx->d_st, ctx->n, ctx->d_mol_rep, ctx->d_scale, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return G6_OK;
+}
+
+int g6_last_epot(g6_ctx* ctx, double* epot) {
+  if (!ctx || !epot) return G6_ERR_ARG;
+  if (!ctx->have_system) return fail(ctx, G6_ERR_STATE, "no system defined (g6_system)");
+  for (int r = 0; r < ctx->nrep; ++r) epot[r] = ctx->last_epot[r];
+  return G6_OK;
 }
 
 }  // extern "C"

@@ -210,7 +210,8 @@ struct ForceArgs {
   double* tl;     // 3 SoA lab torque
   double* emol;   // n
   double* wmol;   // 9 SoA
-  int* npair_in;  // per molecule: pairs within rc (diagnostic, optional)
+  int* npair_in;  // per molecule: pairs within rc (diagnostic, optional; required by the mixed MD step)
+  float4* fres;   // mixed MD step: per molecule 4 float4 of float pairs (F, energy; lab torque, virial trace)
 };
 
 struct SitesArgs {
@@ -336,7 +337,96 @@ struct ExchArgs {
   int numb;             // parabolic umbrellas per replica (Umbrella.F90), 0 for none
   double* umb;          // (nrep, numb, 2): center, coefficient; swapped with beta on acceptance
   const double* op;     // (nrep, numb): the order parameters the umbrellas act on
+  double* temp;         // scratch (nrep): thermostat targets, permuted with beta
+  int* slot;            // scratch (nrep): replica of each temperature slot
+  int* moved;           // scratch (nrep): 1 for a replica whose temperature changed
 };
+
+// ---------------------------------------------------------------------------
+// Replica exchange, shared by the device kernel (one context) and the host
+// plan (replicas spread over processes): replica_exchange_trial
+// (Replica.F90:7-73) as the MD driver applies it (Mixture.F90:1589-1653).
+// The reference keeps node_in_charge(j), the replica that holds temperature
+// slot j, and tests neighbouring slots (j, jj); here the slots are the
+// replicas ordered by decreasing beta (ties by index), which is
+// node_in_charge for a ladder of distinct temperatures.  The pairs (j, j+1)
+// with j % 2 == parity are tested in increasing j (disjoint pairs, so their
+// order does not matter); pair j uses the uniform of Philox key seed, counter
+// (j, counter, 0x52).  An accepted pair trades beta, the thermostat
+// temperature and the umbrellas; both replicas get the velocity factor
+// sqrt(T_new / T_old) and are marked moved (their Nose zeta is reset).
+// ---------------------------------------------------------------------------
+struct ExchangeIO {
+  int nrep, parity;
+  unsigned long long seed, counter;
+  const double* epot;
+  double* beta;
+  double* temp;
+  int numb;
+  double* umb;
+  const double* op;
+  int* slot;
+  double* scale;
+  int* moved;
+  int* accepted;   // optional: 1 for the replica in the lower slot of an accepted pair
+};
+
+__host__ __device__ inline double umbrella_sum(const ExchangeIO& x, int r, int u) {
+  // coeffi (op - center)^2 of replica r's order parameters under replica u's umbrellas (Umbrella.F90:11-16)
+  double a = 0.0;
+  for (int k = 0; k < x.numb; ++k) {
+    const double* uu = x.umb + ((size_t)u * x.numb + k) * 2;
+    const double o = x.op[(size_t)r * x.numb + k];
+    a = a + uu[1] * ((o - uu[0]) * (o - uu[0]));
+  }
+  return a;
+}
+
+__host__ __device__ inline void exchange_run(const ExchangeIO& x) {
+  const int R = x.nrep;
+  for (int r = 0; r < R; ++r) {
+    x.scale[r] = 1.0;
+    x.moved[r] = 0;
+    if (x.accepted) x.accepted[r] = 0;
+    x.slot[r] = r;
+  }
+  for (int j = 1; j < R; ++j) {   // slots: decreasing beta, stable
+    const int v = x.slot[j];
+    int q = j - 1;
+    while (q >= 0 && x.beta[x.slot[q]] < x.beta[v]) { x.slot[q + 1] = x.slot[q]; --q; }
+    x.slot[q + 1] = v;
+  }
+  for (int j = x.parity; j + 1 < R; j += 2) {
+    const int n0 = x.slot[j], n1 = x.slot[j + 1];
+    const double b0 = x.beta[n0], b1 = x.beta[n1];
+    double a0 = x.epot[n0], a1 = x.epot[n1];
+    if (x.numb > 0) { a0 = a0 + umbrella_sum(x, n0, n0); a1 = a1 + umbrella_sum(x, n1, n1); }
+    const double acc0 = -(a0 * b0 + a1 * b1) * I2J * J2K;
+    a0 = x.epot[n0]; a1 = x.epot[n1];
+    if (x.numb > 0) { a0 = a0 + umbrella_sum(x, n0, n1); a1 = a1 + umbrella_sum(x, n1, n0); }
+    const double acc1 = -(a0 * b1 + a1 * b0) * I2J * J2K;
+    bool accept = acc0 < acc1;
+    if (!accept) {
+      double u[2];
+      uniform2(x.seed, (uint32_t)j, (uint32_t)x.counter, (uint32_t)(x.counter >> 32), 0x52u, u);
+      accept = u[0] < exp(acc1 - acc0);
+    }
+    if (x.accepted) x.accepted[n0] = accept ? 1 : 0;
+    if (!accept) continue;
+    x.beta[n0] = b1; x.beta[n1] = b0;
+    for (int k = 0; k < 2 * x.numb; ++k) {
+      const double t = x.umb[(size_t)n0 * x.numb * 2 + k];
+      x.umb[(size_t)n0 * x.numb * 2 + k] = x.umb[(size_t)n1 * x.numb * 2 + k];
+      x.umb[(size_t)n1 * x.numb * 2 + k] = t;
+    }
+    const double t0 = x.temp[n0], t1 = x.temp[n1];
+    x.scale[n0] = sqrt(t1 / t0);
+    x.scale[n1] = sqrt(t0 / t1);
+    x.temp[n0] = t1; x.temp[n1] = t0;
+    x.moved[n0] = 1; x.moved[n1] = 1;
+    x.slot[j] = n1; x.slot[j + 1] = n0;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Host-side declarations shared between translation units.
@@ -403,6 +493,13 @@ void make_pair_const(const ModelHost& m, int path, PairConst& pc);
 void make_cut_const(double rin, double rout, CutConst& cc);
 
 cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
+// Mixed-precision list kernel (g6_pairs.cu): force only, and the MD step as the
+// pair kernel plus the integrator kernel (`between`, optional, is recorded
+// between the two).
+cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStream_t s);
+cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
+                              cudaEvent_t between);
+int pairs_max_cap(int lpi);
 cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s);
 int pk64_width(int model);
 int pk32_width(int model);
@@ -421,5 +518,6 @@ cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, flo
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);
 cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s);
 cudaError_t launch_exchange(const ExchArgs& a, double* st, int n, const int* mol_rep, cudaStream_t s);
+cudaError_t launch_scale_velocity(double* st, int n, const int* mol_rep, const double* scale, cudaStream_t s);
 
 }  // namespace g6

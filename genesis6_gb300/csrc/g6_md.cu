@@ -97,54 +97,17 @@ cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, do
 // sqrt(T_new/T_old) (Rigid_ScaleVelocity) and its Nose zeta stack zeroed.
 
 __global__ void k_exchange(ExchArgs a) {
-  for (int r = threadIdx.x; r < a.nrep; r += blockDim.x) a.scale[r] = 1.0;
-  __syncthreads();
-  for (int r = threadIdx.x; r + 1 < a.nrep; r += blockDim.x) {
-    if ((r & 1) != a.parity) continue;
-    const int r1 = r + 1;
-    const double b0 = a.beta[r], b1 = a.beta[r1];
-    // replica_exchange_trial (Replica.F90:7-73): energies plus the umbrella
-    // potentials coeffi (op - center)^2 (Umbrella.F90:11-16), before and after
-    // the replicas trade temperatures and umbrellas
-    double a0 = a.epot[r], a1 = a.epot[r1];
-    for (int k = 0; k < a.numb; ++k) {
-      const double* u0 = a.umb + ((size_t)r * a.numb + k) * 2;
-      const double* u1 = a.umb + ((size_t)r1 * a.numb + k) * 2;
-      const double o0 = a.op[(size_t)r * a.numb + k], o1 = a.op[(size_t)r1 * a.numb + k];
-      a0 = a0 + u0[1] * ((o0 - u0[0]) * (o0 - u0[0]));
-      a1 = a1 + u1[1] * ((o1 - u1[0]) * (o1 - u1[0]));
-    }
-    const double acc0 = -(a0 * b0 + a1 * b1) * I2J * J2K;
-    a0 = a.epot[r]; a1 = a.epot[r1];
-    for (int k = 0; k < a.numb; ++k) {
-      const double* u0 = a.umb + ((size_t)r * a.numb + k) * 2;
-      const double* u1 = a.umb + ((size_t)r1 * a.numb + k) * 2;
-      const double o0 = a.op[(size_t)r * a.numb + k], o1 = a.op[(size_t)r1 * a.numb + k];
-      a0 = a0 + u1[1] * ((o0 - u1[0]) * (o0 - u1[0]));
-      a1 = a1 + u0[1] * ((o1 - u0[0]) * (o1 - u0[0]));
-    }
-    const double acc1 = -(a0 * b1 + a1 * b0) * I2J * J2K;
-    bool accept = false;
-    if (acc0 < acc1) accept = true;
-    else {
-      double u[2];
-      uniform2(a.seed, (uint32_t)r, (uint32_t)a.counter, (uint32_t)(a.counter >> 32), 0x52u, u);
-      accept = u[0] < exp(acc1 - acc0);
-    }
-    if (a.accepted) a.accepted[r] = accept ? 1 : 0;
-    if (accept) {
-      a.beta[r] = b1; a.beta[r1] = b0;
-      for (int k = 0; k < 2 * a.numb; ++k) {
-        const double t = a.umb[(size_t)r * a.numb * 2 + k];
-        a.umb[(size_t)r * a.numb * 2 + k] = a.umb[(size_t)r1 * a.numb * 2 + k];
-        a.umb[(size_t)r1 * a.numb * 2 + k] = t;
-      }
-      const double t0 = a.th[r].temp, t1 = a.th[r1].temp;
-      a.scale[r] = sqrt(t1 / t0);
-      a.scale[r1] = sqrt(t0 / t1);
-      a.th[r].temp = t1; a.th[r1].temp = t0;
-      for (int k = 0; k < 5; ++k) { a.th[r].z[k] = 0.0; a.th[r1].z[k] = 0.0; }
-    }
+  if (threadIdx.x != 0) return;
+  for (int r = 0; r < a.nrep; ++r) a.temp[r] = a.th[r].temp;
+  ExchangeIO x;
+  x.nrep = a.nrep; x.parity = a.parity; x.seed = a.seed; x.counter = a.counter; x.epot = a.epot; x.beta = a.beta;
+  x.temp = a.temp; x.numb = a.numb; x.umb = a.umb; x.op = a.op; x.slot = a.slot; x.scale = a.scale;
+  x.moved = a.moved; x.accepted = a.accepted;
+  exchange_run(x);
+  for (int r = 0; r < a.nrep; ++r) {
+    if (!a.moved[r]) continue;
+    a.th[r].temp = a.temp[r];
+    for (int k = 0; k < 5; ++k) a.th[r].z[k] = 0.0;
   }
 }
 
@@ -156,8 +119,13 @@ __global__ void k_scale_velocity(double* st, int n, const int* mol_rep, const do
   for (int c = 0; c < 3; ++c) { ST(3 + c) *= f; ST(18 + c) *= f; }
 }
 
+cudaError_t launch_scale_velocity(double* st, int n, const int* mol_rep, const double* scale, cudaStream_t s) {
+  if (n > 0) k_scale_velocity<<<(n + 127) / 128, 128, 0, s>>>(st, n, mol_rep, scale);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_exchange(const ExchArgs& a, double* st, int n, const int* mol_rep, cudaStream_t s) {
-  k_exchange<<<1, 128, 0, s>>>(a);
+  k_exchange<<<1, 32, 0, s>>>(a);
   if (n > 0) k_scale_velocity<<<(n + 127) / 128, 128, 0, s>>>(st, n, mol_rep, a.scale);
   return cudaGetLastError();
 }

@@ -1,0 +1,370 @@
+// g6_pairs.cu -- mixed-precision site-site forces over the Verlet list, and the
+// integrator kernel of the mixed MD step.
+//
+// k_pairs<Model, LPI, MODE>: LPI lanes cooperate on one molecule i; a warp
+// holds 32/LPI molecules and never waits for another warp (no block barrier).
+// Per molecule, two phases:
+//   1. test: the lanes read the neighbour row (coalesced) and the 32-bit
+//      fixed-point COM of each listed j (one 16-byte load), keep the pairs
+//      with |d|^2 < rc^2 (the FP32 distance of exact integer COM differences;
+//      within 1e-3 A^2 of rc^2 the reference's FP64 test decides) and append
+//      them to the molecule's row in shared memory with a ballot and a prefix
+//      count.  Four row entries per lane are in flight at a time.
+//   2. pairs: the lanes share out the compacted row (every lane of a group has
+//      an in-range pair until the row's tail), load j's packed pose one pair
+//      ahead and run the FP32 site loop of pair_math, keeping per-lane sums of
+//      the i-site forces, the COM switch force, the energy and the virial.
+// The lanes of a molecule are then combined: in FP64 for the force-only call
+// (MODE 0: F, lab torque, energy, full virial), with error-free float-pair
+// addition for the MD step (MODE 1: F, lab torque, energy and virial trace as
+// float pairs, read by k_integrate_mixed).
+//
+// k_integrate_mixed<NQ>: one molecule per lane, 32 per block: rigid_correct
+// with the small Gear terms in float (correct_mixed), the next predict and
+// placement, and the per-step reductions (step_reduce / finish_replica).
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "g6_internal.cuh"
+#include "g6_pairmath.cuh"
+#include "g6_rigid.cuh"
+
+namespace g6 {
+
+// Residency of k_pairs: 128 threads per block, at least MINB blocks per SM
+// (5: 96 registers, enough for the 3-charge models in the MD step without
+// spills; 4: 128 registers for the 4-charge models and the full virial).
+template <int LPI>
+struct PairShape {
+  static constexpr int THREADS = 128;
+  static constexpr int GROUPS = 32 / LPI;   // molecules per warp
+  static constexpr int UNROLL = 4;          // row entries per lane in flight during the test
+};
+template <class M, int MODE>
+struct PairMinBlocks {
+  static constexpr int value = (M::NQ == 3 && MODE == 1) ? 5 : 4;
+};
+
+// Fixed-point COM difference (units L/2^32, the wrap is the minimum image) to A.
+__device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi, const float4& qj, float sx, float sy,
+                                          float sz, float d[3]) {
+  d[0] = i32_to_f32((int)(xi - __float_as_uint(qj.x))) * sx;
+  d[1] = i32_to_f32((int)(yi - __float_as_uint(qj.y))) * sy;
+  d[2] = i32_to_f32((int)(zi - __float_as_uint(qj.z))) * sz;
+}
+
+template <class M, int LPI, int MODE>
+__global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MODE>::value)) k_pairs(ForceArgs a) {
+  constexpr int NW = MODE == 0 ? 9 : 1;
+  constexpr int G = PairShape<LPI>::GROUPS;
+  constexpr int U = PairShape<LPI>::UNROLL;
+  constexpr int NPK = M::NPK;
+  extern __shared__ int s_rows[];
+  const int n = a.n;
+  const int step = a.ctrl ? a.ctrl[1] : 0;
+  const bool odd = (step & 1) != 0;
+  const double* pk64 = odd ? a.pk64_1 : a.pk64;
+  const float4* pk32 = odd ? a.pk32_1 : a.pk32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane / LPI, sub = lane % LPI;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / LPI;
+  const bool valid = i < n;
+  int* srow = s_rows + (size_t)(warp * G + g) * a.cap;
+
+  // pose of i: fixed-point COM and float site offsets
+  float ri[M::NQ + 1][3];
+  uint32_t xi = 0, yi = 0, zi = 0;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  int r = 0, nn = 0;
+  if (valid) {
+    r = a.rep.mol_rep[i];
+    float wi[4 * NPK];
+#pragma unroll
+    for (int q = 0; q < NPK; ++q) {
+      const float4 t = pk32[(size_t)i * NPK + q];
+      wi[4 * q] = t.x; wi[4 * q + 1] = t.y; wi[4 * q + 2] = t.z; wi[4 * q + 3] = t.w;
+    }
+    xi = __float_as_uint(wi[0]); yi = __float_as_uint(wi[1]); zi = __float_as_uint(wi[2]);
+#pragma unroll
+    for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) ri[s][k] = wi[3 + 3 * s + k];
+    sx = a.rep.fscale[3 * r]; sy = a.rep.fscale[3 * r + 1]; sz = a.rep.fscale[3 * r + 2];
+    nn = a.nnb[i];
+  } else {
+#pragma unroll
+    for (int s = 0; s <= M::NQ; ++s) ri[s][0] = ri[s][1] = ri[s][2] = 0.f;
+  }
+
+  // ---- phase 1: in-range entries of the row into shared memory ----
+  int nmax = nn;
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, m));
+  const int* row = a.nbr + (size_t)(valid ? i : 0) * a.cap;
+  const float rout2 = a.cc.frout2;
+  const float band = 1e-3f;   // |dd32 - dd64| is below 1e-4 A^2 for boxes up to 1000 A
+  int cnt = 0;
+  for (int base = 0; base < nmax; base += LPI * U) {
+    int jj[U];
+    float4 qj[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = base + u * LPI + sub;
+      jj[u] = k < nn ? __ldg(row + k) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? pk32[(size_t)jj[u] * NPK] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      bool in = false;
+      if (jj[u] >= 0) {
+        float d[3];
+        fix_delta(xi, yi, zi, qj[u], sx, sy, sz, d);
+        const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        in = dd < rout2;
+        if (fabsf(dd - rout2) < band) {
+          // borderline: decide with the reference's FP64 arithmetic (Interaction_Compress2)
+          const double* pi = pk64 + (size_t)i * M::W64;
+          const double* pj = pk64 + (size_t)jj[u] * M::W64;
+          const double ci[3] = {pi[0], pi[1], pi[2]}, cj[3] = {pj[0], pj[1], pj[2]};
+          const double Ld[3] = {a.rep.L[3 * r], a.rep.L[3 * r + 1], a.rep.L[3 * r + 2]};
+          const double iLd[3] = {a.rep.invL[3 * r], a.rep.invL[3 * r + 1], a.rep.invL[3 * r + 2]};
+          double o[3], dx[3];
+          in = exact_dd(ci, cj, Ld, iLd, o, dx) < a.cc.rout2;
+        }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, in);
+      const unsigned mine = LPI == 32 ? bal : (bal >> (g * LPI)) & ((1u << LPI) - 1u);
+      if (in) srow[cnt + __popc(mine & ((1u << sub) - 1u))] = jj[u];
+      cnt += __popc(mine);
+    }
+  }
+  __syncwarp();
+
+  // ---- phase 2: site loops over the compacted row ----
+  Acc<M, float, NW> acc;
+  acc.zero();
+  {
+    const float frin2 = a.cc.frin2, frin = a.cc.frin, frout = a.cc.frout, fc1 = a.cc.fc1, fc2 = a.cc.fc2;
+    int t = sub;
+    float4 tn[NPK];
+    if (t < cnt) {
+      const int j0 = srow[t];
+#pragma unroll
+      for (int q = 0; q < NPK; ++q) tn[q] = pk32[(size_t)j0 * NPK + q];
+    }
+    for (; t < cnt; t += LPI) {
+      float wj[4 * NPK];
+#pragma unroll
+      for (int q = 0; q < NPK; ++q) {
+        wj[4 * q] = tn[q].x; wj[4 * q + 1] = tn[q].y; wj[4 * q + 2] = tn[q].z; wj[4 * q + 3] = tn[q].w;
+      }
+      if (t + LPI < cnt) {   // the next pair's pose, one pair ahead
+        const int jn = srow[t + LPI];
+#pragma unroll
+        for (int q = 0; q < NPK; ++q) tn[q] = pk32[(size_t)jn * NPK + q];
+      }
+      float d[3];
+      fix_delta(xi, yi, zi, make_float4(wj[0], wj[1], wj[2], 0.f), sx, sy, sz, d);
+      const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      float rj[M::NQ + 1][3];
+#pragma unroll
+      for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) rj[s][k] = wj[3 + 3 * s + k];
+      pair_math<M, float, NW>(d, dd, ri, rj, a.pc, frin2, frin, frout, fc1, fc2, a.pc.frl, a.pc.fru, a.pc.fw3, acc);
+    }
+  }
+
+  // ---- lane partials -> F, lab torque (rigid_collectforce), energy, virial ----
+  float fo[3], to[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float t = acc.fc[k];
+#pragma unroll
+    for (int q = 0; q <= M::NQ; ++q) t += acc.fs[q][k];
+    fo[k] = t;
+  }
+  {
+    float tx = 0.f, ty = 0.f, tz = 0.f;
+#pragma unroll
+    for (int q = 0; q <= M::NQ; ++q) {
+      tx += ri[q][1] * acc.fs[q][2] - ri[q][2] * acc.fs[q][1];
+      ty += ri[q][2] * acc.fs[q][0] - ri[q][0] * acc.fs[q][2];
+      tz += ri[q][0] * acc.fs[q][1] - ri[q][1] * acc.fs[q][0];
+    }
+    to[0] = tx; to[1] = ty; to[2] = tz;
+  }
+  if constexpr (MODE == 0) {
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { v[k] = (double)fo[k]; v[3 + k] = (double)to[k]; }
+    v[6] = (double)acc.e;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[7 + k] = (double)acc.w[k];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = group_sum<LPI>(v[k]);
+    if (valid && sub == 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
+      a.emol[i] = 0.5 * v[6];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
+      if (a.npair_in) a.npair_in[i] = cnt;
+    }
+  } else {
+    FF q8[8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { q8[k] = FF{fo[k], 0.0f}; q8[3 + k] = FF{to[k], 0.0f}; }
+    q8[6] = FF{acc.e, 0.0f};
+    q8[7] = FF{acc.w[0], 0.0f};
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+      for (int m = LPI / 2; m >= 1; m >>= 1) q8[k] = ff_add(q8[k], red_shfl(q8[k], m));
+    if (valid && sub == 0) {
+      float4* o = a.fres + (size_t)4 * i;
+      o[0] = make_float4(q8[0].hi, q8[1].hi, q8[2].hi, q8[6].hi);
+      o[1] = make_float4(q8[0].lo, q8[1].lo, q8[2].lo, q8[6].lo);
+      o[2] = make_float4(q8[3].hi, q8[4].hi, q8[5].hi, q8[7].hi);
+      o[3] = make_float4(q8[3].lo, q8[4].lo, q8[5].lo, q8[7].lo);
+      a.npair_in[i] = cnt;
+    }
+  }
+}
+
+// Mixed MD step, second kernel: Gear corrector, next predict + placement and
+// the step's reductions for 32 molecules per block.  MPW molecules per warp
+// (32 / MPW warps per block): the corrector's FP64 instructions cost a warp
+// 64 cycles each whatever the number of active lanes, so fewer molecules per
+// warp spread them over more schedulers (small systems, latency) and more
+// molecules per warp issue fewer of them (large systems, FP64 throughput).
+// The block's 32 results meet in shared memory for step_reduce.
+template <int NQ, int MPW>
+__global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a, StepArgs sa) {
+  __shared__ FF s_vv[32][NRED];
+  __shared__ float s_dm[32];
+  __shared__ int s_bad[32], s_rr[32];
+  const int step = a.ctrl[1];
+  const bool odd = (step & 1) != 0;
+  const bool predict_next = step + 1 < sa.ctrl[2];
+  const int n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane < MPW) {
+    const int m = warp * MPW + lane;
+    const int im = blockIdx.x * 32 + m;
+    FF vv[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = FF{0.0f, 0.0f};
+    float dmax2 = 0.0f;
+    int bad = 0, rr = -1;
+    if (im < n) {
+      rr = a.rep.mol_rep[im];
+      const float4* o = a.fres + (size_t)4 * im;
+      const float4 h0 = o[0], l0 = o[1], h1 = o[2], l1 = o[3];
+      const float F[3] = {h0.x + l0.x, h0.y + l0.y, h0.z + l0.z};
+      const float tl[3] = {h1.x + l1.x, h1.y + l1.y, h1.z + l1.z};
+      float ekt2, ekr2;
+      correct_mixed<NQ>(sa, im, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
+      vv[0] = FF{0.5f * h0.w, 0.5f * l0.w};
+      vv[1] = FF{0.5f * h1.w, 0.5f * l1.w};
+      vv[2] = FF{ekt2, 0.0f};
+      vv[3] = FF{ekr2, 0.0f};
+      vv[4] = FF{0.5f * (float)a.npair_in[im], 0.0f};
+    }
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) s_vv[m][k] = vv[k];
+    s_dm[m] = dmax2; s_bad[m] = bad; s_rr[m] = rr;
+  }
+  __syncthreads();
+  FF vv[NRED];
+  float dmax2 = 0.0f;
+  int bad = 0, rr = -1;
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = s_vv[lane][k];
+    dmax2 = s_dm[lane]; bad = s_bad[lane]; rr = s_rr[lane];
+  }
+  step_reduce<FF>(sa, vv, rr, dmax2, bad, 32, step, 0);
+}
+
+template <int LPI>
+size_t pairs_smem_bytes(int cap) {
+  return (size_t)(PairShape<LPI>::THREADS / 32) * PairShape<LPI>::GROUPS * cap * sizeof(int);
+}
+
+template <class M, int LPI, int MODE>
+static cudaError_t launch_pairs_t(const ForceArgs& a, cudaStream_t s) {
+  const int threads = PairShape<LPI>::THREADS;
+  const long long total = (long long)a.n * LPI;
+  const int blocks = (int)((total + threads - 1) / threads);
+  if (blocks == 0) return cudaSuccess;
+  const size_t smem = pairs_smem_bytes<LPI>(a.cap);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_pairs<M, LPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_pairs<M, LPI, MODE><<<blocks, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <class M, int MODE>
+static cudaError_t launch_pairs_l(const ForceArgs& a, int lpi, cudaStream_t s) {
+  switch (lpi) {
+    case 4: return launch_pairs_t<M, 4, MODE>(a, s);
+    case 8: return launch_pairs_t<M, 8, MODE>(a, s);
+    case 16: return launch_pairs_t<M, 16, MODE>(a, s);
+    default: return launch_pairs_t<M, 32, MODE>(a, s);
+  }
+}
+
+template <int MODE>
+static cudaError_t launch_pairs_any(const ForceArgs& a, int model, int lpi, cudaStream_t s) {
+  if (model_nq(model) == 3) return launch_pairs_l<MT<3, false>, MODE>(a, lpi, s);
+  if (a.pc.taper) return launch_pairs_l<MT<4, true>, MODE>(a, lpi, s);
+  return launch_pairs_l<MT<4, false>, MODE>(a, lpi, s);
+}
+
+// Largest row capacity (entries) whose shared-memory rows fit one block.
+int pairs_max_cap(int lpi) {
+  const size_t lim = 200 * 1024;
+  switch (lpi) {
+    case 4: return (int)(lim / pairs_smem_bytes<4>(1));
+    case 8: return (int)(lim / pairs_smem_bytes<8>(1));
+    case 16: return (int)(lim / pairs_smem_bytes<16>(1));
+    default: return (int)(lim / pairs_smem_bytes<32>(1));
+  }
+}
+
+// Mixed force only: F, lab torque, per-molecule energy and virial in FP64.
+cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStream_t s) {
+  return launch_pairs_any<0>(a, model, lpi, s);
+}
+
+template <int NQ>
+static void launch_integrate(const ForceArgs& a, const StepArgs& sa, int mpw, int blocks, cudaStream_t s) {
+  switch (mpw) {
+    case 8: k_integrate_mixed<NQ, 8><<<blocks, 128, 0, s>>>(a, sa); break;
+    case 16: k_integrate_mixed<NQ, 16><<<blocks, 64, 0, s>>>(a, sa); break;
+    default: k_integrate_mixed<NQ, 32><<<blocks, 32, 0, s>>>(a, sa); break;
+  }
+}
+
+// Mixed MD step: pair kernel, then the integrator kernel (mpw molecules per warp).
+cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
+                              cudaEvent_t between) {
+  cudaError_t e = launch_pairs_any<1>(a, model, lpi, s);
+  if (e != cudaSuccess) return e;
+  if (between) {
+    e = cudaEventRecordWithFlags(between, s, cudaEventRecordExternal);
+    if (e != cudaSuccess) return e;
+  }
+  const int blocks = (a.n + 31) / 32;
+  if (blocks == 0) return cudaSuccess;
+  if (model_nq(model) == 3) launch_integrate<3>(a, sa, mpw, blocks, s);
+  else launch_integrate<4>(a, sa, mpw, blocks, s);
+  return cudaGetLastError();
+}
+
+}  // namespace g6

@@ -187,6 +187,17 @@ class RigidWater:
         return {"accepted": counts[0::2].copy(), "trials": counts[1::2].copy(), "energy": energy,
                 "samples": samples[:, :nsm], "trace": tr}
 
+    def last_epot(self):
+        """Potential energy of each replica at the last MD step (g6_last_epot)."""
+        e = np.zeros(self.nrep)
+        self._check(self.L.g6_last_epot(self.ctx, dptr(e)))
+        return e
+
+    def replica_scale(self, scale):
+        """Scale every replica's COM and angular velocities (g6_replica_scale)."""
+        scale = np.ascontiguousarray(scale, dtype=np.float64)
+        self._check(self.L.g6_replica_scale(self.ctx, dptr(scale)))
+
     def replica_exchange(self, parity, seed, counter, beta, thermo, umbrella=None, op=None):
         """Neighbour exchange (Replica.F90:7-73).  With umbrella (nrep, k, 2) =
         (center, coeffi) and op (nrep, k), the umbrella-aware test; the umbrellas

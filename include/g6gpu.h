@@ -206,6 +206,31 @@ int g6_time_force(g6_ctx* ctx, double* ms);
 int g6_tune(g6_ctx* ctx, int* lpi);
 int g6_set_lpi(g6_ctx* ctx, int lpi);
 
+/* Kernel shape of a context: the parameters that change the speed of the
+   force and MD-step kernels but not the set of interacting pairs (every
+   listed pair is re-tested against r_out each step).  No counterpart in the
+   reference, whose CPU loops have no launch shape. */
+typedef struct g6_shape {
+  int lpi;         /* lanes per molecule, force-only kernel (4, 8, 16, 32)           */
+  int step_lpi;    /* lanes per molecule, pair kernel of the MD step (4, 8, 16, 32)  */
+  int step_mpw;    /* molecules per warp, mixed MD integrator kernel (8, 16, 32)     */
+  double skin;     /* Verlet margin [A] (g6_set_skin)                                */
+  int cap;         /* neighbour-list row capacity that follows from the skin         */
+  double step_ms;  /* g6_tune_shape: the chosen shape's MD step time in the search   */
+} g6_shape;
+#define G6_TUNE_SKIN 1
+/* Autotuner: times the candidates on the uploaded state (restored after every
+   trial run) with CUDA events -- the force kernel for lpi, short NVE runs for
+   every (step_lpi, step_mpw) pair and, with G6_TUNE_SKIN, 128-step runs for
+   skins of 0.5, 0.75, 1.0 and 1.5 A (the rebuild frequency depends on the
+   skin) -- and keeps the fastest.  The choice is cached per model, path,
+   precision, replica count, molecule count and cutoff: a context of the same
+   size that has no shape of its own starts from it.  g6_tune is
+   g6_tune_shape(ctx, 0, NULL) returning step_lpi. */
+int g6_tune_shape(g6_ctx* ctx, int flags, g6_shape* shape);
+int g6_get_shape(g6_ctx* ctx, g6_shape* shape);
+int g6_set_shape(g6_ctx* ctx, const g6_shape* shape);
+
 /* One MD step with the state in caller-owned host memory: uploads rec,
    advances one step, downloads rec and the step's log record.  This is the
    call a host-side driver makes when it keeps the state itself.  With rec in
@@ -220,8 +245,10 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
    the replicas of this context, FP64 acceptance.  beta[nrep] is in 1/K and is
    permuted in place on acceptance (with the MD side effects of
    Mixture.F90:1630-1653: velocities scaled by sqrt(T'/T), Nose zeta reset).
-   parity selects the pairs (r, r+1) with r % 2 == parity.  accepted[nrep]
-   (optional) gets 1 for each lower member of an accepted pair. */
+   The temperature slots are the replicas ordered by decreasing beta (the
+   reference's node_in_charge, Mixture.F90:1589-1611); parity selects the slot
+   pairs (j, j+1) with j % 2 == parity.  accepted[nrep] (optional) gets 1 for
+   the replica in the lower slot of each accepted pair. */
 int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
                         g6_thermostat* thermo, int* accepted);
 /* The same with numbrella parabolic umbrellas per replica on order parameters
@@ -232,6 +259,29 @@ int g6_replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter
 int g6_replica_exchange_umbrella(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,
                                  g6_thermostat* thermo, int numbrella, double* umbrella, const double* op,
                                  int* accepted);
+
+/* The decision step of g6_replica_exchange(_umbrella) on the host, for an
+   ensemble whose replicas live in several contexts, processes or GPUs: the
+   gather -> replica_exchange_trial -> scatter of mc2.F90:901-1001 and
+   Mixture.F90:1583-1653, where every process gathers the (E, beta, T,
+   umbrella, op) of all nrep replicas, calls this with the same arguments
+   (same seed and counter) and so reaches the same decisions.  Host only, no
+   context and no device.  epot[nrep] (internal units), beta[nrep] [1/K] and
+   temp[nrep] [K, the thermostat targets] are permuted in place on acceptance
+   (umbrella[nrep][numbrella][2] too); scale[nrep] gets the velocity factor
+   sqrt(T_new/T_old) (1 when unchanged), accepted[nrep] (optional) as above.
+   Decisions and draws are those of g6_replica_exchange_umbrella; apply the
+   factors to a context's replicas with g6_replica_scale and reset the Nose
+   zeta of each replica whose temperature changed. */
+int g6_exchange_plan(int nrep, int parity, uint64_t seed, uint64_t counter, const double* epot, double* beta,
+                     double* temp, int numbrella, double* umbrella, const double* op, double* scale, int* accepted);
+/* Rigid_ScaleVelocity (Mixture.F90:1631-1637) for every replica of the
+   context: the COM and angular-velocity first derivatives of replica r are
+   multiplied by scale[r] (> 0). */
+int g6_replica_scale(g6_ctx* ctx, const double* scale);
+/* Potential energy epot[nrep] of each replica at the last MD step (the
+   rep_energy that replica_exchange_trial reads, Mixture.F90:1587). */
+int g6_last_epot(g6_ctx* ctx, double* epot);
 
 /* Monte Carlo, mc2.F90:544-832: the replicas of the context are independent
    chains; each advances ntrial single-molecule trials (uniform target,

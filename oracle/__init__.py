@@ -73,6 +73,8 @@ def lib():
         L.orc_mc_run.argtypes = [c_int, c_int, c_int, dp, dp, dp, c_double, c_double, c_double, c_double, c_double,
                                  c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, dp, dp]
         L.orc_max_threads.restype = c_int
+        L.orc_vreset2.argtypes = [c_int, c_int, c_double, c_double, dp, dp, dp]
+        L.orc_replica_exchange_trial.argtypes = [c_int, c_int, ip, c_double, dp, dp, c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -229,6 +231,23 @@ def mc_run(model, path, com, quat, L, rin, rc, beta, sig_t, sig_r, ntrial, seed,
     lib().orc_mc_run(MODEL[model], PATH[path], com.shape[0], com, quat, _f64(L), rin, rc, beta, sig_t, sig_r, ntrial,
                      seed, chain, counter, e, trace)
     return com, quat, e[0], trace
+
+
+def vreset2(model, n, temp, dt, u):
+    """rigid_vreset2 on a given stream of uniforms u (n, 12): returns d1 (n,3) = v*dt and w1 (n,3)."""
+    d1 = np.zeros((n, 3)); w1 = np.zeros((n, 3))
+    lib().orc_vreset2(MODEL[model], n, temp, dt, _f64(u), d1, w1)
+    return d1, w1
+
+
+def replica_exchange_trial(j, jj, node_in_charge, u, energy, beta, umbrella=None, op=None):
+    """Replica.F90:7-73 on temperature slots j, jj (0-based); node_in_charge (int32),
+    beta and umbrella (nrep, numbrella, 2) are updated in place.  Returns accept."""
+    nb = 0 if umbrella is None else umbrella.shape[1]
+    umb = np.zeros(1) if umbrella is None else umbrella
+    opv = np.zeros(1) if op is None else _f64(op)
+    return bool(lib().orc_replica_exchange_trial(int(j), int(jj), node_in_charge, float(u), _f64(energy), beta, nb,
+                                                 umb, opv))
 
 
 def max_threads() -> int:

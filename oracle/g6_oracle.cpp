@@ -1333,6 +1333,61 @@ int orc_mc_run(int model, int path, int n, double* com, double* quat, const doub
   return 0;
 }
 
+// rigid_vreset2 (RigidModule.F90:1016-1053): per molecule, in this order,
+// dx(1), dy(1), dz(1) = Random_Normal(0, temp*rgas*J2I/mass, r1, r2) * dt and
+// wx(1), wy(1), wz(1) = Random_Normal(0, temp*rgas*J2I/I_k, r1, r2), each
+// from the next two numbers of the stream u (the caller's Random_GetNext
+// values, 12 per molecule).  Random_Normal is RandomModule.F90:28-36.
+void orc_vreset2(int model, int n, double temp, double dt, const double* u, double* d1 /*n,3*/, double* w1 /*n,3*/) {
+  Model m;
+  if (!make_model(model, m)) return;
+  const double kT = temp * RGAS * J2I;
+  const double var[6] = {kT / m.mass, kT / m.mass, kT / m.mass, kT / m.Ixx, kT / m.Iyy, kT / m.Izz};
+  for (int i = 0; i < n; ++i) {
+    const double* ui = u + 12 * (size_t)i;
+    for (int k = 0; k < 3; ++k) d1[3 * i + k] = random_normal(0.0, var[k], ui[2 * k], ui[2 * k + 1]) * dt;
+    for (int k = 0; k < 3; ++k) w1[3 * i + k] = random_normal(0.0, var[3 + k], ui[6 + 2 * k], ui[7 + 2 * k]);
+  }
+}
+
+// replica_exchange_trial (Replica.F90:7-73) for temperature slots j, jj
+// (0-based): node_in_charge[slot] is the replica holding that slot; u is the
+// random_getnext value for the Metropolis test; umbrella (nrep, numbrella, 2)
+// holds (center, coeffi), op (nrep, numbrella) the order parameters
+// (umbrella_potential = coeffi (op - center)^2, Umbrella.F90:11-16).  On
+// acceptance beta, the umbrellas and node_in_charge are swapped.  Returns 1
+// when accepted.
+int orc_replica_exchange_trial(int j, int jj, int* node_in_charge, double u, const double* rep_energy,
+                               double* rep_beta, int numbrella, double* rep_umbrella, const double* rep_op) {
+  const int n0 = node_in_charge[j], n1 = node_in_charge[jj];
+  auto up = [&](int owner, int at) {   // umbrella of replica `owner` on the order parameter of replica `at`
+    double a = 0.0;
+    for (int k = 0; k < numbrella; ++k) {
+      const double* uu = rep_umbrella + ((size_t)owner * numbrella + k) * 2;
+      const double o = rep_op[(size_t)at * numbrella + k];
+      a = a + uu[1] * ((o - uu[0]) * (o - uu[0]));
+    }
+    return a;
+  };
+  double a0 = rep_energy[n0], a1 = rep_energy[n1];
+  if (numbrella > 0) { a0 = a0 + up(n0, n0); a1 = a1 + up(n1, n1); }
+  const double acceptance0 = -(a0 * rep_beta[n0] + a1 * rep_beta[n1]) * I2J * J2K;
+  a0 = rep_energy[n0]; a1 = rep_energy[n1];
+  if (numbrella > 0) { a0 = a0 + up(n1, n0); a1 = a1 + up(n0, n1); }
+  const double acceptance1 = -(a0 * rep_beta[n1] + a1 * rep_beta[n0]) * I2J * J2K;
+  bool accept = false;
+  if (acceptance0 < acceptance1) accept = true;
+  else if (u < std::exp(acceptance1 - acceptance0)) accept = true;
+  if (accept) {
+    for (int k = 0; k < 2 * numbrella; ++k)
+      std::swap(rep_umbrella[(size_t)n0 * numbrella * 2 + k], rep_umbrella[(size_t)n1 * numbrella * 2 + k]);
+    std::swap(rep_beta[n0], rep_beta[n1]);
+    node_in_charge[j] = n1;
+    node_in_charge[jj] = n0;
+  }
+  return accept ? 1 : 0;
+}
+
 int orc_max_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -32,7 +32,7 @@ def _canon(p):
     return key
 
 
-@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (1000, 7.0)])
+@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (1000, 7.0), (32768, 9.0)])
 def test_cells_bitexact(orc, n, rc):
     s, b = _system("TIP4P", "custom", n, 11 + n, rc=rc, jitter=3.0)
     cell_gpu = s.cells()
@@ -40,7 +40,7 @@ def test_cells_bitexact(orc, n, rc):
     assert np.array_equal(cell_gpu, cell_orc)
 
 
-@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (512, 9.5)])
+@pytest.mark.parametrize("n,rc", [(256, 8.5), (4096, 9.0), (512, 9.5), (32768, 9.0)])
 def test_pairset_bitexact(orc, n, rc):
     s, b = _system("TIP4P", "custom", n, 3 + n, rc=rc, jitter=3.0)
     pg = s.pairsearch()
@@ -73,14 +73,18 @@ def test_force_fp64_matches_oracle(orc, model, path):
     assert np.abs(tau - to).max() <= 1e-12 * trms
 
 
-def test_force_fp64_4096(orc):
-    s, b = _system("TIP4P", "custom", 4096, 4, rc=9.0)
+@pytest.mark.parametrize("n,seed", [(4096, 4), (32768, 17)])
+def test_force_fp64_large(orc, n, seed):
+    """TIP4P-4096 and TIP4P-32768 (ndiv 11 at rc 9 A): FP64 energy, virial and
+    per-molecule force/torque against the oracle's full force path."""
+    s, b = _system("TIP4P", "custom", n, seed, rc=9.0)
     F, tau, ep, vir = s.force()
-    Fo, to, Eo, Vo, _ = orc.compute("TIP4P", "custom", b["com"], b["quat"], b["L"], [9.0] * 3, 7.0, 9.0)
+    Fo, to, Eo, Vo, npair = orc.compute("TIP4P", "custom", b["com"], b["quat"], b["L"], [9.0] * 3, 7.0, 9.0)
     assert ep[0] == pytest.approx(Eo, rel=1e-12)
     assert np.abs(vir[0] - Vo).max() <= 1e-12 * np.abs(Vo).max()
-    frms = np.sqrt((Fo ** 2).sum(1).mean())
+    frms = np.sqrt((Fo ** 2).sum(1).mean()); trms = np.sqrt((to ** 2).sum(1).mean())
     assert np.abs(F - Fo).max() <= 1e-12 * frms
+    assert np.abs(tau - to).max() <= 1e-12 * trms
 
 
 @pytest.mark.parametrize("model,path", CASES)
@@ -140,6 +144,10 @@ def test_md_fp64_follows_oracle(orc, model, path):
     rec_o, _, log_o = orc.md_run(model, path, b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 20, np.zeros(10))
     assert np.abs(log[:, 0, 0] - log_o[:, 0]).max() <= 1e-9 * np.abs(log_o[:, 0]).max()
     assert np.abs(log[:, 0, 5] - log_o[:, 5]).max() <= 1e-9 * np.abs(log_o[:, 5]).max()
+    # kinetic energies, temperature and pressure (rigid_ek, Rigid_PressureTensor; Mixture.F90:2251-2264)
+    for c in (1, 2, 3):
+        assert np.abs(log[:, 0, c] - log_o[:, c]).max() <= 1e-9 * np.abs(log_o[:, c]).max(), c
+    assert np.abs(log[:, 0, 4] - log_o[:, 4]).max() <= 1e-8 * np.abs(log_o[:, 4]).max()
     assert np.abs(rec_g[:, :3] - rec_o[:, :3]).max() < 1e-9
     assert np.abs(rec_g[:, 33:37] - rec_o[:, 33:37]).max() < 1e-9
     assert np.array_equal(log[:, 0, 6], log_o[:, 6])   # pairs within rc, every step
