@@ -63,6 +63,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
     p.add_argument("--n", type=int, default=N_MAIN, help="molecules of the 'md' profiling case")
+    p.add_argument("--shape", default=None,
+                   help="'md' profiling case: lanes,step_lanes,molecules_per_warp,skin instead of running the tuner "
+                        "(keeps the tuner's many launches out of a profiler capture)")
     p.add_argument("--profile", choices=["md", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
                         "--n TIP4P molecules (mixed, Nose 300 K, one g6_md_run after a 20-step start); 'mc' = two runs of --steps trials on "
@@ -328,11 +331,13 @@ def ess_geyer(x):
     return n / tau
 
 
-def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
+def bench_replicas(torch, steps=50000, every=500, loop_steps=200, seed=20261203):
     """64 TIP4P replicas (216-2,048 molecules, log-uniform), 220-360 K geometric,
     stochastic-collision thermostat, rc 8.5 A, dt 2 fs, neighbour swaps every
-    500 steps: all replicas in one context (CUDA-graph steps) vs one context
-    per replica run one after the other.  Aggregate ns/day."""
+    500 steps over 50,000 steps (the temperature slots alternate parity; FP64
+    acceptance): all replicas in one context (CUDA-graph steps) vs one context
+    per replica run one after the other.  Aggregate ns/day, and the acceptance
+    of every neighbouring pair of temperature slots."""
     import genesis6_gb300 as g6
     from genesis6_gb300 import config
     R = 64
@@ -345,26 +350,29 @@ def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
     rate = 1.0   # collisions per molecule per ps
 
     def thermo(s, tr):
-        th = s.thermostats(len(tr), "andersen", temp=tr, rate=rate, seed=seed)
-        return th
+        return s.thermostats(len(tr), "andersen", temp=tr, rate=rate, seed=seed)
     # batched
     s = g6.RigidWater("TIP4P", sizes, np.array(boxes), path="custom", precision="mixed", rc=8.5)
     s.upload_state(np.concatenate(recs))
     th = thermo(s, temps)
-    s.md_run(DT, 50, th, log=False)   # warm-up (graph capture, list build)
+    s.md_run(DT, 500, th, log=False)   # warm-up (graph capture, list builds, the lattice start relaxes)
     beta = 1.0 / np.array([th[r].temp for r in range(R)])
+    pair_att = np.zeros(R - 1, int)
+    pair_acc = np.zeros(R - 1, int)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    acc = np.zeros(R)
     done = 0
     swap = 0
     while done < steps:
-        k = min(500, steps - done)
+        k = min(every, steps - done)
         s.md_run(DT, k, th, log=False)
         done += k
-        if done % 500 == 0:
+        if done % every == 0:
+            slots = np.array(sorted(range(R), key=lambda r: (-beta[r], r)))   # temperature slots before the attempt
             beta, a = s.replica_exchange(swap & 1, seed, swap, beta, th)
-            acc += a
+            for j in range(swap & 1, R - 1, 2):
+                pair_att[j] += 1
+                pair_acc[j] += int(a[slots[j]])
             swap += 1
     torch.cuda.synchronize()
     t_batched = time.perf_counter() - t0
@@ -387,11 +395,17 @@ def bench_replicas(torch, steps=1000, loop_steps=100, seed=20261203):
     agg_loop = R * loop_steps * DT * 1e-3 * 86400.0 / t_loop
     for c, _ in ctxs:
         c.close()
+    rates = pair_acc / np.maximum(pair_att, 1)
     return {"replicas": R, "molecules": int(sizes.sum()), "min_size": int(sizes.min()), "max_size": int(sizes.max()),
             "batched_ns_per_day_aggregate": agg_batched, "loop_ns_per_day_aggregate": agg_loop,
-            "batched_over_loop": agg_batched / agg_loop, "batched_steps": steps, "loop_steps": loop_steps,
-            "swap_attempts": int(swap), "accepted_swaps": int(acc.sum()),
-            "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed"}
+            "batched_over_loop": agg_batched / agg_loop, "batched_steps": steps, "batched_seconds": t_batched,
+            "loop_steps": loop_steps, "swap_every": every, "swap_attempts": int(pair_att.sum()),
+            "accepted_swaps": int(pair_acc.sum()),
+            "acceptance_per_slot_pair": [round(float(x), 3) for x in rates],
+            "acceptance_slot_pairs_K": [[round(float(temps[j]), 1), round(float(temps[j + 1]), 1)] for j in range(R - 1)],
+            "thermostat": "stochastic collisions, 1 per molecule per ps", "precision": "mixed",
+            "structure": "all 64 replicas in every kernel of a step (head, pair kernel, integrator kernel), "
+                         "16-step CUDA graphs; a swap attempt between graph launches"}
 
 
 def mc_chains(C=32, N=1024, T=260.0, rc=9.0, seed=20261203, melt_steps=5000, md_steps=30000):
@@ -853,7 +867,12 @@ def run_profile(args):
         s.md_run(DT, 20, thermo_for(s), log=False)
         from genesis6_gb300 import _capi
         shape = _capi.Shape()
-        s._check(s.L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))
+        if args.shape:
+            lp, slp, mpw, sk = args.shape.split(",")
+            shape = _capi.Shape(lpi=int(lp), step_lpi=int(slp), step_mpw=int(mpw), skin=float(sk), cap=0, step_ms=0.0)
+            s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(shape)))
+        else:
+            s._check(s.L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))
         print("shape:", shape.as_dict())
         log = s.md_run(DT, args.steps, thermo_for(s))
         print("md ok: %d steps, last T %.1f K" % (args.steps, float(log[-1, 0, 3])))

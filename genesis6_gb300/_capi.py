@@ -14,7 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libg6gpu.so")
 
-G6_OK, G6_ERR_ARG, G6_ERR_CUDA, G6_ERR_CAPACITY, G6_ERR_NONFINITE, G6_ERR_TIMEOUT, G6_ERR_STATE = range(7)
+G6_OK, G6_ERR_ARG, G6_ERR_CUDA, G6_ERR_CAPACITY, G6_ERR_NONFINITE = range(5)
+G6_ERR_STATE = 6   # (5 is unused)
 TIP4P, TIP5P, ST2, SPCE = 1, 2, 3, 4
 MODELS = {"TIP4P": TIP4P, "TIP5P": TIP5P, "ST2": ST2, "SPCE": SPCE}
 PATH_STD, PATH_CUSTOM = 0, 1

@@ -245,6 +245,9 @@ struct g6_ctx {
   double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
   int* d_npin = nullptr;
   float4* d_fres = nullptr;       // mixed MD step: per-molecule float-pair results of the pair kernel
+  double* d_save = nullptr;       // state at the start of the current run (row-overflow recovery)
+  int cap_request = 0;            // neighbour-list row capacity set by g6_set_shape or raised after an overflow
+  bool overflow_recovered = false;   // the last run overflowed a row and was rolled back
   double* d_stage = nullptr;      // AoS staging (53 n)
   // grids
   HostGrid gref, glist;
@@ -460,6 +463,7 @@ static int prepare_list(g6_ctx* ctx) {
   int cap = (int)(2.0 * expect + 64.0);
   int nmax = 0;
   for (int r = 0; r < ctx->nrep; ++r) nmax = std::max(nmax, ctx->off[r + 1] - ctx->off[r]);
+  if (ctx->cap_request > 0) cap = ctx->cap_request;
   cap = std::min(cap, std::max(nmax - 1, 1));
   cap = (cap + 31) / 32 * 32;
   if (cap != ctx->cap) {
@@ -584,7 +588,6 @@ const char* g6_status_string(int s) {
     case G6_ERR_CUDA: return "CUDA error";
     case G6_ERR_CAPACITY: return "capacity exceeded";
     case G6_ERR_NONFINITE: return "non-finite value";
-    case G6_ERR_TIMEOUT: return "device wait timed out";
     case G6_ERR_STATE: return "call order";
     default: return "unknown status";
   }
@@ -714,6 +717,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_fres, 4 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_save, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
@@ -749,7 +753,8 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
 
 int g6_set_cutoff(g6_ctx* ctx, double r_in, double r_out) {
   if (!ctx) return G6_ERR_ARG;
-  if (!(r_out > 0.0) || !(r_in < r_out)) return fail(ctx, G6_ERR_ARG, "need r_in < r_out, r_out > 0");
+  if (!(r_out > 0.0) || !(r_in >= 0.0) || !(r_in < r_out))
+    return fail(ctx, G6_ERR_ARG, "need 0 <= r_in < r_out");
   make_cut_const(r_in, r_out, ctx->cc);
   ctx->have_cut = true;
   ctx->gref.valid = false; ctx->glist.valid = false; ctx->cap = 0;
@@ -1170,7 +1175,7 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
     // pair kernel, then the integrator kernel; the kernel events bracket the pair kernel
     CK(launch_step_mixed(fa, sa, ctx->model, ctx->step_lpi, ctx->step_mpw, ctx->stream, kev ? ev[2] : nullptr));
   } else {
-    CK(launch_step(fa, sa, ctx->model, false, ctx->step_lpi, ctx->stream));
+    CK(launch_step_fp64(fa, sa, ctx->model, ctx->step_lpi, ctx->stream));
     if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
   }
   if (ev) CK(cudaEventRecordWithFlags(ev[3], ctx->stream, cudaEventRecordExternal));
@@ -1192,8 +1197,13 @@ static int md_start(g6_ctx* ctx, double dt) {
   return G6_OK;
 }
 
-static int md_stop(g6_ctx* ctx) {
-  if (ctx->prec == G6_MIXED) CK(launch_stf_move(ctx->d_st, ctx->d_stf, ctx->n, 0, ctx->stream));
+// End of a run: the mixed path finishes its last step's replicas here (every
+// other step is finished inside the next step's pair kernel).
+static int md_stop(g6_ctx* ctx, const StepArgs& sa) {
+  if (ctx->prec == G6_MIXED) {
+    CK(launch_finish_step(sa, ctx->nrep, ctx->stream));
+    CK(launch_stf_move(ctx->d_st, ctx->d_stf, ctx->n, 0, ctx->stream));
+  }
   return G6_OK;
 }
 
@@ -1329,6 +1339,12 @@ static int md_check(g6_ctx* ctx, int nsteps, g6_thermostat* thermo) {
   const int* ctrl = pr.ctrl_dn;
   const ThermoDev* th = pr.th_dn;
   const double* red = pr.red;
+  // errors first: a failed run leaves the caller's thermostats untouched
+  const int ovf = *pr.ovf;
+  if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
+  if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow");
+  if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");
+  if (ctrl[1] != nsteps) return fail(ctx, G6_ERR_STATE, "step counter mismatch");
   for (int r = 0; r < ctx->nrep; ++r) {
     ctx->last_epot[r] = red[(size_t)r * NRED];
     if (thermo) {
@@ -1337,14 +1353,25 @@ static int md_check(g6_ctx* ctx, int nsteps, g6_thermostat* thermo) {
       thermo[r].zetasum = th[r].zsum;
     }
   }
-  const int ovf = *pr.ovf;
-  if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
-  if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow (raise the skin or density)");
-  if (ctrl[3] & 1) return fail(ctx, G6_ERR_NONFINITE, "non-finite force, torque or position");
-  if (ctrl[1] != nsteps) return fail(ctx, G6_ERR_STATE, "step counter mismatch");
   ctx->steps_done += (unsigned long long)nsteps;
   ctx->list_valid = true;   // every step leaves the list valid for its positions
   return G6_OK;
+}
+
+// A neighbour-list row overflowed during a run: the steps after it used
+// truncated rows, so the state goes back to the run's start (saved at
+// g6_md_begin) and the row capacity is raised by half for the next attempt.
+static int recover_overflow(g6_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->d_st, ctx->d_save, (size_t)REC * ctx->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->cap_request = (ctx->cap * 3 / 2 + 31) / 32 * 32;
+  ctx->glist.valid = false; ctx->cap = 0; ctx->list_valid = false;
+  ctx->overflow_recovered = true;
+  drop_graphs(ctx);
+  return fail(ctx, G6_ERR_CAPACITY,
+              "neighbour-list row overflow: the state is back at the start of the run and the row capacity was "
+              "raised; repeat the run");
 }
 
 static int md_finish(g6_ctx* ctx, int nsteps, g6_thermostat* thermo, double* log) {
@@ -1391,6 +1418,8 @@ int g6_md_begin(g6_ctx* ctx, double dt, int max_steps, const g6_thermostat* ther
   rc = md_prepare(ctx, dt, max_steps, const_cast<g6_thermostat*>(thermo), want_log != 0, 0);
   if (rc) return rc;
   ctx->run_dt = dt; ctx->run_log = want_log != 0; ctx->run_max = max_steps; ctx->run_done = 0; ctx->in_run = true;
+  CK(cudaMemcpyAsync(ctx->d_save, ctx->d_st, (size_t)REC * ctx->n * sizeof(double), cudaMemcpyDeviceToDevice,
+                     ctx->stream));
   return md_start(ctx, dt);
 }
 
@@ -1408,9 +1437,10 @@ int g6_md_end(g6_ctx* ctx, g6_thermostat* thermo, double* log) {
   if (!ctx || !ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_md_end without g6_md_begin");
   ctx->in_run = false;
   CK(cudaSetDevice(ctx->device));
-  int rc = md_stop(ctx);
+  int rc = md_stop(ctx, step_args(ctx, ctx->run_dt, ctx->run_log ? ctx->d_log : nullptr));
   if (rc) return rc;
   rc = md_finish(ctx, ctx->run_done, thermo, ctx->run_log ? log : nullptr);
+  if (rc == G6_ERR_CAPACITY && *pinned_runs(ctx).ovf == 1) return recover_overflow(ctx);
   if (rc) return rc;
   // every step but the last predicts the next one; the state is a corrected
   // (reference-consistent) state only after exactly max_steps steps
@@ -1665,8 +1695,12 @@ int g6_set_shape(g6_ctx* ctx, const g6_shape* shape) {
   if (!ok(shape->lpi) || !ok(shape->step_lpi) || (shape->step_mpw != 8 && shape->step_mpw != 16 && shape->step_mpw != 32))
     return fail(ctx, G6_ERR_ARG, "lanes per molecule must be 4, 8, 16 or 32 and molecules per warp 8, 16 or 32");
   if (!(shape->skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
+  if (shape->cap < 0) return fail(ctx, G6_ERR_ARG, "cap must be >= 0 (0: from the skin and density)");
   ctx->lpi = shape->lpi; ctx->step_lpi = shape->step_lpi; ctx->step_mpw = shape->step_mpw;
-  if (shape->skin != ctx->skin) { ctx->skin = shape->skin; ctx->glist.valid = false; ctx->cap = 0; }
+  if (shape->skin != ctx->skin || shape->cap != ctx->cap_request) {
+    ctx->skin = shape->skin; ctx->cap_request = shape->cap;
+    ctx->glist.valid = false; ctx->cap = 0; ctx->list_valid = false;
+  }
   drop_graphs(ctx);
   return G6_OK;
 }
@@ -1688,26 +1722,41 @@ int g6_stream(g6_ctx* ctx, void** stream) {
 
 int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double* log) {
   if (nsteps == 0 && ctx) return G6_OK;
-  int rc = g6_md_begin(ctx, dt, nsteps, thermo, log != nullptr);
-  if (rc) return rc;
-  rc = g6_md_advance(ctx, nsteps);
-  if (rc) { ctx->in_run = false; md_stop(ctx); cudaStreamSynchronize(ctx->stream); return rc; }
-  return g6_md_end(ctx, thermo, log);
+  if (!ctx) return G6_ERR_ARG;
+  // a row overflow is repeated from the run's start with a larger capacity
+  for (int attempt = 0;; ++attempt) {
+    int rc = g6_md_begin(ctx, dt, nsteps, thermo, log != nullptr);
+    if (rc) return rc;
+    rc = g6_md_advance(ctx, nsteps);
+    if (rc) {
+      ctx->in_run = false;
+      md_stop(ctx, step_args(ctx, ctx->run_dt, ctx->run_log ? ctx->d_log : nullptr));
+      cudaStreamSynchronize(ctx->stream);
+      return rc;
+    }
+    ctx->overflow_recovered = false;
+    rc = g6_md_end(ctx, thermo, log);
+    if (rc != G6_ERR_CAPACITY || !ctx->overflow_recovered || attempt == 3) return rc;
+  }
 }
 
 // Enqueue the whole host-buffer step on the context's stream (used directly,
 // or captured once into graph_host).  log_dst: host destination of the log.
-static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log) {
+// upload = false repeats a step from the state kept in d_save (row-overflow recovery).
+static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log, bool upload = true) {
   const int n = ctx->n;
   const size_t bytes = (size_t)REC * n * sizeof(double);
-  CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));
+  if (upload) {
+    CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_save, ctx->d_st, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   int rc = md_upload(ctx);
   if (rc) return rc;
   StepArgs sa = step_args(ctx, dt, want_log ? ctx->d_log : nullptr);
   if ((rc = md_start(ctx, dt))) return rc;
   if ((rc = enqueue_step(ctx, sa))) return rc;
-  if ((rc = md_stop(ctx))) return rc;
+  if ((rc = md_stop(ctx, sa))) return rc;
   CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
   CK(cudaMemcpyAsync(rec, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return md_readback(ctx, 1, want_log ? log_dst : nullptr);
@@ -1753,7 +1802,16 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   }
   CK(cudaStreamSynchronize(ctx->stream));
   if (pinned && log) std::memcpy(log, pr.log1, (size_t)ctx->nrep * G6_LOG_WIDTH * sizeof(double));
-  return md_check(ctx, 1, thermo);
+  rc = md_check(ctx, 1, thermo);
+  // a row overflow: the step again from the uploaded state with a larger capacity
+  for (int attempt = 0; rc == G6_ERR_CAPACITY && *pr.ovf == 1 && attempt < 3; ++attempt) {
+    recover_overflow(ctx);
+    if ((rc = md_fill(ctx, dt, 1, thermo, log != nullptr))) return rc;
+    if ((rc = enqueue_step_host(ctx, dt, rec, log, log != nullptr, false))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    rc = md_check(ctx, 1, thermo);
+  }
+  return rc;
 }
 
 static int replica_exchange(g6_ctx* ctx, int parity, uint64_t seed, uint64_t counter, double* beta,

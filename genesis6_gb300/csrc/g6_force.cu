@@ -1,12 +1,14 @@
 // g6_force.cu -- site-site Lennard-Jones + Coulomb under the COM switch.
 //
-// k_force<Model, Real, LPI>: the hot kernel.  LPI lanes cooperate on one
-// i-molecule and walk its neighbour-list row (full list, both directions, so
-// no scatter to j and no atomics); each lane keeps FP32 (mixed) or FP64
-// (plain) partial sums of the i-site forces, the COM-site switch force, the
-// pair energy and the 3x3 molecular virial, and the lanes are combined in FP64
-// with warp shuffles.  The epilogue is rigid_collectforce: F = sum of site
-// forces, lab torque = sum r_s x f_s.
+// k_force<Model, LPI, FUSED>: the FP64 (plain) force kernel.  LPI lanes
+// cooperate on one i-molecule and walk its neighbour-list row (full list, both
+// directions, so no scatter to j and no atomics); each lane keeps FP64 partial
+// sums of the i-site forces, the COM-site switch force, the pair energy and
+// the 3x3 molecular virial, and the lanes are combined with warp shuffles.
+// The epilogue is rigid_collectforce: F = sum of site forces, lab torque = sum
+// r_s x f_s; in the fused MD step one warp of the block then runs the FP64
+// Gear corrector for the block's molecules.  The mixed-precision kernels are
+// in g6_pairs.cu.
 //
 // The per-pair arithmetic (pair_math) is in g6_pairmath.cuh.
 #include <cuda_runtime.h>
@@ -26,20 +28,16 @@ namespace g6 {
 // threads (128, or 256 at 32 lanes) and one of its warps runs the integrator
 // with one molecule per lane.  Small blocks let several blocks share an SM, so one
 // block's integrator epilogue overlaps the site loops of the others; at least 8
-// molecules per epilogue warp keep the FP64 instruction count low.  The mixed
-// kernel is capped at 128 registers.
-template <bool MIXED, int LPI>
+// molecules per epilogue warp keep the FP64 instruction count low.
+template <int LPI>
 struct StepShape {
   static constexpr int MPB = (128 / LPI) > 8 ? (128 / LPI) : 8;
   static constexpr int THREADS = MPB * LPI;
-  static constexpr int MINB = MIXED ? 65536 / (THREADS * 128) : 1;
 };
 
-template <class M, bool MIXED, int LPI, bool FUSED>
-__global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
-                                  FUSED ? StepShape<MIXED, LPI>::MINB : 1)
-    k_force(ForceArgs a, StepArgs sa) {
-  using R = typename std::conditional<MIXED, float, double>::type;
+template <class M, int LPI, bool FUSED>
+__global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_force(ForceArgs a, StepArgs sa) {
+  using R = double;
   constexpr int NW = FUSED ? 1 : 9;
   int step = 0;
   if (a.ctrl) step = a.ctrl[1];
@@ -65,63 +63,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
     double ci[3] = {pi[0], pi[1], pi[2]};
     const int nn = a.nnb[i];
     const int* row = a.nbr + (size_t)i * a.cap;
-    if (MIXED) {
-      float wi[4 * M::NPK];
-#pragma unroll
-      for (int q = 0; q < M::NPK; ++q) {
-        float4 t = pk32[(size_t)i * M::NPK + q];
-        wi[4 * q] = t.x; wi[4 * q + 1] = t.y; wi[4 * q + 2] = t.z; wi[4 * q + 3] = t.w;
-      }
-      const uint32_t xi = __float_as_uint(wi[0]), yi = __float_as_uint(wi[1]), zi = __float_as_uint(wi[2]);
-#pragma unroll
-      for (int s = 0; s <= M::NQ; ++s)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) ri[s][k] = (R)wi[3 + 3 * s + k];
-      const float sx = a.rep.fscale[3 * r], sy = a.rep.fscale[3 * r + 1], sz = a.rep.fscale[3 * r + 2];
-      const float rout2 = a.cc.frout2;
-      const float band = 1e-3f;   // |dd32 - dd64| is below 1e-4 A^2 for boxes up to 1000 A
-      // the next neighbour's index and packed pose are loaded one iteration ahead
-      int jn = sub < nn ? row[sub] : 0;
-      float4 tn[M::NPK];
-#pragma unroll
-      for (int q = 0; q < M::NPK; ++q) tn[q] = sub < nn ? pk32[(size_t)jn * M::NPK + q] : make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int k = sub; k < nn; k += LPI) {
-        const int j = jn;
-        float wj[4 * M::NPK];
-#pragma unroll
-        for (int q = 0; q < M::NPK; ++q) {
-          const float4 t = tn[q];
-          wj[4 * q] = t.x; wj[4 * q + 1] = t.y; wj[4 * q + 2] = t.z; wj[4 * q + 3] = t.w;
-        }
-        if (k + LPI < nn) {
-          jn = row[k + LPI];
-#pragma unroll
-          for (int q = 0; q < M::NPK; ++q) tn[q] = pk32[(size_t)jn * M::NPK + q];
-        }
-        float d[3];
-        d[0] = (float)(int)(xi - __float_as_uint(wj[0])) * sx;
-        d[1] = (float)(int)(yi - __float_as_uint(wj[1])) * sy;
-        d[2] = (float)(int)(zi - __float_as_uint(wj[2])) * sz;
-        float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        bool in = dd < rout2;
-        if (fabsf(dd - rout2) < band) {
-          // borderline: decide with the reference's FP64 arithmetic
-          const double* pj = pk64 + (size_t)j * M::W64;
-          double cj[3] = {pj[0], pj[1], pj[2]}, o[3], dx[3];
-          in = exact_dd(ci, cj, Ld, iLd, o, dx) < a.cc.rout2;
-        }
-        if (!in) continue;
-        ++npin;
-        R rj[M::NQ + 1][3];
-#pragma unroll
-        for (int s = 0; s <= M::NQ; ++s)
-#pragma unroll
-          for (int q = 0; q < 3; ++q) rj[s][q] = (R)wj[3 + 3 * s + q];
-        R dr[3] = {(R)d[0], (R)d[1], (R)d[2]};
-        pair_math<M, R, NW>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.frin2, (R)a.cc.frin, (R)a.cc.frout, (R)a.cc.fc1,
-                        (R)a.cc.fc2, (R)a.pc.frl, (R)a.pc.fru, (R)a.pc.fw3, acc);
-      }
-    } else {
+    {
 #pragma unroll
       for (int s = 0; s <= M::NQ; ++s)
 #pragma unroll
@@ -184,57 +126,9 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
       for (int k = 0; k < 9; ++k) a.wmol[k * n + i] = 0.5 * v[7 + k];
       if (a.npair_in) a.npair_in[i] = np_tot;
     }
-  } else if constexpr (MIXED) {
-    // fused mixed step: error-free float-pair combine of the lanes, then warp 0
-    // runs the integrator for the block's MPB molecules (one per lane)
-    constexpr int MPB = StepShape<MIXED, LPI>::MPB;
-    const bool predict_next = step + 1 < sa.ctrl[2];
-    FF q8[8];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { q8[k] = FF{fo[k], 0.0f}; q8[3 + k] = FF{to[k], 0.0f}; }
-    q8[6] = FF{acc.e, 0.0f};
-    q8[7] = FF{acc.w[0], 0.0f};
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-#pragma unroll
-      for (int m = LPI / 2; m >= 1; m >>= 1) q8[k] = ff_add(q8[k], red_shfl(q8[k], m));
-    __shared__ FF smf[MPB][8];
-    __shared__ int smn[MPB];
-    if (sub == 0) {
-      const int m = threadIdx.x / LPI;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) smf[m][k] = q8[k];
-      smn[m] = np_tot;
-    }
-    __syncthreads();
-    FF vv[NRED];
-#pragma unroll
-    for (int k = 0; k < NRED; ++k) vv[k] = FF{0.0f, 0.0f};
-    float dmax2 = 0.0f;
-    int bad = 0, rr = -1;
-    // the integrator warp rotates with the block so that the blocks resident on an
-    // SM spread their FP64 work over its four schedulers
-    const int ew = blockIdx.x % (StepShape<MIXED, LPI>::THREADS / 32);
-    if ((int)(threadIdx.x >> 5) == ew && (threadIdx.x & 31) < MPB) {
-      const int m = threadIdx.x & 31;
-      const int im = blockIdx.x * MPB + m;
-      if (im < n) {
-        rr = a.rep.mol_rep[im];
-        const float F[3] = {smf[m][0].hi + smf[m][0].lo, smf[m][1].hi + smf[m][1].lo, smf[m][2].hi + smf[m][2].lo};
-        const float tl[3] = {smf[m][3].hi + smf[m][3].lo, smf[m][4].hi + smf[m][4].lo, smf[m][5].hi + smf[m][5].lo};
-        float ekt2, ekr2;
-        correct_mixed<M::NQ>(sa, im, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
-        vv[0] = FF{0.5f * smf[m][6].hi, 0.5f * smf[m][6].lo};
-        vv[1] = FF{0.5f * smf[m][7].hi, 0.5f * smf[m][7].lo};
-        vv[2] = FF{ekt2, 0.0f};
-        vv[3] = FF{ekr2, 0.0f};
-        vv[4] = FF{0.5f * (float)smn[m], 0.0f};
-      }
-    }
-    step_reduce<FF>(sa, vv, rr, dmax2, bad, MPB, step, ew);
   } else {
     // fused FP64 step: FP64 lane combine, FP64 integrator in warp 0
-    constexpr int MPB = StepShape<MIXED, LPI>::MPB;
+    constexpr int MPB = StepShape<LPI>::MPB;
     const bool predict_next = step + 1 < sa.ctrl[2];
     double v8[8];
 #pragma unroll
@@ -256,7 +150,7 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
     int bad = 0, rr = -1;
     // the integrator warp rotates with the block so that the blocks resident on an
     // SM spread their FP64 work over its four schedulers
-    const int ew = blockIdx.x % (StepShape<MIXED, LPI>::THREADS / 32);
+    const int ew = blockIdx.x % (StepShape<LPI>::THREADS / 32);
     if ((int)(threadIdx.x >> 5) == ew && (threadIdx.x & 31) < MPB) {
       const int m = threadIdx.x & 31;
       const int im = blockIdx.x * MPB + m;
@@ -271,38 +165,32 @@ __global__ void __launch_bounds__(FUSED ? StepShape<MIXED, LPI>::THREADS : 128,
   }
 }
 
-template <class M, bool MIXED, int LPI, bool FUSED>
+template <class M, int LPI, bool FUSED>
 static cudaError_t launch_force_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
   // force only: 128 threads; fused step: MPB molecules (MPB x LPI threads) per block
-  const int threads = FUSED ? StepShape<MIXED, LPI>::THREADS : 128;
+  const int threads = FUSED ? StepShape<LPI>::THREADS : 128;
   const long long total = (long long)a.n * LPI;
   const int blocks = (int)((total + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;
-  k_force<M, MIXED, LPI, FUSED><<<blocks, threads, 0, s>>>(a, sa);
+  k_force<M, LPI, FUSED><<<blocks, threads, 0, s>>>(a, sa);
   return cudaGetLastError();
 }
 
-template <class M, bool MIXED, bool FUSED>
+template <class M, bool FUSED>
 static cudaError_t launch_force_l(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
   switch (lpi) {
-    case 4: return launch_force_t<M, MIXED, 4, FUSED>(a, sa, s);
-    case 8: return launch_force_t<M, MIXED, 8, FUSED>(a, sa, s);
-    case 16: return launch_force_t<M, MIXED, 16, FUSED>(a, sa, s);
-    default: return launch_force_t<M, MIXED, 32, FUSED>(a, sa, s);
+    case 4: return launch_force_t<M, 4, FUSED>(a, sa, s);
+    case 8: return launch_force_t<M, 8, FUSED>(a, sa, s);
+    case 16: return launch_force_t<M, 16, FUSED>(a, sa, s);
+    default: return launch_force_t<M, 32, FUSED>(a, sa, s);
   }
 }
 
-template <class M, bool FUSED>
-static cudaError_t launch_force_m(const ForceArgs& a, const StepArgs& sa, bool mixed, int lpi, cudaStream_t s) {
-  return mixed ? launch_force_l<M, true, FUSED>(a, sa, lpi, s) : launch_force_l<M, false, FUSED>(a, sa, lpi, s);
-}
-
 template <bool FUSED>
-static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int model, bool mixed, int lpi,
-                                    cudaStream_t s) {
-  if (model_nq(model) == 3) return launch_force_m<MT<3, false>, FUSED>(a, sa, mixed, lpi, s);
-  if (a.pc.taper) return launch_force_m<MT<4, true>, FUSED>(a, sa, mixed, lpi, s);
-  return launch_force_m<MT<4, false>, FUSED>(a, sa, mixed, lpi, s);
+static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
+  if (model_nq(model) == 3) return launch_force_l<MT<3, false>, FUSED>(a, sa, lpi, s);
+  if (a.pc.taper) return launch_force_l<MT<4, true>, FUSED>(a, sa, lpi, s);
+  return launch_force_l<MT<4, false>, FUSED>(a, sa, lpi, s);
 }
 
 // Force only (outputs F, lab torque, per-molecule energy and virial); the
@@ -311,13 +199,13 @@ cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cud
   if (mixed) return launch_pairs_force(a, model, lpi, s);
   StepArgs none;
   memset(&none, 0, sizeof none);
-  return launch_force_any<false>(a, none, model, false, lpi, s);
+  return launch_force_any<false>(a, none, model, lpi, s);
 }
 
-// One fused MD step: force, then the Gear corrector, reductions and the next
-// step's predict + placement in the kernel's epilogue.
-cudaError_t launch_step(const ForceArgs& a, const StepArgs& sa, int model, bool mixed, int lpi, cudaStream_t s) {
-  return launch_force_any<true>(a, sa, model, mixed, lpi, s);
+// One fused FP64 MD step: force, then the Gear corrector, reductions and the
+// next step's predict + placement in the kernel's epilogue.
+cudaError_t launch_step_fp64(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
+  return launch_force_any<true>(a, sa, model, lpi, s);
 }
 
 int pk64_width(int model) { return model_nq(model) == 3 ? MT<3, false>::W64 : MT<4, false>::W64; }

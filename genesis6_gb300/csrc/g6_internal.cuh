@@ -500,6 +500,7 @@ cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStrea
 cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
                               cudaEvent_t between);
 int pairs_max_cap(int lpi);
+cudaError_t launch_finish_step(const StepArgs& sa, int nrep, cudaStream_t s);
 cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s);
 int pk64_width(int model);
 int pk32_width(int model);
@@ -513,7 +514,7 @@ cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
 cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s);
 cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, double dt, cudaStream_t s);
-cudaError_t launch_step(const ForceArgs& f, const StepArgs& a, int model, bool mixed, int lpi, cudaStream_t s);
+cudaError_t launch_step_fp64(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);
 cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s);

@@ -40,7 +40,7 @@ namespace g6 {
 namespace noalloc {
 
 constexpr int MAXN = G6_NOALLOC_MAX_MOL;
-constexpr int CAP = 224;          // neighbour-list row capacity
+constexpr int CAP = 224;          // neighbour-list row capacity: r_out + skin up to ~11.7 A at 1 g/cm^3 water
 constexpr int MAXCELL = 32768;    // cells of the list grid
 constexpr int W64MAX = 18;        // doubles per molecule in pk64 (5-site models)
 constexpr int NPKMAX = 5;         // float4 per molecule in pk32
@@ -168,7 +168,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   if (precision != G6_FP64 && precision != G6_MIXED) return G6_ERR_ARG;
   if (n > MAXN) return G6_ERR_CAPACITY;   // beyond the static tables
   if (n < 2 || !box || !d_com || !d_quat || !d_F || !d_tau || !d_epot) return G6_ERR_ARG;
-  if (!(r_out > 0.0) || !(r_in < r_out) || !(skin >= 0.0)) return G6_ERR_ARG;
+  if (!(r_out > 0.0) || !(r_in >= 0.0) || !(r_in < r_out) || !(skin >= 0.0)) return G6_ERR_ARG;
   for (int d = 0; d < 3; ++d)
     if (!(box[d] > 0.0) || !(r_out <= 0.5 * box[d])) return G6_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
@@ -184,7 +184,8 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
     }
     base = base_of[dev];
   }
-  // geometry of the list grid: edge >= r_out + skin, at most MAXCELL cells
+  // geometry of the list grid: edge >= (r_out + skin) / 2 (list_row visits two
+  // cells each way), at most MAXCELL cells (coarser cells stay correct)
   Setup su;
   std::memset(&su, 0, sizeof su);
   su.n = n;
@@ -194,7 +195,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   const double rlist = r_out + sk;
   for (int d = 0; d < 3; ++d) {
     su.L[d] = box[d]; su.invL[d] = 1.0 / box[d]; su.fs[d] = (float)(box[d] / 4294967296.0);
-    su.nd[d] = std::max(1, (int)(box[d] / rlist));
+    su.nd[d] = std::max(1, (int)(box[d] / (0.5 * rlist)));
   }
   while ((long long)su.nd[0] * su.nd[1] * su.nd[2] > MAXCELL) {   // coarser cells stay correct
     int d = (int)(std::max_element(su.nd, su.nd + 3) - su.nd);

@@ -9,7 +9,7 @@
 //      with |d|^2 < rc^2 (the FP32 distance of exact integer COM differences;
 //      within 1e-3 A^2 of rc^2 the reference's FP64 test decides) and append
 //      them to the molecule's row in shared memory with a ballot and a prefix
-//      count.  Four row entries per lane are in flight at a time.
+//      count.  Up to six row entries per lane are in flight at a time.
 //   2. pairs: the lanes share out the compacted row (every lane of a group has
 //      an in-range pair until the row's tail), load j's packed pose one pair
 //      ahead and run the FP32 site loop of pair_math, keeping per-lane sums of
@@ -39,7 +39,9 @@ template <int LPI>
 struct PairShape {
   static constexpr int THREADS = 128;
   static constexpr int GROUPS = 32 / LPI;   // molecules per warp
-  static constexpr int UNROLL = 4;          // row entries per lane in flight during the test
+  // row entries per lane in flight during the test (4 to 6: deeper unrolling
+  // spills the 3-charge MD variant at its 96-register budget)
+  static constexpr int UNROLL = (160 / LPI) > 6 ? 6 : ((160 / LPI) < 4 ? 4 : (160 / LPI));
 };
 template <class M, int MODE>
 struct PairMinBlocks {
@@ -55,8 +57,19 @@ __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi,
 }
 
 template <class M, int LPI, int MODE>
-__global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MODE>::value)) k_pairs(ForceArgs a) {
+__global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MODE>::value))
+    k_pairs(ForceArgs a, StepArgs sa) {
   constexpr int NW = MODE == 0 ? 9 : 1;
+  int bid = blockIdx.x;
+  if constexpr (MODE == 1) {
+    // the first nrep blocks finish the previous step's replicas (sums,
+    // thermostat, log), overlapped with the pair work of the others
+    if (bid < a.rep.nrep) {
+      finish_pending(sa, bid, 32);
+      return;
+    }
+    bid -= a.rep.nrep;
+  }
   constexpr int G = PairShape<LPI>::GROUPS;
   constexpr int U = PairShape<LPI>::UNROLL;
   constexpr int NPK = M::NPK;
@@ -68,7 +81,7 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   const float4* pk32 = odd ? a.pk32_1 : a.pk32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane / LPI, sub = lane % LPI;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / LPI;
+  const int i = (bid * blockDim.x + threadIdx.x) / LPI;
   const bool valid = i < n;
   int* srow = s_rows + (size_t)(warp * G + g) * a.cap;
 
@@ -286,8 +299,11 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
     for (int k = 0; k < NRED; ++k) vv[k] = s_vv[lane][k];
     dmax2 = s_dm[lane]; bad = s_bad[lane]; rr = s_rr[lane];
   }
-  step_reduce<FF>(sa, vv, rr, dmax2, bad, 32, step, 0);
+  step_partials<FF>(sa, vv, rr, dmax2, bad, 32, step, 0);
 }
+
+// Finish of the last step of a mixed run (one replica per block).
+__global__ void __launch_bounds__(128) k_finish_step(StepArgs sa) { finish_pending(sa, blockIdx.x, 32); }
 
 template <int LPI>
 size_t pairs_smem_bytes(int cap) {
@@ -295,35 +311,35 @@ size_t pairs_smem_bytes(int cap) {
 }
 
 template <class M, int LPI, int MODE>
-static cudaError_t launch_pairs_t(const ForceArgs& a, cudaStream_t s) {
+static cudaError_t launch_pairs_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
   const int threads = PairShape<LPI>::THREADS;
   const long long total = (long long)a.n * LPI;
-  const int blocks = (int)((total + threads - 1) / threads);
+  const int blocks = (int)((total + threads - 1) / threads) + (MODE == 1 ? a.rep.nrep : 0);
   if (blocks == 0) return cudaSuccess;
   const size_t smem = pairs_smem_bytes<LPI>(a.cap);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_pairs<M, LPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_pairs<M, LPI, MODE><<<blocks, threads, smem, s>>>(a);
+  k_pairs<M, LPI, MODE><<<blocks, threads, smem, s>>>(a, sa);
   return cudaGetLastError();
 }
 
 template <class M, int MODE>
-static cudaError_t launch_pairs_l(const ForceArgs& a, int lpi, cudaStream_t s) {
+static cudaError_t launch_pairs_l(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
   switch (lpi) {
-    case 4: return launch_pairs_t<M, 4, MODE>(a, s);
-    case 8: return launch_pairs_t<M, 8, MODE>(a, s);
-    case 16: return launch_pairs_t<M, 16, MODE>(a, s);
-    default: return launch_pairs_t<M, 32, MODE>(a, s);
+    case 4: return launch_pairs_t<M, 4, MODE>(a, sa, s);
+    case 8: return launch_pairs_t<M, 8, MODE>(a, sa, s);
+    case 16: return launch_pairs_t<M, 16, MODE>(a, sa, s);
+    default: return launch_pairs_t<M, 32, MODE>(a, sa, s);
   }
 }
 
 template <int MODE>
-static cudaError_t launch_pairs_any(const ForceArgs& a, int model, int lpi, cudaStream_t s) {
-  if (model_nq(model) == 3) return launch_pairs_l<MT<3, false>, MODE>(a, lpi, s);
-  if (a.pc.taper) return launch_pairs_l<MT<4, true>, MODE>(a, lpi, s);
-  return launch_pairs_l<MT<4, false>, MODE>(a, lpi, s);
+static cudaError_t launch_pairs_any(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
+  if (model_nq(model) == 3) return launch_pairs_l<MT<3, false>, MODE>(a, sa, lpi, s);
+  if (a.pc.taper) return launch_pairs_l<MT<4, true>, MODE>(a, sa, lpi, s);
+  return launch_pairs_l<MT<4, false>, MODE>(a, sa, lpi, s);
 }
 
 // Largest row capacity (entries) whose shared-memory rows fit one block.
@@ -339,7 +355,15 @@ int pairs_max_cap(int lpi) {
 
 // Mixed force only: F, lab torque, per-molecule energy and virial in FP64.
 cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStream_t s) {
-  return launch_pairs_any<0>(a, model, lpi, s);
+  StepArgs none;
+  memset(&none, 0, sizeof none);
+  return launch_pairs_any<0>(a, none, model, lpi, s);
+}
+
+// After the last step of a mixed run: its replica finish.
+cudaError_t launch_finish_step(const StepArgs& sa, int nrep, cudaStream_t s) {
+  k_finish_step<<<nrep, 128, 0, s>>>(sa);
+  return cudaGetLastError();
 }
 
 template <int NQ>
@@ -354,7 +378,7 @@ static void launch_integrate(const ForceArgs& a, const StepArgs& sa, int mpw, in
 // Mixed MD step: pair kernel, then the integrator kernel (mpw molecules per warp).
 cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
                               cudaEvent_t between) {
-  cudaError_t e = launch_pairs_any<1>(a, model, lpi, s);
+  cudaError_t e = launch_pairs_any<1>(a, sa, model, lpi, s);
   if (e != cudaSuccess) return e;
   if (between) {
     e = cudaEventRecordWithFlags(between, s, cudaEventRecordExternal);

@@ -601,7 +601,7 @@ __device__ __forceinline__ double red_double(double v) { return v; }
 // summed in a fixed order, T, P and the conserved quantity
 // (Mixture.F90:2251-2264, 2431-2453), Nose_Correct and the next Nose_Predict
 // (NoseModule.F90:43-87).
-__device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int step) {
+__device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int step, int rebuilt) {
   __shared__ double wsum[32][NRED];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
   const int b0 = a.p.rep.off[rr] / mpb, b1 = (a.p.rep.off[rr + 1] - 1) / mpb;
@@ -660,7 +660,7 @@ __device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int st
       double* lg = a.log + ((size_t)step * a.p.rep.nrep + rr) * G6_LOG_WIDTH;
       lg[0] = s[0]; lg[1] = ekt; lg[2] = ekr; lg[3] = temperature; lg[4] = pressure;
       lg[5] = (s[0] + ekt + ekr) * I2J + nose_ep + nose_ek;
-      lg[6] = s[4]; lg[7] = th.z[0]; lg[8] = (double)a.ctrl[0]; lg[9] = (double)step;
+      lg[6] = s[4]; lg[7] = th.z[0]; lg[8] = (double)rebuilt; lg[9] = (double)step;
     }
     if (predict_next && th.kind == G6_NOSE) {   // Nose_Predict for the next step
       th.z[0] = th.z[0] + th.z[1] + th.z[2] + th.z[3] + th.z[4];
@@ -727,7 +727,7 @@ __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float 
   for (int sl = 0; sl < s_nslots; ++sl) {
     if (!s_last[sl]) continue;
     __threadfence();
-    finish_replica(a, s_rfirst + sl, mpb, step);
+    finish_replica(a, s_rfirst + sl, mpb, step, a.ctrl[0]);
     if (threadIdx.x == 0) a.repcnt[s_rfirst + sl] = 0;
   }
   // (every block has read ctrl[1] before it arrives at the counter)
@@ -736,6 +736,62 @@ __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float 
     a.ctrl[4] = 1;
     *a.done = 0u;
   }
+}
+
+// Mixed MD step: the block partials of step_reduce without the replica finish,
+// which runs in the next kernel (finish_pending): per replica slot the sums
+// over the block's molecules (warp ew holds one per lane), the displacement
+// maximum and the error flag; the last block overall keeps the step's rebuild
+// flag for the log (ctrl[7]) and advances the step counter.
+template <class V>
+__device__ void step_partials(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step,
+                              int ew) {
+  const int n = a.p.n;
+  if ((int)(threadIdx.x >> 5) == ew) {
+    const int lane = threadIdx.x & 31;
+    const int first_i = blockIdx.x * mpb;
+    const int last_i = min(n, first_i + mpb) - 1;
+    const int rfirst = a.p.rep.mol_rep[first_i];
+    const int nslots = a.p.rep.mol_rep[last_i] - rfirst + 1;
+    for (int s = 0; s < nslots; ++s) {
+      const bool mine = (r == rfirst + s);
+#pragma unroll
+      for (int k = 0; k < NRED; ++k) {
+        V x = mine ? v[k] : red_zero(v[k]);
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) x = red_add(x, red_shfl(x, m));
+        if (lane == 0) a.part[((size_t)blockIdx.x * MAXREP_PER_BLOCK + s) * NRED + k] = red_double(x);
+      }
+    }
+    float m = dmax2;
+    int b = bad;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+      b |= __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      if (m > 0.0f) atomicMax(&a.gmax[step & 1], __float_as_uint(m));
+      if (b) atomicOr(&a.ctrl[3], 1);
+    }
+  }
+  __syncthreads();
+  // (every block has read ctrl[0] and ctrl[1] before it arrives at the counter)
+  if (threadIdx.x == 0 && atomicAdd(a.done, 1u) == gridDim.x - 1) {
+    a.ctrl[7] = a.ctrl[0];
+    a.ctrl[1] = step + 1;
+    a.ctrl[4] = 1;
+    *a.done = 0u;
+  }
+}
+
+// The deferred replica finish of the mixed MD step (block-wide, one replica
+// per block): sums, thermostat, log and the next Nose_Predict of step
+// ctrl[1]-1, from the partials its integrator kernel wrote.  Runs in the next
+// step's pair kernel, overlapped with its pair work, or after the last step.
+__device__ inline void finish_pending(const StepArgs& a, int rr, int mpb) {
+  if (!a.ctrl[4]) return;   // no step of this run has finished yet
+  finish_replica(a, rr, mpb, a.ctrl[1] - 1, a.ctrl[7]);
 }
 
 // Largest squared displacement since the last list build over the finished

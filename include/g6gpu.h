@@ -31,7 +31,7 @@ extern "C" {
 #define G6_ERR_CUDA 2       /* CUDA runtime error (message in g6_last_error)    */
 #define G6_ERR_CAPACITY 3   /* a fixed-capacity device table overflowed          */
 #define G6_ERR_NONFINITE 4  /* NaN/Inf coordinates or forces detected            */
-#define G6_ERR_TIMEOUT 5    /* a bounded device-side wait gave up                */
+/* 5 is unused: no kernel of this library waits on a flag or a peer */
 #define G6_ERR_STATE 6      /* call order violated (e.g. no system defined)      */
 
 /* models: site order is the reference's, the centre of mass is the last site */
@@ -174,6 +174,13 @@ int g6_pair_potential(g6_ctx* ctx, int nsites, const double* x, const double* y,
    log (optional) receives nsteps*nrep*G6_LOG_WIDTH doubles, step-major.
    The steps run as CUDA-graph launches with no host synchronisation inside. */
 int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double* log);
+/* Row overflow: a neighbour-list row longer than the capacity would leave the
+   steps after it on truncated rows.  g6_md_run and g6_md_step_host then put
+   the state back to where the run started, raise the capacity by half and
+   repeat the run (up to three times); g6_md_end returns G6_ERR_CAPACITY with
+   the state put back and the capacity raised, so that the caller repeats the
+   run from g6_md_begin with the same thermostats (which a failed run leaves
+   untouched). */
 
 /* g6_md_run split into its three phases so that a driver can interleave its
    own stream work: g6_md_begin uploads the thermostats and performs the first
@@ -215,7 +222,8 @@ typedef struct g6_shape {
   int step_lpi;    /* lanes per molecule, pair kernel of the MD step (4, 8, 16, 32)  */
   int step_mpw;    /* molecules per warp, mixed MD integrator kernel (8, 16, 32)     */
   double skin;     /* Verlet margin [A] (g6_set_skin)                                */
-  int cap;         /* neighbour-list row capacity that follows from the skin         */
+  int cap;         /* neighbour-list row capacity (entries); g6_set_shape: 0 derives it
+                      from the skin and the density (twice the expected row + 64)    */
   double step_ms;  /* g6_tune_shape: the chosen shape's MD step time in the search   */
 } g6_shape;
 #define G6_TUNE_SKIN 1
@@ -353,7 +361,10 @@ int g6_mlp_train(g6_ctx* ctx, int epochs, int batch, double lr, uint64_t seed, d
    grow the process's device footprint -- and that hold their own device
    buffers.  Same computation as g6_force (sites, cell grid, neighbour list,
    force, collect) for ONE system of at most G6_NOALLOC_MAX_MOL molecules;
-   larger n returns G6_ERR_CAPACITY.  d_com (n,3), d_quat (n,4) are device
+   larger n returns G6_ERR_CAPACITY, and so does a neighbour-list row of more
+   than 224 entries (r_out + skin above about 11.7 A in water at 1 g/cm^3).
+   0 <= r_in < r_out <= box/2 and skin >= 0 are required (G6_ERR_ARG
+   otherwise).  d_com (n,3), d_quat (n,4) are device
    inputs; d_F (n,3), d_tau (n,3, body frame) and d_epot (1) are device
    outputs; box (3) is host memory; stream is a cudaStream_t (NULL = default).
    Intermediate tables live in one static device array of 7,195,392 bytes (6.9 MiB) that

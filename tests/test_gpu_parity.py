@@ -240,3 +240,44 @@ def test_nonfinite_state_is_reported():
     with pytest.raises(g6.G6Error) as e:
         s.md_run(0.002, 3)
     assert e.value.status == g6._capi.G6_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_row_overflow_is_recovered(prec):
+    """Neighbour-list rows longer than the capacity: g6_md_run puts the state
+    back to the run's start, raises the capacity and repeats the run, so the
+    result is the trajectory of a run that never overflowed; g6_md_end on its
+    own reports G6_ERR_CAPACITY with the start state restored."""
+    from genesis6_gb300 import _capi
+    import ctypes
+    n = 512
+    b = config.water_box("TIP4P", n, 44, temp=300.0, dt=0.002, jitter=0.2)
+
+    def make(cap):
+        s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision=prec, rc=9.0)
+        s.upload_state(b["rec"])
+        sh = _capi.Shape(lpi=16, step_lpi=16, step_mpw=8, skin=1.0, cap=cap, step_ms=0.0)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+        return s
+
+    q = 300.0 * 0.25 / 0.002
+    a = make(0)
+    th_a = a.thermostats(1, "nose", temp=300.0, q=q)
+    log_a = a.md_run(0.002, 20, th_a)
+    s = make(64)                       # about 140 entries per row at rc + skin = 10 A
+    th_s = s.thermostats(1, "nose", temp=300.0, q=q)
+    log_s = s.md_run(0.002, 20, th_s)
+    assert np.array_equal(a.download_state(), s.download_state())
+    assert np.array_equal(log_a, log_s)
+    assert list(th_a[0].zeta) == list(th_s[0].zeta)
+    got = _capi.Shape()
+    s._check(s.L.g6_get_shape(s.ctx, ctypes.byref(got)))
+    assert got.cap > 64
+    # the three-phase API: the overflow is reported and the start state restored
+    t = make(64)
+    th_t = t.thermostats(1, "nose", temp=300.0, q=q)
+    assert t.L.g6_md_begin(t.ctx, 0.002, 5, th_t, 0) == _capi.G6_OK
+    assert t.L.g6_md_advance(t.ctx, 5) == _capi.G6_OK
+    assert t.L.g6_md_end(t.ctx, th_t, None) == _capi.G6_ERR_CAPACITY
+    assert np.array_equal(t.download_state(), b["rec"])
+    assert th_t[0].zeta[0] == 0.0
