@@ -16,8 +16,8 @@ LIB_PATH = os.path.join(HERE, "libg6gpu.so")
 
 G6_OK, G6_ERR_ARG, G6_ERR_CUDA, G6_ERR_CAPACITY, G6_ERR_NONFINITE = range(5)
 G6_ERR_STATE = 6   # (5 is unused)
-TIP4P, TIP5P, ST2, SPCE = 1, 2, 3, 4
-MODELS = {"TIP4P": TIP4P, "TIP5P": TIP5P, "ST2": ST2, "SPCE": SPCE}
+TIP4P, TIP5P, ST2, SPCE, OPLSMEOH = 1, 2, 3, 4, 5
+MODELS = {"TIP4P": TIP4P, "TIP5P": TIP5P, "ST2": ST2, "SPCE": SPCE, "OPLSMEOH": OPLSMEOH}
 PATH_STD, PATH_CUSTOM = 0, 1
 PATHS = {"std": PATH_STD, "custom": PATH_CUSTOM}
 FP64, MIXED = 0, 1
@@ -33,7 +33,8 @@ SYMBOLS = [
     "g6_version", "g6_last_error", "g6_status_string", "g6_model_info", "g6_ctx_create", "g6_ctx_destroy",
     "g6_system", "g6_set_cutoff", "g6_set_grid", "g6_set_skin", "g6_set_box", "g6_upload_state",
     "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
-    "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_md_run", "g6_md_step_host",
+    "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_pairsearch_hetero",
+    "g6_force_sites_hetero", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_exchange_plan", "g6_replica_scale", "g6_last_epot",
     "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
     "g6_time_force", "g6_tune", "g6_set_lpi", "g6_tune_shape", "g6_get_shape", "g6_set_shape", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
@@ -103,6 +104,9 @@ def lib():
     L.g6_hbonds.argtypes = [vp, i64, ip, ip, ip, ctypes.POINTER(i64)]
     L.g6_force_sites.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, i64, ip, ip, dp, dp, dp, dp, dp, dp, dp]
     L.g6_pair_potential.argtypes = [vp, ctypes.c_int, dp, dp, dp, i64, ip, ip, dp, dp, dp, dp, dp]
+    L.g6_pairsearch_hetero.argtypes = [vp, dp, ctypes.c_int, dp, ctypes.c_int, dp, ctypes.POINTER(i64)]
+    L.g6_force_sites_hetero.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp,
+                                        dp, ctypes.c_int, ctypes.c_int, i64, ip, ip, dp, dp, dp, dp, dp, dp, dp]
     L.g6_md_run.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Thermostat), dp]
     L.g6_md_step_host.argtypes = [vp, ctypes.c_double, ctypes.POINTER(Thermostat), dp, dp]
     L.g6_replica_exchange.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,

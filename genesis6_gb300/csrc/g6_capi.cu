@@ -58,13 +58,33 @@ static bool make_model_sites(int model, ModelHost& m);
 
 bool make_model(int model, ModelHost& m) {
   if (!make_model_sites(model, m)) return false;
-  if (model != G6_SPCE) reference_layout(m);
+  if (model != G6_SPCE && model != G6_OPLSMEOH) reference_layout(m);
   return true;
 }
 
 static bool make_model_sites(int model, ModelHost& m) {
   m = ModelHost();
   m.model = model;
+  if (model == G6_OPLSMEOH) {
+    // Rigid_OPLSMeOH_Constructor RigidModule.F90:391-426 (Me, O, H, COM; masses
+    // 15, 16, 1), oplsmeoh_setinteraction OPLSMeOHModule.F90:82-101.  Two LJ
+    // sites: only the site-pair-table kernels (g6_force_sites_hetero) run it.
+    const double mass[4] = {15.0, 16.0, 1.0, 0.0};
+    const double x[4] = {0.0133, -0.0634, 0.8152, 0.0}, y[4] = {0.7666, -0.6559, -1.0042, 0.0};
+    m.nref = 4;
+    for (int s = 0; s < 4; ++s) {
+      m.rbody[s][0] = x[s]; m.rbody[s][1] = y[s]; m.rbody[s][2] = 0.0;
+      m.I[0] = m.I[0] + mass[s] * (y[s] * y[s]);
+      m.I[1] = m.I[1] + mass[s] * (x[s] * x[s]);
+      m.I[2] = m.I[2] + mass[s] * (x[s] * x[s] + y[s] * y[s]);
+      m.mass = m.mass + mass[s];
+    }
+    m.rparam[0][0] = 0.265; m.rparam[0][1] = 0.207 * CA; m.rparam[0][2] = 3.775;
+    m.rparam[1][0] = -0.700; m.rparam[1][1] = 0.170 * CA; m.rparam[1][2] = 3.070;
+    m.rparam[2][0] = 0.435;
+    m.nsite = 0; m.nq = 0;   // no layout for the LJ-site + charged-site kernels
+    return true;
+  }
   if (model == G6_SPCE) {
     const double theta = 109.5 * PI / 180.0, l1 = 1.0, hmass = 1.0, omass = 16.0;
     double y[4] = {0.0, l1 * std::sin(0.5 * theta), -l1 * std::sin(0.5 * theta), 0.0};
@@ -256,6 +276,7 @@ struct g6_ctx {
   int* d_sten = nullptr; int* d_sten_off = nullptr;
   // neighbour list
   int cap = 0;
+  int ccap = 0;   // in-range entries per row held by the mixed list kernel's shared memory
   int* d_nbr = nullptr; int* d_nnb = nullptr; double* d_com_build = nullptr; int* d_overflow = nullptr;
   uint32_t* d_fix_build = nullptr;
   float* d_stf = nullptr;   // mixed precision: small Gear terms during a run
@@ -470,6 +491,12 @@ static int prepare_list(g6_ctx* ctx) {
     CK(dalloc(ctx, &ctx->d_nbr, (size_t)cap * ctx->n));
     ctx->cap = cap;
   }
+  // the in-range part of a row (rc, not rc + skin): 1.5x the expected count +
+  // 64; a row beyond it is reported as an overflow and the run repeated with
+  // the full capacity (cap_request set by the recovery)
+  const double rcut = ctx->cc.rout;
+  const int want = (int)(1.5 * 4.18879020478639 * rcut * rcut * rcut * rho + 64.0);
+  ctx->ccap = ctx->cap_request > 0 ? cap : std::min(cap, (want + 31) / 32 * 32);
   return G6_OK;
 }
 
@@ -518,6 +545,7 @@ static ForceArgs force_args(g6_ctx* c) {
   a.pk64 = c->d_pk64; a.pk32 = c->d_pk32; a.pk64_1 = c->d_pk64_1; a.pk32_1 = c->d_pk32_1; a.ctrl = nullptr;
   a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
   a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin; a.fres = c->d_fres;
+  a.ccap = c->ccap; a.overflow = c->d_overflow;
   return a;
 }
 
@@ -538,7 +566,7 @@ static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 8 : (c->n <= 245
 // (32/lpi rows per warp): widen lpi until the rows of a block fit.
 static int fit_lpi(const g6_ctx* c, int lpi) {
   if (c->prec != G6_MIXED) return lpi;
-  while (lpi < 32 && c->cap > pairs_max_cap(lpi)) lpi *= 2;
+  while (lpi < 32 && c->ccap > pairs_max_cap(lpi)) lpi *= 2;
   return lpi;
 }
 
@@ -563,7 +591,7 @@ static int force_once(g6_ctx* ctx) {
   CK(launch_predict_place(place_args(ctx), 0, ctx->d_th, 0, ctx->stream));
   rc = enqueue_rebuild(ctx, nullptr);
   if (rc) return rc;
-  if (ctx->prec == G6_MIXED && ctx->cap > pairs_max_cap(32))
+  if (ctx->prec == G6_MIXED && ctx->ccap > pairs_max_cap(32))
     return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
   ctx->lpi = fit_lpi(ctx, ctx->lpi);
   CK(launch_force(force_args(ctx), ctx->model, ctx->prec == G6_MIXED, ctx->lpi, ctx->stream));
@@ -671,6 +699,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   if (precision != G6_FP64 && precision != G6_MIXED) return fail(ctx, G6_ERR_ARG, "unknown precision");
   ModelHost mh;
   if (!make_model(model, mh)) return fail(ctx, G6_ERR_ARG, "unknown model");
+  if (mh.nsite == 0) return fail(ctx, G6_ERR_ARG, "this model runs only through the site-pair-table entry points");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
   free_all(ctx);
@@ -1135,6 +1164,119 @@ int g6_pair_potential(g6_ctx* ctx, int nsites, const double* x, const double* y,
 }
 
 // ---------------------------------------------------------------------------
+// Two components: hetero pair search and the site-pair-table force
+// ---------------------------------------------------------------------------
+int g6_pairsearch_hetero(g6_ctx* ctx, const double* box, int na, const double* com_a, int nb, const double* com_b,
+                         int64_t* npair) {
+  if (!ctx) return G6_ERR_ARG;
+  if (!ctx->have_cut) return fail(ctx, G6_ERR_STATE, "no cutoff defined (g6_set_cutoff)");
+  if (!box || na < 0 || nb < 0 || (na > 0 && !com_a) || (nb > 0 && !com_b)) return fail(ctx, G6_ERR_ARG, "bad arrays");
+  for (int d = 0; d < 3; ++d)
+    if (!(box[d] > 0.0) || !(ctx->cc.rout <= 0.5 * box[d]))
+      return fail(ctx, G6_ERR_ARG, "box edges must be positive and at least twice the cutoff");
+  CK(cudaSetDevice(ctx->device));
+  const double edge = ctx->req > 0.0 ? ctx->req : ctx->cc.rout;
+  const double req[3] = {edge, edge, edge};
+  const size_t cbytes = ((size_t)3 * na * 8 + 255) / 256 * 256 + ((size_t)3 * nb * 8 + 255) / 256 * 256;
+  const size_t sbytes = pairsearch_hetero_scratch(box, req, na, nb);
+  int rc = ensure_scratch(ctx, cbytes + sbytes);
+  if (rc) return rc;
+  double* dca = (double*)ctx->d_scratch;
+  double* dcb = dca + ((size_t)3 * na * 8 + 255) / 256 * 32;
+  char* work = (char*)ctx->d_scratch + cbytes;
+  if (na) CK(cudaMemcpyAsync(dca, com_a, (size_t)3 * na * 8, cudaMemcpyHostToDevice, ctx->stream));
+  if (nb) CK(cudaMemcpyAsync(dcb, com_b, (size_t)3 * nb * 8, cudaMemcpyHostToDevice, ctx->stream));
+  HetOutputs out;
+  std::memset(&out, 0, sizeof out);
+  long long total = 0;
+  CK(launch_pairsearch_hetero(box, req, ctx->cc, na, dca, nb, dcb, work, sbytes, &total, ctx->stream, out, false));
+  if ((size_t)total > ctx->pair_capacity) {
+    const size_t cap = (size_t)(total * 1.25) + 1024;
+    CK(dalloc(ctx, &ctx->d_pi, cap)); CK(dalloc(ctx, &ctx->d_pj, cap));
+    CK(dalloc(ctx, &ctx->d_ox, cap)); CK(dalloc(ctx, &ctx->d_oy, cap)); CK(dalloc(ctx, &ctx->d_oz, cap));
+    CK(dalloc(ctx, &ctx->d_hh, cap)); CK(dalloc(ctx, &ctx->d_dh, cap));
+    ctx->pair_capacity = cap;
+  }
+  out.pi = ctx->d_pi; out.pj = ctx->d_pj; out.ox = ctx->d_ox; out.oy = ctx->d_oy; out.oz = ctx->d_oz;
+  out.hh = ctx->d_hh; out.dh = ctx->d_dh;
+  CK(launch_pairsearch_hetero(box, req, ctx->cc, na, dca, nb, dcb, work, sbytes, &total, ctx->stream, out, true));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->npairs = total;
+  if (npair) *npair = total;
+  return G6_OK;
+}
+
+int g6_force_sites_hetero(g6_ctx* ctx, int model_i, int model_j, int path, int nsites, const double* x, const double* y,
+                          const double* z, double* fx, double* fy, double* fz, int offset_i, int offset_j,
+                          int64_t npair, const int* pair_i, const int* pair_j, const double* ox, const double* oy,
+                          const double* oz, const double* eratio, const double* fratio, double* ep, double* vrmat) {
+  if (!ctx) return G6_ERR_ARG;
+  ModelHost mi, mj;
+  if (!make_model(model_i, mi) || !make_model(model_j, mj)) return fail(ctx, G6_ERR_ARG, "unknown model");
+  if (path != G6_PATH_STD && path != G6_PATH_CUSTOM) return fail(ctx, G6_ERR_ARG, "unknown path");
+  if (nsites < 0 || npair < 0 || offset_i < 0 || offset_j < 0) return fail(ctx, G6_ERR_ARG, "negative size");
+  const bool with_force = fx != nullptr;
+  if (!x || !y || !z || (npair > 0 && (!pair_i || !pair_j || !ox || !oy || !oz || !eratio || !ep)))
+    return fail(ctx, G6_ERR_ARG, "NULL array");
+  if (with_force && (!fy || !fz || !vrmat || (npair > 0 && !fratio))) return fail(ctx, G6_ERR_ARG, "NULL array");
+  for (int64_t k = 0; k < npair; ++k)
+    if (pair_i[k] < 0 || pair_j[k] < 0 || (int64_t)offset_i + ((int64_t)pair_i[k] + 1) * mi.nref > nsites ||
+        (int64_t)offset_j + ((int64_t)pair_j[k] + 1) * mj.nref > nsites)
+      return fail(ctx, G6_ERR_ARG, "pair index outside the site store");
+  TableArgs a;
+  std::memset(&a, 0, sizeof a);
+  if (!pair_table2(mi, mj, path, a)) return fail(ctx, G6_ERR_ARG, "site-pair table too large");
+  CK(cudaSetDevice(ctx->device));
+  const size_t S = (size_t)nsites, P = (size_t)npair;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bytes = (with_force ? 6 : 3) * al(S * 8) + 2 * al(P * 4) + 6 * al(P * 8) + al(9 * 8);
+  int rc = ensure_scratch(ctx, bytes);
+  if (rc) return rc;
+  char* p = (char*)ctx->d_scratch;
+  auto take = [&](size_t b) { char* q = p; p += al(b); return (void*)q; };
+  double* dx = (double*)take(S * 8); double* dy = (double*)take(S * 8); double* dz = (double*)take(S * 8);
+  double *dfx = nullptr, *dfy = nullptr, *dfz = nullptr;
+  if (with_force) { dfx = (double*)take(S * 8); dfy = (double*)take(S * 8); dfz = (double*)take(S * 8); }
+  int* dpi = (int*)take(P * 4); int* dpj = (int*)take(P * 4);
+  double* dox = (double*)take(P * 8); double* doy = (double*)take(P * 8); double* doz = (double*)take(P * 8);
+  double* dhh = (double*)take(P * 8); double* ddh = (double*)take(P * 8); double* dep = (double*)take(P * 8);
+  double* dvir = (double*)take(9 * 8);
+  cudaStream_t s = ctx->stream;
+  CK(cudaMemcpyAsync(dx, x, S * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dy, y, S * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dz, z, S * 8, cudaMemcpyHostToDevice, s));
+  if (with_force) {
+    CK(cudaMemcpyAsync(dfx, fx, S * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dfy, fy, S * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dfz, fz, S * 8, cudaMemcpyHostToDevice, s));
+  }
+  if (P) {
+    CK(cudaMemcpyAsync(dpi, pair_i, P * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dpj, pair_j, P * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dox, ox, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(doy, oy, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(doz, oz, P * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dhh, eratio, P * 8, cudaMemcpyHostToDevice, s));
+    if (with_force) CK(cudaMemcpyAsync(ddh, fratio, P * 8, cudaMemcpyHostToDevice, s));
+  }
+  CK(cudaMemsetAsync(dvir, 0, 9 * 8, s));
+  a.nsi = mi.nref; a.nsj = mj.nref; a.offi = offset_i; a.offj = offset_j; a.npair = npair;
+  a.x = dx; a.y = dy; a.z = dz; a.fx = dfx; a.fy = dfy; a.fz = dfz; a.pi = dpi; a.pj = dpj;
+  a.ox = dox; a.oy = doy; a.oz = doz; a.hh = dhh; a.dh = ddh; a.ep = dep; a.vir = dvir;
+  a.with_force = with_force ? 1 : 0;
+  CK(launch_table_force(a, s));
+  if (P) CK(cudaMemcpyAsync(ep, dep, P * 8, cudaMemcpyDeviceToHost, s));
+  if (with_force) {
+    CK(cudaMemcpyAsync(fx, dfx, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(fy, dfy, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(fz, dfz, S * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(vrmat, dvir, 9 * 8, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  return G6_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Molecular dynamics
 // ---------------------------------------------------------------------------
 static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
@@ -1254,7 +1396,7 @@ static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bo
     if (ctx->step_lpi != 4 && ctx->step_lpi != 8 && ctx->step_lpi != 16 && ctx->step_lpi != 32)
       ctx->step_lpi = default_lpi(ctx);
   }
-  if (ctx->prec == G6_MIXED && ctx->cap > pairs_max_cap(32))
+  if (ctx->prec == G6_MIXED && ctx->ccap > pairs_max_cap(32))
     return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
   ctx->lpi = fit_lpi(ctx, ctx->lpi);
   ctx->step_lpi = fit_lpi(ctx, ctx->step_lpi);

@@ -212,6 +212,8 @@ struct ForceArgs {
   double* wmol;   // 9 SoA
   int* npair_in;  // per molecule: pairs within rc (diagnostic, optional; required by the mixed MD step)
   float4* fres;   // mixed MD step: per molecule 4 float4 of float pairs (F, energy; lab torque, virial trace)
+  int ccap;       // mixed list kernel: in-range entries per molecule its shared-memory rows hold (<= cap)
+  int* overflow;  // set to 1 when a row holds more in-range entries than ccap
 };
 
 struct SitesArgs {
@@ -469,6 +471,35 @@ struct HbArgs {
   int *from, *which, *to;         // per bond: donor, its hydrogen (1, 2), acceptor
 };
 cudaError_t launch_hbonds(const HbArgs& a, cudaStream_t s);
+
+// Two-component pair lists and the site-pair-table force (g6_mixture.cu).
+constexpr int TMAXS = 6;                     // sites per molecule (COM included)
+constexpr int TMAX = (TMAXS - 1) * (TMAXS - 1);
+struct TableArgs {
+  int nsi, nsj, offi, offj, ntab;
+  int si[TMAX], sj[TMAX];
+  double qq[TMAX], aa[TMAX], bb[TMAX];
+  int kind[TMAX];                            // bit 0: Coulomb, bit 1: LJ
+  long long npair;
+  const double *x, *y, *z;
+  double *fx, *fy, *fz;
+  const int *pi, *pj;
+  const double *ox, *oy, *oz, *hh, *dh;
+  double* ep;
+  double* vir;
+  int with_force;
+};
+struct HetOutputs {
+  int *pi, *pj;
+  double *ox, *oy, *oz, *hh, *dh;
+};
+struct ModelHost;
+bool pair_table2(const ModelHost& mi, const ModelHost& mj, int path, TableArgs& t);
+cudaError_t launch_table_force(const TableArgs& a, cudaStream_t s);
+cudaError_t launch_pairsearch_hetero(const double L[3], const double req[3], const CutConst& cc, int na,
+                                     const double* ca, int nb, const double* cb, char* scratch, size_t scratch_bytes,
+                                     long long* total, cudaStream_t s, HetOutputs& out, bool write);
+size_t pairsearch_hetero_scratch(const double L[3], const double req[3], int na, int nb);
 cudaError_t launch_site_positions(const SitePosArgs& a, cudaStream_t s);
 cudaError_t launch_rdf(const RdfArgs& a, int num_sms, cudaStream_t s);
 size_t rdf_smem_bytes(int nrep, int nsite, int nbin);

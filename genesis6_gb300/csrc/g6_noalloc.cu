@@ -238,6 +238,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   make_cut_const(r_in, r_out, fa.cc);
   fa.F = (double*)(base + O_F); fa.tl = (double*)(base + O_TL); fa.emol = (double*)(base + O_EMOL);
   fa.wmol = (double*)(base + O_WMOL); fa.npair_in = (int*)(base + O_NPIN);
+  fa.ccap = CAP; fa.overflow = la.overflow;
 
   const int blocks = (n + 255) / 256;
   k_setup<<<blocks, 256, 0, s>>>(su, base);

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   const int g = lane / LPI, sub = lane % LPI;
   const int i = (bid * blockDim.x + threadIdx.x) / LPI;
   const bool valid = i < n;
-  int* srow = s_rows + (size_t)(warp * G + g) * a.cap;
+  int* srow = s_rows + (size_t)(warp * G + g) * a.ccap;
 
   // pose of i: fixed-point COM and float site offsets
   float ri[M::NQ + 1][3];
@@ -149,9 +149,16 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
       }
       const unsigned bal = __ballot_sync(0xffffffffu, in);
       const unsigned mine = LPI == 32 ? bal : (bal >> (g * LPI)) & ((1u << LPI) - 1u);
-      if (in) srow[cnt + __popc(mine & ((1u << sub) - 1u))] = jj[u];
+      if (in) {
+        const int pos = cnt + __popc(mine & ((1u << sub) - 1u));
+        if (pos < a.ccap) srow[pos] = jj[u];
+      }
       cnt += __popc(mine);
     }
+  }
+  if (cnt > a.ccap) {   // more in-range pairs than the shared row holds: reported, the run is repeated
+    if (sub == 0) atomicExch(a.overflow, 1);
+    cnt = a.ccap;
   }
   __syncwarp();
 
@@ -316,7 +323,7 @@ static cudaError_t launch_pairs_t(const ForceArgs& a, const StepArgs& sa, cudaSt
   const long long total = (long long)a.n * LPI;
   const int blocks = (int)((total + threads - 1) / threads) + (MODE == 1 ? a.rep.nrep : 0);
   if (blocks == 0) return cudaSuccess;
-  const size_t smem = pairs_smem_bytes<LPI>(a.cap);
+  const size_t smem = pairs_smem_bytes<LPI>(a.ccap);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_pairs<M, LPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -39,6 +39,8 @@ extern "C" {
 #define G6_TIP5P 2 /* O, H, H, L, L, COM   TIP5PModule.F90:57-83, RigidModule.F90:429-477 */
 #define G6_ST2 3   /* O, H, H, M, M, COM   ST2Module.F90:10-100                */
 #define G6_SPCE 4  /* O, H, H, COM         SPCEModule.F90:8-71 (StdForce path only) */
+#define G6_OPLSMEOH 5 /* Me, O, H, COM   OPLSMeOHModule.F90:40-101, RigidModule.F90:391-426
+                         (site-pair-table entry points only: g6_force_sites_hetero) */
 
 /* force path, the reference's `custom` flag (@FAST) of Interaction2.F90:19-68 */
 #define G6_PATH_STD 0    /* StdForce / StdPairPotential (LB mixing, no ST2 taper)   */
@@ -166,6 +168,32 @@ int g6_force_sites(g6_ctx* ctx, int nsites, const double* x, const double* y, co
 int g6_pair_potential(g6_ctx* ctx, int nsites, const double* x, const double* y, const double* z, int64_t npair,
                       const int* pair_i, const int* pair_j, const double* ox, const double* oy, const double* oz,
                       const double* eratio, double* ep);
+
+/* Two components in one box, the reference's mixture path.
+   g6_pairsearch_hetero: Grid_Update + Address_Assign of both components +
+   Grid_NeighborList over the hetero stencil (NeighborCell_ListHetero,
+   GridModule.F90:757-899: the 27 neighbouring cells, clipped to the grid) +
+   Interaction_Compress2 + CutOff_Dimmer2 (InteractionModule.F90:398;
+   CutoffModule.F90:220): the exact pair set (i in A, j in B) with the
+   reference's FP64 arithmetic, for com_a (na,3) and com_b (nb,3) in the box
+   box[3]; cutoff and requested cell edge from g6_set_cutoff / g6_set_grid (no
+   g6_system needed).  g6_get_pairs returns the list.
+   g6_force_sites_hetero: force(iv, mi, mj, site, ep, vrmat, custom, si, sj),
+   Interaction2.F90:19-68, for components of models model_i and model_j on one
+   global site store (site arrays of nsites entries; molecule m of component i
+   at sites offset_i + m*nsite_i + s, the reference's mi%offset; the COM is the
+   last site of each model): the TIP4P-OPLS methanol hand kernel
+   (interaction_force_tip4p_oplsmeoh, OPLSMeOHModule.F90:1201-1480) on the
+   custom path, StdForce (StdInteraction.F90:63-630) otherwise, FP64.  Site
+   forces are ACCUMULATED into fx/fy/fz; ep[npair] and vrmat[9] are outputs.
+   fx == NULL gives the energies only (PairPotential, Interaction2.F90:71-121;
+   fratio and vrmat may then be NULL). */
+int g6_pairsearch_hetero(g6_ctx* ctx, const double* box, int na, const double* com_a, int nb, const double* com_b,
+                         int64_t* npair);
+int g6_force_sites_hetero(g6_ctx* ctx, int model_i, int model_j, int path, int nsites, const double* x, const double* y,
+                          const double* z, double* fx, double* fy, double* fz, int offset_i, int offset_j,
+                          int64_t npair, const int* pair_i, const int* pair_j, const double* ox, const double* oy,
+                          const double* oz, const double* eratio, const double* fratio, double* ep, double* vrmat);
 
 /* Molecular dynamics on the device-resident state: per step rigid_predict,
    Nose_Predict, site placement, pair search, force, rigid_collectforce,

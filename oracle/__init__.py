@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "g6_oracle.cpp")
 LIB = os.path.join(HERE, "libg6oracle.so")
 
-MODEL = {"TIP4P": 1, "TIP5P": 2, "ST2": 3, "SPCE": 4}
+MODEL = {"TIP4P": 1, "TIP5P": 2, "ST2": 3, "SPCE": 4, "OPLSMEOH": 5}
 PATH = {"std": 0, "custom": 1}
 REC = 53  # per-molecule rigid record: com[3], d[5][3], w[5][3], q[5][4]
 
@@ -75,6 +75,11 @@ def lib():
         L.orc_max_threads.restype = c_int
         L.orc_vreset2.argtypes = [c_int, c_int, c_double, c_double, dp, dp, dp]
         L.orc_replica_exchange_trial.argtypes = [c_int, c_int, ip, c_double, dp, dp, c_int, dp, dp]
+        L.orc_pairsearch_hetero.restype = c_long
+        L.orc_pairsearch_hetero.argtypes = [c_int, dp, c_int, dp, dp, dp, c_double, c_double, ip, ip, c_long, ip, ip,
+                                            dp, dp, dp, dp, dp]
+        L.orc_force_sites_hetero.argtypes = [c_int, c_int, c_int, dp, dp, dp, dp, dp, dp, c_int, c_int, c_long, ip,
+                                             ip, dp, dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -140,6 +145,39 @@ def pairsearch(com, L, req, rin, rc):
     s = slice(0, npair)
     return cell, dict(i=pi[s].copy(), j=pj[s].copy(), ox=ox[s].copy(), oy=oy[s].copy(), oz=oz[s].copy(),
                       hh=hh[s].copy(), dh=dh[s].copy())
+
+
+def pairsearch_hetero(com_a, com_b, L, req, rin, rc):
+    """Cell ids of both components and the exact pair set (i in A, j in B) of the hetero stencil."""
+    ca = _f64(com_a); cb = _f64(com_b)
+    na, nb = ca.shape[0], cb.shape[0]
+    cell_a = np.zeros(na, dtype=np.int32); cell_b = np.zeros(nb, dtype=np.int32)
+    cap = 1
+    while True:
+        pi = np.zeros(cap, dtype=np.int32); pj = np.zeros(cap, dtype=np.int32)
+        ox, oy, oz, hh, dh = (np.zeros(cap) for _ in range(5))
+        npair = lib().orc_pairsearch_hetero(na, ca, nb, cb, _f64(L), _f64(req), rin, rc, cell_a, cell_b, cap, pi, pj,
+                                            ox, oy, oz, hh, dh)
+        if npair <= cap:
+            break
+        cap = npair
+    s = slice(0, npair)
+    return cell_a, cell_b, dict(i=pi[s].copy(), j=pj[s].copy(), ox=ox[s].copy(), oy=oy[s].copy(), oz=oz[s].copy(),
+                                hh=hh[s].copy(), dh=dh[s].copy())
+
+
+def force_sites_hetero(model_i, model_j, path, x, y, z, offi, offj, pairs):
+    """force(iv, mi, mj, site, ...) for two components on one global site store."""
+    x = _f64(x); y = _f64(y); z = _f64(z)
+    nt = x.shape[0]
+    fx = np.zeros(nt); fy = np.zeros(nt); fz = np.zeros(nt)
+    np_ = len(pairs["i"])
+    ep = np.zeros(max(np_, 1)); vr = np.zeros(9)
+    pi = np.ascontiguousarray(pairs["i"], dtype=np.int32); pj = np.ascontiguousarray(pairs["j"], dtype=np.int32)
+    lib().orc_force_sites_hetero(MODEL[model_i], MODEL[model_j], PATH[path], x, y, z, fx, fy, fz, int(offi),
+                                 int(offj), np_, pi, pj, _f64(pairs["ox"]), _f64(pairs["oy"]), _f64(pairs["oz"]),
+                                 _f64(pairs["hh"]), _f64(pairs["dh"]), ep, vr)
+    return fx, fy, fz, ep[:np_], vr.reshape(3, 3)
 
 
 def force_sites(model, path, x, y, z, pairs, fx=None, fy=None, fz=None):

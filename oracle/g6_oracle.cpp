@@ -82,7 +82,7 @@ inline double dnint(double x) { return std::round(x); }
 // ---------------------------------------------------------------------------
 // Models
 // ---------------------------------------------------------------------------
-enum { M_TIP4P = 1, M_TIP5P = 2, M_ST2 = 3, M_SPCE = 4 };
+enum { M_TIP4P = 1, M_TIP5P = 2, M_ST2 = 3, M_SPCE = 4, M_OPLSMEOH = 5 };
 enum { P_STD = 0, P_CUSTOM = 1 };
 const int MAXS = 8;
 
@@ -168,12 +168,33 @@ void model_spce(Model& m) {
   m.eps[0] = 78.208 / J2K * 1e-3; m.sig[0] = 3.166;
 }
 
+// OPLS methanol: Rigid_OPLSMeOH_Constructor RigidModule.F90:391-426 (Me, O,
+// H, COM; masses 15, 16, 1), oplsmeoh_setinteraction OPLSMeOHModule.F90:82-101
+// (charges :44-46, LJ of Me and O :53-56, J. Chem. Phys. 105, 11199 (1996)).
+void model_oplsmeoh(Model& m) {
+  m.id = M_OPLSMEOH; m.nsite = 4;
+  const double mass[4] = {15.0, 16.0, 1.0, 0.0};
+  const double x[4] = {0.0133, -0.0634, 0.8152, 0.0}, y[4] = {0.7666, -0.6559, -1.0042, 0.0};
+  for (int s = 0; s < 4; ++s) { m.molx[s] = x[s]; m.moly[s] = y[s]; m.molz[s] = 0.0; }
+  m.Ixx = m.Iyy = m.Izz = m.mass = 0.0;
+  for (int s = 0; s < 4; ++s) {
+    m.Ixx = m.Ixx + mass[s] * (m.moly[s] * m.moly[s] + m.molz[s] * m.molz[s]);
+    m.Iyy = m.Iyy + mass[s] * (m.molz[s] * m.molz[s] + m.molx[s] * m.molx[s]);
+    m.Izz = m.Izz + mass[s] * (m.molx[s] * m.molx[s] + m.moly[s] * m.moly[s]);
+    m.mass = m.mass + mass[s];
+  }
+  m.q[0] = 0.265; m.q[1] = -0.700; m.q[2] = 0.435;
+  m.eps[0] = 0.207 * CA; m.sig[0] = 3.775;
+  m.eps[1] = 0.170 * CA; m.sig[1] = 3.070;
+}
+
 bool make_model(int id, Model& m) {
   m = Model();
   if (id == M_TIP4P) model_tip4p(m);
   else if (id == M_TIP5P) model_tip5p(m);
   else if (id == M_ST2) model_st2(m);
   else if (id == M_SPCE) model_spce(m);
+  else if (id == M_OPLSMEOH) model_oplsmeoh(m);
   else return false;
   return true;
 }
@@ -375,6 +396,63 @@ void pairsearch(int n, const double* com, const double L[3], const double req[3]
   }
 }
 
+// NeighborCell_ListHetero GridModule.F90:757-899 (maxradius == 0, the adaptive
+// grid): every offset of -1..1 per axis, clipped to (ndiv-1)/2 and -ndiv/2,
+// as a cell offset in [0, ndiv).  No mirror marks: the two components' pairs
+// are ordered, so all cells of the stencil are visited.
+std::vector<int> neighborcell_listhetero(const Grid& g) {
+  int nmax[3], nmin[3];
+  for (int d = 0; d < 3; ++d) {
+    nmax[d] = 1; nmin[d] = -1;
+    if (nmax[d] > (g.nd[d] - 1) / 2) nmax[d] = (g.nd[d] - 1) / 2;
+    if (nmin[d] < -(g.nd[d] / 2)) nmin[d] = -(g.nd[d] / 2);
+  }
+  std::vector<int> st;
+  for (int jz = nmin[2]; jz <= nmax[2]; ++jz)
+    for (int jy = nmin[1]; jy <= nmax[1]; ++jy)
+      for (int jx = nmin[0]; jx <= nmax[0]; ++jx) {
+        st.push_back(jx < 0 ? jx + g.nd[0] : jx);
+        st.push_back(jy < 0 ? jy + g.nd[1] : jy);
+        st.push_back(jz < 0 ? jz + g.nd[2] : jz);
+      }
+  return st;
+}
+
+// Grid_NeighborList(g, g%hetero, iv, ai, aj) + Interaction_Compress2 for two
+// components in one box (GridModule.F90:557-752; the same grid, one address
+// table per component, InteractionModule.F90:398-470): for every cell, its A
+// residents against the B residents of each stencil cell, strict cutoff test.
+// Pairs (i in A, j in B) in the reference's order: cell, i, stencil entry, j.
+void pairsearch_hetero(int na, const double* ca, int nb, const double* cb, const double L[3], const double req[3],
+                       double rc, std::vector<int>& cella, std::vector<int>& cellb, Pairs& P) {
+  double invL[3] = {1.0 / L[0], 1.0 / L[1], 1.0 / L[2]};
+  Grid g;
+  grid_update(g, L, req);
+  const std::vector<int> st = neighborcell_listhetero(g);
+  const int ng = g.nd[0] * g.nd[1] * g.nd[2], ns = (int)st.size() / 3;
+  cella.assign(na, 0); cellb.assign(nb, 0);
+  std::vector<std::vector<int>> ra(ng), rb(ng);
+  for (int i = 0; i < na; ++i) { cella[i] = cell_of(g, ca + 3 * i, L, invL); ra[cella[i]].push_back(i); }
+  for (int j = 0; j < nb; ++j) { cellb[j] = cell_of(g, cb + 3 * j, L, invL); rb[cellb[j]].push_back(j); }
+  const double rr = rc * rc;
+  P.clear();
+  for (int c = 0; c < ng; ++c) {
+    const int cx = c % g.nd[0], cy = (c / g.nd[0]) % g.nd[1], cz = c / (g.nd[0] * g.nd[1]);
+    for (int i : ra[c])
+      for (int s = 0; s < ns; ++s) {
+        const int nx = (cx + st[3 * s]) % g.nd[0], ny = (cy + st[3 * s + 1]) % g.nd[1], nz = (cz + st[3 * s + 2]) % g.nd[2];
+        for (int j : rb[(nz * g.nd[1] + ny) * g.nd[0] + nx]) {
+          double o[3];
+          if (compress_test(ca + 3 * i, cb + 3 * j, L, invL, rr, o)) {
+            P.i.push_back(i); P.j.push_back(j);
+            P.ox.push_back(o[0]); P.oy.push_back(o[1]); P.oz.push_back(o[2]);
+            P.hh.push_back(1.0); P.dh.push_back(0.0);
+          }
+        }
+      }
+  }
+}
+
 // pairsearch split over cells on nthreads host threads (CPU-baseline timing
 // only): the same candidates and test, concatenated per cell in cell order.
 void pairsearch_threaded(int n, const double* com, const double L[3], const double req[3], double rc, Grid& g,
@@ -434,10 +512,10 @@ inline void cutoff_func(double rin, double rout, double dd, double& hh, double& 
 }
 
 // CutOff_Dimmer2 CutoffModule.F90:220-278
-void cutoff_dimmer2(double rin, double rout, const double* com, Pairs& P) {
+void cutoff_dimmer2(double rin, double rout, const double* com_i, const double* com_j, Pairs& P) {
   for (size_t k = 0; k < P.i.size(); ++k) {
-    const double* a = com + 3 * P.i[k];
-    const double* b = com + 3 * P.j[k];
+    const double* a = com_i + 3 * P.i[k];
+    const double* b = com_j + 3 * P.j[k];
     double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
     dx = dx - P.ox[k]; dy = dy - P.oy[k]; dz = dz - P.oz[k];
     cutoff_func(rin, rout, dx * dx + dy * dy + dz * dz, P.hh[k], P.dh[k]);
@@ -449,20 +527,21 @@ void cutoff_dimmer2(double rin, double rout, const double* com, Pairs& P) {
 // ---------------------------------------------------------------------------
 struct SiteArrays { const double *x, *y, *z; double *fx, *fy, *fz; };
 
-// Std site-pair constants, StdInteraction.F90:201-222
+// Std site-pair constants, StdInteraction.F90:201-222 (si: sites of the
+// i-component, sj: of the j-component; LB mixing of eps and sigma)
 struct StdPairConst { int si, sj; double qq, aa, bb; bool lj, coul; };
-std::vector<StdPairConst> std_table(const Model& m, double scale) {
+std::vector<StdPairConst> std_table2(const Model& mi, const Model& mj, double scale) {
   std::vector<StdPairConst> t;
-  for (int is = 0; is < m.nsite; ++is)
-    for (int js = 0; js < m.nsite; ++js) {
+  for (int is = 0; is < mi.nsite; ++is)
+    for (int js = 0; js < mj.nsite; ++js) {
       StdPairConst c{is, js, 0, 0, 0, false, false};
-      c.qq = m.q[is] * m.q[js] * COEFF * KX2X * J2I * scale;
-      double aa = m.eps[is] * m.eps[js];
+      c.qq = mi.q[is] * mj.q[js] * COEFF * KX2X * J2I * scale;
+      double aa = mi.eps[is] * mj.eps[js];
       if (c.qq == 0.0 && aa == 0.0) continue;
       c.coul = c.qq != 0.0;
       if (aa != 0.0) {
         double ljeps = std::sqrt(aa);
-        double ljsig = pow6((m.sig[is] + m.sig[js]) * 0.5);
+        double ljsig = pow6((mi.sig[is] + mj.sig[js]) * 0.5);
         c.aa = 4.0 * ljeps * ljsig * ljsig * KX2X * J2I * scale;
         c.bb = -4.0 * ljeps * ljsig * KX2X * J2I * scale;
         c.lj = true;
@@ -471,18 +550,47 @@ std::vector<StdPairConst> std_table(const Model& m, double scale) {
     }
   return t;
 }
+std::vector<StdPairConst> std_table(const Model& m, double scale) { return std_table2(m, m, scale); }
 
-// StdForce StdInteraction.F90:63-630.  Accumulation orders follow the
-// reference: per pair and site, j-sites in ascending order for the i buffer
-// and i-sites in ascending order for the j buffer; the scatter adds every
-// i-side contribution before every j-side one (TEST22 branch :566-581).
-void std_force(const Model& m, const SiteArrays& S, const Pairs& P, double* ep, double vrmat[9], double scale) {
-  const int ns = m.nsite;
+// Constants of the hand kernel interaction_force_tip4p_oplsmeoh
+// (OPLSMeOHModule.F90:1-7, 1189-1198, 1201-1480): water O with methyl and
+// methanol O by LB mixing of EPSWO/SIGWO (TIP4PConst.F90:17-18), the TIP4P
+// charges M, H with Me, O, H.  i: TIP4P sites (O, M, H, H, COM), j: OPLS-MeOH
+// sites (Me, O, H, COM).
+std::vector<StdPairConst> tip4p_meoh_table() {
+  const double EPSM = 0.207 * CA, SIGM = 3.775, EPSO = 0.170 * CA, SIGO = 3.070;
+  const double QM = 0.265, QO = -0.700, QH = 0.435;
+  auto p12 = [](double x) { return pow12(x); };
+  const double AAOMXS = p12((T4_SIGWO + SIGM) * 0.5) * 100.0, BBOMXS = pow6((T4_SIGWO + SIGM) * 0.5) * 100.0;
+  const double AAOOXS = p12((T4_SIGWO + SIGO) * 0.5) * 100.0, BBOOXS = pow6((T4_SIGWO + SIGO) * 0.5) * 100.0;
+  std::vector<StdPairConst> t;
+  t.push_back({0, 0, 0.0, 4.0 * std::sqrt(T4_EPSWO * EPSM) * AAOMXS, -4.0 * std::sqrt(T4_EPSWO * EPSM) * BBOMXS, true, false});
+  t.push_back({0, 1, 0.0, 4.0 * std::sqrt(T4_EPSWO * EPSO) * AAOOXS, -4.0 * std::sqrt(T4_EPSWO * EPSO) * BBOOXS, true, false});
+  const double qw[4] = {0.0, T4_WM, T4_WH, T4_WH}, qm[3] = {QM, QO, QH};
+  for (int a = 1; a <= 3; ++a)
+    for (int b = 0; b < 3; ++b) t.push_back({a, b, qw[a] * qm[b] * COEFF * 100.0, 0.0, 0.0, false, true});
+  return t;
+}
+
+// The site-pair table of force() for components mi, mj (Interaction2.F90:19-68):
+// the TIP4P-OPLSMeOH hand kernel on the custom path, StdForce otherwise.
+std::vector<StdPairConst> pair_table2(const Model& mi, const Model& mj, int path) {
+  if (path == P_CUSTOM && mi.id == M_TIP4P && mj.id == M_OPLSMEOH) return tip4p_meoh_table();
+  return std_table2(mi, mj, 1.0);
+}
+
+// StdForce StdInteraction.F90:63-630 on a site-pair table, for molecules of
+// nsi sites (component at site offset offi) against molecules of nsj sites
+// (offset offj); the COM is the last site of each.  Accumulation orders follow
+// the reference: per pair and site, j-sites in ascending order for the i
+// buffer and i-sites in ascending order for the j buffer; the scatter adds
+// every i-side contribution before every j-side one (TEST22 branch :566-581).
+void table_force(int nsi, int nsj, const std::vector<StdPairConst>& tab, const SiteArrays& S, int offi, int offj,
+                 const Pairs& P, double* ep, double vrmat[9]) {
   const size_t np = P.i.size();
-  auto tab = std_table(m, scale);
-  std::vector<double> fi(np * ns * 3, 0.0), fj(np * ns * 3, 0.0);
+  std::vector<double> fi(np * nsi * 3, 0.0), fj(np * nsj * 3, 0.0);
   for (size_t k = 0; k < np; ++k) {
-    int ii = P.i[k] * ns, jj = P.j[k] * ns;
+    int ii = offi + P.i[k] * nsi, jj = offj + P.j[k] * nsj;
     double e = 0;
     for (const auto& c : tab) {
       double dx = S.x[ii + c.si] - S.x[jj + c.sj];
@@ -506,53 +614,59 @@ void std_force(const Model& m, const SiteArrays& S, const Pairs& P, double* ep, 
         f0 = dd * (c.aa * 12.0 * d12 + c.bb * 6.0 * d6);
       }
       double fxv = dx * f0, fyv = dy * f0, fzv = dz * f0;
-      double* a = &fi[(k * ns + c.si) * 3];
-      double* b = &fj[(k * ns + c.sj) * 3];
+      double* a = &fi[(k * nsi + c.si) * 3];
+      double* b = &fj[(k * nsj + c.sj) * 3];
       a[0] += fxv; a[1] += fyv; a[2] += fzv;
       b[0] += fxv; b[1] += fyv; b[2] += fzv;
       e += e0;
     }
     ep[k] = e;
   }
-  const int last = ns - 1;
+  const int lasti = nsi - 1, lastj = nsj - 1;
   for (size_t k = 0; k < np; ++k) {
     double hh = P.hh[k];
-    for (int l = 0; l < ns; ++l)
-      for (int c = 0; c < 3; ++c) { fi[(k * ns + l) * 3 + c] *= hh; fj[(k * ns + l) * 3 + c] *= hh; }
-    int ii = P.i[k] * ns, jj = P.j[k] * ns;
-    double dx00 = S.x[ii + last] - S.x[jj + last] - P.ox[k];
-    double dy00 = S.y[ii + last] - S.y[jj + last] - P.oy[k];
-    double dz00 = S.z[ii + last] - S.z[jj + last] - P.oz[k];
+    for (int l = 0; l < nsi; ++l)
+      for (int c = 0; c < 3; ++c) fi[(k * nsi + l) * 3 + c] *= hh;
+    for (int l = 0; l < nsj; ++l)
+      for (int c = 0; c < 3; ++c) fj[(k * nsj + l) * 3 + c] *= hh;
+    int ii = offi + P.i[k] * nsi, jj = offj + P.j[k] * nsj;
+    double dx00 = S.x[ii + lasti] - S.x[jj + lastj] - P.ox[k];
+    double dy00 = S.y[ii + lasti] - S.y[jj + lastj] - P.oy[k];
+    double dz00 = S.z[ii + lasti] - S.z[jj + lastj] - P.oz[k];
     double dh = P.dh[k];
     double dhx = dh * dx00 * ep[k], dhy = dh * dy00 * ep[k], dhz = dh * dz00 * ep[k];
-    double* a = &fi[(k * ns + last) * 3];
-    double* b = &fj[(k * ns + last) * 3];
+    double* a = &fi[(k * nsi + lasti) * 3];
+    double* b = &fj[(k * nsj + lastj) * 3];
     a[0] += dhx; a[1] += dhy; a[2] += dhz;
     b[0] += dhx; b[1] += dhy; b[2] += dhz;
   }
-  for (int l = 0; l < ns; ++l)
+  for (int l = 0; l < nsi; ++l)
     for (size_t k = 0; k < np; ++k) {
-      int ii = P.i[k] * ns + l;
-      S.fx[ii] += fi[(k * ns + l) * 3]; S.fy[ii] += fi[(k * ns + l) * 3 + 1]; S.fz[ii] += fi[(k * ns + l) * 3 + 2];
+      int ii = offi + P.i[k] * nsi + l;
+      S.fx[ii] += fi[(k * nsi + l) * 3]; S.fy[ii] += fi[(k * nsi + l) * 3 + 1]; S.fz[ii] += fi[(k * nsi + l) * 3 + 2];
     }
-  for (int l = 0; l < ns; ++l)
+  for (int l = 0; l < nsj; ++l)
     for (size_t k = 0; k < np; ++k) {
-      int jj = P.j[k] * ns + l;
-      S.fx[jj] -= fj[(k * ns + l) * 3]; S.fy[jj] -= fj[(k * ns + l) * 3 + 1]; S.fz[jj] -= fj[(k * ns + l) * 3 + 2];
+      int jj = offj + P.j[k] * nsj + l;
+      S.fx[jj] -= fj[(k * nsj + l) * 3]; S.fy[jj] -= fj[(k * nsj + l) * 3 + 1]; S.fz[jj] -= fj[(k * nsj + l) * 3 + 2];
     }
   for (size_t k = 0; k < np; ++k) ep[k] = ep[k] * P.hh[k];
   for (int c = 0; c < 9; ++c) vrmat[c] = 0;
   for (size_t k = 0; k < np; ++k) {
-    int ii = P.i[k] * ns, jj = P.j[k] * ns;
-    double d00[3] = {S.x[ii + last] - S.x[jj + last] - P.ox[k], S.y[ii + last] - S.y[jj + last] - P.oy[k],
-                     S.z[ii + last] - S.z[jj + last] - P.oz[k]};
+    int ii = offi + P.i[k] * nsi, jj = offj + P.j[k] * nsj;
+    double d00[3] = {S.x[ii + lasti] - S.x[jj + lastj] - P.ox[k], S.y[ii + lasti] - S.y[jj + lastj] - P.oy[k],
+                     S.z[ii + lasti] - S.z[jj + lastj] - P.oz[k]};
     double vr[3] = {0, 0, 0};
-    for (int l = 0; l < ns; ++l)
-      for (int c = 0; c < 3; ++c) vr[c] += fi[(k * ns + l) * 3 + c];
+    for (int l = 0; l < nsi; ++l)
+      for (int c = 0; c < 3; ++c) vr[c] += fi[(k * nsi + l) * 3 + c];
     // vrmat(a,b) += d00(a) * vr(b); stored row-major [a][b]
     for (int a = 0; a < 3; ++a)
       for (int b = 0; b < 3; ++b) vrmat[3 * a + b] += d00[a] * vr[b];
   }
+}
+
+void std_force(const Model& m, const SiteArrays& S, const Pairs& P, double* ep, double vrmat[9], double scale) {
+  table_force(m.nsite, m.nsite, std_table(m, scale), S, 0, 0, P, ep, vrmat);
 }
 
 // StdPairPotential StdInteraction.F90:633-762
@@ -958,7 +1072,7 @@ void full_force(const Model& m, int path, int n, const double* com, const double
   std::vector<int> cells;
   Pairs P;
   pairsearch(n, com, L, req, rc, g, cells, P);
-  cutoff_dimmer2(rin, rc, com, P);
+  cutoff_dimmer2(rin, rc, com, com, P);
   std::vector<double> fx(n * ns, 0.0), fy(n * ns, 0.0), fz(n * ns, 0.0), ep(P.i.size());
   SiteArrays S{sx.data(), sy.data(), sz.data(), fx.data(), fy.data(), fz.data()};
   force_dispatch(m, path, S, P, ep.data(), out.vir);
@@ -1078,7 +1192,7 @@ long orc_pairsearch(int n, const double* com, const double* L, const double* req
   std::vector<int> cells;
   Pairs P;
   pairsearch(n, com, L, req, rc, g, cells, P);
-  cutoff_dimmer2(rin, rc, com, P);
+  cutoff_dimmer2(rin, rc, com, com, P);
   if (cell) for (int i = 0; i < n; ++i) cell[i] = cells[i];
   long np = (long)P.i.size();
   for (long k = 0; k < np && k < cap; ++k) {
@@ -1102,6 +1216,43 @@ int orc_force_sites(int model, int path, int nsites_total, const double* x, cons
   P.hh.assign(eratio, eratio + npair); P.dh.assign(fratio, fratio + npair);
   SiteArrays S{x, y, z, fx, fy, fz};
   force_dispatch(m, path, S, P, ep, vrmat);
+  return 0;
+}
+
+// Grid_NeighborList with the hetero stencil + Interaction_Compress2 +
+// CutOff_Dimmer2 for components A (na COMs) and B (nb COMs) in one box:
+// cell ids of both and the pairs (i in A, j in B).
+long orc_pairsearch_hetero(int na, const double* ca, int nb, const double* cb, const double* L, const double* req,
+                           double rin, double rc, int* cella, int* cellb, long cap, int* pi, int* pj, double* ox,
+                           double* oy, double* oz, double* hh, double* dh) {
+  std::vector<int> ia, ib;
+  Pairs P;
+  pairsearch_hetero(na, ca, nb, cb, L, req, rc, ia, ib, P);
+  cutoff_dimmer2(rin, rc, ca, cb, P);
+  if (cella) for (int i = 0; i < na; ++i) cella[i] = ia[i];
+  if (cellb) for (int j = 0; j < nb; ++j) cellb[j] = ib[j];
+  long np = (long)P.i.size();
+  for (long k = 0; k < np && k < cap; ++k) {
+    pi[k] = P.i[k]; pj[k] = P.j[k]; ox[k] = P.ox[k]; oy[k] = P.oy[k]; oz[k] = P.oz[k]; hh[k] = P.hh[k]; dh[k] = P.dh[k];
+  }
+  return np;
+}
+
+// The reference `force(iv, mi, mj, site, ...)` for two components (mi != mj,
+// or a model with no hand kernel): one global site store, component i at site
+// offset offi and j at offj (mi%offset, mj%offset); site forces ACCUMULATED.
+int orc_force_sites_hetero(int model_i, int model_j, int path, const double* x, const double* y, const double* z,
+                           double* fx, double* fy, double* fz, int offi, int offj, long npair, const int* pi,
+                           const int* pj, const double* ox, const double* oy, const double* oz, const double* eratio,
+                           const double* fratio, double* ep, double* vrmat) {
+  Model mi, mj;
+  if (!make_model(model_i, mi) || !make_model(model_j, mj)) return 1;
+  Pairs P;
+  P.i.assign(pi, pi + npair); P.j.assign(pj, pj + npair);
+  P.ox.assign(ox, ox + npair); P.oy.assign(oy, oy + npair); P.oz.assign(oz, oz + npair);
+  P.hh.assign(eratio, eratio + npair); P.dh.assign(fratio, fratio + npair);
+  SiteArrays S{x, y, z, fx, fy, fz};
+  table_force(mi.nsite, mj.nsite, pair_table2(mi, mj, path), S, offi, offj, P, ep, vrmat);
   return 0;
 }
 
@@ -1215,7 +1366,7 @@ double orc_molecule_energy(int model, int path, int n, const double* com, const 
       P.hh.push_back(1.0); P.dh.push_back(0.0);
     }
   }
-  cutoff_dimmer2(rin, rc, allcom.data(), P);
+  cutoff_dimmer2(rin, rc, allcom.data(), allcom.data(), P);
   std::vector<double> ep(P.i.size());
   pairpot_dispatch(m, path, sx.data(), sy.data(), sz.data(), P, ep.data());
   double e = 0;
@@ -1235,7 +1386,7 @@ long orc_compute_threaded(int model, int n, const double* com, const double* qua
   Grid g;
   Pairs P;
   pairsearch_threaded(n, com, L, req, rc, g, P, nthreads);
-  cutoff_dimmer2(rin, rc, com, P);
+  cutoff_dimmer2(rin, rc, com, com, P);
   std::vector<double> fx(n * ns, 0.0), fy(n * ns, 0.0), fz(n * ns, 0.0);
   std_force_threaded(m, sx.data(), sy.data(), sz.data(), P, fx.data(), fy.data(), fz.data(), *epot, vir, nthreads,
                      (int)(n * ns));
