@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--shape", default=None,
                    help="'md' profiling case: lanes,step_lanes,molecules_per_warp,skin instead of running the tuner "
                         "(keeps the tuner's many launches out of a profiler capture)")
-    p.add_argument("--profile", choices=["md", "mc", "mc-learned", "rdf"], default=None,
+    p.add_argument("--profile", choices=["md", "e2e", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
                         "--n TIP4P molecules (mixed, Nose 300 K, one g6_md_run after a 20-step start); 'mc' = two runs of --steps trials on "
                         "32 chains x 1,024 ST2 (fixed widths) from a short MD start; 'mc-learned' = the same "
@@ -429,31 +429,16 @@ def mc_chains(C=32, N=1024, T=260.0, rc=9.0, seed=20261203, melt_steps=5000, md_
                                   "md_T_last_quarter": float(log[3 * q:, :, 3].mean())}
 
 
-def bench_mc(torch, seed=20261203, sweeps=2000, records=1_000_000, equil_sweeps=1000, w_move=0.0, w_energy=1.0,
-             T=260.0, rc=9.0, md_steps=30000):
-    """32 chains x 1,024 ST2 (custom path, Coulomb taper), T = 260 K, rc 9 A with
-    a 2 A switch.  Chains start from MD-equilibrated liquid (melt at 400 K, then
-    MD at T), are equilibrated further by the fixed-width sampler, then the MLP
-    is trained on `records` plain-sampler moves and both samplers run `sweeps`
-    sweeps from the same state: fixed widths (0.15 A, 0.15 rad) vs the learned
-    widths.  ESS of U per GPU-second (U sampled every sweep of 1,024 trials),
-    <U> of both, and the running energies against a full recomputation."""
-    import genesis6_gb300 as g6
+def mc_compare(torch, s, rec_state, beta, seed, sweeps, records, w_move, w_energy):
+    """One learned-vs-fixed comparison from rec_state with its own draws:
+    training records from the fixed sampler, training, then `sweeps` sweeps of
+    each sampler.  Returns the two samplers' numbers and the learned widths."""
     from genesis6_gb300 import _capi
-    C, N = 32, 1024
+    C, N = s.nrep, s.nmol[0]
     NF, NREC = _capi.MLP_NFEAT, _capi.MLP_RECORD
-    t0 = time.perf_counter()
-    boxes, rec0, md = mc_chains(C, N, T, rc, seed, md_steps=md_steps)
-    t_md = time.perf_counter() - t0
-    s = g6.RigidWater("ST2", [N] * C, boxes, path="custom", precision="mixed", rc=rc, switch=2.0, skin=0.0)
-    s.upload_state(rec0)
-    beta = 1.0 / T
-    t0 = time.perf_counter()
-    eq = s.mc_run(equil_sweeps * N, seed, 0, beta, 0.15, 0.15, sample_every=N)["samples"]
-    torch.cuda.synchronize()
-    t_equil = time.perf_counter() - t0
-    rec_state = s.download_state()
+    s.upload_state(rec_state)
     ntr = records // C
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     s.mc_run(ntr, seed, 10 ** 8, beta, 0.15, 0.15, mode="collect")       # training records
     loss = np.zeros(8)
@@ -469,7 +454,11 @@ def bench_mc(torch, seed=20261203, sweeps=2000, records=1_000_000, equil_sweeps=
     feat = np.ascontiguousarray(rec[:, :NF])
     wt = np.zeros(nrec); wr = np.zeros(nrec)
     s._check(s.L.g6_mlp_widths(s.ctx, _capi.fptr(feat), nrec, _capi.dptr(wt), _capi.dptr(wr)))
-    out = {}
+    out = {"training_records": ntr * C, "training_loss_first_last": [float(loss[0]), float(loss[-1])],
+           "collect_and_train_seconds": t_train,
+           "learned_widths_on_records": {"sigma_t_mean": float(wt.mean()), "sigma_r_mean": float(wr.mean()),
+                                         "sigma_t_p10_p90": [float(np.percentile(wt, 10)), float(np.percentile(wt, 90))],
+                                         "sigma_r_p10_p90": [float(np.percentile(wr, 10)), float(np.percentile(wr, 90))]}}
     for name in ("plain", "learned"):
         s.upload_state(rec_state)
         torch.cuda.synchronize()
@@ -482,31 +471,60 @@ def bench_mc(torch, seed=20261203, sweeps=2000, records=1_000_000, equil_sweeps=
         ess = np.array([ess_geyer(samples[c]) for c in range(C)])
         u = samples.mean(1)
         var_mean = np.array([np.var(samples[c]) / max(ess[c], 1.0) for c in range(C)])
-        half = samples.shape[1] // 2
         out["fixed" if name == "plain" else name] = {
             "ess_total": float(ess.sum()), "gpu_seconds": gpu_s, "ess_per_gpu_s": float(ess.sum() / gpu_s),
             "us_per_trial": gpu_s / (sweeps * N) * 1e6,
             "mean_U_internal": float(u.mean()), "stderr_U": float(np.sqrt(var_mean.sum()) / C),
-            "mean_U_first_second_half": [float(samples[:, :half].mean()), float(samples[:, half:].mean())],
             "acceptance": float(r["accepted"].sum() / r["trials"].sum()), "sweeps": sweeps,
             "running_minus_full_energy_rel": float(np.abs(r["energy"] - ep).max() / np.abs(ep).max())}
+    f, l = out["fixed"], out["learned"]
+    out["ess_per_gpu_s_learned_over_fixed"] = l["ess_per_gpu_s"] / f["ess_per_gpu_s"]
+    out["with_collect_and_train_charged"] = (l["ess_total"] / (l["gpu_seconds"] + t_train)) / f["ess_per_gpu_s"]
+    out["ess_per_trial_learned_over_fixed"] = l["ess_total"] / f["ess_total"]
+    sig = np.hypot(l["stderr_U"], f["stderr_U"])
+    out["mean_U_difference_in_sigma"] = float(abs(l["mean_U_internal"] - f["mean_U_internal"]) / sig) if sig > 0 else None
+    return out
+
+
+def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equil_sweeps=1000, w_move=0.0,
+             w_energy=1.0, T=260.0, rc=9.0, md_steps=30000):
+    """32 chains x 1,024 ST2 (custom path, Coulomb taper), T = 260 K, rc 9 A with
+    a 2 A switch.  Chains start from MD-equilibrated liquid (melt at 400 K, then
+    MD at T) and are equilibrated further by the fixed-width sampler; then, for
+    each of `seeds` independent draw streams, the MLP is trained on `records`
+    plain-sampler moves and both samplers run `sweeps` sweeps from the same
+    state: fixed widths (0.15 A, 0.15 rad) vs the learned widths.  ESS of U per
+    GPU-second (U sampled every sweep of 1,024 trials), <U> agreement per seed,
+    and the ratio with the collect + train time charged to the learned sampler."""
+    import genesis6_gb300 as g6
+    C, N = 32, 1024
+    t0 = time.perf_counter()
+    boxes, rec0, md = mc_chains(C, N, T, rc, seed, md_steps=md_steps)
+    t_md = time.perf_counter() - t0
+    s = g6.RigidWater("ST2", [N] * C, boxes, path="custom", precision="mixed", rc=rc, switch=2.0, skin=0.0)
+    s.upload_state(rec0)
+    beta = 1.0 / T
+    t0 = time.perf_counter()
+    eq = s.mc_run(equil_sweeps * N, seed, 0, beta, 0.15, 0.15, sample_every=N)["samples"]
+    torch.cuda.synchronize()
+    t_equil = time.perf_counter() - t0
+    rec_state = s.download_state()
+    runs = [mc_compare(torch, s, rec_state, beta, seed + 17 * k, sweeps, records, w_move, w_energy)
+            for k in range(seeds)]
     s.close()
-    d = abs(out["learned"]["mean_U_internal"] - out["fixed"]["mean_U_internal"])
-    sig = np.hypot(out["learned"]["stderr_U"], out["fixed"]["stderr_U"])
+    ratios = [r["ess_per_gpu_s_learned_over_fixed"] for r in runs]
+    charged = [r["with_collect_and_train_charged"] for r in runs]
     q = max(equil_sweeps // 4, 1)
     return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": T,
             "rc_A": rc, "start": "lattice, MD melt 5,000 steps at 400 K, MD %d steps at %g K (%.1f s)" % (md_steps, T, t_md),
             "md": md, "equilibration_sweeps": equil_sweeps, "equilibration_seconds": t_equil,
             "equilibration_U_quarters": [float(eq[:, k * q:(k + 1) * q].mean()) for k in range(4)],
-            "training_records": ntr * C, "objective": {"w_move": w_move, "w_energy": w_energy},
-            "training_loss_first_last": [float(loss[0]), float(loss[-1])],
-            "collect_and_train_seconds": t_train,
-            "learned_widths_on_records": {"sigma_t_mean": float(wt.mean()), "sigma_t_p10_p90": [float(np.percentile(wt, 10)), float(np.percentile(wt, 90))],
-                                          "sigma_r_mean": float(wr.mean()), "sigma_r_p10_p90": [float(np.percentile(wr, 10)), float(np.percentile(wr, 90))]},
-            "fixed": out["fixed"], "learned": out["learned"],
-            "ess_per_gpu_s_learned_over_fixed": out["learned"]["ess_per_gpu_s"] / out["fixed"]["ess_per_gpu_s"],
-            "mean_U_difference_in_sigma": float(d / sig) if sig > 0 else None,
-            "U_unit": "10 J/mol per chain (internal)"}
+            "objective": {"w_move": w_move, "w_energy": w_energy}, "seeds": seeds, "sweeps_per_sampler": sweeps,
+            "ess_per_gpu_s_learned_over_fixed": float(np.median(ratios)),
+            "ess_per_gpu_s_learned_over_fixed_per_seed": ratios,
+            "with_collect_and_train_charged_per_seed": charged,
+            "mean_U_difference_in_sigma_per_seed": [r["mean_U_difference_in_sigma"] for r in runs],
+            "runs": runs, "U_unit": "10 J/mol per chain (internal)"}
 
 
 def bench_rdf(torch, n=N_BIG, rc=9.0, nbin=200, width=0.05, reps=5, seed=20261207):
@@ -858,6 +876,12 @@ def run_profile(args):
         for _ in range(args.steps):
             h = s.rdf_counts(200, 0.05)
         print("rdf ok: %d counts" % int(h.sum()))
+    elif args.profile == "e2e":   # --steps host-buffer steps (g6_md_step_host, pinned record) of TIP4P-4096
+        import torch
+        b = equilibrated_start()
+        s = make_system("TIP4P", N_MAIN, "mixed", b["L"], b["rec"])
+        ms, _, _ = e2e_md(torch, s, b["rec"], args.steps)
+        print("e2e ok: %.1f us per host-buffer step" % (1e3 * ms))
     elif args.profile == "md":
         if args.n == N_MAIN:
             b = equilibrated_start()

@@ -262,6 +262,7 @@ struct g6_ctx {
   double* d_st = nullptr; double* d_tmat = nullptr; double* d_pk64 = nullptr; float4* d_pk32 = nullptr;
   uint32_t* d_fix = nullptr;
   double* d_tmat1 = nullptr; double* d_pk64_1 = nullptr; float4* d_pk32_1 = nullptr; uint32_t* d_fix1 = nullptr;
+  float4* d_pkq = nullptr; float4* d_pkq_1 = nullptr;   // list-kernel records (fixed COM, float quaternion)
   double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
   int* d_npin = nullptr;
   float4* d_fres = nullptr;       // mixed MD step: per-molecule float-pair results of the pair kernel
@@ -512,7 +513,7 @@ static PlaceArgs place_args(g6_ctx* c) {
   p.rep = rep_dev(c);
   for (int s = 0; s < MAXSITE; ++s)
     for (int k = 0; k < 3; ++k) { p.body[s][k] = c->mh.body[s][k]; p.fbody[s][k] = (float)c->mh.body[s][k]; }
-  p.st = c->d_st; p.tmat = c->d_tmat; p.pk64 = c->d_pk64; p.pk32 = c->d_pk32; p.fix = c->d_fix;
+  p.st = c->d_st; p.tmat = c->d_tmat; p.pk64 = c->d_pk64; p.pk32 = c->d_pk32; p.pkq = c->d_pkq; p.fix = c->d_fix;
   return p;
 }
 
@@ -546,6 +547,9 @@ static ForceArgs force_args(g6_ctx* c) {
   a.pc = c->pc; a.cc = c->cc; a.F = c->d_F; a.tl = c->d_tl;
   a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin; a.fres = c->d_fres;
   a.ccap = c->ccap; a.overflow = c->d_overflow;
+  a.pkq = c->d_pkq; a.pkq_1 = c->d_pkq_1;
+  for (int s = 0; s < MAXSITE; ++s)
+    for (int k = 0; k < 3; ++k) a.fbody[s][k] = (float)c->mh.body[s][k];
   return a;
 }
 
@@ -743,6 +747,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_tmat1, 9 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_pk64_1, (size_t)ctx->w64 * n)); CK(dalloc(ctx, &ctx->d_pk32_1, (size_t)ctx->npk * n));
   CK(dalloc(ctx, &ctx->d_fix1, 3 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_pkq, 2 * (size_t)n)); CK(dalloc(ctx, &ctx->d_pkq_1, 2 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_fres, 4 * (size_t)n));
@@ -1283,7 +1288,8 @@ static StepArgs step_args(g6_ctx* ctx, double dt, double* log) {
   StepArgs a;
   std::memset(&a, 0, sizeof a);
   a.p = place_args(ctx);
-  a.tmat1 = ctx->d_tmat1; a.pk64_1 = ctx->d_pk64_1; a.pk32_1 = ctx->d_pk32_1; a.fix1 = ctx->d_fix1;
+  a.tmat1 = ctx->d_tmat1; a.pk64_1 = ctx->d_pk64_1; a.pk32_1 = ctx->d_pk32_1; a.pkq_1 = ctx->d_pkq_1;
+  a.fix1 = ctx->d_fix1;
   a.mass = ctx->mh.mass; a.I[0] = ctx->mh.I[0]; a.I[1] = ctx->mh.I[1]; a.I[2] = ctx->mh.I[2]; a.dt = dt;
   a.com_build = ctx->d_com_build;
   a.fix_build = ctx->d_fix_build;
@@ -1884,10 +1890,25 @@ int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double*
 
 // Enqueue the whole host-buffer step on the context's stream (used directly,
 // or captured once into graph_host).  log_dst: host destination of the log.
-// upload = false repeats a step from the state kept in d_save (row-overflow recovery).
+// upload = false repeats a step from the state kept in d_save (FP64) or the
+// records in d_stage (mixed) -- the row-overflow recovery.
 static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log, bool upload = true) {
   const int n = ctx->n;
   const size_t bytes = (size_t)REC * n * sizeof(double);
+  if (ctx->prec == G6_MIXED) {
+    // records -> state + first predict in one kernel, the step, finish + state
+    // -> records in one kernel; the input records stay in d_stage, the output
+    // goes through d_save
+    if (upload) CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = md_upload(ctx);
+    if (rc) return rc;
+    StepArgs sa = step_args(ctx, dt, want_log ? ctx->d_log : nullptr);
+    CK(launch_host_in_mixed(place_args(ctx), ctx->d_stage, ctx->d_stf, ctx->d_th, dt, ctx->stream));
+    if ((rc = enqueue_step(ctx, sa))) return rc;
+    CK(launch_host_out_mixed(sa, ctx->d_save, ctx->stream));
+    CK(cudaMemcpyAsync(rec, ctx->d_save, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return md_readback(ctx, 1, want_log ? log_dst : nullptr);
+  }
   if (upload) {
     CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
     CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 1, ctx->stream));

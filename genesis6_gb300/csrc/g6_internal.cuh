@@ -10,6 +10,10 @@
 //   pk32    float4 AoS packed pose for the mixed site loop: 32-bit fixed-point
 //           COM (x,y,z as uint32 in units of L/2^32), then float offsets of
 //           the LJ site and the charged sites relative to the COM
+//   pkq     2 float4 per molecule for the mixed list kernel: the fixed-point
+//           COM words, then the float quaternion (q0..q3) and a zero; the
+//           kernel rebuilds the float site offsets from the quaternion
+//           (rotmat_f / site_off_f, the same roundings as the placement's)
 //   fix     uint32 SoA fixed-point COM (list building and cell-free tests)
 //   F, tl   per-molecule force and lab-frame torque (FP64 SoA)
 //   emol, wmol  per-molecule energy (1/2 of its pair sum) and virial rows
@@ -214,6 +218,9 @@ struct ForceArgs {
   float4* fres;   // mixed MD step: per molecule 4 float4 of float pairs (F, energy; lab torque, virial trace)
   int ccap;       // mixed list kernel: in-range entries per molecule its shared-memory rows hold (<= cap)
   int* overflow;  // set to 1 when a row holds more in-range entries than ccap
+  const float4* pkq;     // mixed list kernel: 2 float4 per molecule (fixed-point COM, float quaternion)
+  const float4* pkq_1;   // the same for pose buffer 1
+  float fbody[MAXSITE][3];   // body-frame site coordinates (LJ site, charged sites) as float
 };
 
 struct SitesArgs {
@@ -298,6 +305,7 @@ struct PlaceArgs {
   double* tmat;
   double* pk64;
   float4* pk32;
+  float4* pkq;   // 2 float4 per molecule (layout above)
   uint32_t* fix;
 };
 
@@ -306,6 +314,7 @@ struct StepArgs {
   double* tmat1;       // pose buffer 1 (the buffers alternate with the step parity)
   double* pk64_1;
   float4* pk32_1;
+  float4* pkq_1;
   uint32_t* fix1;
   double mass, I[3], dt;
   double inv_dt2;      // 1 / dt^2
@@ -545,6 +554,10 @@ cudaError_t launch_pairset_write(PairSetArgs a, cudaStream_t s);
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict, cudaStream_t s);
 cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s);
 cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, double dt, cudaStream_t s);
+// Host-buffer step of the mixed path: records in -> state + first predict; finish + state -> records out.
+cudaError_t launch_host_in_mixed(const PlaceArgs& a, const double* rec, float* stf, ThermoDev* th, double dt,
+                                 cudaStream_t s);
+cudaError_t launch_host_out_mixed(const StepArgs& sa, double* out, cudaStream_t s);
 cudaError_t launch_step_fp64(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);

@@ -31,7 +31,7 @@ __global__ void k_predict_place(PlaceArgs a, int do_predict, ThermoDev* th, int 
   }
   if (i >= a.n) return;
   if (do_predict) predict_one(a.st, a.n, i);
-  place_to(a, i, a.tmat, a.pk64, a.pk32, a.fix);
+  place_to(a, i, a.tmat, a.pk64, a.pk32, a.pkq, a.fix);
 }
 
 cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* th, int nose_predict,
@@ -44,16 +44,119 @@ cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* 
 // Mixed-precision runs: the small Gear terms move from the FP64 state into
 // the float SoA at the start of a run (to_float) and back at its end, so the
 // FP64 state is the complete rigid record whenever no run is active.
+// State column (of the 53-double record) of float column c.
+__device__ __forceinline__ int stf_state_col(int c) {
+  if (c < STF_W2) return 6 + c;                    // d2..d5
+  if (c < STF_Q2) return 21 + (c - STF_W2);        // w2..w5
+  return 37 + (c - STF_Q2);                        // q2..q5 stacks
+}
+
 __global__ void k_stf_move(double* st, float* stf, int n, int to_float) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)n * STF_COLS) return;
   const int c = (int)(t / n), i = (int)(t % n);
-  int sc;   // state column of float column c
-  if (c < STF_W2) sc = 6 + c;                      // d2..d5
-  else if (c < STF_Q2) sc = 21 + (c - STF_W2);     // w2..w5
-  else sc = 37 + (c - STF_Q2);                     // q2..q5 stacks
+  const int sc = stf_state_col(c);
   if (to_float) stf[t] = (float)st[(size_t)sc * n + i];
   else st[(size_t)sc * n + i] = (double)stf[t];
+}
+
+// Float column of state column sc, or -1 for the columns kept in FP64 (com,
+// d1, w1, q); the inverse of stf_state_col.
+__device__ __forceinline__ int state_float_col(int sc) {
+  if (sc < 6) return -1;
+  if (sc < 18) return sc - 6;
+  if (sc < 21) return -1;
+  if (sc < 33) return STF_W2 + (sc - 21);
+  if (sc < 37) return -1;
+  return STF_Q2 + (sc - 37);
+}
+
+// Records move between the AoS layout (n,53) and the column layout through a
+// shared-memory tile of REC_TILE molecules: the record block is read or
+// written as one contiguous run, the columns as 32-molecule runs, so both
+// sides are coalesced.
+constexpr int REC_TILE = 32;
+constexpr int REC_THREADS = 128;
+
+// One mixed-precision step with the state in the caller's record buffer
+// (g6_md_step_host): the records (n,53) become the FP64 state (com, d1, w1,
+// q) and the float small terms, followed by the step's first predict and
+// placement and the Nose predict -- the work of k_rec_transpose, k_stf_move
+// and k_begin_mixed in one pass, with the same arithmetic.
+__global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, const double* rec, float* stf,
+                                                               ThermoDev* th, double dt) {
+  __shared__ double tile[REC_TILE * REC];
+  if (blockIdx.x == 0) {
+    for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
+      ThermoDev& T = th[r];
+      if (T.kind == G6_NOSE) {
+        T.z[0] = T.z[0] + T.z[1] + T.z[2] + T.z[3] + T.z[4];
+        T.z[1] = T.z[1] + 2.0 * T.z[2] + 3.0 * T.z[3] + 4.0 * T.z[4];
+        T.z[2] = T.z[2] + 3.0 * T.z[3] + 6.0 * T.z[4];
+        T.z[3] = T.z[3] + 4.0 * T.z[4];
+        T.fext = (float)(T.z[0] * dt);
+      }
+    }
+  }
+  const int n = a.n;
+  const int i0 = blockIdx.x * REC_TILE;
+  const int m = min(REC_TILE, n - i0);
+  if (m <= 0) return;
+  const double* src = rec + (size_t)i0 * REC;
+  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) tile[t] = src[t];
+  __syncthreads();
+  double* st = a.st;
+  for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
+    const int c = t / REC_TILE, k = t % REC_TILE;
+    if (k >= m) continue;
+    const double v = tile[k * REC + c];
+    const int fc = state_float_col(c);
+    if (fc < 0) st[(size_t)c * n + i0 + k] = v;
+    else stf[(size_t)fc * n + i0 + k] = (float)v;
+  }
+  __syncthreads();   // the block's columns are visible to the block
+  if ((int)threadIdx.x < m) {
+    const int i = i0 + threadIdx.x;
+    double x[3], q[4];
+    predict_mixed(st, stf, n, i, x, q);
+    if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+    else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+  }
+}
+
+// The end of that step: the replica finish of the step (the first nrep
+// blocks) beside the state going back to the FP64 record, both in the device
+// state and as records (n,53) in `out` for the copy to the caller -- the work
+// of k_finish_step, k_stf_move and k_rec_transpose in one launch.
+__global__ void __launch_bounds__(REC_THREADS) k_host_out_mixed(StepArgs sa, double* out) {
+  __shared__ double tile[REC_TILE * REC];
+  const int nfin = sa.p.rep.nrep;
+  if ((int)blockIdx.x < nfin) {
+    finish_pending(sa, blockIdx.x, 32);
+    return;
+  }
+  const int n = sa.p.n;
+  const int i0 = (blockIdx.x - nfin) * REC_TILE;
+  const int m = min(REC_TILE, n - i0);
+  if (m <= 0) return;
+  double* st = sa.p.st;
+  for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
+    const int c = t / REC_TILE, k = t % REC_TILE;
+    if (k >= m) continue;
+    const size_t at = (size_t)c * n + i0 + k;
+    const int fc = state_float_col(c);
+    double v;
+    if (fc < 0) {
+      v = st[at];
+    } else {
+      v = (double)sa.stf[(size_t)fc * n + i0 + k];
+      st[at] = v;
+    }
+    tile[k * REC + c] = v;
+  }
+  __syncthreads();
+  double* dst = out + (size_t)i0 * REC;
+  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) dst[t] = tile[t];
 }
 
 // First predict + placement of a mixed run (plus the first Nose_Predict).
@@ -74,14 +177,27 @@ __global__ void k_begin_mixed(PlaceArgs a, float* stf, ThermoDev* th, double dt)
   if (i >= a.n) return;
   double x[3], q[4];
   predict_mixed(a.st, stf, a.n, i, x, q);
-  if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.fix);
-  else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.fix);
+  if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+  else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
 }
 
 cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s) {
   const long long total = (long long)n * STF_COLS;
   if (total == 0) return cudaSuccess;
   k_stf_move<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(st, stf, n, to_float);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_host_in_mixed(const PlaceArgs& a, const double* rec, float* stf, ThermoDev* th, double dt,
+                                 cudaStream_t s) {
+  const int blocks = a.n > 0 ? (a.n + REC_TILE - 1) / REC_TILE : 1;
+  k_host_in_mixed<<<blocks, REC_THREADS, 0, s>>>(a, rec, stf, th, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_host_out_mixed(const StepArgs& sa, double* out, cudaStream_t s) {
+  const int blocks = sa.p.rep.nrep + (sa.p.n + REC_TILE - 1) / REC_TILE;
+  k_host_out_mixed<<<blocks, REC_THREADS, 0, s>>>(sa, out);
   return cudaGetLastError();
 }
 
@@ -130,19 +246,33 @@ cudaError_t launch_exchange(const ExchArgs& a, double* st, int n, const int* mol
   return cudaGetLastError();
 }
 
-// AoS rigid records (n x 53) <-> SoA device state (53 x n).
-__global__ void k_rec_transpose(double* aos, double* soa, int n, int to_soa) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n * REC) return;
-  const int c = (int)(t / n), i = (int)(t % n);
-  if (to_soa) soa[t] = aos[(size_t)i * REC + c];
-  else aos[(size_t)i * REC + c] = soa[t];
+// AoS rigid records (n x 53) <-> SoA device state (53 x n), one tile of
+// REC_TILE molecules per block.
+__global__ void __launch_bounds__(REC_THREADS) k_rec_transpose(double* aos, double* soa, int n, int to_soa) {
+  __shared__ double tile[REC_TILE * REC];
+  const int i0 = blockIdx.x * REC_TILE;
+  const int m = min(REC_TILE, n - i0);
+  double* blk = aos + (size_t)i0 * REC;
+  if (to_soa) {
+    for (int t = threadIdx.x; t < m * REC; t += blockDim.x) tile[t] = blk[t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
+      const int c = t / REC_TILE, k = t % REC_TILE;
+      if (k < m) soa[(size_t)c * n + i0 + k] = tile[k * REC + c];
+    }
+  } else {
+    for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
+      const int c = t / REC_TILE, k = t % REC_TILE;
+      if (k < m) tile[k * REC + c] = soa[(size_t)c * n + i0 + k];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < m * REC; t += blockDim.x) blk[t] = tile[t];
+  }
 }
 
 cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s) {
-  const long long total = (long long)n * REC;
-  if (total == 0) return cudaSuccess;
-  k_rec_transpose<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(aos, soa, n, to_soa);
+  if (n <= 0) return cudaSuccess;
+  k_rec_transpose<<<(n + REC_TILE - 1) / REC_TILE, REC_THREADS, 0, s>>>(aos, soa, n, to_soa);
   return cudaGetLastError();
 }
 

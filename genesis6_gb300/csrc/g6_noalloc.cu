@@ -53,7 +53,8 @@ constexpr size_t O_TMAT = O_ST + al(37ull * MAXN * 8);
 constexpr size_t O_PK64 = O_TMAT + al(9ull * MAXN * 8);
 constexpr size_t O_PK32 = O_PK64 + al((size_t)W64MAX * MAXN * 8);
 constexpr size_t O_FIX = O_PK32 + al((size_t)NPKMAX * MAXN * 16);
-constexpr size_t O_F = O_FIX + al(3ull * MAXN * 4);
+constexpr size_t O_PKQ = O_FIX + al(3ull * MAXN * 4);                // 2 float4 per molecule
+constexpr size_t O_F = O_PKQ + al(2ull * MAXN * 16);
 constexpr size_t O_TL = O_F + al(3ull * MAXN * 8);
 constexpr size_t O_EMOL = O_TL + al(3ull * MAXN * 8);
 constexpr size_t O_WMOL = O_EMOL + al((size_t)MAXN * 8);
@@ -217,7 +218,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   for (int q = 0; q < MAXSITE; ++q)
     for (int k = 0; k < 3; ++k) { pa.body[q][k] = mh.body[q][k]; pa.fbody[q][k] = (float)mh.body[q][k]; }
   pa.st = (double*)(base + O_ST); pa.tmat = (double*)(base + O_TMAT); pa.pk64 = (double*)(base + O_PK64);
-  pa.pk32 = (float4*)(base + O_PK32); pa.fix = (uint32_t*)(base + O_FIX);
+  pa.pk32 = (float4*)(base + O_PK32); pa.pkq = (float4*)(base + O_PKQ); pa.fix = (uint32_t*)(base + O_FIX);
 
   CellArgs ca;
   ca.n = n; ca.rep = rep; ca.g = g; ca.com = pa.st; ca.cell = (int*)(base + O_CELL); ca.slot = (int*)(base + O_SLOT);
@@ -239,6 +240,9 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   fa.F = (double*)(base + O_F); fa.tl = (double*)(base + O_TL); fa.emol = (double*)(base + O_EMOL);
   fa.wmol = (double*)(base + O_WMOL); fa.npair_in = (int*)(base + O_NPIN);
   fa.ccap = CAP; fa.overflow = la.overflow;
+  fa.pkq = pa.pkq; fa.pkq_1 = pa.pkq;
+  for (int q = 0; q < MAXSITE; ++q)
+    for (int k = 0; k < 3; ++k) fa.fbody[q][k] = pa.fbody[q][k];
 
   const int blocks = (n + 255) / 256;
   k_setup<<<blocks, 256, 0, s>>>(su, base);

@@ -11,9 +11,13 @@
 //      them to the molecule's row in shared memory with a ballot and a prefix
 //      count.  Up to six row entries per lane are in flight at a time.
 //   2. pairs: the lanes share out the compacted row (every lane of a group has
-//      an in-range pair until the row's tail), load j's packed pose one pair
-//      ahead and run the FP32 site loop of pair_math, keeping per-lane sums of
-//      the i-site forces, the COM switch force, the energy and the virial.
+//      an in-range pair until the row's tail), load j's 32-byte record (pkq:
+//      fixed-point COM and float quaternion, one 256-bit load) one pair ahead,
+//      rebuild its float site offsets from the quaternion and run the FP32
+//      site loop of pair_math, keeping per-lane sums of the i-site forces, the
+//      COM switch force, the energy and the virial.  The record is a quarter
+//      of the L1 lines of the site offsets it replaces; the kernel is bound by
+//      L1 line gathers, not by the 40-odd flops of the rebuild.
 // The lanes of a molecule are then combined: in FP64 for the force-only call
 // (MODE 0: F, lab torque, energy, full virial), with error-free float-pair
 // addition for the MD step (MODE 1: F, lab torque, energy and virial trace as
@@ -48,6 +52,26 @@ struct PairMinBlocks {
   static constexpr int value = (M::NQ == 3 && MODE == 1) ? 5 : 4;
 };
 
+// The 32-byte record of molecule j (pkq: fixed-point COM words, float
+// quaternion, zero) in one 256-bit load through the non-coherent path: no
+// pose buffer is written while a pair kernel runs.
+__device__ __forceinline__ void load_pose_q(const float4* pkq, int j, float (&v)[8]) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+      : "l"(pkq + 2 * (size_t)j));
+}
+
+// Float site offsets (LJ site, charged sites) from the record's quaternion:
+// the placement's arithmetic (setmatrix_f, site_off_f), so the same bits as
+// the offsets it wrote to pk32.
+template <class M>
+__device__ __forceinline__ void sites_from_q(const ForceArgs& a, const float* q, float (&r)[M::NQ + 1][3]) {
+  float t[9];
+  setmatrix_f(q, t);
+#pragma unroll
+  for (int s = 0; s <= M::NQ; ++s) site_off_f(t, a.fbody[s][0], a.fbody[s][1], a.fbody[s][2], r[s]);
+}
+
 // Fixed-point COM difference (units L/2^32, the wrap is the minimum image) to A.
 __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi, const float4& qj, float sx, float sy,
                                           float sz, float d[3]) {
@@ -72,13 +96,12 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   }
   constexpr int G = PairShape<LPI>::GROUPS;
   constexpr int U = PairShape<LPI>::UNROLL;
-  constexpr int NPK = M::NPK;
   extern __shared__ int s_rows[];
   const int n = a.n;
   const int step = a.ctrl ? a.ctrl[1] : 0;
   const bool odd = (step & 1) != 0;
   const double* pk64 = odd ? a.pk64_1 : a.pk64;
-  const float4* pk32 = odd ? a.pk32_1 : a.pk32;
+  const float4* pkq = odd ? a.pkq_1 : a.pkq;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane / LPI, sub = lane % LPI;
   const int i = (bid * blockDim.x + threadIdx.x) / LPI;
@@ -92,17 +115,10 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   int r = 0, nn = 0;
   if (valid) {
     r = a.rep.mol_rep[i];
-    float wi[4 * NPK];
-#pragma unroll
-    for (int q = 0; q < NPK; ++q) {
-      const float4 t = pk32[(size_t)i * NPK + q];
-      wi[4 * q] = t.x; wi[4 * q + 1] = t.y; wi[4 * q + 2] = t.z; wi[4 * q + 3] = t.w;
-    }
+    float wi[8];
+    load_pose_q(pkq, i, wi);
     xi = __float_as_uint(wi[0]); yi = __float_as_uint(wi[1]); zi = __float_as_uint(wi[2]);
-#pragma unroll
-    for (int s = 0; s <= M::NQ; ++s)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) ri[s][k] = wi[3 + 3 * s + k];
+    sites_from_q<M>(a, wi + 3, ri);
     sx = a.rep.fscale[3 * r]; sy = a.rep.fscale[3 * r + 1]; sz = a.rep.fscale[3 * r + 2];
     nn = a.nnb[i];
   } else {
@@ -127,7 +143,7 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
       jj[u] = k < nn ? __ldg(row + k) : -1;
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? pk32[(size_t)jj[u] * NPK] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? __ldg(pkq + 2 * (size_t)jj[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bool in = false;
@@ -168,31 +184,18 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   {
     const float frin2 = a.cc.frin2, frin = a.cc.frin, frout = a.cc.frout, fc1 = a.cc.fc1, fc2 = a.cc.fc2;
     int t = sub;
-    float4 tn[NPK];
-    if (t < cnt) {
-      const int j0 = srow[t];
-#pragma unroll
-      for (int q = 0; q < NPK; ++q) tn[q] = pk32[(size_t)j0 * NPK + q];
-    }
+    float tn[8];
+    if (t < cnt) load_pose_q(pkq, srow[t], tn);
     for (; t < cnt; t += LPI) {
-      float wj[4 * NPK];
+      float wj[8];
 #pragma unroll
-      for (int q = 0; q < NPK; ++q) {
-        wj[4 * q] = tn[q].x; wj[4 * q + 1] = tn[q].y; wj[4 * q + 2] = tn[q].z; wj[4 * q + 3] = tn[q].w;
-      }
-      if (t + LPI < cnt) {   // the next pair's pose, one pair ahead
-        const int jn = srow[t + LPI];
-#pragma unroll
-        for (int q = 0; q < NPK; ++q) tn[q] = pk32[(size_t)jn * NPK + q];
-      }
+      for (int k = 0; k < 8; ++k) wj[k] = tn[k];
+      if (t + LPI < cnt) load_pose_q(pkq, srow[t + LPI], tn);   // the next pair's record, one pair ahead
       float d[3];
       fix_delta(xi, yi, zi, make_float4(wj[0], wj[1], wj[2], 0.f), sx, sy, sz, d);
       const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
       float rj[M::NQ + 1][3];
-#pragma unroll
-      for (int s = 0; s <= M::NQ; ++s)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) rj[s][k] = wj[3 + 3 * s + k];
+      sites_from_q<M>(a, wj + 3, rj);
       pair_math<M, float, NW>(d, dd, ri, rj, a.pc, frin2, frin, frout, fc1, fc2, a.pc.frl, a.pc.fru, a.pc.fw3, acc);
     }
   }

@@ -38,6 +38,13 @@ __device__ __forceinline__ void setmatrix(const double q[4], double t[9]) {
   t[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
 }
 
+// The mixed list kernel's record of molecule i (pkq): fixed-point COM words
+// and the float quaternion the offsets were built from.
+__device__ __forceinline__ void write_pose_q(float4* pkq, int i, const float w[3], const float q[4]) {
+  pkq[2 * (size_t)i] = make_float4(w[0], w[1], w[2], q[0]);
+  pkq[2 * (size_t)i + 1] = make_float4(q[1], q[2], q[3], 0.0f);
+}
+
 __device__ __forceinline__ void predict_one(double* st, int n, int i) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -70,7 +77,7 @@ __device__ __forceinline__ void predict_one(double* st, int n, int i) {
 
 // Placement of molecule i (its current com and q in st) into one buffer set.
 __device__ __forceinline__ void place_to(const PlaceArgs& a, int i, double* tmat, double* pk64, float4* pk32,
-                                         uint32_t* fix) {
+                                         float4* pkq, uint32_t* fix) {
   const int n = a.n;
   const double* st = a.st;
   double q[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
@@ -99,6 +106,10 @@ __device__ __forceinline__ void place_to(const PlaceArgs& a, int i, double* tmat
   for (int k = 3 + 3 * (a.nq + 1); k < a.w64; ++k) p64[k] = 0.0;
   for (int q4 = 0; q4 < a.npk; ++q4)
     pk32[(size_t)i * a.npk + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+  if (pkq) {
+    const float qf[4] = {(float)q[0], (float)q[1], (float)q[2], (float)q[3]};
+    write_pose_q(pkq, i, w, qf);
+  }
 }
 
 // (1/2) W(w) q pattern of RigidModule.F90:1337-1348
@@ -122,12 +133,13 @@ struct PoseBuf {
   double* tmat;
   double* pk64;
   float4* pk32;
+  float4* pkq;
   uint32_t* fix;
 };
 __device__ __forceinline__ PoseBuf pose_buf(const StepArgs& a, int which) {
   PoseBuf b;
-  if (which == 0) { b.tmat = a.p.tmat; b.pk64 = a.p.pk64; b.pk32 = a.p.pk32; b.fix = a.p.fix; }
-  else { b.tmat = a.tmat1; b.pk64 = a.pk64_1; b.pk32 = a.pk32_1; b.fix = a.fix1; }
+  if (which == 0) { b.tmat = a.p.tmat; b.pk64 = a.p.pk64; b.pk32 = a.p.pk32; b.pkq = a.p.pkq; b.fix = a.p.fix; }
+  else { b.tmat = a.tmat1; b.pk64 = a.pk64_1; b.pk32 = a.pk32_1; b.pkq = a.pkq_1; b.fix = a.fix1; }
   return b;
 }
 
@@ -251,7 +263,7 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
   v[4] = npair_half;
   if (predict_next) {
     predict_one(st, n, i);
-    place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.fix);
+    place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.pkq, next.fix);
     const double dx = G6_ST(0) - a.com_build[i], dy = G6_ST(1) - a.com_build[n + i],
                  dz = G6_ST(2) - a.com_build[2 * n + i];
     dmax2 = dx * dx + dy * dy + dz * dz;
@@ -266,17 +278,28 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
 // ---------------------------------------------------------------------------
 #define G6_SF(c) stf[(size_t)(c) * n + i]
 
+// setmatrix in float with every rounding spelled out (no contraction left to
+// the compiler): the placement and the mixed list kernel, which rebuilds a
+// neighbour's site offsets from its quaternion, get the same bits.
 __device__ __forceinline__ void setmatrix_f(const float q[4], float t[9]) {
   const float qa = q[0], qb = q[1], qc = q[2], qd = q[3];
-  t[0] = (qa * qa + qb * qb - (qc * qc + qd * qd));
-  t[1] = -2.0f * (qa * qd + qb * qc);
-  t[2] = 2.0f * (qb * qd - qa * qc);
-  t[3] = 2.0f * (qa * qd - qb * qc);
-  t[4] = qa * qa + qc * qc - (qb * qb + qd * qd);
-  t[5] = -2.0f * (qa * qb + qc * qd);
-  t[6] = 2.0f * (qa * qc + qb * qd);
-  t[7] = 2.0f * (qa * qb - qc * qd);
-  t[8] = qa * qa + qd * qd - (qb * qb + qc * qc);
+  const float aa = __fmul_rn(qa, qa), bb = __fmul_rn(qb, qb), cc = __fmul_rn(qc, qc), dd = __fmul_rn(qd, qd);
+  t[0] = __fsub_rn(__fadd_rn(aa, bb), __fadd_rn(cc, dd));
+  t[1] = __fmul_rn(-2.0f, __fmaf_rn(qa, qd, __fmul_rn(qb, qc)));
+  t[2] = __fmul_rn(2.0f, __fmaf_rn(qb, qd, __fmul_rn(-qa, qc)));
+  t[3] = __fmul_rn(2.0f, __fmaf_rn(qa, qd, __fmul_rn(-qb, qc)));
+  t[4] = __fsub_rn(__fadd_rn(aa, cc), __fadd_rn(bb, dd));
+  t[5] = __fmul_rn(-2.0f, __fmaf_rn(qa, qb, __fmul_rn(qc, qd)));
+  t[6] = __fmul_rn(2.0f, __fmaf_rn(qa, qc, __fmul_rn(qb, qd)));
+  t[7] = __fmul_rn(2.0f, __fmaf_rn(qa, qb, __fmul_rn(-qc, qd)));
+  t[8] = __fsub_rn(__fadd_rn(aa, dd), __fadd_rn(bb, cc));
+}
+
+// Lab-frame offset t * b of a body-frame site, rounding spelled out.
+__device__ __forceinline__ void site_off_f(const float t[9], float bx, float by, float bz, float o[3]) {
+  o[0] = __fmaf_rn(t[0], bx, __fmaf_rn(t[1], by, __fmul_rn(t[2], bz)));
+  o[1] = __fmaf_rn(t[3], bx, __fmaf_rn(t[4], by, __fmul_rn(t[5], bz)));
+  o[2] = __fmaf_rn(t[6], bx, __fmaf_rn(t[7], by, __fmul_rn(t[8], bz)));
 }
 
 __device__ __forceinline__ void qdot_f(const float w[3], const float q[4], float o[4]) {
@@ -293,7 +316,7 @@ __device__ __forceinline__ float uniform_f(uint32_t x) { return ((float)(x >> 8)
 // fixed-point com (x * 2^32 / L, wrapped), float site offsets, FP64 com.
 template <int NQ>
 __device__ __forceinline__ void place_mixed(const PlaceArgs& a, int i, const double x[3], const double q[4],
-                                            double* pk64, float4* pk32, uint32_t* fix) {
+                                            double* pk64, float4* pk32, float4* pkq, uint32_t* fix) {
   constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
   const int n = a.n;
   const int r = a.rep.mol_rep[i];
@@ -311,15 +334,11 @@ __device__ __forceinline__ void place_mixed(const PlaceArgs& a, int i, const dou
     pk64[(size_t)i * a.w64 + k] = x[k];
   }
 #pragma unroll
-  for (int s = 0; s <= NQ; ++s) {
-    const float bx = a.fbody[s][0], by = a.fbody[s][1], bz = a.fbody[s][2];
-    w[3 + 3 * s] = t[0] * bx + t[1] * by + t[2] * bz;
-    w[4 + 3 * s] = t[3] * bx + t[4] * by + t[5] * bz;
-    w[5 + 3 * s] = t[6] * bx + t[7] * by + t[8] * bz;
-  }
+  for (int s = 0; s <= NQ; ++s) site_off_f(t, a.fbody[s][0], a.fbody[s][1], a.fbody[s][2], w + 3 + 3 * s);
 #pragma unroll
   for (int q4 = 0; q4 < NPK; ++q4)
     pk32[(size_t)i * NPK + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+  write_pose_q(pkq, i, w, qf);
 }
 
 // rigid_predict (RigidModule.F90:480-559) with the small terms in float.
@@ -553,15 +572,11 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
     dd += e * e;
   }
 #pragma unroll
-  for (int s = 0; s <= NQ; ++s) {
-    const float bx = a.p.fbody[s][0], by = a.p.fbody[s][1], bz = a.p.fbody[s][2];
-    w[3 + 3 * s] = tp[0] * bx + tp[1] * by + tp[2] * bz;
-    w[4 + 3 * s] = tp[3] * bx + tp[4] * by + tp[5] * bz;
-    w[5 + 3 * s] = tp[6] * bx + tp[7] * by + tp[8] * bz;
-  }
+  for (int s = 0; s <= NQ; ++s) site_off_f(tp, a.p.fbody[s][0], a.p.fbody[s][1], a.p.fbody[s][2], w + 3 + 3 * s);
 #pragma unroll
   for (int q4 = 0; q4 < NPK; ++q4)
     next.pk32[(size_t)i * NPK + q4] = make_float4(w[4 * q4], w[4 * q4 + 1], w[4 * q4 + 2], w[4 * q4 + 3]);
+  write_pose_q(next.pkq, i, w, qp);
   dmax2 = dd;
   if (!isfinite(dd)) { bad = 1; dmax2 = 3.0e38f; }
 }
