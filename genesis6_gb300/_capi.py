@@ -24,6 +24,7 @@ FP64, MIXED = 0, 1
 PRECISIONS = {"fp64": FP64, "mixed": MIXED}
 NVE, NOSE, ANDERSEN = 0, 1, 2
 MC_PLAIN, MC_LEARNED, MC_COLLECT = 0, 1, 2
+OP_EP, OP_Q6, OP_TRIANGLE, OP_NBIN = 0, 1, 2, 21   # g6gpu.h G6_OP_*
 MLP_NPARAM, MLP_NFEAT, MLP_RECORD = 5890, 24, 51
 LOG_WIDTH = 10
 REC = 53
@@ -37,7 +38,7 @@ SYMBOLS = [
     "g6_force_sites_hetero", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_exchange_plan", "g6_replica_scale", "g6_last_epot",
     "g6_md_begin", "g6_md_advance", "g6_md_end", "g6_stream",
-    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_tune_shape", "g6_get_shape", "g6_set_shape", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
+    "g6_time_force", "g6_tune", "g6_set_lpi", "g6_tune_shape", "g6_get_shape", "g6_set_shape", "g6_set_step_timing", "g6_step_times", "g6_force_noalloc", "g6_mc_run", "g6_order_parameter", "g6_mc_run_umbrella", "g6_mlp_set", "g6_mlp_get", "g6_mlp_objective", "g6_mlp_widths",
     "g6_mlp_records", "g6_mlp_grad", "g6_mlp_train",
 ]
 
@@ -125,6 +126,10 @@ def lib():
                                    ctypes.c_double, ctypes.c_double, vp, vp, vp, vp, vp, vp]
     L.g6_mc_run.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp, ctypes.c_int,
                             ctypes.c_int, dp, ctypes.POINTER(ctypes.c_int64), dp, dp]
+    L.g6_order_parameter.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, dp]
+    L.g6_mc_run_umbrella.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp, dp, dp, ctypes.c_int, dp,
+                                     dp, ctypes.c_int, dp, ctypes.c_int, dp, dp, ctypes.POINTER(ctypes.c_int64), dp,
+                                     dp]
     fp = ctypes.POINTER(ctypes.c_float)
     L.g6_mlp_set.argtypes = [vp, fp, fp, fp, ctypes.c_double, ctypes.c_double]
     L.g6_mlp_get.argtypes = [vp, fp, fp, fp]

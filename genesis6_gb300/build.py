@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libg6gpu.so")
-SOURCES = ["g6_capi.cu", "g6_force.cu", "g6_pairs.cu", "g6_cells.cu", "g6_md.cu", "g6_noalloc.cu", "g6_mc.cu", "g6_train.cu",
+SOURCES = ["g6_capi.cu", "g6_force.cu", "g6_pairs.cu", "g6_cells.cu", "g6_md.cu", "g6_noalloc.cu", "g6_mc.cu", "g6_opmc.cu", "g6_train.cu",
            "g6_analysis.cu", "g6_mixture.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas",

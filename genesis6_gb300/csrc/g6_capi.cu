@@ -14,6 +14,7 @@
 
 #include "g6_internal.cuh"
 #include "g6_mlp.cuh"
+#include "g6_op.cuh"
 
 namespace g6 {
 
@@ -301,6 +302,10 @@ struct g6_ctx {
   int* d_fcache = nullptr;         // per-molecule features at the current pose (Monte Carlo)
   int* d_mcflag = nullptr;         // Monte Carlo: too many feature neighbours
   float* d_udir = nullptr;         // Monte Carlo: charged-site directions per molecule
+  OpDev opd{};                     // umbrella Monte Carlo: order-parameter state (allocated on first use)
+  bool have_op = false;
+  double* d_umb = nullptr;         // per chain: umbrella center, coefficient
+  double* d_opsamp = nullptr; size_t opsamp_cap = 0;
   float h_mean[MLP_IN] = {0}, h_istd[MLP_IN] = {0};
   double sig0_t = 0.15, sig0_r = 0.15;
   double obj_move = 1.0, obj_energy = 0.0;   // training objective weights (g6_mlp_objective)
@@ -381,6 +386,7 @@ static void free_all(g6_ctx* c) {
   if (c->d_log) { cudaFree(c->d_log); c->d_log = nullptr; c->log_cap = 0; }
   if (c->d_samples) { cudaFree(c->d_samples); c->d_samples = nullptr; c->samples_cap = 0; }
   if (c->d_trace) { cudaFree(c->d_trace); c->d_trace = nullptr; c->trace_cap = 0; }
+  if (c->d_opsamp) { cudaFree(c->d_opsamp); c->d_opsamp = nullptr; c->opsamp_cap = 0; }
   if (c->d_rec) { cudaFree(c->d_rec); c->d_rec = nullptr; c->rec_cap = 0; c->nrec = 0; }
   c->have_mlp = false;
   if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
@@ -2100,6 +2106,80 @@ static MlpDev mlp_dev(g6_ctx* ctx) {
 
 extern "C" {
 
+// Start of a Monte Carlo call: the energy of every chain from a full force
+// evaluation (which also places the poses), and the inverse temperatures,
+// widths and energies on the device; etot gets the energies.
+static int mc_begin(g6_ctx* ctx, const double* beta, const double* sigma_t, const double* sigma_r,
+                    std::vector<double>& etot) {
+  const int R = ctx->nrep;
+  int rc = force_once(ctx);
+  if (rc) return rc;
+  std::vector<double> e(ctx->n);
+  etot.assign(R, 0.0);
+  CK(cudaMemcpy(e.data(), ctx->d_emol, ctx->n * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int r = 0; r < R; ++r)
+    for (int i = ctx->off[r]; i < ctx->off[r + 1]; ++i) etot[r] += e[i];
+  std::vector<double> st(R, ctx->sig0_t), sr(R, ctx->sig0_r);
+  if (sigma_t) st.assign(sigma_t, sigma_t + R);
+  if (sigma_r) sr.assign(sigma_r, sigma_r + R);
+  if (beta) CK(cudaMemcpy(ctx->d_beta, beta, R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_sig_t, st.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_sig_r, sr.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_energy, etot.data(), R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(ctx->d_counts, 0, 2 * R * sizeof(long long)));
+  return G6_OK;
+}
+
+static McArgs mc_args(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter) {
+  McArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.n = ctx->n; a.ntrial = ntrial;
+  a.rep = rep_dev(ctx);
+  for (int q = 0; q < MAXSITE; ++q)
+    for (int k = 0; k < 3; ++k) { a.body[q][k] = ctx->mh.body[q][k]; a.fbody[q][k] = (float)ctx->mh.body[q][k]; }
+  a.st = ctx->d_st; a.pk64 = ctx->d_pk64; a.pk32f = (float*)ctx->d_pk32; a.fix = ctx->d_fix;
+  a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
+  a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.seed = seed; a.counter = counter;
+  a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
+  for (int r = 0; r < ctx->nrep; ++r) a.ncmax = std::max(a.ncmax, ctx->off[r + 1] - ctx->off[r]);
+  return a;
+}
+
+// Order-parameter state (first use) and its kind, reference histogram and
+// umbrellas for one call.
+static int op_setup(g6_ctx* ctx, int kind, const double* refhist, int logarithmic, const double* umbrella) {
+  if (kind < G6_OP_EP || kind > G6_OP_TRIANGLE) return fail(ctx, G6_ERR_ARG, "unknown order parameter");
+  if (kind == G6_OP_TRIANGLE) {
+    if (!refhist) return fail(ctx, G6_ERR_ARG, "the triangle order parameter needs a reference histogram");
+    double sum = 0.0;
+    for (int b = 0; b < OP_NBIN; ++b) {
+      if (!(refhist[b] >= 0.0) || !std::isfinite(refhist[b]))
+        return fail(ctx, G6_ERR_ARG, "reference histogram entries must be finite and >= 0");
+      sum += refhist[b];
+    }
+    if (!(sum > 0.0)) return fail(ctx, G6_ERR_ARG, "reference histogram is empty");
+  }
+  const int n = ctx->n, R = ctx->nrep;
+  OpDev& o = ctx->opd;
+  if (!ctx->have_op) {
+    CK(dalloc(ctx, &o.n5c, n)); CK(dalloc(ctx, &o.n5j, (size_t)n * OP_N5)); CK(dalloc(ctx, &o.n5v, (size_t)n * OP_N5));
+    CK(dalloc(ctx, &o.bc, n)); CK(dalloc(ctx, &o.bj, (size_t)n * OP_NB));
+    CK(dalloc(ctx, &o.bq, (size_t)n * OP_NB * OP_NM)); CK(dalloc(ctx, &o.qs, (size_t)n * OP_NM));
+    CK(dalloc(ctx, &o.nb, n)); CK(dalloc(ctx, &o.q6, n));
+    CK(dalloc(ctx, &o.hist, (size_t)R * OP_NBIN)); CK(dalloc(ctx, &o.op, R)); CK(dalloc(ctx, &o.flag, 1));
+    CK(dalloc(ctx, &ctx->d_umb, 2 * (size_t)R));
+    ctx->have_op = true;
+  }
+  o.kind = kind;
+  o.logarithmic = logarithmic ? 1 : 0;
+  for (int b = 0; b < OP_NBIN; ++b) o.ref[b] = refhist ? refhist[b] : 0.0;
+  o.umb = ctx->d_umb;
+  o.opsamp = nullptr;
+  if (umbrella) CK(cudaMemcpy(ctx->d_umb, umbrella, 2 * (size_t)R * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemsetAsync(o.flag, 0, sizeof(int), ctx->stream));
+  return G6_OK;
+}
+
 int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const double* beta, const double* sigma_t,
               const double* sigma_r, int mode, int sample_every, double* samples, int64_t* counts, double* energy,
               double* trace) {
@@ -2111,21 +2191,8 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   if (mode == G6_MC_LEARNED && !ctx->have_mlp) return fail(ctx, G6_ERR_STATE, "no trained network (g6_mlp_set / g6_mlp_train)");
   if (sample_every < 0) return fail(ctx, G6_ERR_ARG, "sample_every must be >= 0");
   const int R = ctx->nrep;
-  // current energies of every chain from a full force evaluation (also places the poses)
-  rc = force_once(ctx);
-  if (rc) return rc;
-  std::vector<double> e(ctx->n), etot(R, 0.0);
-  CK(cudaMemcpy(e.data(), ctx->d_emol, ctx->n * sizeof(double), cudaMemcpyDeviceToHost));
-  for (int r = 0; r < R; ++r)
-    for (int i = ctx->off[r]; i < ctx->off[r + 1]; ++i) etot[r] += e[i];
-  std::vector<double> st(R, ctx->sig0_t), sr(R, ctx->sig0_r);
-  if (sigma_t) st.assign(sigma_t, sigma_t + R);
-  if (sigma_r) sr.assign(sigma_r, sigma_r + R);
-  CK(cudaMemcpy(ctx->d_beta, beta, R * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_sig_t, st.data(), R * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_sig_r, sr.data(), R * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_energy, etot.data(), R * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemset(ctx->d_counts, 0, 2 * R * sizeof(long long)));
+  std::vector<double> etot;
+  if ((rc = mc_begin(ctx, beta, sigma_t, sigma_r, etot))) return rc;
   const int nsamples = sample_every > 0 ? ntrial / sample_every : 0;
   if (samples && nsamples > 0)
     if ((rc = grow(ctx, (void**)&ctx->d_samples, &ctx->samples_cap, (size_t)R * nsamples * sizeof(double), false))) return rc;
@@ -2137,18 +2204,10 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
     if ((rc = grow(ctx, (void**)&ctx->d_rec, &ctx->rec_cap, need, true))) return rc;
     rec_out = ctx->d_rec + (size_t)ctx->nrec * MLP_REC;
   }
-  McArgs a;
-  std::memset(&a, 0, sizeof a);
-  a.n = ctx->n; a.ntrial = ntrial; a.nsamples = nsamples; a.sample_every = samples ? sample_every : 0;
-  a.rep = rep_dev(ctx);
-  for (int q = 0; q < MAXSITE; ++q)
-    for (int k = 0; k < 3; ++k) { a.body[q][k] = ctx->mh.body[q][k]; a.fbody[q][k] = (float)ctx->mh.body[q][k]; }
-  a.st = ctx->d_st; a.pk64 = ctx->d_pk64; a.pk32f = (float*)ctx->d_pk32; a.fix = ctx->d_fix;
-  a.pc = ctx->pc; a.cc = ctx->cc; a.beta = ctx->d_beta; a.sigma_t = ctx->d_sig_t; a.sigma_r = ctx->d_sig_r;
-  a.energy = ctx->d_energy; a.counts = ctx->d_counts; a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
-  a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out; a.seed = seed; a.counter = counter;
-  a.fcache = ctx->d_fcache; a.flag = ctx->d_mcflag; a.udir = ctx->d_udir;
-  for (int r = 0; r < R; ++r) a.ncmax = std::max(a.ncmax, ctx->off[r + 1] - ctx->off[r]);
+  McArgs a = mc_args(ctx, ntrial, seed, counter);
+  a.nsamples = nsamples; a.sample_every = samples ? sample_every : 0;
+  a.samples = (samples && nsamples) ? ctx->d_samples : nullptr;
+  a.trace = trace ? ctx->d_trace : nullptr; a.records = rec_out;
   a.mlp = mlp_dev(ctx);
   CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
   if (ntrial > 0) CK(launch_mc(a, ctx->model, ctx->prec == G6_MIXED, mode, ctx->stream));
@@ -2165,6 +2224,76 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
   if (mcflag) return fail(ctx, G6_ERR_CAPACITY, "more than 64 molecules within 6 A of a Monte Carlo pose");
   if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
   drop_graphs(ctx);   // poses changed outside the MD state machine
+  return G6_OK;
+}
+
+int g6_order_parameter(g6_ctx* ctx, int kind, const double* refhist, int logarithmic, double* op) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (!op) return fail(ctx, G6_ERR_ARG, "op is required");
+  if ((rc = op_setup(ctx, kind, refhist, logarithmic, nullptr))) return rc;
+  std::vector<double> etot;
+  if ((rc = mc_begin(ctx, nullptr, nullptr, nullptr, etot))) return rc;
+  McArgs a = mc_args(ctx, 0, 0, 0);
+  CK(launch_op_prepare(a, ctx->opd, ctx->stream));
+  int flag = 0;
+  CK(cudaMemcpyAsync(op, ctx->opd.op, ctx->nrep * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&flag, ctx->opd.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (flag) return fail(ctx, G6_ERR_CAPACITY, "more than 48 molecules within 5 A or more than 10 bonds of a molecule");
+  return G6_OK;
+}
+
+int g6_mc_run_umbrella(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const double* beta,
+                       const double* sigma_t, const double* sigma_r, int kind, const double* umbrella,
+                       const double* refhist, int logarithmic, double* op, int sample_every, double* samples,
+                       double* op_samples, int64_t* counts, double* energy, double* trace) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (ntrial < 0 || !beta || !sigma_t || !sigma_r || !umbrella)
+    return fail(ctx, G6_ERR_ARG, "ntrial >= 0, beta, widths and umbrellas are required");
+  if (sample_every < 0) return fail(ctx, G6_ERR_ARG, "sample_every must be >= 0");
+  const int R = ctx->nrep;
+  for (int r = 0; r < 2 * R; ++r)
+    if (!std::isfinite(umbrella[r])) return fail(ctx, G6_ERR_ARG, "umbrella parameters must be finite");
+  if ((rc = op_setup(ctx, kind, refhist, logarithmic, umbrella))) return rc;
+  std::vector<double> etot;
+  if ((rc = mc_begin(ctx, beta, sigma_t, sigma_r, etot))) return rc;
+  const int nsamples = sample_every > 0 ? ntrial / sample_every : 0;
+  if ((samples || op_samples) && nsamples > 0) {
+    if ((rc = grow(ctx, (void**)&ctx->d_samples, &ctx->samples_cap, (size_t)R * nsamples * sizeof(double), false))) return rc;
+    if ((rc = grow(ctx, (void**)&ctx->d_opsamp, &ctx->opsamp_cap, (size_t)R * nsamples * sizeof(double), false))) return rc;
+  }
+  if (trace && ntrial > 0)
+    if ((rc = grow(ctx, (void**)&ctx->d_trace, &ctx->trace_cap, (size_t)R * ntrial * 5 * sizeof(double), false))) return rc;
+  McArgs a = mc_args(ctx, ntrial, seed, counter);
+  const bool sampling = (samples || op_samples) && nsamples > 0;
+  a.nsamples = nsamples; a.sample_every = sampling ? sample_every : 0;
+  a.samples = sampling ? ctx->d_samples : nullptr;
+  a.trace = trace ? ctx->d_trace : nullptr;
+  OpDev o = ctx->opd;
+  o.opsamp = sampling ? ctx->d_opsamp : nullptr;
+  CK(cudaMemsetAsync(ctx->d_mcflag, 0, sizeof(int), ctx->stream));
+  CK(launch_op_prepare(a, o, ctx->stream));
+  if (ntrial > 0) CK(launch_mc_op(a, o, ctx->model, ctx->prec == G6_MIXED, ctx->stream));
+  std::vector<long long> cnt(2 * R);
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, o.flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(etot.data(), ctx->d_energy, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(cnt.data(), ctx->d_counts, 2 * R * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+  if (op) CK(cudaMemcpyAsync(op, o.op, R * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (sampling && samples)
+    CK(cudaMemcpyAsync(samples, ctx->d_samples, (size_t)R * nsamples * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (sampling && op_samples)
+    CK(cudaMemcpyAsync(op_samples, ctx->d_opsamp, (size_t)R * nsamples * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (a.trace) CK(cudaMemcpyAsync(trace, ctx->d_trace, (size_t)R * ntrial * 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (energy) for (int r = 0; r < R; ++r) energy[r] = etot[r];
+  if (counts) for (int k = 0; k < 2 * R; ++k) counts[k] = cnt[k];
+  drop_graphs(ctx);   // poses changed outside the MD state machine
+  if (flag)
+    return fail(ctx, G6_ERR_CAPACITY,
+                "order parameter: more than 48 molecules within 5 A, 10 bonds of a molecule or 64 molecules near a trial");
   return G6_OK;
 }
 

@@ -187,6 +187,47 @@ class RigidWater:
         return {"accepted": counts[0::2].copy(), "trials": counts[1::2].copy(), "energy": energy,
                 "samples": samples[:, :nsm], "trace": tr}
 
+    _OP_KINDS = {"ep": _capi.OP_EP, "q6": _capi.OP_Q6, "triangle": _capi.OP_TRIANGLE}
+
+    def order_parameter(self, kind, refhist=None, logarithmic=False):
+        """Order parameter of every chain at the current state (g6_order_parameter):
+        kind "q6" (local Q6, Q6Local.F90), "triangle" (divergence of the
+        4-neighbour angle histogram from refhist, Triangle.F90) or "ep"."""
+        op = np.zeros(self.nrep)
+        ref = None if refhist is None else np.ascontiguousarray(refhist, dtype=np.float64)
+        self._check(self.L.g6_order_parameter(self.ctx, self._OP_KINDS[kind], dptr(ref), int(bool(logarithmic)),
+                                              dptr(op)))
+        return op
+
+    def mc_run_umbrella(self, ntrial, seed, counter, beta, kind, center, coeff, sigma_t=0.15, sigma_r=0.15,
+                        refhist=None, logarithmic=False, sample_every=0, trace=False):
+        """Umbrella Monte Carlo (g6_mc_run_umbrella): fixed-width trials with
+        coeff (op - center)^2 on the order parameter `kind` added to dE in the
+        Metropolis test (mc2.F90:684-722).  center, coeff and the other
+        parameters are scalars or per-chain arrays.  Returns accepted/trial
+        counts, energies, final order parameters, sampled energies and order
+        parameters and, with trace=True, (dE, energy, accepted, target, op) per
+        trial."""
+        R = self.nrep
+        per = lambda v: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (R,)))
+        beta, st, sr = per(beta), per(sigma_t), per(sigma_r)
+        umb = np.ascontiguousarray(np.stack([per(center), per(coeff)], axis=1))
+        ref = None if refhist is None else np.ascontiguousarray(refhist, dtype=np.float64)
+        counts = np.zeros(2 * R, np.int64)
+        energy = np.zeros(R)
+        op = np.zeros(R)
+        nsm = ntrial // sample_every if sample_every else 0
+        samples = np.zeros((R, max(nsm, 1)))
+        opsamp = np.zeros((R, max(nsm, 1)))
+        tr = np.zeros((R, ntrial, 5)) if trace else None
+        self._check(self.L.g6_mc_run_umbrella(
+            self.ctx, int(ntrial), int(seed), int(counter), dptr(beta), dptr(st), dptr(sr), self._OP_KINDS[kind],
+            dptr(umb), dptr(ref), int(bool(logarithmic)), dptr(op), int(sample_every), dptr(samples) if nsm else None,
+            dptr(opsamp) if nsm else None, counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(energy),
+            dptr(tr)))
+        return {"accepted": counts[0::2].copy(), "trials": counts[1::2].copy(), "energy": energy, "op": op,
+                "samples": samples[:, :nsm], "op_samples": opsamp[:, :nsm], "trace": tr}
+
     def last_epot(self):
         """Potential energy of each replica at the last MD step (g6_last_epot)."""
         e = np.zeros(self.nrep)

@@ -349,6 +349,44 @@ int g6_mc_run(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const do
               const double* sigma_r, int mode, int sample_every, double* samples, int64_t* counts, double* energy,
               double* trace);
 
+/* Order parameters of umbrella Monte Carlo (mc2.F90 OP_EP, OP_Q6T,
+   OP_TRIANGLE), per chain (replica):
+   G6_OP_EP        the chain's potential energy;
+   G6_OP_Q6        local Q6 (Q6Local.F90): bonds are pairs within 3 A, the
+                   neighbourhood of a molecule is itself and the molecules
+                   within 5 A, q6(k) = sqrt(4 pi/13 sum_m |sum Y_6m(b)|^2) /
+                   nbond(k) over the directed bonds b with both ends in k's
+                   neighbourhood; op = mean of q6 over the chain;
+   G6_OP_TRIANGLE  Triangle.F90: the cosines of the angles spanned at every
+                   molecule by its (at most) 4 nearest neighbours within 5 A,
+                   in G6_OP_NBIN bins of 0.1 on [-1, 1]; op = Kullback
+                   divergence of that histogram from refhist (its log when
+                   logarithmic != 0).
+   Distances use the minimum image of the COMs.  A bond along the z axis
+   (x = y = 0) gives 0/0 in e^{i phi} as in the reference. */
+#define G6_OP_EP 0
+#define G6_OP_Q6 1
+#define G6_OP_TRIANGLE 2
+#define G6_OP_NBIN 21
+/* op[nrep] of the current state (refhist[G6_OP_NBIN] for G6_OP_TRIANGLE). */
+int g6_order_parameter(g6_ctx* ctx, int kind, const double* refhist, int logarithmic, double* op);
+/* g6_mc_run (G6_MC_PLAIN proposal) with a parabolic umbrella per chain,
+   umbrella[nrep][2] = (center, coeff), on the order parameter `kind`: the
+   trial's order parameter is evaluated incrementally on the device
+   (Differentiate / Integrate / Reject of Q6Local.F90 and Triangle.F90) and
+   coeff (op_new - center)^2 - coeff (op - center)^2 is added to dE in the
+   Metropolis test (mc2.F90:684-722).  op[nrep] (optional) gets the final
+   order parameters, samples/op_samples (optional, nrep x ntrial/sample_every)
+   the running energy and order parameter, trace (optional, nrep x ntrial x
+   5) dE, energy, accepted, target and op per trial.  Returns
+   G6_ERR_CAPACITY when a molecule has more than 48 neighbours within 5 A or
+   more than 10 bonds, or a trial more than 64 molecules within 5 A of its
+   two poses. */
+int g6_mc_run_umbrella(g6_ctx* ctx, int ntrial, uint64_t seed, uint64_t counter, const double* beta,
+                       const double* sigma_t, const double* sigma_r, int kind, const double* umbrella,
+                       const double* refhist, int logarithmic, double* op, int sample_every, double* samples,
+                       double* op_samples, int64_t* counts, double* energy, double* trace);
+
 /* Proposal-width network: 24 local-environment features -> 64 -> 64 (tanh)
    -> 2 widths, sigma = sigma0 * (0.1 + 2.9 sigmoid(z)).  Parameters are one
    float array of G6_MLP_NPARAM values: W1[64][24], b1[64], W2[64][64],

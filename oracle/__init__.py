@@ -80,6 +80,11 @@ def lib():
                                             dp, dp, dp, dp, dp]
         L.orc_force_sites_hetero.argtypes = [c_int, c_int, c_int, dp, dp, dp, dp, dp, dp, c_int, c_int, c_long, ip,
                                              ip, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_order_parameter.restype = c_double
+        L.orc_order_parameter.argtypes = [c_int, c_int, dp, dp, dp, c_int, c_double, dp, dp]
+        L.orc_mc_umbrella_run.argtypes = [c_int, c_int, c_int, dp, dp, dp, c_double, c_double, c_double, c_double,
+                                          c_double, c_int, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, c_int,
+                                          c_double, c_double, dp, c_int, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -269,6 +274,39 @@ def mc_run(model, path, com, quat, L, rin, rc, beta, sig_t, sig_r, ntrial, seed,
     lib().orc_mc_run(MODEL[model], PATH[path], com.shape[0], com, quat, _f64(L), rin, rc, beta, sig_t, sig_r, ntrial,
                      seed, chain, counter, e, trace)
     return com, quat, e[0], trace
+
+
+OP_EP, OP_Q6, OP_TRIANGLE = 0, 1, 2
+
+
+def order_parameter(kind, com, L, ref=None, logarithmic=False, energy=0.0):
+    """Order parameter of one configuration (kind OP_Q6: local Q6, Q6Local.F90;
+    OP_TRIANGLE: divergence of the 4-neighbour angle histogram from ref,
+    Triangle.F90; OP_EP: the given energy).  Returns (op, per-molecule q6 (n),
+    triangle counts (21))."""
+    com = _f64(com)
+    n = com.shape[0]
+    q6 = np.zeros(n)
+    hist = np.zeros(21)
+    refv = _f64(np.ones(21) if ref is None else ref)
+    op = lib().orc_order_parameter(int(kind), n, com, _f64(L), refv, int(bool(logarithmic)), float(energy), q6, hist)
+    return op, q6, hist
+
+
+def mc_umbrella_run(model, path, com, quat, L, rin, rc, beta, sig_t, sig_r, ntrial, seed, chain, counter, kind, center,
+                    coeff, energy, op, ref=None, logarithmic=False):
+    """Umbrella Monte Carlo chain on the CPU (same draws as the device).
+    Returns com, quat, energy, op, trace (ntrial, 5): dE, energy, accepted, target, op."""
+    com = np.ascontiguousarray(com, dtype=np.float64).copy()
+    quat = np.ascontiguousarray(quat, dtype=np.float64).copy()
+    e = np.array([energy], dtype=np.float64)
+    o = np.array([op], dtype=np.float64)
+    trace = np.zeros((ntrial, 5))
+    refv = _f64(np.ones(21) if ref is None else ref)
+    lib().orc_mc_umbrella_run(MODEL[model], PATH[path], com.shape[0], com, quat, _f64(L), rin, rc, beta, sig_t, sig_r,
+                              ntrial, seed, chain, counter, int(kind), center, coeff, refv, int(bool(logarithmic)), e, o,
+                              trace)
+    return com, quat, e[0], o[0], trace
 
 
 def vreset2(model, n, temp, dt, u):

@@ -22,6 +22,7 @@
 // 0-based here; the reference is 1-based.
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1139,6 +1140,183 @@ void std_force_threaded(const Model& m, const double* x, const double* y, const 
   for (int c = 0; c < 9; ++c) vir[c] = v[c];
 }
 
+
+// ---------------------------------------------------------------------------
+// Order parameters of umbrella Monte Carlo (mc2.F90:505-520, 684-705):
+// OP_Q6T (Q6Local.F90 sq6system_prepareall :98-223), OP_TRIANGLE
+// (Triangle.F90 sTriangle_prepareall :53-100), each computed from scratch
+// for a configuration -- the value the reference's incremental
+// Differentiate/Integrate must reproduce (its own DEBUG3 check, mc2.F90:745-760).
+// ---------------------------------------------------------------------------
+// Separation of molecule b seen from a, as neighbors_all2 stores it
+// (Neighbor.F90:85-130): dx = ca - cb - o with the Compress2 image o, the
+// entry of nei(a) holds -dx; returns dd = dx^2 + dy^2 + dz^2.
+inline double nb_vec(const double* a, const double* b, const double L[3], const double iL[3], double v[3]) {
+  double d[3];
+  for (int k = 0; k < 3; ++k) {
+    const double delta = a[k] - b[k];
+    const double o = dnint(delta * iL[k]) * L[k];
+    d[k] = delta - o;
+    v[k] = -d[k];
+  }
+  return d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+}
+
+struct NbEntry { int j; double v[3]; double dd; };
+
+// Neighbours of every molecule with dd <= radius^2 (the reference's
+// `radius**2 < dd` rejection), ordered by label (ORDER_BY_LABEL).
+std::vector<std::vector<NbEntry>> neighbours_within(int n, const double* com, const double L[3], double radius) {
+  const double iL[3] = {1.0 / L[0], 1.0 / L[1], 1.0 / L[2]};
+  std::vector<std::vector<NbEntry>> nb(n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      NbEntry e;
+      e.j = j;
+      e.dd = nb_vec(com + 3 * i, com + 3 * j, L, iL, e.v);
+      if (!(radius * radius < e.dd)) nb[i].push_back(e);
+    }
+  return nb;
+}
+
+// Associated Legendre function P_l^m(x), 0 <= m <= l (the upward recurrence of
+// q6.F90 plgndr :69-100).
+double legendre_plm(int l, int m, double x) {
+  double pmm = 1.0;
+  if (m > 0) {
+    const double somx2 = std::sqrt((1.0 - x) * (1.0 + x));
+    double fact = 1.0;
+    for (int i = 1; i <= m; ++i) { pmm = -pmm * fact * somx2; fact = fact + 2.0; }
+  }
+  if (l == m) return pmm;
+  double pmmp1 = x * (2 * m + 1) * pmm;
+  if (l == m + 1) return pmmp1;
+  double pll = 0.0;
+  for (int ll = m + 2; ll <= l; ++ll) {
+    pll = (x * (2 * ll - 1) * pmmp1 - (ll + m - 1) * pmm) / (ll - m);
+    pmm = pmmp1;
+    pmmp1 = pll;
+  }
+  return pll;
+}
+
+struct Cplx { double re, im; };
+inline Cplx cmul(Cplx a, Cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+
+// q_6m of a bond along (x, y, z), |(x,y,z)| = 1: the spherical harmonic Y_6m
+// with cos(theta) = z and e^{i phi} = (x + iy)/sqrt(x^2 + y^2) (q6.F90 qlm,
+// ylm2, ylm :24-66), m = -6..6 at index m + 6.
+void q6_of_bond(double x, double y, double z, Cplx out[13]) {
+  static const double fact[13] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0, 3628800.0,
+                                  39916800.0, 479001600.0};
+  const double rxy = std::sqrt(x * x + y * y);
+  const Cplx w = {x / rxy, y / rxy};
+  Cplx wm = {1.0, 0.0};
+  for (int m = 0; m <= 6; ++m) {
+    if (m > 0) wm = cmul(wm, w);
+    const double norm = std::sqrt((2.0 * 6 + 1.0) * fact[6 - m] / (4.0 * PI * fact[6 + m]));
+    const double p = norm * legendre_plm(6, m, z);
+    const Cplx y6 = {p * wm.re, p * wm.im};
+    out[6 + m] = y6;
+    if (m > 0) {
+      const double sg = (m & 1) ? -1.0 : 1.0;   // Y_{6,-m} = (-1)^m conj(Y_6m)
+      out[6 - m] = {sg * y6.re, -sg * y6.im};
+    }
+  }
+}
+
+// Local Q6 (sq6system_prepareall): bonds are pairs within 3 A, the
+// neighbourhood of a molecule is itself plus the molecules within 5 A, and
+// q6(k) = sqrt(4 pi / 13 sum_m |sum q_6m(b)|^2) / nbond(k) over the directed
+// bonds b = (i -> j) with both i and j in k's neighbourhood; the order
+// parameter is the mean of q6 over the molecules.
+double op_q6(int n, const double* com, const double L[3], double* q6out) {
+  auto nei5 = neighbours_within(n, com, L, 5.0);
+  auto in5 = [&](int k, int j) {
+    if (j == k) return true;
+    for (const NbEntry& e : nei5[k]) if (e.j == j) return true;
+    return false;
+  };
+  std::vector<std::array<Cplx, 13>> qsum(n);
+  std::vector<int> nbond(n, 0);
+  for (auto& q : qsum) for (auto& c : q) c = {0.0, 0.0};
+  for (int i = 0; i < n; ++i)
+    for (const NbEntry& b : nei5[i]) {
+      if (9.0 < b.dd) continue;   // nei3: bonds within 3 A
+      const double pp = 1.0 / std::sqrt(b.dd);
+      Cplx q[13];
+      q6_of_bond(b.v[0] * pp, b.v[1] * pp, b.v[2] * pp, q);
+      // neib = neis(i) ^ neis(j): k = i, j and the common neighbours
+      std::vector<int> ks = {i};
+      for (const NbEntry& e : nei5[i]) if (in5(b.j, e.j)) ks.push_back(e.j);
+      for (int k : ks) {
+        nbond[k] += 1;
+        for (int m = 0; m < 13; ++m) { qsum[k][m].re += q[m].re; qsum[k][m].im += q[m].im; }
+      }
+    }
+  double sum = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double s2 = 0.0;
+    for (int m = 0; m < 13; ++m) {
+      const double a = std::hypot(qsum[k][m].re, qsum[k][m].im);
+      s2 = s2 + a * a;
+    }
+    const double q6 = std::sqrt(s2 * 4.0 * PI / (2.0 * 6 + 1.0)) / nbond[k];
+    if (q6out) q6out[k] = q6;
+    sum = sum + q6;
+  }
+  return sum / n;
+}
+
+// Histogram bin (DistribModule.F90 histogram_accumulate): nint((x - min) /
+// width) + 1, kept when 1 <= bin <= nbin; 0-based here, -1 when outside.
+inline int tri_bin(double costh) {
+  const int bin = (int)dnint((costh - (-1.0)) / 0.1);
+  return (bin >= 0 && bin < 21) ? bin : -1;
+}
+
+// kullback_div (DistribModule.F90:304-326) of counts h against the reference
+// histogram ref (21 bins each).
+double kullback(const double* h, const double* ref) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = 0; i < 21; ++i) { s1 = s1 + h[i]; s2 = s2 + ref[i]; }
+  double div = 0.0;
+  for (int i = 0; i < 21; ++i) {
+    const double p = h[i] / s1;
+    double q = ref[i] / s2;
+    if (q == 0) q = p;
+    if (p != 0) div = div + p * std::log(p / q);
+  }
+  return div;
+}
+
+// Triangle order parameter (sTriangle_prepareall): for every molecule its (at
+// most) 4 nearest neighbours within 5 A, the cosines of the 6 angles they
+// span at the molecule in a 21-bin histogram on [-1, 1], and the Kullback
+// divergence of that histogram from ref (its log when logarithmic).  Equal
+// distances are ordered by label.
+double op_triangle(int n, const double* com, const double L[3], const double* ref, int logarithmic, double* hist) {
+  auto nei = neighbours_within(n, com, L, 5.0);
+  double h[21] = {0.0};
+  for (int i = 0; i < n; ++i) {
+    std::vector<NbEntry>& v = nei[i];
+    std::stable_sort(v.begin(), v.end(), [](const NbEntry& a, const NbEntry& b) { return a.dd < b.dd; });
+    const int m = std::min<int>(4, (int)v.size());
+    for (int a = 0; a < m; ++a)
+      for (int b = a + 1; b < m; ++b) {
+        double c = v[a].v[0] * v[b].v[0] + v[a].v[1] * v[b].v[1] + v[a].v[2] * v[b].v[2];
+        c = c / std::sqrt(v[a].dd * v[b].dd);
+        const int bin = tri_bin(c);
+        if (bin >= 0) h[bin] = h[bin] + 1.0;
+      }
+  }
+  if (hist) for (int i = 0; i < 21; ++i) hist[i] = h[i];
+  double op = kullback(h, ref);
+  if (logarithmic) op = std::log(op);
+  return op;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1537,6 +1715,85 @@ int orc_replica_exchange_trial(int j, int jj, int* node_in_charge, double u, con
     node_in_charge[jj] = n0;
   }
   return accept ? 1 : 0;
+}
+
+// Order parameter `kind` (0: potential energy, given; 1: local Q6; 2:
+// triangle histogram divergence) of one configuration com (n,3).  q6 (n,
+// optional) gets the per-molecule Q6, hist (21, optional) the triangle counts.
+double orc_order_parameter(int kind, int n, const double* com, const double* L, const double* ref, int logarithmic,
+                           double energy, double* q6, double* hist) {
+  if (kind == 1) return op_q6(n, com, L, q6);
+  if (kind == 2) return op_triangle(n, com, L, ref, logarithmic, hist);
+  return energy;
+}
+
+// Umbrella Monte Carlo chain: orc_mc_run's trials with the order parameter of
+// the trial configuration (mc2.F90:684-697; computed from scratch here) and
+// the umbrella term coeff (op - center)^2 (Umbrella.F90:11-16) added to dE in
+// the Metropolis test (mc2.F90:700-722).  op (1) is the current order
+// parameter (in/out); trace (ntrial,5) gets dE, energy, accepted, target, op.
+int orc_mc_umbrella_run(int model, int path, int n, double* com, double* quat, const double* L, double rin, double rc,
+                        double beta, double sig_t, double sig_r, int ntrial, uint64_t seed, uint32_t chain,
+                        uint64_t counter, int kind, double center, double coeff, const double* ref, int logarithmic,
+                        double* energy, double* op, double* trace) {
+  Model m;
+  if (!make_model(model, m)) return 1;
+  double e = *energy, o = *op;
+  std::vector<double> trial_com(com, com + 3 * (size_t)n);
+  for (int t = 0; t < ntrial; ++t) {
+    const uint64_t trial = counter + (uint64_t)t;
+    const uint32_t lo = (uint32_t)trial, hi = (uint32_t)(trial >> 32);
+    double u0[2];
+    uniform2(seed, chain, lo, hi, 0u, u0);
+    int tg = (int)(u0[0] * n);
+    if (tg >= n) tg = n - 1;
+    double rot[3], dx[3];
+    for (int k = 0; k < 3; ++k) {
+      double u[2];
+      uniform2(seed, chain, lo, hi, 1u + k, u);
+      rot[k] = random_normal(0.0, sig_r * sig_r, u[0], u[1]);
+    }
+    for (int k = 0; k < 3; ++k) {
+      double u[2];
+      uniform2(seed, chain, lo, hi, 4u + k, u);
+      dx[k] = random_normal(0.0, sig_t * sig_t, u[0], u[1]);
+    }
+    double a = 1.0, b = rot[0], c = rot[1], d = rot[2];
+    const double r = 1.0 / std::sqrt(a * a + b * b + c * c + d * d);
+    a *= r; b *= r; c *= r; d *= r;
+    const double* qo = quat + 4 * tg;
+    double qn[4] = {a * qo[0] - b * qo[1] - c * qo[2] - d * qo[3], a * qo[1] + b * qo[0] + c * qo[3] - d * qo[2],
+                    a * qo[2] + c * qo[0] - b * qo[3] + d * qo[1], a * qo[3] + d * qo[0] + b * qo[2] - c * qo[1]};
+    if (qn[0] < 0) for (int k = 0; k < 4; ++k) qn[k] = -qn[k];
+    double cn[3] = {com[3 * tg] + dx[0], com[3 * tg + 1] + dx[1], com[3 * tg + 2] + dx[2]};
+    const double eo = orc_molecule_energy(model, path, n, com, quat, tg, com + 3 * tg, quat + 4 * tg, L, rin, rc);
+    const double en = orc_molecule_energy(model, path, n, com, quat, tg, cn, qn, L, rin, rc);
+    const double dE = en - eo;
+    double newop;
+    if (kind == 0) {
+      newop = e + dE;
+    } else {
+      for (int k = 0; k < 3; ++k) trial_com[3 * tg + k] = cn[k];
+      newop = orc_order_parameter(kind, n, trial_com.data(), L, ref, logarithmic, 0.0, nullptr, nullptr);
+      for (int k = 0; k < 3; ++k) trial_com[3 * tg + k] = com[3 * tg + k];
+    }
+    const double dU = coeff * ((newop - center) * (newop - center)) - coeff * ((o - center) * (o - center));
+    const double x = -((dE + dU) * I2J * J2K) * beta;
+    const bool acc = x >= 0.0 || u0[1] < std::exp(x);
+    if (acc) {
+      for (int k = 0; k < 3; ++k) { com[3 * tg + k] = cn[k]; trial_com[3 * tg + k] = cn[k]; }
+      for (int k = 0; k < 4; ++k) quat[4 * tg + k] = qn[k];
+      e += dE;
+      o = newop;
+    }
+    if (trace) {
+      double* tr = trace + 5 * (size_t)t;
+      tr[0] = dE; tr[1] = e; tr[2] = acc ? 1.0 : 0.0; tr[3] = tg; tr[4] = o;
+    }
+  }
+  *energy = e;
+  *op = o;
+  return 0;
 }
 
 int orc_max_threads() {
