@@ -486,6 +486,39 @@ def mc_compare(torch, s, rec_state, beta, seed, sweeps, records, w_move, w_energ
     return out
 
 
+def bench_umbrella(torch, s, rec_state, beta, seed, sweeps=20):
+    """Umbrella chains (g6_mc_run_umbrella, mc2.F90:684-830) on the same 32 x 1,024 ST2
+    state: fixed widths 0.15 A / 0.15 rad, an umbrella centred at each chain's current order
+    parameter, `sweeps` sweeps per kind.  Wall time per trial (all chains in parallel) next to
+    the plain chain's, and the incremental order parameter against a fresh evaluation."""
+    N = s.nmol[0]
+    ntr = sweeps * N
+    ref = np.ones(21)
+    coeff = {"ep": 1.0e-3, "q6": 1.0e5, "triangle": 1.0e3}
+    out = {"sweeps": sweeps, "triangle_reference": "flat (21 bins)"}
+    s.upload_state(rec_state)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.mc_run(ntr, seed + 5, 10 ** 9, beta, 0.15, 0.15)
+    torch.cuda.synchronize()
+    plain = time.perf_counter() - t0
+    out["plain_us_per_trial"] = plain / ntr * 1e6
+    for kind in ("ep", "q6", "triangle"):
+        s.upload_state(rec_state)
+        op0 = s.order_parameter(kind, refhist=ref)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = s.mc_run_umbrella(ntr, seed + 5, 10 ** 9, beta, kind, op0, coeff[kind], refhist=ref)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        fresh = s.order_parameter(kind, refhist=ref)
+        out[kind] = {"us_per_trial": wall / ntr * 1e6, "over_plain": wall / plain, "coeff": coeff[kind],
+                     "acceptance": float(r["accepted"].sum() / r["trials"].sum()),
+                     "op_start_mean": float(np.mean(op0)), "op_end_mean": float(np.mean(r["op"])),
+                     "incremental_minus_fresh_max_rel": float(np.abs(r["op"] - fresh).max() / np.abs(fresh).max())}
+    return out
+
+
 def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equil_sweeps=1000, w_move=0.0,
              w_energy=1.0, T=260.0, rc=9.0, md_steps=30000):
     """32 chains x 1,024 ST2 (custom path, Coulomb taper), T = 260 K, rc 9 A with
@@ -511,6 +544,7 @@ def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equi
     rec_state = s.download_state()
     runs = [mc_compare(torch, s, rec_state, beta, seed + 17 * k, sweeps, records, w_move, w_energy)
             for k in range(seeds)]
+    umbrella = bench_umbrella(torch, s, rec_state, beta, seed)
     s.close()
     ratios = [r["ess_per_gpu_s_learned_over_fixed"] for r in runs]
     charged = [r["with_collect_and_train_charged"] for r in runs]
@@ -524,7 +558,7 @@ def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equi
             "ess_per_gpu_s_learned_over_fixed_per_seed": ratios,
             "with_collect_and_train_charged_per_seed": charged,
             "mean_U_difference_in_sigma_per_seed": [r["mean_U_difference_in_sigma"] for r in runs],
-            "runs": runs, "U_unit": "10 J/mol per chain (internal)"}
+            "runs": runs, "umbrella": umbrella, "U_unit": "10 J/mol per chain (internal)"}
 
 
 def bench_rdf(torch, n=N_BIG, rc=9.0, nbin=200, width=0.05, reps=5, seed=20261207):
