@@ -292,15 +292,8 @@ __global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
   if (a.with_step) {
     const int* ctrl = a.s.ctrl;
     if (ctrl[4]) {
-      // the rebuild decision from the previous step's displacement test (the
-      // same in every block)
-      const int step = ctrl[1];
-      const double gmax = step_gmax(a.s);
-      rebuild = step < ctrl[2] && gmax > a.s.half_skin2;
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.s.ctrl[0] = rebuild ? 1 : 0;
-        a.s.gmax[step & 1] = 0u;   // the word of step-2, read by the previous head only
-      }
+      // the decision the previous step's last block made from its displacement test
+      rebuild = ctrl[0] != 0;
     } else if (ctrl[0] == 2) {
       // first step of a run over a list built earlier: rebuild only if some
       // molecule has moved more than half the skin since that build (the

@@ -39,6 +39,8 @@ namespace g6 {
 // Residency of k_pairs: 128 threads per block, at least MINB blocks per SM
 // (5: 96 registers, enough for the 3-charge models in the MD step without
 // spills; 4: 128 registers for the 4-charge models and the full virial).
+// Blocks of 32 or 64 threads measured the same (the SMs' 3-or-4-block split
+// of a 4,096-molecule grid is not what leaves them idle at its end).
 template <int LPI>
 struct PairShape {
   static constexpr int THREADS = 128;
@@ -80,12 +82,16 @@ __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi,
   d[2] = i32_to_f32((int)(zi - __float_as_uint(qj.z))) * sz;
 }
 
+// MODE 0: force only; 1: MD step.
 template <class M, int LPI, int MODE>
 __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MODE>::value))
     k_pairs(ForceArgs a, StepArgs sa) {
   constexpr int NW = MODE == 0 ? 9 : 1;
   int bid = blockIdx.x;
   if constexpr (MODE == 1) {
+    // the integrator kernel (a programmatic dependent launch) may start its
+    // loads now; it waits for this grid before reading forces or thermostats
+    asm volatile("griddepcontrol.launch_dependents;");
     // the first nrep blocks finish the previous step's replicas (sums,
     // thermostat, log), overlapped with the pair work of the others
     if (bid < a.rep.nrep) {
@@ -269,11 +275,21 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
   __shared__ FF s_vv[32][NRED];
   __shared__ float s_dm[32];
   __shared__ int s_bad[32], s_rr[32];
+  const int n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the state of this lane's molecule, before the pair kernel has finished
+  MixedIn min;
+  {
+    const int im = blockIdx.x * 32 + warp * MPW + lane;
+    if (lane < MPW && im < n) load_mixed(sa, im, min);
+  }
+  // forces, the thermostats and the control words are the pair kernel's (and
+  // its replica finish's) results: wait for that grid (a no-op when the kernel
+  // was not launched as its programmatic dependent)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
   const bool predict_next = step + 1 < sa.ctrl[2];
-  const int n = a.n;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane < MPW) {
     const int m = warp * MPW + lane;
     const int im = blockIdx.x * 32 + m;
@@ -289,7 +305,7 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
       const float F[3] = {h0.x + l0.x, h0.y + l0.y, h0.z + l0.z};
       const float tl[3] = {h1.x + l1.x, h1.y + l1.y, h1.z + l1.z};
       float ekt2, ekr2;
-      correct_mixed<NQ>(sa, im, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
+      correct_mixed<NQ>(sa, im, min, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
       vv[0] = FF{0.5f * h0.w, 0.5f * l0.w};
       vv[1] = FF{0.5f * h1.w, 0.5f * l1.w};
       vv[2] = FF{ekt2, 0.0f};
@@ -376,12 +392,30 @@ cudaError_t launch_finish_step(const StepArgs& sa, int nrep, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The integrator as a programmatic dependent of the pair kernel launched just
+// before it (pdl), so that its blocks start and load the state during the pair
+// kernel's tail; a plain launch when an event separates the two.
+template <int NQ, int MPW>
+static cudaError_t launch_integrate_k(const ForceArgs& a, const StepArgs& sa, int blocks, bool pdl, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(32 * (32 / MPW));
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_integrate_mixed<NQ, MPW>, a, sa);
+}
+
 template <int NQ>
-static void launch_integrate(const ForceArgs& a, const StepArgs& sa, int mpw, int blocks, cudaStream_t s) {
+static cudaError_t launch_integrate(const ForceArgs& a, const StepArgs& sa, int mpw, int blocks, bool pdl,
+                                    cudaStream_t s) {
   switch (mpw) {
-    case 8: k_integrate_mixed<NQ, 8><<<blocks, 128, 0, s>>>(a, sa); break;
-    case 16: k_integrate_mixed<NQ, 16><<<blocks, 64, 0, s>>>(a, sa); break;
-    default: k_integrate_mixed<NQ, 32><<<blocks, 32, 0, s>>>(a, sa); break;
+    case 8: return launch_integrate_k<NQ, 8>(a, sa, blocks, pdl, s);
+    case 16: return launch_integrate_k<NQ, 16>(a, sa, blocks, pdl, s);
+    default: return launch_integrate_k<NQ, 32>(a, sa, blocks, pdl, s);
   }
 }
 
@@ -396,9 +430,9 @@ cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model,
   }
   const int blocks = (a.n + 31) / 32;
   if (blocks == 0) return cudaSuccess;
-  if (model_nq(model) == 3) launch_integrate<3>(a, sa, mpw, blocks, s);
-  else launch_integrate<4>(a, sa, mpw, blocks, s);
-  return cudaGetLastError();
+  const bool pdl = between == nullptr;
+  return model_nq(model) == 3 ? launch_integrate<3>(a, sa, mpw, blocks, pdl, s)
+                              : launch_integrate<4>(a, sa, mpw, blocks, pdl, s);
 }
 
 }  // namespace g6

@@ -385,22 +385,54 @@ __device__ __forceinline__ void predict_mixed(double* st, float* stf, int n, int
 // increments of the corrector and of the predictor are summed in float and
 // each FP64 quantity receives them in one FP64 addition.  F: COM force, tl: lab
 // torque (float); outputs the kinetic sums and the displacement test.
+// The inputs of correct_mixed that depend neither on the step's forces nor on
+// the thermostat (which the pair kernel's first blocks finish): loaded
+// together, before the integrator waits for the pair kernel, so that their
+// latencies overlap each other and the pair kernel's tail.
+struct MixedIn {
+  double xd[3], d1d[3], w1d[3], qd[4];   // com, d1, w1, q (FP64 state)
+  float sd[12], sw[12], sq[4];           // d2..d5, w2..w5, q2 (float small terms)
+  double fixs[3];                        // 2^32 / L of the molecule's replica
+  uint32_t fixb[3];                      // fixed-point COM at the last list build
+  float fs[3];                           // L / 2^32
+  int r;                                 // replica
+};
+
+__device__ __forceinline__ void load_mixed(const StepArgs& a, int i, MixedIn& m) {
+  const int n = a.p.n;
+  const double* st = a.p.st;
+  const float* stf = a.stf;
+  m.r = a.p.rep.mol_rep[i];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { m.xd[c] = G6_ST(c); m.d1d[c] = G6_ST(3 + c); m.w1d[c] = G6_ST(18 + c); }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) { m.qd[c] = G6_ST(33 + c); m.sq[c] = G6_SF(STF_Q2 + c); }
+#pragma unroll
+  for (int c = 0; c < 12; ++c) { m.sd[c] = G6_SF(STF_D2 + c); m.sw[c] = G6_SF(STF_W2 + c); }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    m.fixs[c] = a.fixs[3 * m.r + c];
+    m.fixb[c] = a.fix_build[(size_t)c * n + i];
+    m.fs[c] = a.p.rep.fscale[3 * m.r + c];
+  }
+}
+
 template <int NQ>
-__device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const float F[3], const float tl[3], int step,
-                                              bool predict_next, const PoseBuf& next, float& ekt2, float& ekr2,
-                                              float& dmax2, int& bad) {
+__device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const MixedIn& m, const float F[3],
+                                              const float tl[3], int step, bool predict_next, const PoseBuf& next,
+                                              float& ekt2, float& ekr2, float& dmax2, int& bad) {
   const int n = a.p.n;
   double* st = a.p.st;
   float* stf = a.stf;
-  const int r = a.p.rep.mol_rep[i];
+  const int r = m.r;
   const ThermoDev& th = a.th[r];
   const int kind = th.kind;
   const float dt = a.fdt;
   double xd[3], d1d[3], w1d[3], qd[4];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) { xd[c] = G6_ST(c); d1d[c] = G6_ST(3 + c); w1d[c] = G6_ST(18 + c); }
+  for (int c = 0; c < 3; ++c) { xd[c] = m.xd[c]; d1d[c] = m.d1d[c]; w1d[c] = m.w1d[c]; }
 #pragma unroll
-  for (int c = 0; c < 4; ++c) qd[c] = G6_ST(33 + c);
+  for (int c = 0; c < 4; ++c) qd[c] = m.qd[c];
   float d1f[3], w1f[3], qf[4];
 #pragma unroll
   for (int c = 0; c < 3; ++c) { d1f[c] = (float)d1d[c]; w1f[c] = (float)w1d[c]; }
@@ -419,19 +451,19 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float nf = F[c] * a.fcf - d1f[c] * ext_t;
-    const float delta = nf - G6_SF(STF_D2 + c);
+    const float delta = nf - m.sd[c];
     dx_c[c] = (float)G50 * delta;
     dd1_c[c] = (float)G51 * delta;
     D[0][c] = nf;
-    D[1][c] = G6_SF(STF_D2 + 3 + c) + (float)G53 * delta;
-    D[2][c] = G6_SF(STF_D2 + 6 + c) + (float)G54 * delta;
-    D[3][c] = G6_SF(STF_D2 + 9 + c) + (float)G55 * delta;
+    D[1][c] = m.sd[3 + c] + (float)G53 * delta;
+    D[2][c] = m.sd[6 + c] + (float)G54 * delta;
+    D[3][c] = m.sd[9 + c] + (float)G55 * delta;
   }
   // quaternion value
   float nw[4], dq_c[4];
   qdot_f(w1f, qf, nw);
 #pragma unroll
-  for (int c = 0; c < 4; ++c) dq_c[c] = (float)G40 * (nw[c] * dt * 0.5f - G6_SF(STF_Q2 + c));
+  for (int c = 0; c < 4; ++c) dq_c[c] = (float)G40 * (nw[c] * dt * 0.5f - m.sq[c]);
   // angular velocity: Gear-4 with Euler's equations
   const float Ix = a.fI[0], Iy = a.fI[1], Iz = a.fI[2];
   float nfw[3], Wk[4][3], dw1_c[3];
@@ -440,12 +472,12 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   nfw[2] = (tau[2] + (Ix - Iy) * w1f[0] * w1f[1]) * dt / Iz - w1f[2] * ext_r;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float delta = nfw[c] - G6_SF(STF_W2 + c);
+    const float delta = nfw[c] - m.sw[c];
     dw1_c[c] = (float)G40 * delta;
     Wk[0][c] = nfw[c];
-    Wk[1][c] = G6_SF(STF_W2 + 3 + c) + (float)G42 * delta;
-    Wk[2][c] = G6_SF(STF_W2 + 6 + c) + (float)G43 * delta;
-    Wk[3][c] = G6_SF(STF_W2 + 9 + c) + (float)G44 * delta;
+    Wk[1][c] = m.sw[3 + c] + (float)G42 * delta;
+    Wk[2][c] = m.sw[6 + c] + (float)G43 * delta;
+    Wk[3][c] = m.sw[9 + c] + (float)G44 * delta;
   }
   // corrected d1, w1 in float (kinetic sums, quaternion stacks)
   float d1c[3], w1c[3];
@@ -560,15 +592,14 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const fl
   float w[24];
 #pragma unroll
   for (int k = 0; k < 24; ++k) w[k] = 0.0f;
-  const float* fs = a.p.rep.fscale + 3 * r;
   float dd = 0.0f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const uint32_t fw = (uint32_t)(unsigned long long)__double2ll_rn(x[c] * a.fixs[3 * r + c]);
+    const uint32_t fw = (uint32_t)(unsigned long long)__double2ll_rn(x[c] * m.fixs[c]);
     next.fix[(size_t)c * n + i] = fw;
     w[c] = __uint_as_float(fw);
     next.pk64[(size_t)i * a.p.w64 + c] = x[c];
-    const float e = (float)(int)(fw - a.fix_build[(size_t)c * n + i]) * fs[c];
+    const float e = (float)(int)(fw - m.fixb[c]) * m.fs[c];
     dd += e * e;
   }
 #pragma unroll
@@ -693,6 +724,17 @@ __device__ inline void finish_replica(const StepArgs& a, int rr, int mpb, int st
 // addition in the mixed path); the largest displacement goes to an atomic max
 // word.  The last block of each replica to arrive finishes that replica
 // (finish_replica); the last block overall advances the step counter.
+// The last block of step `step` (every block's displacement maximum is in
+// gmax[step & 1]): the next step's list decision for its head, ctrl[0] = 1
+// when some molecule has moved more than half the skin since the last build,
+// and the word the next step's blocks raise reset to 0.
+__device__ __forceinline__ void next_step_decision(const StepArgs& a, int step) {
+  __threadfence();
+  const double gm = (double)__uint_as_float(__ldcg(&a.gmax[step & 1]));
+  a.ctrl[0] = (step + 1 < a.ctrl[2] && gm > a.half_skin2) ? 1 : 0;
+  a.gmax[(step + 1) & 1] = 0u;
+}
+
 template <class V>
 __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float dmax2, int bad, int mpb, int step,
                             int ew) {
@@ -745,8 +787,9 @@ __device__ void step_reduce(const StepArgs& a, const V (&v)[NRED], int r, float 
     finish_replica(a, s_rfirst + sl, mpb, step, a.ctrl[0]);
     if (threadIdx.x == 0) a.repcnt[s_rfirst + sl] = 0;
   }
-  // (every block has read ctrl[1] before it arrives at the counter)
+  // (every block has read ctrl[0] and ctrl[1] before it arrives at the counter)
   if (threadIdx.x == 0 && atomicAdd(a.done, 1u) == gridDim.x - 1) {
+    next_step_decision(a, step);
     a.ctrl[1] = step + 1;
     a.ctrl[4] = 1;
     *a.done = 0u;
@@ -791,9 +834,12 @@ __device__ void step_partials(const StepArgs& a, const V (&v)[NRED], int r, floa
     }
   }
   __syncthreads();
-  // (every block has read ctrl[0] and ctrl[1] before it arrives at the counter)
+  // (every block has read ctrl[0] and ctrl[1] before it arrives at the counter;
+  // its displacement maximum is published before it does)
+  if (threadIdx.x == 0) __threadfence();
   if (threadIdx.x == 0 && atomicAdd(a.done, 1u) == gridDim.x - 1) {
     a.ctrl[7] = a.ctrl[0];
+    next_step_decision(a, step);
     a.ctrl[1] = step + 1;
     a.ctrl[4] = 1;
     *a.done = 0u;
@@ -807,12 +853,6 @@ __device__ void step_partials(const StepArgs& a, const V (&v)[NRED], int r, floa
 __device__ inline void finish_pending(const StepArgs& a, int rr, int mpb) {
   if (!a.ctrl[4]) return;   // no step of this run has finished yet
   finish_replica(a, rr, mpb, a.ctrl[1] - 1, a.ctrl[7]);
-}
-
-// Largest squared displacement since the last list build over the finished
-// step ctrl[1]-1.
-__device__ __forceinline__ double step_gmax(const StepArgs& a) {
-  return (double)__uint_as_float(__ldcg(&a.gmax[(a.ctrl[1] - 1) & 1]));
 }
 
 #undef G6_ST
