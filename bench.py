@@ -855,7 +855,7 @@ def run_gpu(args, rank, world, local):
     kmean = float(kms.mean())
     achieved = FLOPS_PER_PAIR["TIP4P"] * pairs / (kmean * 1e-3) / 1e12
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "step_tip4p4096_mixed.txt")
+    tpath = os.path.join(ROOT, "profiles", "k_pairs_tip4p4096_step.txt")
     if os.path.exists(tpath):
         for l in open(tpath):
             if l.startswith("traffic_bytes_per_launch:"):
