@@ -570,7 +570,7 @@ static int default_lpi(const g6_ctx* c) {
 // Molecules per warp of the mixed integrator kernel: 8 spreads a small system's
 // FP64 corrector work over more schedulers, 32 issues the fewest FP64
 // instructions for a large one.
-static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 8 : (c->n <= 24576 ? 16 : 32); }
+static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 4 : (c->n <= 24576 ? 16 : 32); }
 
 // The mixed list kernel keeps each molecule's in-range row in shared memory
 // (32/lpi rows per warp): widen lpi until the rows of a block fit.
@@ -1735,8 +1735,8 @@ static int tune_force_lpi(g6_ctx* ctx) {
 // pair on a short run; returns the best shape's time for `timed` steps.
 static int tune_step_shape(g6_ctx* ctx, cudaEvent_t e0, cudaEvent_t e1, float* best_ms) {
   static const int lcand[4] = {4, 8, 16, 32};
-  static const int mcand[3] = {8, 16, 32};
-  const int nm = ctx->prec == G6_MIXED ? 3 : 1;
+  static const int mcand[4] = {4, 8, 16, 32};   // 4: the component-parallel integrator
+  const int nm = ctx->prec == G6_MIXED ? 4 : 1;
   int bl = ctx->step_lpi, bm = ctx->step_mpw;
   float sb = 1e30f;
   for (int k = 0; k < 4; ++k) {
@@ -1846,8 +1846,8 @@ int g6_get_shape(g6_ctx* ctx, g6_shape* shape) {
 int g6_set_shape(g6_ctx* ctx, const g6_shape* shape) {
   if (!ctx || !shape) return G6_ERR_ARG;
   auto ok = [](int l) { return l == 4 || l == 8 || l == 16 || l == 32; };
-  if (!ok(shape->lpi) || !ok(shape->step_lpi) || (shape->step_mpw != 8 && shape->step_mpw != 16 && shape->step_mpw != 32))
-    return fail(ctx, G6_ERR_ARG, "lanes per molecule must be 4, 8, 16 or 32 and molecules per warp 8, 16 or 32");
+  if (!ok(shape->lpi) || !ok(shape->step_lpi) || !ok(shape->step_mpw))
+    return fail(ctx, G6_ERR_ARG, "lanes per molecule must be 4, 8, 16 or 32 and step_mpw 4, 8, 16 or 32");
   if (!(shape->skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
   if (shape->cap < 0) return fail(ctx, G6_ERR_ARG, "cap must be >= 0 (0: from the skin and density)");
   ctx->lpi = shape->lpi; ctx->step_lpi = shape->step_lpi; ctx->step_mpw = shape->step_mpw;

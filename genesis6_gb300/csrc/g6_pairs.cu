@@ -328,6 +328,67 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
   step_partials<FF>(sa, vv, rr, dmax2, bad, 32, step, 0);
 }
 
+// The component-parallel integrator: four lanes per molecule (correct_quad),
+// 8 molecules per warp, 32 per block of 128 threads.
+template <int NQ>
+__global__ void __launch_bounds__(128) k_integrate_quad(ForceArgs a, StepArgs sa) {
+  __shared__ FF s_vv[32][NRED];
+  __shared__ float s_dm[32];
+  __shared__ int s_bad[32], s_rr[32];
+  const int n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, c = lane & 3;
+  const int m = warp * 8 + (lane >> 2);
+  const int im = blockIdx.x * 32 + m;
+  const bool ok = im < n;
+  QuadIn qin;
+  if (ok) load_quad(sa, im, c, qin);
+  else quad_dummy(c, qin);
+  asm volatile("griddepcontrol.wait;" ::: "memory");   // forces, thermostats, control words (see k_integrate_mixed)
+  const int step = a.ctrl[1];
+  const bool odd = (step & 1) != 0;
+  const bool predict_next = step + 1 < sa.ctrl[2];
+  float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), l0 = h0, h1 = h0, l1 = h0;
+  if (ok) {
+    const float4* o = a.fres + (size_t)4 * im;
+    h0 = o[0]; l0 = o[1]; h1 = o[2]; l1 = o[3];
+  }
+  const float Fc = c == 0 ? h0.x + l0.x : (c == 1 ? h0.y + l0.y : (c == 2 ? h0.z + l0.z : 0.0f));
+  const float tl[3] = {h1.x + l1.x, h1.y + l1.y, h1.z + l1.z};
+  float ekt2 = 0.0f, ekr2 = 0.0f, dmax2 = 0.0f;
+  int bad = 0;
+  correct_quad<NQ>(sa, im, ok, c, qin, Fc, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
+  if (c == 0) {
+    FF vv[NRED];
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = FF{0.0f, 0.0f};
+    int rr = -1;
+    if (ok) {
+      rr = qin.r;
+      vv[0] = FF{0.5f * h0.w, 0.5f * l0.w};
+      vv[1] = FF{0.5f * h1.w, 0.5f * l1.w};
+      vv[2] = FF{ekt2, 0.0f};
+      vv[3] = FF{ekr2, 0.0f};
+      vv[4] = FF{0.5f * (float)a.npair_in[im], 0.0f};
+    } else {
+      dmax2 = 0.0f;
+      bad = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) s_vv[m][k] = vv[k];
+    s_dm[m] = dmax2; s_bad[m] = bad; s_rr[m] = rr;
+  }
+  __syncthreads();
+  FF vv[NRED];
+  float dm = 0.0f;
+  int bd = 0, rr = -1;
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) vv[k] = s_vv[lane][k];
+    dm = s_dm[lane]; bd = s_bad[lane]; rr = s_rr[lane];
+  }
+  step_partials<FF>(sa, vv, rr, dm, bd, 32, step, 0);
+}
+
 // Finish of the last step of a mixed run (one replica per block).
 __global__ void __launch_bounds__(128) k_finish_step(StepArgs sa) { finish_pending(sa, blockIdx.x, 32); }
 
@@ -410,9 +471,26 @@ static cudaError_t launch_integrate_k(const ForceArgs& a, const StepArgs& sa, in
 }
 
 template <int NQ>
+static cudaError_t launch_integrate_quad(const ForceArgs& a, const StepArgs& sa, int blocks, bool pdl, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(128);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_integrate_quad<NQ>, a, sa);
+}
+
+// mpw: molecules per warp of the one-lane-per-molecule integrator (8, 16 or
+// 32), or 4 for the component-parallel one (4 lanes per molecule).
+template <int NQ>
 static cudaError_t launch_integrate(const ForceArgs& a, const StepArgs& sa, int mpw, int blocks, bool pdl,
                                     cudaStream_t s) {
   switch (mpw) {
+    case 4: return launch_integrate_quad<NQ>(a, sa, blocks, pdl, s);
     case 8: return launch_integrate_k<NQ, 8>(a, sa, blocks, pdl, s);
     case 16: return launch_integrate_k<NQ, 16>(a, sa, blocks, pdl, s);
     default: return launch_integrate_k<NQ, 32>(a, sa, blocks, pdl, s);

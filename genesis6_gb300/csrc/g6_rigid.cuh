@@ -612,6 +612,266 @@ __device__ __forceinline__ void correct_mixed(const StepArgs& a, int i, const Mi
   if (!isfinite(dd)) { bad = 1; dmax2 = 3.0e38f; }
 }
 
+
+// ---------------------------------------------------------------------------
+// Component-parallel corrector (the mixed MD step's k_integrate_quad): four
+// lanes per molecule, lane c = lane & 3 owning component c of every vector
+// (x, y, z for c < 3; quaternion component c), so a molecule's chain of
+// dependent instructions is about a third of correct_mixed's.  The same
+// arithmetic per component as correct_mixed; full vectors come from the
+// quad's lanes by warp shuffles, and a quaternion product takes the three
+// components it needs from the lanes that own them.  Every lane of the warp
+// calls it (ok = false for a lane whose molecule does not exist: no stores).
+// ---------------------------------------------------------------------------
+struct QuadIn {
+  double xd, d1d, w1d, qd;   // component c of com, d1, w1 (c < 3) and of q
+  float sd[4], sw[4];        // component c of d2..d5 and of w2..w5 (c < 3)
+  float sq;                  // component c of q2
+  double fixs;               // 2^32 / L on axis c
+  uint32_t fixb;             // fixed-point COM word c at the last list build
+  float fs;                  // L / 2^32 on axis c
+  int r;
+};
+
+__device__ __forceinline__ void load_quad(const StepArgs& a, int i, int c, QuadIn& m) {
+  const int n = a.p.n;
+  const double* st = a.p.st;
+  const float* stf = a.stf;
+  m.r = a.p.rep.mol_rep[i];
+  m.qd = G6_ST(33 + c);
+  m.sq = G6_SF(STF_Q2 + c);
+  if (c < 3) {
+    m.xd = G6_ST(c); m.d1d = G6_ST(3 + c); m.w1d = G6_ST(18 + c);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { m.sd[k] = G6_SF(STF_D2 + 3 * k + c); m.sw[k] = G6_SF(STF_W2 + 3 * k + c); }
+    m.fixs = a.fixs[3 * m.r + c];
+    m.fixb = a.fix_build[(size_t)c * n + i];
+    m.fs = a.p.rep.fscale[3 * m.r + c];
+  } else {
+    m.xd = m.d1d = m.w1d = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { m.sd[k] = 0.0f; m.sw[k] = 0.0f; }
+    m.fixs = 0.0; m.fixb = 0u; m.fs = 0.0f;
+  }
+}
+
+__device__ __forceinline__ void quad_dummy(int c, QuadIn& m) {
+  m.r = 0; m.qd = c == 0 ? 1.0 : 0.0; m.sq = 0.0f; m.xd = m.d1d = m.w1d = 0.0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { m.sd[k] = 0.0f; m.sw[k] = 0.0f; }
+  m.fixs = 0.0; m.fixb = 0u; m.fs = 0.0f;
+}
+
+// value of lane (quad base | k)
+template <class T>
+__device__ __forceinline__ T qsh(T v, int k) { return __shfl_sync(0xffffffffu, v, (int)((threadIdx.x & 31) & ~3) | k); }
+template <class T>
+__device__ __forceinline__ T quad_sum(T v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  return v;
+}
+__device__ __forceinline__ float sel3(int c, float a0, float a1, float a2) { return c == 0 ? a0 : (c == 1 ? a1 : a2); }
+
+// The quaternion product of qdot_f, component c: o_c = sum_k s_ck w_k q[c ^ (k + 1)]
+// with the signs of qdot_f (negative terms: c = 0: k 0, 2; c = 1: k 1, 2; c = 2: k 0, 1).
+struct QuadQ {   // the three components of one quaternion that lane c's products need
+  float q0, q1, q2;
+  __device__ void load(float own, int c) { q0 = qsh(own, c ^ 1); q1 = qsh(own, c ^ 2); q2 = qsh(own, c ^ 3); }
+};
+__device__ __forceinline__ float qdot_c(const float w[3], const QuadQ& q, int c) {
+  const int b = 3 * c;
+  const float s0 = ((0xF5 >> b) & 1) ? -1.0f : 1.0f;
+  const float s1 = ((0xF5 >> (b + 1)) & 1) ? -1.0f : 1.0f;
+  const float s2 = ((0xF5 >> (b + 2)) & 1) ? -1.0f : 1.0f;
+  return (s0 * w[0]) * q.q0 + (s1 * w[1]) * q.q1 + (s2 * w[2]) * q.q2;
+}
+
+template <int NQ>
+__device__ __forceinline__ void correct_quad(const StepArgs& a, int i, bool ok, int c, const QuadIn& m, float Fc,
+                                             const float tl[3], int step, bool predict_next, const PoseBuf& next,
+                                             float& ekt2, float& ekr2, float& dmax2, int& bad) {
+  const int n = a.p.n;
+  double* st = a.p.st;
+  float* stf = a.stf;
+  const bool v3 = c < 3;   // owns a vector component
+  const ThermoDev& th = a.th[m.r];
+  const int kind = th.kind;
+  const float dt = a.fdt;
+  double xd = m.xd, d1d = m.d1d, w1d = m.w1d;
+  const double qd = m.qd;
+  const float d1f = (float)d1d, w1f = (float)w1d, qf = (float)qd;
+  float w[3], q4[4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = qsh(w1f, k);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) q4[k] = qsh(qf, k);
+  float t[9];
+  setmatrix_f(q4, t);
+  const float tau = sel3(c, t[0], t[1], t[2]) * tl[0] + sel3(c, t[3], t[4], t[5]) * tl[1] +
+                    sel3(c, t[6], t[7], t[8]) * tl[2];
+  int bd = (v3 && !(isfinite(Fc) && isfinite(tau))) ? 1 : 0;
+  const float ext_r = kind == G6_NOSE ? th.fext : 0.0f, ext_t = 0.5f * ext_r;
+  // COM: Gear-5 corrector
+  const float nf = Fc * a.fcf - d1f * ext_t;
+  const float delta = nf - m.sd[0];
+  float dx_c = (float)G50 * delta, dd1_c = (float)G51 * delta;
+  const float D0 = nf, D1 = m.sd[1] + (float)G53 * delta, D2 = m.sd[2] + (float)G54 * delta,
+              D3 = m.sd[3] + (float)G55 * delta;
+  // quaternion value
+  QuadQ qq;
+  qq.load(qf, c);
+  const float nw = qdot_c(w, qq, c);
+  const float dq_c = (float)G40 * (nw * dt * 0.5f - m.sq);
+  // angular velocity: Gear-4 with Euler's equations (axis c, cyclic c+1, c+2)
+  const float I0 = sel3(c, a.fI[0], a.fI[1], a.fI[2]);
+  const float I1 = sel3(c, a.fI[1], a.fI[2], a.fI[0]);
+  const float I2 = sel3(c, a.fI[2], a.fI[0], a.fI[1]);
+  const float wa = sel3(c, w[1], w[2], w[0]), wb = sel3(c, w[2], w[0], w[1]);
+  const float nfw = (tau + (I1 - I2) * wa * wb) * dt / I0 - w1f * ext_r;
+  const float dlw = nfw - m.sw[0];
+  float dw1_c = (float)G40 * dlw;
+  const float Wk0 = nfw, Wk1 = m.sw[1] + (float)G42 * dlw, Wk2 = m.sw[2] + (float)G43 * dlw,
+              Wk3 = m.sw[3] + (float)G44 * dlw;
+  float d1c = d1f + dd1_c, w1c = w1f + dw1_c;
+  if (kind == G6_ANDERSEN) {   // stochastic collisions: the quad draws the same numbers
+    uint32_t ctr[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, 0u};
+    philox4x32(ctr, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+    if (uniform_f(ctr[0]) <= th.frdt) {
+      const float kT = th.fkT;
+      float z[6];
+      for (int p = 0; p < 3; ++p) {
+        uint32_t g[4] = {(uint32_t)i, (uint32_t)(a.ctrl[6] + step), 0x41u, (uint32_t)(p + 1)};
+        philox4x32(g, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+        const float rr = sqrtf(-2.0f * logf(uniform_f(g[0])));
+        float sn, cs;
+        sincospif(2.0f * uniform_f(g[1]), &sn, &cs);
+        z[2 * p] = rr * sn;
+        z[2 * p + 1] = rr * cs;
+      }
+      const float sv = sqrtf(kT / a.fmass) * dt;
+      d1c = sel3(c, z[0], z[1], z[2]) * sv; d1d = 0.0; dd1_c = d1c;
+      w1c = sel3(c, z[3], z[4], z[5]) * sqrtf(kT / I0); w1d = 0.0; dw1_c = w1c;
+    }
+  }
+  if (!v3) { d1c = 0.0f; w1c = 0.0f; }
+  // quaternion stacks from the corrected angular-velocity stack
+  float W0[3], W1[3], W2[3], W3[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { W0[k] = qsh(w1c, k); W1[k] = qsh(Wk0, k); W2[k] = qsh(Wk1, k); W3[k] = qsh(Wk2, k); }
+  const float Q0 = qf + dq_c;
+  QuadQ a0, a1, a2, a3;
+  a0.load(Q0, c);
+  const float Q1 = qdot_c(W0, a0, c) * dt * 0.5f;
+  a1.load(Q1, c);
+  const float Q2 = (qdot_c(W1, a0, c) + qdot_c(W0, a1, c)) * dt * 0.25f;
+  a2.load(Q2, c);
+  const float Q3 = (qdot_c(W2, a0, c) + qdot_c(W0, a2, c) + qdot_c(W1, a1, c)) * dt * (1.0f / 6.0f);
+  a3.load(Q3, c);
+  const float Q4 = (qdot_c(W3, a0, c) + qdot_c(W2, a1, c) + qdot_c(W1, a2, c) + qdot_c(W0, a3, c)) * dt * (1.0f / 8.0f);
+  // kinetic sums (Rigid_Ek)
+  ekt2 = quad_sum(d1c * d1c);
+  ekr2 = quad_sum(I0 * (w1c * w1c));   // w1c is 0 on lane 3
+  if (!predict_next) {   // last step of a run: the corrected state
+    if (ok) {
+      if (v3) {
+        G6_ST(c) = xd + (double)dx_c;
+        G6_ST(3 + c) = d1d + (double)dd1_c;
+        G6_ST(18 + c) = w1d + (double)dw1_c;
+        const float Dk[4] = {D0, D1, D2, D3}, Wn[4] = {Wk0, Wk1, Wk2, Wk3};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) { G6_SF(STF_D2 + 3 * k + c) = Dk[k]; G6_SF(STF_W2 + 3 * k + c) = Wn[k]; }
+      }
+      G6_ST(33 + c) = qd + (double)dq_c;
+      G6_SF(STF_Q2 + c) = Q1; G6_SF(STF_Q2 + 4 + c) = Q2; G6_SF(STF_Q2 + 8 + c) = Q3; G6_SF(STF_Q2 + 12 + c) = Q4;
+    }
+    if (quad_sum(bd)) bad = 1;
+    dmax2 = 0.0f;
+    return;
+  }
+  // the next step's prediction, added to the corrected state in one FP64 add each
+  double x = 0.0;
+  if (v3) {
+    const float dsum = D0 + D1 + D2 + D3;
+    x = (xd + d1d) + (double)(dx_c + dd1_c + dsum);
+    if (ok) {
+      G6_ST(c) = x;
+      G6_ST(3 + c) = d1d + (double)(dd1_c + 2.0f * D0 + 3.0f * D1 + 4.0f * D2 + 5.0f * D3);
+      G6_SF(STF_D2 + c) = D0 + 3.0f * D1 + 6.0f * D2 + 10.0f * D3;
+      G6_SF(STF_D2 + 3 + c) = D1 + 4.0f * D2 + 10.0f * D3;
+      G6_SF(STF_D2 + 6 + c) = D2 + 5.0f * D3;
+      G6_SF(STF_D2 + 9 + c) = D3;
+      G6_ST(18 + c) = w1d + (double)(dw1_c + Wk0 + Wk1 + Wk2 + Wk3);
+      G6_SF(STF_W2 + c) = Wk0 + 2.0f * Wk1 + 3.0f * Wk2 + 4.0f * Wk3;
+      G6_SF(STF_W2 + 3 + c) = Wk1 + 3.0f * Wk2 + 6.0f * Wk3;
+      G6_SF(STF_W2 + 6 + c) = Wk2 + 4.0f * Wk3;
+      G6_SF(STF_W2 + 9 + c) = Wk3;
+    }
+  }
+  const float qsum = dq_c + Q1 + Q2 + Q3 + Q4;
+  double q = qd + (double)qsum;
+  float qp = qf + qsum;
+  if (ok) {
+    G6_SF(STF_Q2 + c) = Q1 + 2.0f * Q2 + 3.0f * Q3 + 4.0f * Q4;
+    G6_SF(STF_Q2 + 4 + c) = Q2;
+    G6_SF(STF_Q2 + 8 + c) = Q3;
+    G6_SF(STF_Q2 + 12 + c) = Q4;
+  }
+  // 1/|q| = 1 - e/2 + 3e^2/8 for |q|^2 = 1 + e: the small factor in float
+  const double e2 = quad_sum(q * q) - 1.0;
+  const float ef = (float)e2;
+  const float cfac = ef * (-0.5f + 0.375f * ef);
+  const double cd = (double)cfac;
+  q = q + q * cd;
+  qp = qp + qp * cfac;
+  if (ok) G6_ST(33 + c) = q;
+  // placement of the predicted pose: fixed-point COM, FP64 COM, float offsets, the pose record
+  constexpr int NPK = ((6 + 3 * NQ) + 3) / 4;
+  float qv[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qv[k] = qsh(qp, k);
+  float tp[9];
+  setmatrix_f(qv, tp);
+  float e = 0.0f;
+  uint32_t fw = 0u;
+  if (v3) {
+    fw = (uint32_t)(unsigned long long)__double2ll_rn(x * m.fixs);
+    e = (float)(int)(fw - m.fixb) * m.fs;
+  }
+  const float dd = quad_sum(e * e);
+  if (ok) {
+    float* pf = reinterpret_cast<float*>(next.pk32) + (size_t)i * 4 * NPK;
+    float* qf8 = reinterpret_cast<float*>(next.pkq) + 8 * (size_t)i;
+    if (v3) {
+      next.fix[(size_t)c * n + i] = fw;
+      next.pk64[(size_t)i * a.p.w64 + c] = x;
+      pf[c] = __uint_as_float(fw);
+      qf8[c] = __uint_as_float(fw);
+    }
+    qf8[3 + c] = qp;
+    if (c == 3) qf8[7] = 0.0f;
+    // site c (and, with 4 charged sites, site 4 on lane 0)
+    if (c <= NQ) {
+      float o[3];
+      site_off_f(tp, a.p.fbody[c][0], a.p.fbody[c][1], a.p.fbody[c][2], o);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pf[3 + 3 * c + k] = o[k];
+    }
+    if (NQ == 4 && c == 0) {
+      float o[3];
+      site_off_f(tp, a.p.fbody[4][0], a.p.fbody[4][1], a.p.fbody[4][2], o);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pf[15 + k] = o[k];
+    }
+    if (c == 3)
+      for (int k = 3 + 3 * (NQ + 1); k < 4 * NPK; ++k) pf[k] = 0.0f;
+  }
+  dmax2 = dd;
+  const int anybad = quad_sum(bd);
+  if (anybad) bad = 1;
+  if (!isfinite(dd)) { bad = 1; dmax2 = 3.0e38f; }
+}
+
 #undef G6_SF
 
 // ---------------------------------------------------------------------------

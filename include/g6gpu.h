@@ -248,7 +248,8 @@ int g6_set_lpi(g6_ctx* ctx, int lpi);
 typedef struct g6_shape {
   int lpi;         /* lanes per molecule, force-only kernel (4, 8, 16, 32)           */
   int step_lpi;    /* lanes per molecule, pair kernel of the MD step (4, 8, 16, 32)  */
-  int step_mpw;    /* molecules per warp, mixed MD integrator kernel (8, 16, 32)     */
+  int step_mpw;    /* mixed MD integrator: molecules per warp, one lane each (8, 16,
+                      32), or 4: four lanes per molecule (component-parallel)      */
   double skin;     /* Verlet margin [A] (g6_set_skin)                                */
   int cap;         /* neighbour-list row capacity (entries); g6_set_shape: 0 derives it
                       from the skin and the density (twice the expected row + 64)    */

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import genesis6_gb300 as g6
-from genesis6_gb300 import config
+from genesis6_gb300 import _capi, config
 from genesis6_gb300.interaction import Interaction, Sites, force, pair_potential, site_positions
 
 pytestmark = pytest.mark.gpu
@@ -167,6 +167,59 @@ def test_md_nose_follows_oracle(orc):
     assert np.abs(log[:, 0, 7] - log_o[:, 7]).max() <= 1e-9 * max(1e-30, np.abs(log_o[:, 7]).max())
     assert np.abs(log[:, 0, 5] - log_o[:, 5]).max() <= 1e-9 * np.abs(log_o[:, 5]).max()
     assert th[0].zeta[0] == pytest.approx(t_o[4], rel=1e-8)
+
+
+@pytest.mark.parametrize("model,mpw", [("TIP4P", 4), ("TIP4P", 8), ("TIP4P", 16), ("TIP4P", 32), ("ST2", 4),
+                                       ("ST2", 16)])
+def test_md_mixed_integrators_follow_oracle(orc, model, mpw):
+    """Mixed-precision Gear MD with each integrator kernel (one lane per molecule
+    with 8, 16 or 32 molecules per warp; four lanes per molecule for step_mpw 4)
+    under a Nose-Hoover thermostat tracks the oracle's FP64 trajectory for 20
+    steps within the error of FP32 site forces."""
+    import ctypes
+    n = 256
+    b = config.water_box(model, n, 7, temp=320.0, dt=0.002, jitter=0.2)
+    L = b["L"]
+    q = 300.0 * 0.1 ** 2 / 0.002
+    s = g6.RigidWater(model, n, L, path="custom", precision="mixed", rc=8.5, skin=1.0)
+    s.upload_state(b["rec"])
+    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=mpw, skin=1.0, cap=0, step_ms=0.0)
+    s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+    th = s.thermostats(1, "nose", temp=300.0, q=q, dump=0.0)
+    log = s.md_run(0.002, 20, th)
+    rec_g = s.download_state()
+    t_o = np.array([1, q, 0.0, 300.0, 0, 0, 0, 0, 0, 0], float)
+    rec_o, t_o, log_o = orc.md_run(model, "custom", b["rec"], L, [8.5] * 3, 6.5, 8.5, 0.002, 20, t_o)
+    assert np.abs(rec_g[:, :3] - rec_o[:, :3]).max() < 1e-5
+    assert np.abs(rec_g[:, 33:37] - rec_o[:, 33:37]).max() < 1e-5
+    assert np.abs(rec_g[:, 3:6] - rec_o[:, 3:6]).max() < 1e-6          # d1 = v dt
+    assert np.abs(rec_g[:, 18:21] - rec_o[:, 18:21]).max() < 1e-5 * np.abs(rec_o[:, 18:21]).max()
+    for c in (0, 1, 2, 3, 5):   # Epot, Ekt, Ekr, T, H
+        assert np.abs(log[:, 0, c] - log_o[:, c]).max() <= 2e-5 * np.abs(log_o[:, c]).max(), c
+    assert np.array_equal(log[:, 0, 6], log_o[:, 6])   # pairs within rc
+    assert th[0].zeta[0] == pytest.approx(t_o[4], rel=1e-4, abs=1e-9)
+
+
+def test_md_mixed_quad_integrator_collisions():
+    """The four-lane integrator draws the stochastic collisions of the
+    one-lane integrator (same Philox counters per molecule and step): the two
+    trajectories agree within FP32 rounding."""
+    import ctypes
+    n = 343
+    b = config.water_box("TIP4P", n, 9, temp=300.0, dt=0.002, jitter=0.2)
+    out = []
+    for mpw in (4, 8):
+        s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision="mixed", rc=8.5, skin=1.0)
+        s.upload_state(b["rec"])
+        sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=mpw, skin=1.0, cap=0, step_ms=0.0)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+        th = s.thermostats(1, "andersen", temp=300.0, rate=20.0, seed=77)
+        log = s.md_run(0.002, 30, th)
+        out.append((s.download_state(), log))
+    (ra, la), (rb, lb) = out
+    assert np.abs(ra[:, :3] - rb[:, :3]).max() < 1e-5
+    assert np.abs(ra[:, 3:6] - rb[:, 3:6]).max() < 1e-6
+    assert np.abs(la[:, 0, 3] - lb[:, 0, 3]).max() < 1e-4 * lb[:, 0, 3].max()
 
 
 def test_md_mixed_conserves_energy():
