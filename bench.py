@@ -64,7 +64,8 @@ def parse():
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
     p.add_argument("--n", type=int, default=N_MAIN, help="molecules of the 'md' profiling case")
     p.add_argument("--shape", default=None,
-                   help="'md' profiling case: lanes,step_lanes,molecules_per_warp,skin instead of running the tuner "
+                   help="'md' profiling case: lanes,step_lanes,molecules_per_warp,skin[,half (1: half list, the "
+                        "default; 0: full list)] instead of running the tuner "
                         "(keeps the tuner's many launches out of a profiler capture)")
     p.add_argument("--profile", choices=["md", "e2e", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
@@ -884,8 +885,10 @@ def run_gpu(args, rank, world, local):
         "rdf_32k": rdf,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": traffic,
-                     "kernel": "k_pairs<TIP4P, mixed, MD step> (in-range compaction of the Verlet rows + FP32 "
-                               "site loops; the Gear corrector runs in k_integrate_mixed)",
+                     "kernel": ("k_pairs<TIP4P, mixed, MD step, %s> (in-range compaction of the Verlet rows + "
+                                "FP32 site loops%s; the Gear corrector runs in k_integrate_mixed)"
+                                % (("half list", ", each pair once, the partner's share by vector atomics")
+                                   if shape.get("step_half") else ("full list", ", each pair from both sides"))),
                      "flops_per_pair": FLOPS_PER_PAIR["TIP4P"],
                      "pairs_per_launch": pairs, "kernel_ms": kmean, "shape": shape,
                      "peak_source": "cuBLAS SGEMM 8192^3 with TF32 off, measured in this run (FP32 CUDA-core "
@@ -926,8 +929,11 @@ def run_profile(args):
         from genesis6_gb300 import _capi
         shape = _capi.Shape()
         if args.shape:
-            lp, slp, mpw, sk = args.shape.split(",")
-            shape = _capi.Shape(lpi=int(lp), step_lpi=int(slp), step_mpw=int(mpw), skin=float(sk), cap=0, step_ms=0.0)
+            f = args.shape.split(",")
+            lp, slp, mpw, sk = f[:4]
+            half = int(f[4]) if len(f) > 4 else 1
+            shape = _capi.Shape(lpi=int(lp), step_lpi=int(slp), step_mpw=int(mpw), skin=float(sk), cap=0, step_ms=0.0,
+                                step_half=half)
             s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(shape)))
         else:
             s._check(s.L.g6_tune_shape(s.ctx, _capi.TUNE_SKIN, ctypes.byref(shape)))

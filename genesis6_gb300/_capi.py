@@ -57,7 +57,8 @@ class Thermostat(ctypes.Structure):
 
 class Shape(ctypes.Structure):
     _fields_ = [("lpi", ctypes.c_int), ("step_lpi", ctypes.c_int), ("step_mpw", ctypes.c_int),
-                ("skin", ctypes.c_double), ("cap", ctypes.c_int), ("step_ms", ctypes.c_double)]
+                ("skin", ctypes.c_double), ("cap", ctypes.c_int), ("step_ms", ctypes.c_double),
+                ("step_half", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

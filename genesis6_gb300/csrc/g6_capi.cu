@@ -256,6 +256,8 @@ struct g6_ctx {
   int lpi = 0;                    // lanes per molecule in the force kernel (0 = default)
   int step_lpi = 0;               // lanes per molecule in the fused MD step kernel (0 = default)
   int step_mpw = 0;               // mixed MD step: molecules per warp of the integrator kernel (0 = default)
+  int step_half = -1;             // mixed MD step: 1 half list, 0 full list, -1 default
+  bool half_fixed = false;        // step_half set by g6_set_shape (the tuner keeps it)
   int coop_grid = 0;              // blocks of the cooperative rebuild kernel
   // device arrays
   int* d_off = nullptr; int* d_mol_rep = nullptr; double* d_L = nullptr; double* d_invL = nullptr;
@@ -267,6 +269,7 @@ struct g6_ctx {
   double *d_F = nullptr, *d_tl = nullptr, *d_emol = nullptr, *d_wmol = nullptr;
   int* d_npin = nullptr;
   float4* d_fres = nullptr;       // mixed MD step: per-molecule float-pair results of the pair kernel
+  float4* d_jacc = nullptr;       // mixed MD step, half list: j-side force and torque (zero between steps)
   double* d_save = nullptr;       // state at the start of the current run (row-overflow recovery)
   int cap_request = 0;            // neighbour-list row capacity set by g6_set_shape or raised after an overflow
   bool overflow_recovered = false;   // the last run overflowed a row and was rolled back
@@ -274,6 +277,7 @@ struct g6_ctx {
   // grids
   HostGrid gref, glist;
   bool list_valid = false;   // the device neighbour list matches glist (built since the grid was made)
+  bool rows_half = false;    // the device rows hold only the half-list pairs (built by a half-list MD run)
   std::vector<int> sten, sten_off;
   int* d_sten = nullptr; int* d_sten_off = nullptr;
   // neighbour list
@@ -531,7 +535,7 @@ static CellArgs cell_args(g6_ctx* c, HostGrid& g, const int* ctrl) {
   return a;
 }
 
-static ListArgs list_args(g6_ctx* c, const int* ctrl) {
+static ListArgs list_args(g6_ctx* c, const int* ctrl, bool half = false) {
   ListArgs a;
   std::memset(&a, 0, sizeof a);
   a.n = c->n; a.cap = c->cap; a.rep = rep_dev(c); a.g = grid_dev(c->glist); a.cell = c->glist.d_cell;
@@ -542,8 +546,12 @@ static ListArgs list_args(g6_ctx* c, const int* ctrl) {
   const double rl = c->cc.rout + effective_skin(c);
   a.rlist2 = (float)(rl * rl) + 1e-3f;   // superset margin over the fixed-point rounding
   a.nbr = c->d_nbr; a.nnb = c->d_nnb; a.overflow = c->d_overflow; a.ctrl = ctrl;
+  a.half = half ? 1 : 0;
   return a;
 }
+
+// MD steps of this context evaluate each pair once (mixed precision, half list).
+static bool step_uses_half(const g6_ctx* c) { return c->prec == G6_MIXED && c->step_half > 0; }
 
 static ForceArgs force_args(g6_ctx* c) {
   ForceArgs a;
@@ -554,6 +562,7 @@ static ForceArgs force_args(g6_ctx* c) {
   a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin; a.fres = c->d_fres;
   a.ccap = c->ccap; a.overflow = c->d_overflow;
   a.pkq = c->d_pkq; a.pkq_1 = c->d_pkq_1;
+  a.jacc = c->d_jacc; a.half = 0;
   for (int s = 0; s < MAXSITE; ++s)
     for (int k = 0; k < 3; ++k) a.fbody[s][k] = (float)c->mh.body[s][k];
   return a;
@@ -572,6 +581,11 @@ static int default_lpi(const g6_ctx* c) {
 // instructions for a large one.
 static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 4 : (c->n <= 24576 ? 16 : 32); }
 
+// Mixed MD steps use the half list (each pair evaluated once, the other
+// molecule's share added with float atomics: sums in a varying order, so runs
+// are not bit-reproducible); FP64 steps always use the full list.
+static int default_half(const g6_ctx* c) { return c->prec == G6_MIXED ? 1 : 0; }
+
 // The mixed list kernel keeps each molecule's in-range row in shared memory
 // (32/lpi rows per warp): widen lpi until the rows of a block fit.
 static int fit_lpi(const g6_ctx* c, int lpi) {
@@ -585,8 +599,8 @@ static int fit_lpi(const g6_ctx* c, int lpi) {
 static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl, const StepArgs* step = nullptr) {
   if (ctx->coop_grid == 0) ctx->coop_grid = rebuild_grid_limit();
   CellArgs ca = cell_args(ctx, ctx->glist, ctrl);
-  CK(launch_rebuild(ca, list_args(ctx, ctrl), ctx->glist.d_start, ctx->glist.d_cellmol, ctx->coop_grid, step,
-                    ctx->stream));
+  CK(launch_rebuild(ca, list_args(ctx, ctrl, step != nullptr && step_uses_half(ctx)), ctx->glist.d_start,
+                    ctx->glist.d_cellmol, ctx->coop_grid, step, ctx->stream));
   return G6_OK;
 }
 
@@ -601,6 +615,7 @@ static int force_once(g6_ctx* ctx) {
   CK(launch_predict_place(place_args(ctx), 0, ctx->d_th, 0, ctx->stream));
   rc = enqueue_rebuild(ctx, nullptr);
   if (rc) return rc;
+  ctx->rows_half = false;   // the rebuild wrote full rows
   if (ctx->prec == G6_MIXED && ctx->ccap > pairs_max_cap(32))
     return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
   ctx->lpi = fit_lpi(ctx, ctx->lpi);
@@ -757,6 +772,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_F, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_tl, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_fres, 4 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_jacc, 2 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_save, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
@@ -1324,6 +1340,7 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
   if (rc) return rc;
   ForceArgs fa = force_args(ctx);
   fa.ctrl = ctx->d_ctrl;
+  fa.half = ctx->step_half > 0 ? 1 : 0;
   if (kev) CK(cudaEventRecordWithFlags(ev[1], ctx->stream, cudaEventRecordExternal));
   if (ctx->prec == G6_MIXED) {
     // pair kernel, then the integrator kernel; the kernel events bracket the pair kernel
@@ -1413,6 +1430,7 @@ static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bo
   ctx->lpi = fit_lpi(ctx, ctx->lpi);
   ctx->step_lpi = fit_lpi(ctx, ctx->step_lpi);
   if (ctx->step_mpw == 0) ctx->step_mpw = default_mpw(ctx);
+  if (ctx->step_half < 0) ctx->step_half = default_half(ctx);
   const PinnedRuns pr = pinned_runs(ctx);
   ThermoDev* th = pr.th_up;
   for (int r = 0; r < ctx->nrep; ++r) {
@@ -1439,7 +1457,9 @@ static int md_fill(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, bo
   }
   // first step: rebuild the list (1), or let the step head test the displacements
   // since the last build (2) when a list for this grid exists
-  const int ctrl[8] = {ctx->list_valid ? 2 : 1, 0, nsteps, 0, 0, want_log ? nsteps : 0,
+  // (a list of the other row form is rebuilt: a full-list step needs every pair)
+  const bool keep = ctx->list_valid && ctx->rows_half == step_uses_half(ctx);
+  const int ctrl[8] = {keep ? 2 : 1, 0, nsteps, 0, 0, want_log ? nsteps : 0,
                        (int)(ctx->steps_done & 0x3fffffffULL), 0};
   std::memcpy(pr.ctrl_up, ctrl, sizeof ctrl);
   // temperature and pressure factors of each replica (Mixture.F90:2251-2264)
@@ -1509,6 +1529,7 @@ static int md_check(g6_ctx* ctx, int nsteps, g6_thermostat* thermo) {
   }
   ctx->steps_done += (unsigned long long)nsteps;
   ctx->list_valid = true;   // every step leaves the list valid for its positions
+  ctx->rows_half = step_uses_half(ctx);   // the first step rebuilt the rows unless they had this form
   return G6_OK;
 }
 
@@ -1682,6 +1703,7 @@ ShapeKey shape_key(const g6_ctx* c) {
 static void fill_shape(const g6_ctx* ctx, g6_shape* out, double step_ms) {
   out->lpi = ctx->lpi; out->step_lpi = ctx->step_lpi; out->step_mpw = ctx->step_mpw;
   out->skin = ctx->skin; out->cap = ctx->cap; out->step_ms = step_ms;
+  out->step_half = ctx->step_half < 0 ? default_half(ctx) : ctx->step_half;
 }
 
 // A context without a chosen shape takes the cached one for its size.
@@ -1691,6 +1713,7 @@ static void apply_cached_shape(g6_ctx* ctx) {
   auto it = shape_cache().find(shape_key(ctx));
   if (it == shape_cache().end()) return;
   ctx->lpi = it->second.lpi; ctx->step_lpi = it->second.step_lpi; ctx->step_mpw = it->second.step_mpw;
+  ctx->step_half = it->second.step_half;
 }
 
 // Duration of `timed` NVE steps (after `warm` untimed ones) from the state
@@ -1732,25 +1755,32 @@ static int tune_force_lpi(g6_ctx* ctx) {
 }
 
 // MD-step kernel shape at the current skin: every (lanes, molecules per warp)
-// pair on a short run; returns the best shape's time for `timed` steps.
+// pair on a short run, with the half and the full list in mixed precision;
+// returns the best shape's time for `timed` steps.  A context whose list form
+// was set (g6_set_shape) keeps it.
 static int tune_step_shape(g6_ctx* ctx, cudaEvent_t e0, cudaEvent_t e1, float* best_ms) {
   static const int lcand[4] = {4, 8, 16, 32};
   static const int mcand[4] = {4, 8, 16, 32};   // 4: the component-parallel integrator
   const int nm = ctx->prec == G6_MIXED ? 4 : 1;
-  int bl = ctx->step_lpi, bm = ctx->step_mpw;
+  const bool fixed_half = ctx->half_fixed;
+  const int h0 = fixed_half ? ctx->step_half : 0;
+  const int h1 = fixed_half ? ctx->step_half : (ctx->prec == G6_MIXED ? 1 : 0);
+  int bl = ctx->step_lpi, bm = ctx->step_mpw, bh = h0;
   float sb = 1e30f;
-  for (int k = 0; k < 4; ++k) {
-    if (fit_lpi(ctx, lcand[k]) != lcand[k]) continue;
-    for (int q = 0; q < nm; ++q) {
-      ctx->step_lpi = lcand[k];
-      ctx->step_mpw = ctx->prec == G6_MIXED ? mcand[q] : 8;
-      float ms = 0.0f;
-      int rc = time_md_steps(ctx, 2, 10, e0, e1, &ms);
-      if (rc) return rc;
-      if (ms < sb) { sb = ms; bl = ctx->step_lpi; bm = ctx->step_mpw; }
+  for (int h = h0; h <= h1; ++h)
+    for (int k = 0; k < 4; ++k) {
+      if (fit_lpi(ctx, lcand[k]) != lcand[k]) continue;
+      for (int q = 0; q < nm; ++q) {
+        ctx->step_lpi = lcand[k];
+        ctx->step_mpw = ctx->prec == G6_MIXED ? mcand[q] : 8;
+        ctx->step_half = h;
+        float ms = 0.0f;
+        int rc = time_md_steps(ctx, 2, 10, e0, e1, &ms);
+        if (rc) return rc;
+        if (ms < sb) { sb = ms; bl = ctx->step_lpi; bm = ctx->step_mpw; bh = h; }
+      }
     }
-  }
-  ctx->step_lpi = bl; ctx->step_mpw = bm;
+  ctx->step_lpi = bl; ctx->step_mpw = bm; ctx->step_half = bh;
   *best_ms = sb / 10.0f;
   return G6_OK;
 }
@@ -1779,8 +1809,10 @@ static int tune(g6_ctx* ctx, int flags, g6_shape* out) {
   }
   double best_skin = skin0;
   float best_long = 1e30f;
-  int bl = 0, bs = 0, bm = 0;
+  int bl = 0, bs = 0, bm = 0, bh = 0;
+  const int half0 = ctx->step_half;
   for (size_t k = 0; k < skins.size() && rc == G6_OK; ++k) {
+    ctx->step_half = half0;
     if (skins.size() > 1) {
       ctx->skin = skins[k]; ctx->glist.valid = false; ctx->cap = 0;
     }
@@ -1798,15 +1830,19 @@ static int tune(g6_ctx* ctx, int flags, g6_shape* out) {
     }
     if (rc == G6_OK && long_ms < best_long) {
       best_long = long_ms; best_skin = ctx->skin; bl = ctx->lpi; bs = ctx->step_lpi; bm = ctx->step_mpw;
+      bh = ctx->step_half;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc == G6_OK) {
     if (skins.size() > 1 && best_skin != ctx->skin) { ctx->skin = best_skin; ctx->glist.valid = false; ctx->cap = 0; }
-    ctx->lpi = bl; ctx->step_lpi = bs; ctx->step_mpw = bm;
+    ctx->lpi = bl; ctx->step_lpi = bs; ctx->step_mpw = bm; ctx->step_half = bh;
     step_ms = best_long;
-  } else if (skins.size() > 1) {
+  } else {
+    ctx->step_half = half0;
+  }
+  if (rc != G6_OK && skins.size() > 1) {
     ctx->skin = skin0; ctx->glist.valid = false; ctx->cap = 0;
   }
   ctx->steps_done = steps0;
@@ -1850,7 +1886,13 @@ int g6_set_shape(g6_ctx* ctx, const g6_shape* shape) {
     return fail(ctx, G6_ERR_ARG, "lanes per molecule must be 4, 8, 16 or 32 and step_mpw 4, 8, 16 or 32");
   if (!(shape->skin >= 0.0)) return fail(ctx, G6_ERR_ARG, "skin must be >= 0");
   if (shape->cap < 0) return fail(ctx, G6_ERR_ARG, "cap must be >= 0 (0: from the skin and density)");
+  if (shape->step_half != 0 && shape->step_half != 1)
+    return fail(ctx, G6_ERR_ARG, "step_half must be 0 (full list) or 1 (half list)");
+  if (shape->step_half == 1 && ctx->prec != G6_MIXED)
+    return fail(ctx, G6_ERR_ARG, "the half list is a mixed-precision MD step (FP64 steps use the full list)");
   ctx->lpi = shape->lpi; ctx->step_lpi = shape->step_lpi; ctx->step_mpw = shape->step_mpw;
+  ctx->step_half = shape->step_half;
+  ctx->half_fixed = true;
   if (shape->skin != ctx->skin || shape->cap != ctx->cap_request) {
     ctx->skin = shape->skin; ctx->cap_request = shape->cap;
     ctx->glist.valid = false; ctx->cap = 0; ctx->list_valid = false;
@@ -1897,22 +1939,37 @@ int g6_md_run(g6_ctx* ctx, double dt, int nsteps, g6_thermostat* thermo, double*
 // Enqueue the whole host-buffer step on the context's stream (used directly,
 // or captured once into graph_host).  log_dst: host destination of the log.
 // upload = false repeats a step from the state kept in d_save (FP64) or the
-// records in d_stage (mixed) -- the row-overflow recovery.
-static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log, bool upload = true) {
+// records in d_stage (mixed) -- the row-overflow recovery.  dev_rec (mixed):
+// the device address of a page-locked rec, which the records-in and
+// records-out kernels then read and write over the host link themselves
+// instead of two staged copies.
+static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_dst, bool want_log, bool upload = true,
+                             double* dev_rec = nullptr) {
   const int n = ctx->n;
   const size_t bytes = (size_t)REC * n * sizeof(double);
   if (ctx->prec == G6_MIXED) {
     // records -> state + first predict in one kernel, the step, finish + state
-    // -> records in one kernel; the input records stay in d_stage, the output
-    // goes through d_save
-    if (upload) CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    // -> records in one kernel; the input records stay in d_stage (a copy made
+    // by the first kernel when it reads rec directly), the output goes to rec
+    // directly or through d_save
+    HostInArgs h;
+    std::memset(&h, 0, sizeof h);
+    h.fix_build = ctx->d_fix_build;
+    h.gmax = ctx->d_gmax;
+    if (upload && dev_rec) {
+      h.rec = dev_rec;
+      h.keep = ctx->d_stage;
+    } else {
+      if (upload) CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
+      h.rec = ctx->d_stage;
+    }
     int rc = md_upload(ctx);
     if (rc) return rc;
     StepArgs sa = step_args(ctx, dt, want_log ? ctx->d_log : nullptr);
-    CK(launch_host_in_mixed(place_args(ctx), ctx->d_stage, ctx->d_stf, ctx->d_th, dt, ctx->stream));
+    CK(launch_host_in_mixed(place_args(ctx), h, ctx->d_stf, ctx->d_th, dt, ctx->stream));
     if ((rc = enqueue_step(ctx, sa))) return rc;
-    CK(launch_host_out_mixed(sa, ctx->d_save, ctx->stream));
-    CK(cudaMemcpyAsync(rec, ctx->d_save, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(launch_host_out_mixed(sa, dev_rec ? dev_rec : ctx->d_save, ctx->stream));
+    if (!dev_rec) CK(cudaMemcpyAsync(rec, ctx->d_save, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return md_readback(ctx, 1, want_log ? log_dst : nullptr);
   }
   if (upload) {
@@ -1946,7 +2003,12 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   cudaPointerAttributes at;
   bool pinned = cudaPointerGetAttributes(&at, rec) == cudaSuccess && at.type == cudaMemoryTypeHost;
   if (!pinned) cudaGetLastError();   // clear the lookup's status for a pageable pointer
+  // mixed: page-locked records that the device can address are read and written
+  // by the step's kernels directly
+  double* dev_rec = (pinned && ctx->prec == G6_MIXED) ? (double*)at.devicePointer : nullptr;
   const PinnedRuns pr = pinned_runs(ctx);
+  // mixed: the records-in kernel makes the keep-the-list test (ctrl[0] = 3)
+  if (ctx->prec == G6_MIXED && pr.ctrl_up[0] == 2) pr.ctrl_up[0] = 3;
   if (pinned) {
     const bool want_log = log != nullptr;
     if (ctx->graph_host && (ctx->ghost_rec != rec || ctx->ghost_dt != dt || ctx->ghost_log != want_log ||
@@ -1957,7 +2019,7 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
     if (!ctx->graph_host) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      rc = enqueue_step_host(ctx, dt, rec, pr.log1, want_log);
+      rc = enqueue_step_host(ctx, dt, rec, pr.log1, want_log, true, dev_rec);
       if (rc) { cudaStreamEndCapture(ctx->stream, &g); return rc; }
       CK(cudaStreamEndCapture(ctx->stream, &g));
       cudaError_t e = cudaGraphInstantiate(&ctx->graph_host, g, 0);

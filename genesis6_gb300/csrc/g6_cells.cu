@@ -220,7 +220,7 @@ __device__ void list_row(const ListArgs& a, int i, int lane) {
     const float dx = (float)(int)(xi - q.x) * sx;
     const float dy = (float)(int)(yi - q.y) * sy;
     const float dz = (float)(int)(zi - q.z) * sz;
-    return (int)q.w != i && dx * dx + dy * dy + dz * dz < a.rlist2;
+    return (int)q.w != i && (!a.half || half_keep(i, (int)q.w)) && dx * dx + dy * dy + dz * dz < a.rlist2;
   };
   int cnt = 0;
 #pragma unroll 4
@@ -320,6 +320,12 @@ __global__ void __launch_bounds__(256) k_rebuild(RebuildArgs a) {
       for (int m = 16; m >= 1; m >>= 1) dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, m));
       if ((threadIdx.x & 31) == 0) atomicMax(&a.s.gmax[1], __float_as_uint(dmax));   // the word is 0 at run start
       grid.sync();
+      rebuild = (double)__uint_as_float(__ldcg(&a.s.gmax[1])) > a.s.half_skin2;
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.s.ctrl[0] = rebuild ? 1 : 0;
+    } else if (ctrl[0] == 3) {
+      // first step of a host-buffer step: the records-in kernel raised each
+      // molecule's displacement since the last build into gmax[1]; a block that
+      // reads ctrl[0] after block 0 has written the decision reads the same decision
       rebuild = (double)__uint_as_float(__ldcg(&a.s.gmax[1])) > a.s.half_skin2;
       if (blockIdx.x == 0 && threadIdx.x == 0) a.s.ctrl[0] = rebuild ? 1 : 0;
     } else {

@@ -221,6 +221,8 @@ struct ForceArgs {
   const float4* pkq;     // mixed list kernel: 2 float4 per molecule (fixed-point COM, float quaternion)
   const float4* pkq_1;   // the same for pose buffer 1
   float fbody[MAXSITE][3];   // body-frame site coordinates (LJ site, charged sites) as float
+  float4* jacc;   // mixed MD step, half list: per molecule 2 float4 (force, lab torque) from the pairs others hold
+  int half;       // mixed MD step: 1 = half list (each pair once, j side by atomics), 0 = full list
 };
 
 struct SitesArgs {
@@ -266,7 +268,13 @@ struct ListArgs {
   int* overflow;
   const int* ctrl;
   uint4* cellfix;        // n: (fixed-point COM, molecule) of each cell-sorted slot, filled before the rows
+  int half;              // 1: each row keeps only the pairs its molecule evaluates in a half-list step (half_keep)
 };
+
+// Half list: of the two row entries of a pair, molecule i keeps j when i and j
+// have the same parity and j > i, or different parity and j < i, so every
+// molecule keeps about half of its row whatever the index order.
+__device__ __forceinline__ bool half_keep(int i, int j) { return ((i ^ j) & 1) ? (j < i) : (j > i); }
 
 struct PairSetArgs {
   int n;
@@ -555,7 +563,13 @@ cudaError_t launch_predict_place(const PlaceArgs& a, int do_predict, ThermoDev* 
 cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStream_t s);
 cudaError_t launch_begin_mixed(const PlaceArgs& a, float* stf, ThermoDev* th, double dt, cudaStream_t s);
 // Host-buffer step of the mixed path: records in -> state + first predict; finish + state -> records out.
-cudaError_t launch_host_in_mixed(const PlaceArgs& a, const double* rec, float* stf, ThermoDev* th, double dt,
+struct HostInArgs {
+  const double* rec;          // the caller's records (device copy, or the page-locked buffer itself)
+  double* keep;               // optional: device copy of rec kept for a repeat of the step (row overflow)
+  const uint32_t* fix_build;  // fixed-point COM at the last list build
+  unsigned int* gmax;         // gmax[1]: the largest squared displacement since that build (float bits)
+};
+cudaError_t launch_host_in_mixed(const PlaceArgs& a, const HostInArgs& h, float* stf, ThermoDev* th, double dt,
                                  cudaStream_t s);
 cudaError_t launch_host_out_mixed(const StepArgs& sa, double* out, cudaStream_t s);
 cudaError_t launch_step_fp64(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);

@@ -82,9 +82,14 @@ constexpr int REC_THREADS = 128;
 // (g6_md_step_host): the records (n,53) become the FP64 state (com, d1, w1,
 // q) and the float small terms, followed by the step's first predict and
 // placement and the Nose predict -- the work of k_rec_transpose, k_stf_move
-// and k_begin_mixed in one pass, with the same arithmetic.
-__global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, const double* rec, float* stf,
-                                                               ThermoDev* th, double dt) {
+// and k_begin_mixed in one pass, with the same arithmetic.  h.rec may be the
+// caller's page-locked buffer itself (read over the host link by the tiles);
+// h.keep then receives a device copy for a repeat of the step.  With h.gmax,
+// each molecule's displacement since the last list build (the step head's
+// keep-the-list test, on the new fixed-point COM) is raised into h.gmax[1],
+// so the head only compares one word.
+__global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, HostInArgs h, float* stf, ThermoDev* th,
+                                                               double dt) {
   __shared__ double tile[REC_TILE * REC];
   if (blockIdx.x == 0) {
     for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
@@ -102,8 +107,12 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, cons
   const int i0 = blockIdx.x * REC_TILE;
   const int m = min(REC_TILE, n - i0);
   if (m <= 0) return;
-  const double* src = rec + (size_t)i0 * REC;
-  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) tile[t] = src[t];
+  const double* src = h.rec + (size_t)i0 * REC;
+  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) {
+    const double v = src[t];
+    tile[t] = v;
+    if (h.keep) h.keep[(size_t)i0 * REC + t] = v;
+  }
   __syncthreads();
   double* st = a.st;
   for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
@@ -115,12 +124,29 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, cons
     else stf[(size_t)fc * n + i0 + k] = (float)v;
   }
   __syncthreads();   // the block's columns are visible to the block
-  if ((int)threadIdx.x < m) {
-    const int i = i0 + threadIdx.x;
-    double x[3], q[4];
-    predict_mixed(st, stf, n, i, x, q);
-    if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
-    else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+  if (threadIdx.x < 32) {
+    float dd = 0.0f;
+    if ((int)threadIdx.x < m) {
+      const int i = i0 + threadIdx.x;
+      double x[3], q[4];
+      predict_mixed(st, stf, n, i, x, q);
+      if (a.nq == 3) place_mixed<3>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+      else place_mixed<4>(a, i, x, q, a.pk64, a.pk32, a.pkq, a.fix);
+      if (h.gmax) {
+        const int r = a.rep.mol_rep[i];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float e =
+              (float)(int)(a.fix[(size_t)k * n + i] - h.fix_build[(size_t)k * n + i]) * a.rep.fscale[3 * r + k];
+          dd += e * e;
+        }
+      }
+    }
+    if (h.gmax) {
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) dd = fmaxf(dd, __shfl_xor_sync(0xffffffffu, dd, o));
+      if (threadIdx.x == 0) atomicMax(&h.gmax[1], __float_as_uint(dd));
+    }
   }
 }
 
@@ -188,10 +214,10 @@ cudaError_t launch_stf_move(double* st, float* stf, int n, int to_float, cudaStr
   return cudaGetLastError();
 }
 
-cudaError_t launch_host_in_mixed(const PlaceArgs& a, const double* rec, float* stf, ThermoDev* th, double dt,
+cudaError_t launch_host_in_mixed(const PlaceArgs& a, const HostInArgs& h, float* stf, ThermoDev* th, double dt,
                                  cudaStream_t s) {
   const int blocks = a.n > 0 ? (a.n + REC_TILE - 1) / REC_TILE : 1;
-  k_host_in_mixed<<<blocks, REC_THREADS, 0, s>>>(a, rec, stf, th, dt);
+  k_host_in_mixed<<<blocks, REC_THREADS, 0, s>>>(a, h, stf, th, dt);
   return cudaGetLastError();
 }
 

@@ -92,10 +92,23 @@ struct Acc {
   }
 };
 
-template <class M, class R, int NW>
+// The j side of one pair for the half list (each pair evaluated once): the
+// force on j is minus the pair force on i, and j's torque about its COM
+// follows from the site forces being central: (d + r_ia - r_jb) x f_ab = 0, so
+// sum_ab r_jb x (-f_ab) = -sum_a (d + r_ia) x F_ia with F_ia the (switched)
+// force on i's site a from all of j's sites.  The COM switch force acts along
+// d and turns neither molecule.
+template <class R>
+struct PairJ {
+  R f[3];
+  R t[3];
+};
+
+template <class M, class R, int NW, bool HALF = false>
 __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::NQ + 1][3],
                                           const R (&rj)[M::NQ + 1][3], const PairConst& pc, R rin2, R rin, R rout,
-                                          R c1, R c2, R trl, R tru, R tw3, Acc<M, R, NW>& acc) {
+                                          R c1, R c2, R trl, R tru, R tw3, Acc<M, R, NW>& acc,
+                                          PairJ<R>* pj = nullptr) {
   R hh, dh;
   switch_fn<R>(dd, rin2, rin, rout, c1, c2, hh, dh);
   // LJ site pair (site 0 - site 0)
@@ -137,14 +150,17 @@ __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::N
   }
   R fcom = dh * elj + dcc * ec;
   R fp[3];
+  R us[M::NQ + 1][3];   // switched site forces on i
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     R t = hh * fsite[0][k];
+    us[0][k] = t;
     acc.fs[0][k] += t;
     R sum = t;
 #pragma unroll
     for (int a = 1; a <= M::NQ; ++a) {
       R u = scc * fsite[a][k];
+      us[a][k] = u;
       acc.fs[a][k] += u;
       sum += u;
     }
@@ -153,6 +169,18 @@ __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::N
     fp[k] = sum + c;
   }
   acc.e += hh * elj + scc * ec;
+  if constexpr (HALF) {
+    R tx = R(0), ty = R(0), tz = R(0);
+#pragma unroll
+    for (int a = 0; a <= M::NQ; ++a) {
+      const R vx = d[0] + ri[a][0], vy = d[1] + ri[a][1], vz = d[2] + ri[a][2];
+      tx += vz * us[a][1] - vy * us[a][2];
+      ty += vx * us[a][2] - vz * us[a][0];
+      tz += vy * us[a][0] - vx * us[a][1];
+    }
+    pj->t[0] = tx; pj->t[1] = ty; pj->t[2] = tz;
+    pj->f[0] = -fp[0]; pj->f[1] = -fp[1]; pj->f[2] = -fp[2];
+  }
   if constexpr (NW == 9) {
 #pragma unroll
     for (int a = 0; a < 3; ++a)

@@ -74,6 +74,55 @@ __device__ __forceinline__ void sites_from_q(const ForceArgs& a, const float* q,
   for (int s = 0; s <= M::NQ; ++s) site_off_f(t, a.fbody[s][0], a.fbody[s][1], a.fbody[s][2], r[s]);
 }
 
+// The pose record a pair kernel reads per molecule: the 64-byte pk32 record
+// (fixed-point COM words, float offsets of the LJ site and the three charged
+// sites) in two 256-bit loads, or the 32-byte pkq record, whose quaternion
+// gives the offsets again with the placement's roundings (the same bits).
+// OFFS = the pk32 record: the full list of the 3-charge models, where each
+// record load is followed by a pair's whole site loop.  The half list does half
+// the site work per row and is bound by the L1 line gathers of the records, so
+// it takes the quarter-size pkq record; 4-charge models always do (their
+// 80-byte pk32 record is not 32-byte aligned).  Measured on TIP4P: full list
+// 59.7 (pk32) vs 61.8 us (pkq) at 32,768 molecules; half list 54.9 vs 49.1 us.
+template <class M, bool HALF>
+struct PoseRec {
+  static constexpr bool OFFS = M::NPK == 4 && !HALF;
+  static constexpr int W = OFFS ? 16 : 8;   // floats
+};
+template <class M, bool HALF>
+__device__ __forceinline__ void load_rec(const float4* pk32, const float4* pkq, int j,
+                                         float (&v)[PoseRec<M, HALF>::W]) {
+  if constexpr (PoseRec<M, HALF>::OFFS) {
+    const float4* p = pk32 + 4 * (size_t)j;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+        : "l"(p + 2));
+  } else {
+    load_pose_q(pkq, j, v);
+  }
+}
+template <class M, bool HALF>
+__device__ __forceinline__ void rec_sites(const ForceArgs& a, const float (&v)[PoseRec<M, HALF>::W],
+                                          float (&r)[M::NQ + 1][3]) {
+  if constexpr (PoseRec<M, HALF>::OFFS) {
+#pragma unroll
+    for (int s = 0; s <= M::NQ; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) r[s][k] = v[3 + 3 * s + k];
+  } else {
+    sites_from_q<M>(a, v + 3, r);
+  }
+}
+// The first float4 of a record: the fixed-point COM words.
+template <class M, bool HALF>
+__device__ __forceinline__ float4 load_com(const float4* pk32, const float4* pkq, int j) {
+  if constexpr (PoseRec<M, HALF>::OFFS) return __ldg(pk32 + 4 * (size_t)j);
+  else return __ldg(pkq + 2 * (size_t)j);
+}
+
 // Fixed-point COM difference (units L/2^32, the wrap is the minimum image) to A.
 __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi, const float4& qj, float sx, float sy,
                                           float sz, float d[3]) {
@@ -82,10 +131,15 @@ __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi,
   d[2] = i32_to_f32((int)(zi - __float_as_uint(qj.z))) * sz;
 }
 
-// MODE 0: force only; 1: MD step.
-template <class M, int LPI, int MODE>
+// MODE 0: force only; 1: MD step.  HALF (MD step only): each pair within rc is
+// evaluated once, by the molecule that keeps it (half_keep: rows built for a
+// half-list run hold only those; a full row is filtered here); j's force and
+// torque go to a.jacc with vector float atomics, read and cleared by the
+// integrator kernel.
+template <class M, int LPI, int MODE, bool HALF>
 __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MODE>::value))
     k_pairs(ForceArgs a, StepArgs sa) {
+  static_assert(!HALF || MODE == 1, "the half list is an MD-step variant");
   constexpr int NW = MODE == 0 ? 9 : 1;
   int bid = blockIdx.x;
   if constexpr (MODE == 1) {
@@ -108,6 +162,8 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   const bool odd = (step & 1) != 0;
   const double* pk64 = odd ? a.pk64_1 : a.pk64;
   const float4* pkq = odd ? a.pkq_1 : a.pkq;
+  const float4* pk32 = odd ? a.pk32_1 : a.pk32;
+  constexpr int RW = PoseRec<M, HALF>::W;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane / LPI, sub = lane % LPI;
   const int i = (bid * blockDim.x + threadIdx.x) / LPI;
@@ -121,10 +177,10 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   int r = 0, nn = 0;
   if (valid) {
     r = a.rep.mol_rep[i];
-    float wi[8];
-    load_pose_q(pkq, i, wi);
+    float wi[RW];
+    load_rec<M, HALF>(pk32, pkq, i, wi);
     xi = __float_as_uint(wi[0]); yi = __float_as_uint(wi[1]); zi = __float_as_uint(wi[2]);
-    sites_from_q<M>(a, wi + 3, ri);
+    rec_sites<M, HALF>(a, wi, ri);
     sx = a.rep.fscale[3 * r]; sy = a.rep.fscale[3 * r + 1]; sz = a.rep.fscale[3 * r + 2];
     nn = a.nnb[i];
   } else {
@@ -147,9 +203,10 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
     for (int u = 0; u < U; ++u) {
       const int k = base + u * LPI + sub;
       jj[u] = k < nn ? __ldg(row + k) : -1;
+      if (HALF && jj[u] >= 0 && !half_keep(i, jj[u])) jj[u] = -1;
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? __ldg(pkq + 2 * (size_t)jj[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? load_com<M, HALF>(pk32, pkq, jj[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bool in = false;
@@ -190,19 +247,28 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   {
     const float frin2 = a.cc.frin2, frin = a.cc.frin, frout = a.cc.frout, fc1 = a.cc.fc1, fc2 = a.cc.fc2;
     int t = sub;
-    float tn[8];
-    if (t < cnt) load_pose_q(pkq, srow[t], tn);
+    float tn[RW];
+    if (t < cnt) load_rec<M, HALF>(pk32, pkq, srow[t], tn);
     for (; t < cnt; t += LPI) {
-      float wj[8];
+      float wj[RW];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) wj[k] = tn[k];
-      if (t + LPI < cnt) load_pose_q(pkq, srow[t + LPI], tn);   // the next pair's record, one pair ahead
+      for (int k = 0; k < RW; ++k) wj[k] = tn[k];
+      if (t + LPI < cnt) load_rec<M, HALF>(pk32, pkq, srow[t + LPI], tn);   // the next pair's record, one pair ahead
       float d[3];
       fix_delta(xi, yi, zi, make_float4(wj[0], wj[1], wj[2], 0.f), sx, sy, sz, d);
       const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
       float rj[M::NQ + 1][3];
-      sites_from_q<M>(a, wj + 3, rj);
-      pair_math<M, float, NW>(d, dd, ri, rj, a.pc, frin2, frin, frout, fc1, fc2, a.pc.frl, a.pc.fru, a.pc.fw3, acc);
+      rec_sites<M, HALF>(a, wj, rj);
+      if constexpr (HALF) {
+        const int jc = srow[t];
+        PairJ<float> pj;
+        pair_math<M, float, NW, true>(d, dd, ri, rj, a.pc, frin2, frin, frout, fc1, fc2, a.pc.frl, a.pc.fru, a.pc.fw3,
+                                      acc, &pj);
+        atomicAdd(a.jacc + 2 * (size_t)jc, make_float4(pj.f[0], pj.f[1], pj.f[2], 0.f));
+        atomicAdd(a.jacc + 2 * (size_t)jc + 1, make_float4(pj.t[0], pj.t[1], pj.t[2], 0.f));
+      } else {
+        pair_math<M, float, NW>(d, dd, ri, rj, a.pc, frin2, frin, frout, fc1, fc2, a.pc.frl, a.pc.fru, a.pc.fw3, acc);
+      }
     }
   }
 
@@ -263,6 +329,16 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   }
 }
 
+// Half list: the j-side force and torque the pair kernel accumulated for
+// molecule im, cleared for the next step's atomics.
+__device__ __forceinline__ void take_jside(const ForceArgs& a, int im, float4& jf, float4& jt) {
+  float4* p = a.jacc + 2 * (size_t)im;
+  jf = p[0];
+  jt = p[1];
+  p[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+  p[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 // Mixed MD step, second kernel: Gear corrector, next predict + placement and
 // the step's reductions for 32 molecules per block.  MPW molecules per warp
 // (32 / MPW warps per block): the corrector's FP64 instructions cost a warp
@@ -302,15 +378,18 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
       rr = a.rep.mol_rep[im];
       const float4* o = a.fres + (size_t)4 * im;
       const float4 h0 = o[0], l0 = o[1], h1 = o[2], l1 = o[3];
-      const float F[3] = {h0.x + l0.x, h0.y + l0.y, h0.z + l0.z};
-      const float tl[3] = {h1.x + l1.x, h1.y + l1.y, h1.z + l1.z};
+      float4 jf = make_float4(0.f, 0.f, 0.f, 0.f), jt = jf;
+      if (a.half) take_jside(a, im, jf, jt);
+      const float F[3] = {h0.x + (l0.x + jf.x), h0.y + (l0.y + jf.y), h0.z + (l0.z + jf.z)};
+      const float tl[3] = {h1.x + (l1.x + jt.x), h1.y + (l1.y + jt.y), h1.z + (l1.z + jt.z)};
       float ekt2, ekr2;
       correct_mixed<NQ>(sa, im, min, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
-      vv[0] = FF{0.5f * h0.w, 0.5f * l0.w};
-      vv[1] = FF{0.5f * h1.w, 0.5f * l1.w};
+      const float pf = a.half ? 1.0f : 0.5f;   // a full list holds every pair twice
+      vv[0] = FF{pf * h0.w, pf * l0.w};
+      vv[1] = FF{pf * h1.w, pf * l1.w};
       vv[2] = FF{ekt2, 0.0f};
       vv[3] = FF{ekr2, 0.0f};
-      vv[4] = FF{0.5f * (float)a.npair_in[im], 0.0f};
+      vv[4] = FF{pf * (float)a.npair_in[im], 0.0f};
     }
 #pragma unroll
     for (int k = 0; k < NRED; ++k) s_vv[m][k] = vv[k];
@@ -347,13 +426,24 @@ __global__ void __launch_bounds__(128) k_integrate_quad(ForceArgs a, StepArgs sa
   const int step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
   const bool predict_next = step + 1 < sa.ctrl[2];
-  float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), l0 = h0, h1 = h0, l1 = h0;
+  float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), l0 = h0, h1 = h0, l1 = h0, jf = h0, jt = h0;
   if (ok) {
     const float4* o = a.fres + (size_t)4 * im;
     h0 = o[0]; l0 = o[1]; h1 = o[2]; l1 = o[3];
+    if (a.half) {
+      jf = a.jacc[2 * (size_t)im];
+      jt = a.jacc[2 * (size_t)im + 1];
+    }
   }
-  const float Fc = c == 0 ? h0.x + l0.x : (c == 1 ? h0.y + l0.y : (c == 2 ? h0.z + l0.z : 0.0f));
-  const float tl[3] = {h1.x + l1.x, h1.y + l1.y, h1.z + l1.z};
+  if (a.half) {
+    __syncwarp();   // every lane of the quad has read the j side before lane 0 clears it
+    if (ok && c == 0) {
+      a.jacc[2 * (size_t)im] = make_float4(0.f, 0.f, 0.f, 0.f);
+      a.jacc[2 * (size_t)im + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  const float Fc = c == 0 ? h0.x + (l0.x + jf.x) : (c == 1 ? h0.y + (l0.y + jf.y) : (c == 2 ? h0.z + (l0.z + jf.z) : 0.0f));
+  const float tl[3] = {h1.x + (l1.x + jt.x), h1.y + (l1.y + jt.y), h1.z + (l1.z + jt.z)};
   float ekt2 = 0.0f, ekr2 = 0.0f, dmax2 = 0.0f;
   int bad = 0;
   correct_quad<NQ>(sa, im, ok, c, qin, Fc, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
@@ -364,11 +454,12 @@ __global__ void __launch_bounds__(128) k_integrate_quad(ForceArgs a, StepArgs sa
     int rr = -1;
     if (ok) {
       rr = qin.r;
-      vv[0] = FF{0.5f * h0.w, 0.5f * l0.w};
-      vv[1] = FF{0.5f * h1.w, 0.5f * l1.w};
+      const float pf = a.half ? 1.0f : 0.5f;   // a full list holds every pair twice
+      vv[0] = FF{pf * h0.w, pf * l0.w};
+      vv[1] = FF{pf * h1.w, pf * l1.w};
       vv[2] = FF{ekt2, 0.0f};
       vv[3] = FF{ekr2, 0.0f};
-      vv[4] = FF{0.5f * (float)a.npair_in[im], 0.0f};
+      vv[4] = FF{pf * (float)a.npair_in[im], 0.0f};
     } else {
       dmax2 = 0.0f;
       bad = 0;
@@ -397,7 +488,7 @@ size_t pairs_smem_bytes(int cap) {
   return (size_t)(PairShape<LPI>::THREADS / 32) * PairShape<LPI>::GROUPS * cap * sizeof(int);
 }
 
-template <class M, int LPI, int MODE>
+template <class M, int LPI, int MODE, bool HALF>
 static cudaError_t launch_pairs_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
   const int threads = PairShape<LPI>::THREADS;
   const long long total = (long long)a.n * LPI;
@@ -405,21 +496,30 @@ static cudaError_t launch_pairs_t(const ForceArgs& a, const StepArgs& sa, cudaSt
   if (blocks == 0) return cudaSuccess;
   const size_t smem = pairs_smem_bytes<LPI>(a.ccap);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_pairs<M, LPI, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_pairs<M, LPI, MODE, HALF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_pairs<M, LPI, MODE><<<blocks, threads, smem, s>>>(a, sa);
+  k_pairs<M, LPI, MODE, HALF><<<blocks, threads, smem, s>>>(a, sa);
   return cudaGetLastError();
+}
+
+template <class M, int MODE, bool HALF>
+static cudaError_t launch_pairs_h(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
+  switch (lpi) {
+    case 4: return launch_pairs_t<M, 4, MODE, HALF>(a, sa, s);
+    case 8: return launch_pairs_t<M, 8, MODE, HALF>(a, sa, s);
+    case 16: return launch_pairs_t<M, 16, MODE, HALF>(a, sa, s);
+    default: return launch_pairs_t<M, 32, MODE, HALF>(a, sa, s);
+  }
 }
 
 template <class M, int MODE>
 static cudaError_t launch_pairs_l(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
-  switch (lpi) {
-    case 4: return launch_pairs_t<M, 4, MODE>(a, sa, s);
-    case 8: return launch_pairs_t<M, 8, MODE>(a, sa, s);
-    case 16: return launch_pairs_t<M, 16, MODE>(a, sa, s);
-    default: return launch_pairs_t<M, 32, MODE>(a, sa, s);
+  if constexpr (MODE == 1) {
+    if (a.half) return launch_pairs_h<M, 1, true>(a, sa, lpi, s);
   }
+  return launch_pairs_h<M, MODE, false>(a, sa, lpi, s);
 }
 
 template <int MODE>
@@ -444,7 +544,9 @@ int pairs_max_cap(int lpi) {
 cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStream_t s) {
   StepArgs none;
   memset(&none, 0, sizeof none);
-  return launch_pairs_any<0>(a, none, model, lpi, s);
+  ForceArgs f = a;
+  f.half = 0;
+  return launch_pairs_any<0>(f, none, model, lpi, s);
 }
 
 // After the last step of a mixed run: its replica finish.

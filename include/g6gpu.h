@@ -254,6 +254,13 @@ typedef struct g6_shape {
   int cap;         /* neighbour-list row capacity (entries); g6_set_shape: 0 derives it
                       from the skin and the density (twice the expected row + 64)    */
   double step_ms;  /* g6_tune_shape: the chosen shape's MD step time in the search   */
+  int step_half;   /* mixed MD step: 1 = half list (each pair within rc evaluated once;
+                      the other molecule's force and torque added with float atomics,
+                      so the order of those sums varies and runs are not
+                      bit-reproducible), 0 = full list (every pair from both sides,
+                      fixed summation order, bit-reproducible).  FP64 steps always use
+                      the full list.  Default (no g6_set_shape): half in mixed
+                      precision; g6_tune_shape times both unless g6_set_shape chose */
 } g6_shape;
 #define G6_TUNE_SKIN 1
 /* Autotuner: times the candidates on the uploaded state (restored after every
@@ -273,8 +280,10 @@ int g6_set_shape(g6_ctx* ctx, const g6_shape* shape);
    call a host-side driver makes when it keeps the state itself.  With rec in
    page-locked memory the whole call runs as one CUDA graph, captured on the
    first call for that rec pointer, dt, log choice and lane width (so that
-   first call must not come during a stream capture); pageable rec works
-   too, operation by operation.  The neighbour list of the previous call is
+   first call must not come during a stream capture); in mixed precision its
+   kernels then read and write rec directly through the buffer's device
+   address instead of staging copies.  Pageable rec works too, operation by
+   operation.  The neighbour list of the previous call is
    kept when no molecule moved more than half the skin since it was built. */
 int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log);
 

@@ -212,7 +212,10 @@ def test_md_resumes_from_a_restart_file(precision):
     log_b = s.md_run(dt, 15, th)
     rec_b = s.download_state()
     s.close()
-    tol = 1e-9 if precision == "fp64" else 1e-5
+    # mixed: the split run builds its own neighbour list (another order of the
+    # pair sums) and the half list adds the other molecule's share with atomics
+    # in a varying order; 40 steps of a liquid amplify those FP32 roundings
+    tol = 1e-9 if precision == "fp64" else 1e-4
     np.testing.assert_allclose(rec_b[:, 0:3], rec_a[:, 0:3], rtol=0, atol=tol)
     np.testing.assert_allclose(rec_b[:, 33:37], rec_a[:, 33:37], rtol=0, atol=tol)
     np.testing.assert_allclose(log_b[-1, 0, 5], log_a[-1, 0, 5], rtol=tol)   # H, with the Nose terms

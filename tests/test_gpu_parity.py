@@ -169,13 +169,16 @@ def test_md_nose_follows_oracle(orc):
     assert th[0].zeta[0] == pytest.approx(t_o[4], rel=1e-8)
 
 
-@pytest.mark.parametrize("model,mpw", [("TIP4P", 4), ("TIP4P", 8), ("TIP4P", 16), ("TIP4P", 32), ("ST2", 4),
-                                       ("ST2", 16)])
-def test_md_mixed_integrators_follow_oracle(orc, model, mpw):
+@pytest.mark.parametrize("model,mpw,half", [("TIP4P", 4, 0), ("TIP4P", 8, 0), ("TIP4P", 16, 0), ("TIP4P", 32, 0),
+                                            ("ST2", 4, 0), ("ST2", 16, 0), ("TIP4P", 4, 1), ("TIP4P", 8, 1),
+                                            ("TIP4P", 32, 1), ("ST2", 4, 1), ("ST2", 16, 1), ("TIP5P", 4, 1)])
+def test_md_mixed_integrators_follow_oracle(orc, model, mpw, half):
     """Mixed-precision Gear MD with each integrator kernel (one lane per molecule
     with 8, 16 or 32 molecules per warp; four lanes per molecule for step_mpw 4)
-    under a Nose-Hoover thermostat tracks the oracle's FP64 trajectory for 20
-    steps within the error of FP32 site forces."""
+    and either list form (half: each pair once, the other molecule's force and
+    torque by atomics; full: each pair from both sides) under a Nose-Hoover
+    thermostat tracks the oracle's FP64 trajectory for 20 steps within the
+    error of FP32 site forces."""
     import ctypes
     n = 256
     b = config.water_box(model, n, 7, temp=320.0, dt=0.002, jitter=0.2)
@@ -183,7 +186,7 @@ def test_md_mixed_integrators_follow_oracle(orc, model, mpw):
     q = 300.0 * 0.1 ** 2 / 0.002
     s = g6.RigidWater(model, n, L, path="custom", precision="mixed", rc=8.5, skin=1.0)
     s.upload_state(b["rec"])
-    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=mpw, skin=1.0, cap=0, step_ms=0.0)
+    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=mpw, skin=1.0, cap=0, step_ms=0.0, step_half=half)
     s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
     th = s.thermostats(1, "nose", temp=300.0, q=q, dump=0.0)
     log = s.md_run(0.002, 20, th)
@@ -235,15 +238,26 @@ def test_md_mixed_conserves_energy():
     assert np.ptp(H) < 0.02 * ek
 
 
-@pytest.mark.parametrize("prec,pinned", [("fp64", False), ("mixed", False), ("mixed", True)])
-def test_host_buffer_step_equals_device_step(prec, pinned):
+@pytest.mark.parametrize("prec,pinned,half", [("fp64", False, 0), ("mixed", False, 0), ("mixed", True, 0),
+                                              ("mixed", False, 1), ("mixed", True, 1)])
+def test_host_buffer_step_equals_device_step(prec, pinned, half):
     """g6_md_step_host (state in a host buffer, copied in and out; a page-locked
     buffer takes the cached-graph route) gives the same state, log and
     thermostat as one device-resident step from the same state, on two calls in
-    a row."""
+    a row: bit for bit with the full list, within FP32 rounding with the half
+    list (its atomics sum in a varying order)."""
+    import ctypes
     n = 343
     b = config.water_box("TIP4P", n, 12, temp=300.0, dt=0.002, jitter=0.2)
     s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision=prec, rc=8.5)
+    if prec == "mixed":
+        sh = _capi.Shape()
+        s._check(s.L.g6_get_shape(s.ctx, ctypes.byref(sh)))
+        sh.lpi = sh.lpi or 8
+        sh.step_lpi = sh.step_lpi or 8
+        sh.step_mpw = sh.step_mpw or 4
+        sh.step_half = half
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
     s.upload_state(b["rec"])
     s.md_run(0.002, 50, s.thermostats(1, "nose", temp=300.0, q=300.0 * 0.25 / 0.002))
     rec = s.download_state()
@@ -262,9 +276,17 @@ def test_host_buffer_step_equals_device_step(prec, pinned):
         want = s.download_state()
         lg = np.zeros(10)
         s.md_step_host(0.002, host, th_b, lg)
-        assert np.array_equal(host, want)
-        assert np.array_equal(lg, log_a[0, 0])
-        assert list(th_a[0].zeta) == list(th_b[0].zeta)
+        if half:
+            assert np.abs(host[:, :3] - want[:, :3]).max() < 1e-9
+            assert np.abs(host - want).max() <= 1e-5 * np.abs(want).max()
+            assert np.abs(lg - log_a[0, 0]).max() <= 1e-6 * np.abs(log_a[0, 0]).max()
+            assert lg[6] == log_a[0, 0, 6]
+            host[:] = want      # the next call starts from the same state on both routes
+            ctypes.memmove(ctypes.byref(th_b[0]), ctypes.byref(th_a[0]), ctypes.sizeof(th_a[0]))
+        else:
+            assert np.array_equal(host, want)
+            assert np.array_equal(lg, log_a[0, 0])
+            assert list(th_a[0].zeta) == list(th_b[0].zeta)
 
 
 def test_replicas_equal_separate_systems(orc):
