@@ -565,6 +565,10 @@ static ForceArgs force_args(g6_ctx* c) {
   a.jacc = c->d_jacc; a.half = 0;
   for (int s = 0; s < MAXSITE; ++s)
     for (int k = 0; k < 3; ++k) a.fbody[s][k] = (float)c->mh.body[s][k];
+  a.planar = planar_sites(c->nq, a.fbody) ? 1 : 0;
+  double lmax = 0.0;
+  for (double l : c->L) lmax = std::max(lmax, l);
+  a.band = row_test_band(c->cc.rout + effective_skin(c), lmax);
   return a;
 }
 

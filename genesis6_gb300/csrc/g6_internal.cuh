@@ -223,6 +223,8 @@ struct ForceArgs {
   float fbody[MAXSITE][3];   // body-frame site coordinates (LJ site, charged sites) as float
   float4* jacc;   // mixed MD step, half list: per molecule 2 float4 (force, lab torque) from the pairs others hold
   int half;       // mixed MD step: 1 = half list (each pair once, j side by atomics), 0 = full list
+  int planar;     // 3-charge model with the planar site layout of MT::PLANAR
+  float band;     // mixed row test: |d^2 - rc^2| below this (A^2) is decided by the FP64 test
 };
 
 struct SitesArgs {
@@ -536,6 +538,22 @@ struct ModelHost {
 };
 // charged sites of a model's kernels: 3 (TIP4P, SPC/E) or 4 (TIP5P, ST2)
 inline int model_nq(int model) { return (model == G6_TIP4P || model == G6_SPCE) ? 3 : 4; }
+
+// Band of the mixed row test (ForceArgs::band): its squared separation is off
+// by less than 2 sqrt(3) rlist L/2^23 (coarse_delta drops 9 of the 32 bits of
+// each fixed-point difference) plus a few FP32 roundings; 1e-3 A^2 at least.
+inline float row_test_band(double rlist, double lmax) {
+  const double b = 1.25 * 2.0 * 1.7320508075688772 * rlist * lmax / 8388608.0 + 1e-4;
+  return (float)(b > 1e-3 ? b : 1e-3);
+}
+
+// The planar site layout of MT::PLANAR, checked on the float body coordinates.
+inline bool planar_sites(int nq, const float (&b)[MAXSITE][3]) {
+  if (nq != 3) return false;
+  for (int s = 0; s < 4; ++s)
+    if (b[s][0] != 0.0f) return false;
+  return b[0][1] == 0.0f && b[1][1] == 0.0f && b[2][1] == -b[3][1] && b[2][2] == b[3][2];
+}
 bool make_model(int model, ModelHost& m);
 void make_pair_const(const ModelHost& m, int path, PairConst& pc);
 void make_cut_const(double rin, double rout, CutConst& cc);

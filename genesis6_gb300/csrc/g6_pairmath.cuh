@@ -20,10 +20,15 @@
 
 namespace g6 {
 
-template <int NQ_, bool TAPER_>
+// PLANAR_ (3-charge models): every site has body x = 0, the LJ site and the
+// first charged site lie on the z axis and the other two charged sites are
+// mirror images in y with one z (TIP4P, SPC/E), so a site offset needs only
+// two columns of the rotation.
+template <int NQ_, bool TAPER_, bool PLANAR_ = false>
 struct MT {
   static constexpr int NQ = NQ_;
   static constexpr bool TAPER = TAPER_;
+  static constexpr bool PLANAR = PLANAR_;
   static constexpr int W64 = ((6 + 3 * NQ_) + 1) / 2 * 2;   // doubles per molecule in pk64
   static constexpr int NPK = ((6 + 3 * NQ_) + 3) / 4;        // float4 per molecule in pk32
 };

@@ -65,13 +65,37 @@ __device__ __forceinline__ void load_pose_q(const float4* pkq, int j, float (&v)
 
 // Float site offsets (LJ site, charged sites) from the record's quaternion:
 // the placement's arithmetic (setmatrix_f, site_off_f), so the same bits as
-// the offsets it wrote to pk32.
+// the offsets it wrote to pk32.  A planar model (M::PLANAR: body x = 0 for
+// every site, y = 0 for sites 0 and 1, sites 2 and 3 at (0, +-y, z)) needs only
+// the rotation's second and third columns; its terms with a zero body
+// coordinate are left out, which changes no value (x * 0 + y = y), and the
+// two mirror sites share their z term.
 template <class M>
 __device__ __forceinline__ void sites_from_q(const ForceArgs& a, const float* q, float (&r)[M::NQ + 1][3]) {
-  float t[9];
-  setmatrix_f(q, t);
+  if constexpr (M::PLANAR) {
+    const float qa = q[0], qb = q[1], qc = q[2], qd = q[3];
+    const float aa = __fmul_rn(qa, qa), bb = __fmul_rn(qb, qb), cc = __fmul_rn(qc, qc), dd = __fmul_rn(qd, qd);
+    const float t1 = __fmul_rn(-2.0f, __fmaf_rn(qa, qd, __fmul_rn(qb, qc)));
+    const float t2 = __fmul_rn(2.0f, __fmaf_rn(qb, qd, __fmul_rn(-qa, qc)));
+    const float t4 = __fsub_rn(__fadd_rn(aa, cc), __fadd_rn(bb, dd));
+    const float t5 = __fmul_rn(-2.0f, __fmaf_rn(qa, qb, __fmul_rn(qc, qd)));
+    const float t7 = __fmul_rn(2.0f, __fmaf_rn(qa, qb, __fmul_rn(-qc, qd)));
+    const float t8 = __fsub_rn(__fadd_rn(aa, dd), __fadd_rn(bb, cc));
 #pragma unroll
-  for (int s = 0; s <= M::NQ; ++s) site_off_f(t, a.fbody[s][0], a.fbody[s][1], a.fbody[s][2], r[s]);
+    for (int s = 0; s < 2; ++s) {
+      const float z = a.fbody[s][2];
+      r[s][0] = __fmul_rn(t2, z); r[s][1] = __fmul_rn(t5, z); r[s][2] = __fmul_rn(t8, z);
+    }
+    const float y = a.fbody[2][1], z = a.fbody[2][2];
+    const float zx = __fmul_rn(t2, z), zy = __fmul_rn(t5, z), zz = __fmul_rn(t8, z);
+    r[2][0] = __fmaf_rn(t1, y, zx); r[2][1] = __fmaf_rn(t4, y, zy); r[2][2] = __fmaf_rn(t7, y, zz);
+    r[3][0] = __fmaf_rn(t1, -y, zx); r[3][1] = __fmaf_rn(t4, -y, zy); r[3][2] = __fmaf_rn(t7, -y, zz);
+  } else {
+    float t[9];
+    setmatrix_f(q, t);
+#pragma unroll
+    for (int s = 0; s <= M::NQ; ++s) site_off_f(t, a.fbody[s][0], a.fbody[s][1], a.fbody[s][2], r[s]);
+  }
 }
 
 // The pose record a pair kernel reads per molecule: the 64-byte pk32 record
@@ -123,12 +147,50 @@ __device__ __forceinline__ float4 load_com(const float4* pk32, const float4* pkq
   else return __ldg(pkq + 2 * (size_t)j);
 }
 
+// The row test's COM separation: the integer difference without its low 9
+// bits (|h| < 2^22, converted exactly by the 1.5 * 2^23 bit pattern), times
+// 512 L/2^32.  Each component is low by less than L/2^23 (the band that
+// sends a pair to the FP64 test covers it); 5 instructions per component
+// instead of fix_delta's 9.
+__device__ __forceinline__ float coarse_delta(uint32_t xi, uint32_t xj, float s512) {
+  const int h = (int)(xi - xj) >> 9;
+  return (__int_as_float(0x4B400000 + h) - 12582912.0f) * s512;
+}
+
 // Fixed-point COM difference (units L/2^32, the wrap is the minimum image) to A.
 __device__ __forceinline__ void fix_delta(uint32_t xi, uint32_t yi, uint32_t zi, const float4& qj, float sx, float sy,
                                           float sz, float d[3]) {
   d[0] = i32_to_f32((int)(xi - __float_as_uint(qj.x))) * sx;
   d[1] = i32_to_f32((int)(yi - __float_as_uint(qj.y))) * sy;
   d[2] = i32_to_f32((int)(zi - __float_as_uint(qj.z))) * sz;
+}
+
+// The LPI lanes of a molecule combine their 8 float-pair partials by a
+// butterfly that halves the values each lane carries at every level
+// (reduce-scatter): 4 + 2 + 1 float-pair exchanges instead of 8 per level.
+// Lane sub ends with the sums of values idx .. idx + 8/LPI - 1 (LPI <= 8) or
+// of value idx (LPI > 8, after all-reducing that value over the groups of 8).
+template <int CNT>
+__device__ __forceinline__ void scatter_level(FF (&v)[8], int sub, int m, int& idx) {
+  constexpr int H = CNT / 2;
+  const bool up = (sub & m) != 0;
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    const FF keep = up ? v[k + H] : v[k];
+    const FF send = up ? v[k] : v[k + H];
+    v[k] = ff_add(keep, red_shfl(send, m));
+  }
+  if (up) idx += H;
+}
+template <int LPI>
+__device__ __forceinline__ int ff_reduce_scatter8(FF (&v)[8], int sub) {
+  int idx = 0;
+  if constexpr (LPI >= 2) scatter_level<8>(v, sub, LPI / 2, idx);
+  if constexpr (LPI >= 4) scatter_level<4>(v, sub, LPI / 4, idx);
+  if constexpr (LPI >= 8) scatter_level<2>(v, sub, LPI / 8, idx);
+#pragma unroll
+  for (int m = LPI / 16; m >= 1; m >>= 1) v[0] = ff_add(v[0], red_shfl(v[0], m));
+  return idx;
 }
 
 // MODE 0: force only; 1: MD step.  HALF (MD step only): each pair within rc is
@@ -194,7 +256,8 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   for (int m = 16; m >= 1; m >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, m));
   const int* row = a.nbr + (size_t)(valid ? i : 0) * a.cap;
   const float rout2 = a.cc.frout2;
-  const float band = 1e-3f;   // |dd32 - dd64| is below 1e-4 A^2 for boxes up to 1000 A
+  const float band = a.band;   // above the test's error (coarse_delta, FP32 rounding); set per system
+  const float sx5 = sx * 512.0f, sy5 = sy * 512.0f, sz5 = sz * 512.0f;
   int cnt = 0;
   for (int base = 0; base < nmax; base += LPI * U) {
     int jj[U];
@@ -211,9 +274,10 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
     for (int u = 0; u < U; ++u) {
       bool in = false;
       if (jj[u] >= 0) {
-        float d[3];
-        fix_delta(xi, yi, zi, qj[u], sx, sy, sz, d);
-        const float dd = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float d0 = coarse_delta(xi, __float_as_uint(qj[u].x), sx5);
+        const float d1 = coarse_delta(yi, __float_as_uint(qj[u].y), sy5);
+        const float d2 = coarse_delta(zi, __float_as_uint(qj[u].z), sz5);
+        const float dd = d0 * d0 + d1 * d1 + d2 * d2;
         in = dd < rout2;
         if (fabsf(dd - rout2) < band) {
           // borderline: decide with the reference's FP64 arithmetic (Interaction_Compress2)
@@ -314,18 +378,20 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
     for (int k = 0; k < 3; ++k) { q8[k] = FF{fo[k], 0.0f}; q8[3 + k] = FF{to[k], 0.0f}; }
     q8[6] = FF{acc.e, 0.0f};
     q8[7] = FF{acc.w[0], 0.0f};
+    const int idx = ff_reduce_scatter8<LPI>(q8, sub);
+    constexpr int C = LPI >= 8 ? 1 : 8 / LPI;   // values each lane ends with
+    if (valid && (LPI <= 8 || (sub & (LPI / 8 - 1)) == 0)) {
+      // fres: [F.hi, E.hi] [F.lo, E.lo] [tau.hi, W.hi] [tau.lo, W.lo]
+      float* o = (float*)(a.fres + (size_t)4 * i);
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
-#pragma unroll
-      for (int m = LPI / 2; m >= 1; m >>= 1) q8[k] = ff_add(q8[k], red_shfl(q8[k], m));
-    if (valid && sub == 0) {
-      float4* o = a.fres + (size_t)4 * i;
-      o[0] = make_float4(q8[0].hi, q8[1].hi, q8[2].hi, q8[6].hi);
-      o[1] = make_float4(q8[0].lo, q8[1].lo, q8[2].lo, q8[6].lo);
-      o[2] = make_float4(q8[3].hi, q8[4].hi, q8[5].hi, q8[7].hi);
-      o[3] = make_float4(q8[3].lo, q8[4].lo, q8[5].lo, q8[7].lo);
-      a.npair_in[i] = cnt;
+      for (int c = 0; c < C; ++c) {
+        const int k = idx + c;
+        const int pos = k < 3 ? k : (k < 6 ? 5 + k : (k == 6 ? 3 : 11));
+        o[pos] = q8[c].hi;
+        o[pos + 4] = q8[c].lo;
+      }
     }
+    if (valid && sub == 0) a.npair_in[i] = cnt;
   }
 }
 
@@ -524,7 +590,10 @@ static cudaError_t launch_pairs_l(const ForceArgs& a, const StepArgs& sa, int lp
 
 template <int MODE>
 static cudaError_t launch_pairs_any(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
-  if (model_nq(model) == 3) return launch_pairs_l<MT<3, false>, MODE>(a, sa, lpi, s);
+  if (model_nq(model) == 3) {
+    if (MODE == 1 && a.planar) return launch_pairs_l<MT<3, false, true>, MODE>(a, sa, lpi, s);
+    return launch_pairs_l<MT<3, false>, MODE>(a, sa, lpi, s);
+  }
   if (a.pc.taper) return launch_pairs_l<MT<4, true>, MODE>(a, sa, lpi, s);
   return launch_pairs_l<MT<4, false>, MODE>(a, sa, lpi, s);
 }
