@@ -569,6 +569,7 @@ static ForceArgs force_args(g6_ctx* c) {
   double lmax = 0.0;
   for (double l : c->L) lmax = std::max(lmax, l);
   a.band = row_test_band(c->cc.rout + effective_skin(c), lmax);
+  for (int k = 0; k < 3; ++k) a.fs1[k] = (float)(c->L[k] / 4294967296.0);   // the values of d_fscale
   return a;
 }
 

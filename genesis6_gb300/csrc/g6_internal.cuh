@@ -221,10 +221,12 @@ struct ForceArgs {
   const float4* pkq;     // mixed list kernel: 2 float4 per molecule (fixed-point COM, float quaternion)
   const float4* pkq_1;   // the same for pose buffer 1
   float fbody[MAXSITE][3];   // body-frame site coordinates (LJ site, charged sites) as float
-  float4* jacc;   // mixed MD step, half list: per molecule 2 float4 (force, lab torque) from the pairs others hold
+  float4* jacc;   // mixed MD step, half list: per molecule 2 float4 (minus its force, its lab torque) from the
+                  // pairs others hold
   int half;       // mixed MD step: 1 = half list (each pair once, j side by atomics), 0 = full list
   int planar;     // 3-charge model with the planar site layout of MT::PLANAR
   float band;     // mixed row test: |d^2 - rc^2| below this (A^2) is decided by the FP64 test
+  float fs1[3];   // one replica: its fixed-point scales L/2^32 (rep.fscale[0..2]), read without a load
 };
 
 struct SitesArgs {

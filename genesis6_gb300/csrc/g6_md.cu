@@ -77,6 +77,51 @@ __device__ __forceinline__ int state_float_col(int sc) {
 // sides are coalesced.
 constexpr int REC_TILE = 32;
 constexpr int REC_THREADS = 128;
+constexpr int REC_V2 = REC_TILE * REC / 2;                                // double2 per full tile (848)
+constexpr int REC_V2_PER = (REC_V2 + REC_THREADS - 1) / REC_THREADS;      // per thread (7)
+constexpr int REC_PER = (REC_TILE * REC + REC_THREADS - 1) / REC_THREADS;  // doubles per thread (14)
+
+// One tile of records (m molecules from src) into shared memory and, when
+// keep is set, into a device copy.  Every load of the thread is issued before
+// the first store (a store to global memory between them would order each
+// load after it: one round trip per element, costly when src is host memory
+// read over the host link); a full tile on a 16-byte boundary moves as double2.
+__device__ __forceinline__ void rec_tile_in(const double* src, int m, double* tile, double* keep) {
+  if (m == REC_TILE && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    double2 v[REC_V2_PER];
+#pragma unroll
+    for (int u = 0; u < REC_V2_PER; ++u) {
+      const int t = threadIdx.x + u * REC_THREADS;
+      if (t < REC_V2) v[u] = s2[t];
+    }
+    double2* t2 = reinterpret_cast<double2*>(tile);
+    double2* k2 = reinterpret_cast<double2*>(keep);   // device copy: 16-byte aligned at a full tile
+#pragma unroll
+    for (int u = 0; u < REC_V2_PER; ++u) {
+      const int t = threadIdx.x + u * REC_THREADS;
+      if (t < REC_V2) {
+        t2[t] = v[u];
+        if (keep) k2[t] = v[u];
+      }
+    }
+  } else {
+    double v[REC_PER];
+#pragma unroll
+    for (int u = 0; u < REC_PER; ++u) {
+      const int t = threadIdx.x + u * REC_THREADS;
+      if (t < m * REC) v[u] = src[t];
+    }
+#pragma unroll
+    for (int u = 0; u < REC_PER; ++u) {
+      const int t = threadIdx.x + u * REC_THREADS;
+      if (t < m * REC) {
+        tile[t] = v[u];
+        if (keep) keep[t] = v[u];
+      }
+    }
+  }
+}
 
 // One mixed-precision step with the state in the caller's record buffer
 // (g6_md_step_host): the records (n,53) become the FP64 state (com, d1, w1,
@@ -90,7 +135,7 @@ constexpr int REC_THREADS = 128;
 // so the head only compares one word.
 __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, HostInArgs h, float* stf, ThermoDev* th,
                                                                double dt) {
-  __shared__ double tile[REC_TILE * REC];
+  __shared__ __align__(16) double tile[REC_TILE * REC];
   if (blockIdx.x == 0) {
     for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
       ThermoDev& T = th[r];
@@ -107,12 +152,7 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, Host
   const int i0 = blockIdx.x * REC_TILE;
   const int m = min(REC_TILE, n - i0);
   if (m <= 0) return;
-  const double* src = h.rec + (size_t)i0 * REC;
-  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) {
-    const double v = src[t];
-    tile[t] = v;
-    if (h.keep) h.keep[(size_t)i0 * REC + t] = v;
-  }
+  rec_tile_in(h.rec + (size_t)i0 * REC, m, tile, h.keep ? h.keep + (size_t)i0 * REC : nullptr);
   __syncthreads();
   double* st = a.st;
   for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
@@ -155,7 +195,7 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, Host
 // state and as records (n,53) in `out` for the copy to the caller -- the work
 // of k_finish_step, k_stf_move and k_rec_transpose in one launch.
 __global__ void __launch_bounds__(REC_THREADS) k_host_out_mixed(StepArgs sa, double* out) {
-  __shared__ double tile[REC_TILE * REC];
+  __shared__ __align__(16) double tile[REC_TILE * REC];
   const int nfin = sa.p.rep.nrep;
   if ((int)blockIdx.x < nfin) {
     finish_pending(sa, blockIdx.x, 32);
@@ -166,23 +206,41 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_out_mixed(StepArgs sa, dou
   const int m = min(REC_TILE, n - i0);
   if (m <= 0) return;
   double* st = sa.p.st;
-  for (int t = threadIdx.x; t < REC_TILE * REC; t += blockDim.x) {
+  // all loads of the thread first (the FP64 columns and the float small
+  // terms), then the small terms back into the FP64 state and the tile
+  double v[REC_PER];
+#pragma unroll
+  for (int u = 0; u < REC_PER; ++u) {
+    const int t = threadIdx.x + u * REC_THREADS;
     const int c = t / REC_TILE, k = t % REC_TILE;
-    if (k >= m) continue;
-    const size_t at = (size_t)c * n + i0 + k;
-    const int fc = state_float_col(c);
-    double v;
-    if (fc < 0) {
-      v = st[at];
-    } else {
-      v = (double)sa.stf[(size_t)fc * n + i0 + k];
-      st[at] = v;
+    v[u] = 0.0;
+    if (t < REC_TILE * REC && k < m) {
+      const int fc = state_float_col(c);
+      v[u] = fc < 0 ? st[(size_t)c * n + i0 + k] : (double)sa.stf[(size_t)fc * n + i0 + k];
     }
-    tile[k * REC + c] = v;
+  }
+#pragma unroll
+  for (int u = 0; u < REC_PER; ++u) {
+    const int t = threadIdx.x + u * REC_THREADS;
+    const int c = t / REC_TILE, k = t % REC_TILE;
+    if (t < REC_TILE * REC && k < m) {
+      if (state_float_col(c) >= 0) st[(size_t)c * n + i0 + k] = v[u];
+      tile[k * REC + c] = v[u];
+    }
   }
   __syncthreads();
   double* dst = out + (size_t)i0 * REC;
-  for (int t = threadIdx.x; t < m * REC; t += blockDim.x) dst[t] = tile[t];
+  if (m == REC_TILE && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    const double2* t2 = reinterpret_cast<const double2*>(tile);
+#pragma unroll
+    for (int u = 0; u < REC_V2_PER; ++u) {
+      const int t = threadIdx.x + u * REC_THREADS;
+      if (t < REC_V2) d2[t] = t2[t];
+    }
+  } else {
+    for (int t = threadIdx.x; t < m * REC; t += blockDim.x) dst[t] = tile[t];
+  }
 }
 
 // First predict + placement of a mixed run (plus the first Nose_Predict).

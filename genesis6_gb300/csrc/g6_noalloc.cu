@@ -244,6 +244,7 @@ extern "C" int g6_force_noalloc(int model, int path, int precision, int n, const
   for (int q = 0; q < MAXSITE; ++q)
     for (int k = 0; k < 3; ++k) fa.fbody[q][k] = pa.fbody[q][k];
   fa.band = row_test_band(rlist, std::max(box[0], std::max(box[1], box[2])));
+  for (int k = 0; k < 3; ++k) fa.fs1[k] = (float)(box[k] / 4294967296.0);
 
   const int blocks = (n + 255) / 256;
   k_setup<<<blocks, 256, 0, s>>>(su, base);

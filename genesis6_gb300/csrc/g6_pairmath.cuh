@@ -98,7 +98,8 @@ struct Acc {
 };
 
 // The j side of one pair for the half list (each pair evaluated once): the
-// force on j is minus the pair force on i, and j's torque about its COM
+// force on j is minus the pair force on i (f holds the pair force on i; the
+// consumer subtracts it), and j's torque about its COM
 // follows from the site forces being central: (d + r_ia - r_jb) x f_ab = 0, so
 // sum_ab r_jb x (-f_ab) = -sum_a (d + r_ia) x F_ia with F_ia the (switched)
 // force on i's site a from all of j's sites.  The COM switch force acts along
@@ -184,7 +185,7 @@ __device__ __forceinline__ void pair_math(const R d[3], R dd, const R (&ri)[M::N
       tz += vy * us[a][0] - vx * us[a][1];
     }
     pj->t[0] = tx; pj->t[1] = ty; pj->t[2] = tz;
-    pj->f[0] = -fp[0]; pj->f[1] = -fp[1]; pj->f[2] = -fp[2];
+    pj->f[0] = fp[0]; pj->f[1] = fp[1]; pj->f[2] = fp[2];
   }
   if constexpr (NW == 9) {
 #pragma unroll

@@ -238,12 +238,16 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   float sx = 0.f, sy = 0.f, sz = 0.f;
   int r = 0, nn = 0;
   if (valid) {
-    r = a.rep.mol_rep[i];
     float wi[RW];
     load_rec<M, HALF>(pk32, pkq, i, wi);
+    if (a.rep.nrep == 1) {   // one replica: the scales are kernel arguments (no dependent load)
+      sx = a.fs1[0]; sy = a.fs1[1]; sz = a.fs1[2];
+    } else {
+      r = a.rep.mol_rep[i];
+      sx = a.rep.fscale[3 * r]; sy = a.rep.fscale[3 * r + 1]; sz = a.rep.fscale[3 * r + 2];
+    }
     xi = __float_as_uint(wi[0]); yi = __float_as_uint(wi[1]); zi = __float_as_uint(wi[2]);
     rec_sites<M, HALF>(a, wi, ri);
-    sx = a.rep.fscale[3 * r]; sy = a.rep.fscale[3 * r + 1]; sz = a.rep.fscale[3 * r + 2];
     nn = a.nnb[i];
   } else {
 #pragma unroll
@@ -395,8 +399,9 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   }
 }
 
-// Half list: the j-side force and torque the pair kernel accumulated for
-// molecule im, cleared for the next step's atomics.
+// Half list: the j side the pair kernel accumulated for molecule im (the
+// sum of its partners' pair forces, which the caller subtracts, and its lab
+// torque from those pairs), cleared for the next step's atomics.
 __device__ __forceinline__ void take_jside(const ForceArgs& a, int im, float4& jf, float4& jt) {
   float4* p = a.jacc + 2 * (size_t)im;
   jf = p[0];
@@ -446,7 +451,7 @@ __global__ void __launch_bounds__(32 * (32 / MPW)) k_integrate_mixed(ForceArgs a
       const float4 h0 = o[0], l0 = o[1], h1 = o[2], l1 = o[3];
       float4 jf = make_float4(0.f, 0.f, 0.f, 0.f), jt = jf;
       if (a.half) take_jside(a, im, jf, jt);
-      const float F[3] = {h0.x + (l0.x + jf.x), h0.y + (l0.y + jf.y), h0.z + (l0.z + jf.z)};
+      const float F[3] = {h0.x + (l0.x - jf.x), h0.y + (l0.y - jf.y), h0.z + (l0.z - jf.z)};
       const float tl[3] = {h1.x + (l1.x + jt.x), h1.y + (l1.y + jt.y), h1.z + (l1.z + jt.z)};
       float ekt2, ekr2;
       correct_mixed<NQ>(sa, im, min, F, tl, step, predict_next, pose_buf(sa, odd ? 0 : 1), ekt2, ekr2, dmax2, bad);
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(128) k_integrate_quad(ForceArgs a, StepArgs sa
       a.jacc[2 * (size_t)im + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
-  const float Fc = c == 0 ? h0.x + (l0.x + jf.x) : (c == 1 ? h0.y + (l0.y + jf.y) : (c == 2 ? h0.z + (l0.z + jf.z) : 0.0f));
+  const float Fc = c == 0 ? h0.x + (l0.x - jf.x) : (c == 1 ? h0.y + (l0.y - jf.y) : (c == 2 ? h0.z + (l0.z - jf.z) : 0.0f));
   const float tl[3] = {h1.x + (l1.x + jt.x), h1.y + (l1.y + jt.y), h1.z + (l1.z + jt.z)};
   float ekt2 = 0.0f, ekr2 = 0.0f, dmax2 = 0.0f;
   int bad = 0;
