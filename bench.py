@@ -549,6 +549,20 @@ def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equi
     s.close()
     ratios = [r["ess_per_gpu_s_learned_over_fixed"] for r in runs]
     charged = [r["with_collect_and_train_charged"] for r in runs]
+    # <U> over the seeds: each seed's mean is one independent estimate, so the
+    # scatter between seeds gives a standard error that does not rest on one
+    # run's ESS estimate
+    uf = np.array([r["fixed"]["mean_U_internal"] for r in runs])
+    ul = np.array([r["learned"]["mean_U_internal"] for r in runs])
+    pooled = None
+    if len(runs) > 1:
+        se = np.sqrt(uf.var(ddof=1) / len(uf) + ul.var(ddof=1) / len(ul))
+        pooled = {"fixed": float(uf.mean()), "learned": float(ul.mean()),
+                  "stderr_between_seeds": float(se),
+                  "difference_in_sigma": float((ul.mean() - uf.mean()) / se) if se > 0 else 0.0,
+                  "per_seed_stderr_over_between_seed_scatter_fixed":
+                      float(np.mean([r["fixed"]["stderr_U"] for r in runs]) / uf.std(ddof=1)) if uf.std(ddof=1) > 0
+                      else None}
     q = max(equil_sweeps // 4, 1)
     return {"chains": C, "molecules_per_chain": N, "model": "ST2 (custom path, Coulomb taper)", "T_K": T,
             "rc_A": rc, "start": "lattice, MD melt 5,000 steps at 400 K, MD %d steps at %g K (%.1f s)" % (md_steps, T, t_md),
@@ -559,6 +573,7 @@ def bench_mc(torch, seed=20261203, seeds=3, sweeps=3000, records=1_000_000, equi
             "ess_per_gpu_s_learned_over_fixed_per_seed": ratios,
             "with_collect_and_train_charged_per_seed": charged,
             "mean_U_difference_in_sigma_per_seed": [r["mean_U_difference_in_sigma"] for r in runs],
+            "mean_U_over_seeds": pooled,
             "runs": runs, "umbrella": umbrella, "U_unit": "10 J/mol per chain (internal)"}
 
 
