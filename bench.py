@@ -629,21 +629,27 @@ def bench_rms(torch, rec_eq, L, snapshots=100, every=20):
     sm = make_system("TIP4P", N_MAIN, "mixed", L, rec_eq)
     s64 = make_system("TIP4P", N_MAIN, "fp64", L, rec_eq)
     th = thermo_for(sm)
-    num_f = den_f = num_t = den_t = 0.0
+    num_f = den_f = num_t = den_t = num_fs = num_ts = 0.0
     worst = 0.0
     for k in range(snapshots):
         sm.md_run(DT, every, th, log=False)
         rec = sm.download_state()
         s64.upload_state(rec)
         Fm, tm, _, _ = sm.force()
+        Fs, ts, _ = sm.step_forces()
         F6, t6, _, _ = s64.force()
         num_f += float(np.sum((Fm - F6) ** 2)); den_f += float(np.sum(F6 ** 2))
         num_t += float(np.sum((tm - t6) ** 2)); den_t += float(np.sum(t6 ** 2))
+        num_fs += float(np.sum((Fs - F6) ** 2)); num_ts += float(np.sum((ts - t6) ** 2))
         worst = max(worst, float(np.sqrt(np.sum((Fm - F6) ** 2) / np.sum(F6 ** 2))))
     sm.close(); s64.close()
     return {"snapshots": snapshots, "every_steps": every, "rms_force_rel": float(np.sqrt(num_f / den_f)),
             "rms_torque_rel": float(np.sqrt(num_t / den_t)), "worst_snapshot_force_rel": worst,
-            "against": "the FP64 path on the same configurations"}
+            "md_step_rms_force_rel": float(np.sqrt(num_fs / den_f)),
+            "md_step_rms_torque_rel": float(np.sqrt(num_ts / den_t)),
+            "against": "the FP64 path on the same configurations; rms_*: the force-only call (full list, lanes "
+                       "combined in FP64), md_step_*: the MD step's pair kernel (g6_step_forces: its list form, "
+                       "float-pair lanes, partner shares by float atomics)"}
 
 
 def c3_state(model, seed, melt=2000, equil=2000, dt=0.001):
@@ -687,17 +693,21 @@ def bench_c3(torch, flush, model="TIP4P", seed=20261205, steps=5000, snapshots=2
     sm = make_system(model, n, "mixed", L, start)
     s64 = make_system(model, n, "fp64", L, start)
     # RMS force/torque error on snapshots of the mixed trajectory
-    num_f = den_f = num_t = den_t = 0.0
+    num_f = den_f = num_t = den_t = num_fs = num_ts = 0.0
     for k in range(snapshots):
         sm.md_run(dt, every, sm.thermostats(1, "nve"), log=False)
         rec = sm.download_state()
         s64.upload_state(rec)
         Fm, tm, _, _ = sm.force()
+        Fs, ts, _ = sm.step_forces()
         F6, t6, _, _ = s64.force()
         num_f += float(np.sum((Fm - F6) ** 2)); den_f += float(np.sum(F6 ** 2))
         num_t += float(np.sum((tm - t6) ** 2)); den_t += float(np.sum(t6 ** 2))
+        num_fs += float(np.sum((Fs - F6) ** 2)); num_ts += float(np.sum((ts - t6) ** 2))
     out["rms_force_rel"] = float(np.sqrt(num_f / den_f))
     out["rms_torque_rel"] = float(np.sqrt(num_t / den_t))
+    out["md_step_rms_force_rel"] = float(np.sqrt(num_fs / den_f))     # the MD step's own pair-kernel forces
+    out["md_step_rms_torque_rel"] = float(np.sqrt(num_ts / den_t))
     out["rms_snapshots"] = {"count": snapshots, "every_steps": every, "against": "the FP64 path (oracle-pinned to 1e-12)"}
     # device-timed steps (NVE, one-step graphs with events, L2 flushed between steps)
     nve = lambda s: s.thermostats(1, "nve")

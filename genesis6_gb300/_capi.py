@@ -33,7 +33,7 @@ REC = 53
 SYMBOLS = [
     "g6_version", "g6_last_error", "g6_status_string", "g6_model_info", "g6_ctx_create", "g6_ctx_destroy",
     "g6_system", "g6_set_cutoff", "g6_set_grid", "g6_set_skin", "g6_set_box", "g6_upload_state",
-    "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force",
+    "g6_download_state", "g6_upload_poses", "g6_cells", "g6_pairsearch", "g6_get_pairs", "g6_force", "g6_step_forces",
     "g6_molecule_energies", "g6_rdf", "g6_hbonds", "g6_force_sites", "g6_pair_potential", "g6_pairsearch_hetero",
     "g6_force_sites_hetero", "g6_md_run", "g6_md_step_host",
     "g6_replica_exchange", "g6_replica_exchange_umbrella", "g6_exchange_plan", "g6_replica_scale", "g6_last_epot",
@@ -101,6 +101,7 @@ def lib():
     L.g6_pairsearch.argtypes = [vp, ctypes.POINTER(i64)]
     L.g6_get_pairs.argtypes = [vp, i64, ip, ip, dp, dp, dp, dp, dp]
     L.g6_force.argtypes = [vp, dp, dp, dp, dp]
+    L.g6_step_forces.argtypes = [vp, dp, dp, dp]
     L.g6_molecule_energies.argtypes = [vp, dp]
     L.g6_rdf.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(i64)]
     L.g6_hbonds.argtypes = [vp, i64, ip, ip, ip, ctypes.POINTER(i64)]

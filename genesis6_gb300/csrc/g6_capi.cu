@@ -610,6 +610,9 @@ static int enqueue_rebuild(g6_ctx* ctx, const int* ctrl, const StepArgs* step = 
 }
 
 static void apply_cached_shape(g6_ctx* ctx);
+extern "C" {
+static StepArgs step_args(g6_ctx* ctx, double dt, double* log);   // defined with the MD entry points
+}
 
 static int force_once(g6_ctx* ctx) {
   int rc = prepare_list(ctx);
@@ -963,11 +966,10 @@ int g6_get_pairs(g6_ctx* ctx, int64_t cap, int* pi, int* pj, double* ox, double*
   return G6_OK;
 }
 
-int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir) {
-  int rc = check_ready(ctx, true);
-  if (rc) return rc;
-  rc = force_once(ctx);
-  if (rc) return rc;
+// Per-molecule F and lab torque (d_F, d_tl), rotation (d_tmat), energies
+// (d_emol) and virials (d_wmol, when vir is wanted) to the caller's arrays:
+// F (n,3), body torque (n,3), epot and vir per replica.
+static int copy_forces(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir) {
   const int n = ctx->n;
   std::vector<double> hF(3 * (size_t)n), hT(3 * (size_t)n), hM(9 * (size_t)n), hE(n), hW(9 * (size_t)n);
   CK(cudaMemcpy(hF.data(), ctx->d_F, hF.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -998,6 +1000,52 @@ int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir) {
       for (int k = 0; k < 9; ++k) vir[9 * r + k] = w[k];
   }
   return G6_OK;
+}
+
+int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  rc = force_once(ctx);
+  if (rc) return rc;
+  return copy_forces(ctx, F, tau, epot, vir);
+}
+
+int g6_step_forces(g6_ctx* ctx, double* F, double* tau, double* epot) {
+  int rc = check_ready(ctx, true);
+  if (rc) return rc;
+  if (ctx->prec != G6_MIXED)
+    return fail(ctx, G6_ERR_STATE, "g6_step_forces: mixed precision only (the FP64 step fuses force and corrector)");
+  if (ctx->in_run) return fail(ctx, G6_ERR_STATE, "g6_step_forces inside g6_md_begin/g6_md_end");
+  if ((rc = prepare_list(ctx))) return rc;
+  apply_cached_shape(ctx);
+  if (ctx->lpi == 0) ctx->lpi = default_lpi(ctx);
+  if (ctx->step_lpi == 0) ctx->step_lpi = default_lpi(ctx);
+  if (ctx->step_mpw == 0) ctx->step_mpw = default_mpw(ctx);
+  if (ctx->step_half < 0) ctx->step_half = default_half(ctx);
+  if (ctx->ccap > pairs_max_cap(32))
+    return fail(ctx, G6_ERR_CAPACITY, "neighbour-list rows too long for the shared-memory rows (lower the skin)");
+  ctx->step_lpi = fit_lpi(ctx, ctx->step_lpi);
+  const bool half = step_uses_half(ctx);
+  CK(cudaMemsetAsync(ctx->d_overflow, 0, sizeof(int), ctx->stream));
+  // step 0 (pose buffer 0) with no finished step for the pair kernel's first blocks to finish
+  CK(cudaMemsetAsync(ctx->d_ctrl, 0, 8 * sizeof(int), ctx->stream));
+  CK(launch_predict_place(place_args(ctx), 0, ctx->d_th, 0, ctx->stream));
+  if (ctx->coop_grid == 0) ctx->coop_grid = rebuild_grid_limit();
+  CellArgs ca = cell_args(ctx, ctx->glist, nullptr);
+  CK(launch_rebuild(ca, list_args(ctx, nullptr, half), ctx->glist.d_start, ctx->glist.d_cellmol, ctx->coop_grid,
+                    nullptr, ctx->stream));
+  ctx->rows_half = half;
+  ForceArgs fa = force_args(ctx);
+  fa.ctrl = ctx->d_ctrl;
+  fa.half = half ? 1 : 0;
+  const StepArgs sa = step_args(ctx, 1.0, nullptr);
+  CK(launch_step_pair_forces(fa, sa, ctx->model, ctx->step_lpi, ctx->stream));
+  int ovf = 0;
+  CK(cudaMemcpyAsync(&ovf, ctx->d_overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ovf == 2) return fail(ctx, G6_ERR_CUDA, "neighbour-list rebuild was not launched cooperatively");
+  if (ovf) return fail(ctx, G6_ERR_CAPACITY, "neighbour-list row overflow");
+  return copy_forces(ctx, F, tau, epot, nullptr);
 }
 
 int g6_molecule_energies(g6_ctx* ctx, double* e) {

@@ -567,6 +567,8 @@ cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cud
 cudaError_t launch_pairs_force(const ForceArgs& a, int model, int lpi, cudaStream_t s);
 cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
                               cudaEvent_t between);
+// The mixed MD step's pair kernel alone, its forces to F, tl and emol (FP64).
+cudaError_t launch_step_pair_forces(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s);
 int pairs_max_cap(int lpi);
 cudaError_t launch_finish_step(const StepArgs& sa, int nrep, cudaStream_t s);
 cudaError_t launch_force_sites(const SitesArgs& a, int model, cudaStream_t s);

@@ -673,6 +673,34 @@ static cudaError_t launch_integrate(const ForceArgs& a, const StepArgs& sa, int 
   }
 }
 
+// The forces of the MD step's pair kernel without the integrator: fres (and,
+// for the half list, minus the partner share in jacc, which is cleared) to
+// FP64 F and lab torque, the energy share to emol.
+__global__ void __launch_bounds__(128) k_step_forces(ForceArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const float4* o = a.fres + (size_t)4 * i;
+  const float4 h0 = o[0], l0 = o[1], h1 = o[2], l1 = o[3];
+  double f[3] = {(double)h0.x + (double)l0.x, (double)h0.y + (double)l0.y, (double)h0.z + (double)l0.z};
+  double t[3] = {(double)h1.x + (double)l1.x, (double)h1.y + (double)l1.y, (double)h1.z + (double)l1.z};
+  if (a.half) {
+    float4 jf, jt;
+    take_jside(a, i, jf, jt);
+    f[0] -= jf.x; f[1] -= jf.y; f[2] -= jf.z;
+    t[0] += jt.x; t[1] += jt.y; t[2] += jt.z;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { a.F[(size_t)k * a.n + i] = f[k]; a.tl[(size_t)k * a.n + i] = t[k]; }
+  a.emol[i] = (a.half ? 1.0 : 0.5) * ((double)h0.w + (double)l0.w);
+}
+
+cudaError_t launch_step_pair_forces(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
+  cudaError_t e = launch_pairs_any<1>(a, sa, model, lpi, s);
+  if (e != cudaSuccess || a.n == 0) return e;
+  k_step_forces<<<(a.n + 127) / 128, 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 // Mixed MD step: pair kernel, then the integrator kernel (mpw molecules per warp).
 cudaError_t launch_step_mixed(const ForceArgs& a, const StepArgs& sa, int model, int lpi, int mpw, cudaStream_t s,
                               cudaEvent_t between) {

@@ -108,6 +108,14 @@ class RigidWater:
         self._check(self.L.g6_force(self.ctx, dptr(F), dptr(tau), dptr(ep), dptr(vir)))
         return F, tau, ep, vir.reshape(self.nrep, 3, 3)
 
+    def step_forces(self):
+        """The mixed MD step's pair-kernel forces on the uploaded poses (its
+        list form and lanes): F (n,3), body torque (n,3), epot (nrep,)."""
+        F = np.zeros((self.n, 3)); tau = np.zeros((self.n, 3))
+        ep = np.zeros(self.nrep)
+        self._check(self.L.g6_step_forces(self.ctx, dptr(F), dptr(tau), dptr(ep)))
+        return F, tau, ep
+
     def molecule_energies(self):
         e = np.zeros(self.n)
         self._check(self.L.g6_molecule_energies(self.ctx, dptr(e)))

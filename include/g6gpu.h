@@ -131,6 +131,14 @@ int g6_get_pairs(g6_ctx* ctx, int64_t cap, int* pi, int* pj, double* ox, double*
    F (n,3), body-frame torque tau (n,3), per-replica potential energy
    epot[nrep] and virial vir[nrep*9].  Any output pointer may be NULL. */
 int g6_force(g6_ctx* ctx, double* F, double* tau, double* epot, double* vir);
+
+/* No counterpart in the reference: the forces exactly as the mixed MD step's
+   pair kernel computes them on the uploaded poses (the context's list form
+   and lanes: with the half list each pair is evaluated once and the other
+   molecule's share added by float atomics), before its integrator uses them.
+   F, tau and epot as in g6_force (no virial).  Mixed precision only; returns
+   G6_ERR_STATE for an FP64 context, whose step fuses force and corrector. */
+int g6_step_forces(g6_ctx* ctx, double* F, double* tau, double* epot);
 /* Per-molecule potential energy e_i = 1/2 sum_j e_ij (n) of the uploaded poses. */
 int g6_molecule_energies(g6_ctx* ctx, double* e);
 /* Site-site distance histograms of the uploaded poses, radialdistrib

@@ -102,6 +102,59 @@ def test_force_mixed_rms_error(orc, model, path):
     assert ep[0] == pytest.approx(Eo, rel=1e-5)
 
 
+@pytest.mark.parametrize("model,path,half", [("TIP4P", "custom", 1), ("TIP4P", "custom", 0), ("TIP4P", "std", 1),
+                                            ("TIP5P", "custom", 1), ("ST2", "custom", 1), ("ST2", "std", 1),
+                                            ("SPCE", "std", 1)])
+def test_md_step_forces_rms_error(orc, model, path, half):
+    """The forces of the mixed MD step's pair kernel itself (g6_step_forces:
+    half list with the partner's share by float atomics, or the full list)
+    against the FP64 oracle: relative RMS force and torque error <= 1e-5."""
+    import ctypes
+    n = 512
+    L = config.box_edge(n)
+    rc = min(9.0, 0.5 * L - 0.05)
+    s, b = _system(model, path, n, 33, prec="mixed", rc=rc)
+    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=4, skin=1.0, cap=0, step_ms=0.0, step_half=half)
+    s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+    F, tau, ep = s.step_forces()
+    Fo, to, Eo, Vo, _ = orc.compute(model, path, b["com"], b["quat"], b["L"], [rc] * 3, rc - 2.0, rc)
+    ef = np.sqrt(((F - Fo) ** 2).sum() / (Fo ** 2).sum())
+    et = np.sqrt(((tau - to) ** 2).sum() / (to ** 2).sum())
+    assert ef <= 1e-5, ef
+    assert et <= 1e-5, et
+    assert ep[0] == pytest.approx(Eo, rel=1e-5)
+    # the step's forces also agree with the force-only entry's mixed forces
+    F2, tau2, ep2, _ = s.force()
+    assert np.sqrt(((F - F2) ** 2).sum() / (F2 ** 2).sum()) <= 1e-5
+
+
+def test_md_step_forces_then_md_run():
+    """A half-row list left by g6_step_forces is rebuilt in full form for a
+    full-list run, and the run follows the same run on a fresh context."""
+    import ctypes
+    n = 343
+    b = config.water_box("TIP4P", n, 14, temp=300.0, dt=0.002, jitter=0.2)
+    runs = []
+    for first in (True, False):
+        s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision="mixed", rc=8.5)
+        s.upload_state(b["rec"])
+        if first:
+            s.step_forces()   # half rows (the default list form)
+        sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=4, skin=1.0, cap=0, step_ms=0.0, step_half=0)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+        runs.append((s.md_run(0.002, 10), s.download_state()))
+        s.close()
+    assert np.array_equal(runs[0][0][:, 0, 6], runs[1][0][:, 0, 6])   # pairs within rc
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_step_forces_refuses_fp64():
+    s, b = _system("TIP4P", "custom", 216, 3, prec="fp64", rc=8.0)
+    with pytest.raises(g6.G6Error) as e:
+        s.step_forces()
+    assert e.value.status == _capi.G6_ERR_STATE
+
+
 @pytest.mark.parametrize("model,path", CASES)
 def test_force_sites_entry_matches_reference_call(orc, model, path):
     """g6_force_sites / g6_pair_potential mirror force()/PairPotential() on the caller's pair list."""
