@@ -1,31 +1,37 @@
 // g6_pairs.cu -- mixed-precision site-site forces over the Verlet list, and the
-// integrator kernel of the mixed MD step.
+// integrator kernels of the mixed MD step.
 //
-// k_pairs<Model, LPI, MODE>: LPI lanes cooperate on one molecule i; a warp
-// holds 32/LPI molecules and never waits for another warp (no block barrier).
-// Per molecule, two phases:
+// k_pairs<Model, LPI, MODE, HALF>: LPI lanes cooperate on one molecule i; a
+// warp holds 32/LPI molecules and never waits for another warp (no block
+// barrier).  Per molecule, two phases:
 //   1. test: the lanes read the neighbour row (coalesced) and the 32-bit
 //      fixed-point COM of each listed j (one 16-byte load), keep the pairs
-//      with |d|^2 < rc^2 (the FP32 distance of exact integer COM differences;
-//      within 1e-3 A^2 of rc^2 the reference's FP64 test decides) and append
-//      them to the molecule's row in shared memory with a ballot and a prefix
-//      count.  Up to six row entries per lane are in flight at a time.
+//      with |d|^2 < rc^2 (an FP32 distance from the integer COM differences
+//      without their low 9 bits; within a band of rc^2 that covers that
+//      truncation the reference's FP64 test decides) and append them to the
+//      molecule's row in shared memory with a ballot and a prefix count.  Up
+//      to six row entries per lane are in flight at a time.
 //   2. pairs: the lanes share out the compacted row (every lane of a group has
-//      an in-range pair until the row's tail), load j's 32-byte record (pkq:
-//      fixed-point COM and float quaternion, one 256-bit load) one pair ahead,
-//      rebuild its float site offsets from the quaternion and run the FP32
-//      site loop of pair_math, keeping per-lane sums of the i-site forces, the
-//      COM switch force, the energy and the virial.  The record is a quarter
-//      of the L1 lines of the site offsets it replaces; the kernel is bound by
-//      L1 line gathers, not by the 40-odd flops of the rebuild.
+//      an in-range pair until the row's tail), load j's pose record one pair
+//      ahead and run the FP32 site loop of pair_math, keeping per-lane sums of
+//      the i-site forces, the COM switch force, the energy and the virial.
+// HALF (the MD step's default): the rows hold only the pairs i evaluates
+// (half_keep), the record is the 32-byte pkq (fixed-point COM and float
+// quaternion, one 256-bit load) whose quaternion gives j's site offsets again
+// (two rotation columns for the planar TIP4P/SPC-E layout), and each pair's
+// force and torque on j go to jacc by two vector float atomics.  The full
+// list (MODE 0, and the MD step when chosen) evaluates every pair from both
+// molecules with the 64-byte pk32 record (offsets included, two loads).
 // The lanes of a molecule are then combined: in FP64 for the force-only call
-// (MODE 0: F, lab torque, energy, full virial), with error-free float-pair
-// addition for the MD step (MODE 1: F, lab torque, energy and virial trace as
-// float pairs, read by k_integrate_mixed).
+// (MODE 0: F, lab torque, energy, full virial), by a reduce-scatter of
+// error-free float pairs for the MD step (MODE 1: F, lab torque, energy and
+// virial trace as float pairs in fres, read by the integrator).
 //
-// k_integrate_mixed<NQ>: one molecule per lane, 32 per block: rigid_correct
-// with the small Gear terms in float (correct_mixed), the next predict and
-// placement, and the per-step reductions (step_reduce / finish_replica).
+// k_integrate_mixed<NQ, MPW> (one lane per molecule) and k_integrate_quad<NQ>
+// (four lanes per molecule, one per component): rigid_correct with the small
+// Gear terms in float, the next predict and placement, and the per-step
+// partial sums (step_partials; the replica finish runs in the next pair
+// kernel's first blocks).
 #include <cuda_runtime.h>
 
 #include <cstring>
