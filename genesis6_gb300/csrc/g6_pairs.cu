@@ -269,17 +269,29 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   const float band = a.band;   // above the test's error (coarse_delta, FP32 rounding); set per system
   const float sx5 = sx * 512.0f, sy5 = sy * 512.0f, sz5 = sz * 512.0f;
   int cnt = 0;
+  // the row entries of the next batch are loaded while this batch's COM words
+  // are in flight (one round trip of row loads in all, not one per batch)
+  int jn[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int k = u * LPI + sub;
+    jn[u] = k < nn ? __ldg(row + k) : -1;
+  }
   for (int base = 0; base < nmax; base += LPI * U) {
     int jj[U];
     float4 qj[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int k = base + u * LPI + sub;
-      jj[u] = k < nn ? __ldg(row + k) : -1;
+      jj[u] = jn[u];
       if (HALF && jj[u] >= 0 && !half_keep(i, jj[u])) jj[u] = -1;
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) qj[u] = jj[u] >= 0 ? load_com<M, HALF>(pk32, pkq, jj[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = base + LPI * U + u * LPI + sub;
+      jn[u] = k < nn ? __ldg(row + k) : -1;
+    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bool in = false;
