@@ -270,19 +270,21 @@ __global__ void __launch_bounds__(PairShape<LPI>::THREADS, (PairMinBlocks<M, MOD
   const float sx5 = sx * 512.0f, sy5 = sy * 512.0f, sz5 = sz * 512.0f;
   int cnt = 0;
   // the row entries of the next batch are loaded while this batch's COM words
-  // are in flight (one round trip of row loads in all, not one per batch)
+  // are in flight (one round trip of row loads in all, not one per batch);
+  // the first batch's are loaded within the row's capacity before its length
+  // arrives and masked by it afterwards
   int jn[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int k = u * LPI + sub;
-    jn[u] = k < nn ? __ldg(row + k) : -1;
+    jn[u] = (valid && k < a.cap) ? __ldg(row + k) : -1;
   }
   for (int base = 0; base < nmax; base += LPI * U) {
     int jj[U];
     float4 qj[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      jj[u] = jn[u];
+      jj[u] = base + u * LPI + sub < nn ? jn[u] : -1;
       if (HALF && jj[u] >= 0 && !half_keep(i, jj[u])) jj[u] = -1;
     }
 #pragma unroll
