@@ -254,7 +254,7 @@ struct g6_ctx {
   std::vector<int> off;
   std::vector<double> L;
   int lpi = 0;                    // lanes per molecule in the force kernel (0 = default)
-  int step_lpi = 0;               // lanes per molecule in the fused MD step kernel (0 = default)
+  int step_lpi = 0;               // lanes per molecule of the MD step's force kernel (0 = default)
   int step_mpw = 0;               // mixed MD step: molecules per warp of the integrator kernel (0 = default)
   int step_half = -1;             // mixed MD step: 1 half list, 0 full list, -1 default
   bool half_fixed = false;        // step_half set by g6_set_shape (the tuner keeps it)
@@ -785,7 +785,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_fix_build, 3 * (size_t)n)); CK(dalloc(ctx, &ctx->d_stf, (size_t)STF_COLS * n));
-  ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // blocks of the fused step kernel at 32 lanes/molecule
+  ctx->nblk = (int)(((long long)n * 32 + 127) / 128);   // partial-sum slots: blocks of the FP64 fused step kernel at 32 lanes per molecule (the most blocks of any step kernel)
   CK(dalloc(ctx, &ctx->d_part, (size_t)ctx->nblk * MAXREP_PER_BLOCK * NRED));
   {
     const CtlLayout cl = ctl_layout(nrep);

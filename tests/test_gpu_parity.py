@@ -148,6 +148,22 @@ def test_md_step_forces_then_md_run():
     assert np.array_equal(runs[0][1], runs[1][1])
 
 
+def test_half_list_shape_is_mixed_only():
+    """g6_set_shape accepts the half list only for a mixed-precision context
+    (the FP64 step always uses the full list) and reports the list form back."""
+    import ctypes
+    s, b = _system("TIP4P", "custom", 216, 4, prec="fp64", rc=8.0)
+    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=1)
+    assert s.L.g6_set_shape(s.ctx, ctypes.byref(sh)) == _capi.G6_ERR_ARG
+    m, _ = _system("TIP4P", "custom", 216, 4, prec="mixed", rc=8.0)
+    assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_OK
+    got = _capi.Shape()
+    m._check(m.L.g6_get_shape(m.ctx, ctypes.byref(got)))
+    assert got.step_half == 1
+    sh.step_half = 2
+    assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_ERR_ARG
+
+
 def test_step_forces_refuses_fp64():
     s, b = _system("TIP4P", "custom", 216, 3, prec="fp64", rc=8.0)
     with pytest.raises(g6.G6Error) as e:
