@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -328,6 +329,7 @@ struct g6_ctx {
   // pinned host block for the small per-run transfers (thermostats, control
   // words, per-replica factors, read-backs), so that they are asynchronous
   char* h_pinned = nullptr; size_t pinned_bytes = 0;
+  char* d_pinned = nullptr;   // the device's address of h_pinned
   cudaEvent_t pin_ev = nullptr;   // the last uploads from the block have been read
   // graph of a block of MD steps
   cudaGraphExec_t graph = nullptr;
@@ -393,7 +395,7 @@ static void free_all(g6_ctx* c) {
   if (c->d_opsamp) { cudaFree(c->d_opsamp); c->d_opsamp = nullptr; c->opsamp_cap = 0; }
   if (c->d_rec) { cudaFree(c->d_rec); c->d_rec = nullptr; c->rec_cap = 0; c->nrec = 0; }
   c->have_mlp = false;
-  if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->pinned_bytes = 0; }
+  if (c->h_pinned) { cudaFreeHost(c->h_pinned); c->h_pinned = nullptr; c->d_pinned = nullptr; c->pinned_bytes = 0; }
   if (c->pin_ev) { cudaEventDestroy(c->pin_ev); c->pin_ev = nullptr; }
   c->gref = HostGrid(); c->glist = HostGrid();
   c->list_valid = false;
@@ -809,6 +811,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   ctx->pinned_bytes = pinned_runs_bytes(nrep);
   CK(cudaMallocHost((void**)&ctx->h_pinned, ctx->pinned_bytes));
   std::memset(ctx->h_pinned, 0, ctx->pinned_bytes);   // the up block's counters stay zero
+  CK(cudaHostGetDevicePointer((void**)&ctx->d_pinned, ctx->h_pinned, 0));
   CK(cudaEventCreateWithFlags(&ctx->pin_ev, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->pin_ev, ctx->stream));
   ctx->have_system = true;
@@ -1447,9 +1450,11 @@ struct PinnedRuns {
   int* ovf;
   double* log1;   // one step's log (g6_md_step_host)
 };
-static PinnedRuns pinned_runs(g6_ctx* ctx) {
+// The pinned block's parts at host addresses, or at the device's addresses
+// when base is d_pinned.
+static PinnedRuns pinned_runs(g6_ctx* ctx, char* base = nullptr) {
   const int R = ctx->nrep;
-  char* b = ctx->h_pinned;
+  char* b = base ? base : ctx->h_pinned;
   const CtlLayout cl = ctl_layout(R);
   PinnedRuns p;
   char* up = b;
@@ -2009,6 +2014,13 @@ static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_ds
     std::memset(&h, 0, sizeof h);
     h.fix_build = ctx->d_fix_build;
     h.gmax = ctx->d_gmax;
+    HostOutArgs o;
+    std::memset(&o, 0, sizeof o);
+    o.rec = dev_rec ? dev_rec : ctx->d_save;
+    // with direct record access the control words move through the pinned
+    // block's device address as well: no copy-engine transfer in the step
+    const bool direct = upload && dev_rec && ctx->d_pinned;
+    const PinnedRuns pd = pinned_runs(ctx, ctx->d_pinned);
     if (upload && dev_rec) {
       h.rec = dev_rec;
       h.keep = ctx->d_stage;
@@ -2016,14 +2028,24 @@ static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_ds
       if (upload) CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
       h.rec = ctx->d_stage;
     }
-    int rc = md_upload(ctx);
-    if (rc) return rc;
-    StepArgs sa = step_args(ctx, dt, want_log ? ctx->d_log : nullptr);
+    int rc = G6_OK;
+    if (direct) {
+      const CtlLayout cl = ctl_layout(ctx->nrep);
+      h.ctl_up = (const uint4*)pd.up;
+      h.ctl = (uint4*)ctx->d_ctl;
+      h.ctl_n16 = (int)(cl.up_bytes / 16);
+      h.gmax16 = (int)(cl.gmax / 16);
+      o.th_dn = pd.th_dn; o.red_dn = pd.red; o.ctrl_dn = pd.ctrl_dn; o.ovf_dn = pd.ovf; o.ovf = ctx->d_overflow;
+    } else if ((rc = md_upload(ctx))) {
+      return rc;
+    }
+    // the direct form writes the log row into the pinned log block (log_dst)
+    StepArgs sa = step_args(ctx, dt, want_log ? (direct ? pd.log1 : ctx->d_log) : nullptr);
     CK(launch_host_in_mixed(place_args(ctx), h, ctx->d_stf, ctx->d_th, dt, ctx->stream));
     if ((rc = enqueue_step(ctx, sa))) return rc;
-    CK(launch_host_out_mixed(sa, dev_rec ? dev_rec : ctx->d_save, ctx->stream));
+    CK(launch_host_out_mixed(sa, o, ctx->stream));
     if (!dev_rec) CK(cudaMemcpyAsync(rec, ctx->d_save, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    return md_readback(ctx, 1, want_log ? log_dst : nullptr);
+    return direct ? G6_OK : md_readback(ctx, 1, want_log ? log_dst : nullptr);
   }
   if (upload) {
     CK(cudaMemcpyAsync(ctx->d_stage, rec, bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -2039,6 +2061,18 @@ static int enqueue_step_host(g6_ctx* ctx, double dt, double* rec, double* log_ds
   CK(launch_rec_transpose(ctx->d_stage, ctx->d_st, n, 0, ctx->stream));
   CK(cudaMemcpyAsync(rec, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   return md_readback(ctx, 1, want_log ? log_dst : nullptr);
+}
+
+// The end of a host-buffer step, which takes tens of microseconds: the
+// stream's status polled for up to 2 ms (a blocking synchronisation returns
+// several microseconds after the work ends), then the blocking wait.
+static cudaError_t wait_spin(cudaStream_t s) {
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    const cudaError_t e = cudaStreamQuery(s);
+    if (e != cudaErrorNotReady) return e;
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(2)) return cudaStreamSynchronize(s);
+  }
 }
 
 int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log) {
@@ -2081,10 +2115,11 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
       ctx->ghost_rec = rec; ctx->ghost_dt = dt; ctx->ghost_log = want_log; ctx->ghost_lpi = ctx->step_lpi;
     }
     CK(cudaGraphLaunch(ctx->graph_host, ctx->stream));
+    CK(wait_spin(ctx->stream));
   } else {
     if ((rc = enqueue_step_host(ctx, dt, rec, log, log != nullptr))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
   }
-  CK(cudaStreamSynchronize(ctx->stream));
   if (pinned && log) std::memcpy(log, pr.log1, (size_t)ctx->nrep * G6_LOG_WIDTH * sizeof(double));
   rc = md_check(ctx, 1, thermo);
   // a row overflow: the step again from the uploaded state with a larger capacity

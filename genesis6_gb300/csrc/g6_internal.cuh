@@ -590,10 +590,29 @@ struct HostInArgs {
   double* keep;               // optional: device copy of rec kept for a repeat of the step (row overflow)
   const uint32_t* fix_build;  // fixed-point COM at the last list build
   unsigned int* gmax;         // gmax[1]: the largest squared displacement since that build (float bits)
+  // optional: the run's control block read by block 0 from page-locked memory
+  // into the device block (instead of a copy before the kernel); the 16-byte
+  // word gmax16 holds gmax[0..3], of which gmax[1] is left to the other blocks'
+  // atomics
+  const uint4* ctl_up;
+  uint4* ctl;
+  int ctl_n16, gmax16;
+};
+// Optional read-back of the step's control words straight into page-locked
+// memory by the replica-finish blocks of the records-out kernel (instead of a
+// copy after it): per replica its thermostat and sums; block 0 also the
+// control words and the overflow flag.  th_dn == nullptr: none.
+struct HostOutArgs {
+  double* rec;        // records out (page-locked or a device copy)
+  ThermoDev* th_dn;
+  double* red_dn;
+  int* ctrl_dn;
+  int* ovf_dn;
+  const int* ovf;     // the device overflow flag
 };
 cudaError_t launch_host_in_mixed(const PlaceArgs& a, const HostInArgs& h, float* stf, ThermoDev* th, double dt,
                                  cudaStream_t s);
-cudaError_t launch_host_out_mixed(const StepArgs& sa, double* out, cudaStream_t s);
+cudaError_t launch_host_out_mixed(const StepArgs& sa, const HostOutArgs& o, cudaStream_t s);
 cudaError_t launch_step_fp64(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);

@@ -123,6 +123,34 @@ __device__ __forceinline__ void rec_tile_in(const double* src, int m, double* ti
   }
 }
 
+// Block 0 of the records-in kernel, after its tile: the control block from
+// page-locked memory (when h.ctl_up is set) and the Nose predict of the step.
+// The thermostats are read by no other block of this kernel.
+__device__ __forceinline__ void host_in_control(const PlaceArgs& a, const HostInArgs& h, ThermoDev* th, double dt) {
+  if (h.ctl_up) {
+    for (int w = threadIdx.x; w < h.ctl_n16; w += blockDim.x) {
+      const uint4 v = h.ctl_up[w];
+      if (w != h.gmax16) {
+        h.ctl[w] = v;
+      } else {
+        unsigned int* g = reinterpret_cast<unsigned int*>(h.ctl + w);
+        g[0] = v.x; g[2] = v.z; g[3] = v.w;
+      }
+    }
+    __syncthreads();
+  }
+  for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
+    ThermoDev& T = th[r];
+    if (T.kind == G6_NOSE) {
+      T.z[0] = T.z[0] + T.z[1] + T.z[2] + T.z[3] + T.z[4];
+      T.z[1] = T.z[1] + 2.0 * T.z[2] + 3.0 * T.z[3] + 4.0 * T.z[4];
+      T.z[2] = T.z[2] + 3.0 * T.z[3] + 6.0 * T.z[4];
+      T.z[3] = T.z[3] + 4.0 * T.z[4];
+      T.fext = (float)(T.z[0] * dt);
+    }
+  }
+}
+
 // One mixed-precision step with the state in the caller's record buffer
 // (g6_md_step_host): the records (n,53) become the FP64 state (com, d1, w1,
 // q) and the float small terms, followed by the step's first predict and
@@ -132,26 +160,19 @@ __device__ __forceinline__ void rec_tile_in(const double* src, int m, double* ti
 // h.keep then receives a device copy for a repeat of the step.  With h.gmax,
 // each molecule's displacement since the last list build (the step head's
 // keep-the-list test, on the new fixed-point COM) is raised into h.gmax[1],
-// so the head only compares one word.
+// so the head only compares one word.  With h.ctl_up, block 0 also reads the
+// run's control block from page-locked memory after its tile (the upload that
+// is otherwise a copy before this kernel).
 __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, HostInArgs h, float* stf, ThermoDev* th,
                                                                double dt) {
   __shared__ __align__(16) double tile[REC_TILE * REC];
-  if (blockIdx.x == 0) {
-    for (int r = threadIdx.x; r < a.rep.nrep; r += blockDim.x) {
-      ThermoDev& T = th[r];
-      if (T.kind == G6_NOSE) {
-        T.z[0] = T.z[0] + T.z[1] + T.z[2] + T.z[3] + T.z[4];
-        T.z[1] = T.z[1] + 2.0 * T.z[2] + 3.0 * T.z[3] + 4.0 * T.z[4];
-        T.z[2] = T.z[2] + 3.0 * T.z[3] + 6.0 * T.z[4];
-        T.z[3] = T.z[3] + 4.0 * T.z[4];
-        T.fext = (float)(T.z[0] * dt);
-      }
-    }
-  }
   const int n = a.n;
   const int i0 = blockIdx.x * REC_TILE;
   const int m = min(REC_TILE, n - i0);
-  if (m <= 0) return;
+  if (m <= 0) {
+    if (blockIdx.x == 0) host_in_control(a, h, th, dt);
+    return;
+  }
   rec_tile_in(h.rec + (size_t)i0 * REC, m, tile, h.keep ? h.keep + (size_t)i0 * REC : nullptr);
   __syncthreads();
   double* st = a.st;
@@ -188,19 +209,41 @@ __global__ void __launch_bounds__(REC_THREADS) k_host_in_mixed(PlaceArgs a, Host
       if (threadIdx.x == 0) atomicMax(&h.gmax[1], __float_as_uint(dd));
     }
   }
+  if (blockIdx.x == 0) {
+    __syncthreads();
+    host_in_control(a, h, th, dt);
+  }
 }
 
 // The end of that step: the replica finish of the step (the first nrep
 // blocks) beside the state going back to the FP64 record, both in the device
-// state and as records (n,53) in `out` for the copy to the caller -- the work
-// of k_finish_step, k_stf_move and k_rec_transpose in one launch.
-__global__ void __launch_bounds__(REC_THREADS) k_host_out_mixed(StepArgs sa, double* out) {
+// state and as records (n,53) in o.rec (the caller's page-locked buffer or a
+// device copy) -- the work of k_finish_step, k_stf_move and k_rec_transpose in
+// one launch.  With o.th_dn the finish blocks also write the words the host
+// reads after the step (thermostats, sums, control words, overflow flag) to
+// page-locked memory.
+__global__ void __launch_bounds__(REC_THREADS) k_host_out_mixed(StepArgs sa, HostOutArgs o) {
   __shared__ __align__(16) double tile[REC_TILE * REC];
   const int nfin = sa.p.rep.nrep;
   if ((int)blockIdx.x < nfin) {
-    finish_pending(sa, blockIdx.x, 32);
+    const int rr = blockIdx.x;
+    finish_pending(sa, rr, 32);
+    if (o.th_dn) {
+      __syncthreads();   // the replica's thermostat and sums as finish_pending left them
+      constexpr int TW = (int)(sizeof(ThermoDev) / sizeof(double));
+      static_assert(sizeof(ThermoDev) % sizeof(double) == 0, "ThermoDev is copied as doubles");
+      const double* ts = reinterpret_cast<const double*>(sa.th + rr);
+      double* td = reinterpret_cast<double*>(o.th_dn + rr);
+      for (int w = threadIdx.x; w < TW; w += blockDim.x) td[w] = ts[w];
+      for (int k = threadIdx.x; k < NRED; k += blockDim.x) o.red_dn[(size_t)rr * NRED + k] = sa.red[(size_t)rr * NRED + k];
+      if (rr == 0) {
+        if (threadIdx.x < 8) o.ctrl_dn[threadIdx.x] = sa.ctrl[threadIdx.x];
+        if (threadIdx.x == 8) *o.ovf_dn = *o.ovf;
+      }
+    }
     return;
   }
+  double* out = o.rec;
   const int n = sa.p.n;
   const int i0 = (blockIdx.x - nfin) * REC_TILE;
   const int m = min(REC_TILE, n - i0);
@@ -279,9 +322,9 @@ cudaError_t launch_host_in_mixed(const PlaceArgs& a, const HostInArgs& h, float*
   return cudaGetLastError();
 }
 
-cudaError_t launch_host_out_mixed(const StepArgs& sa, double* out, cudaStream_t s) {
+cudaError_t launch_host_out_mixed(const StepArgs& sa, const HostOutArgs& o, cudaStream_t s) {
   const int blocks = sa.p.rep.nrep + (sa.p.n + REC_TILE - 1) / REC_TILE;
-  k_host_out_mixed<<<blocks, REC_THREADS, 0, s>>>(sa, out);
+  k_host_out_mixed<<<blocks, REC_THREADS, 0, s>>>(sa, o);
   return cudaGetLastError();
 }
 

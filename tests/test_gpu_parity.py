@@ -358,6 +358,63 @@ def test_host_buffer_step_equals_device_step(prec, pinned, half):
             assert list(th_a[0].zeta) == list(th_b[0].zeta)
 
 
+@pytest.mark.parametrize("half", [0, 1])
+def test_consecutive_host_steps_follow_a_device_run(half):
+    """Twenty g6_md_step_host calls in a row on a page-locked buffer (two
+    replicas, a short skin so that the keep-the-list test of the records-in
+    kernel triggers rebuilds) end where one 20-step device run ends: state,
+    per-replica log rows and Nose thermostats (the control words travel through
+    the page-locked block, not through copies)."""
+    import ctypes
+    import torch
+    sizes = [216, 250]
+    boxes, recs = [], []
+    for k, n in enumerate(sizes):
+        b = config.water_box("TIP4P", n, 40 + k, temp=300.0, dt=0.002, jitter=0.2)
+        boxes.append(b["L"]); recs.append(b["rec"])
+    s = g6.RigidWater("TIP4P", sizes, np.array(boxes), path="custom", precision="mixed", rc=8.0)
+    sh = _capi.Shape()
+    s._check(s.L.g6_get_shape(s.ctx, ctypes.byref(sh)))
+    sh.lpi = sh.lpi or 8
+    sh.step_lpi = sh.step_lpi or 8
+    sh.step_mpw = sh.step_mpw or 4
+    sh.step_half = half
+    sh.skin = 0.3
+    s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+    rec0 = np.concatenate(recs)
+    nose = lambda: s.thermostats(2, "nose", temp=[300.0, 330.0], q=300.0 * 0.25 / 0.002)
+    s.upload_state(rec0)
+    s.md_run(0.002, 30, nose())
+    start = s.download_state()
+    th_a, th_b = nose(), nose()
+    s.upload_state(start)
+    log_a = s.md_run(0.002, 20, th_a)
+    want = s.download_state()
+    host = torch.empty(start.shape, dtype=torch.float64, pin_memory=True).numpy()
+    host[:] = start
+    s.upload_state(start)
+    logs = []
+    for _ in range(20):
+        lg = np.zeros((2, 10))
+        s.md_step_host(0.002, host, th_b, lg)
+        logs.append(lg)
+    logs = np.array(logs)
+    assert logs[:, :, 8].sum() >= 2          # the list was rebuilt on the way
+    # the two routes may rebuild the rows at different steps, which changes the
+    # FP32 summation order of the forces (~1e-6 relative): positions move ~0.2 A
+    # under the forces in 20 steps, so they agree to ~1e-7 A
+    assert np.abs(host[:, :3] - want[:, :3]).max() < 2e-6
+    assert np.abs(host - want).max() <= 1e-5 * np.abs(want).max()
+    for r in range(2):
+        for col in (0, 1, 2, 3, 5, 7):
+            a, b_ = log_a[:, r, col], logs[:, r, col]
+            assert np.abs(a - b_).max() <= 1e-5 * np.abs(a).max() + 1e-12
+        # every pair within rc was in the rows at every step on both routes
+        assert np.array_equal(logs[:, r, 6], log_a[:, r, 6])
+        assert th_b[r].zeta[0] == pytest.approx(th_a[r].zeta[0], rel=1e-5, abs=1e-12)
+        assert th_b[r].zetasum == pytest.approx(th_a[r].zetasum, rel=1e-5)
+
+
 def test_replicas_equal_separate_systems(orc):
     sizes = [216, 300, 250]
     boxes, recs = [], []
