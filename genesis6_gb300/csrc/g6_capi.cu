@@ -271,6 +271,7 @@ struct g6_ctx {
   int* d_npin = nullptr;
   float4* d_fres = nullptr;       // mixed MD step: per-molecule float-pair results of the pair kernel
   float4* d_jacc = nullptr;       // mixed MD step, half list: j-side force and torque (zero between steps)
+  double* d_jacc64 = nullptr;     // FP64 MD step, half list: the same in FP64, 6 SoA columns
   double* d_save = nullptr;       // state at the start of the current run (row-overflow recovery)
   int cap_request = 0;            // neighbour-list row capacity set by g6_set_shape or raised after an overflow
   bool overflow_recovered = false;   // the last run overflowed a row and was rolled back
@@ -553,7 +554,7 @@ static ListArgs list_args(g6_ctx* c, const int* ctrl, bool half = false) {
 }
 
 // MD steps of this context evaluate each pair once (mixed precision, half list).
-static bool step_uses_half(const g6_ctx* c) { return c->prec == G6_MIXED && c->step_half > 0; }
+static bool step_uses_half(const g6_ctx* c) { return c->step_half > 0; }
 
 static ForceArgs force_args(g6_ctx* c) {
   ForceArgs a;
@@ -564,7 +565,7 @@ static ForceArgs force_args(g6_ctx* c) {
   a.emol = c->d_emol; a.wmol = c->d_wmol; a.npair_in = c->d_npin; a.fres = c->d_fres;
   a.ccap = c->ccap; a.overflow = c->d_overflow;
   a.pkq = c->d_pkq; a.pkq_1 = c->d_pkq_1;
-  a.jacc = c->d_jacc; a.half = 0;
+  a.jacc = c->d_jacc; a.jacc64 = c->d_jacc64; a.half = 0;
   for (int s = 0; s < MAXSITE; ++s)
     for (int k = 0; k < 3; ++k) a.fbody[s][k] = (float)c->mh.body[s][k];
   a.planar = planar_sites(c->nq, a.fbody) ? 1 : 0;
@@ -783,6 +784,7 @@ int g6_system(g6_ctx* ctx, int model, int path, int precision, int nrep, const i
   CK(dalloc(ctx, &ctx->d_emol, n)); CK(dalloc(ctx, &ctx->d_wmol, 9 * (size_t)n)); CK(dalloc(ctx, &ctx->d_npin, n));
   CK(dalloc(ctx, &ctx->d_fres, 4 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_jacc, 2 * (size_t)n));
+  CK(dalloc(ctx, &ctx->d_jacc64, 6 * (size_t)n));
   CK(dalloc(ctx, &ctx->d_save, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_stage, (size_t)REC * n));
   CK(dalloc(ctx, &ctx->d_nnb, n)); CK(dalloc(ctx, &ctx->d_com_build, 3 * (size_t)n));
@@ -1401,6 +1403,10 @@ static int enqueue_step(g6_ctx* ctx, const StepArgs& sa, cudaEvent_t* ev = nullp
   if (ctx->prec == G6_MIXED) {
     // pair kernel, then the integrator kernel; the kernel events bracket the pair kernel
     CK(launch_step_mixed(fa, sa, ctx->model, ctx->step_lpi, ctx->step_mpw, ctx->stream, kev ? ev[2] : nullptr));
+  } else if (fa.half) {
+    // pair kernel (partner shares by FP64 atomics), then the integrator kernel
+    CK(launch_step_fp64_half(fa, sa, ctx->model, ctx->step_lpi, ctx->stream));
+    if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
   } else {
     CK(launch_step_fp64(fa, sa, ctx->model, ctx->step_lpi, ctx->stream));
     if (kev) CK(cudaEventRecordWithFlags(ev[2], ctx->stream, cudaEventRecordExternal));
@@ -1813,7 +1819,7 @@ static int tune_force_lpi(g6_ctx* ctx) {
 }
 
 // MD-step kernel shape at the current skin: every (lanes, molecules per warp)
-// pair on a short run, with the half and the full list in mixed precision;
+// pair on a short run (FP64: lanes only), with the half and the full list;
 // returns the best shape's time for `timed` steps.  A context whose list form
 // was set (g6_set_shape) keeps it.
 static int tune_step_shape(g6_ctx* ctx, cudaEvent_t e0, cudaEvent_t e1, float* best_ms) {
@@ -1822,7 +1828,7 @@ static int tune_step_shape(g6_ctx* ctx, cudaEvent_t e0, cudaEvent_t e1, float* b
   const int nm = ctx->prec == G6_MIXED ? 4 : 1;
   const bool fixed_half = ctx->half_fixed;
   const int h0 = fixed_half ? ctx->step_half : 0;
-  const int h1 = fixed_half ? ctx->step_half : (ctx->prec == G6_MIXED ? 1 : 0);
+  const int h1 = fixed_half ? ctx->step_half : 1;
   int bl = ctx->step_lpi, bm = ctx->step_mpw, bh = h0;
   float sb = 1e30f;
   for (int h = h0; h <= h1; ++h)
@@ -1946,8 +1952,6 @@ int g6_set_shape(g6_ctx* ctx, const g6_shape* shape) {
   if (shape->cap < 0) return fail(ctx, G6_ERR_ARG, "cap must be >= 0 (0: from the skin and density)");
   if (shape->step_half != 0 && shape->step_half != 1)
     return fail(ctx, G6_ERR_ARG, "step_half must be 0 (full list) or 1 (half list)");
-  if (shape->step_half == 1 && ctx->prec != G6_MIXED)
-    return fail(ctx, G6_ERR_ARG, "the half list is a mixed-precision MD step (FP64 steps use the full list)");
   ctx->lpi = shape->lpi; ctx->step_lpi = shape->step_lpi; ctx->step_mpw = shape->step_mpw;
   ctx->step_half = shape->step_half;
   ctx->half_fixed = true;

@@ -35,10 +35,14 @@ struct StepShape {
   static constexpr int THREADS = MPB * LPI;
 };
 
-template <class M, int LPI, bool FUSED>
+// HALF (with FUSED = false): the pair kernel of the FP64 step on half rows --
+// each pair within rc once, i-side sums as in the force-only form but with
+// the virial trace only, the partner's share (minus the pair force, its lab
+// torque) added with FP64 atomics to a.jacc64 for k_integrate_fp64.
+template <class M, int LPI, bool FUSED, bool HALF = false>
 __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_force(ForceArgs a, StepArgs sa) {
   using R = double;
-  constexpr int NW = FUSED ? 1 : 9;
+  constexpr int NW = (FUSED || HALF) ? 1 : 9;
   int step = 0;
   if (a.ctrl) step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
@@ -81,8 +85,19 @@ __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_fo
 #pragma unroll
           for (int q = 0; q < 3; ++q) rj[s][q] = (R)pj[3 + 3 * s + q];
         R dr[3] = {(R)dx[0], (R)dx[1], (R)dx[2]};
-        pair_math<M, R, NW>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1, (R)a.cc.c2,
-                        (R)a.pc.rl, (R)a.pc.ru, (R)a.pc.w3, acc);
+        if constexpr (HALF) {
+          PairJ<R> pj;
+          pair_math<M, R, NW, true>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1,
+                                    (R)a.cc.c2, (R)a.pc.rl, (R)a.pc.ru, (R)a.pc.w3, acc, &pj);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            atomicAdd(a.jacc64 + (size_t)q * n + j, pj.f[q]);
+            atomicAdd(a.jacc64 + (size_t)(3 + q) * n + j, pj.t[q]);
+          }
+        } else {
+          pair_math<M, R, NW>(dr, (R)dd, ri, rj, a.pc, (R)a.cc.rin2, (R)a.cc.rin, (R)a.cc.rout, (R)a.cc.c1,
+                              (R)a.cc.c2, (R)a.pc.rl, (R)a.pc.ru, (R)a.pc.w3, acc);
+        }
       }
     }
   }
@@ -108,7 +123,21 @@ __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_fo
   int np_tot = npin;
 #pragma unroll
   for (int m = LPI / 2; m >= 1; m >>= 1) np_tot += __shfl_xor_sync(0xffffffffu, np_tot, m);
-  if constexpr (!FUSED) {
+  if constexpr (HALF) {
+    // each pair once: the molecule's own sums in full (energy, virial trace, count)
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { v[k] = group_sum<LPI>((double)fo[k]); v[3 + k] = group_sum<LPI>((double)to[k]); }
+    v[6] = group_sum<LPI>((double)acc.e);
+    v[7] = group_sum<LPI>((double)acc.w[0]);
+    if (valid && sub == 0) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { a.F[k * n + i] = v[k]; a.tl[k * n + i] = v[3 + k]; }
+      a.emol[i] = v[6];
+      a.wmol[i] = v[7];
+      a.npair_in[i] = np_tot;
+    }
+  } else if constexpr (!FUSED) {
     // combine the LPI lanes in FP64
     double v[16];
 #pragma unroll
@@ -165,32 +194,67 @@ __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_fo
   }
 }
 
-template <class M, int LPI, bool FUSED>
+template <class M, int LPI, bool FUSED, bool HALF>
 static cudaError_t launch_force_t(const ForceArgs& a, const StepArgs& sa, cudaStream_t s) {
   // force only: 128 threads; fused step: MPB molecules (MPB x LPI threads) per block
   const int threads = FUSED ? StepShape<LPI>::THREADS : 128;
   const long long total = (long long)a.n * LPI;
   const int blocks = (int)((total + threads - 1) / threads);
   if (blocks == 0) return cudaSuccess;
-  k_force<M, LPI, FUSED><<<blocks, threads, 0, s>>>(a, sa);
+  k_force<M, LPI, FUSED, HALF><<<blocks, threads, 0, s>>>(a, sa);
   return cudaGetLastError();
 }
 
-template <class M, bool FUSED>
+template <class M, bool FUSED, bool HALF>
 static cudaError_t launch_force_l(const ForceArgs& a, const StepArgs& sa, int lpi, cudaStream_t s) {
   switch (lpi) {
-    case 4: return launch_force_t<M, 4, FUSED>(a, sa, s);
-    case 8: return launch_force_t<M, 8, FUSED>(a, sa, s);
-    case 16: return launch_force_t<M, 16, FUSED>(a, sa, s);
-    default: return launch_force_t<M, 32, FUSED>(a, sa, s);
+    case 4: return launch_force_t<M, 4, FUSED, HALF>(a, sa, s);
+    case 8: return launch_force_t<M, 8, FUSED, HALF>(a, sa, s);
+    case 16: return launch_force_t<M, 16, FUSED, HALF>(a, sa, s);
+    default: return launch_force_t<M, 32, FUSED, HALF>(a, sa, s);
   }
 }
 
-template <bool FUSED>
+template <bool FUSED, bool HALF = false>
 static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
-  if (model_nq(model) == 3) return launch_force_l<MT<3, false>, FUSED>(a, sa, lpi, s);
-  if (a.pc.taper) return launch_force_l<MT<4, true>, FUSED>(a, sa, lpi, s);
-  return launch_force_l<MT<4, false>, FUSED>(a, sa, lpi, s);
+  if (model_nq(model) == 3) return launch_force_l<MT<3, false>, FUSED, HALF>(a, sa, lpi, s);
+  if (a.pc.taper) return launch_force_l<MT<4, true>, FUSED, HALF>(a, sa, lpi, s);
+  return launch_force_l<MT<4, false>, FUSED, HALF>(a, sa, lpi, s);
+}
+
+// The FP64 MD step on half rows, second kernel: each molecule's force and lab
+// torque (its own pairs' sums minus / plus the shares its partners added to
+// jacc64, which are cleared for the next step), then the Gear corrector, the
+// next predict and placement and the step's reductions as in the fused step;
+// one molecule per lane, 32 per block (an FP64 instruction costs a warp the
+// same whatever the number of active lanes).
+__global__ void __launch_bounds__(32) k_integrate_fp64(ForceArgs a, StepArgs sa) {
+  const int n = a.n;
+  const int step = a.ctrl[1];
+  const bool odd = (step & 1) != 0;
+  const bool predict_next = step + 1 < sa.ctrl[2];
+  const int im = blockIdx.x * 32 + threadIdx.x;
+  double vv[NRED];
+#pragma unroll
+  for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
+  double dmax2 = 0.0;
+  int bad = 0, rr = -1;
+  if (im < n) {
+    rr = a.rep.mol_rep[im];
+    double F[3], tl[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double* jf = a.jacc64 + (size_t)k * n + im;
+      double* jt = a.jacc64 + (size_t)(3 + k) * n + im;
+      F[k] = a.F[(size_t)k * n + im] - *jf;
+      tl[k] = a.tl[(size_t)k * n + im] + *jt;
+      *jf = 0.0;
+      *jt = 0.0;
+    }
+    correct_one(sa, im, F, tl, a.emol[im], a.wmol[im], (double)a.npair_in[im], step, predict_next,
+                pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+  }
+  step_reduce<double>(sa, vv, rr, (float)dmax2, bad, 32, step, 0);
 }
 
 // Force only (outputs F, lab torque, per-molecule energy and virial); the
@@ -206,6 +270,13 @@ cudaError_t launch_force(const ForceArgs& a, int model, bool mixed, int lpi, cud
 // next step's predict + placement in the kernel's epilogue.
 cudaError_t launch_step_fp64(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
   return launch_force_any<true>(a, sa, model, lpi, s);
+}
+
+cudaError_t launch_step_fp64_half(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
+  cudaError_t e = launch_force_any<false, true>(a, sa, model, lpi, s);
+  if (e != cudaSuccess || a.n == 0) return e;
+  k_integrate_fp64<<<(a.n + 31) / 32, 32, 0, s>>>(a, sa);
+  return cudaGetLastError();
 }
 
 int pk64_width(int model) { return model_nq(model) == 3 ? MT<3, false>::W64 : MT<4, false>::W64; }

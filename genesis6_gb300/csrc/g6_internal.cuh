@@ -223,7 +223,8 @@ struct ForceArgs {
   float fbody[MAXSITE][3];   // body-frame site coordinates (LJ site, charged sites) as float
   float4* jacc;   // mixed MD step, half list: per molecule 2 float4 (minus its force, its lab torque) from the
                   // pairs others hold
-  int half;       // mixed MD step: 1 = half list (each pair once, j side by atomics), 0 = full list
+  double* jacc64; // FP64 MD step, half list: 6 SoA columns per molecule (minus-force share, lab torque share)
+  int half;       // MD step: 1 = half list (each pair once, j side by atomics), 0 = full list
   int planar;     // 3-charge model with the planar site layout of MT::PLANAR
   float band;     // mixed row test: |d^2 - rc^2| below this (A^2) is decided by the FP64 test
   float fs1[3];   // one replica: its fixed-point scales L/2^32 (rep.fscale[0..2]), read without a load
@@ -614,6 +615,9 @@ cudaError_t launch_host_in_mixed(const PlaceArgs& a, const HostInArgs& h, float*
                                  cudaStream_t s);
 cudaError_t launch_host_out_mixed(const StepArgs& sa, const HostOutArgs& o, cudaStream_t s);
 cudaError_t launch_step_fp64(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);
+// The FP64 MD step on half rows: the pair kernel (own sums per molecule, the
+// partner's share by FP64 atomics into f.jacc64), then the integrator kernel.
+cudaError_t launch_step_fp64_half(const ForceArgs& f, const StepArgs& a, int model, int lpi, cudaStream_t s);
 cudaError_t launch_feat_stats(const float* rec, long long nrec, float* mean, float* istd, cudaStream_t s);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);
 cudaError_t launch_rec_transpose(double* aos, double* soa, int n, int to_soa, cudaStream_t s);

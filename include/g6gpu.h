@@ -262,13 +262,14 @@ typedef struct g6_shape {
   int cap;         /* neighbour-list row capacity (entries); g6_set_shape: 0 derives it
                       from the skin and the density (twice the expected row + 64)    */
   double step_ms;  /* g6_tune_shape: the chosen shape's MD step time in the search   */
-  int step_half;   /* mixed MD step: 1 = half list (each pair within rc evaluated once;
-                      the other molecule's force and torque added with float atomics,
-                      so the order of those sums varies and runs are not
-                      bit-reproducible), 0 = full list (every pair from both sides,
-                      fixed summation order, bit-reproducible).  FP64 steps always use
-                      the full list.  Default (no g6_set_shape): half in mixed
-                      precision; g6_tune_shape times both unless g6_set_shape chose */
+  int step_half;   /* MD step: 1 = half list (each pair within rc evaluated once;
+                      the other molecule's force and torque added with atomics --
+                      float in mixed precision, FP64 in FP64 -- so the order of those
+                      sums varies and runs are not bit-reproducible), 0 = full list
+                      (every pair from both sides, fixed summation order,
+                      bit-reproducible).  Default (no g6_set_shape): half in mixed
+                      precision, full in FP64; g6_tune_shape times both unless
+                      g6_set_shape chose */
 } g6_shape;
 #define G6_TUNE_SKIN 1
 /* Autotuner: times the candidates on the uploaded state (restored after every

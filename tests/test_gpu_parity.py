@@ -148,20 +148,19 @@ def test_md_step_forces_then_md_run():
     assert np.array_equal(runs[0][1], runs[1][1])
 
 
-def test_half_list_shape_is_mixed_only():
-    """g6_set_shape accepts the half list only for a mixed-precision context
-    (the FP64 step always uses the full list) and reports the list form back."""
+def test_half_list_shape_is_set_and_reported():
+    """g6_set_shape accepts the half or the full list in both precisions,
+    reports the list form back and refuses any other value."""
     import ctypes
-    s, b = _system("TIP4P", "custom", 216, 4, prec="fp64", rc=8.0)
-    sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=1)
-    assert s.L.g6_set_shape(s.ctx, ctypes.byref(sh)) == _capi.G6_ERR_ARG
-    m, _ = _system("TIP4P", "custom", 216, 4, prec="mixed", rc=8.0)
-    assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_OK
-    got = _capi.Shape()
-    m._check(m.L.g6_get_shape(m.ctx, ctypes.byref(got)))
-    assert got.step_half == 1
-    sh.step_half = 2
-    assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_ERR_ARG
+    for prec in ("fp64", "mixed"):
+        m, _ = _system("TIP4P", "custom", 216, 4, prec=prec, rc=8.0)
+        sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=1)
+        assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_OK
+        got = _capi.Shape()
+        m._check(m.L.g6_get_shape(m.ctx, ctypes.byref(got)))
+        assert got.step_half == 1
+        sh.step_half = 2
+        assert m.L.g6_set_shape(m.ctx, ctypes.byref(sh)) == _capi.G6_ERR_ARG
 
 
 def test_step_forces_refuses_fp64():
@@ -199,14 +198,22 @@ def test_force_sites_entry_matches_reference_call(orc, model, path):
     assert np.abs(hx - x).max() < 1e-12
 
 
-@pytest.mark.parametrize("model,path", [("TIP4P", "custom"), ("TIP4P", "std"), ("TIP5P", "custom"), ("ST2", "custom"), ("SPCE", "std"),
-                                        ("ST2", "std")])
-def test_md_fp64_follows_oracle(orc, model, path):
-    """Short Gear MD: the device trajectory tracks the oracle's step by step."""
+@pytest.mark.parametrize("model,path,half", [("TIP4P", "custom", 0), ("TIP4P", "std", 0), ("TIP5P", "custom", 0),
+                                             ("ST2", "custom", 0), ("SPCE", "std", 0), ("ST2", "std", 0),
+                                             ("TIP4P", "custom", 1), ("TIP4P", "std", 1), ("TIP5P", "custom", 1),
+                                             ("ST2", "custom", 1), ("SPCE", "std", 1)])
+def test_md_fp64_follows_oracle(orc, model, path, half):
+    """Short Gear MD: the device trajectory tracks the oracle's step by step,
+    with the full list (the default) and with the half list (each pair once,
+    the partner's share by FP64 atomics, then a separate integrator kernel)."""
+    import ctypes
     n = 256
     b = config.water_box(model, n, 5, temp=300.0, dt=0.002, jitter=0.2)
     L = b["L"]
     s = g6.RigidWater(model, n, L, path=path, rc=8.5, skin=1.0)
+    if half:
+        sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=1)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
     s.upload_state(b["rec"])
     log = s.md_run(0.002, 20)
     rec_g = s.download_state()
@@ -222,12 +229,17 @@ def test_md_fp64_follows_oracle(orc, model, path):
     assert np.array_equal(log[:, 0, 6], log_o[:, 6])   # pairs within rc, every step
 
 
-def test_md_nose_follows_oracle(orc):
+@pytest.mark.parametrize("half", [0, 1])
+def test_md_nose_follows_oracle(orc, half):
+    import ctypes
     n = 216
     b = config.water_box("TIP4P", n, 6, temp=350.0, dt=0.002, jitter=0.2)
     L = b["L"]
     q = 300.0 * 0.1 ** 2 / 0.002
     s = g6.RigidWater("TIP4P", n, L, path="custom", rc=8.5)
+    if half:
+        sh = _capi.Shape(lpi=16, step_lpi=16, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=1)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
     s.upload_state(b["rec"])
     th = s.thermostats(1, "nose", temp=300.0, q=q, dump=0.0)
     log = s.md_run(0.002, 25, th)
