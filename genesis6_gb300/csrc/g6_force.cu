@@ -186,8 +186,9 @@ __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_fo
       if (im < n) {
         rr = a.rep.mol_rep[im];
         const double F[3] = {smd[m][0], smd[m][1], smd[m][2]}, tl[3] = {smd[m][3], smd[m][4], smd[m][5]};
-        correct_one(sa, im, F, tl, 0.5 * smd[m][6], 0.5 * smd[m][7], 0.5 * smd[m][8], step, predict_next,
-                    pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+        correct_one(sa, im, sa.p.st, n, im, F, tl, 0.5 * smd[m][6], 0.5 * smd[m][7], 0.5 * smd[m][8], step,
+                    predict_next, pose_buf(sa, odd ? 1 : 0), vv, bad);
+        if (predict_next) place_next(sa, im, pose_buf(sa, odd ? 0 : 1), dmax2, bad);
       }
     }
     step_reduce<double>(sa, vv, rr, (float)dmax2, bad, MPB, step, ew);
@@ -251,8 +252,17 @@ __global__ void __launch_bounds__(32) k_integrate_fp64(ForceArgs a, StepArgs sa)
       *jf = 0.0;
       *jt = 0.0;
     }
-    correct_one(sa, im, F, tl, a.emol[im], a.wmol[im], (double)a.npair_in[im], step, predict_next,
-                pose_buf(sa, odd ? 1 : 0), pose_buf(sa, odd ? 0 : 1), vv, dmax2, bad);
+    // the molecule's record in registers: the corrector's read-modify-write
+    // chain then waits on no memory round trip (in the fused step it does, but
+    // other blocks' pair work hides it)
+    double rs[REC];
+#pragma unroll
+    for (int c = 0; c < REC; ++c) rs[c] = sa.p.st[(size_t)c * n + im];
+    correct_one(sa, im, rs, 1, 0, F, tl, a.emol[im], a.wmol[im], (double)a.npair_in[im], step, predict_next,
+                pose_buf(sa, odd ? 1 : 0), vv, bad);
+#pragma unroll
+    for (int c = 0; c < REC; ++c) sa.p.st[(size_t)c * n + im] = rs[c];
+    if (predict_next) place_next(sa, im, pose_buf(sa, odd ? 0 : 1), dmax2, bad);
   }
   step_reduce<double>(sa, vv, rr, (float)dmax2, bad, 32, step, 0);
 }

@@ -24,6 +24,9 @@
 namespace g6 {
 
 #define G6_ST(c) st[(size_t)(c) * n + i]
+// correct_one's state: column c of the molecule's record at sst[c * sn + si]
+// (the state columns, or a copy in registers with sn = 1, si = 0)
+#define G6_SS(c) sst[(size_t)(c) * sn + si]
 
 __device__ __forceinline__ void setmatrix(const double q[4], double t[9]) {
   const double qa = q[0], qb = q[1], qc = q[2], qd = q[3];
@@ -145,12 +148,10 @@ __device__ __forceinline__ PoseBuf pose_buf(const StepArgs& a, int which) {
 
 // rigid_correct + energy/virial/kinetic terms + the next predict and placement
 // for molecule i.  F: COM force; tl: lab-frame torque; cur/next: pose buffers.
-__device__ __forceinline__ void correct_one(const StepArgs& a, int i, const double F[3], const double tl[3],
-                                            double emol, double wtr, double npair_half, int step,
-                                            bool predict_next, const PoseBuf& cur, const PoseBuf& next,
-                                            double (&v)[NRED], double& dmax2, int& bad) {
+__device__ __forceinline__ void correct_one(const StepArgs& a, int i, double* sst, int sn, int si, const double F[3],
+                                            const double tl[3], double emol, double wtr, double npair_half, int step,
+                                            bool predict_next, const PoseBuf& cur, double (&v)[NRED], int& bad) {
   const int n = a.p.n;
-  double* st = a.p.st;
   const int r = a.p.rep.mol_rep[i];
   const ThermoDev th = a.th[r];
   const double dt = a.dt;
@@ -174,25 +175,25 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     double nf = F[c] * (dt * dt * 0.5 * massi);
-    nf = nf - G6_ST(3 + c) * ext_t;
-    const double delta = nf - G6_ST(6 + c);
-    G6_ST(c) = G6_ST(c) + G50 * delta;
-    G6_ST(3 + c) = G6_ST(3 + c) + G51 * delta;
-    G6_ST(6 + c) = nf;
-    G6_ST(9 + c) = G6_ST(9 + c) + G53 * delta;
-    G6_ST(12 + c) = G6_ST(12 + c) + G54 * delta;
-    G6_ST(15 + c) = G6_ST(15 + c) + G55 * delta;
+    nf = nf - G6_SS(3 + c) * ext_t;
+    const double delta = nf - G6_SS(6 + c);
+    G6_SS(c) = G6_SS(c) + G50 * delta;
+    G6_SS(3 + c) = G6_SS(3 + c) + G51 * delta;
+    G6_SS(6 + c) = nf;
+    G6_SS(9 + c) = G6_SS(9 + c) + G53 * delta;
+    G6_SS(12 + c) = G6_SS(12 + c) + G54 * delta;
+    G6_SS(15 + c) = G6_SS(15 + c) + G55 * delta;
   }
   // quaternion value
-  double q1[4] = {G6_ST(33), G6_ST(34), G6_ST(35), G6_ST(36)};
-  double w1[3] = {G6_ST(18), G6_ST(19), G6_ST(20)};
+  double q1[4] = {G6_SS(33), G6_SS(34), G6_SS(35), G6_SS(36)};
+  double w1[3] = {G6_SS(18), G6_SS(19), G6_SS(20)};
   double nw[4];
   qdot(w1, q1, nw);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const double dw = nw[c] * dt * 0.5 - G6_ST(37 + c);
+    const double dw = nw[c] * dt * 0.5 - G6_SS(37 + c);
     q1[c] = q1[c] + G40 * dw;
-    G6_ST(33 + c) = q1[c];
+    G6_SS(33 + c) = q1[c];
   }
   // angular velocity: Gear-4 with Euler's equations
   const double Ix = a.I[0], Iy = a.I[1], Iz = a.I[2];
@@ -203,12 +204,12 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     nf[c] = nf[c] - w1[c] * ext_r;
-    const double delta = nf[c] - G6_ST(21 + c);
-    G6_ST(18 + c) = G6_ST(18 + c) + G40 * delta;
-    G6_ST(21 + c) = nf[c];
-    G6_ST(24 + c) = G6_ST(24 + c) + G42 * delta;
-    G6_ST(27 + c) = G6_ST(27 + c) + G43 * delta;
-    G6_ST(30 + c) = G6_ST(30 + c) + G44 * delta;
+    const double delta = nf[c] - G6_SS(21 + c);
+    G6_SS(18 + c) = G6_SS(18 + c) + G40 * delta;
+    G6_SS(21 + c) = nf[c];
+    G6_SS(24 + c) = G6_SS(24 + c) + G42 * delta;
+    G6_SS(27 + c) = G6_SS(27 + c) + G43 * delta;
+    G6_SS(30 + c) = G6_SS(30 + c) + G44 * delta;
   }
   // stochastic collisions (new thermostat; velocity resampled from Maxwell-Boltzmann)
   if (th.kind == G6_ANDERSEN) {
@@ -224,10 +225,10 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
         z[2 * p] = normal_pair(g[0], g[1], z[2 * p + 1]);
       }
       const double sv = sqrt(kT * massi) * dt;
-      for (int c = 0; c < 3; ++c) G6_ST(3 + c) = z[c] * sv;
-      G6_ST(18) = z[3] * sqrt(kT / Ix);
-      G6_ST(19) = z[4] * sqrt(kT / Iy);
-      G6_ST(20) = z[5] * sqrt(kT / Iz);
+      for (int c = 0; c < 3; ++c) G6_SS(3 + c) = z[c] * sv;
+      G6_SS(18) = z[3] * sqrt(kT / Ix);
+      G6_SS(19) = z[4] * sqrt(kT / Iy);
+      G6_SS(20) = z[5] * sqrt(kT / Iz);
     }
   }
   // quaternion derivative stacks from the corrected angular-velocity stack
@@ -235,7 +236,7 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
 #pragma unroll
   for (int k = 0; k < 5; ++k)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) W[k][c] = G6_ST(18 + 3 * k + c);
+    for (int c = 0; c < 3; ++c) W[k][c] = G6_SS(18 + 3 * k + c);
 #pragma unroll
   for (int c = 0; c < 4; ++c) Q[0][c] = q1[c];
   qdot(W[0], Q[0], tq);
@@ -253,22 +254,28 @@ __device__ __forceinline__ void correct_one(const StepArgs& a, int i, const doub
 #pragma unroll
   for (int k = 1; k < 5; ++k)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) G6_ST(33 + 4 * k + c) = Q[k][c];
+    for (int c = 0; c < 4; ++c) G6_SS(33 + 4 * k + c) = Q[k][c];
   // reductions: Epot, virial trace, kinetic sums (Rigid_Ek), pairs
-  const double d1[3] = {G6_ST(3), G6_ST(4), G6_ST(5)};
+  const double d1[3] = {G6_SS(3), G6_SS(4), G6_SS(5)};
   v[0] = emol;
   v[1] = wtr;
   v[2] = d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2];
   v[3] = a.I[0] * (W[0][0] * W[0][0]) + a.I[1] * (W[0][1] * W[0][1]) + a.I[2] * (W[0][2] * W[0][2]);
   v[4] = npair_half;
-  if (predict_next) {
-    predict_one(st, n, i);
-    place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.pkq, next.fix);
-    const double dx = G6_ST(0) - a.com_build[i], dy = G6_ST(1) - a.com_build[n + i],
-                 dz = G6_ST(2) - a.com_build[2 * n + i];
-    dmax2 = dx * dx + dy * dy + dz * dz;
-    if (!isfinite(dmax2)) { bad = 1; dmax2 = 1e300; }
-  }
+  if (predict_next) predict_one(sst, sn, si);
+}
+
+// After correct_one with the next step predicted and the state in the
+// columns: placement into the next pose buffer and the displacement since the
+// last list build.
+__device__ __forceinline__ void place_next(const StepArgs& a, int i, const PoseBuf& next, double& dmax2, int& bad) {
+  const int n = a.p.n;
+  const double* st = a.p.st;
+  place_to(a.p, i, next.tmat, next.pk64, next.pk32, next.pkq, next.fix);
+  const double dx = G6_ST(0) - a.com_build[i], dy = G6_ST(1) - a.com_build[n + i],
+               dz = G6_ST(2) - a.com_build[2 * n + i];
+  dmax2 = dx * dx + dy * dy + dz * dz;
+  if (!isfinite(dmax2)) { bad = 1; dmax2 = 1e300; }
 }
 
 // ---------------------------------------------------------------------------
@@ -1116,5 +1123,6 @@ __device__ inline void finish_pending(const StepArgs& a, int rr, int mpb) {
 }
 
 #undef G6_ST
+#undef G6_SS
 
 }  // namespace g6
