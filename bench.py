@@ -307,8 +307,12 @@ def e2e_md(torch, s, rec, steps):
         s.md_step_host(DT, hv, th, lg)
     wall = time.perf_counter() - t0
     rec_b = n * 53 * 8
-    h2d = rec_b + 88 + 32                       # records, thermostat, control words
-    d2h = rec_b + 32 + 4 + 88 + 24 * 8 + 80     # records, control, overflow flag, thermostat, sums, log
+    # records in, and the run's control block (thermostat, factors, control words
+    # and counters: 256 bytes for one replica) that the records-in kernel reads
+    h2d = rec_b + 256
+    # records out, and the thermostat (112 bytes), the 5 step sums, the control
+    # words, the overflow flag and the log row the records-out kernel writes
+    d2h = rec_b + 112 + 5 * 8 + 32 + 4 + 80
     return 1e3 * wall / steps, h2d, d2h
 
 
@@ -725,6 +729,8 @@ def bench_c3(torch, flush, model="TIP4P", seed=20261205, steps=5000, snapshots=2
             out["force_kernel_ms"] = float(km.mean())
             out["force_tflops"] = FLOPS_PER_PAIR[model] * pairs / (float(km.mean()) * 1e-3) / 1e12
             out["shape"] = shape.as_dict()
+        else:
+            out["fp64_shape"] = shape.as_dict()
     out["mixed_over_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
     # NVE drift from the same start
     for prec, s in (("mixed", sm), ("fp64", s64)):
@@ -858,7 +864,7 @@ def run_gpu(args, rank, world, local):
     # plain FP64 mode, same state
     s64 = make_system("TIP4P", N_MAIN, "fp64", L, rec_eq)
     k64 = max(5, min(args.steps, 60))
-    step64, kms64, log64, _ = timed_md(torch, s64, k64, min(args.warmup, 5), flush)
+    step64, kms64, log64, shape64 = timed_md(torch, s64, k64, min(args.warmup, 5), flush)
     ms64 = float(step64.mean())
 
     # e2e through the host-buffer entry point
@@ -899,6 +905,7 @@ def run_gpu(args, rank, world, local):
         "dtype": "f32 site math / f64 accumulation", "data": "synthetic (seeded lattice, random quaternions, "
         "Maxwell-Boltzmann 300 K, then 2,000 FP64 Nose-Hoover steps: the stored state both arms start from)", "config": config_block(args, world),
         "fp64_ns_per_day": world * ns_per_day(ms64), "fp64_ms_per_step": ms64, "mixed_over_fp64": ms64 / ms,
+        "fp64_shape": shape64,
         "first_step_epot": first_epot,
         "fp64_gpu_over_fp64_cpu": None if cpu is None else ns_per_day(ms64) / cpu["value"],
         "tip4p_32k": big,

@@ -444,6 +444,41 @@ def test_replicas_equal_separate_systems(orc):
         assert np.abs(F[off[k]:off[k + 1]] - Fo).max() <= 1e-12 * frms
 
 
+@pytest.mark.parametrize("half", [0, 1])
+def test_fp64_md_replicas_equal_separate_runs(half):
+    """Ten FP64 MD steps of three uneven replicas in one context (Nose at three
+    temperatures) end where three separate single-replica runs end, with the
+    full list and with the half list (whose j-side FP64 atomics and 32-molecule
+    integrator blocks straddle replica boundaries)."""
+    import ctypes
+    sizes, temps = [216, 300, 250], [260.0, 300.0, 340.0]
+    boxes, recs = [], []
+    for k, n in enumerate(sizes):
+        b = config.water_box("TIP4P", n, 70 + k, temp=temps[k], dt=0.002, jitter=0.2)
+        boxes.append(b["L"]); recs.append(b["rec"])
+    q = 300.0 * 0.1 ** 2 / 0.002
+
+    def shaped(sys_):
+        sh = _capi.Shape(lpi=8, step_lpi=8, step_mpw=8, skin=1.0, cap=0, step_ms=0.0, step_half=half)
+        sys_._check(sys_.L.g6_set_shape(sys_.ctx, ctypes.byref(sh)))
+        return sys_
+
+    s = shaped(g6.RigidWater("TIP4P", sizes, np.array(boxes), path="custom", rc=8.5))
+    s.upload_state(np.concatenate(recs))
+    log = s.md_run(0.002, 10, s.thermostats(3, "nose", temp=temps, q=q))
+    got = s.download_state()
+    off = np.concatenate([[0], np.cumsum(sizes)])
+    for k, n in enumerate(sizes):
+        one = shaped(g6.RigidWater("TIP4P", n, boxes[k], path="custom", rc=8.5))
+        one.upload_state(recs[k])
+        log1 = one.md_run(0.002, 10, one.thermostats(1, "nose", temp=temps[k], q=q))
+        want = one.download_state()
+        assert np.abs(got[off[k]:off[k + 1]] - want).max() <= 1e-10 * np.abs(want).max()
+        for c in (0, 3, 5, 7):
+            assert np.abs(log[:, k, c] - log1[:, 0, c]).max() <= 1e-10 * np.abs(log1[:, 0, c]).max() + 1e-14
+        assert np.array_equal(log[:, k, 6], log1[:, 0, 6])
+
+
 def test_nonfinite_state_is_reported():
     b = config.water_box("TIP4P", 256, 1)
     s = g6.RigidWater("TIP4P", 256, b["L"], rc=8.5)
