@@ -589,9 +589,11 @@ static int default_lpi(const g6_ctx* c) {
 // instructions for a large one.
 static int default_mpw(const g6_ctx* c) { return c->n <= 8192 ? 4 : (c->n <= 24576 ? 16 : 32); }
 
-// Mixed MD steps use the half list (each pair evaluated once, the other
-// molecule's share added with float atomics: sums in a varying order, so runs
-// are not bit-reproducible); FP64 steps always use the full list.
+// Default list form of the MD step: the half list in mixed precision (each
+// pair evaluated once, the other molecule's share added with float atomics:
+// sums in a varying order, so runs are not bit-reproducible), the full list in
+// FP64 (bit-reproducible; the FP64 half list is there for g6_set_shape and the
+// tuner).
 static int default_half(const g6_ctx* c) { return c->prec == G6_MIXED ? 1 : 0; }
 
 // The mixed list kernel keeps each molecule's in-range row in shared memory
