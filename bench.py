@@ -63,13 +63,14 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--no-extra", action="store_true", help="skip the replica-exchange and Monte Carlo legs")
     p.add_argument("--n", type=int, default=N_MAIN, help="molecules of the 'md' profiling case")
+    p.add_argument("--prec", choices=["mixed", "fp64"], default="mixed", help="precision of the 'md' profiling case")
     p.add_argument("--shape", default=None,
                    help="'md' profiling case: lanes,step_lanes,molecules_per_warp,skin[,half (1: half list, the "
                         "default; 0: full list)] instead of running the tuner "
                         "(keeps the tuner's many launches out of a profiler capture)")
     p.add_argument("--profile", choices=["md", "e2e", "mc", "mc-learned", "rdf"], default=None,
                    help="run a short untimed case for a profiler capture and exit: 'md' = --steps MD steps of "
-                        "--n TIP4P molecules (mixed, Nose 300 K, one g6_md_run after a 20-step start); 'mc' = two runs of --steps trials on "
+                        "--n TIP4P molecules (--prec, Nose 300 K, one g6_md_run after a 20-step start); 'mc' = two runs of --steps trials on "
                         "32 chains x 1,024 ST2 (fixed widths) from a short MD start; 'mc-learned' = the same "
                         "with the network trained on 32,768 records first, then learned widths; 'rdf' = --steps "
                         "g6_rdf calls on TIP4P-32768")
@@ -956,7 +957,7 @@ def run_profile(args):
             b = equilibrated_start()
         else:
             b = config.water_box("TIP4P", args.n, 20261203, temp=TEMP, dt=DT)
-        s = make_system("TIP4P", args.n, "mixed", b["L"], b["rec"])
+        s = make_system("TIP4P", args.n, args.prec, b["L"], b["rec"])
         s.md_run(DT, 20, thermo_for(s), log=False)
         from genesis6_gb300 import _capi
         shape = _capi.Shape()

@@ -112,6 +112,10 @@ def lib():
                                         dp, ctypes.c_int, ctypes.c_int, i64, ip, ip, dp, dp, dp, dp, dp, dp, dp]
     L.g6_md_run.argtypes = [vp, ctypes.c_double, ctypes.c_int, ctypes.POINTER(Thermostat), dp]
     L.g6_md_step_host.argtypes = [vp, ctypes.c_double, ctypes.POINTER(Thermostat), dp, dp]
+    # the same entry point with every pointer an integer address: the per-step
+    # host-buffer call pays no typed-pointer conversions (RigidWater.md_step_host)
+    L.md_step_host_addr = ctypes.CFUNCTYPE(ctypes.c_int, vp, ctypes.c_double, vp, vp, vp)(
+        ctypes.cast(L.g6_md_step_host, vp).value)
     L.g6_replica_exchange.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,
                                       ctypes.POINTER(Thermostat), ip]
     L.g6_replica_exchange_umbrella.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, dp,

@@ -168,7 +168,11 @@ class RigidWater:
     def md_step_host(self, dt, rec, thermo=None, log=None):
         if thermo is None:
             thermo = self.thermostats(self.nrep)
-        self._check(self.L.g6_md_step_host(self.ctx, float(dt), thermo, dptr(rec), dptr(log)))
+        for a in (rec, log):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError("rec and log must be C-contiguous float64 arrays")
+        adr = lambda a: None if a is None else a.__array_interface__["data"][0]
+        self._check(self.L.md_step_host_addr(self.ctx, float(dt), ctypes.addressof(thermo), adr(rec), adr(log)))
         return rec
 
     # -- Monte Carlo (mc2.F90 trial/accept loop, one chain per replica) --------
