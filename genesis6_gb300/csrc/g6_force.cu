@@ -47,7 +47,6 @@ __global__ void __launch_bounds__(FUSED ? StepShape<LPI>::THREADS : 128, 1) k_fo
   if (a.ctrl) step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
   const double* pk64 = odd ? a.pk64_1 : a.pk64;
-  const float4* pk32 = odd ? a.pk32_1 : a.pk32;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = gt / LPI;
   const int sub = gt % LPI;
@@ -223,48 +222,215 @@ static cudaError_t launch_force_any(const ForceArgs& a, const StepArgs& sa, int 
   return launch_force_l<MT<4, false>, FUSED, HALF>(a, sa, lpi, s);
 }
 
+// Component c of qdot(w, q) (RigidModule.F90:1337-1348) from the three
+// quaternion components it uses, qo[k] = q[c ^ (k + 1)]: every component is
+// sum_k s_ck w_k qo[k] with the signs of qdot (the bits of 0xF5, three per
+// component), so the four lanes of a quad run one instruction stream.
+__device__ __forceinline__ double qdot64_c(const double w[3], const double qo[3], int c) {
+  const int b = 3 * c;
+  const double s0 = ((0xF5 >> b) & 1) ? -1.0 : 1.0;
+  const double s1 = ((0xF5 >> (b + 1)) & 1) ? -1.0 : 1.0;
+  const double s2 = ((0xF5 >> (b + 2)) & 1) ? -1.0 : 1.0;
+  return (s0 * w[0]) * qo[0] + (s1 * w[1]) * qo[1] + (s2 * w[2]) * qo[2];
+}
+
 // The FP64 MD step on half rows, second kernel: each molecule's force and lab
 // torque (its own pairs' sums minus / plus the shares its partners added to
-// jacc64, which are cleared for the next step), then the Gear corrector, the
-// next predict and placement and the step's reductions as in the fused step;
-// one molecule per lane, 32 per block (an FP64 instruction costs a warp the
-// same whatever the number of active lanes).
-__global__ void __launch_bounds__(32) k_integrate_fp64(ForceArgs a, StepArgs sa) {
+// jacc64, which are cleared for the next step), then the FP64 Gear corrector
+// and the next step's predict (the arithmetic of correct_one and predict_one),
+// placement and the step's reductions.  Four lanes per molecule, lane c owning
+// component c of every vector (x, y, z for c < 3; quaternion component c) and
+// the state columns of that component, full vectors by shuffles within the
+// quad: an FP64 instruction costs a warp 64 cycles however few lanes are
+// active, so the quad's lanes split the corrector's chain (about a quarter of
+// the instructions per warp of one molecule per lane) and the 8 molecules of a
+// warp share each instruction.  32 molecules per block of 128 threads; the
+// placement (place_to) runs on the quad's first lane.
+__global__ void __launch_bounds__(128) k_integrate_fp64(ForceArgs a, StepArgs sa) {
+  __shared__ double s_vv[32][NRED];
+  __shared__ float s_dm[32];
+  __shared__ int s_bad[32], s_rr[32];
   const int n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, c = lane & 3;
+  const int m = warp * 8 + (lane >> 2);
+  const int im = blockIdx.x * 32 + m;
+  const bool ok = im < n;
+  const bool v3 = c < 3;
+  const int ii = ok ? im : 0;   // a lane without a molecule computes on molecule 0 and stores nothing
   const int step = a.ctrl[1];
   const bool odd = (step & 1) != 0;
   const bool predict_next = step + 1 < sa.ctrl[2];
-  const int im = blockIdx.x * 32 + threadIdx.x;
+  double* st = sa.p.st;
+  const int r = sa.p.rep.mol_rep[ii];
+  const ThermoDev th = sa.th[r];
+  const double dt = sa.dt;
+  // the state columns of component c: x[k] = column 3k + c (com, d1..d5),
+  // w[k] = 18 + 3k + c (w1..w5), q[k] = 33 + 4k + c (q, q2..q5)
+  double x[6], w[5], q[5];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) x[k] = v3 ? st[(size_t)(3 * k + c) * n + ii] : 0.0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) w[k] = v3 ? st[(size_t)(18 + 3 * k + c) * n + ii] : 0.0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) q[k] = st[(size_t)(33 + 4 * k + c) * n + ii];
+  double Fc = 0.0, tlc = 0.0;
+  if (v3 && ok) {
+    double* jf = a.jacc64 + (size_t)c * n + im;
+    double* jt = a.jacc64 + (size_t)(3 + c) * n + im;
+    Fc = a.F[(size_t)c * n + im] - *jf;
+    tlc = a.tl[(size_t)c * n + im] + *jt;
+    *jf = 0.0;
+    *jt = 0.0;
+  }
+  // body torque component c: column c of the rotation against the lab torque
+  const PoseBuf cur = pose_buf(sa, odd ? 1 : 0);
+  const double tl0 = qsh(tlc, 0), tl1 = qsh(tlc, 1), tl2 = qsh(tlc, 2);
+  double tauc = 0.0;
+  if (v3)
+    tauc = cur.tmat[(size_t)c * n + ii] * tl0 + cur.tmat[(size_t)(3 + c) * n + ii] * tl1 +
+           cur.tmat[(size_t)(6 + c) * n + ii] * tl2;
+  int bd = (v3 && ok && !(isfinite(Fc) && isfinite(tauc))) ? 1 : 0;
+  double ext_t = 0.0, ext_r = 0.0;
+  if (th.kind == G6_NOSE) {
+    const double nc = th.z[0] * dt;
+    ext_t = nc * 0.5;
+    ext_r = nc;
+  }
+  const double massi = 1.0 / sa.mass;
+  // COM: Gear-5
+  if (v3) {
+    double nf = Fc * (dt * dt * 0.5 * massi);
+    nf = nf - x[1] * ext_t;
+    const double delta = nf - x[2];
+    x[0] = x[0] + G50 * delta;
+    x[1] = x[1] + G51 * delta;
+    x[2] = nf;
+    x[3] = x[3] + G53 * delta;
+    x[4] = x[4] + G54 * delta;
+    x[5] = x[5] + G55 * delta;
+  }
+  // quaternion value, from the angular velocity before its correction
+  const double w1v[3] = {qsh(w[0], 0), qsh(w[0], 1), qsh(w[0], 2)};
+  {
+    const double qo[3] = {qsh(q[0], c ^ 1), qsh(q[0], c ^ 2), qsh(q[0], c ^ 3)};
+    const double dw = qdot64_c(w1v, qo, c) * dt * 0.5 - q[1];
+    q[0] = q[0] + G40 * dw;
+  }
+  // angular velocity: Gear-4 with Euler's equations (axis c, cyclic c1, c2)
+  if (v3) {
+    const int c1 = c == 2 ? 0 : c + 1, c2 = c == 0 ? 2 : c - 1;
+    const double Ic = c == 0 ? sa.I[0] : (c == 1 ? sa.I[1] : sa.I[2]);
+    const double I1 = c1 == 0 ? sa.I[0] : (c1 == 1 ? sa.I[1] : sa.I[2]);
+    const double I2 = c2 == 0 ? sa.I[0] : (c2 == 1 ? sa.I[1] : sa.I[2]);
+    const double wa = c1 == 0 ? w1v[0] : (c1 == 1 ? w1v[1] : w1v[2]);
+    const double wb = c2 == 0 ? w1v[0] : (c2 == 1 ? w1v[1] : w1v[2]);
+    double nf = (tauc + (I1 - I2) * wa * wb) * dt * (1.0 / Ic);
+    nf = nf - w[0] * ext_r;
+    const double delta = nf - w[1];
+    w[0] = w[0] + G40 * delta;
+    w[1] = nf;
+    w[2] = w[2] + G42 * delta;
+    w[3] = w[3] + G43 * delta;
+    w[4] = w[4] + G44 * delta;
+  }
+  // stochastic collisions: every lane of the quad draws the same numbers
+  if (th.kind == G6_ANDERSEN) {
+    double u[2];
+    const uint32_t sc = (uint32_t)(sa.ctrl[6] + step);
+    uniform2(sa.seed, (uint32_t)im, sc, 0x41u, 0u, u);
+    if (u[0] <= th.rate * dt) {
+      const double kT = th.temp * RGAS * J2I;
+      double z[6];
+      for (int p = 0; p < 3; ++p) {
+        double g[2];
+        uniform2(sa.seed, (uint32_t)im, sc, 0x41u, (uint32_t)(p + 1), g);
+        z[2 * p] = normal_pair(g[0], g[1], z[2 * p + 1]);
+      }
+      const double sv = sqrt(kT * massi) * dt;
+      if (v3) {
+        const double Ic = c == 0 ? sa.I[0] : (c == 1 ? sa.I[1] : sa.I[2]);
+        x[1] = (c == 0 ? z[0] : (c == 1 ? z[1] : z[2])) * sv;
+        w[0] = (c == 0 ? z[3] : (c == 1 ? z[4] : z[5])) * sqrt(kT / Ic);
+      }
+    }
+  }
+  // quaternion derivative stacks from the corrected angular-velocity stack
+  double W[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) W[k][j] = qsh(w[k], j);
+  double a0[3], a1[3], a2[3], a3[3];
+  a0[0] = qsh(q[0], c ^ 1); a0[1] = qsh(q[0], c ^ 2); a0[2] = qsh(q[0], c ^ 3);
+  q[1] = qdot64_c(W[0], a0, c) * dt * 0.5;
+  a1[0] = qsh(q[1], c ^ 1); a1[1] = qsh(q[1], c ^ 2); a1[2] = qsh(q[1], c ^ 3);
+  q[2] = (qdot64_c(W[1], a0, c) + qdot64_c(W[0], a1, c)) * dt * 0.25;
+  a2[0] = qsh(q[2], c ^ 1); a2[1] = qsh(q[2], c ^ 2); a2[2] = qsh(q[2], c ^ 3);
+  q[3] = (qdot64_c(W[2], a0, c) + qdot64_c(W[0], a2, c) + qdot64_c(W[1], a1, c)) * dt * (1.0 / 6.0);
+  a3[0] = qsh(q[3], c ^ 1); a3[1] = qsh(q[3], c ^ 2); a3[2] = qsh(q[3], c ^ 3);
+  q[4] = (qdot64_c(W[3], a0, c) + qdot64_c(W[2], a1, c) + qdot64_c(W[1], a2, c) + qdot64_c(W[0], a3, c)) * dt *
+         (1.0 / 8.0);
+  // reductions: kinetic sums (Rigid_Ek) over the quad
+  const double ekt = quad_sum(v3 ? x[1] * x[1] : 0.0);
+  const double Icw = v3 ? (c == 0 ? sa.I[0] : (c == 1 ? sa.I[1] : sa.I[2])) : 0.0;
+  const double ekr = quad_sum(Icw * (W[0][c == 3 ? 0 : c] * W[0][c == 3 ? 0 : c]));
+  // the next step's predict (predict_one)
+  if (predict_next) {
+    if (v3) {
+      const double d1 = x[1], d2 = x[2], d3 = x[3], d4 = x[4], d5 = x[5];
+      x[0] = x[0] + d1 + d2 + d3 + d4 + d5;
+      x[1] = d1 + 2.0 * d2 + 3.0 * d3 + 4.0 * d4 + 5.0 * d5;
+      x[2] = d2 + 3.0 * d3 + 6.0 * d4 + 10.0 * d5;
+      x[3] = d3 + 4.0 * d4 + 10.0 * d5;
+      x[4] = d4 + 5.0 * d5;
+      const double w1 = w[0], w2 = w[1], w3 = w[2], w4 = w[3], w5 = w[4];
+      w[0] = w1 + w2 + w3 + w4 + w5;
+      w[1] = w2 + 2.0 * w3 + 3.0 * w4 + 4.0 * w5;
+      w[2] = w3 + 3.0 * w4 + 6.0 * w5;
+      w[3] = w4 + 4.0 * w5;
+    }
+    const double qs = q[0] + q[1] + q[2] + q[3] + q[4];
+    q[1] = q[1] + 2.0 * q[2] + 3.0 * q[3] + 4.0 * q[4];
+    const double re = 1.0 / sqrt(quad_sum(qs * qs));
+    q[0] = qs * re;
+  }
+  if (ok) {
+    if (v3) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) st[(size_t)(3 * k + c) * n + im] = x[k];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) st[(size_t)(18 + 3 * k + c) * n + im] = w[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) st[(size_t)(33 + 4 * k + c) * n + im] = q[k];
+  }
+  bd = quad_sum(bd);
+  __syncwarp();   // the quad's columns are written before its first lane places the molecule
+  if (c == 0) {
+    double dmax2 = 0.0;
+    int bad = bd ? 1 : 0;
+    if (ok && predict_next) place_next(sa, im, pose_buf(sa, odd ? 0 : 1), dmax2, bad);
+    s_vv[m][0] = ok ? a.emol[im] : 0.0;
+    s_vv[m][1] = ok ? a.wmol[im] : 0.0;
+    s_vv[m][2] = ok ? ekt : 0.0;
+    s_vv[m][3] = ok ? ekr : 0.0;
+    s_vv[m][4] = ok ? (double)a.npair_in[im] : 0.0;
+    s_dm[m] = (float)dmax2;
+    s_bad[m] = ok ? bad : 0;
+    s_rr[m] = ok ? r : -1;
+  }
+  __syncthreads();
   double vv[NRED];
+  float dm = 0.0f;
+  int bdd = 0, rr = -1;
 #pragma unroll
   for (int k = 0; k < NRED; ++k) vv[k] = 0.0;
-  double dmax2 = 0.0;
-  int bad = 0, rr = -1;
-  if (im < n) {
-    rr = a.rep.mol_rep[im];
-    double F[3], tl[3];
+  if (warp == 0) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      double* jf = a.jacc64 + (size_t)k * n + im;
-      double* jt = a.jacc64 + (size_t)(3 + k) * n + im;
-      F[k] = a.F[(size_t)k * n + im] - *jf;
-      tl[k] = a.tl[(size_t)k * n + im] + *jt;
-      *jf = 0.0;
-      *jt = 0.0;
-    }
-    // the molecule's record in registers: the corrector's read-modify-write
-    // chain then waits on no memory round trip (in the fused step it does, but
-    // other blocks' pair work hides it)
-    double rs[REC];
-#pragma unroll
-    for (int c = 0; c < REC; ++c) rs[c] = sa.p.st[(size_t)c * n + im];
-    correct_one(sa, im, rs, 1, 0, F, tl, a.emol[im], a.wmol[im], (double)a.npair_in[im], step, predict_next,
-                pose_buf(sa, odd ? 1 : 0), vv, bad);
-#pragma unroll
-    for (int c = 0; c < REC; ++c) sa.p.st[(size_t)c * n + im] = rs[c];
-    if (predict_next) place_next(sa, im, pose_buf(sa, odd ? 0 : 1), dmax2, bad);
+    for (int k = 0; k < NRED; ++k) vv[k] = s_vv[lane][k];
+    dm = s_dm[lane]; bdd = s_bad[lane]; rr = s_rr[lane];
   }
-  step_reduce<double>(sa, vv, rr, (float)dmax2, bad, 32, step, 0);
+  step_reduce<double>(sa, vv, rr, dm, bdd, 32, step, 0);
 }
 
 // Force only (outputs F, lab torque, per-molecule energy and virial); the
@@ -285,7 +451,7 @@ cudaError_t launch_step_fp64(const ForceArgs& a, const StepArgs& sa, int model, 
 cudaError_t launch_step_fp64_half(const ForceArgs& a, const StepArgs& sa, int model, int lpi, cudaStream_t s) {
   cudaError_t e = launch_force_any<false, true>(a, sa, model, lpi, s);
   if (e != cudaSuccess || a.n == 0) return e;
-  k_integrate_fp64<<<(a.n + 31) / 32, 32, 0, s>>>(a, sa);
+  k_integrate_fp64<<<(a.n + 31) / 32, 128, 0, s>>>(a, sa);
   return cudaGetLastError();
 }
 
