@@ -490,6 +490,50 @@ def test_nonfinite_state_is_reported():
     assert e.value.status == g6._capi.G6_ERR_NONFINITE
 
 
+@pytest.mark.parametrize("half", [0, 1])
+def test_host_buffer_step_recovers_row_overflow(half):
+    """Host-buffer steps on a page-locked buffer with rows too short for the
+    list: the overflow flag comes back through the pinned block, the step is
+    repeated from the kept input records with a larger capacity, and three
+    steps end where three steps of a context that never overflowed end (bit
+    for bit with the full list, within FP32 summation order with the half)."""
+    import ctypes
+    import torch
+    from genesis6_gb300 import _capi
+    n = 512
+    b = config.water_box("TIP4P", n, 44, temp=300.0, dt=0.002, jitter=0.2)
+    q = 300.0 * 0.25 / 0.002
+    out = []
+    for cap in (0, 64):   # about 140 full-row or 70 half-row entries at rc + skin = 10 A
+        s = g6.RigidWater("TIP4P", n, b["L"], path="custom", precision="mixed", rc=9.0)
+        s.upload_state(b["rec"])
+        sh = _capi.Shape(lpi=16, step_lpi=16, step_mpw=8, skin=1.0, cap=cap, step_ms=0.0, step_half=half)
+        s._check(s.L.g6_set_shape(s.ctx, ctypes.byref(sh)))
+        th = s.thermostats(1, "nose", temp=300.0, q=q)
+        host = torch.empty((n, 53), dtype=torch.float64, pin_memory=True).numpy()
+        host[:] = b["rec"]
+        logs = []
+        for _ in range(3):
+            lg = np.zeros(10)
+            s.md_step_host(0.002, host, th, lg)
+            logs.append(lg)
+        if cap:
+            got = _capi.Shape()
+            s._check(s.L.g6_get_shape(s.ctx, ctypes.byref(got)))
+            assert got.cap > cap
+        out.append((host.copy(), np.array(logs), list(th[0].zeta)))
+    (ha, la, za), (hb, lb, zb) = out
+    if half:
+        assert np.abs(ha - hb).max() <= 1e-5 * np.abs(ha).max()
+        cols = [0, 1, 2, 3, 5, 7]
+        assert np.abs(la[:, cols] - lb[:, cols]).max() <= 1e-6 * np.abs(la[:, cols]).max()
+        assert np.array_equal(la[:, 6], lb[:, 6])
+    else:
+        assert np.array_equal(ha, hb)
+        assert np.array_equal(la[:, [0, 1, 2, 3, 4, 5, 6, 7, 9]], lb[:, [0, 1, 2, 3, 4, 5, 6, 7, 9]])
+        assert za == zb
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_row_overflow_is_recovered(prec):
     """Neighbour-list rows longer than the capacity: g6_md_run puts the state
