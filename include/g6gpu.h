@@ -291,9 +291,12 @@ int g6_set_shape(g6_ctx* ctx, const g6_shape* shape);
    first call for that rec pointer, dt, log choice and lane width (so that
    first call must not come during a stream capture); in mixed precision its
    kernels then read and write rec directly through the buffer's device
-   address instead of staging copies.  Pageable rec works too, operation by
-   operation.  The neighbour list of the previous call is
-   kept when no molecule moved more than half the skin since it was built. */
+   address instead of staging copies, the run's control words (thermostat,
+   control, sums, log row) travel through the context's own page-locked block
+   the same way, and the call polls the stream for the end of the step.
+   Pageable rec works too, operation by operation.  The neighbour list of the
+   previous call is kept when no molecule moved more than half the skin since
+   it was built. */
 int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, double* log);
 
 /* replica_exchange_trial (Replica.F90:7-73) for neighbouring temperatures of
