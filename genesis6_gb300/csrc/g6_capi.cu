@@ -2086,8 +2086,12 @@ int g6_md_step_host(g6_ctx* ctx, double dt, g6_thermostat* thermo, double* rec, 
   if (rc) return rc;
   if (!rec) return fail(ctx, G6_ERR_ARG, "rec is NULL");
   // the pinned block is free: every earlier use ended with a stream synchronisation or pin_ev
-  CK(cudaEventSynchronize(ctx->pin_ev));
-  CK(cudaStreamSynchronize(ctx->stream));
+  // (both recorded on the context's stream: an idle stream answers for both in one query)
+  if (cudaStreamQuery(ctx->stream) != cudaSuccess) {
+    cudaGetLastError();   // a busy stream's status is not an error
+    CK(cudaEventSynchronize(ctx->pin_ev));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   if ((rc = md_fill(ctx, dt, 1, thermo, log != nullptr))) return rc;
   ctx->have_state = true;
   // a page-locked record: the call runs as one cached graph (launch overhead of

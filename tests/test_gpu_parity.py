@@ -421,8 +421,10 @@ def test_consecutive_host_steps_follow_a_device_run(half):
         for col in (0, 1, 2, 3, 5, 7):
             a, b_ = log_a[:, r, col], logs[:, r, col]
             assert np.abs(a - b_).max() <= 1e-5 * np.abs(a).max() + 1e-12
-        # every pair within rc was in the rows at every step on both routes
-        assert np.array_equal(logs[:, r, 6], log_a[:, r, 6])
+        # every pair within rc was in the rows at every step on both routes; a
+        # pair within ~1e-7 A of rc may fall on either side on the two routes
+        dn = np.abs(logs[:, r, 6] - log_a[:, r, 6])
+        assert dn.max() <= 2 and (dn > 0).sum() <= 2
         assert th_b[r].zeta[0] == pytest.approx(th_a[r].zeta[0], rel=1e-5, abs=1e-12)
         assert th_b[r].zetasum == pytest.approx(th_a[r].zetasum, rel=1e-5)
 
@@ -527,7 +529,7 @@ def test_host_buffer_step_recovers_row_overflow(half):
         assert np.abs(ha - hb).max() <= 1e-5 * np.abs(ha).max()
         cols = [0, 1, 2, 3, 5, 7]
         assert np.abs(la[:, cols] - lb[:, cols]).max() <= 1e-6 * np.abs(la[:, cols]).max()
-        assert np.array_equal(la[:, 6], lb[:, 6])
+        assert np.abs(la[:, 6] - lb[:, 6]).max() <= 2   # a pair at rc may fall on either side
     else:
         assert np.array_equal(ha, hb)
         assert np.array_equal(la[:, [0, 1, 2, 3, 4, 5, 6, 7, 9]], lb[:, [0, 1, 2, 3, 4, 5, 6, 7, 9]])
